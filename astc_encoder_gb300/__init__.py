@@ -1,0 +1,287 @@
+"""GB300-native ASTC LDR block encoder (sm_103a CUDA behind a C ABI).
+
+Python mirror of the reference's host interface (niepp/astc_encoder):
+
+* :class:`EncodeOption`   -- ``encode_option`` (astc_encode.h:14-28)
+* :func:`encode_astc`     -- ``encode_astc`` + ``read_gpu``
+                             (astc_encode.h:87-194, astc_save.h:34-50)
+* :func:`save_astc`       -- ``save_astc`` (astc_save.h:52-76)
+
+Everything here is a thin ``ctypes`` layer over ``libastc_gb300.so``
+(``include/astc_gb300.h``); the encode runs in the library's CUDA kernels.
+There is no CPU fallback: if the library is missing, every call raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import dataclasses
+import enum
+import os
+from typing import Any
+
+import numpy as np
+
+__all__ = [
+    "AstcError", "Status", "Border", "Precision", "Memory", "EncodeOption", "AstcOpts",
+    "library_path", "load_library", "encoded_size", "encode", "encode_astc", "encode_device",
+    "save_astc", "load_astc", "decode", "decode_device", "sse", "psnr_from_sse",
+    "kernel_launch_count", "shutdown",
+]
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+
+
+class Status(enum.IntEnum):
+    OK = 0
+    INVALID_ARG = 1
+    UNSUPPORTED = 2
+    CUDA = 3
+    OUT_OF_MEMORY = 4
+    IO = 5
+    TIMEOUT = 6
+    BUSY = 7
+    CANCELLED = 8
+    FORMAT = 9
+
+
+class Border(enum.IntEnum):
+    ZERO = 0
+    CLAMP = 1
+
+
+class Precision(enum.IntEnum):
+    FP32 = 0
+    HALF2 = 1
+
+
+class Memory(enum.IntEnum):
+    HOST = 0
+    DEVICE = 1
+
+
+class AstcError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        self.status = Status(status) if status in Status._value2member_map_ else status
+        super().__init__(f"{self.status!s}: {message}")
+
+
+class AstcOpts(ctypes.Structure):
+    """``astc_opts`` of include/astc_gb300.h."""
+    _fields_ = [
+        ("block_dim", ctypes.c_int),
+        ("has_alpha", ctypes.c_int),
+        ("is_normal", ctypes.c_int),
+        ("srgb", ctypes.c_int),
+        ("border", ctypes.c_int),
+        ("precision", ctypes.c_int),
+        ("memory", ctypes.c_int),
+        ("stream", ctypes.c_void_p),
+    ]
+
+
+@dataclasses.dataclass
+class EncodeOption:
+    """Mirror of the reference's ``encode_option`` (astc_encode.h:14-28).
+
+    The reference derives the block size from ``is4x4`` only and never reads
+    ``is6x6``, so its ``-6x6`` flag is a no-op; here ``is6x6`` selects 6x6
+    (the README's intent).
+    """
+    is4x4: bool = True
+    is6x6: bool = False
+    is_normal_map: bool = False
+    has_alpha: bool = False
+    srgb: bool = False
+
+    @property
+    def block_dim(self) -> int:
+        return 6 if (self.is6x6 or not self.is4x4) else 4
+
+
+def library_path() -> str:
+    return os.path.join(_PKG, "_lib", "libastc_gb300.so")
+
+
+_LIB: ctypes.CDLL | None = None
+
+
+def load_library() -> ctypes.CDLL:
+    """Load libastc_gb300.so (built in-tree by astc_encoder_gb300.build)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = library_path()
+    if not os.path.exists(path):
+        raise AstcError(Status.UNSUPPORTED,
+                        f"native library not built: {path} (run python -m astc_encoder_gb300.build)")
+    lib = ctypes.CDLL(path)
+    u8p, vp, sz = ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t
+    lib.astc_opts_init.argtypes = [ctypes.POINTER(AstcOpts)]
+    lib.astc_opts_init.restype = None
+    lib.astc_encoded_size.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    lib.astc_encoded_size.restype = sz
+    lib.astc_encode_gpu.argtypes = [u8p, ctypes.c_int, ctypes.c_int, ctypes.POINTER(AstcOpts), u8p]
+    lib.astc_encode_gpu.restype = ctypes.c_int
+    lib.astc_encode_gpu_pitched.argtypes = [u8p, ctypes.c_int, ctypes.c_int, sz,
+                                            ctypes.POINTER(AstcOpts), u8p]
+    lib.astc_encode_gpu_pitched.restype = ctypes.c_int
+    lib.astc_save_file.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                   ctypes.c_int, u8p, sz]
+    lib.astc_save_file.restype = ctypes.c_int
+    ip = ctypes.POINTER(ctypes.c_int)
+    lib.astc_load_file.argtypes = [ctypes.c_char_p, ip, ip, ip, ip, u8p, sz, ctypes.POINTER(sz)]
+    lib.astc_load_file.restype = ctypes.c_int
+    lib.astc_decode_gpu.argtypes = [u8p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                    ctypes.c_int, ctypes.c_int, vp, u8p]
+    lib.astc_decode_gpu.restype = ctypes.c_int
+    lib.astc_sse_gpu.argtypes = [u8p, u8p, sz, ctypes.c_int, vp, ctypes.POINTER(ctypes.c_uint64)]
+    lib.astc_sse_gpu.restype = ctypes.c_int
+    lib.astc_last_error.argtypes = []
+    lib.astc_last_error.restype = ctypes.c_char_p
+    lib.astc_status_string.argtypes = [ctypes.c_int]
+    lib.astc_status_string.restype = ctypes.c_char_p
+    lib.astc_kernel_launch_count.argtypes = []
+    lib.astc_kernel_launch_count.restype = ctypes.c_uint64
+    lib.astc_shutdown.argtypes = []
+    lib.astc_shutdown.restype = None
+    _LIB = lib
+    return lib
+
+
+def _check(status: int) -> None:
+    if status != 0:
+        msg = load_library().astc_last_error().decode(errors="replace")
+        raise AstcError(status, msg)
+
+
+def make_opts(block_dim: int = 4, has_alpha: bool = False, is_normal: bool = False,
+              srgb: bool = False, border: int = Border.ZERO, precision: int = Precision.FP32,
+              memory: int = Memory.HOST, stream: int | None = None) -> AstcOpts:
+    o = AstcOpts()
+    load_library().astc_opts_init(ctypes.byref(o))
+    o.block_dim = int(block_dim)
+    o.has_alpha = int(bool(has_alpha))
+    o.is_normal = int(bool(is_normal))
+    o.srgb = int(bool(srgb))
+    o.border = int(border)
+    o.precision = int(precision)
+    o.memory = int(memory)
+    o.stream = stream or None
+    return o
+
+
+def encoded_size(width: int, height: int, block_dim: int) -> int:
+    return 16 * ((width + block_dim - 1) // block_dim) * ((height + block_dim - 1) // block_dim)
+
+
+def encode(rgba: np.ndarray, block_dim: int = 4, has_alpha: bool = False, is_normal: bool = False,
+           srgb: bool = False, border: int = Border.ZERO, precision: int = Precision.FP32,
+           out: np.ndarray | None = None) -> np.ndarray:
+    """Encode a host (H, W, 4) uint8 image; returns (nblocks, 16) uint8 blocks."""
+    a = np.asarray(rgba)
+    if a.dtype != np.uint8 or a.ndim != 3 or a.shape[2] != 4:
+        raise AstcError(Status.INVALID_ARG, "rgba must be a (H, W, 4) uint8 array")
+    h, w = a.shape[:2]
+    if h == 0 or w == 0:
+        raise AstcError(Status.INVALID_ARG, "empty image")
+    a = np.ascontiguousarray(a)
+    n = encoded_size(w, h, block_dim)
+    if out is None:
+        out = np.empty((n // 16, 16), np.uint8)
+    elif out.nbytes != n or not out.flags.c_contiguous or out.dtype != np.uint8:
+        raise AstcError(Status.INVALID_ARG, "out has the wrong size or layout")
+    o = make_opts(block_dim, has_alpha, is_normal, srgb, border, precision, Memory.HOST)
+    _check(load_library().astc_encode_gpu(a.ctypes.data, w, h, ctypes.byref(o), out.ctypes.data))
+    return out
+
+
+def encode_astc(rgba: np.ndarray, option: EncodeOption | None = None, **kw: Any) -> np.ndarray:
+    """The reference's encode_astc + read_gpu: image in, block bytes out."""
+    option = option or EncodeOption()
+    return encode(rgba, block_dim=option.block_dim, has_alpha=option.has_alpha,
+                  is_normal=option.is_normal_map, srgb=option.srgb, **kw)
+
+
+def encode_device(rgba_ptr: int, width: int, height: int, out_ptr: int, block_dim: int = 4,
+                  has_alpha: bool = False, is_normal: bool = False, srgb: bool = False,
+                  border: int = Border.ZERO, precision: int = Precision.FP32,
+                  stream: int | None = None, row_pitch: int | None = None) -> None:
+    """Encode from device memory to device memory (pointers, e.g. tensor.data_ptr()).
+
+    With ``stream`` (a cudaStream_t handle) the call is asynchronous on it.
+    """
+    o = make_opts(block_dim, has_alpha, is_normal, srgb, border, precision, Memory.DEVICE, stream)
+    pitch = row_pitch if row_pitch is not None else width * 4
+    _check(load_library().astc_encode_gpu_pitched(rgba_ptr, width, height, pitch, ctypes.byref(o),
+                                                  out_ptr))
+
+
+def save_astc(path: str, xdim: int, ydim: int, xsize: int, ysize: int, blocks: np.ndarray) -> None:
+    """The reference's save_astc(path, xdim, ydim, xsize, ysize, buf, size)."""
+    b = np.ascontiguousarray(blocks, dtype=np.uint8)
+    _check(load_library().astc_save_file(os.fsencode(path), xdim, ydim, xsize, ysize,
+                                         b.ctypes.data, b.nbytes))
+
+
+def load_astc(path: str) -> tuple[np.ndarray, int, int, int, int]:
+    """Read a .astc file: (blocks (n,16), block_x, block_y, width, height)."""
+    lib = load_library()
+    bx, by, w, h = (ctypes.c_int() for _ in range(4))
+    size = ctypes.c_size_t()
+    _check(lib.astc_load_file(os.fsencode(path), ctypes.byref(bx), ctypes.byref(by), ctypes.byref(w),
+                              ctypes.byref(h), None, 0, ctypes.byref(size)))
+    out = np.empty((size.value // 16, 16), np.uint8)
+    _check(lib.astc_load_file(os.fsencode(path), ctypes.byref(bx), ctypes.byref(by), ctypes.byref(w),
+                              ctypes.byref(h), out.ctypes.data, out.nbytes, ctypes.byref(size)))
+    return out, bx.value, by.value, w.value, h.value
+
+
+def decode(blocks: np.ndarray, width: int, height: int, block_w: int, block_h: int | None = None,
+           srgb: bool = False) -> np.ndarray:
+    """Integer-only ASTC LDR decode on the GPU; returns (H, W, 4) uint8."""
+    block_h = block_h or block_w
+    b = np.ascontiguousarray(blocks, dtype=np.uint8)
+    need = encoded_size_xy(width, height, block_w, block_h)
+    if b.nbytes != need:
+        raise AstcError(Status.INVALID_ARG, "blocks has the wrong size")
+    out = np.empty((height, width, 4), np.uint8)
+    _check(load_library().astc_decode_gpu(b.ctypes.data, width, height, block_w, block_h, int(srgb),
+                                          Memory.HOST, None, out.ctypes.data))
+    return out
+
+
+def decode_device(blocks_ptr: int, width: int, height: int, block_w: int, block_h: int,
+                  out_ptr: int, srgb: bool = False, stream: int | None = None) -> None:
+    _check(load_library().astc_decode_gpu(blocks_ptr, width, height, block_w, block_h, int(srgb),
+                                          Memory.DEVICE, stream or None, out_ptr))
+
+
+def encoded_size_xy(width: int, height: int, bw: int, bh: int) -> int:
+    return 16 * ((width + bw - 1) // bw) * ((height + bh - 1) // bh)
+
+
+def sse(a: np.ndarray, b: np.ndarray) -> np.ndarray:
+    """Per-channel (R, G, B, A) sum of squared differences of two RGBA8 images, on the GPU."""
+    x = np.ascontiguousarray(a, dtype=np.uint8)
+    y = np.ascontiguousarray(b, dtype=np.uint8)
+    if x.shape != y.shape or x.size % 4:
+        raise AstcError(Status.INVALID_ARG, "images must have the same RGBA8 shape")
+    res = (ctypes.c_uint64 * 4)()
+    _check(load_library().astc_sse_gpu(x.ctypes.data, y.ctypes.data, x.size // 4, Memory.HOST, None,
+                                       res))
+    return np.array(list(res), dtype=np.uint64)
+
+
+def psnr_from_sse(sse_value: float, count: int, peak: float = 255.0) -> float:
+    if sse_value == 0:
+        return float("inf")
+    return float(10.0 * np.log10(peak * peak * count / float(sse_value)))
+
+
+def kernel_launch_count() -> int:
+    return int(load_library().astc_kernel_launch_count())
+
+
+def shutdown() -> None:
+    if _LIB is not None:
+        _LIB.astc_shutdown()

@@ -1,0 +1,440 @@
+// astc_capi.cu -- the C ABI (include/astc_gb300.h): argument checks, pooled
+// device staging, host<->device copies, .astc file I/O and error reporting.
+//
+// Replaces the D3D11 host side of niepp/astc_encoder:
+//   encode_astc        astc_encode.h:87-194 (SRV/UAV/cbuffer setup, grid
+//                      math 124-134, Dispatch 190)  -> astc_encode_gpu
+//   read_gpu           astc_save.h:34-50 (staging buffer + Map)
+//                                                   -> cudaMemcpyAsync D2H
+//   save_astc          astc_save.h:52-76            -> astc_save_file
+// Unlike the reference, every failure returns a status (the reference leaked
+// its D3D objects on each error path and never checked fopen).
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <atomic>
+#include <mutex>
+#include <new>
+#include <string>
+
+#include "astc_internal.h"
+
+namespace astc {
+namespace {
+
+thread_local std::string t_last_error;
+std::atomic<uint64_t> g_launches{0};
+
+// Per-device pool: one stream and grow-only staging buffers for host-memory
+// calls.  Calls on one device serialise on its mutex while they use the pool.
+struct DevicePool {
+    std::mutex mu;
+    bool ready = false;
+    cudaStream_t stream = nullptr;
+    uint8_t* d_in = nullptr;
+    size_t in_cap = 0;
+    uint8_t* d_out = nullptr;
+    size_t out_cap = 0;
+    unsigned long long* d_sse = nullptr;
+};
+
+constexpr int kMaxDevices = 64;
+DevicePool g_pools[kMaxDevices];
+
+astc_status grow(uint8_t** p, size_t* cap, size_t need) {
+    if (*cap >= need) return ASTC_OK;
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    *cap = 0;
+    size_t want = need < (1u << 20) ? (1u << 20) : need;
+    want = (want + 255) & ~(size_t)255;
+    const cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), want);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return set_error(ASTC_ERR_OUT_OF_MEMORY,
+                         std::string("cudaMalloc of staging buffer failed: ") + cudaGetErrorString(e));
+    }
+    *cap = want;
+    return ASTC_OK;
+}
+
+astc_status pool_for_current(DevicePool** out, int* dev_out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_error(e, "cudaGetDevice");
+    if (dev < 0 || dev >= kMaxDevices) return set_error(ASTC_ERR_UNSUPPORTED, "device index out of range");
+    DevicePool& p = g_pools[dev];
+    *out = &p;
+    *dev_out = dev;
+    return ASTC_OK;
+}
+
+astc_status pool_init_locked(DevicePool& p, int dev) {
+    if (p.ready) return ASTC_OK;
+    cudaError_t e = cudaStreamCreateWithFlags(&p.stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return cuda_error(e, "cudaStreamCreateWithFlags");
+    e = ensure_encode_constants(dev);
+    if (e != cudaSuccess) return cuda_error(e, "upload of the sRGB table");
+    p.ready = true;
+    return ASTC_OK;
+}
+
+astc_status check_device_pointer(const void* ptr, const char* what) {
+    cudaPointerAttributes a;
+    const cudaError_t e = cudaPointerGetAttributes(&a, ptr);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return set_error(ASTC_ERR_INVALID_ARG, std::string(what) + " is not a CUDA pointer");
+    }
+    if (a.type != cudaMemoryTypeDevice && a.type != cudaMemoryTypeManaged)
+        return set_error(ASTC_ERR_INVALID_ARG,
+                         std::string(what) + " is not device memory (memory = ASTC_MEMORY_DEVICE)");
+    return ASTC_OK;
+}
+
+astc_status validate_opts(const astc_opts* o, int w, int h) {
+    if (!o) return set_error(ASTC_ERR_INVALID_ARG, "opts is NULL");
+    if (o->block_dim != 4 && o->block_dim != 6)
+        return set_error(ASTC_ERR_INVALID_ARG, "block_dim must be 4 or 6");
+    if (o->border != ASTC_BORDER_ZERO && o->border != ASTC_BORDER_CLAMP)
+        return set_error(ASTC_ERR_INVALID_ARG, "border must be ASTC_BORDER_ZERO or ASTC_BORDER_CLAMP");
+    if (o->precision != ASTC_PRECISION_FP32 && o->precision != ASTC_PRECISION_HALF2)
+        return set_error(ASTC_ERR_INVALID_ARG, "precision must be FP32 or HALF2");
+    if (o->memory != ASTC_MEMORY_HOST && o->memory != ASTC_MEMORY_DEVICE)
+        return set_error(ASTC_ERR_INVALID_ARG, "memory must be ASTC_MEMORY_HOST or ASTC_MEMORY_DEVICE");
+    if (w <= 0 || h <= 0) return set_error(ASTC_ERR_INVALID_ARG, "width and height must be positive");
+    if (w > 0xFFFFFF || h > 0xFFFFFF)
+        return set_error(ASTC_ERR_INVALID_ARG, "width and height must fit the 24-bit .astc size fields");
+    const long long nb = (long long)blocks_x(w, o->block_dim) * blocks_y(h, o->block_dim);
+    if (nb > (1LL << 31)) return set_error(ASTC_ERR_INVALID_ARG, "image has more than 2^31 blocks");
+    return ASTC_OK;
+}
+
+}  // namespace
+
+astc_status set_error(astc_status st, const std::string& msg) {
+    t_last_error = msg;
+    return st;
+}
+
+astc_status cuda_error(cudaError_t e, const char* what) {
+    const std::string msg = std::string(what) + ": " + cudaGetErrorString(e);
+    cudaGetLastError();
+    return set_error(e == cudaErrorMemoryAllocation ? ASTC_ERR_OUT_OF_MEMORY : ASTC_ERR_CUDA, msg);
+}
+
+void count_launches(uint64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+}  // namespace astc
+
+using namespace astc;
+
+extern "C" {
+
+void astc_opts_init(astc_opts* o) {
+    if (!o) return;
+    memset(o, 0, sizeof(*o));
+    o->block_dim = 4;                 // encode_option(): is4x4 = true
+    o->border = ASTC_BORDER_ZERO;
+    o->precision = ASTC_PRECISION_FP32;
+    o->memory = ASTC_MEMORY_HOST;
+}
+
+size_t astc_encoded_size(int width, int height, int block_dim) {
+    if (width <= 0 || height <= 0 || (block_dim != 4 && block_dim != 6)) return 0;
+    return (size_t)16 * blocks_x(width, block_dim) * blocks_y(height, block_dim);
+}
+
+astc_status astc_encode_gpu_pitched(const uint8_t* rgba8, int width, int height, size_t row_pitch,
+                                    const astc_opts* opts, uint8_t* out) {
+    try {
+        astc_status st = validate_opts(opts, width, height);
+        if (st != ASTC_OK) return st;
+        if (!rgba8 || !out) return set_error(ASTC_ERR_INVALID_ARG, "rgba8 and out must be non-NULL");
+        if (row_pitch < (size_t)width * 4 || row_pitch % 4 != 0)
+            return set_error(ASTC_ERR_INVALID_ARG, "row_pitch must be >= 4*width and a multiple of 4");
+        if (opts->precision == ASTC_PRECISION_HALF2)
+            return set_error(ASTC_ERR_UNSUPPORTED, "HALF2 precision is not built in this library");
+        DevicePool* pool = nullptr;
+        int dev = 0;
+        if ((st = pool_for_current(&pool, &dev)) != ASTC_OK) return st;
+        std::lock_guard<std::mutex> lk(pool->mu);
+        if ((st = pool_init_locked(*pool, dev)) != ASTC_OK) return st;
+
+        const size_t out_bytes = astc_encoded_size(width, height, opts->block_dim);
+        const size_t in_bytes = row_pitch * (size_t)(height - 1) + (size_t)width * 4;
+        cudaStream_t s = opts->stream ? static_cast<cudaStream_t>(opts->stream) : pool->stream;
+
+        EncodeJob job;
+        job.width = width;
+        job.height = height;
+        job.block_dim = opts->block_dim;
+        job.has_alpha = opts->has_alpha;
+        job.is_normal = opts->is_normal;
+        job.srgb = opts->srgb;
+        job.border = opts->border;
+        job.precision = opts->precision;
+
+        if (opts->memory == ASTC_MEMORY_DEVICE) {
+            if ((st = check_device_pointer(rgba8, "rgba8")) != ASTC_OK) return st;
+            if ((st = check_device_pointer(out, "out")) != ASTC_OK) return st;
+            if (reinterpret_cast<uintptr_t>(rgba8) % 4 != 0)
+                return set_error(ASTC_ERR_INVALID_ARG, "device rgba8 must be 4-byte aligned");
+            if (reinterpret_cast<uintptr_t>(out) % 16 != 0)
+                return set_error(ASTC_ERR_INVALID_ARG, "device out must be 16-byte aligned");
+            job.in = rgba8;
+            job.pitch = row_pitch;
+            job.out = out;
+            cudaError_t e = launch_encode(job, s);
+            if (e != cudaSuccess) return cuda_error(e, "encode kernel launch");
+            if (!opts->stream) {
+                e = cudaStreamSynchronize(s);
+                if (e != cudaSuccess) return cuda_error(e, "encode");
+            }
+            return ASTC_OK;
+        }
+
+        // host memory: stage through the pool (tight rows on the device)
+        const size_t tight = (size_t)width * 4;
+        if ((st = grow(&pool->d_in, &pool->in_cap, tight * height)) != ASTC_OK) return st;
+        if ((st = grow(&pool->d_out, &pool->out_cap, out_bytes)) != ASTC_OK) return st;
+        (void)in_bytes;
+        cudaError_t e = cudaMemcpy2DAsync(pool->d_in, tight, rgba8, row_pitch, tight, height,
+                                          cudaMemcpyHostToDevice, s);
+        if (e != cudaSuccess) return cuda_error(e, "host-to-device copy");
+        job.in = pool->d_in;
+        job.pitch = tight;
+        job.out = pool->d_out;
+        e = launch_encode(job, s);
+        if (e != cudaSuccess) return cuda_error(e, "encode kernel launch");
+        e = cudaMemcpyAsync(out, pool->d_out, out_bytes, cudaMemcpyDeviceToHost, s);
+        if (e != cudaSuccess) return cuda_error(e, "device-to-host copy");
+        // The pooled buffers are reused by the next call: finish before returning.
+        e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) return cuda_error(e, "encode");
+        return ASTC_OK;
+    } catch (const std::bad_alloc&) {
+        return set_error(ASTC_ERR_OUT_OF_MEMORY, "host allocation failed");
+    } catch (...) {
+        return set_error(ASTC_ERR_CUDA, "unexpected exception");
+    }
+}
+
+astc_status astc_encode_gpu(const uint8_t* rgba8, int width, int height, const astc_opts* opts,
+                            uint8_t* out) {
+    if (width <= 0) return astc_encode_gpu_pitched(rgba8, width, height, 4, opts, out);
+    return astc_encode_gpu_pitched(rgba8, width, height, (size_t)width * 4, opts, out);
+}
+
+astc_status astc_save_file(const char* path, int bdx, int bdy, int width, int height,
+                           const uint8_t* blocks, size_t blocks_size) {
+    if (!path || !blocks) return set_error(ASTC_ERR_INVALID_ARG, "path and blocks must be non-NULL");
+    if (bdx < 2 || bdx > 12 || bdy < 2 || bdy > 12)
+        return set_error(ASTC_ERR_INVALID_ARG, "block dimensions must be 2..12");
+    if (width <= 0 || height <= 0 || width > 0xFFFFFF || height > 0xFFFFFF)
+        return set_error(ASTC_ERR_INVALID_ARG, "image size must be 1..2^24-1");
+    const size_t need = (size_t)16 * ((width + bdx - 1) / bdx) * ((height + bdy - 1) / bdy);
+    if (blocks_size != need)
+        return set_error(ASTC_ERR_INVALID_ARG, "blocks_size does not match the image and block size");
+    // astc_header (astc_save.h:5-14): magic 0x5CA1AB13 little-endian, block
+    // dims, 24-bit little-endian x/y/z sizes in texels, z = 1.
+    uint8_t hdr[16];
+    const uint32_t magic = 0x5CA1AB13u;
+    for (int i = 0; i < 4; ++i) hdr[i] = (uint8_t)(magic >> (8 * i));
+    hdr[4] = (uint8_t)bdx;
+    hdr[5] = (uint8_t)bdy;
+    hdr[6] = 1;
+    for (int i = 0; i < 3; ++i) {
+        hdr[7 + i] = (uint8_t)(width >> (8 * i));
+        hdr[10 + i] = (uint8_t)(height >> (8 * i));
+    }
+    hdr[13] = 1; hdr[14] = 0; hdr[15] = 0;
+    FILE* f = fopen(path, "wb");
+    if (!f) return set_error(ASTC_ERR_IO, std::string("cannot open for writing: ") + path);
+    const bool ok = fwrite(hdr, 1, 16, f) == 16 && fwrite(blocks, 1, blocks_size, f) == blocks_size;
+    const bool closed = fclose(f) == 0;
+    if (!ok || !closed) return set_error(ASTC_ERR_IO, std::string("write failed: ") + path);
+    return ASTC_OK;
+}
+
+astc_status astc_load_file(const char* path, int* bdx, int* bdy, int* width, int* height,
+                           uint8_t* blocks, size_t capacity, size_t* blocks_size) {
+    if (!path || !bdx || !bdy || !width || !height || !blocks_size)
+        return set_error(ASTC_ERR_INVALID_ARG, "NULL argument");
+    FILE* f = fopen(path, "rb");
+    if (!f) return set_error(ASTC_ERR_IO, std::string("cannot open: ") + path);
+    uint8_t hdr[16];
+    if (fread(hdr, 1, 16, f) != 16) {
+        fclose(f);
+        return set_error(ASTC_ERR_FORMAT, "file shorter than the 16-byte header");
+    }
+    const uint32_t magic = hdr[0] | (hdr[1] << 8) | (hdr[2] << 16) | ((uint32_t)hdr[3] << 24);
+    if (magic != 0x5CA1AB13u) {
+        fclose(f);
+        return set_error(ASTC_ERR_FORMAT, "bad magic (expected 0x5CA1AB13)");
+    }
+    const int x = hdr[7] | (hdr[8] << 8) | (hdr[9] << 16);
+    const int y = hdr[10] | (hdr[11] << 8) | (hdr[12] << 16);
+    const int z = hdr[13] | (hdr[14] << 8) | (hdr[15] << 16);
+    if (hdr[4] < 2 || hdr[5] < 2 || hdr[6] != 1 || x <= 0 || y <= 0 || z != 1) {
+        fclose(f);
+        return set_error(ASTC_ERR_FORMAT, "unsupported header (only 2-D, z = 1)");
+    }
+    const size_t need = (size_t)16 * ((x + hdr[4] - 1) / hdr[4]) * ((y + hdr[5] - 1) / hdr[5]);
+    *bdx = hdr[4];
+    *bdy = hdr[5];
+    *width = x;
+    *height = y;
+    *blocks_size = need;
+    astc_status st = ASTC_OK;
+    if (blocks) {
+        if (capacity < need) {
+            st = set_error(ASTC_ERR_INVALID_ARG, "capacity smaller than the block data");
+        } else if (fread(blocks, 1, need, f) != need) {
+            st = set_error(ASTC_ERR_FORMAT, "file truncated");
+        }
+    }
+    fclose(f);
+    return st;
+}
+
+astc_status astc_decode_gpu(const uint8_t* blocks, int width, int height, int block_w, int block_h,
+                            int srgb, int memory, void* stream, uint8_t* out_rgba8) {
+    try {
+        if (!blocks || !out_rgba8) return set_error(ASTC_ERR_INVALID_ARG, "NULL pointer");
+        if (width <= 0 || height <= 0 || width > 0xFFFFFF || height > 0xFFFFFF)
+            return set_error(ASTC_ERR_INVALID_ARG, "bad image size");
+        if (block_w < 4 || block_w > 12 || block_h < 4 || block_h > 12)
+            return set_error(ASTC_ERR_INVALID_ARG, "block footprint must be 4..12 per axis");
+        if (memory != ASTC_MEMORY_HOST && memory != ASTC_MEMORY_DEVICE)
+            return set_error(ASTC_ERR_INVALID_ARG, "bad memory kind");
+        DevicePool* pool = nullptr;
+        int dev = 0;
+        astc_status st;
+        if ((st = pool_for_current(&pool, &dev)) != ASTC_OK) return st;
+        std::lock_guard<std::mutex> lk(pool->mu);
+        if ((st = pool_init_locked(*pool, dev)) != ASTC_OK) return st;
+        cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : pool->stream;
+        const size_t nblk = (size_t)((width + block_w - 1) / block_w) * ((height + block_h - 1) / block_h);
+        const size_t in_bytes = 16 * nblk, out_bytes = (size_t)width * height * 4;
+        if (memory == ASTC_MEMORY_DEVICE) {
+            if ((st = check_device_pointer(blocks, "blocks")) != ASTC_OK) return st;
+            if ((st = check_device_pointer(out_rgba8, "out_rgba8")) != ASTC_OK) return st;
+            if (reinterpret_cast<uintptr_t>(blocks) % 16 != 0 || reinterpret_cast<uintptr_t>(out_rgba8) % 4 != 0)
+                return set_error(ASTC_ERR_INVALID_ARG, "blocks must be 16-byte and out 4-byte aligned");
+            cudaError_t e = launch_decode(blocks, width, height, block_w, block_h, srgb, out_rgba8, s);
+            if (e != cudaSuccess) return cuda_error(e, "decode kernel launch");
+            if (!stream && (e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_error(e, "decode");
+            return ASTC_OK;
+        }
+        if ((st = grow(&pool->d_in, &pool->in_cap, in_bytes)) != ASTC_OK) return st;
+        if ((st = grow(&pool->d_out, &pool->out_cap, out_bytes)) != ASTC_OK) return st;
+        cudaError_t e = cudaMemcpyAsync(pool->d_in, blocks, in_bytes, cudaMemcpyHostToDevice, s);
+        if (e != cudaSuccess) return cuda_error(e, "host-to-device copy");
+        e = launch_decode(pool->d_in, width, height, block_w, block_h, srgb, pool->d_out, s);
+        if (e != cudaSuccess) return cuda_error(e, "decode kernel launch");
+        e = cudaMemcpyAsync(out_rgba8, pool->d_out, out_bytes, cudaMemcpyDeviceToHost, s);
+        if (e != cudaSuccess) return cuda_error(e, "device-to-host copy");
+        e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) return cuda_error(e, "decode");
+        return ASTC_OK;
+    } catch (...) {
+        return set_error(ASTC_ERR_CUDA, "unexpected exception");
+    }
+}
+
+astc_status astc_sse_gpu(const uint8_t* a, const uint8_t* b, size_t texels, int memory, void* stream,
+                         uint64_t sse_rgba[4]) {
+    try {
+        if (!a || !b || !sse_rgba) return set_error(ASTC_ERR_INVALID_ARG, "NULL pointer");
+        if (memory != ASTC_MEMORY_HOST && memory != ASTC_MEMORY_DEVICE)
+            return set_error(ASTC_ERR_INVALID_ARG, "bad memory kind");
+        DevicePool* pool = nullptr;
+        int dev = 0;
+        astc_status st;
+        if ((st = pool_for_current(&pool, &dev)) != ASTC_OK) return st;
+        std::lock_guard<std::mutex> lk(pool->mu);
+        if ((st = pool_init_locked(*pool, dev)) != ASTC_OK) return st;
+        cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : pool->stream;
+        if (!pool->d_sse) {
+            cudaError_t e = cudaMalloc(reinterpret_cast<void**>(&pool->d_sse), 4 * sizeof(unsigned long long));
+            if (e != cudaSuccess) return cuda_error(e, "cudaMalloc of the SSE accumulator");
+        }
+        const uint8_t* da = a;
+        const uint8_t* db = b;
+        if (memory == ASTC_MEMORY_HOST) {
+            const size_t bytes = texels * 4;
+            if ((st = grow(&pool->d_in, &pool->in_cap, bytes)) != ASTC_OK) return st;
+            if ((st = grow(&pool->d_out, &pool->out_cap, bytes)) != ASTC_OK) return st;
+            cudaError_t e = cudaMemcpyAsync(pool->d_in, a, bytes, cudaMemcpyHostToDevice, s);
+            if (e == cudaSuccess) e = cudaMemcpyAsync(pool->d_out, b, bytes, cudaMemcpyHostToDevice, s);
+            if (e != cudaSuccess) return cuda_error(e, "host-to-device copy");
+            da = pool->d_in;
+            db = pool->d_out;
+        } else {
+            if ((st = check_device_pointer(a, "a")) != ASTC_OK) return st;
+            if ((st = check_device_pointer(b, "b")) != ASTC_OK) return st;
+            if (reinterpret_cast<uintptr_t>(a) % 4 != 0 || reinterpret_cast<uintptr_t>(b) % 4 != 0)
+                return set_error(ASTC_ERR_INVALID_ARG, "images must be 4-byte aligned");
+        }
+        cudaError_t e = cudaMemsetAsync(pool->d_sse, 0, 4 * sizeof(unsigned long long), s);
+        if (e != cudaSuccess) return cuda_error(e, "cudaMemsetAsync");
+        e = launch_sse(da, db, texels, pool->d_sse, s);
+        if (e != cudaSuccess) return cuda_error(e, "sse kernel launch");
+        unsigned long long h[4];
+        e = cudaMemcpyAsync(h, pool->d_sse, sizeof(h), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) return cuda_error(e, "sse");
+        for (int i = 0; i < 4; ++i) sse_rgba[i] = h[i];
+        return ASTC_OK;
+    } catch (...) {
+        return set_error(ASTC_ERR_CUDA, "unexpected exception");
+    }
+}
+
+const char* astc_last_error(void) { return t_last_error.c_str(); }
+
+const char* astc_status_string(astc_status s) {
+    switch (s) {
+    case ASTC_OK: return "ok";
+    case ASTC_ERR_INVALID_ARG: return "invalid argument";
+    case ASTC_ERR_UNSUPPORTED: return "unsupported";
+    case ASTC_ERR_CUDA: return "CUDA error";
+    case ASTC_ERR_OUT_OF_MEMORY: return "out of memory";
+    case ASTC_ERR_IO: return "I/O error";
+    case ASTC_ERR_TIMEOUT: return "timeout";
+    case ASTC_ERR_BUSY: return "busy";
+    case ASTC_ERR_CANCELLED: return "cancelled";
+    case ASTC_ERR_FORMAT: return "bad .astc format";
+    }
+    return "unknown status";
+}
+
+uint64_t astc_kernel_launch_count(void) { return g_launches.load(); }
+
+void astc_shutdown(void) {
+    int cur = 0;
+    const bool have = cudaGetDevice(&cur) == cudaSuccess;
+    for (int d = 0; d < kMaxDevices; ++d) {
+        DevicePool& p = g_pools[d];
+        std::lock_guard<std::mutex> lk(p.mu);
+        if (!p.ready && !p.d_in && !p.d_out && !p.d_sse) continue;
+        if (cudaSetDevice(d) != cudaSuccess) { cudaGetLastError(); continue; }
+        if (p.stream) cudaStreamSynchronize(p.stream);
+        if (p.d_in) cudaFree(p.d_in);
+        if (p.d_out) cudaFree(p.d_out);
+        if (p.d_sse) cudaFree(p.d_sse);
+        if (p.stream) cudaStreamDestroy(p.stream);
+        p.d_in = p.d_out = nullptr;
+        p.d_sse = nullptr;
+        p.in_cap = p.out_cap = 0;
+        p.stream = nullptr;
+        p.ready = false;
+    }
+    if (have) cudaSetDevice(cur);
+    cudaGetLastError();
+}
+
+}  // extern "C"

@@ -1,0 +1,45 @@
+// astc_internal.h -- declarations shared by the library's translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "../../include/astc_gb300.h"
+
+namespace astc {
+
+// One texture to encode, everything already on the device.
+struct EncodeJob {
+    const uint8_t* in;    // RGBA8, 4-byte aligned
+    size_t pitch;         // bytes between rows, multiple of 4
+    int width, height;
+    int block_dim;        // 4 or 6
+    int has_alpha, is_normal, srgb, border, precision;
+    uint8_t* out;         // 16 * nblocks bytes, 16-byte aligned
+};
+
+inline int blocks_x(int w, int dim) { return (w + dim - 1) / dim; }
+inline int blocks_y(int h, int dim) { return (h + dim - 1) / dim; }
+
+// Kernel launchers (astc_encode.cu).  Return cudaSuccess or the launch error.
+cudaError_t launch_encode(const EncodeJob& job, cudaStream_t stream);
+cudaError_t ensure_encode_constants(int device);
+
+// Decoder / SSE launchers (astc_decode.cu).
+cudaError_t launch_decode(const uint8_t* blocks, int width, int height, int bw, int bh,
+                          int srgb, uint8_t* out, cudaStream_t stream);
+cudaError_t launch_sse(const uint8_t* a, const uint8_t* b, size_t texels,
+                       unsigned long long* d_sse4, cudaStream_t stream);
+
+// Error plumbing (astc_capi.cu).
+astc_status set_error(astc_status st, const std::string& msg);
+astc_status cuda_error(cudaError_t e, const char* what);
+void count_launches(uint64_t n);
+
+// sRGB -> linear, the committed formula: IEC 61966-2-1 piecewise curve in
+// double, rounded once to float, then multiplied by 255 in float.
+float srgb_texel_value(int code);
+
+}  // namespace astc

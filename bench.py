@@ -1,0 +1,432 @@
+"""Benchmark of the GB300 ASTC encoder (one JSON line on rank 0).
+
+Workload (default): the 6x6 LDR RGBA sRGB encode with edge clamp of a
+2048x2048 RGBA8 texture (342x342 blocks) -- the configuration the headline
+metric "encoded Mtexels/s" is quoted on.  One step encodes a batch of 16
+distinct 2048x2048 textures (268 MB of input, larger than the 129 MB L2, so
+no step reads its inputs from L2), each through the C ABI
+(astc_encode_gpu_pitched, device memory, on torch's current stream).
+
+* value      -- Mtexels/s with inputs resident in HBM, timed with CUDA events
+                around every launch on the launching stream (max over ranks).
+* e2e        -- the same metric through the same entry point with pinned
+                HOST buffers: each texture's host->device copy, the encode and
+                the device->host copy of its blocks are inside the timed region.
+* roofline   -- the dominant kernel's algorithmic bytes (4 B/texel read +
+                16 B/block written) per launch over its mean launch time,
+                against the measured HBM copy bandwidth; roofline_fp32 gives
+                the same launch in algorithmic FP32 FLOPs (counted from the
+                oracle) against an FP32 SGEMM peak measured in this run.
+* cpu_baseline -- the FP32 oracle (a CPU restatement of the reference
+                shader; the reference itself is D3D11-only) with OpenMP on all
+                host cores, on a bounded sample of the same workload.
+``--impl reference`` times that CPU restatement alone (the reference arm).
+Under torchrun each rank encodes its own batch (weak scaling, no data-path
+collective); a barrier and a max-reduce of the elapsed time bracket the run.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+TEXTURES_PER_STEP = 16
+METRIC = "encoded Mtexels/s"
+
+
+def _parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="6x6_rgba_srgb_2048")
+    ap.add_argument("--no-extra", action="store_true", help="skip the secondary workloads")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region (NVML through ctypes; nvidia-smi fallback)
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    REASONS = {0x1: "gpu_idle", 0x2: "applications_clocks_setting", 0x4: "sw_power_cap",
+               0x8: "hw_slowdown", 0x10: "sync_boost", 0x20: "sw_thermal_slowdown",
+               0x40: "hw_thermal_slowdown", 0x80: "hw_power_brake_slowdown",
+               0x100: "display_clock_setting"}
+
+    def __init__(self, index: int):
+        self.index = index
+        self.samples: list[tuple[int, int]] = []
+        self.max_mhz = None
+        self._stop = threading.Event()
+        self._thr = None
+        self._nvml = None
+        self._handle = None
+        try:
+            nv = ctypes.CDLL("libnvidia-ml.so.1")
+            if nv.nvmlInit_v2() == 0:
+                h = ctypes.c_void_p()
+                if nv.nvmlDeviceGetHandleByIndex_v2(index, ctypes.byref(h)) == 0:
+                    self._nvml, self._handle = nv, h
+                    m = ctypes.c_uint()
+                    if nv.nvmlDeviceGetMaxClockInfo(h, 1, ctypes.byref(m)) == 0:   # NVML_CLOCK_SM
+                        self.max_mhz = int(m.value)
+        except OSError:
+            pass
+
+    def _sample(self):
+        nv, h = self._nvml, self._handle
+        c, r = ctypes.c_uint(), ctypes.c_ulonglong()
+        ok = nv.nvmlDeviceGetClockInfo(h, 1, ctypes.byref(c)) == 0
+        ok &= nv.nvmlDeviceGetCurrentClocksEventReasons(h, ctypes.byref(r)) == 0
+        if ok:
+            self.samples.append((int(c.value), int(r.value)))
+
+    def _run(self):
+        while not self._stop.is_set():
+            self._sample()
+            time.sleep(0.002)
+
+    def start(self):
+        if self._nvml is not None:
+            self._thr = threading.Thread(target=self._run, daemon=True)
+            self._thr.start()
+
+    def stop(self) -> dict:
+        if self._thr is not None:
+            self._stop.set()
+            self._thr.join()
+            self._sample()
+        if not self.samples:
+            return self._smi_once()
+        mhz = sorted(s[0] for s in self.samples)
+        bits = 0
+        for _, r in self.samples:
+            bits |= r
+        reasons = [n for b, n in self.REASONS.items() if bits & b and n != "gpu_idle"]
+        return {"sm_mhz": mhz[len(mhz) // 2], "sm_max_mhz": self.max_mhz, "reasons": reasons,
+                "samples": len(self.samples), "source": "nvml"}
+
+    def _smi_once(self) -> dict:
+        try:
+            q = subprocess.run(["nvidia-smi", "-i", str(self.index), "--query-gpu=clocks.sm,clocks.max.sm",
+                                "--format=csv,noheader,nounits"], capture_output=True, text=True,
+                               timeout=20).stdout.strip().split(",")
+            return {"sm_mhz": int(q[0]), "sm_max_mhz": int(q[1]), "reasons": [], "samples": 1,
+                    "source": "nvidia-smi (after the timed region)"}
+        except Exception as exc:  # noqa: BLE001
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "error": str(exc)}
+
+
+def _peaks() -> dict:
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except OSError:
+        return {}
+
+
+def _dist():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def _texture_batch(torch, base: np.ndarray, count: int, salt: int):
+    """`count` distinct device textures with the statistics of `base` (2-D shifts)."""
+    dev = torch.from_numpy(base).cuda()
+    h, w = base.shape[:2]
+    out = []
+    for i in range(count):
+        dy = (i * 97 + salt * 389) % h
+        dx = (i * 331 + salt * 151) % w
+        out.append(torch.roll(dev, shifts=(dy, dx), dims=(0, 1)).contiguous())
+    return out
+
+
+def _fp32_peak_tflops(torch) -> float:
+    """FP32 peak of this GPU, measured as an 8192^3 SGEMM with TF32 off."""
+    prev = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    n = 8192
+    a = torch.randn(n, n, device="cuda", dtype=torch.float32)
+    b = torch.randn(n, n, device="cuda", dtype=torch.float32)
+    for _ in range(2):
+        torch.mm(a, b)
+    best = float("inf")
+    for _ in range(5):
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        torch.mm(a, b)
+        e.record()
+        torch.cuda.synchronize()
+        best = min(best, s.elapsed_time(e) / 1e3)
+    torch.backends.cuda.matmul.allow_tf32 = prev
+    del a, b
+    return 2.0 * n ** 3 / best / 1e12
+
+
+def _cpu_baseline(img: np.ndarray, spec: dict, min_seconds: float = 2.0) -> dict:
+    from oracle import oracle
+    threads = os.cpu_count() or 1
+    oracle.encode(img[:64, :64], **spec, threads=threads)            # build + warm
+    reps, t0 = 0, time.perf_counter()
+    while True:
+        oracle.encode(img, **spec, threads=threads)
+        reps += 1
+        el = time.perf_counter() - t0
+        if el >= min_seconds:
+            break
+    texels = img.shape[0] * img.shape[1] * reps
+    return {"value": texels / el / 1e6, "unit": "Mtexels/s", "cores": threads, "kind": "port",
+            "sample": f"{reps} full encodes of one {img.shape[1]}x{img.shape[0]} texture "
+                      f"({el:.2f} s wall on {threads} threads)"}
+
+
+def run_reference(args) -> None:
+    world, rank, _ = _dist()
+    if rank != 0:
+        return
+    from astc_encoder_gb300 import synth
+    from oracle import oracle
+    img, spec = synth.workload(args.workload)
+    threads = os.cpu_count() or 1
+    oracle.encode(img[:64, :64], **spec, threads=threads)
+    for _ in range(args.warmup):
+        oracle.encode(img, **spec, threads=threads)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        oracle.encode(img, **spec, threads=threads)
+    el = time.perf_counter() - t0
+    texels = img.shape[0] * img.shape[1]
+    value = texels * args.steps / el / 1e6
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "Mtexels/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": el / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": args.workload, "texture": f"{img.shape[1]}x{img.shape[0]}",
+                   "textures_per_step": 1, **spec},
+        "cpu_baseline": {"value": value, "unit": "Mtexels/s", "cores": threads, "kind": "port",
+                         "sample": f"{args.steps} timed encodes of one texture; the reference "
+                                   "shader is D3D11-only (unavailable on this box), so its FP32 "
+                                   "CPU restatement (oracle/) runs with OpenMP"},
+        "e2e": {"value": value, "unit": "Mtexels/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def _time_launches(torch, native, texs, outs, spec, steps, counted=True):
+    """Runs `steps` steps over the batch; returns (per-launch ms list, step ms list, launches)."""
+    h, w = texs[0].shape[:2]
+    stream = torch.cuda.current_stream()
+    lib = native.load_library()
+    opts = ctypes.byref(native.make_opts(memory=native.Memory.DEVICE, stream=stream.cuda_stream,
+                                         **spec))
+    ptrs = [(t.data_ptr(), o.data_ptr()) for t, o in zip(texs, outs)]
+    enc = lib.astc_encode_gpu_pitched
+    ev = [[(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+           for _ in texs] for _ in range(steps)]
+    l0 = native.kernel_launch_count()
+    for s in range(steps):
+        for i, (src, dst) in enumerate(ptrs):
+            a, b = ev[s][i]
+            a.record(stream)
+            st = enc(src, w, h, w * 4, opts, dst)
+            b.record(stream)
+            if st != 0:
+                raise native.AstcError(st, lib.astc_last_error().decode())
+    torch.cuda.synchronize()
+    launches = native.kernel_launch_count() - l0
+    per = [a.elapsed_time(b) for row in ev for a, b in row]
+    per_step = [ev[s][0][0].elapsed_time(ev[s][-1][1]) for s in range(steps)]
+    return per, per_step, launches
+
+
+def run_ours(args) -> None:
+    import torch
+    world, rank, local = _dist()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    import astc_encoder_gb300 as native
+    from astc_encoder_gb300 import build, synth
+    build.build()
+    native.load_library()
+
+    img, spec = synth.workload(args.workload)
+    h, w = img.shape[:2]
+    dim = spec["block_dim"]
+    nblocks = ((w + dim - 1) // dim) * ((h + dim - 1) // dim)
+    texs = _texture_batch(torch, img, TEXTURES_PER_STEP, salt=rank)
+    outs = [torch.empty((nblocks, 16), dtype=torch.uint8, device="cuda") for _ in texs]
+
+    # warm-up (untimed) + a short sustained burn so clocks settle
+    _time_launches(torch, native, texs, outs, spec, max(3, args.warmup))
+    t_end = time.perf_counter() + 0.5
+    while time.perf_counter() < t_end:
+        _time_launches(torch, native, texs, outs, spec, 2)
+
+    clocks = ClockSampler(local)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    t0 = time.perf_counter()
+    per, per_step, launches = _time_launches(torch, native, texs, outs, spec, args.steps)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    dev_s = sum(per_step) / 1e3
+    if world > 1:
+        t = torch.tensor([dev_s], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        dev_s = float(t.item())
+    texels_step = h * w * len(texs)
+    value = world * texels_step * args.steps / dev_s / 1e6
+
+    # e2e through the same entry point with pinned host buffers
+    host_in = [t.cpu().pin_memory() for t in texs]
+    host_out = [torch.empty((nblocks, 16), dtype=torch.uint8).pin_memory() for _ in texs]
+    lib = native.load_library()
+    opts = native.make_opts(memory=native.Memory.HOST, **spec)
+
+    def e2e_step():
+        for hi, ho in zip(host_in, host_out):
+            st = lib.astc_encode_gpu(hi.data_ptr(), w, h, ctypes.byref(opts), ho.data_ptr())
+            if st != 0:
+                raise native.AstcError(st, lib.astc_last_error().decode())
+
+    for _ in range(max(3, args.warmup)):
+        e2e_step()
+    e2e_steps = max(5, args.steps // 2)
+    if world > 1:
+        torch.distributed.barrier()
+    t1 = time.perf_counter()
+    for _ in range(e2e_steps):
+        e2e_step()
+    e2e_s = time.perf_counter() - t1
+    if world > 1:
+        t = torch.tensor([e2e_s], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = world * texels_step * e2e_steps / e2e_s / 1e6
+
+    if rank != 0:
+        if world > 1:
+            torch.distributed.barrier()
+            torch.distributed.destroy_process_group()
+        return
+
+    # roofline of the dominant kernel
+    from oracle import oracle
+    peaks = _peaks()
+    mean_launch_s = float(np.mean(per)) / 1e3
+    alg_bytes = h * w * 4 + nblocks * 16
+    hbm_peak = peaks.get("hbm_gbs")
+    achieved_gbs = alg_bytes / mean_launch_s / 1e9
+    flops = oracle.flops_per_block(dim, spec["has_alpha"], spec["is_normal"]) * nblocks
+    fp32_peak = _fp32_peak_tflops(torch)
+    achieved_tf = flops / mean_launch_s / 1e12
+    kernel = (f"astc_encode_blocks_fp32<{dim},{int(spec['has_alpha'])},{int(spec['is_normal'])},"
+              f"{int(spec['srgb'])}>")
+
+    # quality of this workload: CUDA vs FP32 oracle (identical blocks) and
+    # PSNR of both against the FP64 twin's PSNR, decoded by the GPU decoder
+    got = outs[0].cpu().numpy()
+    tex0 = texs[0].cpu().numpy()
+    ora = oracle.encode(tex0, **spec)
+    f64 = oracle.encode(tex0, **spec, fp64=True)
+
+    def psnr(blocks):
+        d = native.decode(blocks, w, h, dim)
+        s = native.sse(d, tex0)
+        ch = 4 if spec["has_alpha"] else 3
+        return native.psnr_from_sse(float(s[:ch].sum()), h * w * ch)
+
+    quality = {"identical_blocks_vs_fp32_oracle": float(np.all(got == ora, axis=1).mean()),
+               "psnr_db": psnr(got), "psnr_fp32_oracle_db": psnr(ora), "psnr_fp64_oracle_db": psnr(f64)}
+    quality["psnr_gap_to_fp64_db"] = quality["psnr_fp64_oracle_db"] - quality["psnr_db"]
+
+    extra = {}
+    if not args.no_extra:
+        for name in ("4x4_rgb_512", "4x4_normal_4096"):
+            if name == args.workload:
+                continue
+            ximg, xspec = synth.workload(name)
+            xh, xw = ximg.shape[:2]
+            xd = xspec["block_dim"]
+            xnb = ((xw + xd - 1) // xd) * ((xh + xd - 1) // xd)
+            reps = max(1, (268 << 20) // (xh * xw * 4))     # keep each step above L2 size
+            xt = _texture_batch(torch, ximg, reps, salt=7)
+            xo = [torch.empty((xnb, 16), dtype=torch.uint8, device="cuda") for _ in xt]
+            _time_launches(torch, native, xt, xo, xspec, 3)
+            xper, xsteps, _ = _time_launches(torch, native, xt, xo, xspec, 10)
+            extra[name] = {"value": xh * xw * reps * 10 / (sum(xsteps) / 1e3) / 1e6, "unit": "Mtexels/s",
+                           "mean_launch_us": float(np.mean(xper)) * 1e3,
+                           "textures_per_step": reps}
+            del xt, xo
+
+    cpu = None if args.no_cpu else _cpu_baseline(img, spec)
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "Mtexels/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_s / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": args.workload, "texture": f"{w}x{h}", "blocks_per_texture": nblocks,
+                   "textures_per_step": len(texs), "block_dim": dim, "has_alpha": spec["has_alpha"],
+                   "is_normal": spec["is_normal"], "srgb": spec["srgb"],
+                   "border": "clamp" if spec["border"] else "zero", "precision": "fp32",
+                   "l2": f"inputs {texels_step * 4 / 2**20:.0f} MiB per step, distinct per texture "
+                         "(> 129 MB L2); no flush needed",
+                   "parallelism": f"replicas{world}"},
+        "e2e": {"value": e2e_value, "unit": "Mtexels/s",
+                "h2d_bytes_per_step": texels_step * 4, "d2h_bytes_per_step": nblocks * 16 * len(texs),
+                "entry_point": "astc_encode_gpu (ASTC_MEMORY_HOST, pinned buffers)",
+                "steps": e2e_steps},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "kernel": kernel, "achieved": achieved_gbs,
+                     "peak": hbm_peak, "unit": "GB/s",
+                     "frac": (achieved_gbs / hbm_peak) if hbm_peak else None,
+                     "traffic": None, "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)",
+                     "alg_bytes_per_launch": alg_bytes, "mean_launch_us": mean_launch_s * 1e6},
+        "roofline_fp32": {"bound": "fp32_issue", "achieved": achieved_tf, "peak": fp32_peak,
+                          "unit": "TFLOP/s", "frac": achieved_tf / fp32_peak,
+                          "flops_per_launch": flops,
+                          "peak_source": "SGEMM 8192^3 fp32 (TF32 off) measured in this run"},
+        "quality": quality,
+        "clocks": clk,
+        "wall_s_timed_region": wall,
+        "extra_workloads": extra,
+    }
+    if cpu is not None:
+        line["cpu_baseline"] = cpu
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.barrier()
+        torch.distributed.destroy_process_group()
+
+
+def main() -> None:
+    args = _parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

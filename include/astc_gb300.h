@@ -1,0 +1,143 @@
+/*
+ * astc_gb300.h -- C ABI of the GB300 (sm_103a) ASTC LDR block encoder.
+ *
+ * Plain pointers and sizes only; no CUDA, torch or C++ types in any
+ * signature (streams are passed as void*, i.e. a cudaStream_t).
+ *
+ * Reference interfaces replaced (niepp/astc_encoder):
+ *   encode_option                 astc_encode.h:14-28   -> astc_opts
+ *   encode_astc + Dispatch        astc_encode.h:87-194  -> astc_encode_gpu
+ *   read_gpu (staging + Map)      astc_save.h:34-50     -> the D2H copy inside
+ *                                                          astc_encode_gpu
+ *   astc_header / save_astc       astc_save.h:5-14,52-76 -> astc_save_file
+ *   MainCS (one block per thread) ASTC_Encode.hlsl:553-582 -> the CUDA kernels
+ *                                                          behind astc_encode_gpu
+ *
+ * Errors: every entry point returns an astc_status; a human-readable message
+ * for the last failure on the calling thread is in astc_last_error().  No
+ * entry point aborts the process or lets a C++ exception escape.
+ */
+#ifndef ASTC_GB300_H
+#define ASTC_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ASTC_GB300_VERSION_MAJOR 1
+#define ASTC_GB300_VERSION_MINOR 0
+
+typedef enum astc_status {
+    ASTC_OK = 0,
+    ASTC_ERR_INVALID_ARG = 1,    /* bad pointer, size or option            */
+    ASTC_ERR_UNSUPPORTED = 2,    /* option combination not implemented     */
+    ASTC_ERR_CUDA = 3,           /* a CUDA runtime call failed             */
+    ASTC_ERR_OUT_OF_MEMORY = 4,  /* device or pinned allocation failed     */
+    ASTC_ERR_IO = 5,             /* file open / read / write failed        */
+    ASTC_ERR_TIMEOUT = 6,        /* a bounded device wait ran out          */
+    ASTC_ERR_BUSY = 7,           /* admission refused (no memory / slots)  */
+    ASTC_ERR_CANCELLED = 8,      /* request cancelled before it ran        */
+    ASTC_ERR_FORMAT = 9          /* malformed .astc file                   */
+} astc_status;
+
+typedef enum astc_border {
+    ASTC_BORDER_ZERO = 0,        /* texels outside the image read as 0
+                                    (the reference's Texture2D.Load rule,
+                                    ASTC_Encode.hlsl:574)                   */
+    ASTC_BORDER_CLAMP = 1        /* texels outside repeat the edge texel    */
+} astc_border;
+
+typedef enum astc_precision {
+    ASTC_PRECISION_FP32 = 0,     /* the reference's FP32 math, bit-exact
+                                    with the FP32 oracle                    */
+    ASTC_PRECISION_HALF2 = 1     /* per-texel projections in packed half2,
+                                    FP32 accumulation                       */
+} astc_precision;
+
+typedef enum astc_memory {
+    ASTC_MEMORY_HOST = 0,        /* input and output are host pointers      */
+    ASTC_MEMORY_DEVICE = 1       /* input and output are device pointers    */
+} astc_memory;
+
+/* Encoder options: the reference's encode_option (astc_encode.h:14-28) plus
+ * the GPU-side controls.  Use astc_opts_init() for the reference defaults. */
+typedef struct astc_opts {
+    int block_dim;   /* 4 (ASTC 4x4) or 6 (ASTC 6x6)               is4x4   */
+    int has_alpha;   /* CEM 12 + QUANT_6 weights, else CEM 8 + QUANT_12    */
+    int is_normal;   /* normal map: blue and alpha forced to 1.0           */
+    int srgb;        /* input is sRGB-encoded: RGB are linearised before
+                        the fit (R8G8B8A8_UNORM_SRGB sampling, main.cpp:38) */
+    int border;      /* astc_border                                        */
+    int precision;   /* astc_precision                                     */
+    int memory;      /* astc_memory: where `rgba8` and `out` live          */
+    void* stream;    /* cudaStream_t to run on asynchronously; NULL = the
+                        library's own stream, and the call returns when
+                        the result is in `out`                              */
+} astc_opts;
+
+/* Fills the reference defaults: 4x4, no alpha, not a normal map, linear,
+ * zero border, FP32, host memory, synchronous. */
+void astc_opts_init(astc_opts* opts);
+
+/* Bytes of ASTC blocks for a w x h image: 16 * ceil(w/dim) * ceil(h/dim). */
+size_t astc_encoded_size(int width, int height, int block_dim);
+
+/* Encode one RGBA8 image (tightly packed rows, row 0 first, 4 bytes per
+ * texel) into 16-byte ASTC blocks in row-major block order.
+ * Replaces encode_astc (astc_encode.h:87) + read_gpu (astc_save.h:34).
+ * `out` must hold astc_encoded_size(width, height, opts->block_dim) bytes. */
+astc_status astc_encode_gpu(const uint8_t* rgba8, int width, int height,
+                            const astc_opts* opts, uint8_t* out);
+
+/* As astc_encode_gpu with an explicit input row pitch in bytes (>= 4*width,
+ * a multiple of 4). */
+astc_status astc_encode_gpu_pitched(const uint8_t* rgba8, int width, int height,
+                                    size_t row_pitch, const astc_opts* opts,
+                                    uint8_t* out);
+
+/* Write a .astc file: the 16-byte header of astc_save.h:5-14 (magic
+ * 0x5CA1AB13, block dims, 24-bit x/y/z sizes, z = 1) then the blocks.
+ * Replaces save_astc (astc_save.h:52-76), which did not check fopen. */
+astc_status astc_save_file(const char* path, int block_dim_x, int block_dim_y,
+                           int width, int height, const uint8_t* blocks,
+                           size_t blocks_size);
+
+/* Read a .astc file written by astc_save_file (or any 2-D .astc).  On
+ * ASTC_OK *width/*height/*block_dim_x/*block_dim_y are set; when `blocks` is
+ * non-NULL up to `capacity` block bytes are copied.  *blocks_size receives
+ * the block byte count.  (No counterpart in the reference, which only
+ * writes.) */
+astc_status astc_load_file(const char* path, int* block_dim_x, int* block_dim_y,
+                           int* width, int* height, uint8_t* blocks,
+                           size_t capacity, size_t* blocks_size);
+
+/* Integer-only ASTC LDR decode of `blocks` (block_w x block_h footprint) to
+ * tightly packed RGBA8 on the GPU; memory/stream as in astc_opts.  Error
+ * blocks decode to magenta.  (No counterpart in the reference.) */
+astc_status astc_decode_gpu(const uint8_t* blocks, int width, int height,
+                            int block_w, int block_h, int srgb, int memory,
+                            void* stream, uint8_t* out_rgba8);
+
+/* Sum of squared differences between two RGBA8 images per channel (R, G, B,
+ * A), reduced on the GPU; both images in `memory`.  (No counterpart in the
+ * reference.) */
+astc_status astc_sse_gpu(const uint8_t* a, const uint8_t* b, size_t texels,
+                         int memory, void* stream, uint64_t sse_rgba[4]);
+
+/* Message for the last failed call on this thread ("" if none). */
+const char* astc_last_error(void);
+const char* astc_status_string(astc_status status);
+
+/* Number of kernels this library has launched in this process. */
+uint64_t astc_kernel_launch_count(void);
+
+/* Free the library's pooled device and pinned memory and streams. */
+void astc_shutdown(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,1136 @@
+/*
+ * astc_oracle.cpp -- CPU oracle for the ASTC block encoder.
+ *
+ * TEST INFRASTRUCTURE ONLY: the checker the CUDA encoder is compared with.
+ * The product library never links or loads this file.
+ *
+ * What it restates (niepp/astc_encoder, file:line):
+ *   texel fetch            ASTC_Encode.hlsl:561-580  (OOB Load = 0, normal map
+ *                                                      b=a=1, then x255)
+ *   encode_block           ASTC_Encode.hlsl:510-550
+ *   PCA / mean / cov       ASTC_Encode.hlsl:139-168
+ *   eigen_vector           ASTC_Encode.hlsl:93-106
+ *   find_min_max           ASTC_Encode.hlsl:108-137
+ *   encode_color           ASTC_Encode.hlsl:233-245, endpoint_ise 475-489
+ *   weights                ASTC_Encode.hlsl:256-260, 268-314, 316-393, 491-508
+ *   assemble_blockmode     ASTC_Encode.hlsl:446-473
+ *   assemble_block         ASTC_Encode.hlsl:400-444
+ *   ISE                    ASTC_IntegerSequenceEncoding.hlsl:5-276
+ *   scramble tables        ASTC_Table.hlsl:4-66
+ *
+ * The lookup tables are GENERATED here from the ASTC specification's
+ * definitions (trit/quint decode, weight unquantisation), never copied; the
+ * test suite compares them element-wise with the reference's arrays.
+ *
+ * FP32 arithmetic model (the shader's HLSL semantics, pinned once):
+ *   - round()        = round half to even (rintf), HLSL round / DXBC round_ne
+ *   - a*b+c (mad)    = ORACLE_FUSED_MAD ? fmaf(a,b,c) : (a*b)+c
+ *   - dot(a,b)       = a.x*b.x, then mad over y, z, w in that order
+ *   - length(v)      = sqrt(dot(v,v))        (correctly rounded sqrt)
+ *   - normalize(v)   = v * (1 / sqrt(dot(v,v)))
+ *   - x / N (const)  = ORACLE_CONST_DIV_AS_MUL ? x * (1/N) : x / N
+ *   - 1.0f / x       = correctly rounded division
+ *   - min/max/clamp  = fminf/fmaxf (no NaN can reach them)
+ *   - UNORM8 fetch   = c / 255 * 255 (exact: equals c for all 256 codes)
+ *   - sRGB fetch     = float(srgb_to_linear_f64(c / 255)) * 255
+ * Build with -ffp-contract=off so the compiler fuses nothing on its own.
+ * The default model was chosen by the identical-block count against the
+ * reference's own output textures/leaf.astc (see the golden tests).
+ */
+#include "astc_oracle.h"
+
+#include <cmath>
+#include <cstdint>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#ifndef ORACLE_FUSED_MAD
+#define ORACLE_FUSED_MAD 1
+#endif
+#ifndef ORACLE_CONST_DIV_AS_MUL
+#define ORACLE_CONST_DIV_AS_MUL 1
+#endif
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// quant methods (ASTC_Encode.hlsl:47-68)
+// ---------------------------------------------------------------------------
+enum {
+    QUANT_2 = 0, QUANT_3, QUANT_4, QUANT_5, QUANT_6, QUANT_8, QUANT_10, QUANT_12,
+    QUANT_16, QUANT_20, QUANT_24, QUANT_32, QUANT_40, QUANT_48, QUANT_64, QUANT_80,
+    QUANT_96, QUANT_128, QUANT_160, QUANT_192, QUANT_256, QUANT_MAX
+};
+const int kQuantLevels[QUANT_MAX] = {2, 3, 4, 5, 6, 8, 10, 12, 16, 20, 24, 32,
+                                     40, 48, 64, 80, 96, 128, 160, 192, 256};
+
+// ---------------------------------------------------------------------------
+// Tables generated from the specification
+// ---------------------------------------------------------------------------
+struct Tables {
+    int btq[QUANT_MAX][3];       // bits, trits, quints per range
+    int trits_enc[243];          // 5 trits -> 8-bit T
+    int trits_dec[256][5];       // 8-bit T -> 5 trits
+    int quints_enc[125];         // 3 quints -> 7-bit Q
+    int quints_dec[128][3];      // 7-bit Q -> 3 quints
+    int scramble[12][32];        // linear weight index -> ISE symbol
+    int unscramble[12][32];      // ISE symbol -> linear weight index
+    int wunq[12][32];            // ISE symbol -> weight 0..64
+    int cunq[QUANT_MAX][256];    // ISE symbol -> colour 0..255
+    float srgb_lut[256];         // float(srgb->linear) (not yet x255)
+    double srgb_lut64[256];
+    Tables();
+};
+
+inline int bit(int x, int i) { return (x >> i) & 1; }
+
+// Spec trit block decode: 8 bits T -> t0..t4.
+void decode_trit_block(int T, int t[5]) {
+    int C;
+    if (((T >> 2) & 7) == 7) {
+        C = (((T >> 5) & 7) << 2) | (T & 3);
+        t[4] = 2; t[3] = 2;
+    } else {
+        C = T & 31;
+        if (((T >> 5) & 3) == 3) { t[4] = 2; t[3] = bit(T, 7); }
+        else { t[4] = bit(T, 7); t[3] = (T >> 5) & 3; }
+    }
+    if ((C & 3) == 3) {
+        t[2] = 2; t[1] = bit(C, 4);
+        t[0] = (bit(C, 3) << 1) | (bit(C, 2) & ~bit(C, 3) & 1);
+    } else if (((C >> 2) & 3) == 3) {
+        t[2] = 2; t[1] = 2; t[0] = C & 3;
+    } else {
+        t[2] = bit(C, 4); t[1] = (C >> 2) & 3;
+        t[0] = (bit(C, 1) << 1) | (bit(C, 0) & ~bit(C, 1) & 1);
+    }
+}
+
+// Spec quint block decode: 7 bits Q -> q0..q2.
+void decode_quint_block(int Q, int q[3]) {
+    if (((Q >> 1) & 3) == 3 && ((Q >> 5) & 3) == 0) {
+        q[2] = (bit(Q, 0) << 2) | ((bit(Q, 4) & ~bit(Q, 0) & 1) << 1) |
+               (bit(Q, 3) & ~bit(Q, 0) & 1);
+        q[1] = 4; q[0] = 4;
+        return;
+    }
+    int C;
+    if (((Q >> 1) & 3) == 3) {
+        q[2] = 4;
+        C = (((Q >> 3) & 3) << 3) | (((~Q >> 5) & 3) << 1) | bit(Q, 0);
+    } else {
+        q[2] = (Q >> 5) & 3;
+        C = Q & 31;
+    }
+    if ((C & 7) == 5) { q[1] = 4; q[0] = (C >> 3) & 3; }
+    else { q[1] = (C >> 3) & 3; q[0] = C & 7; }
+}
+
+// Spec weight unquantisation of ISE symbol v (0..levels-1) -> 0..64.
+int spec_unquant_weight(int quant, int v) {
+    const int levels = kQuantLevels[quant];
+    (void)levels;
+    int bits = 0, trits = 0, quints = 0;
+    int l = kQuantLevels[quant];
+    while ((l & 1) == 0) { l >>= 1; ++bits; }
+    if (l == 3) trits = 1; else if (l == 5) quints = 1;
+    int r;
+    if (!trits && !quints) {
+        // bit replication to 6 bits
+        r = 0; int have = 0;
+        while (have < 6) { r = (r << bits) | v; have += bits; }
+        r >>= (have - 6);
+    } else if (bits == 0) {
+        int D = v;
+        r = trits ? (D == 0 ? 0 : D == 1 ? 32 : 63)
+                  : (D == 0 ? 0 : D == 1 ? 16 : D == 2 ? 32 : D == 3 ? 47 : 63);
+    } else {
+        const int D = v >> bits;
+        const int m = v & ((1 << bits) - 1);
+        const int A = (m & 1) ? 0x7F : 0;
+        const int b1 = bit(m, 1), b2 = bit(m, 2);
+        int B = 0, C = 0;
+        if (trits) {
+            if (bits == 1) { C = 50; B = 0; }
+            else if (bits == 2) { C = 23; B = (b1 << 6) | (b1 << 2) | b1; }
+            else { C = 11; B = (b2 << 6) | (b1 << 5) | (b2 << 1) | b1; }   // bits == 3
+        } else {
+            if (bits == 1) { C = 28; B = 0; }
+            else { C = 13; B = (b1 << 6) | (b1 << 1) | b1; }                 // bits == 2
+        }
+        int T = D * C + B;
+        T ^= A;
+        r = (A & 0x20) | (T >> 2);
+    }
+    if (r > 32) r += 1;
+    return r;
+}
+
+// Spec colour unquantisation of ISE symbol v -> 0..255.
+int spec_unquant_color(int quant, int v) {
+    int bits = 0, trits = 0, quints = 0;
+    int l = kQuantLevels[quant];
+    while ((l & 1) == 0) { l >>= 1; ++bits; }
+    if (l == 3) trits = 1; else if (l == 5) quints = 1;
+    if (!trits && !quints) {
+        int r = 0, have = 0;
+        while (have < 8) { r = (r << bits) | v; have += bits; }
+        return r >> (have - 8);
+    }
+    const int D = v >> bits;
+    const int m = v & ((1 << bits) - 1);
+    const int A = (m & 1) ? 0x1FF : 0;
+    const int b = bit(m, 1), c = bit(m, 2), d = bit(m, 3), e = bit(m, 4), f = bit(m, 5);
+    int B = 0, C = 0;
+    if (trits) {
+        switch (bits) {
+        case 1: C = 204; B = 0; break;
+        case 2: C = 93;  B = (b << 8) | (b << 4) | (b << 2) | (b << 1); break;
+        case 3: C = 44;  B = (c << 8) | (b << 7) | (c << 3) | (b << 2) | (c << 1) | b; break;
+        case 4: C = 22;  B = (d << 8) | (c << 7) | (b << 6) | (d << 2) | (c << 1) | b; break;
+        case 5: C = 11;  B = (e << 8) | (d << 7) | (c << 6) | (b << 5) | (e << 1) | d; break;
+        default: C = 5;  B = (f << 8) | (e << 7) | (d << 6) | (c << 5) | (b << 4) | f; break;
+        }
+    } else {
+        switch (bits) {
+        case 1: C = 113; B = 0; break;
+        case 2: C = 54;  B = (b << 8) | (b << 3) | (b << 2); break;
+        case 3: C = 26;  B = (c << 8) | (b << 7) | (c << 2) | (b << 1) | c; break;
+        case 4: C = 13;  B = (d << 8) | (c << 7) | (b << 6) | (d << 1) | c; break;
+        default: C = 6;  B = (e << 8) | (d << 7) | (c << 6) | (b << 5) | e; break;
+        }
+    }
+    int T = D * C + B;
+    T ^= A;
+    return (A & 0x80) | (T >> 2);
+}
+
+double srgb_to_linear_f64(double x) {
+    return x <= 0.04045 ? x / 12.92 : std::pow((x + 0.055) / 1.055, 2.4);
+}
+
+Tables::Tables() {
+    for (int q = 0; q < QUANT_MAX; ++q) {
+        int l = kQuantLevels[q], b = 0;
+        while ((l & 1) == 0) { l >>= 1; ++b; }
+        btq[q][0] = b; btq[q][1] = (l == 3); btq[q][2] = (l == 5);
+    }
+    // Encoding tables: the inverse of the spec decode.  Where several codes
+    // decode to the same tuple, the largest code is taken (this is the
+    // choice the reference's integer_from_trits / integer_from_quints make).
+    for (int T = 0; T < 256; ++T) {
+        int t[5];
+        decode_trit_block(T, t);
+        for (int i = 0; i < 5; ++i) trits_dec[T][i] = t[i];
+        trits_enc[t[4] * 81 + t[3] * 27 + t[2] * 9 + t[1] * 3 + t[0]] = T;
+    }
+    for (int Q = 0; Q < 128; ++Q) {
+        int q[3];
+        decode_quint_block(Q, q);
+        for (int i = 0; i < 3; ++i) quints_dec[Q][i] = q[i];
+        quints_enc[q[2] * 25 + q[1] * 5 + q[0]] = Q;
+    }
+    // Weight scramble: order the ISE symbols of each weight range by their
+    // unquantised value; scramble[i] is the symbol of the i-th smallest.
+    std::memset(scramble, 0, sizeof(scramble));
+    std::memset(unscramble, 0, sizeof(unscramble));
+    std::memset(wunq, 0, sizeof(wunq));
+    for (int q = 0; q < 12; ++q) {
+        const int n = kQuantLevels[q];
+        int vals[32], order[32];
+        for (int v = 0; v < n; ++v) { vals[v] = spec_unquant_weight(q, v); order[v] = v; wunq[q][v] = vals[v]; }
+        for (int i = 1; i < n; ++i)            // insertion sort, stable
+            for (int j = i; j > 0 && vals[order[j - 1]] > vals[order[j]]; --j) {
+                int t = order[j]; order[j] = order[j - 1]; order[j - 1] = t;
+            }
+        for (int i = 0; i < n; ++i) { scramble[q][i] = order[i]; unscramble[q][order[i]] = i; }
+    }
+    for (int q = 0; q < QUANT_MAX; ++q)
+        for (int v = 0; v < 256; ++v)
+            cunq[q][v] = v < kQuantLevels[q] ? spec_unquant_color(q, v) : 0;
+    for (int c = 0; c < 256; ++c) {
+        srgb_lut64[c] = srgb_to_linear_f64(c / 255.0);
+        srgb_lut[c] = (float)srgb_lut64[c];
+    }
+}
+
+const Tables& tables() {
+    static const Tables t;
+    return t;
+}
+
+// ---------------------------------------------------------------------------
+// 128-bit little-endian bit writer (ASTC_IntegerSequenceEncoding.hlsl:98-119)
+// ---------------------------------------------------------------------------
+struct Bits128 {
+    uint32_t w[4];
+};
+
+// ORs the low `count` bits of `number` at bit offset `pos` (number < 2^count,
+// count <= 8), advancing pos -- orbits8_ptr.
+inline void or_bits(Bits128& o, uint32_t& pos, uint32_t number, uint32_t count) {
+    const uint32_t newpos = pos + count;
+    const uint32_t nidx = newpos >> 5, uidx = pos >> 5, bidx = pos & 31;
+    if (uidx < 4) o.w[uidx] |= number << bidx;
+    if (nidx > uidx && uidx + 1 < 4) o.w[uidx + 1] |= number >> (32 - bidx);
+    pos = newpos;
+}
+
+inline uint32_t read_bits(const uint8_t* p, int pos, int count) {
+    uint32_t v = 0;
+    for (int i = 0; i < count; ++i) {
+        const int b = pos + i;
+        if (b >= 0 && b < 128) v |= (uint32_t)((p[b >> 3] >> (b & 7)) & 1) << i;
+    }
+    return v;
+}
+
+// encode_trits (ISE:142-176): 5 values, b bits each, one packed trit byte.
+void encode_trits(uint32_t b, const uint32_t v[5], Bits128& o, uint32_t& pos) {
+    const Tables& tb = tables();
+    const uint32_t mask = (1u << b) - 1;
+    uint32_t t[5], m[5];
+    for (int i = 0; i < 5; ++i) { m[i] = v[i] & mask; t[i] = (v[i] >> b) & 0xFF; }
+    const uint32_t T = tb.trits_enc[t[4] * 81 + t[3] * 27 + t[2] * 9 + t[1] * 3 + t[0]];
+    or_bits(o, pos, m[0], b); or_bits(o, pos, T & 3, 2);
+    or_bits(o, pos, m[1], b); or_bits(o, pos, (T >> 2) & 3, 2);
+    or_bits(o, pos, m[2], b); or_bits(o, pos, (T >> 4) & 1, 1);
+    or_bits(o, pos, m[3], b); or_bits(o, pos, (T >> 5) & 3, 2);
+    or_bits(o, pos, m[4], b); or_bits(o, pos, (T >> 7) & 1, 1);
+}
+
+// encode_quints (ISE:181-205): 3 values, b bits each, one packed quint.
+void encode_quints(uint32_t b, const uint32_t v[3], Bits128& o, uint32_t& pos) {
+    const Tables& tb = tables();
+    const uint32_t mask = (1u << b) - 1;
+    uint32_t q[3], m[3];
+    for (int i = 0; i < 3; ++i) { m[i] = v[i] & mask; q[i] = (v[i] >> b) & 0xFF; }
+    const uint32_t Q = tb.quints_enc[q[2] * 25 + q[1] * 5 + q[0]];
+    or_bits(o, pos, m[0], b); or_bits(o, pos, Q & 7, 3);
+    or_bits(o, pos, m[1], b); or_bits(o, pos, (Q >> 3) & 3, 2);
+    or_bits(o, pos, m[2], b); or_bits(o, pos, (Q >> 5) & 3, 2);
+}
+
+// bise_endpoints / bise_weights (ISE:207-276) for any count: groups of 5
+// (trits) or 3 (quints) padded with zeros, or plain b-bit fields.
+void ise_encode(int quant, int count, const uint32_t* values, Bits128& o) {
+    const Tables& tb = tables();
+    const uint32_t b = tb.btq[quant][0];
+    uint32_t pos = 0;
+    if (tb.btq[quant][1]) {
+        for (int g = 0; g < count; g += 5) {
+            uint32_t v[5];
+            for (int i = 0; i < 5; ++i) v[i] = g + i < count ? values[g + i] : 0;
+            encode_trits(b, v, o, pos);
+        }
+    } else if (tb.btq[quant][2]) {
+        for (int g = 0; g < count; g += 3) {
+            uint32_t v[3];
+            for (int i = 0; i < 3; ++i) v[i] = g + i < count ? values[g + i] : 0;
+            encode_quints(b, v, o, pos);
+        }
+    } else {
+        for (int i = 0; i < count; ++i) or_bits(o, pos, values[i], b);
+    }
+}
+
+// compute_ise_bitcount (ISE:76-93)
+int ise_bits(int quant, int count) {
+    const Tables& tb = tables();
+    const int b = tb.btq[quant][0];
+    if (tb.btq[quant][1]) return ((8 + 5 * b) * count + 4) / 5;
+    if (tb.btq[quant][2]) return ((7 + 3 * b) * count + 2) / 3;
+    return count * b;
+}
+
+// Spec ISE decode from a little-endian bit stream starting at bit `pos`.
+void ise_decode(int quant, int count, const uint8_t* p, int pos, uint32_t* out) {
+    const Tables& tb = tables();
+    const int b = tb.btq[quant][0];
+    if (tb.btq[quant][1]) {
+        for (int g = 0; g < count; g += 5) {
+            uint32_t m[5] = {0, 0, 0, 0, 0};
+            static const int tbits[5] = {2, 2, 1, 2, 1};
+            uint32_t T = 0;
+            int tshift = 0;
+            for (int i = 0; i < 5; ++i) {
+                m[i] = read_bits(p, pos, b); pos += b;
+                T |= read_bits(p, pos, tbits[i]) << tshift;
+                pos += tbits[i]; tshift += tbits[i];
+            }
+            for (int i = 0; i < 5 && g + i < count; ++i)
+                out[g + i] = ((uint32_t)tb.trits_dec[T][i] << b) | m[i];
+        }
+    } else if (tb.btq[quant][2]) {
+        for (int g = 0; g < count; g += 3) {
+            uint32_t m[3] = {0, 0, 0};
+            static const int qbits[3] = {3, 2, 2};
+            uint32_t Q = 0;
+            int qshift = 0;
+            for (int i = 0; i < 3; ++i) {
+                m[i] = read_bits(p, pos, b); pos += b;
+                Q |= read_bits(p, pos, qbits[i]) << qshift;
+                pos += qbits[i]; qshift += qbits[i];
+            }
+            for (int i = 0; i < 3 && g + i < count; ++i)
+                out[g + i] = ((uint32_t)tb.quints_dec[Q][i] << b) | m[i];
+        }
+    } else {
+        for (int i = 0; i < count; ++i) { out[i] = read_bits(p, pos, b); pos += b; }
+    }
+}
+
+inline uint32_t reverse_byte(uint32_t p) {                 // ISE:131-137
+    p = ((p & 0xF) << 4) | ((p >> 4) & 0xF);
+    p = ((p & 0x33) << 2) | ((p >> 2) & 0x33);
+    p = ((p & 0x55) << 1) | ((p >> 1) & 0x55);
+    return p;
+}
+
+inline uint32_t reverse_word(uint32_t v) {
+    return (reverse_byte(v & 0xFF) << 24) | (reverse_byte((v >> 8) & 0xFF) << 16) |
+           (reverse_byte((v >> 16) & 0xFF) << 8) | reverse_byte((v >> 24) & 0xFF);
+}
+
+// assemble_blockmode (ASTC_Encode.hlsl:446-473), 4x4 weight grid.
+uint32_t assemble_blockmode(uint32_t wq) {
+    const uint32_t a = (4 - 2) & 3, b = (4 - 4) & 3, d = 0;
+    const uint32_t h = wq < 6 ? 0 : 1, r = (wq % 6) + 2;
+    uint32_t m = (r >> 1) & 3;
+    m |= (r & 1) << 4;
+    m |= (a & 3) << 5;
+    m |= (b & 3) << 7;
+    m |= h << 9;
+    m |= d << 10;
+    return m;
+}
+
+// assemble_block (ASTC_Encode.hlsl:400-444), single partition.
+void assemble_block(uint32_t mode, uint32_t cem, const Bits128& ep, const Bits128& wt,
+                    uint8_t out[16]) {
+    uint32_t blk[4] = {0, 0, 0, 0};
+    blk[3] |= reverse_word(wt.w[0]);
+    blk[2] |= reverse_word(wt.w[1]);
+    blk[1] |= reverse_word(wt.w[2]);
+    blk[0] = mode;
+    blk[0] |= (cem & 0xF) << 13;
+    blk[0] |= (ep.w[0] & 0x7FFF) << 17;
+    blk[1] = (ep.w[0] >> 15) & 0x1FFFF;     // '=' as in the shader (line 438)
+    blk[1] |= (ep.w[1] & 0x7FFF) << 17;
+    blk[2] |= (ep.w[1] >> 15) & 0x1FFFF;
+    for (int i = 0; i < 4; ++i)
+        for (int k = 0; k < 4; ++k) out[i * 4 + k] = (uint8_t)(blk[i] >> (8 * k));
+}
+
+// Integer half of encode_block: symbolic endpoints + weights -> 16 bytes.
+void assemble_symbolic(const uint32_t ep_q[8], const uint32_t qw[16], bool alpha,
+                       uint8_t out[16]) {
+    const Tables& tb = tables();
+    const uint32_t wq = alpha ? QUANT_6 : QUANT_12;
+    Bits128 ep = {{0, 0, 0, 0}}, wt = {{0, 0, 0, 0}};
+    uint32_t epv[8];
+    for (int i = 0; i < 8; ++i) epv[i] = ep_q[i];
+    if (!alpha) { epv[6] = 0; epv[7] = 0; }                 // lines 480-483
+    ise_encode(QUANT_256, alpha ? 8 : 6, epv, ep);
+    uint32_t sw[16];
+    for (int i = 0; i < 16; ++i) sw[i] = (uint32_t)tb.scramble[wq][qw[i]];
+    ise_encode((int)wq, 16, sw, wt);
+    assemble_block(assemble_blockmode(wq), alpha ? 12u : 8u, ep, wt, out);
+}
+
+// ---------------------------------------------------------------------------
+// Arithmetic policies: FP32 (the pinned model), FP64 twin, FP32 op counter
+// ---------------------------------------------------------------------------
+struct F32 {
+    typedef float T;
+    static float lit(float f, double) { return f; }
+    static float add(float a, float b) { return a + b; }
+    static float sub(float a, float b) { return a - b; }
+    static float mul(float a, float b) { return a * b; }
+    static float mad(float a, float b, float c) {
+#if ORACLE_FUSED_MAD
+        return std::fmaf(a, b, c);
+#else
+        return a * b + c;
+#endif
+    }
+    static float div(float a, float b) { return a / b; }
+    static float sqrt(float a) { return std::sqrt(a); }
+    static float rint(float a) { return std::rint(a); }
+    static float min(float a, float b) { return std::fmin(a, b); }
+    static float max(float a, float b) { return std::fmax(a, b); }
+    static float srgb(int c) { return tables().srgb_lut[c]; }
+};
+
+struct F64 {
+    typedef double T;
+    static double lit(float, double d) { return d; }
+    static double add(double a, double b) { return a + b; }
+    static double sub(double a, double b) { return a - b; }
+    static double mul(double a, double b) { return a * b; }
+    static double mad(double a, double b, double c) {
+#if ORACLE_FUSED_MAD
+        return std::fma(a, b, c);
+#else
+        return a * b + c;
+#endif
+    }
+    static double div(double a, double b) { return a / b; }
+    static double sqrt(double a) { return std::sqrt(a); }
+    static double rint(double a) { return std::rint(a); }
+    static double min(double a, double b) { return std::fmin(a, b); }
+    static double max(double a, double b) { return std::fmax(a, b); }
+    static double srgb(int c) { return tables().srgb_lut64[c]; }
+};
+
+thread_local double g_flops = 0.0;
+struct F32Count : F32 {
+    static float add(float a, float b) { g_flops += 1; return F32::add(a, b); }
+    static float sub(float a, float b) { g_flops += 1; return F32::sub(a, b); }
+    static float mul(float a, float b) { g_flops += 1; return F32::mul(a, b); }
+    static float mad(float a, float b, float c) { g_flops += 2; return F32::mad(a, b, c); }
+    static float div(float a, float b) { g_flops += 1; return F32::div(a, b); }
+    static float sqrt(float a) { g_flops += 1; return F32::sqrt(a); }
+};
+
+// ---------------------------------------------------------------------------
+// The FP pipeline (templated on the arithmetic policy)
+// ---------------------------------------------------------------------------
+template <class P>
+struct Pipe {
+    typedef typename P::T T;
+
+    static T dot4(const T a[4], const T b[4]) {
+        T d = P::mul(a[0], b[0]);
+        d = P::mad(a[1], b[1], d);
+        d = P::mad(a[2], b[2], d);
+        d = P::mad(a[3], b[3], d);
+        return d;
+    }
+    static T length(const T v[4]) { return P::sqrt(dot4(v, v)); }
+    static void normalize(T v[4]) {
+        const T r = P::div(P::lit(1.0f, 1.0), P::sqrt(dot4(v, v)));
+        for (int i = 0; i < 4; ++i) v[i] = P::mul(v[i], r);
+    }
+    static T div_const(T x, int n) {
+#if ORACLE_CONST_DIV_AS_MUL
+        return P::mul(x, P::div(P::lit(1.0f, 1.0), (T)n));
+#else
+        return P::div(x, (T)n);
+#endif
+    }
+
+    // eigen_vector (ASTC_Encode.hlsl:93-106)
+    static void eigen_vector(const T m[4][4], T v[4]) {
+        v[0] = P::lit(0.26726f, 0.26726); v[1] = P::lit(0.80178f, 0.80178);
+        v[2] = P::lit(0.53452f, 0.53452); v[3] = 0;
+        for (int it = 0; it < 8; ++it) {
+            T t[4];
+            for (int r = 0; r < 4; ++r) t[r] = dot4(m[r], v);
+            for (int r = 0; r < 4; ++r) v[r] = t[r];
+            if (length(v) < P::lit(1e-5f, 1e-5)) return;
+            for (int r = 0; r < 4; ++r) t[r] = dot4(m[r], v);
+            for (int r = 0; r < 4; ++r) v[r] = t[r];
+            normalize(v);
+        }
+    }
+
+    // find_min_max (ASTC_Encode.hlsl:108-137)
+    static void find_min_max(const T (*tex)[4], int n, const T mean[4], const T k[4],
+                             bool alpha, T e0[4], T e1[4]) {
+        T a = P::lit(1e31f, 1e31), b = P::lit(-1e31f, -1e31);
+        for (int i = 0; i < n; ++i) {
+            T d[4];
+            for (int c = 0; c < 4; ++c) d[c] = P::sub(tex[i][c], mean[c]);
+            const T t = dot4(d, k);
+            a = P::min(a, t);
+            b = P::max(b, t);
+        }
+        for (int c = 0; c < 4; ++c) {
+            e0[c] = P::min(P::max(P::mad(k[c], a, mean[c]), (T)0), P::lit(255.0f, 255.0));
+            e1[c] = P::min(P::max(P::mad(k[c], b, mean[c]), (T)0), P::lit(255.0f, 255.0));
+        }
+        const T s0 = P::add(P::add(P::rint(e0[0]), P::rint(e0[1])), P::rint(e0[2]));
+        const T s1 = P::add(P::add(P::rint(e1[0]), P::rint(e1[1])), P::rint(e1[2]));
+        if (s0 > s1)
+            for (int c = 0; c < 4; ++c) { T t = e0[c]; e0[c] = e1[c]; e1[c] = t; }
+        if (!alpha) { e0[3] = P::lit(255.0f, 255.0); e1[3] = P::lit(255.0f, 255.0); }
+    }
+
+    // principal_component_analysis (ASTC_Encode.hlsl:139-168)
+    static void pca(const T (*tex)[4], int n, bool alpha, T e0[4], T e1[4]) {
+        T mean[4] = {0, 0, 0, 0};
+        for (int i = 0; i < n; ++i)
+            for (int c = 0; c < 4; ++c) mean[c] = P::add(mean[c], tex[i][c]);
+        for (int c = 0; c < 4; ++c) mean[c] = div_const(mean[c], n);
+        T cov[4][4];
+        for (int i = 0; i < 4; ++i)
+            for (int j = 0; j < 4; ++j) cov[i][j] = 0;
+        for (int k = 0; k < n; ++k) {
+            T d[4];
+            for (int c = 0; c < 4; ++c) d[c] = P::sub(tex[k][c], mean[c]);
+            for (int i = 0; i < 4; ++i)
+                for (int j = 0; j < 4; ++j) cov[i][j] = P::mad(d[i], d[j], cov[i][j]);
+        }
+        for (int i = 0; i < 4; ++i)
+            for (int j = 0; j < 4; ++j) cov[i][j] = div_const(cov[i][j], n - 1);
+        T k[4];
+        eigen_vector(cov, k);
+        find_min_max(tex, n, mean, k, alpha, e0, e1);
+    }
+
+    // idx_grids / wt_grids (ASTC_Encode.hlsl:268-304): the 4x4 weight grid of
+    // a 6x6 block samples 2x2 texel taps at fixed bilinear weights.
+    static void grid_taps(int g, int idx[4], T wt[4]) {
+        const int gx = g & 3, gy = g >> 2;
+        const int x0 = gx < 2 ? gx : gx + 1;           // texel columns 0,1,3,4
+        const int y0 = gy < 2 ? gy : gy + 1;
+        idx[0] = y0 * 6 + x0; idx[1] = idx[0] + 1; idx[2] = idx[0] + 6; idx[3] = idx[0] + 7;
+        // near tap gets 4/9 along an axis where the grid point sits 1/3 from
+        // it; grid columns 0 and 2 lean left, 1 and 3 lean right.
+        const bool xl = (gx & 1) == 0, yl = (gy & 1) == 0;
+        const T hi = P::lit(0.444f, 0.444), mid = P::lit(0.222f, 0.222), lo = P::lit(0.111f, 0.111);
+        // corner order (x0,y0), (x1,y0), (x0,y1), (x1,y1)
+        const bool nearx[4] = {xl, !xl, xl, !xl};
+        const bool neary[4] = {yl, yl, !yl, !yl};
+        for (int c = 0; c < 4; ++c)
+            wt[c] = (nearx[c] && neary[c]) ? hi : (nearx[c] || neary[c]) ? mid : lo;
+    }
+
+    // calculate_normal_weights + quantize_weights (ASTC_Encode.hlsl:316-393)
+    static void weights(const T (*tex)[4], int dim, const T e0[4], const T e1[4],
+                        uint32_t range, uint32_t qw[16]) {
+        T k[4];
+        for (int c = 0; c < 4; ++c) k[c] = P::sub(e1[c], e0[c]);
+        T w[16];
+        if (length(k) < P::lit(1e-5f, 1e-5)) {
+            for (int i = 0; i < 16; ++i) w[i] = 0;
+        } else {
+            normalize(k);
+            T minw = P::lit(1e31f, 1e31), maxw = P::lit(-1e31f, -1e31);
+            for (int i = 0; i < 16; ++i) {
+                T s[4];
+                if (dim == 6) {                             // sample_texel 307-314
+                    int idx[4]; T cw[4];
+                    grid_taps(i, idx, cw);
+                    for (int c = 0; c < 4; ++c) {
+                        T acc = P::mul(tex[idx[0]][c], cw[0]);
+                        acc = P::mad(tex[idx[1]][c], cw[1], acc);
+                        acc = P::mad(tex[idx[2]][c], cw[2], acc);
+                        acc = P::mad(tex[idx[3]][c], cw[3], acc);
+                        s[c] = acc;
+                    }
+                } else {
+                    for (int c = 0; c < 4; ++c) s[c] = tex[i][c];
+                }
+                T d[4];
+                for (int c = 0; c < 4; ++c) d[c] = P::sub(s[c], e0[c]);
+                const T x = dot4(k, d);
+                minw = P::min(x, minw);
+                maxw = P::max(x, maxw);
+                w[i] = x;
+            }
+            T inv = P::sub(maxw, minw);
+            inv = P::max(P::lit(1e-5f, 1e-5), inv);
+            inv = P::div(P::lit(1.0f, 1.0), inv);
+            for (int i = 0; i < 16; ++i) w[i] = P::mul(P::sub(w[i], minw), inv);
+        }
+        const T rf = (T)range;
+        for (int i = 0; i < 16; ++i) {
+            const T r = P::rint(P::mul(w[i], rf));
+            uint32_t q = r <= 0 ? 0u : (uint32_t)r;
+            qw[i] = q > range ? range : q;
+        }
+    }
+
+    // encode_block (ASTC_Encode.hlsl:510-550)
+    static void encode(const T (*tex)[4], int dim, bool alpha, uint32_t ep_q[8],
+                       uint32_t qw[16], uint8_t out[16]) {
+        T e0[4], e1[4];
+        pca(tex, dim * dim, alpha, e0, e1);
+        for (int c = 0; c < 4; ++c) {                       // encode_color 233-245
+            ep_q[2 * c] = (uint32_t)P::rint(e0[c]);
+            ep_q[2 * c + 1] = (uint32_t)P::rint(e1[c]);
+        }
+        const uint32_t range = alpha ? 5u : 11u;            // weight_range - 1
+        weights(tex, dim, e0, e1, range, qw);
+        assemble_symbolic(ep_q, qw, alpha, out);
+    }
+
+    // MainCS texel fetch (ASTC_Encode.hlsl:561-580)
+    static void fetch(const uint8_t* rgba, int w, int h, int bx, int by,
+                      const oracle_opts& o, T (*tex)[4]) {
+        const int dim = o.block_dim;
+        for (int kk = 0; kk < dim * dim; ++kk) {
+            const int y = kk / dim, x = kk - y * dim;
+            int px = bx * dim + x, py = by * dim + y;
+            const bool inside = px < w && py < h;
+            T c[4] = {0, 0, 0, 0};
+            if (inside || o.border == 1) {
+                if (px >= w) px = w - 1;
+                if (py >= h) py = h - 1;
+                const uint8_t* p = rgba + ((size_t)py * w + px) * 4;
+                for (int ch = 0; ch < 4; ++ch) {
+                    if (o.srgb && ch < 3) c[ch] = P::srgb(p[ch]);
+                    else c[ch] = P::div((T)p[ch], P::lit(255.0f, 255.0));
+                }
+            }
+            if (o.is_normal) { c[2] = P::lit(1.0f, 1.0); c[3] = P::lit(1.0f, 1.0); }
+            for (int ch = 0; ch < 4; ++ch) tex[kk][ch] = P::mul(c[ch], P::lit(255.0f, 255.0));
+        }
+    }
+
+    static int encode_image(const uint8_t* rgba, int w, int h, const oracle_opts* o,
+                            uint8_t* out, int threads) {
+        if (!rgba || !out || !o || w <= 0 || h <= 0) return -1;
+        if (o->block_dim != 4 && o->block_dim != 6) return -2;
+        if (o->border != 0 && o->border != 1) return -3;
+        tables();
+        const int dim = o->block_dim;
+        const int nbx = (w + dim - 1) / dim, nby = (h + dim - 1) / dim;
+        const long long nb = (long long)nbx * nby;
+#ifdef _OPENMP
+        const int nt = threads > 0 ? threads : omp_get_max_threads();
+#pragma omp parallel for schedule(static) num_threads(nt)
+#else
+        (void)threads;
+#endif
+        for (long long b = 0; b < nb; ++b) {
+            const int by = (int)(b / nbx), bx = (int)(b - (long long)by * nbx);
+            T tex[36][4];
+            fetch(rgba, w, h, bx, by, *o, tex);
+            uint32_t ep[8], qw[16];
+            encode(tex, dim, o->has_alpha != 0, ep, qw, out + 16 * b);
+        }
+        return 0;
+    }
+};
+
+// ---------------------------------------------------------------------------
+// Spec LDR decoder (integer only)
+// ---------------------------------------------------------------------------
+struct BlockMode {
+    int gw, gh, dual, quant, ok;
+};
+
+BlockMode decode_block_mode(int m) {
+    BlockMode r = {0, 0, 0, 0, 0};
+    int R, H = bit(m, 9), D = bit(m, 10);
+    if ((m & 3) != 0) {
+        R = bit(m, 4) | (bit(m, 0) << 1) | (bit(m, 1) << 2);
+        const int A = (m >> 5) & 3, B = (m >> 7) & 3;
+        switch ((m >> 2) & 3) {
+        case 0: r.gw = B + 4; r.gh = A + 2; break;
+        case 1: r.gw = B + 8; r.gh = A + 2; break;
+        case 2: r.gw = A + 2; r.gh = B + 8; break;
+        default:
+            if (bit(m, 8) == 0) { r.gw = A + 2; r.gh = bit(m, 7) + 6; }
+            else { r.gw = bit(m, 7) + 2; r.gh = A + 2; }
+        }
+    } else {
+        if (((m >> 2) & 3) == 0) return r;                 // reserved (incl. R<2)
+        R = bit(m, 4) | (bit(m, 2) << 1) | (bit(m, 3) << 2);
+        const int A = (m >> 5) & 3;
+        switch ((m >> 7) & 3) {
+        case 0: r.gw = 12; r.gh = A + 2; break;
+        case 1: r.gw = A + 2; r.gh = 12; break;
+        case 3:
+            if (bit(m, 6)) return r;                       // reserved
+            if (bit(m, 5) == 0) { r.gw = 6; r.gh = 10; } else { r.gw = 10; r.gh = 6; }
+            break;
+        default: {
+            const int B = (m >> 9) & 3;
+            r.gw = A + 6; r.gh = B + 6; H = 0; D = 0;
+        }
+        }
+    }
+    r.dual = D;
+    r.quant = (R - 2) + 6 * H;
+    r.ok = 1;
+    return r;
+}
+
+inline int clamp255(int v) { return v < 0 ? 0 : v > 255 ? 255 : v; }
+
+void bit_transfer_signed(int& a, int& b) {
+    b >>= 1;
+    b |= a & 0x80;
+    a >>= 1;
+    a &= 0x3F;
+    if (a & 0x20) a -= 0x40;
+}
+
+void blue_contract(int c[4]) {
+    c[0] = (c[0] + c[2]) >> 1;
+    c[1] = (c[1] + c[2]) >> 1;
+}
+
+// Returns false for HDR / invalid CEMs.
+bool unpack_endpoints(int cem, const int* v, int e0[4], int e1[4]) {
+    switch (cem) {
+    case 0:
+        e0[0] = e0[1] = e0[2] = v[0]; e0[3] = 255;
+        e1[0] = e1[1] = e1[2] = v[1]; e1[3] = 255;
+        return true;
+    case 1: {
+        const int l0 = (v[0] >> 2) | (v[1] & 0xC0);
+        int l1 = l0 + (v[1] & 0x3F);
+        if (l1 > 255) l1 = 255;
+        e0[0] = e0[1] = e0[2] = l0; e0[3] = 255;
+        e1[0] = e1[1] = e1[2] = l1; e1[3] = 255;
+        return true;
+    }
+    case 4:
+        e0[0] = e0[1] = e0[2] = v[0]; e0[3] = v[2];
+        e1[0] = e1[1] = e1[2] = v[1]; e1[3] = v[3];
+        return true;
+    case 5: {
+        int a0 = v[0], a1 = v[1], a2 = v[2], a3 = v[3];
+        bit_transfer_signed(a1, a0);
+        bit_transfer_signed(a3, a2);
+        e0[0] = e0[1] = e0[2] = a0; e0[3] = a2;
+        const int l = clamp255(a0 + a1);
+        e1[0] = e1[1] = e1[2] = l; e1[3] = clamp255(a2 + a3);
+        return true;
+    }
+    case 6:
+        e0[0] = (v[0] * v[3]) >> 8; e0[1] = (v[1] * v[3]) >> 8; e0[2] = (v[2] * v[3]) >> 8; e0[3] = 255;
+        e1[0] = v[0]; e1[1] = v[1]; e1[2] = v[2]; e1[3] = 255;
+        return true;
+    case 8:
+    case 12: {
+        const int a0 = cem == 12 ? v[6] : 255, a1 = cem == 12 ? v[7] : 255;
+        const int s0 = v[0] + v[2] + v[4], s1 = v[1] + v[3] + v[5];
+        if (s1 >= s0) {
+            e0[0] = v[0]; e0[1] = v[2]; e0[2] = v[4]; e0[3] = a0;
+            e1[0] = v[1]; e1[1] = v[3]; e1[2] = v[5]; e1[3] = a1;
+        } else {
+            e0[0] = v[1]; e0[1] = v[3]; e0[2] = v[5]; e0[3] = a1;
+            e1[0] = v[0]; e1[1] = v[2]; e1[2] = v[4]; e1[3] = a0;
+            blue_contract(e0);
+            blue_contract(e1);
+        }
+        return true;
+    }
+    case 9:
+    case 13: {
+        int a[8];
+        for (int i = 0; i < 8; ++i) a[i] = i < (cem == 13 ? 8 : 6) ? v[i] : 255;
+        bit_transfer_signed(a[1], a[0]);
+        bit_transfer_signed(a[3], a[2]);
+        bit_transfer_signed(a[5], a[4]);
+        if (cem == 13) bit_transfer_signed(a[7], a[6]);
+        const int al0 = cem == 13 ? a[6] : 255;
+        const int al1 = cem == 13 ? clamp255(a[6] + a[7]) : 255;
+        if (a[1] + a[3] + a[5] >= 0) {
+            e0[0] = a[0]; e0[1] = a[2]; e0[2] = a[4]; e0[3] = al0;
+            e1[0] = clamp255(a[0] + a[1]); e1[1] = clamp255(a[2] + a[3]);
+            e1[2] = clamp255(a[4] + a[5]); e1[3] = al1;
+        } else {
+            e0[0] = a[0] + a[1]; e0[1] = a[2] + a[3]; e0[2] = a[4] + a[5]; e0[3] = al1;
+            e1[0] = a[0]; e1[1] = a[2]; e1[2] = a[4]; e1[3] = al0;
+            blue_contract(e0);
+            blue_contract(e1);
+            for (int c = 0; c < 4; ++c) { e0[c] = clamp255(e0[c]); e1[c] = clamp255(e1[c]); }
+        }
+        return true;
+    }
+    case 10:
+        e0[0] = (v[0] * v[3]) >> 8; e0[1] = (v[1] * v[3]) >> 8; e0[2] = (v[2] * v[3]) >> 8; e0[3] = v[4];
+        e1[0] = v[0]; e1[1] = v[1]; e1[2] = v[2]; e1[3] = v[5];
+        return true;
+    default:
+        return false;                                       // HDR modes
+    }
+}
+
+// Spec partition hash (select_partition) for multi-partition blocks.
+int select_partition(int seed, int x, int y, int z, int pcount, bool small) {
+    if (small) { x <<= 1; y <<= 1; z <<= 1; }
+    seed += (pcount - 1) * 1024;
+    uint32_t p = (uint32_t)seed;
+    p ^= p >> 15; p -= p << 17; p += p << 7; p += p << 4;
+    p ^= p >> 5;  p += p << 16; p ^= p >> 7; p ^= p >> 3;
+    p ^= p << 6;  p ^= p >> 17;
+    const uint32_t rnum = p;
+    // seed1..seed8 are the eight nibbles of rnum; seed9..seed12 start at
+    // bits 18, 22, 26 and 30 (the last one wraps around to bit 0).
+    int s[12];
+    for (int i = 0; i < 8; ++i) s[i] = (rnum >> (4 * i)) & 0xF;
+    s[8] = (rnum >> 18) & 0xF;
+    s[9] = (rnum >> 22) & 0xF;
+    s[10] = (rnum >> 26) & 0xF;
+    s[11] = ((rnum >> 30) | (rnum << 2)) & 0xF;
+    for (int i = 0; i < 12; ++i) s[i] *= s[i];
+    int sh1, sh2;
+    if (seed & 1) { sh1 = (seed & 2) ? 4 : 5; sh2 = (pcount == 3) ? 6 : 5; }
+    else { sh1 = (pcount == 3) ? 6 : 5; sh2 = (seed & 2) ? 4 : 5; }
+    const int sh3 = (seed & 0x10) ? sh1 : sh2;
+    s[0] >>= sh1; s[1] >>= sh2; s[2] >>= sh1; s[3] >>= sh2;
+    s[4] >>= sh1; s[5] >>= sh2; s[6] >>= sh1; s[7] >>= sh2;
+    s[8] >>= sh3; s[9] >>= sh3; s[10] >>= sh3; s[11] >>= sh3;
+    int a = s[0] * x + s[1] * y + s[10] * z + (int)(rnum >> 14);
+    int b = s[2] * x + s[3] * y + s[11] * z + (int)(rnum >> 10);
+    int c = s[4] * x + s[5] * y + s[8] * z + (int)(rnum >> 6);
+    int d = s[6] * x + s[7] * y + s[9] * z + (int)(rnum >> 2);
+    a &= 0x3F; b &= 0x3F; c &= 0x3F; d &= 0x3F;
+    if (pcount < 4) d = 0;
+    if (pcount < 3) c = 0;
+    if (a >= b && a >= c && a >= d) return 0;
+    if (b >= c && b >= d) return 1;
+    if (c >= d) return 2;
+    return 3;
+}
+
+void error_block(int bw, int bh, uint8_t* out) {
+    for (int i = 0; i < bw * bh; ++i) {
+        out[i * 4 + 0] = 255; out[i * 4 + 1] = 0; out[i * 4 + 2] = 255; out[i * 4 + 3] = 255;
+    }
+}
+
+// Decode one block to UNORM8 RGBA (bw*bh texels, row-major). Returns 0 on
+// success, 1 for an error block.
+int decode_block(const uint8_t* blk, int bw, int bh, bool srgb, uint8_t* out) {
+    const Tables& tb = tables();
+    const int mode = (int)read_bits(blk, 0, 11);
+    if ((mode & 0x1FF) == 0x1FC) {                          // void extent
+        if (bit(mode, 9)) { error_block(bw, bh, out); return 1; }   // HDR
+        uint8_t c[4];
+        for (int i = 0; i < 4; ++i) c[i] = (uint8_t)(read_bits(blk, 64 + 16 * i, 16) >> 8);
+        for (int i = 0; i < bw * bh; ++i) std::memcpy(out + 4 * i, c, 4);
+        return 0;
+    }
+    const BlockMode bm = decode_block_mode(mode);
+    if (!bm.ok || bm.gw > bw || bm.gh > bh) { error_block(bw, bh, out); return 1; }
+    const int pcount = (int)read_bits(blk, 11, 2) + 1;
+    const int nweights = bm.gw * bm.gh * (bm.dual ? 2 : 1);
+    const int wbits = ise_bits(bm.quant, nweights);
+    if (nweights > 64 || wbits < 24 || wbits > 96 || (pcount == 4 && bm.dual)) {
+        error_block(bw, bh, out);
+        return 1;
+    }
+    int cems[4];
+    int color_start, extra_cem_bits = 0;
+    int below_weights = 128 - wbits;
+    if (pcount == 1) {
+        cems[0] = (int)read_bits(blk, 13, 4);
+        color_start = 17;
+    } else {
+        color_start = 29;
+        const int cem_field = (int)read_bits(blk, 23, 6);
+        if ((cem_field & 3) == 0) {
+            for (int p = 0; p < pcount; ++p) cems[p] = cem_field >> 2;
+        } else {
+            extra_cem_bits = 3 * pcount - 4;
+            const int extra = (int)read_bits(blk, below_weights - extra_cem_bits, extra_cem_bits);
+            const int combined = (cem_field >> 2) | (extra << 4);
+            const int base = (cem_field & 3) - 1;
+            for (int p = 0; p < pcount; ++p) {
+                const int cls = (combined >> p) & 1;
+                const int m = (combined >> (pcount + 2 * p)) & 3;
+                cems[p] = ((base + cls) << 2) | m;
+            }
+        }
+    }
+    const int plane2_bits = bm.dual ? 2 : 0;
+    const int color_end = below_weights - extra_cem_bits - plane2_bits;
+    const int plane2_comp = bm.dual ? (int)read_bits(blk, color_end, 2) : -1;
+    int nvals = 0;
+    for (int p = 0; p < pcount; ++p) nvals += 2 * ((cems[p] >> 2) + 1);
+    const int color_bits = color_end - color_start;
+    if (nvals > 18 || color_bits < 0) { error_block(bw, bh, out); return 1; }
+    int cq = -1;
+    for (int q = QUANT_256; q >= QUANT_2; --q)
+        if (ise_bits(q, nvals) <= color_bits) { cq = q; break; }
+    if (cq < QUANT_6) { error_block(bw, bh, out); return 1; }
+    uint32_t cv[18];
+    ise_decode(cq, nvals, blk, color_start, cv);
+    int ep[4][2][4];
+    int off = 0;
+    for (int p = 0; p < pcount; ++p) {
+        int v[8];
+        const int n = 2 * ((cems[p] >> 2) + 1);
+        for (int i = 0; i < n; ++i) v[i] = tb.cunq[cq][cv[off + i]];
+        off += n;
+        if (!unpack_endpoints(cems[p], v, ep[p][0], ep[p][1])) { error_block(bw, bh, out); return 1; }
+    }
+    // weights: stored bit-reversed from bit 127 downward
+    uint8_t rev[16];
+    for (int i = 0; i < 16; ++i) rev[i] = (uint8_t)reverse_byte(blk[15 - i]);
+    uint32_t wv[64];
+    ise_decode(bm.quant, nweights, rev, 0, wv);
+    int wq[64];
+    for (int i = 0; i < nweights; ++i) wq[i] = tb.wunq[bm.quant][wv[i]];
+    // infill (spec bilinear decimation), per plane
+    const int planes = bm.dual ? 2 : 1;
+    const int ds = (1024 + bw / 2) / (bw - 1), dt = (1024 + bh / 2) / (bh - 1);
+    const bool small = bw * bh < 31;
+    const int seed = pcount > 1 ? (int)read_bits(blk, 13, 10) : 0;
+    for (int t = 0; t < bh; ++t)
+        for (int s = 0; s < bw; ++s) {
+            int w[2] = {0, 0};
+            for (int pl = 0; pl < planes; ++pl) {
+                const int gs = (ds * s * (bm.gw - 1) + 32) >> 6;
+                const int gt = (dt * t * (bm.gh - 1) + 32) >> 6;
+                const int js = gs >> 4, fs = gs & 0xF, jt = gt >> 4, ft = gt & 0xF;
+                const int w11 = (fs * ft + 8) >> 4, w10 = ft - w11, w01 = fs - w11;
+                const int w00 = 16 - fs - ft + w11;
+                const int v0 = js + jt * bm.gw;
+                auto P = [&](int idx) -> int {
+                    return (idx < bm.gw * bm.gh) ? wq[idx * planes + pl] : 0;
+                };
+                int acc = P(v0) * w00;
+                if (w01) acc += P(v0 + 1) * w01;
+                if (w10) acc += P(v0 + bm.gw) * w10;
+                if (w11) acc += P(v0 + bm.gw + 1) * w11;
+                w[pl] = (acc + 8) >> 4;
+            }
+            const int part = pcount > 1 ? select_partition(seed, s, t, 0, pcount, small) : 0;
+            uint8_t* o = out + 4 * (t * bw + s);
+            for (int c = 0; c < 4; ++c) {
+                const int wt = (c == plane2_comp) ? w[1] : w[0];
+                const int c0 = srgb ? ((ep[part][0][c] << 8) | 0x80) : ep[part][0][c] * 257;
+                const int c1 = srgb ? ((ep[part][1][c] << 8) | 0x80) : ep[part][1][c] * 257;
+                const int v = (c0 * (64 - wt) + c1 * wt + 32) >> 6;
+                o[c] = (uint8_t)(v >> 8);
+            }
+        }
+    return 0;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// C interface
+// ---------------------------------------------------------------------------
+extern "C" {
+
+int oracle_encode_fp32(const uint8_t* rgba, int width, int height, const oracle_opts* opts,
+                       uint8_t* out_blocks, int threads) {
+    return Pipe<F32>::encode_image(rgba, width, height, opts, out_blocks, threads);
+}
+
+int oracle_encode_fp64(const uint8_t* rgba, int width, int height, const oracle_opts* opts,
+                       uint8_t* out_blocks, int threads) {
+    return Pipe<F64>::encode_image(rgba, width, height, opts, out_blocks, threads);
+}
+
+int oracle_encode_block_fp32(const float* texels, int block_dim, int has_alpha, uint32_t ep[8],
+                             uint32_t qw[16], uint8_t out[16]) {
+    if (!texels || (block_dim != 4 && block_dim != 6)) return -1;
+    float tex[36][4];
+    for (int i = 0; i < block_dim * block_dim; ++i)
+        for (int c = 0; c < 4; ++c) tex[i][c] = texels[4 * i + c];
+    Pipe<F32>::encode(tex, block_dim, has_alpha != 0, ep, qw, out);
+    return 0;
+}
+
+int oracle_assemble_symbolic(const uint32_t ep[8], const uint32_t qw[16], int has_alpha,
+                             uint8_t out[16]) {
+    const uint32_t range = has_alpha ? 5u : 11u;
+    for (int i = 0; i < 8; ++i) if (ep[i] > 255) return -1;
+    for (int i = 0; i < 16; ++i) if (qw[i] > range) return -1;
+    assemble_symbolic(ep, qw, has_alpha != 0, out);
+    return 0;
+}
+
+int oracle_ise_encode(int quant, int count, const uint32_t* values, uint8_t out[16]) {
+    if (quant < 0 || quant >= QUANT_MAX || count < 0 || ise_bits(quant, count) > 128) return -1;
+    for (int i = 0; i < count; ++i) if (values[i] >= (uint32_t)kQuantLevels[quant]) return -1;
+    Bits128 o = {{0, 0, 0, 0}};
+    ise_encode(quant, count, values, o);
+    for (int i = 0; i < 4; ++i)
+        for (int k = 0; k < 4; ++k) out[4 * i + k] = (uint8_t)(o.w[i] >> (8 * k));
+    return 0;
+}
+
+int oracle_ise_decode(int quant, int count, const uint8_t in[16], int bit_offset,
+                      uint32_t* values) {
+    if (quant < 0 || quant >= QUANT_MAX || count < 0) return -1;
+    ise_decode(quant, count, in, bit_offset, values);
+    return 0;
+}
+
+int oracle_ise_bits(int quant, int count) {
+    if (quant < 0 || quant >= QUANT_MAX || count < 0) return -1;
+    return ise_bits(quant, count);
+}
+
+void oracle_table_trits(int out[243]) { std::memcpy(out, tables().trits_enc, sizeof(int) * 243); }
+void oracle_table_quints(int out[125]) { std::memcpy(out, tables().quints_enc, sizeof(int) * 125); }
+void oracle_table_btq(int out[63]) { std::memcpy(out, tables().btq, sizeof(int) * 63); }
+void oracle_table_scramble(int out[384]) { std::memcpy(out, tables().scramble, sizeof(int) * 384); }
+void oracle_srgb_lut(float out[256]) {
+    for (int c = 0; c < 256; ++c) out[c] = tables().srgb_lut[c] * 255.0f;
+}
+
+int oracle_decode_block(const uint8_t blk[16], int block_w, int block_h, int srgb,
+                        uint8_t* out_rgba) {
+    if (block_w < 2 || block_h < 2 || block_w > 12 || block_h > 12) return -1;
+    return decode_block(blk, block_w, block_h, srgb != 0, out_rgba);
+}
+
+int oracle_decode(const uint8_t* blocks, int width, int height, int block_w, int block_h,
+                  int srgb, uint8_t* out_rgba) {
+    if (!blocks || !out_rgba || width <= 0 || height <= 0) return -1;
+    if (block_w < 2 || block_h < 2 || block_w > 12 || block_h > 12) return -1;
+    const int nbx = (width + block_w - 1) / block_w, nby = (height + block_h - 1) / block_h;
+    int errors = 0;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) reduction(+ : errors)
+#endif
+    for (int by = 0; by < nby; ++by)
+        for (int bx = 0; bx < nbx; ++bx) {
+            uint8_t tmp[144 * 4];
+            errors += decode_block(blocks + 16 * ((size_t)by * nbx + bx), block_w, block_h,
+                                   srgb != 0, tmp);
+            for (int y = 0; y < block_h; ++y)
+                for (int x = 0; x < block_w; ++x) {
+                    const int px = bx * block_w + x, py = by * block_h + y;
+                    if (px < width && py < height)
+                        std::memcpy(out_rgba + 4 * ((size_t)py * width + px),
+                                    tmp + 4 * (y * block_w + x), 4);
+                }
+        }
+    return errors;
+}
+
+int oracle_unquant_weight(int quant, int value) {
+    if (quant < 0 || quant >= 12 || value < 0 || value >= kQuantLevels[quant]) return -1;
+    return spec_unquant_weight(quant, value);
+}
+
+int oracle_unquant_color(int quant, int value) {
+    // colour endpoints are never coded below QUANT_6 (the decoder rejects it)
+    if (quant < QUANT_6 || quant >= QUANT_MAX || value < 0 || value >= kQuantLevels[quant]) return -1;
+    return spec_unquant_color(quant, value);
+}
+
+void oracle_grid_taps(int g, int idx[4], float wt[4]) {
+    Pipe<F32>::grid_taps(g & 15, idx, wt);
+}
+
+double oracle_flops_per_block(int block_dim, int has_alpha, int is_normal) {
+    if (block_dim != 4 && block_dim != 6) return -1.0;
+    // A fixed non-degenerate block: every stage runs its full path.
+    float tex[36][4];
+    uint32_t s = 12345u;
+    for (int i = 0; i < block_dim * block_dim; ++i)
+        for (int c = 0; c < 4; ++c) {
+            s = s * 1664525u + 1013904223u;
+            tex[i][c] = (float)((s >> 24) & 0xFF);
+            if (is_normal && c >= 2) tex[i][c] = 255.0f;
+        }
+    g_flops = 0.0;
+    uint32_t ep[8], qw[16];
+    uint8_t out[16];
+    Pipe<F32Count>::encode(tex, block_dim, has_alpha != 0, ep, qw, out);
+    return g_flops;
+}
+
+}  // extern "C"

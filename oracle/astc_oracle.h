@@ -1,0 +1,94 @@
+/*
+ * astc_oracle.h -- CPU oracle for the ASTC block encoder.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is the checker that the CUDA
+ * encoder is compared against; it is never linked into, loaded by or called
+ * from the product library (libastc_gb300.so) or the CLI.  Only the test
+ * suite, the smoke check and the CPU-baseline leg of the benchmark use it.
+ *
+ * It restates the reference compute shader (ASTC_Encode.hlsl,
+ * ASTC_IntegerSequenceEncoding.hlsl, ASTC_Table.hlsl of niepp/astc_encoder)
+ * on the CPU:
+ *   - oracle_encode_fp32  : FP32, the shader's operation order, one fixed
+ *                           arithmetic model (see astc_oracle.cpp header);
+ *   - oracle_encode_fp64  : the same steps evaluated in double (quality twin);
+ *   - oracle_decode       : integer-only ASTC LDR decoder written from the
+ *                           ASTC specification (Khronos Data Format Spec,
+ *                           "ASTC" chapter), UNORM8 output.
+ */
+#ifndef ASTC_ORACLE_H
+#define ASTC_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct oracle_opts {
+    int block_dim;   /* 4 or 6                                              */
+    int has_alpha;   /* HAS_ALPHA    (ASTC_Encode.hlsl:13-15)               */
+    int is_normal;   /* IS_NORMALMAP (ASTC_Encode.hlsl:17-19, 575-578)      */
+    int srgb;        /* texels are sRGB-decoded before the fit (main.cpp:38)*/
+    int border;      /* 0 = zero outside the texture (D3D11 Load rule),
+                        1 = clamp to the edge texel                         */
+} oracle_opts;
+
+/* Encode a tightly packed RGBA8 image (row 0 first) into 16-byte blocks in
+ * row-major block order.  threads <= 0 uses every OpenMP thread.
+ * Returns 0 on success, negative on bad arguments. */
+int oracle_encode_fp32(const uint8_t* rgba, int width, int height,
+                       const oracle_opts* opts, uint8_t* out_blocks, int threads);
+int oracle_encode_fp64(const uint8_t* rgba, int width, int height,
+                       const oracle_opts* opts, uint8_t* out_blocks, int threads);
+
+/* Per-block FP32 encode exposing the symbolic intermediate results:
+ * ep[8] = quantised endpoints r0 r1 g0 g1 b0 b1 a0 a1,
+ * qw[16] = quantised (unscrambled) weights.  texels: N*4 floats (0..255). */
+int oracle_encode_block_fp32(const float* texels, int block_dim, int has_alpha,
+                             uint32_t ep[8], uint32_t qw[16], uint8_t out[16]);
+
+/* Integer stages only: assemble a block from symbolic endpoints and weights
+ * (weight quant method QUANT_6 when has_alpha, QUANT_12 otherwise). */
+int oracle_assemble_symbolic(const uint32_t ep[8], const uint32_t qw[16],
+                             int has_alpha, uint8_t out[16]);
+
+/* Bounded integer sequence encoding of `count` values in quant method
+ * `quant` (0..20, QUANT_2..QUANT_256).  Writes LSB-first into out[16]. */
+int oracle_ise_encode(int quant, int count, const uint32_t* values, uint8_t out[16]);
+/* Inverse of the above (spec decode).  Returns 0 on success. */
+int oracle_ise_decode(int quant, int count, const uint8_t in[16], int bit_offset,
+                      uint32_t* values);
+int oracle_ise_bits(int quant, int count);
+
+/* Tables generated from the spec definitions (never copied). */
+void oracle_table_trits(int out[243]);     /* integer_from_trits        */
+void oracle_table_quints(int out[125]);    /* integer_from_quints       */
+void oracle_table_btq(int out[63]);        /* bits_trits_quints_table   */
+void oracle_table_scramble(int out[384]);  /* scramble_table, 12 x 32   */
+void oracle_srgb_lut(float out[256]);      /* sRGB code -> linear * 255 */
+
+/* Integer-only ASTC LDR decoder (UNORM8 out, tightly packed RGBA8).
+ * Error blocks decode to magenta (255,0,255,255).  Returns the number of
+ * error blocks, or negative on bad arguments. */
+int oracle_decode(const uint8_t* blocks, int width, int height,
+                  int block_w, int block_h, int srgb, uint8_t* out_rgba);
+/* Decode one block (used by the property tests). */
+int oracle_decode_block(const uint8_t blk[16], int block_w, int block_h, int srgb,
+                        uint8_t* out_rgba);
+/* Spec unquantisation of one weight (to 0..64) / one colour value (0..255). */
+int oracle_unquant_weight(int quant, int value);
+int oracle_unquant_color(int quant, int value);
+
+/* The 2x2 texel taps and weights of grid point g (0..15) of the 4x4 weight
+ * grid of a 6x6 block (idx_grids / wt_grids, ASTC_Encode.hlsl:268-304). */
+void oracle_grid_taps(int g, int idx[4], float wt[4]);
+
+/* Algorithmic FP32 operation count of one block, counted by running the
+ * FP32 pipeline with counting arithmetic (FMA counted as 2). */
+double oracle_flops_per_block(int block_dim, int has_alpha, int is_normal);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
