@@ -272,6 +272,27 @@ def sse(a: np.ndarray, b: np.ndarray) -> np.ndarray:
     return np.array(list(res), dtype=np.uint64)
 
 
+def srgb_texel_values() -> np.ndarray:
+    """The texel value the encoder fits for each sRGB code (RGB channels):
+    float(IEC 61966-2-1 sRGB -> linear, evaluated in double) * 255 in float."""
+    x = np.arange(256, dtype=np.float64) / 255.0
+    lin = np.where(x <= 0.04045, x / 12.92, ((x + 0.055) / 1.055) ** 2.4)
+    return lin.astype(np.float32) * np.float32(255.0)
+
+
+def fitted_reference(rgba: np.ndarray, srgb: bool, is_normal: bool = False) -> np.ndarray:
+    """RGBA8 image in the space the encoder fits: sRGB codes linearised (and
+    rounded back to bytes) when `srgb`, B = A = 255 for normal maps.  This is
+    what a linear decode of the blocks approximates, so PSNR is taken here."""
+    ref = np.array(rgba, dtype=np.uint8, copy=True)
+    if srgb:
+        lut = np.clip(np.rint(srgb_texel_values()), 0, 255).astype(np.uint8)
+        ref[..., :3] = lut[ref[..., :3]]
+    if is_normal:
+        ref[..., 2:] = 255
+    return ref
+
+
 def psnr_from_sse(sse_value: float, count: int, peak: float = 255.0) -> float:
     if sse_value == 0:
         return float("inf")

@@ -53,6 +53,8 @@ def _parse():
     ap.add_argument("--workload", default="6x6_rgba_srgb_2048")
     ap.add_argument("--no-extra", action="store_true", help="skip the secondary workloads")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--profile-case", action="store_true",
+                    help="small case for ncu: 2 textures per step, encode launches only")
     return ap.parse_args()
 
 
@@ -270,8 +272,16 @@ def run_ours(args) -> None:
     h, w = img.shape[:2]
     dim = spec["block_dim"]
     nblocks = ((w + dim - 1) // dim) * ((h + dim - 1) // dim)
-    texs = _texture_batch(torch, img, TEXTURES_PER_STEP, salt=rank)
+    texs = _texture_batch(torch, img, 2 if args.profile_case else TEXTURES_PER_STEP, salt=rank)
     outs = [torch.empty((nblocks, 16), dtype=torch.uint8, device="cuda") for _ in texs]
+
+    if args.profile_case:
+        # only the encode launches: warm-up, then the timed steps; no other kernels
+        _time_launches(torch, native, texs, outs, spec, max(3, args.warmup))
+        per, _, launches = _time_launches(torch, native, texs, outs, spec, args.steps)
+        print(json.dumps({"profile_case": args.workload, "launches": launches,
+                          "mean_launch_us": float(np.mean(per)) * 1e3}), flush=True)
+        return
 
     # warm-up (untimed) + a short sustained burn so clocks settle
     _time_launches(torch, native, texs, outs, spec, max(3, args.warmup))
@@ -350,14 +360,18 @@ def run_ours(args) -> None:
     ora = oracle.encode(tex0, **spec)
     f64 = oracle.encode(tex0, **spec, fp64=True)
 
+    fitted = native.fitted_reference(tex0, spec["srgb"], spec["is_normal"])
+    ch = 4 if spec["has_alpha"] else (2 if spec["is_normal"] else 3)
+
     def psnr(blocks):
         d = native.decode(blocks, w, h, dim)
-        s = native.sse(d, tex0)
-        ch = 4 if spec["has_alpha"] else 3
+        s = native.sse(d, fitted)
         return native.psnr_from_sse(float(s[:ch].sum()), h * w * ch)
 
     quality = {"identical_blocks_vs_fp32_oracle": float(np.all(got == ora, axis=1).mean()),
-               "psnr_db": psnr(got), "psnr_fp32_oracle_db": psnr(ora), "psnr_fp64_oracle_db": psnr(f64)}
+               "psnr_db": psnr(got), "psnr_fp32_oracle_db": psnr(ora), "psnr_fp64_oracle_db": psnr(f64),
+               "psnr_space": ("linearised sRGB x255 (what the encoder fits), " if spec["srgb"] else "") +
+                             f"{ch} channels, spec LDR decode on the GPU"}
     quality["psnr_gap_to_fp64_db"] = quality["psnr_fp64_oracle_db"] - quality["psnr_db"]
 
     extra = {}

@@ -83,3 +83,8 @@ def test_unorm8_fetch_is_exact():
     # returns the integer code exactly for every byte value
     c = np.arange(256, dtype=np.float32)
     assert np.array_equal((c / np.float32(255.0)) * np.float32(255.0), c)
+
+
+def test_product_srgb_values_match_oracle(oracle):
+    import astc_encoder_gb300 as astc
+    assert np.array_equal(astc.srgb_texel_values(), oracle.srgb_lut())
