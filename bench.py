@@ -229,8 +229,11 @@ def run_reference(args) -> None:
     print(json.dumps(line), flush=True)
 
 
-def _time_launches(torch, native, texs, outs, spec, steps, counted=True):
-    """Runs `steps` steps over the batch; returns (per-launch ms list, step ms list, launches)."""
+def _time_launches(torch, native, texs, outs, spec, steps):
+    """Runs `steps` steps over the batch with a CUDA event pair around each step
+    (on the launching stream); returns (mean ms per launch, step ms list, launches).
+    Launches within a step run back to back, so step time / launches is the
+    mean launch duration."""
     h, w = texs[0].shape[:2]
     stream = torch.cuda.current_stream()
     lib = native.load_library()
@@ -238,22 +241,20 @@ def _time_launches(torch, native, texs, outs, spec, steps, counted=True):
                                          **spec))
     ptrs = [(t.data_ptr(), o.data_ptr()) for t, o in zip(texs, outs)]
     enc = lib.astc_encode_gpu_pitched
-    ev = [[(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-           for _ in texs] for _ in range(steps)]
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(steps)]
     l0 = native.kernel_launch_count()
     for s in range(steps):
-        for i, (src, dst) in enumerate(ptrs):
-            a, b = ev[s][i]
-            a.record(stream)
+        ev[s][0].record(stream)
+        for src, dst in ptrs:
             st = enc(src, w, h, w * 4, opts, dst)
-            b.record(stream)
             if st != 0:
                 raise native.AstcError(st, lib.astc_last_error().decode())
+        ev[s][1].record(stream)
     torch.cuda.synchronize()
     launches = native.kernel_launch_count() - l0
-    per = [a.elapsed_time(b) for row in ev for a, b in row]
-    per_step = [ev[s][0][0].elapsed_time(ev[s][-1][1]) for s in range(steps)]
-    return per, per_step, launches
+    per_step = [a.elapsed_time(b) for a, b in ev]
+    return sum(per_step) / max(1, launches), per_step, launches
 
 
 def run_ours(args) -> None:
@@ -280,7 +281,7 @@ def run_ours(args) -> None:
         _time_launches(torch, native, texs, outs, spec, max(3, args.warmup))
         per, _, launches = _time_launches(torch, native, texs, outs, spec, args.steps)
         print(json.dumps({"profile_case": args.workload, "launches": launches,
-                          "mean_launch_us": float(np.mean(per)) * 1e3}), flush=True)
+                          "mean_launch_us": per * 1e3}), flush=True)
         return
 
     # warm-up (untimed) + a short sustained burn so clocks settle
@@ -343,7 +344,7 @@ def run_ours(args) -> None:
     # roofline of the dominant kernel
     from oracle import oracle
     peaks = _peaks()
-    mean_launch_s = float(np.mean(per)) / 1e3
+    mean_launch_s = per / 1e3
     alg_bytes = h * w * 4 + nblocks * 16
     hbm_peak = peaks.get("hbm_gbs")
     achieved_gbs = alg_bytes / mean_launch_s / 1e9
@@ -389,7 +390,7 @@ def run_ours(args) -> None:
             _time_launches(torch, native, xt, xo, xspec, 3)
             xper, xsteps, _ = _time_launches(torch, native, xt, xo, xspec, 10)
             extra[name] = {"value": xh * xw * reps * 10 / (sum(xsteps) / 1e3) / 1e6, "unit": "Mtexels/s",
-                           "mean_launch_us": float(np.mean(xper)) * 1e3,
+                           "mean_launch_us": xper * 1e3,
                            "textures_per_step": reps}
             del xt, xo
 
