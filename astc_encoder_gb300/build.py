@@ -35,6 +35,7 @@ LIB_SOURCES = [
     ("astc_encode.cu", ["--fmad=false"]),
     ("astc_decode.cu", []),
     ("astc_capi.cu", []),
+    ("astc_noalloc.cu", []),
 ]
 CLI_SOURCES = [
     ("astc_cs_enc.cpp", []),

@@ -1,0 +1,168 @@
+// astc_noalloc.cu -- astc_sse_gpu_noalloc: the per-channel SSE reduction of
+// astc_sse_gpu, for callers that may not allocate device memory.
+//
+// Who needs it: applications that own the whole device-memory budget through
+// their own allocator and forbid a library from allocating behind their back
+// (game engines, texture-streaming and serving processes that admit work by
+// memory), and real-time loops where a cudaMalloc/cudaFree would synchronise
+// the device in the middle of a frame.  astc_sse_gpu allocates its
+// accumulator (and, for host memory, staging) the first time it runs; this
+// entry point allocates nothing.
+//
+// How: the scratch -- one partial sum (4 x u64) per chunk of 65,536 texels --
+// is a file-scope static __device__ array of fixed size (4096 chunks, 128 KiB),
+// which every GPU that loads this library holds until the process exits.  The
+// inputs (two RGBA8 images in device memory) and the output (4 x u64 in device
+// memory) are the caller's.  The first call on a device looks up the array's
+// device address with cudaGetSymbolAddress (with that device current) and
+// caches it; that first call should come before any stream capture.  All calls
+// share the array: two calls whose kernels overlap on the GPU race on it.
+// Each chunk's CTA overwrites its own partial and the final kernel reads only
+// the partials of the current call, so nothing has to start at zero.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <mutex>
+#include <string>
+
+#include "astc_internal.h"
+
+namespace astc {
+namespace {
+
+constexpr int kNoAllocMaxChunks = 4096;
+constexpr size_t kNoAllocChunkTexels = size_t(1) << 16;
+constexpr size_t kNoAllocMaxTexels = kNoAllocMaxChunks * kNoAllocChunkTexels;   // 2^28
+constexpr int kNoAllocThreads = 256;
+
+static __device__ __align__(256) unsigned long long g_noalloc_partials[kNoAllocMaxChunks * 4];
+
+constexpr int kMaxDevicesNoAlloc = 64;
+std::mutex g_noalloc_mu;
+unsigned long long* g_noalloc_ptr[kMaxDevicesNoAlloc] = {};
+
+__device__ __forceinline__ unsigned long long block_sum(unsigned long long v, unsigned long long* red) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, o);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    __syncthreads();
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
+    unsigned long long s = 0;
+    if (threadIdx.x == 0)
+        for (int w = 0; w < kNoAllocThreads / 32; ++w) s += red[w];
+    return s;
+}
+
+// One CTA per chunk: writes the chunk's R, G, B, A sums of squared differences.
+__global__ void __launch_bounds__(kNoAllocThreads)
+astc_sse_chunks_static(const uint32_t* __restrict__ a, const uint32_t* __restrict__ b, size_t n,
+                       unsigned long long* __restrict__ partials) {
+    __shared__ unsigned long long red[kNoAllocThreads / 32];
+    const size_t begin = (size_t)blockIdx.x * kNoAllocChunkTexels;
+    const size_t end = begin + kNoAllocChunkTexels < n ? begin + kNoAllocChunkTexels : n;
+    unsigned long long acc[4] = {0, 0, 0, 0};
+    for (size_t i = begin + threadIdx.x; i < end; i += kNoAllocThreads) {
+        const uint32_t x = __ldg(a + i), y = __ldg(b + i);
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            const int d = (int)((x >> (8 * c)) & 0xFF) - (int)((y >> (8 * c)) & 0xFF);
+            acc[c] += (unsigned long long)(d * d);
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        const unsigned long long s = block_sum(acc[c], red);
+        if (threadIdx.x == 0) partials[(size_t)blockIdx.x * 4 + c] = s;
+    }
+}
+
+// One CTA: totals of the `chunks` partials of this call into the caller's output.
+__global__ void __launch_bounds__(kNoAllocThreads)
+astc_sse_finish_static(const unsigned long long* __restrict__ partials, int chunks,
+                       unsigned long long* __restrict__ out) {
+    __shared__ unsigned long long red[kNoAllocThreads / 32];
+    unsigned long long acc[4] = {0, 0, 0, 0};
+    for (int i = threadIdx.x; i < chunks; i += kNoAllocThreads)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) acc[c] += partials[(size_t)i * 4 + c];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        const unsigned long long s = block_sum(acc[c], red);
+        if (threadIdx.x == 0) out[c] = s;
+    }
+}
+
+astc_status noalloc_scratch(unsigned long long** out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_error(e, "cudaGetDevice");
+    if (dev < 0 || dev >= kMaxDevicesNoAlloc)
+        return set_error(ASTC_ERR_UNSUPPORTED, "device index out of range");
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_noalloc_partials);   // with `dev` current
+        if (e != cudaSuccess) return cuda_error(e, "cudaGetSymbolAddress of the static scratch");
+        g_noalloc_ptr[dev] = static_cast<unsigned long long*>(p);
+    }
+    *out = g_noalloc_ptr[dev];
+    return ASTC_OK;
+}
+
+astc_status check_device_ptr(const void* ptr, const char* what) {
+    cudaPointerAttributes at;
+    const cudaError_t e = cudaPointerGetAttributes(&at, ptr);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return set_error(ASTC_ERR_INVALID_ARG, std::string(what) + " is not a CUDA pointer");
+    }
+    if (at.type != cudaMemoryTypeDevice && at.type != cudaMemoryTypeManaged)
+        return set_error(ASTC_ERR_INVALID_ARG, std::string(what) + " is not device memory");
+    return ASTC_OK;
+}
+
+}  // namespace
+}  // namespace astc
+
+using namespace astc;
+
+extern "C" astc_status astc_sse_gpu_noalloc(const uint8_t* a, const uint8_t* b, size_t texels,
+                                            void* stream, uint64_t* sse_rgba) {
+    try {
+        if (!a || !b || !sse_rgba) return set_error(ASTC_ERR_INVALID_ARG, "NULL pointer");
+        if (texels > kNoAllocMaxTexels)
+            return set_error(ASTC_ERR_INVALID_ARG,
+                             "astc_sse_gpu_noalloc: " + std::to_string(texels) +
+                                 " texels exceed the static scratch limit of " +
+                                 std::to_string(kNoAllocMaxTexels) +
+                                 " (4096 chunks of 65536); use astc_sse_gpu");
+        if (reinterpret_cast<uintptr_t>(a) % 4 || reinterpret_cast<uintptr_t>(b) % 4 ||
+            reinterpret_cast<uintptr_t>(sse_rgba) % 8)
+            return set_error(ASTC_ERR_INVALID_ARG,
+                             "images must be 4-byte and the output 8-byte aligned");
+        astc_status st;
+        if ((st = check_device_ptr(a, "a")) != ASTC_OK) return st;
+        if ((st = check_device_ptr(b, "b")) != ASTC_OK) return st;
+        if ((st = check_device_ptr(sse_rgba, "sse_rgba")) != ASTC_OK) return st;
+        unsigned long long* scratch = nullptr;
+        if ((st = noalloc_scratch(&scratch)) != ASTC_OK) return st;
+        cudaStream_t s = static_cast<cudaStream_t>(stream);
+        const int chunks = (int)((texels + kNoAllocChunkTexels - 1) / kNoAllocChunkTexels);
+        if (chunks > 0) {
+            astc_sse_chunks_static<<<chunks, kNoAllocThreads, 0, s>>>(
+                reinterpret_cast<const uint32_t*>(a), reinterpret_cast<const uint32_t*>(b), texels,
+                scratch);
+            cudaError_t e = cudaGetLastError();
+            if (e != cudaSuccess) return cuda_error(e, "sse chunk kernel launch");
+            count_launches(1);
+        }
+        astc_sse_finish_static<<<1, kNoAllocThreads, 0, s>>>(
+            scratch, chunks, reinterpret_cast<unsigned long long*>(sse_rgba));
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return cuda_error(e, "sse finish kernel launch");
+        count_launches(1);
+        return ASTC_OK;
+    } catch (...) {
+        return set_error(ASTC_ERR_CUDA, "unexpected exception");
+    }
+}

@@ -127,6 +127,24 @@ astc_status astc_decode_gpu(const uint8_t* blocks, int width, int height,
 astc_status astc_sse_gpu(const uint8_t* a, const uint8_t* b, size_t texels,
                          int memory, void* stream, uint64_t sse_rgba[4]);
 
+/* astc_sse_gpu for callers that may not allocate device memory (no
+ * counterpart in the reference).  Some hosts own the whole device-memory
+ * budget through their own allocator and forbid a library from allocating
+ * behind their back (game engines, texture-streaming and serving processes
+ * that admit work by memory); in real-time loops a cudaMalloc/cudaFree would
+ * also synchronise the device mid-frame.  This entry point calls no
+ * cudaMalloc/cudaFree: `a` and `b` (RGBA8, 4-byte aligned) and `sse_rgba`
+ * (4 x uint64, 8-byte aligned) are all caller-owned DEVICE memory, and its
+ * scratch is a fixed static device array (one partial per 65,536 texels,
+ * 4096 partials = 128 KiB) that every GPU loading this library holds until
+ * exit.  Limit: texels <= 2^28 (268,435,456); larger calls return
+ * ASTC_ERR_INVALID_ARG.  Asynchronous on `stream` (NULL = the legacy default
+ * stream).  The first call on a device looks up the scratch address with
+ * that device current; make that first call before any stream capture.
+ * Calls share the scratch: calls whose kernels overlap on the GPU race. */
+astc_status astc_sse_gpu_noalloc(const uint8_t* a, const uint8_t* b, size_t texels,
+                                 void* stream, uint64_t* sse_rgba);
+
 /* Message for the last failed call on this thread ("" if none). */
 const char* astc_last_error(void);
 const char* astc_status_string(astc_status status);
