@@ -144,8 +144,42 @@ def load_library() -> ctypes.CDLL:
     lib.astc_kernel_launch_count.restype = ctypes.c_uint64
     lib.astc_shutdown.argtypes = []
     lib.astc_shutdown.restype = None
+    lib.astc_autotune.argtypes = [ctypes.c_int] * 6 + [ctypes.POINTER(TuneResult)]
+    lib.astc_autotune.restype = ctypes.c_int
+    lib.astc_set_kernel_choice.argtypes = [ctypes.c_int] * 6
+    lib.astc_set_kernel_choice.restype = ctypes.c_int
+    lib.astc_get_kernel_choice.argtypes = [ctypes.c_int] * 4 + [ip, ip]
+    lib.astc_get_kernel_choice.restype = ctypes.c_int
     _LIB = lib
     return lib
+
+
+class TuneResult(ctypes.Structure):
+    """``astc_tune_result`` of include/astc_gb300.h."""
+    _fields_ = [("store", ctypes.c_int), ("threads", ctypes.c_int), ("best_us", ctypes.c_float),
+                ("default_us", ctypes.c_float)]
+
+
+def autotune(block_dim: int, has_alpha: bool = False, is_normal: bool = False, srgb: bool = False,
+             width: int = 2048, height: int = 2048) -> TuneResult:
+    """Time every kernel variant for a format and install the fastest."""
+    r = TuneResult()
+    _check(load_library().astc_autotune(block_dim, int(has_alpha), int(is_normal), int(srgb), width,
+                                        height, ctypes.byref(r)))
+    return r
+
+
+def set_kernel_choice(block_dim: int, has_alpha: bool, is_normal: bool, srgb: bool, store: int,
+                      threads: int) -> None:
+    _check(load_library().astc_set_kernel_choice(block_dim, int(has_alpha), int(is_normal), int(srgb),
+                                                 store, threads))
+
+
+def get_kernel_choice(block_dim: int, has_alpha: bool, is_normal: bool, srgb: bool) -> tuple[int, int]:
+    s, t = ctypes.c_int(), ctypes.c_int()
+    _check(load_library().astc_get_kernel_choice(block_dim, int(has_alpha), int(is_normal), int(srgb),
+                                                 ctypes.byref(s), ctypes.byref(t)))
+    return s.value, t.value
 
 
 def _check(status: int) -> None:

@@ -36,12 +36,13 @@ LIB_SOURCES = [
     ("astc_decode.cu", []),
     ("astc_capi.cu", []),
     ("astc_noalloc.cu", []),
+    ("astc_tune.cu", []),
 ]
 CLI_SOURCES = [
     ("astc_cs_enc.cpp", []),
     ("image_load.cpp", []),
 ]
-HEADERS = ["astc_internal.h", "astc_tables.h", "image_load.h"]
+HEADERS = ["astc_internal.h", "astc_tables.h", "astc_block_common.cuh", "image_load.h"]
 
 
 def nvcc() -> str:

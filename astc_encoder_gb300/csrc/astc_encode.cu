@@ -10,10 +10,13 @@
 //                        quantize_weight 256-260
 //   scramble + ISE       weight_ise 491-508, bise_* (ISE.hlsl 207-276)
 //   block assembly       assemble_block 400-444, assemble_blockmode 446-473
-// but written for the GPU: texels stay packed RGBA8 in registers and are
-// expanded to exact floats on use (byte_perm into a 2^23-biased float), the
-// ISE of a fixed weight range is unrolled into 64-bit shifts, and the weight
-// bit reversal is one __brevll.
+// but written for the GPU: each texel is decoded once (UNORM8 by a byte_perm
+// into a 2^23-biased float, sRGB through a shared-memory table) into a texel
+// store -- registers, or for 6x6 a [texel][thread] shared-memory array that
+// keeps the register count (and so the occupancy) of the 36-texel block in
+// check; the length tests compare against an exact threshold instead of
+// taking a square root; the ISE of the fixed weight range is unrolled into
+// 64-bit shifts and the weight bit reversal is one __brevll.
 //
 // Floating point follows the FP32 oracle's model operation by operation:
 // mad = fused (__fmaf_rn), dot(a,b) = a.x*b.x then fused over y, z, w,
@@ -25,190 +28,97 @@
 #include <stdint.h>
 
 #include <cmath>
+#include <mutex>
 
+#include "astc_block_common.cuh"
 #include "astc_internal.h"
-#include "astc_tables.h"
 
 namespace astc {
 namespace {
 
-constexpr int kThreads = 128;
-
-struct TritPack { uint8_t v[256]; };
-constexpr TritPack make_trit_pack() {
-    TritPack p{};
-    const IseTables t = make_ise_tables();
-    for (int i = 0; i < 243; ++i) p.v[i] = t.trit_pack[i];
-    return p;
-}
+constexpr int kMaxThreads = 256;
 
 __constant__ TritPack c_trit_pack = make_trit_pack();
 __constant__ float c_srgb_x255[256];
 
 struct Launch {
-    const uint8_t* in;
-    size_t pitch;
-    int width, height, nbx;
+    TextureView tex;
     long long nblocks;
     uint4* out;
-    int vec_ok;     // row vector loads allowed (alignment of base and pitch)
-    int clamp;      // ASTC_BORDER_CLAMP
 };
 
-// exact float of byte c of a packed RGBA8 texel: bits 0x4B0000cc = 2^23 + c
-__device__ __forceinline__ float byte_to_float(uint32_t px, int c) {
-    const uint32_t bits = __byte_perm(px, 0x4B000000u, 0x7440u + (uint32_t)c);
-    return __fsub_rn(__uint_as_float(bits), 8388608.0f);
-}
-
-// round-half-even of x in [0, 2^22] as an integer: the add rounds to nearest
-// even at unit spacing.
-__device__ __forceinline__ uint32_t rint_u32(float x) {
-    return __float_as_uint(__fadd_rn(x, 8388608.0f)) - 0x4B000000u;
-}
-
-__device__ __forceinline__ float dot4(const float a[4], const float b[4]) {
-    float d = __fmul_rn(a[0], b[0]);
-    d = __fmaf_rn(a[1], b[1], d);
-    d = __fmaf_rn(a[2], b[2], d);
-    d = __fmaf_rn(a[3], b[3], d);
-    return d;
-}
-
-__device__ __forceinline__ void normalize4(float v[4]) {
-    const float r = __frcp_rn(__fsqrt_rn(dot4(v, v)));
-#pragma unroll
-    for (int i = 0; i < 4; ++i) v[i] = __fmul_rn(v[i], r);
-}
-
-template <bool SRGB, bool NORMAL>
-__device__ __forceinline__ float texel(uint32_t px, int c, const float* lut) {
-    if (NORMAL && c >= 2) return 255.0f;                 // b = a = 1.0 (x255)
-    if (SRGB && c < 3) return lut[(px >> (8 * c)) & 0xFFu];
-    return byte_to_float(px, c);                          // c/255*255 == c
-}
-
 // ---------------------------------------------------------------------------
-// texel fetch (MainCS 561-580); zero or clamp outside the image
+// per-block pipeline (encode_block 510-550) over a texel store S
 // ---------------------------------------------------------------------------
-template <int DIM>
-__device__ __forceinline__ void load_block(const Launch& p, int bx, int by,
-                                           uint32_t (&px)[DIM * DIM]) {
-    const int x0 = bx * DIM, y0 = by * DIM;
-    if (x0 + DIM <= p.width && y0 + DIM <= p.height) {
-        const uint8_t* row = p.in + (size_t)y0 * p.pitch + (size_t)x0 * 4;
-#pragma unroll
-        for (int r = 0; r < DIM; ++r) {
-            bool done = false;
-            if constexpr (DIM == 4) {
-                if (p.vec_ok) {
-                    const uint4 v = __ldg(reinterpret_cast<const uint4*>(row));
-                    px[r * 4 + 0] = v.x; px[r * 4 + 1] = v.y; px[r * 4 + 2] = v.z; px[r * 4 + 3] = v.w;
-                    done = true;
-                }
-            } else {
-                if (p.vec_ok) {
-                    const uint2* q = reinterpret_cast<const uint2*>(row);
-                    const uint2 a = __ldg(q), b = __ldg(q + 1), c = __ldg(q + 2);
-                    px[r * 6 + 0] = a.x; px[r * 6 + 1] = a.y; px[r * 6 + 2] = b.x;
-                    px[r * 6 + 3] = b.y; px[r * 6 + 4] = c.x; px[r * 6 + 5] = c.y;
-                    done = true;
-                }
-            }
-            if (!done) {
-                const uint32_t* q = reinterpret_cast<const uint32_t*>(row);
-#pragma unroll
-                for (int x = 0; x < DIM; ++x) px[r * DIM + x] = __ldg(q + x);
-            }
-            row += p.pitch;
-        }
-    } else {
-#pragma unroll
-        for (int k = 0; k < DIM * DIM; ++k) {
-            int x = x0 + k % DIM, y = y0 + k / DIM;
-            const bool inside = x < p.width && y < p.height;
-            uint32_t v = 0;                                   // D3D11 OOB Load -> 0
-            if (inside || p.clamp) {
-                x = x < p.width ? x : p.width - 1;
-                y = y < p.height ? y : p.height - 1;
-                v = __ldg(reinterpret_cast<const uint32_t*>(p.in + (size_t)y * p.pitch) + x);
-            }
-            px[k] = v;
-        }
-    }
-}
-
-// ---------------------------------------------------------------------------
-// per-block pipeline (encode_block 510-550)
-// ---------------------------------------------------------------------------
-template <int DIM, bool ALPHA, bool NORMAL, bool SRGB>
-__device__ __forceinline__ uint4 encode_block(const uint32_t (&px)[DIM * DIM], const float* lut,
-                                              const uint8_t* trits) {
+template <int DIM, bool ALPHA, class S>
+__device__ __forceinline__ uint4 encode_block_fp32(const S& st, const uint8_t* trits) {
     constexpr int N = DIM * DIM;
     // mean (143-147), then x fl(1/N)
-    float mean[4] = {0.f, 0.f, 0.f, 0.f};
-#pragma unroll
-    for (int k = 0; k < N; ++k)
-#pragma unroll
-        for (int c = 0; c < 4; ++c) mean[c] = __fadd_rn(mean[c], texel<SRGB, NORMAL>(px[k], c, lut));
-    constexpr float kInvN = 1.0f / (float)N;
-#pragma unroll
-    for (int c = 0; c < 4; ++c) mean[c] = __fmul_rn(mean[c], kInvN);
-
-    // covariance (149-162): symmetric, 10 unique terms, x fl(1/(N-1))
-    float cv[10] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    float m0 = 0.f, m1 = 0.f, m2 = 0.f, m3 = 0.f;
 #pragma unroll
     for (int k = 0; k < N; ++k) {
-        float d[4];
+        const float4 t = st.get(k);
+        m0 = __fadd_rn(m0, t.x); m1 = __fadd_rn(m1, t.y);
+        m2 = __fadd_rn(m2, t.z); m3 = __fadd_rn(m3, t.w);
+    }
+    constexpr float kInvN = 1.0f / (float)N;
+    m0 = __fmul_rn(m0, kInvN); m1 = __fmul_rn(m1, kInvN);
+    m2 = __fmul_rn(m2, kInvN); m3 = __fmul_rn(m3, kInvN);
+
+    // covariance (149-162): symmetric, 10 unique terms, x fl(1/(N-1))
+    float c00 = 0.f, c01 = 0.f, c02 = 0.f, c03 = 0.f, c11 = 0.f, c12 = 0.f, c13 = 0.f,
+          c22 = 0.f, c23 = 0.f, c33 = 0.f;
 #pragma unroll
-        for (int c = 0; c < 4; ++c) d[c] = __fsub_rn(texel<SRGB, NORMAL>(px[k], c, lut), mean[c]);
-        int e = 0;
-#pragma unroll
-        for (int i = 0; i < 4; ++i)
-#pragma unroll
-            for (int j = i; j < 4; ++j, ++e) cv[e] = __fmaf_rn(d[i], d[j], cv[e]);
+    for (int k = 0; k < N; ++k) {
+        const float4 t = st.get(k);
+        const float d0 = __fsub_rn(t.x, m0), d1 = __fsub_rn(t.y, m1);
+        const float d2 = __fsub_rn(t.z, m2), d3 = __fsub_rn(t.w, m3);
+        c00 = __fmaf_rn(d0, d0, c00); c01 = __fmaf_rn(d0, d1, c01);
+        c02 = __fmaf_rn(d0, d2, c02); c03 = __fmaf_rn(d0, d3, c03);
+        c11 = __fmaf_rn(d1, d1, c11); c12 = __fmaf_rn(d1, d2, c12);
+        c13 = __fmaf_rn(d1, d3, c13); c22 = __fmaf_rn(d2, d2, c22);
+        c23 = __fmaf_rn(d2, d3, c23); c33 = __fmaf_rn(d3, d3, c33);
     }
     constexpr float kInvN1 = 1.0f / (float)(N - 1);
-#pragma unroll
-    for (int e = 0; e < 10; ++e) cv[e] = __fmul_rn(cv[e], kInvN1);
-    const float m[4][4] = {{cv[0], cv[1], cv[2], cv[3]},
-                           {cv[1], cv[4], cv[5], cv[6]},
-                           {cv[2], cv[5], cv[7], cv[8]},
-                           {cv[3], cv[6], cv[8], cv[9]}};
+    c00 = __fmul_rn(c00, kInvN1); c01 = __fmul_rn(c01, kInvN1); c02 = __fmul_rn(c02, kInvN1);
+    c03 = __fmul_rn(c03, kInvN1); c11 = __fmul_rn(c11, kInvN1); c12 = __fmul_rn(c12, kInvN1);
+    c13 = __fmul_rn(c13, kInvN1); c22 = __fmul_rn(c22, kInvN1); c23 = __fmul_rn(c23, kInvN1);
+    c33 = __fmul_rn(c33, kInvN1);
 
-    // power iteration (93-106)
-    float v[4] = {0.26726f, 0.80178f, 0.53452f, 0.0f};
+    // power iteration (93-106): v = M v; stop if |v| < 1e-5; v = normalize(M v)
+    float v0 = 0.26726f, v1 = 0.80178f, v2 = 0.53452f, v3 = 0.0f;
 #pragma unroll 1
     for (int it = 0; it < 8; ++it) {
-        float t[4];
-#pragma unroll
-        for (int r = 0; r < 4; ++r) t[r] = dot4(m[r], v);
-#pragma unroll
-        for (int r = 0; r < 4; ++r) v[r] = t[r];
-        if (__fsqrt_rn(dot4(v, v)) < 1e-5f) break;
-#pragma unroll
-        for (int r = 0; r < 4; ++r) t[r] = dot4(m[r], v);
-#pragma unroll
-        for (int r = 0; r < 4; ++r) v[r] = t[r];
-        normalize4(v);
+        float t0 = dot4(c00, c01, c02, c03, v0, v1, v2, v3);
+        float t1 = dot4(c01, c11, c12, c13, v0, v1, v2, v3);
+        float t2 = dot4(c02, c12, c22, c23, v0, v1, v2, v3);
+        float t3 = dot4(c03, c13, c23, c33, v0, v1, v2, v3);
+        v0 = t0; v1 = t1; v2 = t2; v3 = t3;
+        if (shorter_than_small_value(dot4(v0, v1, v2, v3, v0, v1, v2, v3))) break;
+        t0 = dot4(c00, c01, c02, c03, v0, v1, v2, v3);
+        t1 = dot4(c01, c11, c12, c13, v0, v1, v2, v3);
+        t2 = dot4(c02, c12, c22, c23, v0, v1, v2, v3);
+        t3 = dot4(c03, c13, c23, c33, v0, v1, v2, v3);
+        const float r = rnorm_from_dot(dot4(t0, t1, t2, t3, t0, t1, t2, t3));
+        v0 = __fmul_rn(t0, r); v1 = __fmul_rn(t1, r); v2 = __fmul_rn(t2, r); v3 = __fmul_rn(t3, r);
     }
 
     // find_min_max (108-137)
     float a = 1e31f, b = -1e31f;
 #pragma unroll
     for (int k = 0; k < N; ++k) {
-        float d[4];
-#pragma unroll
-        for (int c = 0; c < 4; ++c) d[c] = __fsub_rn(texel<SRGB, NORMAL>(px[k], c, lut), mean[c]);
-        const float t = dot4(d, v);
-        a = fminf(a, t);
-        b = fmaxf(b, t);
+        const float4 t = st.get(k);
+        const float p = dot4(__fsub_rn(t.x, m0), __fsub_rn(t.y, m1), __fsub_rn(t.z, m2),
+                             __fsub_rn(t.w, m3), v0, v1, v2, v3);
+        a = fminf(a, p);
+        b = fmaxf(b, p);
     }
     float e0[4], e1[4];
+    const float mv[4] = {m0, m1, m2, m3}, vv[4] = {v0, v1, v2, v3};
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
-        e0[c] = fminf(fmaxf(__fmaf_rn(v[c], a, mean[c]), 0.0f), 255.0f);
-        e1[c] = fminf(fmaxf(__fmaf_rn(v[c], b, mean[c]), 0.0f), 255.0f);
+        e0[c] = fminf(fmaxf(__fmaf_rn(vv[c], a, mv[c]), 0.0f), 255.0f);
+        e1[c] = fminf(fmaxf(__fmaf_rn(vv[c], b, mv[c]), 0.0f), 255.0f);
     }
     uint32_t q0[4], q1[4];
 #pragma unroll
@@ -225,105 +135,58 @@ __device__ __forceinline__ uint4 encode_block(const uint32_t (&px)[DIM * DIM], c
     // weights on the 4x4 grid (316-372), quantised (256-260, 374-393)
     constexpr uint32_t R = ALPHA ? 5u : 11u;
     uint32_t qw[16];
-    {
-        float k[4];
+    float k0 = __fsub_rn(e1[0], e0[0]), k1 = __fsub_rn(e1[1], e0[1]);
+    float k2 = __fsub_rn(e1[2], e0[2]), k3 = __fsub_rn(e1[3], e0[3]);
+    const float kk = dot4(k0, k1, k2, k3, k0, k1, k2, k3);
+    if (shorter_than_small_value(kk)) {
 #pragma unroll
-        for (int c = 0; c < 4; ++c) k[c] = __fsub_rn(e1[c], e0[c]);
-        if (__fsqrt_rn(dot4(k, k)) < 1e-5f) {
+        for (int i = 0; i < 16; ++i) qw[i] = 0u;
+    } else {
+        const float r = rnorm_from_dot(kk);
+        k0 = __fmul_rn(k0, r); k1 = __fmul_rn(k1, r); k2 = __fmul_rn(k2, r); k3 = __fmul_rn(k3, r);
+        float w[16];
+        float minw = 1e31f, maxw = -1e31f;
 #pragma unroll
-            for (int i = 0; i < 16; ++i) qw[i] = 0u;
-        } else {
-            normalize4(k);
-            float w[16];
-            float minw = 1e31f, maxw = -1e31f;
-#pragma unroll
-            for (int i = 0; i < 16; ++i) {
-                float s[4];
-                if constexpr (DIM == 6) {
-                    // 2x2 taps of grid point i: columns/rows {0,1,3,4}+{0,1};
-                    // 4/9, 2/9, 1/9 written as 0.444, 0.222, 0.111
-                    const int gx = i & 3, gy = i >> 2;
-                    const int i0 = (gy < 2 ? gy : gy + 1) * 6 + (gx < 2 ? gx : gx + 1);
-                    const bool xl = (gx & 1) == 0, yl = (gy & 1) == 0;
-                    const float w00 = (xl && yl) ? 0.444f : (xl || yl) ? 0.222f : 0.111f;
-                    const float w01 = (!xl && yl) ? 0.444f : (!xl || yl) ? 0.222f : 0.111f;
-                    const float w10 = (xl && !yl) ? 0.444f : (xl || !yl) ? 0.222f : 0.111f;
-                    const float w11 = (!xl && !yl) ? 0.444f : (!xl || !yl) ? 0.222f : 0.111f;
-#pragma unroll
-                    for (int c = 0; c < 4; ++c) {
-                        float acc = __fmul_rn(texel<SRGB, NORMAL>(px[i0], c, lut), w00);
-                        acc = __fmaf_rn(texel<SRGB, NORMAL>(px[i0 + 1], c, lut), w01, acc);
-                        acc = __fmaf_rn(texel<SRGB, NORMAL>(px[i0 + 6], c, lut), w10, acc);
-                        acc = __fmaf_rn(texel<SRGB, NORMAL>(px[i0 + 7], c, lut), w11, acc);
-                        s[c] = acc;
-                    }
-                } else {
-#pragma unroll
-                    for (int c = 0; c < 4; ++c) s[c] = texel<SRGB, NORMAL>(px[i], c, lut);
-                }
-                float d[4];
-#pragma unroll
-                for (int c = 0; c < 4; ++c) d[c] = __fsub_rn(s[c], e0[c]);
-                const float x = dot4(k, d);
-                minw = fminf(x, minw);
-                maxw = fmaxf(x, maxw);
-                w[i] = x;
+        for (int i = 0; i < 16; ++i) {
+            float4 s;
+            if constexpr (DIM == 6) {
+                const int i0 = grid_tap0(i);
+                float w00, w01, w10, w11;
+                grid_weights(i, w00, w01, w10, w11);
+                const float4 t00 = st.get(i0), t01 = st.get(i0 + 1), t10 = st.get(i0 + 6),
+                             t11 = st.get(i0 + 7);
+                s.x = __fmaf_rn(t11.x, w11, __fmaf_rn(t10.x, w10, __fmaf_rn(t01.x, w01, __fmul_rn(t00.x, w00))));
+                s.y = __fmaf_rn(t11.y, w11, __fmaf_rn(t10.y, w10, __fmaf_rn(t01.y, w01, __fmul_rn(t00.y, w00))));
+                s.z = __fmaf_rn(t11.z, w11, __fmaf_rn(t10.z, w10, __fmaf_rn(t01.z, w01, __fmul_rn(t00.z, w00))));
+                s.w = __fmaf_rn(t11.w, w11, __fmaf_rn(t10.w, w10, __fmaf_rn(t01.w, w01, __fmul_rn(t00.w, w00))));
+            } else {
+                s = st.get(i);
             }
-            float inv = fmaxf(1e-5f, __fsub_rn(maxw, minw));
-            inv = __frcp_rn(inv);
+            const float x = dot4(k0, k1, k2, k3, __fsub_rn(s.x, e0[0]), __fsub_rn(s.y, e0[1]),
+                                 __fsub_rn(s.z, e0[2]), __fsub_rn(s.w, e0[3]));
+            minw = fminf(x, minw);
+            maxw = fmaxf(x, maxw);
+            w[i] = x;
+        }
+        const float inv = __frcp_rn(fmaxf(1e-5f, __fsub_rn(maxw, minw)));
 #pragma unroll
-            for (int i = 0; i < 16; ++i) {
-                const float wn = __fmul_rn(__fsub_rn(w[i], minw), inv);
-                const uint32_t q = rint_u32(__fmul_rn(wn, (float)R));
-                qw[i] = q < R ? q : R;
-            }
+        for (int i = 0; i < 16; ++i) {
+            const float wn = __fmul_rn(__fsub_rn(w[i], minw), inv);
+            const uint32_t q = rint_u32(__fmul_rn(wn, (float)R));
+            qw[i] = q < R ? q : R;
         }
     }
-
-    // scramble (491-502) + ISE of 16 weights in trits (ISE.hlsl 142-176, 243-256)
-    constexpr int WQ = ALPHA ? kQuant6 : kQuant12;
-    constexpr int B = ALPHA ? 1 : 2;
-    constexpr uint64_t kScr = scramble_nibbles(WQ);
-    constexpr uint32_t kScrLo = (uint32_t)kScr, kScrHi = (uint32_t)(kScr >> 32);
-    uint64_t ws = 0;
-#pragma unroll
-    for (int g = 0; g < 4; ++g) {
-        uint32_t mm[5], tt[5];
-#pragma unroll
-        for (int j = 0; j < 5; ++j) {
-            const int idx = g * 5 + j;
-            uint32_t s = 0;
-            if (idx < 16) {
-                const uint32_t q = qw[idx < 16 ? idx : 0];
-                s = (q < 8 ? (kScrLo >> (4 * q)) : (kScrHi >> (4 * (q - 8)))) & 0xFu;
-            }
-            mm[j] = s & ((1u << B) - 1u);
-            tt[j] = s >> B;
-        }
-        const uint32_t T = trits[tt[4] * 81 + tt[3] * 27 + tt[2] * 9 + tt[1] * 3 + tt[0]];
-        const uint64_t grp = (uint64_t)mm[0] | ((uint64_t)(T & 3u) << B) |
-                             ((uint64_t)mm[1] << (B + 2)) | ((uint64_t)((T >> 2) & 3u) << (2 * B + 2)) |
-                             ((uint64_t)mm[2] << (2 * B + 4)) | ((uint64_t)((T >> 4) & 1u) << (3 * B + 4)) |
-                             ((uint64_t)mm[3] << (3 * B + 5)) | ((uint64_t)((T >> 5) & 3u) << (4 * B + 5)) |
-                             ((uint64_t)mm[4] << (4 * B + 7)) | ((uint64_t)((T >> 7) & 1u) << (5 * B + 7));
-        ws |= grp << (g * (5 * B + 8));
-    }
-
-    // endpoints in QUANT_256: r0 r1 g0 g1 b0 b1 [a0 a1], 8 bits each (bise_endpoints)
-    uint64_t ep = (uint64_t)q0[0] | ((uint64_t)q1[0] << 8) | ((uint64_t)q0[1] << 16) |
-                  ((uint64_t)q1[1] << 24) | ((uint64_t)q0[2] << 32) | ((uint64_t)q1[2] << 40);
-    if (ALPHA) ep |= ((uint64_t)q0[3] << 48) | ((uint64_t)q1[3] << 56);
-
-    // assemble_block (400-444): mode [10:0], CEM [16:13], endpoints from bit 17,
-    // weight stream bit-reversed from bit 127 down.
-    constexpr uint64_t kHead = (uint64_t)blockmode_4x4_grid(WQ) | ((uint64_t)(ALPHA ? 12u : 8u) << 13);
-    const uint64_t lo = kHead | (ep << 17);
-    const uint64_t hi = (ep >> 47) | __brevll(ws);
-    return make_uint4((uint32_t)lo, (uint32_t)(lo >> 32), (uint32_t)hi, (uint32_t)(hi >> 32));
+    return assemble_block<ALPHA>(q0, q1, qw, trits);
 }
 
-template <int DIM, bool ALPHA, bool NORMAL, bool SRGB>
-__global__ void __launch_bounds__(kThreads) astc_encode_blocks_fp32(const Launch p) {
+// The shared-memory store caps registers (two 256-thread CTAs per SM, <= 128
+// registers) so the compiler re-reads texels from shared memory instead of
+// holding all of them in registers across the passes.
+template <int DIM, bool ALPHA, bool NORMAL, bool SRGB, int STORE>
+__global__ void __launch_bounds__(kMaxThreads, STORE == kStoreShared ? 2 : 1)
+astc_encode_blocks_fp32(const Launch p) {
+    constexpr int N = DIM * DIM;
+    extern __shared__ float4 s_texels[];                  // kStoreShared only
     __shared__ uint8_t s_trits[256];
     __shared__ float s_lut[SRGB ? 256 : 1];
     for (int i = threadIdx.x; i < 256; i += blockDim.x) {
@@ -333,31 +196,88 @@ __global__ void __launch_bounds__(kThreads) astc_encode_blocks_fp32(const Launch
     __syncthreads();
     const long long b = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= p.nblocks) return;
-    const int by = (int)(b / p.nbx);
-    const int bx = (int)(b - (long long)by * p.nbx);
-    uint32_t px[DIM * DIM];
-    load_block<DIM>(p, bx, by, px);
-    p.out[b] = encode_block<DIM, ALPHA, NORMAL, SRGB>(px, s_lut, s_trits);
+    const int by = (int)(b / p.tex.nbx);
+    const int bx = (int)(b - (long long)by * p.tex.nbx);
+    uint32_t px[N];
+    load_block_packed<DIM>(p.tex, bx, by, px);
+    if constexpr (STORE == kStoreShared) {
+        SharedTexels<N> st{s_texels + threadIdx.x, (int)blockDim.x};
+#pragma unroll
+        for (int k = 0; k < N; ++k) st.put(k, decode_texel<SRGB, NORMAL>(px[k], s_lut));
+        p.out[b] = encode_block_fp32<DIM, ALPHA>(st, s_trits);
+    } else {
+        RegTexels<N> st;
+#pragma unroll
+        for (int k = 0; k < N; ++k) st.put(k, decode_texel<SRGB, NORMAL>(px[k], s_lut));
+        p.out[b] = encode_block_fp32<DIM, ALPHA>(st, s_trits);
+    }
 }
 
-template <int DIM, bool ALPHA, bool NORMAL, bool SRGB>
-cudaError_t launch_t(const Launch& p, cudaStream_t s) {
-    const long long grid = (p.nblocks + kThreads - 1) / kThreads;
-    astc_encode_blocks_fp32<DIM, ALPHA, NORMAL, SRGB><<<(unsigned)grid, kThreads, 0, s>>>(p);
+// Kernel choice per format: texel store and CTA size.  Defaults come from
+// measurements on GB300 (profiles/); the autotuner may replace them.
+struct Choice { int store; int threads; };
+Choice g_choice[2][2][2][2] = {};     // [dim6][alpha][normal][srgb]
+bool g_choice_init = false;
+std::mutex g_choice_mu;
+
+// GB300 sweep over 2048x2048 textures (us per launch, registers / shared at
+// 128 threads): 4x4 RGB 28.4 / 27.0, 4x4 RGBA sRGB 29.0 / 28.9, 4x4 normal
+// 20.8 / 20.8, 6x6 RGBA sRGB 26.8 / 39.1, 6x6 RGB 24.8 / 40.9.  The capped
+// shared-memory variant loses for 6x6 (its re-reads cost more than the
+// occupancy it gains) and ties or wins slightly for 4x4.
+Choice default_choice(int dim, bool /*alpha*/, bool /*normal*/, bool /*srgb*/) {
+    return dim == 6 ? Choice{kStoreRegisters, 128} : Choice{kStoreShared, 128};
+}
+
+template <int DIM, bool ALPHA, bool NORMAL, bool SRGB, int STORE>
+cudaError_t launch_t(const Launch& p, int threads, cudaStream_t s) {
+    constexpr int N = DIM * DIM;
+    const size_t smem = STORE == kStoreShared ? (size_t)N * threads * sizeof(float4) : 0;
+    auto kern = astc_encode_blocks_fp32<DIM, ALPHA, NORMAL, SRGB, STORE>;
+    if (smem > 48 * 1024) {
+        const cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                   (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    const long long grid = (p.nblocks + threads - 1) / threads;
+    kern<<<(unsigned)grid, threads, smem, s>>>(p);
     return cudaGetLastError();
 }
 
+template <int DIM, bool ALPHA, bool NORMAL, bool SRGB>
+cudaError_t launch_store(const Launch& p, const Choice& c, cudaStream_t s) {
+    if (c.store == kStoreShared)
+        return launch_t<DIM, ALPHA, NORMAL, SRGB, kStoreShared>(p, c.threads, s);
+    return launch_t<DIM, ALPHA, NORMAL, SRGB, kStoreRegisters>(p, c.threads, s);
+}
 template <int DIM, bool ALPHA, bool NORMAL>
-cudaError_t launch_srgb(const Launch& p, bool srgb, cudaStream_t s) {
-    return srgb ? launch_t<DIM, ALPHA, NORMAL, true>(p, s) : launch_t<DIM, ALPHA, NORMAL, false>(p, s);
+cudaError_t launch_srgb(const Launch& p, bool srgb, const Choice& c, cudaStream_t s) {
+    return srgb ? launch_store<DIM, ALPHA, NORMAL, true>(p, c, s)
+                : launch_store<DIM, ALPHA, NORMAL, false>(p, c, s);
 }
 template <int DIM, bool ALPHA>
-cudaError_t launch_norm(const Launch& p, bool normal, bool srgb, cudaStream_t s) {
-    return normal ? launch_srgb<DIM, ALPHA, true>(p, srgb, s) : launch_srgb<DIM, ALPHA, false>(p, srgb, s);
+cudaError_t launch_norm(const Launch& p, bool normal, bool srgb, const Choice& c, cudaStream_t s) {
+    return normal ? launch_srgb<DIM, ALPHA, true>(p, srgb, c, s)
+                  : launch_srgb<DIM, ALPHA, false>(p, srgb, c, s);
 }
 template <int DIM>
-cudaError_t launch_alpha(const Launch& p, bool alpha, bool normal, bool srgb, cudaStream_t s) {
-    return alpha ? launch_norm<DIM, true>(p, normal, srgb, s) : launch_norm<DIM, false>(p, normal, srgb, s);
+cudaError_t launch_alpha(const Launch& p, bool alpha, bool normal, bool srgb, const Choice& c,
+                         cudaStream_t s) {
+    return alpha ? launch_norm<DIM, true>(p, normal, srgb, c, s)
+                 : launch_norm<DIM, false>(p, normal, srgb, c, s);
+}
+
+Choice current_choice(int dim, bool alpha, bool normal, bool srgb) {
+    std::lock_guard<std::mutex> lk(g_choice_mu);
+    if (!g_choice_init) {
+        for (int d = 0; d < 2; ++d)
+            for (int a = 0; a < 2; ++a)
+                for (int n = 0; n < 2; ++n)
+                    for (int r = 0; r < 2; ++r)
+                        g_choice[d][a][n][r] = default_choice(d ? 6 : 4, a, n, r);
+        g_choice_init = true;
+    }
+    return g_choice[dim == 6][alpha][normal][srgb];
 }
 
 }  // namespace
@@ -376,24 +296,50 @@ cudaError_t ensure_encode_constants(int device) {
     return cudaMemcpyToSymbol(c_srgb_x255, lut, sizeof(lut));
 }
 
-cudaError_t launch_encode(const EncodeJob& j, cudaStream_t stream) {
-    Launch p;
-    p.in = j.in;
-    p.pitch = j.pitch;
-    p.width = j.width;
-    p.height = j.height;
-    p.nbx = blocks_x(j.width, j.block_dim);
-    p.nblocks = (long long)p.nbx * blocks_y(j.height, j.block_dim);
-    p.out = reinterpret_cast<uint4*>(j.out);
+TextureView make_view(const EncodeJob& j) {
+    TextureView t;
+    t.in = j.in;
+    t.pitch = j.pitch;
+    t.width = j.width;
+    t.height = j.height;
+    t.nbx = blocks_x(j.width, j.block_dim);
     const uintptr_t base = reinterpret_cast<uintptr_t>(j.in);
     const size_t va = j.block_dim == 4 ? 16 : 8;
-    p.vec_ok = (base % va == 0) && (j.pitch % va == 0);
-    p.clamp = j.border == ASTC_BORDER_CLAMP;
+    t.vec_ok = (base % va == 0) && (j.pitch % va == 0);
+    t.clamp = j.border == ASTC_BORDER_CLAMP;
+    return t;
+}
+
+cudaError_t launch_encode_variant(const EncodeJob& j, int store, int threads, cudaStream_t stream) {
+    if (threads != 32 && threads != 64 && threads != 128 && threads != 256) return cudaErrorInvalidValue;
+    if (store != kStoreRegisters && store != kStoreShared) return cudaErrorInvalidValue;
+    Launch p;
+    p.tex = make_view(j);
+    p.nblocks = (long long)p.tex.nbx * blocks_y(j.height, j.block_dim);
+    p.out = reinterpret_cast<uint4*>(j.out);
     const bool alpha = j.has_alpha != 0, normal = j.is_normal != 0, srgb = j.srgb != 0;
-    cudaError_t e = j.block_dim == 4 ? launch_alpha<4>(p, alpha, normal, srgb, stream)
-                                     : launch_alpha<6>(p, alpha, normal, srgb, stream);
+    const Choice c{store, threads};
+    cudaError_t e = j.block_dim == 4 ? launch_alpha<4>(p, alpha, normal, srgb, c, stream)
+                                     : launch_alpha<6>(p, alpha, normal, srgb, c, stream);
     if (e == cudaSuccess) count_launches(1);
     return e;
+}
+
+cudaError_t launch_encode(const EncodeJob& j, cudaStream_t stream) {
+    const Choice c = current_choice(j.block_dim, j.has_alpha != 0, j.is_normal != 0, j.srgb != 0);
+    return launch_encode_variant(j, c.store, c.threads, stream);
+}
+
+void set_encode_choice(int dim, bool alpha, bool normal, bool srgb, int store, int threads) {
+    current_choice(dim, alpha, normal, srgb);
+    std::lock_guard<std::mutex> lk(g_choice_mu);
+    g_choice[dim == 6][alpha][normal][srgb] = Choice{store, threads};
+}
+
+void get_encode_choice(int dim, bool alpha, bool normal, bool srgb, int* store, int* threads) {
+    const Choice c = current_choice(dim, alpha, normal, srgb);
+    *store = c.store;
+    *threads = c.threads;
 }
 
 }  // namespace astc

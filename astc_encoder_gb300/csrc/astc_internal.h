@@ -25,6 +25,12 @@ inline int blocks_y(int h, int dim) { return (h + dim - 1) / dim; }
 
 // Kernel launchers (astc_encode.cu).  Return cudaSuccess or the launch error.
 cudaError_t launch_encode(const EncodeJob& job, cudaStream_t stream);
+// One explicit kernel variant: store 0 = texels in registers, 1 = in shared
+// memory; threads per CTA 32/64/128/256.
+cudaError_t launch_encode_variant(const EncodeJob& job, int store, int threads, cudaStream_t stream);
+// The variant launch_encode uses for a format (process-wide; set by the autotuner).
+void set_encode_choice(int dim, bool alpha, bool normal, bool srgb, int store, int threads);
+void get_encode_choice(int dim, bool alpha, bool normal, bool srgb, int* store, int* threads);
 cudaError_t ensure_encode_constants(int device);
 
 // Decoder / SSE launchers (astc_decode.cu).

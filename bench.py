@@ -7,8 +7,9 @@ distinct 2048x2048 textures (268 MB of input, larger than the 129 MB L2, so
 no step reads its inputs from L2), each through the C ABI
 (astc_encode_gpu_pitched, device memory, on torch's current stream).
 
-* value      -- Mtexels/s with inputs resident in HBM, timed with CUDA events
-                around every launch on the launching stream (max over ranks).
+* value      -- Mtexels/s with inputs resident in HBM, timed with one CUDA
+                event pair around each step on the launching stream (a dedicated
+                non-default torch stream passed to the C ABI; max over ranks).
 * e2e        -- the same metric through the same entry point with pinned
                 HOST buffers: each texture's host->device copy, the encode and
                 the device->host copy of its blocks are inside the timed region.
@@ -236,6 +237,9 @@ def _time_launches(torch, native, texs, outs, spec, steps):
     mean launch duration."""
     h, w = texs[0].shape[:2]
     stream = torch.cuda.current_stream()
+    if stream.cuda_stream == 0:
+        # a NULL stream means "synchronous on the library's own stream" in the C ABI
+        raise RuntimeError("run the timed loop on a non-default stream")
     lib = native.load_library()
     opts = ctypes.byref(native.make_opts(memory=native.Memory.DEVICE, stream=stream.cuda_stream,
                                          **spec))
@@ -268,11 +272,16 @@ def run_ours(args) -> None:
     from astc_encoder_gb300 import build, synth
     build.build()
     native.load_library()
+    # every launch and event goes to one dedicated (non-default) stream
+    work_stream = torch.cuda.Stream()
+    torch.cuda.set_stream(work_stream)
 
     img, spec = synth.workload(args.workload)
     h, w = img.shape[:2]
     dim = spec["block_dim"]
     nblocks = ((w + dim - 1) // dim) * ((h + dim - 1) // dim)
+    # the autotuner picks the kernel variant (texel store, CTA size) for this format
+    tuned = native.autotune(dim, spec["has_alpha"], spec["is_normal"], spec["srgb"], w, h)
     texs = _texture_batch(torch, img, 2 if args.profile_case else TEXTURES_PER_STEP, salt=rank)
     outs = [torch.empty((nblocks, 16), dtype=torch.uint8, device="cuda") for _ in texs]
 
@@ -407,7 +416,10 @@ def run_ours(args) -> None:
                    "border": "clamp" if spec["border"] else "zero", "precision": "fp32",
                    "l2": f"inputs {texels_step * 4 / 2**20:.0f} MiB per step, distinct per texture "
                          "(> 129 MB L2); no flush needed",
-                   "parallelism": f"replicas{world}"},
+                   "parallelism": f"replicas{world}",
+                   "kernel_variant": {"store": "shared" if tuned.store else "registers",
+                                      "threads_per_cta": tuned.threads,
+                                      "autotune_best_us": tuned.best_us}},
         "e2e": {"value": e2e_value, "unit": "Mtexels/s",
                 "h2d_bytes_per_step": texels_step * 4, "d2h_bytes_per_step": nblocks * 16 * len(texs),
                 "entry_point": "astc_encode_gpu (ASTC_MEMORY_HOST, pinned buffers)",

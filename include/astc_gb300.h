@@ -75,7 +75,9 @@ typedef struct astc_opts {
     int memory;      /* astc_memory: where `rgba8` and `out` live          */
     void* stream;    /* cudaStream_t to run on asynchronously; NULL = the
                         library's own stream, and the call returns when
-                        the result is in `out`                              */
+                        the result is in `out` (for asynchronous work on
+                        the legacy default stream pass cudaStreamLegacy,
+                        (void*)0x1, not NULL)                               */
 } astc_opts;
 
 /* Fills the reference defaults: 4x4, no alpha, not a normal map, linear,
@@ -126,6 +128,28 @@ astc_status astc_decode_gpu(const uint8_t* blocks, int width, int height,
  * reference.) */
 astc_status astc_sse_gpu(const uint8_t* a, const uint8_t* b, size_t texels,
                          int memory, void* stream, uint64_t sse_rgba[4]);
+
+/* Kernel variant of a format: where a block's decoded texels live
+ * (store 0 = registers, 1 = shared memory) and the CTA size (32/64/128/256).
+ * Every variant produces identical blocks; they differ in speed only.
+ * (No counterpart in the reference, whose shader has one fixed mapping,
+ * [numthreads(8,8,1)] at ASTC_Encode.hlsl:553.) */
+typedef struct astc_tune_result {
+    int store;
+    int threads;
+    float best_us;      /* fastest variant, microseconds per launch       */
+    float default_us;   /* the variant that was installed before tuning   */
+} astc_tune_result;
+
+/* Time every variant for a format on a synthetic width x height texture on
+ * the current device and install the fastest for that format in this
+ * process (it allocates its own test buffers). */
+astc_status astc_autotune(int block_dim, int has_alpha, int is_normal, int srgb,
+                          int width, int height, astc_tune_result* result);
+astc_status astc_set_kernel_choice(int block_dim, int has_alpha, int is_normal, int srgb,
+                                   int store, int threads);
+astc_status astc_get_kernel_choice(int block_dim, int has_alpha, int is_normal, int srgb,
+                                   int* store, int* threads);
 
 /* astc_sse_gpu for callers that may not allocate device memory (no
  * counterpart in the reference).  Some hosts own the whole device-memory

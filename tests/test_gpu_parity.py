@@ -173,3 +173,33 @@ def test_launch_counter_moves(native):
     before = native.kernel_launch_count()
     native.encode(np.zeros((8, 8, 4), np.uint8))
     assert native.kernel_launch_count() == before + 1
+
+
+@pytest.mark.parametrize("dim,alpha,normal,srgb", [(4, False, False, False), (4, True, False, True),
+                                                   (6, True, False, True), (6, False, True, False)])
+def test_every_kernel_variant_bit_exact(native, oracle, dim, alpha, normal, srgb):
+    img = _texture(97, 61, seed=dim * 5 + alpha + srgb)
+    opts = dict(block_dim=dim, has_alpha=alpha, is_normal=normal, srgb=srgb, border=1)
+    want = oracle.encode(img, **opts)
+    saved = native.get_kernel_choice(dim, alpha, normal, srgb)
+    try:
+        for store in (0, 1):
+            for threads in (32, 64, 128, 256):
+                native.set_kernel_choice(dim, alpha, normal, srgb, store, threads)
+                assert np.array_equal(native.encode(img, **opts), want), (store, threads)
+    finally:
+        native.set_kernel_choice(dim, alpha, normal, srgb, *saved)
+
+
+def test_autotune_installs_a_valid_choice(native, oracle):
+    saved = native.get_kernel_choice(6, True, False, True)
+    try:
+        r = native.autotune(6, True, False, True, 512, 384)
+        assert r.store in (0, 1) and r.threads in (64, 128, 256)
+        assert 0 < r.best_us <= r.default_us
+        assert native.get_kernel_choice(6, True, False, True) == (r.store, r.threads)
+        img = _texture(130, 70, seed=77)
+        opts = dict(block_dim=6, has_alpha=True, srgb=True, border=1)
+        assert np.array_equal(native.encode(img, **opts), oracle.encode(img, **opts))
+    finally:
+        native.set_kernel_choice(6, True, False, True, *saved)
