@@ -150,8 +150,93 @@ def load_library() -> ctypes.CDLL:
     lib.astc_set_kernel_choice.restype = ctypes.c_int
     lib.astc_get_kernel_choice.argtypes = [ctypes.c_int] * 4 + [ip, ip]
     lib.astc_get_kernel_choice.restype = ctypes.c_int
+    lib.astc_batch_create.argtypes = [ctypes.c_int, ctypes.c_longlong, ctypes.POINTER(ctypes.c_void_p)]
+    lib.astc_batch_create.restype = ctypes.c_int
+    lib.astc_batch_encode.argtypes = [ctypes.c_void_p, ctypes.POINTER(BatchItem), ctypes.c_int,
+                                      ctypes.c_int, ctypes.c_void_p]
+    lib.astc_batch_encode.restype = ctypes.c_int
+    lib.astc_batch_destroy.argtypes = [ctypes.c_void_p]
+    lib.astc_batch_destroy.restype = ctypes.c_int
+    lib.astc_mip_levels.argtypes = [ctypes.c_int, ctypes.c_int]
+    lib.astc_mip_levels.restype = ctypes.c_int
+    lib.astc_mip_chain_bytes.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    lib.astc_mip_chain_bytes.restype = ctypes.c_size_t
+    lib.astc_generate_mips.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                       ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+    lib.astc_generate_mips.restype = ctypes.c_int
     _LIB = lib
     return lib
+
+
+class BatchItem(ctypes.Structure):
+    """``astc_batch_item`` of include/astc_gb300.h."""
+    _fields_ = [("rgba8", ctypes.c_void_p), ("row_pitch", ctypes.c_size_t), ("width", ctypes.c_int),
+                ("height", ctypes.c_int), ("block_dim", ctypes.c_int), ("has_alpha", ctypes.c_int),
+                ("is_normal", ctypes.c_int), ("srgb", ctypes.c_int), ("border", ctypes.c_int),
+                ("out", ctypes.c_void_p)]
+
+
+class Batch:
+    """Batched encoder handle (astc_batch_*): one graph launch for many textures.
+
+    ``items`` are dicts or tuples (rgba8_ptr, width, height, out_ptr, options...)
+    of device pointers; see :meth:`encode`."""
+
+    def __init__(self, max_textures: int, max_blocks: int):
+        self._lib = load_library()
+        h = ctypes.c_void_p()
+        _check(self._lib.astc_batch_create(max_textures, max_blocks, ctypes.byref(h)))
+        self._h = h
+
+    def encode(self, items: list[dict], precision: int = Precision.FP32, stream: int | None = None) -> None:
+        arr = (BatchItem * max(1, len(items)))()
+        for i, it in enumerate(items):
+            arr[i] = BatchItem(it["rgba8"], it.get("row_pitch", 0), it["width"], it["height"],
+                               it.get("block_dim", 4), int(it.get("has_alpha", False)),
+                               int(it.get("is_normal", False)), int(it.get("srgb", False)),
+                               int(it.get("border", Border.ZERO)), it["out"])
+        _check(self._lib.astc_batch_encode(self._h, arr, len(items), int(precision), stream or None))
+
+    def close(self) -> None:
+        if self._h:
+            self._lib.astc_batch_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:  # noqa: BLE001
+            pass
+
+
+def mip_levels(width: int, height: int) -> int:
+    return int(load_library().astc_mip_levels(width, height))
+
+
+def mip_chain_bytes(width: int, height: int, levels: int) -> int:
+    return int(load_library().astc_mip_chain_bytes(width, height, levels))
+
+
+def mip_sizes(width: int, height: int, levels: int) -> list[tuple[int, int]]:
+    """Sizes of levels 0..levels-1 (level l+1 = max(1, w/2) x max(1, h/2))."""
+    out = [(width, height)]
+    for _ in range(1, levels):
+        width, height = max(1, width // 2), max(1, height // 2)
+        out.append((width, height))
+    return out
+
+
+def generate_mips(rgba_ptr: int, width: int, height: int, levels: int, out_ptr: int, srgb: bool = False,
+                  stream: int | None = None) -> None:
+    """Box-filtered levels 1..levels-1 of a device RGBA8 image into `out_ptr`."""
+    _check(load_library().astc_generate_mips(rgba_ptr, width, height, levels, int(srgb), out_ptr,
+                                             stream or None))
 
 
 class TuneResult(ctypes.Structure):

@@ -33,6 +33,9 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-Wall",
 # compiler contracts nothing: every fused multiply-add is written explicitly.
 LIB_SOURCES = [
     ("astc_encode.cu", ["--fmad=false"]),
+    ("astc_encode_h2.cu", ["--fmad=false"]),
+    ("astc_batch.cu", ["--fmad=false"]),
+    ("astc_mips.cu", []),
     ("astc_decode.cu", []),
     ("astc_capi.cu", []),
     ("astc_noalloc.cu", []),
@@ -42,7 +45,8 @@ CLI_SOURCES = [
     ("astc_cs_enc.cpp", []),
     ("image_load.cpp", []),
 ]
-HEADERS = ["astc_internal.h", "astc_tables.h", "astc_block_common.cuh", "image_load.h"]
+HEADERS = ["astc_internal.h", "astc_tables.h", "astc_block_common.cuh", "astc_pipeline_fp32.cuh",
+           "astc_pipeline_h2.cuh", "astc_srgb_table.h", "image_load.h"]
 
 
 def nvcc() -> str:

@@ -1,0 +1,378 @@
+// astc_batch.cu -- batched encode: one CUDA-graph launch encodes a whole
+// list of textures (different sizes, mip levels and formats).
+//
+// The reference dispatches one texture per call (astc_encode.h:87-194,
+// Dispatch at 190); small textures and mip levels then cost a launch each and
+// leave most of the GPU idle.  Here the host splits every texture into work
+// items of up to 128 blocks, groups the items by format, and uploads the
+// texture descriptors and items in one copy; one persistent kernel per format
+// present (16 formats: 4x4/6x6 x alpha x normal x sRGB, per precision) drains
+// its format's queue: a CTA takes the next item with one atomicAdd on a
+// device counter and encodes its blocks, one thread per block, exactly as the
+// plain kernels do (so a texture's blocks are the same whether it is encoded
+// alone or in a batch).  The descriptor copy and the kernels are captured
+// once per (precision, set of formats) into a CUDA graph and replayed; batch
+// sizes and contents are read from device memory at run time, so one graph
+// serves every batch that fits the handle.
+//
+// No kernel here waits on another CTA or kernel: the only synchronisation is
+// the atomicAdd that hands out items.
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string.h>
+
+#include <map>
+#include <mutex>
+#include <new>
+#include <string>
+#include <unordered_set>
+#include <vector>
+
+#include "astc_internal.h"
+#include "astc_pipeline_fp32.cuh"
+#include "astc_pipeline_h2.cuh"
+
+namespace astc {
+namespace {
+
+constexpr int kBatchThreads = 128;      // blocks per work item = threads per CTA
+constexpr int kFormats = 16;
+
+__constant__ TritPack c_trit_pack_b = make_trit_pack();
+__constant__ SrgbBits c_srgb_bits_b = make_srgb_bits();
+
+struct BatchJob {
+    TextureView tex;
+    uint4* out;
+};
+
+struct WorkItem {
+    int job;
+    int first;
+    int count;
+    int pad;
+};
+
+struct QueueState {
+    int counter[kFormats];
+    int begin[kFormats];
+    int end[kFormats];
+    int pad[kFormats];
+};
+
+inline int format_index(int dim, bool alpha, bool normal, bool srgb) {
+    return (dim == 6 ? 8 : 0) | (alpha ? 4 : 0) | (normal ? 2 : 0) | (srgb ? 1 : 0);
+}
+
+template <int DIM, bool ALPHA, bool NORMAL, bool SRGB, int PREC>
+__global__ void __launch_bounds__(kBatchThreads, (PREC == ASTC_PRECISION_FP32 && DIM == 4) ? 4 : 1)
+astc_encode_persistent(const BatchJob* __restrict__ jobs, const WorkItem* __restrict__ items,
+                       QueueState* __restrict__ q, int fmt) {
+    constexpr int N = DIM * DIM;
+    extern __shared__ float4 s_texels[];            // FP32 4x4 keeps texels in shared memory
+    __shared__ uint8_t s_trits[256];
+    __shared__ float s_lut[SRGB ? 256 : 1];
+    __shared__ int s_item;
+    load_cta_tables<SRGB>(c_trit_pack_b, c_srgb_bits_b, s_trits, s_lut);
+    const int end = q->end[fmt];
+    const int begin = q->begin[fmt];
+    for (;;) {
+        if (threadIdx.x == 0) s_item = begin + atomicAdd(&q->counter[fmt], 1);
+        __syncthreads();
+        const int it = s_item;
+        __syncthreads();
+        if (it >= end) break;
+        const WorkItem w = items[it];
+        if ((int)threadIdx.x < w.count) {
+            const BatchJob j = jobs[w.job];
+            const int b = w.first + threadIdx.x;
+            const int by = b / j.tex.nbx;
+            const int bx = b - by * j.tex.nbx;
+            uint32_t px[N];
+            load_block_packed<DIM>(j.tex, bx, by, px);
+            uint4 r;
+            if constexpr (PREC == ASTC_PRECISION_HALF2) {
+                r = encode_block_h2<DIM, ALPHA, NORMAL, SRGB>(px, s_lut, s_trits);
+            } else if constexpr (DIM == 4) {
+                SharedTexels<N> st{s_texels + threadIdx.x, kBatchThreads};
+#pragma unroll
+                for (int k = 0; k < N; ++k) st.put(k, decode_texel<SRGB, NORMAL>(px[k], s_lut));
+                r = encode_block_fp32<DIM, ALPHA>(st, s_trits);
+            } else {
+                RegTexels<N> st;
+#pragma unroll
+                for (int k = 0; k < N; ++k) st.put(k, decode_texel<SRGB, NORMAL>(px[k], s_lut));
+                r = encode_block_fp32<DIM, ALPHA>(st, s_trits);
+            }
+            j.out[b] = r;
+        }
+    }
+}
+
+using KernelFn = void (*)(const BatchJob*, const WorkItem*, QueueState*, int);
+
+template <int PREC>
+KernelFn kernel_for(int f) {
+    switch (f) {
+#define ASTC_K(F, D, A, NM, S) case F: return astc_encode_persistent<D, A, NM, S, PREC>;
+        ASTC_K(0, 4, false, false, false) ASTC_K(1, 4, false, false, true)
+        ASTC_K(2, 4, false, true, false)  ASTC_K(3, 4, false, true, true)
+        ASTC_K(4, 4, true, false, false)  ASTC_K(5, 4, true, false, true)
+        ASTC_K(6, 4, true, true, false)   ASTC_K(7, 4, true, true, true)
+        ASTC_K(8, 6, false, false, false) ASTC_K(9, 6, false, false, true)
+        ASTC_K(10, 6, false, true, false) ASTC_K(11, 6, false, true, true)
+        ASTC_K(12, 6, true, false, false) ASTC_K(13, 6, true, false, true)
+        ASTC_K(14, 6, true, true, false)  ASTC_K(15, 6, true, true, true)
+#undef ASTC_K
+    }
+    return nullptr;
+}
+
+size_t dyn_smem(int f, int prec) {
+    return (prec == ASTC_PRECISION_FP32 && f < 8) ? (size_t)16 * kBatchThreads * sizeof(float4) : 0;
+}
+
+}  // namespace
+}  // namespace astc
+
+using namespace astc;
+
+struct astc_batch {
+    std::mutex mu;
+    int device = 0;
+    int max_items = 0;
+    long long max_blocks = 0;
+    int max_work = 0;
+    int sms = 0;
+    // device: [QueueState][BatchJob x max_items][WorkItem x max_work]
+    uint8_t* d_buf = nullptr;
+    uint8_t* h_buf = nullptr;       // pinned staging of the same layout
+    size_t buf_bytes = 0;
+    cudaStream_t capture_stream = nullptr;
+    cudaEvent_t done = nullptr;
+    bool pending = false;
+    std::map<unsigned, cudaGraphExec_t> graphs;   // key: precision << 16 | format mask
+    std::unordered_set<uintptr_t> validated;      // device pointers already checked
+};
+
+namespace {
+
+size_t jobs_offset() { return (sizeof(QueueState) + 255) & ~(size_t)255; }
+size_t items_offset(int max_items) {
+    return (jobs_offset() + (size_t)max_items * sizeof(BatchJob) + 255) & ~(size_t)255;
+}
+
+astc_status check_ptr(astc_batch* b, const void* p, const char* what) {
+    const uintptr_t key = reinterpret_cast<uintptr_t>(p);
+    if (b->validated.count(key)) return ASTC_OK;
+    cudaPointerAttributes a;
+    const cudaError_t e = cudaPointerGetAttributes(&a, p);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return set_error(ASTC_ERR_INVALID_ARG, std::string(what) + " is not a CUDA pointer");
+    }
+    if (a.type != cudaMemoryTypeDevice && a.type != cudaMemoryTypeManaged)
+        return set_error(ASTC_ERR_INVALID_ARG, std::string(what) + " is not device memory");
+    if (b->validated.size() > 65536) b->validated.clear();
+    b->validated.insert(key);
+    return ASTC_OK;
+}
+
+// Captures [descriptor upload -> one persistent kernel per format in `mask`].
+astc_status build_graph(astc_batch* b, unsigned mask, int prec, cudaGraphExec_t* out) {
+    cudaStream_t s = b->capture_stream;
+    cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return cuda_error(e, "cudaStreamBeginCapture");
+    auto* q = reinterpret_cast<QueueState*>(b->d_buf);
+    auto* jobs = reinterpret_cast<BatchJob*>(b->d_buf + jobs_offset());
+    auto* items = reinterpret_cast<WorkItem*>(b->d_buf + items_offset(b->max_items));
+    e = cudaMemcpyAsync(b->d_buf, b->h_buf, b->buf_bytes, cudaMemcpyHostToDevice, s);
+    for (int f = 0; f < kFormats && e == cudaSuccess; ++f) {
+        if (!(mask & (1u << f))) continue;
+        KernelFn k = prec == ASTC_PRECISION_HALF2 ? kernel_for<ASTC_PRECISION_HALF2>(f)
+                                                  : kernel_for<ASTC_PRECISION_FP32>(f);
+        const size_t smem = dyn_smem(f, prec);
+        int occ = 0;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, kBatchThreads, smem);
+        if (e != cudaSuccess) break;
+        const int grid = (occ > 0 ? occ : 1) * b->sms;
+        k<<<grid, kBatchThreads, smem, s>>>(jobs, items, q, f);
+        e = cudaGetLastError();
+    }
+    cudaGraph_t g = nullptr;
+    const cudaError_t e2 = cudaStreamEndCapture(s, &g);
+    if (e != cudaSuccess || e2 != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        return cuda_error(e != cudaSuccess ? e : e2, "batch graph capture");
+    }
+    e = cudaGraphInstantiate(out, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return cuda_error(e, "cudaGraphInstantiate");
+    return ASTC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+astc_status astc_batch_create(int max_textures, long long max_blocks, astc_batch** out) {
+    if (!out) return set_error(ASTC_ERR_INVALID_ARG, "out is NULL");
+    *out = nullptr;
+    if (max_textures <= 0 || max_blocks <= 0 || max_blocks > (1LL << 36))
+        return set_error(ASTC_ERR_INVALID_ARG, "max_textures and max_blocks must be positive");
+    const long long work = max_blocks / kBatchThreads + max_textures + 1;
+    if (work > (1LL << 30)) return set_error(ASTC_ERR_INVALID_ARG, "batch too large");
+    astc_batch* b = new (std::nothrow) astc_batch();
+    if (!b) return set_error(ASTC_ERR_OUT_OF_MEMORY, "host allocation failed");
+    b->max_items = max_textures;
+    b->max_blocks = max_blocks;
+    b->max_work = (int)work;
+    b->buf_bytes = items_offset(max_textures) + (size_t)b->max_work * sizeof(WorkItem);
+    cudaError_t e = cudaGetDevice(&b->device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, b->device);
+    if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&b->d_buf), b->buf_bytes);
+    if (e == cudaSuccess) e = cudaMallocHost(reinterpret_cast<void**>(&b->h_buf), b->buf_bytes);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->capture_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+        const astc_status st = cuda_error(e, "batch allocation");
+        astc_batch_destroy(b);
+        return st;
+    }
+    memset(b->h_buf, 0, b->buf_bytes);
+    *out = b;
+    return ASTC_OK;
+}
+
+astc_status astc_batch_encode(astc_batch* b, const astc_batch_item* in, int count, int precision,
+                              void* stream) {
+    if (!b || (!in && count > 0)) return set_error(ASTC_ERR_INVALID_ARG, "NULL argument");
+    if (count < 0 || count > b->max_items)
+        return set_error(ASTC_ERR_INVALID_ARG, "count exceeds the batch's max_textures");
+    if (precision != ASTC_PRECISION_FP32 && precision != ASTC_PRECISION_HALF2)
+        return set_error(ASTC_ERR_INVALID_ARG, "precision must be FP32 or HALF2");
+    try {
+        std::lock_guard<std::mutex> lk(b->mu);
+        int dev = 0;
+        cudaError_t e = cudaGetDevice(&dev);
+        if (e != cudaSuccess) return cuda_error(e, "cudaGetDevice");
+        if (dev != b->device) return set_error(ASTC_ERR_INVALID_ARG, "batch was created on another device");
+        // plan: validate, count work items per format
+        long long blocks = 0;
+        int per_fmt[kFormats] = {};
+        for (int i = 0; i < count; ++i) {
+            const astc_batch_item& t = in[i];
+            if (t.block_dim != 4 && t.block_dim != 6)
+                return set_error(ASTC_ERR_INVALID_ARG, "item " + std::to_string(i) + ": block_dim must be 4 or 6");
+            if (t.width <= 0 || t.height <= 0 || t.width > 0xFFFFFF || t.height > 0xFFFFFF)
+                return set_error(ASTC_ERR_INVALID_ARG, "item " + std::to_string(i) + ": bad size");
+            if (t.border != ASTC_BORDER_ZERO && t.border != ASTC_BORDER_CLAMP)
+                return set_error(ASTC_ERR_INVALID_ARG, "item " + std::to_string(i) + ": bad border");
+            const size_t pitch = t.row_pitch ? t.row_pitch : (size_t)t.width * 4;
+            if (pitch < (size_t)t.width * 4 || pitch % 4)
+                return set_error(ASTC_ERR_INVALID_ARG, "item " + std::to_string(i) + ": bad row_pitch");
+            if (!t.rgba8 || !t.out || reinterpret_cast<uintptr_t>(t.rgba8) % 4 ||
+                reinterpret_cast<uintptr_t>(t.out) % 16)
+                return set_error(ASTC_ERR_INVALID_ARG,
+                                 "item " + std::to_string(i) + ": rgba8 must be 4-byte and out 16-byte aligned");
+            astc_status st;
+            if ((st = check_ptr(b, t.rgba8, "rgba8")) != ASTC_OK) return st;
+            if ((st = check_ptr(b, t.out, "out")) != ASTC_OK) return st;
+            const long long nb = (long long)blocks_x(t.width, t.block_dim) * blocks_y(t.height, t.block_dim);
+            if (nb > (1LL << 31)) return set_error(ASTC_ERR_INVALID_ARG, "texture has more than 2^31 blocks");
+            blocks += nb;
+            per_fmt[format_index(t.block_dim, t.has_alpha, t.is_normal, t.srgb)] +=
+                (int)((nb + kBatchThreads - 1) / kBatchThreads);
+        }
+        if (blocks > b->max_blocks) return set_error(ASTC_ERR_INVALID_ARG, "batch exceeds max_blocks");
+        // the previous batch's upload must have left the pinned staging buffer
+        if (b->pending) {
+            if ((e = cudaEventSynchronize(b->done)) != cudaSuccess) return cuda_error(e, "previous batch");
+            b->pending = false;
+        }
+        auto* q = reinterpret_cast<QueueState*>(b->h_buf);
+        auto* jobs = reinterpret_cast<BatchJob*>(b->h_buf + jobs_offset());
+        auto* items = reinterpret_cast<WorkItem*>(b->h_buf + items_offset(b->max_items));
+        unsigned mask = 0;
+        int cursor[kFormats];
+        int total = 0;
+        for (int f = 0; f < kFormats; ++f) {
+            q->counter[f] = 0;
+            q->begin[f] = total;
+            cursor[f] = total;
+            total += per_fmt[f];
+            q->end[f] = total;
+            if (per_fmt[f]) mask |= 1u << f;
+        }
+        for (int i = 0; i < count; ++i) {
+            const astc_batch_item& t = in[i];
+            EncodeJob j;
+            j.in = t.rgba8;
+            j.pitch = t.row_pitch ? t.row_pitch : (size_t)t.width * 4;
+            j.width = t.width;
+            j.height = t.height;
+            j.block_dim = t.block_dim;
+            j.has_alpha = t.has_alpha;
+            j.is_normal = t.is_normal;
+            j.srgb = t.srgb;
+            j.border = t.border;
+            j.precision = precision;
+            j.out = t.out;
+            jobs[i].tex = make_view(j);
+            jobs[i].out = reinterpret_cast<uint4*>(t.out);
+            const int nb = blocks_x(t.width, t.block_dim) * blocks_y(t.height, t.block_dim);
+            int& c = cursor[format_index(t.block_dim, t.has_alpha, t.is_normal, t.srgb)];
+            for (int first = 0; first < nb; first += kBatchThreads) {
+                items[c].job = i;
+                items[c].first = first;
+                items[c].count = nb - first < kBatchThreads ? nb - first : kBatchThreads;
+                items[c].pad = 0;
+                ++c;
+            }
+        }
+        if (!mask) return ASTC_OK;
+        const unsigned key = ((unsigned)precision << 16) | mask;
+        auto it = b->graphs.find(key);
+        if (it == b->graphs.end()) {
+            cudaGraphExec_t g = nullptr;
+            astc_status st = build_graph(b, mask, precision, &g);
+            if (st != ASTC_OK) return st;
+            it = b->graphs.emplace(key, g).first;
+        }
+        cudaStream_t s = static_cast<cudaStream_t>(stream);
+        if ((e = cudaGraphLaunch(it->second, s)) != cudaSuccess) return cuda_error(e, "cudaGraphLaunch");
+        if ((e = cudaEventRecord(b->done, s)) != cudaSuccess) return cuda_error(e, "cudaEventRecord");
+        b->pending = true;
+        int kernels = 0;
+        for (int f = 0; f < kFormats; ++f) kernels += (mask >> f) & 1;
+        count_launches((uint64_t)kernels);
+        if (!stream) {
+            if ((e = cudaEventSynchronize(b->done)) != cudaSuccess) return cuda_error(e, "batch encode");
+            b->pending = false;
+        }
+        return ASTC_OK;
+    } catch (const std::bad_alloc&) {
+        return set_error(ASTC_ERR_OUT_OF_MEMORY, "host allocation failed");
+    } catch (...) {
+        return set_error(ASTC_ERR_CUDA, "unexpected exception");
+    }
+}
+
+astc_status astc_batch_destroy(astc_batch* b) {
+    if (!b) return ASTC_OK;
+    int cur = 0;
+    const bool have = cudaGetDevice(&cur) == cudaSuccess;
+    cudaSetDevice(b->device);
+    if (b->pending && b->done) cudaEventSynchronize(b->done);
+    for (auto& kv : b->graphs) cudaGraphExecDestroy(kv.second);
+    if (b->done) cudaEventDestroy(b->done);
+    if (b->capture_stream) cudaStreamDestroy(b->capture_stream);
+    if (b->d_buf) cudaFree(b->d_buf);
+    if (b->h_buf) cudaFreeHost(b->h_buf);
+    if (have) cudaSetDevice(cur);
+    cudaGetLastError();
+    delete b;
+    return ASTC_OK;
+}
+
+}  // extern "C"

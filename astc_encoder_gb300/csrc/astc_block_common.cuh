@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "astc_srgb_table.h"
 #include "astc_tables.h"
 
 namespace astc {
@@ -166,6 +167,23 @@ constexpr TritPack make_trit_pack() {
     const IseTables t = make_ise_tables();
     for (int i = 0; i < 243; ++i) p.v[i] = t.trit_pack[i];
     return p;
+}
+
+struct SrgbBits { uint32_t v[256]; };
+constexpr SrgbBits make_srgb_bits() {
+    SrgbBits s{};
+    for (int i = 0; i < 256; ++i) s.v[i] = kSrgbX255Bits[i];
+    return s;
+}
+
+// Per-CTA copies of the constant tables (trit packing, sRGB texel values).
+template <bool SRGB>
+__device__ __forceinline__ void load_cta_tables(const TritPack& tp, const SrgbBits& sb, uint8_t* s_trits,
+                                                float* s_lut) {
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) {
+        s_trits[i] = tp.v[i];
+        if (SRGB) s_lut[i] = __uint_as_float(sb.v[i]);
+    }
 }
 
 // q0/q1: rounded endpoints (RGBA), qw: 16 quantised weights (0..R).

@@ -75,8 +75,7 @@ astc_status pool_init_locked(DevicePool& p, int dev) {
     if (p.ready) return ASTC_OK;
     cudaError_t e = cudaStreamCreateWithFlags(&p.stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) return cuda_error(e, "cudaStreamCreateWithFlags");
-    e = ensure_encode_constants(dev);
-    if (e != cudaSuccess) return cuda_error(e, "upload of the sRGB table");
+    (void)dev;
     p.ready = true;
     return ASTC_OK;
 }
@@ -155,8 +154,9 @@ astc_status astc_encode_gpu_pitched(const uint8_t* rgba8, int width, int height,
         if (!rgba8 || !out) return set_error(ASTC_ERR_INVALID_ARG, "rgba8 and out must be non-NULL");
         if (row_pitch < (size_t)width * 4 || row_pitch % 4 != 0)
             return set_error(ASTC_ERR_INVALID_ARG, "row_pitch must be >= 4*width and a multiple of 4");
-        if (opts->precision == ASTC_PRECISION_HALF2)
-            return set_error(ASTC_ERR_UNSUPPORTED, "HALF2 precision is not built in this library");
+        auto launch = [&](const EncodeJob& j, cudaStream_t st_) {
+            return opts->precision == ASTC_PRECISION_HALF2 ? launch_encode_h2(j, st_) : launch_encode(j, st_);
+        };
         DevicePool* pool = nullptr;
         int dev = 0;
         if ((st = pool_for_current(&pool, &dev)) != ASTC_OK) return st;
@@ -187,7 +187,7 @@ astc_status astc_encode_gpu_pitched(const uint8_t* rgba8, int width, int height,
             job.in = rgba8;
             job.pitch = row_pitch;
             job.out = out;
-            cudaError_t e = launch_encode(job, s);
+            cudaError_t e = launch(job, s);
             if (e != cudaSuccess) return cuda_error(e, "encode kernel launch");
             if (!opts->stream) {
                 e = cudaStreamSynchronize(s);
@@ -207,7 +207,7 @@ astc_status astc_encode_gpu_pitched(const uint8_t* rgba8, int width, int height,
         job.in = pool->d_in;
         job.pitch = tight;
         job.out = pool->d_out;
-        e = launch_encode(job, s);
+        e = launch(job, s);
         if (e != cudaSuccess) return cuda_error(e, "encode kernel launch");
         e = cudaMemcpyAsync(out, pool->d_out, out_bytes, cudaMemcpyDeviceToHost, s);
         if (e != cudaSuccess) return cuda_error(e, "device-to-host copy");

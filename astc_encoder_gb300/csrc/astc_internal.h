@@ -31,7 +31,10 @@ cudaError_t launch_encode_variant(const EncodeJob& job, int store, int threads, 
 // The variant launch_encode uses for a format (process-wide; set by the autotuner).
 void set_encode_choice(int dim, bool alpha, bool normal, bool srgb, int store, int threads);
 void get_encode_choice(int dim, bool alpha, bool normal, bool srgb, int* store, int* threads);
-cudaError_t ensure_encode_constants(int device);
+struct TextureView;
+TextureView make_view(const EncodeJob& job);
+// Packed-half2 pipeline (astc_encode_h2.cu).
+cudaError_t launch_encode_h2(const EncodeJob& job, cudaStream_t stream);
 
 // Decoder / SSE launchers (astc_decode.cu).
 cudaError_t launch_decode(const uint8_t* blocks, int width, int height, int bw, int bh,
@@ -43,9 +46,5 @@ cudaError_t launch_sse(const uint8_t* a, const uint8_t* b, size_t texels,
 astc_status set_error(astc_status st, const std::string& msg);
 astc_status cuda_error(cudaError_t e, const char* what);
 void count_launches(uint64_t n);
-
-// sRGB -> linear, the committed formula: IEC 61966-2-1 piecewise curve in
-// double, rounded once to float, then multiplied by 255 in float.
-float srgb_texel_value(int code);
 
 }  // namespace astc

@@ -100,6 +100,46 @@ astc_status astc_encode_gpu_pitched(const uint8_t* rgba8, int width, int height,
                                     size_t row_pitch, const astc_opts* opts,
                                     uint8_t* out);
 
+/* ---- batched encode (one CUDA-graph launch for many textures) -----------
+ * The reference encodes one texture per Dispatch (astc_encode.h:190).  A
+ * batch encodes any list of textures -- different sizes, mip levels and
+ * formats -- in one graph launch: the blocks are split into work items of
+ * 128 blocks, grouped by format, and persistent kernels drain the items from
+ * a device work queue.  Every texture's blocks are identical to what
+ * astc_encode_gpu returns for it with the same precision. */
+typedef struct astc_batch_item {
+    const uint8_t* rgba8;   /* device memory, 4-byte aligned                 */
+    size_t row_pitch;       /* bytes between rows; 0 = 4 * width             */
+    int width, height;
+    int block_dim, has_alpha, is_normal, srgb, border;   /* as astc_opts     */
+    uint8_t* out;           /* device memory, 16-byte aligned, 16 B / block  */
+} astc_batch_item;
+
+typedef struct astc_batch astc_batch;   /* opaque; owns descriptor buffers,
+                                           a pinned staging copy and the
+                                           captured graphs               */
+
+/* Capacity: up to max_textures items and max_blocks blocks per call. */
+astc_status astc_batch_create(int max_textures, long long max_blocks, astc_batch** out);
+/* Encode `count` items with `precision` on `stream` (asynchronous; NULL =
+ * the legacy default stream, and the call returns when the blocks are
+ * written).  A call waits for the previous call's descriptor upload before
+ * it reuses the staging buffer.  Not thread-safe per handle across streams. */
+astc_status astc_batch_encode(astc_batch* batch, const astc_batch_item* items, int count,
+                              int precision, void* stream);
+astc_status astc_batch_destroy(astc_batch* batch);
+
+/* ---- mip chains (staging in front of the batched encoder) --------------
+ * (No counterpart in the reference, which encodes one level: main.cpp:36.)
+ * Level l+1 is max(1, w/2) x max(1, h/2); each texel is the rounded mean of
+ * the 2x2 texels below it (edge-clamped for a width or height of 1); with
+ * `srgb` the RGB channels are averaged in linear light.  Levels 1..levels-1
+ * are written back to back into `out` (device memory, tight rows). */
+int astc_mip_levels(int width, int height);            /* full chain length   */
+size_t astc_mip_chain_bytes(int width, int height, int levels);
+astc_status astc_generate_mips(const uint8_t* rgba8, int width, int height, int levels,
+                               int srgb, uint8_t* out, void* stream);
+
 /* Write a .astc file: the 16-byte header of astc_save.h:5-14 (magic
  * 0x5CA1AB13, block dims, 24-bit x/y/z sizes, z = 1) then the blocks.
  * Replaces save_astc (astc_save.h:52-76), which did not check fopen. */
