@@ -126,7 +126,9 @@ def test_half2_quality_gate(native, oracle, name):
     f32 = native.encode(img, **spec)
     loss = _psnr(native, f64, img, spec) - _psnr(native, h2, img, spec)
     assert loss <= HALF2_MAX_LOSS_DB, loss
-    assert abs(_psnr(native, f64, img, spec) - _psnr(native, f32, img, spec)) < 0.01
+    # the FP32 kernel is the FP32 oracle bit for bit (its gap to the FP64 twin
+    # is reported by the bench, not gated: it can go either way)
+    assert _psnr(native, f32, img, spec) == _psnr(native, oracle.encode(img, **spec), img, spec)
     # most blocks still agree with the FP32 path bit for bit
     assert np.all(h2 == f32, axis=1).mean() > 0.5
 
