@@ -85,8 +85,6 @@ def _compile(src: str, extra: list[str], force: bool, verbose: bool) -> str:
     obj = os.path.join(BUILD, src + ".o")
     if force or _stale(obj, [path]):
         cmd = [nvcc(), *ARCH, *COMMON, *extra, "-c", path, "-o", obj]
-        if src.endswith(".cpp"):
-            cmd = [nvcc(), "-x", "cu", *ARCH, *COMMON, *extra, "-c", path, "-o", obj]
         _run(cmd, verbose)
     return obj
 

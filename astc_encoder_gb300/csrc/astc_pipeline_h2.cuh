@@ -12,10 +12,10 @@
 //   * power iteration, endpoint fit and rounding: FP32, with the hardware
 //     reciprocal square root for the normalisations;
 //   * per-texel projection (find_min_max) and weights: packed half2, two
-//     channels per instruction, on differences (texel - mean, texel - e0) so
-//     the values stay small and a rounding of the mean or of e0 only shifts
-//     every texel by the same amount, which the min/max normalisation
-//     removes; 0..255 texels are exact in FP16;
+//     channels per instruction, on differences (texel - mean, texel - the
+//     endpoints' midpoint) so the values stay small and a rounding of the
+//     reference point only shifts every texel by the same amount, which the
+//     min/max normalisation removes; 0..255 texels are exact in FP16;
 //   * weight quantisation: one half2 FMA plus the 1024 magic add (FP16 has
 //     unit spacing at 1024, so the add rounds half to even).
 // Blocks are not bit-identical to the FP32 oracle; the gate is PSNR against
@@ -203,7 +203,11 @@ __device__ __forceinline__ uint4 encode_block_h2(const uint32_t (&px)[DIM * DIM]
     } else {
         const float r = rsqrtf(kk);
         const __half2 wrg = __floats2half2_rn(k0 * r, k1 * r), wba = __floats2half2_rn(k2 * r, k3 * r);
-        const __half2 erg = __floats2half2_rn(e0[0], e0[1]), eba = __floats2half2_rn(e0[2], e0[3]);
+        // project relative to the endpoint midpoint: |w| <= range/2 halves the
+        // FP16 rounding of every product; the shift is the same for all
+        // samples, so the min/max normalisation removes it
+        const __half2 erg = __floats2half2_rn(0.5f * (e0[0] + e1[0]), 0.5f * (e0[1] + e1[1]));
+        const __half2 eba = __floats2half2_rn(0.5f * (e0[2] + e1[2]), 0.5f * (e0[3] + e1[3]));
         const bool use_ba = !NORMAL;                     // normal maps: e0.ba == e1.ba, k.b = k.a = 0
         __half2 wv[8];
         __half2 wmin = __floats2half2_rn(65504.0f, 65504.0f), wmax = __floats2half2_rn(-65504.0f, -65504.0f);

@@ -1,0 +1,373 @@
+// image_load.cpp -- PNG / Netpbm reader for the command line tool.
+// Inflate follows RFC 1951 (stored, fixed and dynamic Huffman blocks,
+// canonical codes decoded one bit at a time); the zlib wrapper RFC 1950;
+// PNG chunk layout, filters 0-4 and colour types the PNG specification.
+#include "image_load.h"
+
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+
+namespace astc {
+namespace {
+
+struct Bits {
+    const uint8_t* p;
+    size_t n, pos = 0;
+    uint32_t buf = 0;
+    int cnt = 0;
+    bool over = false;
+    int bit() {
+        if (cnt == 0) {
+            if (pos >= n) { over = true; return 0; }
+            buf = p[pos++];
+            cnt = 8;
+        }
+        const int b = buf & 1;
+        buf >>= 1;
+        --cnt;
+        return b;
+    }
+    uint32_t take(int k) {          // k bits, least significant first
+        uint32_t v = 0;
+        for (int i = 0; i < k; ++i) v |= (uint32_t)bit() << i;
+        return v;
+    }
+};
+
+struct Huffman {
+    uint16_t count[16] = {};        // codes per length
+    uint16_t symbol[320] = {};      // symbols ordered by (length, value)
+};
+
+// Canonical code from lengths; returns false for an over-subscribed set.
+bool build(Huffman& h, const uint8_t* len, int n) {
+    memset(h.count, 0, sizeof(h.count));
+    for (int i = 0; i < n; ++i) h.count[len[i]]++;
+    int left = 1;
+    for (int l = 1; l < 16; ++l) {
+        left <<= 1;
+        left -= h.count[l];
+        if (left < 0) return false;
+    }
+    uint16_t offs[16];
+    offs[1] = 0;
+    for (int l = 1; l < 15; ++l) offs[l + 1] = offs[l] + h.count[l];
+    for (int i = 0; i < n; ++i)
+        if (len[i]) h.symbol[offs[len[i]]++] = (uint16_t)i;
+    return true;
+}
+
+// Walks the code one bit at a time: at each length the first `count` codes
+// of that length map to the next symbols.
+int decode(Bits& b, const Huffman& h) {
+    int code = 0, first = 0, index = 0;
+    for (int l = 1; l < 16; ++l) {
+        code |= b.bit();
+        const int count = h.count[l];
+        if (code - first < count) return h.symbol[index + (code - first)];
+        index += count;
+        first += count;
+        first <<= 1;
+        code <<= 1;
+        if (b.over) return -1;
+    }
+    return -1;
+}
+
+const uint16_t kLenBase[29] = {3,  4,  5,  6,  7,  8,  9,  10, 11,  13,  15,  17,  19,  23, 27,
+                               31, 35, 43, 51, 59, 67, 83, 99, 115, 131, 163, 195, 227, 258};
+const uint8_t kLenExtra[29] = {0, 0, 0, 0, 0, 0, 0, 0, 1, 1, 1, 1, 2, 2, 2,
+                               2, 3, 3, 3, 3, 4, 4, 4, 4, 5, 5, 5, 5, 0};
+const uint16_t kDistBase[30] = {1,   2,   3,   4,   5,   7,    9,    13,   17,   25,
+                                33,  49,  65,  97,  129, 193,  257,  385,  513,  769,
+                                1025, 1537, 2049, 3073, 4097, 6145, 8193, 12289, 16385, 24577};
+const uint8_t kDistExtra[30] = {0, 0, 0, 0, 1, 1, 2, 2,  3,  3,  4,  4,  5,  5,  6,
+                                6, 7, 7, 8, 8, 9, 9, 10, 10, 11, 11, 12, 12, 13, 13};
+
+bool inflate_codes(Bits& b, const Huffman& lit, const Huffman& dist, std::vector<uint8_t>& out,
+                   std::string& err) {
+    for (;;) {
+        const int sym = decode(b, lit);
+        if (sym < 0) { err = "bad literal/length code"; return false; }
+        if (sym < 256) { out.push_back((uint8_t)sym); continue; }
+        if (sym == 256) return true;
+        const int li = sym - 257;
+        if (li >= 29) { err = "bad length symbol"; return false; }
+        const size_t len = kLenBase[li] + b.take(kLenExtra[li]);
+        const int ds = decode(b, dist);
+        if (ds < 0 || ds >= 30) { err = "bad distance code"; return false; }
+        const size_t d = kDistBase[ds] + b.take(kDistExtra[ds]);
+        if (d > out.size()) { err = "distance beyond the output"; return false; }
+        const size_t from = out.size() - d;
+        for (size_t i = 0; i < len; ++i) out.push_back(out[from + i]);
+        if (b.over) { err = "truncated deflate stream"; return false; }
+    }
+}
+
+uint32_t be32(const uint8_t* p) { return (uint32_t)p[0] << 24 | (uint32_t)p[1] << 16 | (uint32_t)p[2] << 8 | p[3]; }
+
+}  // namespace
+
+bool zlib_inflate(const uint8_t* data, size_t size, std::vector<uint8_t>& out, std::string& err) {
+    if (size < 6) { err = "zlib stream too short"; return false; }
+    if ((data[0] & 0x0F) != 8 || ((data[0] << 8) | data[1]) % 31 != 0 || (data[1] & 0x20)) {
+        err = "bad zlib header";
+        return false;
+    }
+    Bits b{data + 2, size - 2};
+    out.clear();
+    int last = 0;
+    do {
+        last = b.bit();
+        const int type = (int)b.take(2);
+        if (type == 0) {
+            b.buf = 0;
+            b.cnt = 0;                                  // to the byte boundary
+            if (b.pos + 4 > b.n) { err = "truncated stored block"; return false; }
+            const uint32_t len = b.p[b.pos] | (b.p[b.pos + 1] << 8);
+            const uint32_t nlen = b.p[b.pos + 2] | (b.p[b.pos + 3] << 8);
+            b.pos += 4;
+            if ((len ^ 0xFFFFu) != nlen || b.pos + len > b.n) { err = "bad stored block"; return false; }
+            out.insert(out.end(), b.p + b.pos, b.p + b.pos + len);
+            b.pos += len;
+        } else if (type == 1) {
+            static Huffman flit, fdist;
+            static bool ready = false;
+            if (!ready) {
+                uint8_t l[288];
+                for (int i = 0; i < 144; ++i) l[i] = 8;
+                for (int i = 144; i < 256; ++i) l[i] = 9;
+                for (int i = 256; i < 280; ++i) l[i] = 7;
+                for (int i = 280; i < 288; ++i) l[i] = 8;
+                build(flit, l, 288);
+                uint8_t d[30];
+                for (int i = 0; i < 30; ++i) d[i] = 5;
+                build(fdist, d, 30);
+                ready = true;
+            }
+            if (!inflate_codes(b, flit, fdist, out, err)) return false;
+        } else if (type == 2) {
+            const int nlen = (int)b.take(5) + 257, ndist = (int)b.take(5) + 1, ncode = (int)b.take(4) + 4;
+            if (nlen > 286 || ndist > 30) { err = "bad dynamic block counts"; return false; }
+            static const uint8_t order[19] = {16, 17, 18, 0, 8, 7, 9, 6, 10, 5, 11, 4, 12, 3, 13, 2, 14, 1, 15};
+            uint8_t cl[19] = {};
+            for (int i = 0; i < ncode; ++i) cl[order[i]] = (uint8_t)b.take(3);
+            Huffman clh;
+            if (!build(clh, cl, 19)) { err = "bad code-length code"; return false; }
+            uint8_t lens[320] = {};
+            int i = 0;
+            while (i < nlen + ndist) {
+                const int sym = decode(b, clh);
+                if (sym < 0) { err = "bad code-length symbol"; return false; }
+                if (sym < 16) { lens[i++] = (uint8_t)sym; continue; }
+                int rep = 0;
+                uint8_t val = 0;
+                if (sym == 16) {
+                    if (i == 0) { err = "repeat with no previous length"; return false; }
+                    val = lens[i - 1];
+                    rep = 3 + (int)b.take(2);
+                } else if (sym == 17) {
+                    rep = 3 + (int)b.take(3);
+                } else {
+                    rep = 11 + (int)b.take(7);
+                }
+                if (i + rep > nlen + ndist) { err = "code lengths overrun"; return false; }
+                while (rep--) lens[i++] = val;
+            }
+            Huffman lit, dist;
+            if (!build(lit, lens, nlen) || !build(dist, lens + nlen, ndist)) {
+                err = "bad dynamic Huffman code";
+                return false;
+            }
+            if (!inflate_codes(b, lit, dist, out, err)) return false;
+        } else {
+            err = "bad deflate block type";
+            return false;
+        }
+        if (b.over) { err = "truncated deflate stream"; return false; }
+    } while (!last);
+    return true;
+}
+
+bool decode_png(const uint8_t* d, size_t n, Image& img, std::string& err) {
+    static const uint8_t sig[8] = {0x89, 'P', 'N', 'G', '\r', '\n', 0x1A, '\n'};
+    if (n < 8 || memcmp(d, sig, 8) != 0) { err = "not a PNG file"; return false; }
+    size_t pos = 8;
+    uint32_t w = 0, h = 0;
+    int depth = 0, ctype = -1, interlace = 0;
+    std::vector<uint8_t> idat, plte, trns;
+    while (pos + 12 <= n) {
+        const uint32_t len = be32(d + pos);
+        const uint8_t* type = d + pos + 4;
+        const uint8_t* body = d + pos + 8;
+        if (pos + 12 + (size_t)len > n) { err = "truncated PNG chunk"; return false; }
+        if (!memcmp(type, "IHDR", 4) && len >= 13) {
+            w = be32(body);
+            h = be32(body + 4);
+            depth = body[8];
+            ctype = body[9];
+            interlace = body[12];
+        } else if (!memcmp(type, "PLTE", 4)) {
+            plte.assign(body, body + len);
+        } else if (!memcmp(type, "tRNS", 4)) {
+            trns.assign(body, body + len);
+        } else if (!memcmp(type, "IDAT", 4)) {
+            idat.insert(idat.end(), body, body + len);
+        } else if (!memcmp(type, "IEND", 4)) {
+            break;
+        }
+        pos += 12 + (size_t)len;
+    }
+    if (w == 0 || h == 0 || w > (1u << 24) || h > (1u << 24)) { err = "bad PNG size"; return false; }
+    if (interlace != 0) { err = "interlaced PNG is not supported"; return false; }
+    int chans = 0;
+    switch (ctype) {
+    case 0: chans = 1; break;
+    case 2: chans = 3; break;
+    case 3: chans = 1; break;
+    case 4: chans = 2; break;
+    case 6: chans = 4; break;
+    default: err = "bad PNG colour type"; return false;
+    }
+    if (!(depth == 8 || (depth == 16 && ctype != 3))) { err = "only 8- and 16-bit PNG is supported"; return false; }
+    const int bps = depth / 8;
+    const size_t bpp = (size_t)chans * bps, stride = (size_t)w * bpp;
+    std::vector<uint8_t> raw;
+    if (!zlib_inflate(idat.data(), idat.size(), raw, err)) return false;
+    if (raw.size() < (stride + 1) * h) { err = "PNG image data too short"; return false; }
+    std::vector<uint8_t> cur(stride), prev(stride, 0);
+    img.width = (int)w;
+    img.height = (int)h;
+    img.rgba.assign((size_t)w * h * 4, 0);
+    for (uint32_t y = 0; y < h; ++y) {
+        const uint8_t* line = raw.data() + y * (stride + 1);
+        const int f = line[0];
+        for (size_t x = 0; x < stride; ++x) {
+            const int a = x >= bpp ? cur[x - bpp] : 0, b = prev[x], c = x >= bpp ? prev[x - bpp] : 0;
+            int p = 0;
+            switch (f) {
+            case 0: p = 0; break;
+            case 1: p = a; break;
+            case 2: p = b; break;
+            case 3: p = (a + b) >> 1; break;
+            case 4: {
+                const int e = a + b - c, pa = abs(e - a), pb = abs(e - b), pc = abs(e - c);
+                p = (pa <= pb && pa <= pc) ? a : (pb <= pc ? b : c);
+                break;
+            }
+            default: err = "bad PNG filter type"; return false;
+            }
+            cur[x] = (uint8_t)(line[1 + x] + p);
+        }
+        uint8_t* o = img.rgba.data() + (size_t)y * w * 4;
+        for (uint32_t x = 0; x < w; ++x) {
+            const uint8_t* s = cur.data() + x * bpp;
+            auto ch = [&](int i) { return s[i * bps]; };             // high byte of 16-bit
+            uint8_t r, g, bl, al = 255;
+            if (ctype == 3) {
+                const int idx = ch(0);
+                if ((size_t)idx * 3 + 2 >= plte.size()) {
+                    err = "palette index out of range";
+                    return false;
+                }
+                r = plte[idx * 3];
+                g = plte[idx * 3 + 1];
+                bl = plte[idx * 3 + 2];
+                if ((size_t)idx < trns.size()) al = trns[idx];
+            } else if (chans >= 3) {
+                r = ch(0); g = ch(1); bl = ch(2);
+                if (chans == 4) al = ch(3);
+            } else {
+                r = g = bl = ch(0);
+                if (chans == 2) al = ch(1);
+            }
+            o[4 * x] = r; o[4 * x + 1] = g; o[4 * x + 2] = bl; o[4 * x + 3] = al;
+        }
+        std::swap(cur, prev);
+    }
+    return true;
+}
+
+bool decode_pnm(const uint8_t* d, size_t n, Image& img, std::string& err) {
+    if (n < 3 || d[0] != 'P') { err = "not a PNM/PAM file"; return false; }
+    size_t pos = 2;
+    auto token = [&](std::string& t) {
+        t.clear();
+        while (pos < n) {
+            if (d[pos] == '#') { while (pos < n && d[pos] != '\n') ++pos; continue; }
+            if (d[pos] == ' ' || d[pos] == '\t' || d[pos] == '\r' || d[pos] == '\n') { ++pos; continue; }
+            break;
+        }
+        while (pos < n && !(d[pos] == ' ' || d[pos] == '\t' || d[pos] == '\r' || d[pos] == '\n'))
+            t.push_back((char)d[pos++]);
+        return !t.empty();
+    };
+    int w = 0, h = 0, depth = 0, maxv = 0;
+    std::string t;
+    if (d[1] == '7') {
+        while (token(t) && t != "ENDHDR") {
+            std::string v;
+            if (t == "WIDTH" && token(v)) w = atoi(v.c_str());
+            else if (t == "HEIGHT" && token(v)) h = atoi(v.c_str());
+            else if (t == "DEPTH" && token(v)) depth = atoi(v.c_str());
+            else if (t == "MAXVAL" && token(v)) maxv = atoi(v.c_str());
+            else if (t == "TUPLTYPE") token(v);
+        }
+    } else if (d[1] == '5' || d[1] == '6') {
+        depth = d[1] == '6' ? 3 : 1;
+        if (!token(t)) { err = "bad PNM header"; return false; }
+        w = atoi(t.c_str());
+        if (!token(t)) { err = "bad PNM header"; return false; }
+        h = atoi(t.c_str());
+        if (!token(t)) { err = "bad PNM header"; return false; }
+        maxv = atoi(t.c_str());
+    } else {
+        err = "unsupported PNM type";
+        return false;
+    }
+    ++pos;                                               // one whitespace byte before the data
+    if (w <= 0 || h <= 0 || depth < 1 || depth > 4 || maxv != 255) { err = "unsupported PNM header"; return false; }
+    if (pos + (size_t)w * h * depth > n) { err = "PNM data too short"; return false; }
+    img.width = w;
+    img.height = h;
+    img.rgba.assign((size_t)w * h * 4, 255);
+    const uint8_t* s = d + pos;
+    for (size_t i = 0; i < (size_t)w * h; ++i, s += depth) {
+        uint8_t* o = img.rgba.data() + i * 4;
+        if (depth >= 3) { o[0] = s[0]; o[1] = s[1]; o[2] = s[2]; if (depth == 4) o[3] = s[3]; }
+        else { o[0] = o[1] = o[2] = s[0]; if (depth == 2) o[3] = s[1]; }
+    }
+    return true;
+}
+
+bool load_image(const std::string& path, Image& img, std::string& err) {
+    FILE* f = fopen(path.c_str(), "rb");
+    if (!f) { err = "cannot open " + path; return false; }
+    std::vector<uint8_t> data;
+    uint8_t buf[1 << 16];
+    size_t got;
+    while ((got = fread(buf, 1, sizeof(buf), f)) > 0) data.insert(data.end(), buf, buf + got);
+    fclose(f);
+    if (data.size() >= 8 && data[0] == 0x89 && data[1] == 'P') return decode_png(data.data(), data.size(), img, err);
+    return decode_pnm(data.data(), data.size(), img, err);
+}
+
+bool save_pam(const std::string& path, const Image& img, std::string& err) {
+    FILE* f = fopen(path.c_str(), "wb");
+    if (!f) { err = "cannot open " + path; return false; }
+    fprintf(f, "P7\nWIDTH %d\nHEIGHT %d\nDEPTH 4\nMAXVAL 255\nTUPLTYPE RGB_ALPHA\nENDHDR\n", img.width, img.height);
+    const bool ok = fwrite(img.rgba.data(), 1, img.rgba.size(), f) == img.rgba.size();
+    if (fclose(f) != 0 || !ok) { err = "write failed: " + path; return false; }
+    return true;
+}
+
+void flip_vertical(Image& img) {
+    const size_t row = (size_t)img.width * 4;
+    for (int y = 0; y < img.height / 2; ++y)
+        std::swap_ranges(img.rgba.begin() + y * row, img.rgba.begin() + (y + 1) * row,
+                         img.rgba.begin() + (size_t)(img.height - 1 - y) * row);
+}
+
+}  // namespace astc

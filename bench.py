@@ -54,6 +54,8 @@ def _parse():
     ap.add_argument("--workload", default="6x6_rgba_srgb_2048")
     ap.add_argument("--no-extra", action="store_true", help="skip the secondary workloads")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--no-batched", action="store_true", help="skip the mixed batched workload")
+    ap.add_argument("--batched-count", type=int, default=256, help="textures in the mixed batch")
     ap.add_argument("--profile-case", action="store_true",
                     help="small case for ncu: 2 textures per step, encode launches only")
     return ap.parse_args()
@@ -261,6 +263,112 @@ def _time_launches(torch, native, texs, outs, spec, steps):
     return sum(per_step) / max(1, launches), per_step, launches
 
 
+def _bench_batched(torch, native, oracle, count: int, reps: int = 5) -> dict:
+    """The mixed workload: `count` textures with full mip chains, mixed formats.
+
+    plain   -- one astc_encode_gpu_pitched launch per texture level (FP32)
+    batched -- one astc_batch_encode graph launch for everything (FP32, HALF2)
+    Inputs resident in HBM; CUDA events on the work stream around each pass.
+    """
+    from astc_encoder_gb300 import synth_gpu
+    stream = torch.cuda.current_stream()
+    t0 = time.perf_counter()
+    texs = synth_gpu.mixed_batch(torch, native, count)
+    gen_s = time.perf_counter() - t0
+    lib = native.load_library()
+    jobs = []            # (w, h, in_tensor, out_tensor, opts)
+    for t in texs:
+        d = t["opts"]["block_dim"]
+        for w, h, lvl in t["levels"]:
+            nb = ((w + d - 1) // d) * ((h + d - 1) // d)
+            jobs.append((w, h, lvl, torch.empty((nb, 16), dtype=torch.uint8, device="cuda"), t["opts"]))
+    texels = sum(w * h for w, h, *_ in jobs)
+    blocks = sum(o.shape[0] for *_, o, _ in jobs)
+    # plain: one launch per level, options prebuilt
+    plain_calls = []
+    for w, h, lvl, out, opts in jobs:
+        o = native.make_opts(memory=native.Memory.DEVICE, stream=stream.cuda_stream, **opts)
+        plain_calls.append((lvl.data_ptr(), w, h, w * 4, o, out.data_ptr()))
+    enc = lib.astc_encode_gpu_pitched
+
+    def plain_pass():
+        for src, w, h, pitch, o, dst in plain_calls:
+            st = enc(src, w, h, pitch, ctypes.byref(o), dst)
+            if st:
+                raise native.AstcError(st, lib.astc_last_error().decode())
+
+    items = (native.BatchItem * len(jobs))()
+    for i, (w, h, lvl, out, opts) in enumerate(jobs):
+        items[i] = native.BatchItem(lvl.data_ptr(), 0, w, h, opts["block_dim"], int(opts["has_alpha"]),
+                                    int(opts["is_normal"]), int(opts["srgb"]), int(opts["border"]),
+                                    out.data_ptr())
+    batch = native.Batch(len(jobs), blocks)
+
+    def batched_pass(prec):
+        st = lib.astc_batch_encode(batch._h, items, len(jobs), prec, stream.cuda_stream)
+        if st:
+            raise native.AstcError(st, lib.astc_last_error().decode())
+
+    def timed(fn):
+        fn()
+        torch.cuda.synchronize()
+        best, l0 = [], native.kernel_launch_count()
+        for _ in range(reps):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            torch.cuda.synchronize()
+            best.append(a.elapsed_time(b))
+        return float(np.median(best)), (native.kernel_launch_count() - l0) // reps
+
+    plain_ms, plain_launches = timed(plain_pass)
+    fp32_ms, fp32_launches = timed(lambda: batched_pass(0))
+    fp32_blocks = [o.cpu().numpy() for *_, o, _ in jobs]
+    h2_ms, h2_launches = timed(lambda: batched_pass(1))
+    # quality per texture (level 0): PSNR of FP32 / HALF2 against the FP64 oracle
+    gaps, same = [], []
+    k = 0
+    for t in texs:
+        w, h, lvl = t["levels"][0]
+        opts = t["opts"]
+        img = lvl.cpu().numpy()
+        h2 = jobs[k][3].cpu().numpy()
+        f32 = fp32_blocks[k]
+        f64 = oracle.encode(img, fp64=True, **opts)
+        ref = native.fitted_reference(img, opts["srgb"], opts["is_normal"])
+        ch = 4 if opts["has_alpha"] else (2 if opts["is_normal"] else 3)
+
+        def psnr(bl):
+            dec = native.decode(bl, w, h, opts["block_dim"])
+            s = native.sse(dec, ref)
+            return native.psnr_from_sse(float(s[:ch].sum()), w * h * ch)
+        p64 = psnr(f64)
+        gaps.append((p64 - psnr(f32), p64 - psnr(h2)))
+        same.append(float(np.all(h2 == f32, axis=1).mean()))
+        k += len(t["levels"])
+    batch.close()
+    g32 = np.array([g[0] for g in gaps])
+    g16 = np.array([g[1] for g in gaps])
+    mtex = lambda ms: texels / (ms / 1e3) / 1e6  # noqa: E731
+    return {
+        "textures": count, "texture_levels": len(jobs), "texels": texels, "blocks": blocks,
+        "formats": {f: sum(1 for t in texs if t["format"] == f) for f in ("4x4_rgb", "6x6_rgba_srgb", "4x4_normal")},
+        "plain_fp32": {"ms": plain_ms, "Mtexels_s": mtex(plain_ms), "launches": plain_launches},
+        "batched_fp32": {"ms": fp32_ms, "Mtexels_s": mtex(fp32_ms), "launches": fp32_launches,
+                         "graph_launches": 1},
+        "batched_half2": {"ms": h2_ms, "Mtexels_s": mtex(h2_ms), "launches": h2_launches, "graph_launches": 1},
+        "speedup_batched_half2_vs_plain_fp32": plain_ms / h2_ms,
+        "speedup_batched_fp32_vs_plain_fp32": plain_ms / fp32_ms,
+        "speedup_half2_vs_fp32_batched": fp32_ms / h2_ms,
+        "psnr_gap_to_fp64_db": {"fp32_mean": float(g32.mean()), "fp32_max": float(g32.max()),
+                                "half2_mean": float(g16.mean()), "half2_max": float(g16.max()),
+                                "half2_textures_within_0.05dB": int((g16 <= 0.05).sum())},
+        "half2_identical_blocks_vs_fp32_mean": float(np.mean(same)),
+        "generation_s": gen_s,
+    }
+
+
 def run_ours(args) -> None:
     import torch
     world, rank, local = _dist()
@@ -403,6 +511,7 @@ def run_ours(args) -> None:
                            "textures_per_step": reps}
             del xt, xo
 
+    batched = None if args.no_batched else _bench_batched(torch, native, oracle, args.batched_count)
     cpu = None if args.no_cpu else _cpu_baseline(img, spec)
 
     line = {
@@ -438,6 +547,7 @@ def run_ours(args) -> None:
         "clocks": clk,
         "wall_s_timed_region": wall,
         "extra_workloads": extra,
+        "batched_mixed": batched,
     }
     if cpu is not None:
         line["cpu_baseline"] = cpu
