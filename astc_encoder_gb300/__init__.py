@@ -164,8 +164,111 @@ def load_library() -> ctypes.CDLL:
     lib.astc_generate_mips.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                        ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
     lib.astc_generate_mips.restype = ctypes.c_int
+    vpp = ctypes.POINTER(ctypes.c_void_p)
+    lib.astc_server_create.argtypes = [ctypes.POINTER(ServerConfig), vpp]
+    lib.astc_server_create.restype = ctypes.c_int
+    lib.astc_server_submit.argtypes = [ctypes.c_void_p, ctypes.POINTER(Request),
+                                       ctypes.POINTER(ctypes.c_uint64)]
+    lib.astc_server_submit.restype = ctypes.c_int
+    lib.astc_server_wait.argtypes = [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int,
+                                     ctypes.POINTER(RequestStats)]
+    lib.astc_server_wait.restype = ctypes.c_int
+    lib.astc_server_cancel.argtypes = [ctypes.c_void_p, ctypes.c_uint64]
+    lib.astc_server_cancel.restype = ctypes.c_int
+    dp = ctypes.POINTER(ctypes.c_double)
+    lib.astc_server_replay.argtypes = [ctypes.c_void_p, ctypes.POINTER(Request), dp, ctypes.c_int, dp, dp]
+    lib.astc_server_replay.restype = ctypes.c_int
+    lib.astc_server_destroy.argtypes = [ctypes.c_void_p]
+    lib.astc_server_destroy.restype = ctypes.c_int
     _LIB = lib
     return lib
+
+
+class ServerConfig(ctypes.Structure):
+    """``astc_server_config`` of include/astc_gb300.h."""
+    _fields_ = [("pool_bytes", ctypes.c_size_t), ("max_batch", ctypes.c_int), ("inflight", ctypes.c_int),
+                ("precision", ctypes.c_int), ("mode", ctypes.c_int)]
+
+
+class Request(ctypes.Structure):
+    """``astc_request`` of include/astc_gb300.h (host buffers)."""
+    _fields_ = [("rgba8", ctypes.c_void_p), ("row_pitch", ctypes.c_size_t), ("width", ctypes.c_int),
+                ("height", ctypes.c_int), ("block_dim", ctypes.c_int), ("has_alpha", ctypes.c_int),
+                ("is_normal", ctypes.c_int), ("srgb", ctypes.c_int), ("border", ctypes.c_int),
+                ("out", ctypes.c_void_p)]
+
+
+class RequestStats(ctypes.Structure):
+    _fields_ = [("submit_us", ctypes.c_double), ("admit_us", ctypes.c_double), ("done_us", ctypes.c_double),
+                ("status", ctypes.c_int)]
+
+
+SERVE_BATCHED, SERVE_PER_REQUEST = 0, 1
+
+
+def make_request(rgba_ptr: int, width: int, height: int, out_ptr: int, block_dim: int = 4,
+                 has_alpha: bool = False, is_normal: bool = False, srgb: bool = False,
+                 border: int = Border.ZERO, row_pitch: int = 0) -> Request:
+    return Request(rgba_ptr, row_pitch, width, height, block_dim, int(has_alpha), int(is_normal), int(srgb),
+                   int(border), out_ptr)
+
+
+class Server:
+    """Continuous-batching request server (astc_server_*) over host buffers."""
+
+    def __init__(self, pool_bytes: int = 2 << 30, max_batch: int = 256, inflight: int = 3,
+                 precision: int = Precision.FP32, mode: int = SERVE_BATCHED):
+        self._lib = load_library()
+        cfg = ServerConfig(pool_bytes, max_batch, inflight, int(precision), int(mode))
+        h = ctypes.c_void_p()
+        _check(self._lib.astc_server_create(ctypes.byref(cfg), ctypes.byref(h)))
+        self._h = h
+
+    def submit(self, req: Request) -> int:
+        t = ctypes.c_uint64()
+        _check(self._lib.astc_server_submit(self._h, ctypes.byref(req), ctypes.byref(t)))
+        return t.value
+
+    def wait(self, ticket: int, timeout_ms: int = -1) -> RequestStats:
+        st = RequestStats()
+        _check(self._lib.astc_server_wait(self._h, ticket, timeout_ms, ctypes.byref(st)))
+        return st
+
+    def try_wait(self, ticket: int, timeout_ms: int) -> tuple[int, RequestStats]:
+        st = RequestStats()
+        rc = self._lib.astc_server_wait(self._h, ticket, timeout_ms, ctypes.byref(st))
+        return rc, st
+
+    def cancel(self, ticket: int) -> int:
+        return int(self._lib.astc_server_cancel(self._h, ticket))
+
+    def replay(self, requests: list[Request], arrival_us) -> tuple[np.ndarray, float]:
+        n = len(requests)
+        arr = (Request * max(1, n))(*requests)
+        arrival = np.ascontiguousarray(arrival_us, dtype=np.float64)
+        lat = np.zeros(n, np.float64)
+        wall = ctypes.c_double()
+        dp = ctypes.POINTER(ctypes.c_double)
+        _check(self._lib.astc_server_replay(self._h, arr, arrival.ctypes.data_as(dp), n,
+                                            lat.ctypes.data_as(dp), ctypes.byref(wall)))
+        return lat, wall.value
+
+    def close(self) -> None:
+        if self._h:
+            self._lib.astc_server_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:  # noqa: BLE001
+            pass
 
 
 class BatchItem(ctypes.Structure):

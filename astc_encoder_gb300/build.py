@@ -36,6 +36,7 @@ LIB_SOURCES = [
     ("astc_encode_h2.cu", ["--fmad=false"]),
     ("astc_batch.cu", ["--fmad=false"]),
     ("astc_mips.cu", []),
+    ("astc_server.cu", []),
     ("astc_decode.cu", []),
     ("astc_capi.cu", []),
     ("astc_noalloc.cu", []),

@@ -56,6 +56,8 @@ def _parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--no-batched", action="store_true", help="skip the mixed batched workload")
     ap.add_argument("--batched-count", type=int, default=256, help="textures in the mixed batch")
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving sweep")
+    ap.add_argument("--serving-rates", default="100,1000,5000,20000", help="offered request rates")
     ap.add_argument("--profile-case", action="store_true",
                     help="small case for ncu: 2 textures per step, encode launches only")
     return ap.parse_args()
@@ -369,6 +371,59 @@ def _bench_batched(torch, native, oracle, count: int, reps: int = 5) -> dict:
     }
 
 
+def _bench_serving(torch, native, rates, seconds: float = 2.0, max_requests: int = 2000) -> dict:
+    """Open-loop serving: Poisson arrivals at each rate, single-texture requests.
+
+    Request side lengths are log-uniform in [128, 2048] (square), formats mixed
+    60% 4x4 RGB / 25% 6x6 RGBA sRGB / 15% 4x4 normal, content cropped from
+    2048x2048 synthetic textures held in pinned host memory; 2 GiB device
+    staging pool with admission by memory.  Batched = continuous batching
+    through astc_batch; per-request = one plain launch per request.
+    """
+    from astc_encoder_gb300 import synth
+    bases = {
+        "4x4_rgb": (synth.rgb_noise(2048, 2048), dict(block_dim=4)),
+        "6x6_rgba_srgb": (synth.rgba_cutout(2048, 2048), dict(block_dim=6, has_alpha=True, srgb=True, border=1)),
+        "4x4_normal": (synth.normal_map(2048, 2048), dict(block_dim=4, is_normal=True)),
+    }
+    pinned = {k: torch.from_numpy(v[0]).pin_memory() for k, v in bases.items()}
+    names, probs = ["4x4_rgb", "6x6_rgba_srgb", "4x4_normal"], [0.60, 0.25, 0.15]
+    rng = np.random.default_rng(synth.SEED_BASE + 4)
+    n_max = max_requests
+    kinds = rng.choice(3, size=n_max, p=probs)
+    sides = np.exp(rng.uniform(np.log(128), np.log(2048), n_max)).astype(int)
+    reqs_meta, out_bytes = [], 0
+    for k, s in zip(kinds, sides):
+        name = names[k]
+        opts = bases[name][1]
+        x0, y0 = int(rng.integers(0, 2048 - s + 1)), int(rng.integers(0, 2048 - s + 1))
+        d = opts["block_dim"]
+        nb = ((s + d - 1) // d) ** 2
+        reqs_meta.append((name, int(s), x0, y0, opts, out_bytes, nb))
+        out_bytes += nb * 16
+    out = torch.empty(out_bytes, dtype=torch.uint8).pin_memory()
+    requests = []
+    for name, s, x0, y0, opts, off, nb in reqs_meta:
+        base = pinned[name]
+        ptr = base.data_ptr() + (y0 * 2048 + x0) * 4
+        requests.append(native.make_request(ptr, s, s, out.data_ptr() + off, row_pitch=2048 * 4, **opts))
+    texels = np.array([m[1] * m[1] for m in reqs_meta], np.float64)
+    result = {"pool_bytes": 2 << 30, "requests_max": n_max, "rates": {}}
+    for mode, label in ((native.SERVE_BATCHED, "batched"), (native.SERVE_PER_REQUEST, "per_request")):
+        with native.Server(pool_bytes=2 << 30, max_batch=256, inflight=3, mode=mode) as srv:
+            srv.replay(requests[:64], np.zeros(64))                       # warm-up (graphs, pools)
+            for rate in rates:
+                n = int(min(n_max, max(64, rate * seconds)))
+                arrival = np.cumsum(np.random.default_rng(int(rate)).exponential(1e6 / rate, n))
+                lat, wall = srv.replay(requests[:n], arrival)
+                result["rates"].setdefault(str(rate), {})[label] = {
+                    "requests": n, "p50_ms": float(np.percentile(lat, 50)) / 1e3,
+                    "p99_ms": float(np.percentile(lat, 99)) / 1e3, "mean_ms": float(lat.mean()) / 1e3,
+                    "throughput_req_s": n / wall, "Mtexels_s": float(texels[:n].sum()) / wall / 1e6,
+                    "offered_req_s": rate}
+    return result
+
+
 def run_ours(args) -> None:
     import torch
     world, rank, local = _dist()
@@ -512,6 +567,8 @@ def run_ours(args) -> None:
             del xt, xo
 
     batched = None if args.no_batched else _bench_batched(torch, native, oracle, args.batched_count)
+    serving = None if args.no_serving else _bench_serving(
+        torch, native, [int(r) for r in args.serving_rates.split(",") if r])
     cpu = None if args.no_cpu else _cpu_baseline(img, spec)
 
     line = {
@@ -548,6 +605,7 @@ def run_ours(args) -> None:
         "wall_s_timed_region": wall,
         "extra_workloads": extra,
         "batched_mixed": batched,
+        "serving": serving,
     }
     if cpu is not None:
         line["cpu_baseline"] = cpu

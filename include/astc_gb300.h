@@ -129,6 +129,66 @@ astc_status astc_batch_encode(astc_batch* batch, const astc_batch_item* items, i
                               int precision, void* stream);
 astc_status astc_batch_destroy(astc_batch* batch);
 
+/* ---- serving: continuous batching of single-texture requests -----------
+ * (No counterpart in the reference, a one-shot command line tool.)  A server
+ * owns a device staging pool and a worker thread.  Requests (host buffers)
+ * queue in arrival order; whenever an in-flight slot is free the worker
+ * admits queued requests, in order, while their inputs and outputs fit in
+ * the free pool memory (admission by memory) and the batch has room, copies
+ * them in, encodes them with one batched graph launch (or, in per-request
+ * mode, one plain kernel launch each) and copies the blocks back, all on the
+ * slot's stream.  Up to `inflight` slots run at once, so requests arriving
+ * while others are on the GPU are admitted as memory and slots free up, and
+ * their copies and kernels overlap with the work in flight.  A request's
+ * blocks are the same as astc_encode_gpu's for it, alone or in any mix. */
+typedef enum astc_serve_mode {
+    ASTC_SERVE_BATCHED = 0,       /* continuous batching through astc_batch */
+    ASTC_SERVE_PER_REQUEST = 1    /* one plain launch per request           */
+} astc_serve_mode;
+
+typedef struct astc_server_config {
+    size_t pool_bytes;   /* device staging pool for inputs + outputs           */
+    int max_batch;       /* requests per batch (batched mode)                   */
+    int inflight;        /* slots (batches or requests) in flight, 1..16        */
+    int precision;       /* astc_precision                                      */
+    int mode;            /* astc_serve_mode                                     */
+} astc_server_config;
+
+typedef struct astc_request {
+    const uint8_t* rgba8;   /* host memory; pinned memory copies asynchronously */
+    size_t row_pitch;       /* 0 = 4 * width                                     */
+    int width, height;
+    int block_dim, has_alpha, is_normal, srgb, border;
+    uint8_t* out;           /* host memory, astc_encoded_size() bytes            */
+} astc_request;
+
+typedef struct astc_request_stats {
+    double submit_us, admit_us, done_us;   /* server clock, microseconds        */
+    int status;                            /* astc_status of the request        */
+} astc_request_stats;
+
+typedef struct astc_server astc_server;
+
+astc_status astc_server_create(const astc_server_config* config, astc_server** out);
+/* Queues a request (non-blocking); *ticket identifies it.  Requests larger
+ * than the whole pool are rejected with ASTC_ERR_BUSY. */
+astc_status astc_server_submit(astc_server* server, const astc_request* request, uint64_t* ticket);
+/* Waits up to timeout_ms (< 0: no limit) for a request; ASTC_ERR_TIMEOUT if
+ * it is not done yet (the ticket stays valid), else the request's status
+ * (the ticket is then released). */
+astc_status astc_server_wait(astc_server* server, uint64_t ticket, int timeout_ms,
+                             astc_request_stats* stats);
+/* Cancels a request that is still queued (ASTC_ERR_BUSY once admitted). */
+astc_status astc_server_cancel(astc_server* server, uint64_t ticket);
+/* Load replay: submits request i at arrival_us[i] after the start (open
+ * loop), waits for all, and returns each request's latency from its
+ * scheduled arrival to its completion, plus the wall time. */
+astc_status astc_server_replay(astc_server* server, const astc_request* requests,
+                               const double* arrival_us, int count, double* latency_us,
+                               double* wall_s);
+/* Waits for the work in flight, then frees the server. */
+astc_status astc_server_destroy(astc_server* server);
+
 /* ---- mip chains (staging in front of the batched encoder) --------------
  * (No counterpart in the reference, which encodes one level: main.cpp:36.)
  * Level l+1 is max(1, w/2) x max(1, h/2); each texel is the rounded mean of
