@@ -10,10 +10,11 @@
 // its format's queue: a CTA takes the next item with one atomicAdd on a
 // device counter and encodes its blocks, one thread per block, exactly as the
 // plain kernels do (so a texture's blocks are the same whether it is encoded
-// alone or in a batch).  The descriptor copy and the kernels are captured
-// once per (precision, set of formats) into a CUDA graph and replayed; batch
-// sizes and contents are read from device memory at run time, so one graph
-// serves every batch that fits the handle.
+// alone or in a batch).  The kernels are captured once per (precision, set
+// of formats) into a CUDA graph and replayed; each call uploads exactly its
+// queue header, descriptors and items (two copies) and launches the graph.
+// Batch sizes and contents are read from device memory at run time, so one
+// graph serves every batch that fits the handle.
 //
 // No kernel here waits on another CTA or kernel: the only synchronisation is
 // the atomicAdd that hands out items.
@@ -178,7 +179,8 @@ astc_status check_ptr(astc_batch* b, const void* p, const char* what) {
     return ASTC_OK;
 }
 
-// Captures [descriptor upload -> one persistent kernel per format in `mask`].
+// Captures one persistent kernel per format in `mask` (the descriptor upload
+// is issued before the launch with the exact sizes of each batch).
 astc_status build_graph(astc_batch* b, unsigned mask, int prec, cudaGraphExec_t* out) {
     cudaStream_t s = b->capture_stream;
     cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
@@ -186,7 +188,6 @@ astc_status build_graph(astc_batch* b, unsigned mask, int prec, cudaGraphExec_t*
     auto* q = reinterpret_cast<QueueState*>(b->d_buf);
     auto* jobs = reinterpret_cast<BatchJob*>(b->d_buf + jobs_offset());
     auto* items = reinterpret_cast<WorkItem*>(b->d_buf + items_offset(b->max_items));
-    e = cudaMemcpyAsync(b->d_buf, b->h_buf, b->buf_bytes, cudaMemcpyHostToDevice, s);
     for (int f = 0; f < kFormats && e == cudaSuccess; ++f) {
         if (!(mask & (1u << f))) continue;
         KernelFn k = prec == ASTC_PRECISION_HALF2 ? kernel_for<ASTC_PRECISION_HALF2>(f)
@@ -340,6 +341,13 @@ astc_status astc_batch_encode(astc_batch* b, const astc_batch_item* in, int coun
             it = b->graphs.emplace(key, g).first;
         }
         cudaStream_t s = static_cast<cudaStream_t>(stream);
+        // upload exactly this batch's queue header + descriptors, and its items
+        const size_t head = jobs_offset() + (size_t)count * sizeof(BatchJob);
+        const size_t ioff = items_offset(b->max_items);
+        if ((e = cudaMemcpyAsync(b->d_buf, b->h_buf, head, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+            (e = cudaMemcpyAsync(b->d_buf + ioff, b->h_buf + ioff, (size_t)total * sizeof(WorkItem),
+                                 cudaMemcpyHostToDevice, s)) != cudaSuccess)
+            return cuda_error(e, "descriptor upload");
         if ((e = cudaGraphLaunch(it->second, s)) != cudaSuccess) return cuda_error(e, "cudaGraphLaunch");
         if ((e = cudaEventRecord(b->done, s)) != cudaSuccess) return cuda_error(e, "cudaEventRecord");
         b->pending = true;

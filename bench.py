@@ -57,7 +57,8 @@ def _parse():
     ap.add_argument("--no-batched", action="store_true", help="skip the mixed batched workload")
     ap.add_argument("--batched-count", type=int, default=256, help="textures in the mixed batch")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving sweep")
-    ap.add_argument("--serving-rates", default="100,1000,5000,20000", help="offered request rates")
+    ap.add_argument("--serving-rates", default="100,1000,5000,20000,50000,100000",
+                    help="offered request rates (req/s)")
     ap.add_argument("--profile-case", action="store_true",
                     help="small case for ncu: 2 textures per step, encode launches only")
     return ap.parse_args()
@@ -398,7 +399,7 @@ def _bench_serving(torch, native, rates, seconds: float = 2.0, max_requests: int
         opts = bases[name][1]
         x0, y0 = int(rng.integers(0, 2048 - s + 1)), int(rng.integers(0, 2048 - s + 1))
         d = opts["block_dim"]
-        nb = ((s + d - 1) // d) ** 2
+        nb = int(((int(s) + d - 1) // d) ** 2)
         reqs_meta.append((name, int(s), x0, y0, opts, out_bytes, nb))
         out_bytes += nb * 16
     out = torch.empty(out_bytes, dtype=torch.uint8).pin_memory()
@@ -406,7 +407,7 @@ def _bench_serving(torch, native, rates, seconds: float = 2.0, max_requests: int
     for name, s, x0, y0, opts, off, nb in reqs_meta:
         base = pinned[name]
         ptr = base.data_ptr() + (y0 * 2048 + x0) * 4
-        requests.append(native.make_request(ptr, s, s, out.data_ptr() + off, row_pitch=2048 * 4, **opts))
+        requests.append(native.make_request(int(ptr), s, s, int(out.data_ptr() + off), row_pitch=2048 * 4, **opts))
     texels = np.array([m[1] * m[1] for m in reqs_meta], np.float64)
     result = {"pool_bytes": 2 << 30, "requests_max": n_max, "rates": {}}
     for mode, label in ((native.SERVE_BATCHED, "batched"), (native.SERVE_PER_REQUEST, "per_request")):
