@@ -65,8 +65,11 @@ inline int format_index(int dim, bool alpha, bool normal, bool srgb) {
     return (dim == 6 ? 8 : 0) | (alpha ? 4 : 0) | (normal ? 2 : 0) | (srgb ? 1 : 0);
 }
 
+// Register caps: <= 128 registers (4 CTAs of 128 per SM) for everything but
+// the FP32 6x6 pipeline, whose 36 FP32 texels are fastest kept in registers
+// (the plain kernel measured the same way: see the kernel-choice table).
 template <int DIM, bool ALPHA, bool NORMAL, bool SRGB, int PREC>
-__global__ void __launch_bounds__(kBatchThreads, (PREC == ASTC_PRECISION_FP32 && DIM == 4) ? 4 : 1)
+__global__ void __launch_bounds__(kBatchThreads, (PREC == ASTC_PRECISION_FP32 && DIM == 6) ? 1 : 4)
 astc_encode_persistent(const BatchJob* __restrict__ jobs, const WorkItem* __restrict__ items,
                        QueueState* __restrict__ q, int fmt) {
     constexpr int N = DIM * DIM;

@@ -59,6 +59,10 @@ def _parse():
     ap.add_argument("--no-serving", action="store_true", help="skip the serving sweep")
     ap.add_argument("--serving-rates", default="100,1000,5000,20000,50000,100000",
                     help="offered request rates (req/s)")
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "half2"],
+                    help="precision of the main workload")
+    ap.add_argument("--profile-batched", action="store_true",
+                    help="small case for ncu: one FP32 and one HALF2 batched graph launch")
     ap.add_argument("--profile-case", action="store_true",
                     help="small case for ncu: 2 textures per step, encode launches only")
     return ap.parse_args()
@@ -440,28 +444,51 @@ def run_ours(args) -> None:
     work_stream = torch.cuda.Stream()
     torch.cuda.set_stream(work_stream)
 
+    if args.profile_batched:
+        # the mixed batch, one FP32 and one HALF2 graph launch; nothing else
+        from astc_encoder_gb300 import synth_gpu
+        texs_b = synth_gpu.mixed_batch(torch, native, args.batched_count)
+        items, n_blocks = [], 0
+        keep = []
+        for t in texs_b:
+            d = t["opts"]["block_dim"]
+            for lw, lh, lvl in t["levels"]:
+                nb = ((lw + d - 1) // d) * ((lh + d - 1) // d)
+                o = torch.empty((nb, 16), dtype=torch.uint8, device="cuda")
+                keep.append(o)
+                items.append(dict(rgba8=lvl.data_ptr(), width=lw, height=lh, out=o.data_ptr(), **t["opts"]))
+                n_blocks += nb
+        with native.Batch(len(items), n_blocks) as b:
+            for prec in (0, 1):
+                b.encode(items, precision=prec, stream=work_stream.cuda_stream)
+            torch.cuda.synchronize()
+        print(json.dumps({"profile_batched": len(items), "blocks": n_blocks}), flush=True)
+        return
+
     img, spec = synth.workload(args.workload)
     h, w = img.shape[:2]
     dim = spec["block_dim"]
     nblocks = ((w + dim - 1) // dim) * ((h + dim - 1) // dim)
+    prec = 1 if args.precision == "half2" else 0
     # the autotuner picks the kernel variant (texel store, CTA size) for this format
     tuned = native.autotune(dim, spec["has_alpha"], spec["is_normal"], spec["srgb"], w, h)
     texs = _texture_batch(torch, img, 2 if args.profile_case else TEXTURES_PER_STEP, salt=rank)
     outs = [torch.empty((nblocks, 16), dtype=torch.uint8, device="cuda") for _ in texs]
+    spec_run = dict(spec, precision=prec)
 
     if args.profile_case:
         # only the encode launches: warm-up, then the timed steps; no other kernels
-        _time_launches(torch, native, texs, outs, spec, max(3, args.warmup))
-        per, _, launches = _time_launches(torch, native, texs, outs, spec, args.steps)
+        _time_launches(torch, native, texs, outs, spec_run, max(3, args.warmup))
+        per, _, launches = _time_launches(torch, native, texs, outs, spec_run, args.steps)
         print(json.dumps({"profile_case": args.workload, "launches": launches,
                           "mean_launch_us": per * 1e3}), flush=True)
         return
 
     # warm-up (untimed) + a short sustained burn so clocks settle
-    _time_launches(torch, native, texs, outs, spec, max(3, args.warmup))
+    _time_launches(torch, native, texs, outs, spec_run, max(3, args.warmup))
     t_end = time.perf_counter() + 0.5
     while time.perf_counter() < t_end:
-        _time_launches(torch, native, texs, outs, spec, 2)
+        _time_launches(torch, native, texs, outs, spec_run, 2)
 
     clocks = ClockSampler(local)
     if world > 1:
@@ -469,7 +496,7 @@ def run_ours(args) -> None:
     torch.cuda.synchronize()
     clocks.start()
     t0 = time.perf_counter()
-    per, per_step, launches = _time_launches(torch, native, texs, outs, spec, args.steps)
+    per, per_step, launches = _time_launches(torch, native, texs, outs, spec_run, args.steps)
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
     clk = clocks.stop()
@@ -485,7 +512,7 @@ def run_ours(args) -> None:
     host_in = [t.cpu().pin_memory() for t in texs]
     host_out = [torch.empty((nblocks, 16), dtype=torch.uint8).pin_memory() for _ in texs]
     lib = native.load_library()
-    opts = native.make_opts(memory=native.Memory.HOST, **spec)
+    opts = native.make_opts(memory=native.Memory.HOST, **spec_run)
 
     def e2e_step():
         for hi, ho in zip(host_in, host_out):
@@ -524,8 +551,8 @@ def run_ours(args) -> None:
     flops = oracle.flops_per_block(dim, spec["has_alpha"], spec["is_normal"]) * nblocks
     fp32_peak = _fp32_peak_tflops(torch)
     achieved_tf = flops / mean_launch_s / 1e12
-    kernel = (f"astc_encode_blocks_fp32<{dim},{int(spec['has_alpha'])},{int(spec['is_normal'])},"
-              f"{int(spec['srgb'])}>")
+    kernel = (f"astc_encode_blocks_{'h2' if prec else 'fp32'}<{dim},{int(spec['has_alpha'])},"
+              f"{int(spec['is_normal'])},{int(spec['srgb'])}>")
 
     # quality of this workload: CUDA vs FP32 oracle (identical blocks) and
     # PSNR of both against the FP64 twin's PSNR, decoded by the GPU decoder
@@ -580,7 +607,7 @@ def run_ours(args) -> None:
         "config": {"workload": args.workload, "texture": f"{w}x{h}", "blocks_per_texture": nblocks,
                    "textures_per_step": len(texs), "block_dim": dim, "has_alpha": spec["has_alpha"],
                    "is_normal": spec["is_normal"], "srgb": spec["srgb"],
-                   "border": "clamp" if spec["border"] else "zero", "precision": "fp32",
+                   "border": "clamp" if spec["border"] else "zero", "precision": args.precision,
                    "l2": f"inputs {texels_step * 4 / 2**20:.0f} MiB per step, distinct per texture "
                          "(> 129 MB L2); no flush needed",
                    "parallelism": f"replicas{world}",
