@@ -164,6 +164,8 @@ def load_library() -> ctypes.CDLL:
     lib.astc_generate_mips.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                        ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
     lib.astc_generate_mips.restype = ctypes.c_int
+    lib.astc_get_device_caps.argtypes = [ctypes.POINTER(DeviceCaps)]
+    lib.astc_get_device_caps.restype = ctypes.c_int
     vpp = ctypes.POINTER(ctypes.c_void_p)
     lib.astc_server_create.argtypes = [ctypes.POINTER(ServerConfig), vpp]
     lib.astc_server_create.restype = ctypes.c_int
@@ -182,6 +184,19 @@ def load_library() -> ctypes.CDLL:
     lib.astc_server_destroy.restype = ctypes.c_int
     _LIB = lib
     return lib
+
+
+class DeviceCaps(ctypes.Structure):
+    """``astc_device_caps`` of include/astc_gb300.h."""
+    _fields_ = [(n, ctypes.c_int) for n in ("sm_count", "l2_bytes", "unified_addressing", "can_map_host_memory",
+                                            "pageable_memory_access", "pageable_uses_host_page_tables",
+                                            "zero_copy")]
+
+
+def device_caps() -> dict:
+    c = DeviceCaps()
+    _check(load_library().astc_get_device_caps(ctypes.byref(c)))
+    return {n: getattr(c, n) for n, _ in DeviceCaps._fields_}
 
 
 class ServerConfig(ctypes.Structure):

@@ -175,8 +175,10 @@ astc_status check_ptr(astc_batch* b, const void* p, const char* what) {
         cudaGetLastError();
         return set_error(ASTC_ERR_INVALID_ARG, std::string(what) + " is not a CUDA pointer");
     }
-    if (a.type != cudaMemoryTypeDevice && a.type != cudaMemoryTypeManaged)
-        return set_error(ASTC_ERR_INVALID_ARG, std::string(what) + " is not device memory");
+    // device or managed memory, or the device view of pinned host memory
+    const bool host_view = a.type == cudaMemoryTypeHost && a.devicePointer == p;
+    if (a.type != cudaMemoryTypeDevice && a.type != cudaMemoryTypeManaged && !host_view)
+        return set_error(ASTC_ERR_INVALID_ARG, std::string(what) + " is not device-accessible memory");
     if (b->validated.size() > 65536) b->validated.clear();
     b->validated.insert(key);
     return ASTC_OK;

@@ -12,6 +12,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <atomic>
@@ -92,6 +93,32 @@ astc_status check_device_pointer(const void* ptr, const char* what) {
                          std::string(what) + " is not device memory (memory = ASTC_MEMORY_DEVICE)");
     return ASTC_OK;
 }
+
+// Device view of a pinned (page-locked, device-mapped) host buffer, or NULL
+// for any other buffer.  Under unified addressing every pinned allocation is
+// mapped; ASTC_GB300_ZERO_COPY=0 turns the zero-copy path off.
+bool zero_copy_enabled() {
+    static const bool on = [] {
+        const char* v = getenv("ASTC_GB300_ZERO_COPY");
+        return !(v && v[0] == '0');
+    }();
+    return on;
+}
+
+}  // namespace
+
+const void* pinned_device_view(const void* host) {
+    if (!host || !zero_copy_enabled()) return nullptr;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, host) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a.type != cudaMemoryTypeHost || a.devicePointer == nullptr) return nullptr;
+    return a.devicePointer;
+}
+
+namespace {
 
 astc_status validate_opts(const astc_opts* o, int w, int h) {
     if (!o) return set_error(ASTC_ERR_INVALID_ARG, "opts is NULL");
@@ -196,21 +223,37 @@ astc_status astc_encode_gpu_pitched(const uint8_t* rgba8, int width, int height,
             return ASTC_OK;
         }
 
-        // host memory: stage through the pool (tight rows on the device)
-        const size_t tight = (size_t)width * 4;
-        if ((st = grow(&pool->d_in, &pool->in_cap, tight * height)) != ASTC_OK) return st;
-        if ((st = grow(&pool->d_out, &pool->out_cap, out_bytes)) != ASTC_OK) return st;
+        // host memory: pinned buffers are read / written in place through their
+        // device view (zero-copy over the host link); other buffers are staged
+        // through the pool (tight rows on the device)
         (void)in_bytes;
-        cudaError_t e = cudaMemcpy2DAsync(pool->d_in, tight, rgba8, row_pitch, tight, height,
-                                          cudaMemcpyHostToDevice, s);
-        if (e != cudaSuccess) return cuda_error(e, "host-to-device copy");
-        job.in = pool->d_in;
-        job.pitch = tight;
-        job.out = pool->d_out;
+        const size_t tight = (size_t)width * 4;
+        const void* in_view = pinned_device_view(rgba8);
+        void* out_view = const_cast<void*>(pinned_device_view(out));
+        if (out_view && reinterpret_cast<uintptr_t>(out_view) % 16 != 0) out_view = nullptr;
+        cudaError_t e = cudaSuccess;
+        if (in_view && reinterpret_cast<uintptr_t>(in_view) % 4 == 0) {
+            job.in = static_cast<const uint8_t*>(in_view);
+            job.pitch = row_pitch;
+        } else {
+            if ((st = grow(&pool->d_in, &pool->in_cap, tight * height)) != ASTC_OK) return st;
+            e = cudaMemcpy2DAsync(pool->d_in, tight, rgba8, row_pitch, tight, height, cudaMemcpyHostToDevice, s);
+            if (e != cudaSuccess) return cuda_error(e, "host-to-device copy");
+            job.in = pool->d_in;
+            job.pitch = tight;
+        }
+        if (out_view) {
+            job.out = static_cast<uint8_t*>(out_view);
+        } else {
+            if ((st = grow(&pool->d_out, &pool->out_cap, out_bytes)) != ASTC_OK) return st;
+            job.out = pool->d_out;
+        }
         e = launch(job, s);
         if (e != cudaSuccess) return cuda_error(e, "encode kernel launch");
-        e = cudaMemcpyAsync(out, pool->d_out, out_bytes, cudaMemcpyDeviceToHost, s);
-        if (e != cudaSuccess) return cuda_error(e, "device-to-host copy");
+        if (!out_view) {
+            e = cudaMemcpyAsync(out, pool->d_out, out_bytes, cudaMemcpyDeviceToHost, s);
+            if (e != cudaSuccess) return cuda_error(e, "device-to-host copy");
+        }
         // The pooled buffers are reused by the next call: finish before returning.
         e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) return cuda_error(e, "encode");
@@ -392,6 +435,26 @@ astc_status astc_sse_gpu(const uint8_t* a, const uint8_t* b, size_t texels, int 
     } catch (...) {
         return set_error(ASTC_ERR_CUDA, "unexpected exception");
     }
+}
+
+astc_status astc_get_device_caps(astc_device_caps* caps) {
+    if (!caps) return set_error(ASTC_ERR_INVALID_ARG, "NULL caps");
+    memset(caps, 0, sizeof(*caps));
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_error(e, "cudaGetDevice");
+    struct Q { cudaDeviceAttr a; int* v; } qs[] = {
+        {cudaDevAttrMultiProcessorCount, &caps->sm_count},
+        {cudaDevAttrL2CacheSize, &caps->l2_bytes},
+        {cudaDevAttrUnifiedAddressing, &caps->unified_addressing},
+        {cudaDevAttrCanMapHostMemory, &caps->can_map_host_memory},
+        {cudaDevAttrPageableMemoryAccess, &caps->pageable_memory_access},
+        {cudaDevAttrPageableMemoryAccessUsesHostPageTables, &caps->pageable_uses_host_page_tables},
+    };
+    for (const Q& q : qs)
+        if ((e = cudaDeviceGetAttribute(q.v, q.a, dev)) != cudaSuccess) return cuda_error(e, "cudaDeviceGetAttribute");
+    caps->zero_copy = zero_copy_enabled() && caps->unified_addressing && caps->can_map_host_memory;
+    return ASTC_OK;
 }
 
 const char* astc_last_error(void) { return t_last_error.c_str(); }

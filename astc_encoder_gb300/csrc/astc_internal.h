@@ -46,5 +46,7 @@ cudaError_t launch_sse(const uint8_t* a, const uint8_t* b, size_t texels,
 astc_status set_error(astc_status st, const std::string& msg);
 astc_status cuda_error(cudaError_t e, const char* what);
 void count_launches(uint64_t n);
+// Device view of a pinned, device-mapped host buffer (zero-copy), else NULL.
+const void* pinned_device_view(const void* host);
 
 }  // namespace astc

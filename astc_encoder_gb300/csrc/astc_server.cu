@@ -90,6 +90,7 @@ struct Req {
     uint64_t id = 0;
     astc_request r{};
     size_t pitch = 0, in_bytes = 0, out_bytes = 0, off = 0, need = 0;
+    bool out_direct = false;        // blocks written straight into pinned host memory
     Clock::time_point t_submit, t_admit, t_done;
     int state = kQueued;
     astc_status status = ASTC_OK;
@@ -140,12 +141,24 @@ cudaError_t launch_slot(astc_server* s, Slot& slot) {
         uint8_t* d_in = s->d_pool + q->off;
         uint8_t* d_out = d_in + round_up(q->in_bytes);
         const size_t row = (size_t)q->r.width * 4;
-        e = cudaMemcpy2DAsync(d_in, row, q->r.rgba8, q->pitch, row, q->r.height, cudaMemcpyHostToDevice,
-                              slot.stream);
-        if (e != cudaSuccess) return e;
+        // pinned requests are read and written in place through their device
+        // views (zero-copy); the pool space stays reserved, so admission by
+        // memory behaves the same for every request
+        const void* in_view = pinned_device_view(q->r.rgba8);
+        void* out_view = const_cast<void*>(pinned_device_view(q->r.out));
+        q->out_direct = out_view && reinterpret_cast<uintptr_t>(out_view) % 16 == 0;
         astc_batch_item it;
-        it.rgba8 = d_in;
-        it.row_pitch = row;
+        if (in_view && reinterpret_cast<uintptr_t>(in_view) % 4 == 0 && q->pitch % 4 == 0) {
+            it.rgba8 = static_cast<const uint8_t*>(in_view);
+            it.row_pitch = q->pitch;
+        } else {
+            e = cudaMemcpy2DAsync(d_in, row, q->r.rgba8, q->pitch, row, q->r.height, cudaMemcpyHostToDevice,
+                                  slot.stream);
+            if (e != cudaSuccess) return e;
+            it.rgba8 = d_in;
+            it.row_pitch = row;
+        }
+        if (q->out_direct) d_out = static_cast<uint8_t*>(out_view);
         it.width = q->r.width;
         it.height = q->r.height;
         it.block_dim = q->r.block_dim;
@@ -180,6 +193,7 @@ cudaError_t launch_slot(astc_server* s, Slot& slot) {
         }
     }
     for (Req* q : slot.reqs) {
+        if (q->out_direct) continue;
         const uint8_t* d_out = s->d_pool + q->off + round_up(q->in_bytes);
         e = cudaMemcpyAsync(q->r.out, d_out, q->out_bytes, cudaMemcpyDeviceToHost, slot.stream);
         if (e != cudaSuccess) return e;

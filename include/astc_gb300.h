@@ -269,6 +269,22 @@ astc_status astc_get_kernel_choice(int block_dim, int has_alpha, int is_normal, 
 astc_status astc_sse_gpu_noalloc(const uint8_t* a, const uint8_t* b, size_t texels,
                                  void* stream, uint64_t* sse_rgba);
 
+/* What the current device offers the host-memory paths.  (No counterpart in
+ * the reference.)  With `zero_copy` set, host-memory calls whose buffers are
+ * pinned (page-locked and device-mapped) let the kernels read texels and
+ * write blocks directly through the host link instead of staging them in
+ * device memory; other host buffers are staged. */
+typedef struct astc_device_caps {
+    int sm_count;
+    int l2_bytes;
+    int unified_addressing;          /* pinned host memory has a device view    */
+    int can_map_host_memory;
+    int pageable_memory_access;      /* reported only; pageable buffers are staged */
+    int pageable_uses_host_page_tables;
+    int zero_copy;                   /* the library uses zero-copy for pinned buffers */
+} astc_device_caps;
+astc_status astc_get_device_caps(astc_device_caps* caps);
+
 /* Message for the last failed call on this thread ("" if none). */
 const char* astc_last_error(void);
 const char* astc_status_string(astc_status status);

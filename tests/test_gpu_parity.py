@@ -6,6 +6,7 @@ construction).  The acceptance floor from the benchmark spec (>= 99.9% identical
 blocks, PSNR within 0.01 dB) is also asserted separately so a regression
 shows up as the right failure.
 """
+import ctypes
 import itertools
 import os
 
@@ -203,3 +204,52 @@ def test_autotune_installs_a_valid_choice(native, oracle):
         assert np.array_equal(native.encode(img, **opts), oracle.encode(img, **opts))
     finally:
         native.set_kernel_choice(6, True, False, True, *saved)
+
+
+def test_host_memory_zero_copy_paths(native, oracle):
+    """Pinned (device-mapped) host buffers are read/written in place; the blocks
+    are the same as for pageable buffers, for every pinned/pageable mix."""
+    import torch
+    caps = native.device_caps()
+    assert caps["sm_count"] > 0 and caps["unified_addressing"] == 1
+    img = _texture(131, 77, seed=41)
+    for opts in (dict(block_dim=4, has_alpha=True), dict(block_dim=6, has_alpha=True, srgb=True, border=1)):
+        want = oracle.encode(img, **opts)
+        pin_in = torch.from_numpy(img).pin_memory()
+        pin_out = torch.zeros(want.shape, dtype=torch.uint8).pin_memory()
+        lib = native.load_library()
+        o = native.make_opts(memory=native.Memory.HOST, **opts)
+        page_out = np.zeros_like(want)
+        for src, dst, arr in ((pin_in.data_ptr(), pin_out.data_ptr(), pin_out),
+                              (pin_in.data_ptr(), page_out.ctypes.data, page_out),
+                              (img.ctypes.data, pin_out.data_ptr(), pin_out)):
+            if isinstance(arr, torch.Tensor):
+                arr.zero_()
+            else:
+                arr[:] = 0
+            st = lib.astc_encode_gpu(src, 77, 131, ctypes.byref(o), dst)
+            assert st == 0, lib.astc_last_error()
+            got = arr.numpy() if isinstance(arr, torch.Tensor) else arr
+            assert np.array_equal(got, want), opts
+        # a row-pitched view into a larger pinned image
+        wide = torch.zeros((131, 100, 4), dtype=torch.uint8).pin_memory()
+        wide[:, :77] = torch.from_numpy(img)
+        pin_out.zero_()
+        st = lib.astc_encode_gpu_pitched(wide.data_ptr(), 77, 131, 400, ctypes.byref(o), pin_out.data_ptr())
+        assert st == 0 and np.array_equal(pin_out.numpy(), want)
+
+
+def test_server_with_pinned_requests(native):
+    import torch
+    imgs = [_texture(97 + 13 * i, 61 + 7 * i, seed=i) for i in range(12)]
+    opts = dict(block_dim=6, has_alpha=True, srgb=True, border=1)
+    pins = [torch.from_numpy(im).pin_memory() for im in imgs]
+    outs = [torch.zeros((((im.shape[1] + 5) // 6) * ((im.shape[0] + 5) // 6), 16), dtype=torch.uint8).pin_memory()
+            for im in imgs]
+    with native.Server(pool_bytes=16 << 20, max_batch=8, inflight=2) as srv:
+        tickets = [srv.submit(native.make_request(p.data_ptr(), im.shape[1], im.shape[0], o.data_ptr(), **opts))
+                   for p, im, o in zip(pins, imgs, outs)]
+        for t in tickets:
+            srv.wait(t)
+    for im, o in zip(imgs, outs):
+        assert np.array_equal(o.numpy(), native.encode(im, **opts))
