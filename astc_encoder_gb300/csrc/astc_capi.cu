@@ -254,7 +254,10 @@ astc_status astc_encode_gpu_pitched(const uint8_t* rgba8, int width, int height,
             e = cudaMemcpyAsync(out, pool->d_out, out_bytes, cudaMemcpyDeviceToHost, s);
             if (e != cudaSuccess) return cuda_error(e, "device-to-host copy");
         }
-        // The pooled buffers are reused by the next call: finish before returning.
+        // Fully zero-copy calls touch no pooled buffer, so with a caller's stream
+        // they stay asynchronous; otherwise the pool is reused by the next call
+        // and the call finishes before returning.
+        if (job.in != pool->d_in && out_view && opts->stream) return ASTC_OK;
         e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) return cuda_error(e, "encode");
         return ASTC_OK;

@@ -90,7 +90,11 @@ size_t astc_encoded_size(int width, int height, int block_dim);
 /* Encode one RGBA8 image (tightly packed rows, row 0 first, 4 bytes per
  * texel) into 16-byte ASTC blocks in row-major block order.
  * Replaces encode_astc (astc_encode.h:87) + read_gpu (astc_save.h:34).
- * `out` must hold astc_encoded_size(width, height, opts->block_dim) bytes. */
+ * `out` must hold astc_encoded_size(width, height, opts->block_dim) bytes.
+ * Host memory: pinned buffers are accessed in place by the kernel
+ * (zero-copy), others are staged; the call returns when `out` is written,
+ * except when both buffers are pinned and opts->stream is set -- then it is
+ * asynchronous on that stream like a device-memory call. */
 astc_status astc_encode_gpu(const uint8_t* rgba8, int width, int height,
                             const astc_opts* opts, uint8_t* out);
 
