@@ -66,10 +66,12 @@ inline int format_index(int dim, bool alpha, bool normal, bool srgb) {
 }
 
 // Register caps: <= 128 registers (4 CTAs of 128 per SM) for everything but
-// the FP32 6x6 pipeline, whose 36 FP32 texels are fastest kept in registers
-// (the plain kernel measured the same way: see the kernel-choice table).
+// the FP32 6x6 pipeline, whose 36 FP32 texels spill heavily at 128; it takes
+// 3 CTAs per SM (<= 168 registers; the queue loop leaves 80-250 bytes of
+// L1-resident spill in the colour formats), which on GB300 ran the mixed
+// 256-texture batch at 211 Gtexel/s against 206 with one CTA per SM.
 template <int DIM, bool ALPHA, bool NORMAL, bool SRGB, int PREC>
-__global__ void __launch_bounds__(kBatchThreads, (PREC == ASTC_PRECISION_FP32 && DIM == 6) ? 1 : 4)
+__global__ void __launch_bounds__(kBatchThreads, (PREC == ASTC_PRECISION_FP32 && DIM == 6) ? 3 : 4)
 astc_encode_persistent(const BatchJob* __restrict__ jobs, const WorkItem* __restrict__ items,
                        QueueState* __restrict__ q, int fmt) {
     constexpr int N = DIM * DIM;

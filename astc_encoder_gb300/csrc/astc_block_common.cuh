@@ -140,7 +140,9 @@ __device__ __forceinline__ void load_block_packed(const TextureView& p, int bx, 
 // ---------------------------------------------------------------------------
 // texel stores: where the decoded FP32 texels of one block live
 // ---------------------------------------------------------------------------
-enum TexelStore : int { kStoreRegisters = 0, kStoreShared = 1 };
+// registers / shared memory / registers with the count capped near 168 (three
+// 128-thread CTAs per SM) so the compiler trades a little spilling for warps
+enum TexelStore : int { kStoreRegisters = 0, kStoreShared = 1, kStoreRegistersCapped = 2 };
 
 template <int N>
 struct RegTexels {

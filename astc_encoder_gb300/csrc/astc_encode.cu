@@ -50,7 +50,8 @@ struct Launch {
 // registers) so the compiler re-reads texels from shared memory instead of
 // holding all of them in registers across the passes.
 template <int DIM, bool ALPHA, bool NORMAL, bool SRGB, int STORE>
-__global__ void __launch_bounds__(kMaxThreads, STORE == kStoreShared ? 2 : 1)
+__global__ void __launch_bounds__(STORE == kStoreRegistersCapped ? 128 : kMaxThreads,
+                                  STORE == kStoreShared ? 2 : (STORE == kStoreRegistersCapped ? 3 : 1))
 astc_encode_blocks_fp32(const Launch p) {
     constexpr int N = DIM * DIM;
     extern __shared__ float4 s_texels[];                  // kStoreShared only
@@ -84,13 +85,15 @@ Choice g_choice[2][2][2][2] = {};     // [dim6][alpha][normal][srgb]
 bool g_choice_init = false;
 std::mutex g_choice_mu;
 
-// GB300 sweep over 2048x2048 textures (us per launch, registers / shared at
-// 128 threads): 4x4 RGB 28.4 / 27.0, 4x4 RGBA sRGB 29.0 / 28.9, 4x4 normal
-// 20.8 / 20.8, 6x6 RGBA sRGB 26.8 / 39.1, 6x6 RGB 24.8 / 40.9.  The capped
-// shared-memory variant loses for 6x6 (its re-reads cost more than the
-// occupancy it gains) and ties or wins slightly for 4x4.
+// GB300 sweep over 2048x2048 textures (us per launch at 128 threads;
+// registers / shared / capped registers): 4x4 RGB 29.0 / 27.1 / 28.9,
+// 4x4 RGBA sRGB 29.0 / 29.0 / 29.0, 4x4 normal 20.8 / 20.9 / 20.8,
+// 6x6 RGBA sRGB 26.8 / 39.1 / 24.0, 6x6 RGB 24.9 / 41.0 / 22.9.  The
+// shared-memory store loses for 6x6 (its re-reads cost more than the
+// occupancy it gains); capping the register store at 168 (no spills) lifts
+// 6x6 from 8 to 12 warps per SM.
 Choice default_choice(int dim, bool /*alpha*/, bool /*normal*/, bool /*srgb*/) {
-    return dim == 6 ? Choice{kStoreRegisters, 128} : Choice{kStoreShared, 128};
+    return dim == 6 ? Choice{kStoreRegistersCapped, 128} : Choice{kStoreShared, 128};
 }
 
 template <int DIM, bool ALPHA, bool NORMAL, bool SRGB, int STORE>
@@ -112,6 +115,8 @@ template <int DIM, bool ALPHA, bool NORMAL, bool SRGB>
 cudaError_t launch_store(const Launch& p, const Choice& c, cudaStream_t s) {
     if (c.store == kStoreShared)
         return launch_t<DIM, ALPHA, NORMAL, SRGB, kStoreShared>(p, c.threads, s);
+    if (c.store == kStoreRegistersCapped)
+        return launch_t<DIM, ALPHA, NORMAL, SRGB, kStoreRegistersCapped>(p, c.threads, s);
     return launch_t<DIM, ALPHA, NORMAL, SRGB, kStoreRegisters>(p, c.threads, s);
 }
 template <int DIM, bool ALPHA, bool NORMAL>
@@ -162,7 +167,9 @@ TextureView make_view(const EncodeJob& j) {
 
 cudaError_t launch_encode_variant(const EncodeJob& j, int store, int threads, cudaStream_t stream) {
     if (threads != 32 && threads != 64 && threads != 128 && threads != 256) return cudaErrorInvalidValue;
-    if (store != kStoreRegisters && store != kStoreShared) return cudaErrorInvalidValue;
+    if (store != kStoreRegisters && store != kStoreShared && store != kStoreRegistersCapped)
+        return cudaErrorInvalidValue;
+    if (store == kStoreRegistersCapped && threads > 128) return cudaErrorInvalidValue;
     Launch p;
     p.tex = make_view(j);
     p.nblocks = (long long)p.tex.nbx * blocks_y(j.height, j.block_dim);

@@ -1,11 +1,11 @@
 // astc_tune.cu -- autotuner for the encode kernel variants.
 //
 // The encoder has one thread per ASTC block (the reference's mapping,
-// ASTC_Encode.hlsl:553-561) and two places to keep a block's decoded texels:
-// registers (best when they fit, 4x4) or a [texel][thread] shared-memory
-// array (6x6: 36 float4 per block would otherwise hold the register count
-// near 255 and the SM near 8 warps).  The CTA size trades scheduling slack
-// against shared memory.  astc_autotune times every (store, CTA size)
+// ASTC_Encode.hlsl:553-561) and three ways to keep a block's decoded texels:
+// registers, a [texel][thread] shared-memory array, or registers with the
+// count capped near 168 (6x6: 36 float4 per block otherwise hold the register
+// count near 255 and the SM near 8 warps).  The CTA size trades scheduling
+// slack against shared memory.  astc_autotune times every (store, CTA size)
 // candidate for a format on a synthetic texture of the caller's size on the
 // current device and installs the fastest for that format in this process.
 #include <cuda_runtime.h>
@@ -44,7 +44,9 @@ extern "C" {
 astc_status astc_set_kernel_choice(int block_dim, int has_alpha, int is_normal, int srgb, int store,
                                    int threads) {
     if (block_dim != 4 && block_dim != 6) return set_error(ASTC_ERR_INVALID_ARG, "block_dim must be 4 or 6");
-    if (store != 0 && store != 1) return set_error(ASTC_ERR_INVALID_ARG, "store must be 0 or 1");
+    if (store < 0 || store > 2) return set_error(ASTC_ERR_INVALID_ARG, "store must be 0, 1 or 2");
+    if (store == 2 && threads > 128)
+        return set_error(ASTC_ERR_INVALID_ARG, "the capped-register store takes at most 128 threads");
     if (threads != 32 && threads != 64 && threads != 128 && threads != 256)
         return set_error(ASTC_ERR_INVALID_ARG, "threads must be 32, 64, 128 or 256");
     set_encode_choice(block_dim, has_alpha != 0, is_normal != 0, srgb != 0, store, threads);
@@ -104,12 +106,13 @@ astc_status astc_autotune(int block_dim, int has_alpha, int is_normal, int srgb,
         job.out = d_out;
         int def_store = 0, def_threads = 128;
         get_encode_choice(block_dim, has_alpha != 0, is_normal != 0, srgb != 0, &def_store, &def_threads);
-        const int stores[2] = {0, 1};
+        const int stores[3] = {0, 1, 2};
         const int sizes[3] = {64, 128, 256};
         float best = 1e30f, def_us = -1.0f;
         int best_store = def_store, best_threads = def_threads;
-        for (int si = 0; si < 2 && st == ASTC_OK; ++si)
+        for (int si = 0; si < 3 && st == ASTC_OK; ++si)
             for (int ti = 0; ti < 3 && st == ASTC_OK; ++ti) {
+                if (stores[si] == 2 && sizes[ti] > 128) continue;      // capped store: <= 128 threads
                 for (int w = 0; w < 2; ++w)
                     if ((e = launch_encode_variant(job, stores[si], sizes[ti], s)) != cudaSuccess) break;
                 if (e != cudaSuccess) { st = cuda_error(e, "variant launch"); break; }

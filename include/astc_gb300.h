@@ -234,7 +234,8 @@ astc_status astc_sse_gpu(const uint8_t* a, const uint8_t* b, size_t texels,
                          int memory, void* stream, uint64_t sse_rgba[4]);
 
 /* Kernel variant of a format: where a block's decoded texels live
- * (store 0 = registers, 1 = shared memory) and the CTA size (32/64/128/256).
+ * (store 0 = registers, 1 = shared memory, 2 = registers with the count
+ * capped for occupancy, at most 128 threads) and the CTA size (32/64/128/256).
  * Every variant produces identical blocks; they differ in speed only.
  * (No counterpart in the reference, whose shader has one fixed mapping,
  * [numthreads(8,8,1)] at ASTC_Encode.hlsl:553.) */

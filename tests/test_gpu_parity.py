@@ -184,8 +184,10 @@ def test_every_kernel_variant_bit_exact(native, oracle, dim, alpha, normal, srgb
     want = oracle.encode(img, **opts)
     saved = native.get_kernel_choice(dim, alpha, normal, srgb)
     try:
-        for store in (0, 1):
+        for store in (0, 1, 2):
             for threads in (32, 64, 128, 256):
+                if store == 2 and threads > 128:
+                    continue
                 native.set_kernel_choice(dim, alpha, normal, srgb, store, threads)
                 assert np.array_equal(native.encode(img, **opts), want), (store, threads)
     finally:
@@ -196,7 +198,7 @@ def test_autotune_installs_a_valid_choice(native, oracle):
     saved = native.get_kernel_choice(6, True, False, True)
     try:
         r = native.autotune(6, True, False, True, 512, 384)
-        assert r.store in (0, 1) and r.threads in (64, 128, 256)
+        assert r.store in (0, 1, 2) and r.threads in (64, 128, 256)
         assert 0 < r.best_us <= r.default_us
         assert native.get_kernel_choice(6, True, False, True) == (r.store, r.threads)
         img = _texture(130, 70, seed=77)
