@@ -22,7 +22,7 @@ from typing import Any
 import numpy as np
 
 __all__ = [
-    "AstcError", "Status", "Border", "Precision", "Memory", "EncodeOption", "AstcOpts",
+    "AstcError", "Status", "Border", "Precision", "Memory", "Axis", "Quality", "EncodeOption", "AstcOpts",
     "library_path", "load_library", "encoded_size", "encode", "encode_astc", "encode_device",
     "save_astc", "load_astc", "decode", "decode_device", "sse", "psnr_from_sse",
     "kernel_launch_count", "shutdown",
@@ -59,6 +59,16 @@ class Memory(enum.IntEnum):
     DEVICE = 1
 
 
+class Axis(enum.IntEnum):
+    PCA = 0                 # principal_component_analysis (ASTC_Encode.hlsl:514)
+    MAX_ACCUMULATION = 1    # max_accumulation_pixel_direction (170-227, unused there)
+
+
+class Quality(enum.IntEnum):
+    FAST = 0                # the reference's fixed mode (518-522)
+    SEARCH = 1              # every single-partition 4x4-grid mode, least decoded error
+
+
 class AstcError(RuntimeError):
     def __init__(self, status: int, message: str):
         self.status = Status(status) if status in Status._value2member_map_ else status
@@ -76,6 +86,8 @@ class AstcOpts(ctypes.Structure):
         ("precision", ctypes.c_int),
         ("memory", ctypes.c_int),
         ("stream", ctypes.c_void_p),
+        ("axis", ctypes.c_int),
+        ("quality", ctypes.c_int),
     ]
 
 
@@ -393,7 +405,8 @@ def _check(status: int) -> None:
 
 def make_opts(block_dim: int = 4, has_alpha: bool = False, is_normal: bool = False,
               srgb: bool = False, border: int = Border.ZERO, precision: int = Precision.FP32,
-              memory: int = Memory.HOST, stream: int | None = None) -> AstcOpts:
+              memory: int = Memory.HOST, stream: int | None = None, axis: int = Axis.PCA,
+              quality: int = Quality.FAST) -> AstcOpts:
     o = AstcOpts()
     load_library().astc_opts_init(ctypes.byref(o))
     o.block_dim = int(block_dim)
@@ -404,6 +417,8 @@ def make_opts(block_dim: int = 4, has_alpha: bool = False, is_normal: bool = Fal
     o.precision = int(precision)
     o.memory = int(memory)
     o.stream = stream or None
+    o.axis = int(axis)
+    o.quality = int(quality)
     return o
 
 
@@ -413,7 +428,8 @@ def encoded_size(width: int, height: int, block_dim: int) -> int:
 
 def encode(rgba: np.ndarray, block_dim: int = 4, has_alpha: bool = False, is_normal: bool = False,
            srgb: bool = False, border: int = Border.ZERO, precision: int = Precision.FP32,
-           out: np.ndarray | None = None) -> np.ndarray:
+           out: np.ndarray | None = None, axis: int = Axis.PCA,
+           quality: int = Quality.FAST) -> np.ndarray:
     """Encode a host (H, W, 4) uint8 image; returns (nblocks, 16) uint8 blocks."""
     a = np.asarray(rgba)
     if a.dtype != np.uint8 or a.ndim != 3 or a.shape[2] != 4:
@@ -427,7 +443,7 @@ def encode(rgba: np.ndarray, block_dim: int = 4, has_alpha: bool = False, is_nor
         out = np.empty((n // 16, 16), np.uint8)
     elif out.nbytes != n or not out.flags.c_contiguous or out.dtype != np.uint8:
         raise AstcError(Status.INVALID_ARG, "out has the wrong size or layout")
-    o = make_opts(block_dim, has_alpha, is_normal, srgb, border, precision, Memory.HOST)
+    o = make_opts(block_dim, has_alpha, is_normal, srgb, border, precision, Memory.HOST, None, axis, quality)
     _check(load_library().astc_encode_gpu(a.ctypes.data, w, h, ctypes.byref(o), out.ctypes.data))
     return out
 
@@ -442,12 +458,14 @@ def encode_astc(rgba: np.ndarray, option: EncodeOption | None = None, **kw: Any)
 def encode_device(rgba_ptr: int, width: int, height: int, out_ptr: int, block_dim: int = 4,
                   has_alpha: bool = False, is_normal: bool = False, srgb: bool = False,
                   border: int = Border.ZERO, precision: int = Precision.FP32,
-                  stream: int | None = None, row_pitch: int | None = None) -> None:
+                  stream: int | None = None, row_pitch: int | None = None, axis: int = Axis.PCA,
+                  quality: int = Quality.FAST) -> None:
     """Encode from device memory to device memory (pointers, e.g. tensor.data_ptr()).
 
     With ``stream`` (a cudaStream_t handle) the call is asynchronous on it.
     """
-    o = make_opts(block_dim, has_alpha, is_normal, srgb, border, precision, Memory.DEVICE, stream)
+    o = make_opts(block_dim, has_alpha, is_normal, srgb, border, precision, Memory.DEVICE, stream, axis,
+                  quality)
     pitch = row_pitch if row_pitch is not None else width * 4
     _check(load_library().astc_encode_gpu_pitched(rgba_ptr, width, height, pitch, ctypes.byref(o),
                                                   out_ptr))

@@ -130,6 +130,12 @@ astc_status validate_opts(const astc_opts* o, int w, int h) {
         return set_error(ASTC_ERR_INVALID_ARG, "precision must be FP32 or HALF2");
     if (o->memory != ASTC_MEMORY_HOST && o->memory != ASTC_MEMORY_DEVICE)
         return set_error(ASTC_ERR_INVALID_ARG, "memory must be ASTC_MEMORY_HOST or ASTC_MEMORY_DEVICE");
+    if (o->axis != ASTC_AXIS_PCA && o->axis != ASTC_AXIS_MAX_ACCUMULATION)
+        return set_error(ASTC_ERR_INVALID_ARG, "axis must be ASTC_AXIS_PCA or ASTC_AXIS_MAX_ACCUMULATION");
+    if (o->quality != ASTC_QUALITY_FAST && o->quality != ASTC_QUALITY_SEARCH)
+        return set_error(ASTC_ERR_INVALID_ARG, "quality must be ASTC_QUALITY_FAST or ASTC_QUALITY_SEARCH");
+    if (o->precision == ASTC_PRECISION_HALF2 && (o->axis != ASTC_AXIS_PCA || o->quality != ASTC_QUALITY_FAST))
+        return set_error(ASTC_ERR_UNSUPPORTED, "the max-accumulation axis and the mode search are FP32 only");
     if (w <= 0 || h <= 0) return set_error(ASTC_ERR_INVALID_ARG, "width and height must be positive");
     if (w > 0xFFFFFF || h > 0xFFFFFF)
         return set_error(ASTC_ERR_INVALID_ARG, "width and height must fit the 24-bit .astc size fields");
@@ -182,7 +188,9 @@ astc_status astc_encode_gpu_pitched(const uint8_t* rgba8, int width, int height,
         if (row_pitch < (size_t)width * 4 || row_pitch % 4 != 0)
             return set_error(ASTC_ERR_INVALID_ARG, "row_pitch must be >= 4*width and a multiple of 4");
         auto launch = [&](const EncodeJob& j, cudaStream_t st_) {
-            return opts->precision == ASTC_PRECISION_HALF2 ? launch_encode_h2(j, st_) : launch_encode(j, st_);
+            if (opts->precision == ASTC_PRECISION_HALF2) return launch_encode_h2(j, st_);
+            if (j.axis != ASTC_AXIS_PCA || j.quality != ASTC_QUALITY_FAST) return launch_encode_search(j, st_);
+            return launch_encode(j, st_);
         };
         DevicePool* pool = nullptr;
         int dev = 0;
@@ -203,6 +211,8 @@ astc_status astc_encode_gpu_pitched(const uint8_t* rgba8, int width, int height,
         job.srgb = opts->srgb;
         job.border = opts->border;
         job.precision = opts->precision;
+        job.axis = opts->axis;
+        job.quality = opts->quality;
 
         if (opts->memory == ASTC_MEMORY_DEVICE) {
             if ((st = check_device_pointer(rgba8, "rgba8")) != ASTC_OK) return st;

@@ -17,6 +17,7 @@ struct EncodeJob {
     int width, height;
     int block_dim;        // 4 or 6
     int has_alpha, is_normal, srgb, border, precision;
+    int axis = ASTC_AXIS_PCA, quality = ASTC_QUALITY_FAST;
     uint8_t* out;         // 16 * nblocks bytes, 16-byte aligned
 };
 
@@ -35,6 +36,8 @@ struct TextureView;
 TextureView make_view(const EncodeJob& job);
 // Packed-half2 pipeline (astc_encode_h2.cu).
 cudaError_t launch_encode_h2(const EncodeJob& job, cudaStream_t stream);
+// FP32 with the max-accumulation axis and/or the mode search (astc_encode_search.cu).
+cudaError_t launch_encode_search(const EncodeJob& job, cudaStream_t stream);
 
 // Decoder / SSE launchers (astc_decode.cu).
 cudaError_t launch_decode(const uint8_t* blocks, int width, int height, int bw, int bh,

@@ -1,0 +1,348 @@
+// astc_pipeline_search.cuh -- search mode of the FP32 encoder: the
+// choose_best_quantmethod that the reference shader sketches but leaves out
+// (niepp/astc_encoder ASTC_Encode.hlsl:524-526).
+//
+// After the endpoint fit (PCA, or the shader's unused
+// max_accumulation_pixel_direction), a block is encoded in the shader's fixed
+// mode and, besides, in every single-partition mode with a 4x4 weight grid:
+// weight ranges QUANT_3..QUANT_32, each with the endpoint range the decoder
+// derives from the bits left over (QUANT_256 down to QUANT_12).  A candidate
+// snaps the rounded endpoints to the nearest representable values (darker
+// one first, so the decoder neither swaps nor blue-contracts), projects the
+// grid colours onto the decoded endpoints and rounds the weights to the
+// range.  Every candidate is scored by the exact squared error of its spec
+// decode against the fit-space texels -- integers for UNORM input (exact
+// below 2^24), fused multiply-adds in texel-major, r-g-b-a order for sRGB --
+// and the first candidate with the least error is kept.  The oracle's search
+// mode follows the same steps, so blocks are bit-identical to it.
+#pragma once
+#include <type_traits>
+
+#include "astc_pipeline_fp32.cuh"
+
+namespace astc {
+
+// Decode steps the compiler may neither hoist nor merge across passes (a
+// merged decode would keep the block's 4 floats per texel live next to the
+// packed words): the byte_to_float permute and the sRGB table read.
+__device__ __forceinline__ float byte_to_float_fresh(uint32_t px, int c) {
+    uint32_t bits;
+    asm volatile("prmt.b32 %0, %1, %2, %3;" : "=r"(bits) : "r"(px), "r"(0x4B000000u), "r"(0x7440u + (uint32_t)c));
+    return __fsub_rn(__uint_as_float(bits), 8388608.0f);
+}
+
+__device__ __forceinline__ float lds_f32_volatile(const float* p) {
+    float v;
+    asm volatile("ld.shared.f32 %0, [%1];" : "=f"(v) : "r"((uint32_t)__cvta_generic_to_shared(p)));
+    return v;
+}
+
+// Texels re-decoded from their packed RGBA8 words on every read: 1 register
+// per texel instead of 4, for the passes over the block.  Same values as
+// decode_texel.
+template <int N, bool SRGB, bool NORMAL>
+struct PackedTexels {
+    const uint32_t (&px)[N];
+    const float* lut;
+    __device__ __forceinline__ float4 get(int k) const {
+        const uint32_t p = px[k];
+        float4 t;
+        if (SRGB) {
+            t.x = lds_f32_volatile(lut + (p & 0xFFu));
+            t.y = lds_f32_volatile(lut + ((p >> 8) & 0xFFu));
+            t.z = NORMAL ? 255.0f : lds_f32_volatile(lut + ((p >> 16) & 0xFFu));
+        } else {
+            t.x = byte_to_float_fresh(p, 0);
+            t.y = byte_to_float_fresh(p, 1);
+            t.z = NORMAL ? 255.0f : byte_to_float_fresh(p, 2);
+        }
+        t.w = NORMAL ? 255.0f : byte_to_float_fresh(p, 3);
+        return t;
+    }
+};
+
+// Per-CTA copies of the search tables (shared memory).
+struct SearchSmem {
+    uint16_t color[8][256];      // this format's endpoint ranges below QUANT_256
+    uint8_t wval[12][32];
+    uint8_t scramble[12][32];
+    uint8_t trits[256];
+    uint8_t quints[128];
+    int8_t cq[12];               // weight range -> endpoint range (-1: illegal)
+    int8_t slot[12];             // weight range -> row of color (-1: QUANT_256)
+    float lut[256];
+};
+
+// ---------------------------------------------------------------------------
+// general bounded integer sequence encoding (ISE) into a 128-bit field
+// ---------------------------------------------------------------------------
+struct Bits128 { uint64_t lo, hi; };
+
+__device__ __forceinline__ void put_bits(Bits128& b, int& pos, uint32_t v, int n) {
+    if (n > 0) {
+        const uint64_t x = v;
+        if (pos < 64) {
+            b.lo |= x << pos;
+            if (pos > 0 && pos + n > 64) b.hi |= x >> (64 - pos);
+        } else {
+            b.hi |= x << (pos - 64);
+        }
+    }
+    pos += n;
+}
+
+__device__ __forceinline__ void keep_low_bits(Bits128& b, int n) {
+    if (n < 64) { b.lo &= (n ? (~0ull >> (64 - n)) : 0ull); b.hi = 0; }
+    else if (n < 128) { b.hi &= (n > 64 ? (~0ull >> (128 - n)) : 0ull); }
+}
+
+// COUNT symbols of quant method `quant` (runtime), LSB first: groups of five
+// (trits: m0 T[1:0] m1 T[3:2] m2 T[4] m3 T[6:5] m4 T[7]) or three (quints:
+// m0 Q[2:0] m1 Q[4:3] m2 Q[6:5]) padded with zeros, or plain bit fields
+// (ASTC_IntegerSequenceEncoding.hlsl encode_trits 142-176, encode_quints
+// 181-205, bise_* 207-276), cut to the ISE length of COUNT values.
+template <int COUNT>
+__device__ __forceinline__ Bits128 ise_encode(int quant, const uint32_t (&v)[COUNT], const uint8_t* trits,
+                                              const uint8_t* quints) {
+    const RangeShape sh = range_shape(quant);
+    const int b = sh.bits;
+    const uint32_t mask = (1u << b) - 1u;
+    Bits128 o{0ull, 0ull};
+    int pos = 0;
+    if (sh.trits) {
+#pragma unroll
+        for (int g = 0; g < (COUNT + 4) / 5; ++g) {
+            uint32_t m[5], t[5];
+#pragma unroll
+            for (int j = 0; j < 5; ++j) {
+                const uint32_t x = (g * 5 + j < COUNT) ? v[(g * 5 + j < COUNT) ? g * 5 + j : 0] : 0u;
+                m[j] = x & mask;
+                t[j] = x >> b;
+            }
+            const uint32_t T = trits[t[4] * 81 + t[3] * 27 + t[2] * 9 + t[1] * 3 + t[0]];
+            put_bits(o, pos, m[0], b); put_bits(o, pos, T & 3u, 2);
+            put_bits(o, pos, m[1], b); put_bits(o, pos, (T >> 2) & 3u, 2);
+            put_bits(o, pos, m[2], b); put_bits(o, pos, (T >> 4) & 1u, 1);
+            put_bits(o, pos, m[3], b); put_bits(o, pos, (T >> 5) & 3u, 2);
+            put_bits(o, pos, m[4], b); put_bits(o, pos, (T >> 7) & 1u, 1);
+        }
+    } else if (sh.quints) {
+#pragma unroll
+        for (int g = 0; g < (COUNT + 2) / 3; ++g) {
+            uint32_t m[3], q[3];
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                const uint32_t x = (g * 3 + j < COUNT) ? v[(g * 3 + j < COUNT) ? g * 3 + j : 0] : 0u;
+                m[j] = x & mask;
+                q[j] = x >> b;
+            }
+            const uint32_t Q = quints[q[2] * 25 + q[1] * 5 + q[0]];
+            put_bits(o, pos, m[0], b); put_bits(o, pos, Q & 7u, 3);
+            put_bits(o, pos, m[1], b); put_bits(o, pos, (Q >> 3) & 3u, 2);
+            put_bits(o, pos, m[2], b); put_bits(o, pos, (Q >> 5) & 3u, 2);
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < COUNT; ++i) put_bits(o, pos, v[i], b);
+    }
+    keep_low_bits(o, ise_bit_count(quant, COUNT));
+    return o;
+}
+
+// Single-partition block, 4x4 weight grid of range wq, endpoint range cq:
+// mode [10:0], CEM [16:13], endpoint ISE from bit 17 up, weight ISE
+// bit-reversed from bit 127 down.
+template <bool ALPHA>
+__device__ __forceinline__ uint4 assemble_search_block(int wq, int cq, const uint32_t (&ev)[ALPHA ? 8 : 6],
+                                                       const uint32_t (&sw)[16], const SearchSmem& sm) {
+    const Bits128 ep = ise_encode<ALPHA ? 8 : 6>(cq, ev, sm.trits, sm.quints);
+    const Bits128 wt = ise_encode<16>(wq, sw, sm.trits, sm.quints);
+    const uint64_t head = (uint64_t)blockmode_4x4_grid(wq) | ((uint64_t)(ALPHA ? 12u : 8u) << 13);
+    const uint64_t lo = head | (ep.lo << 17) | __brevll(wt.hi);
+    const uint64_t hi = (ep.lo >> 47) | (ep.hi << 17) | __brevll(wt.lo);
+    return make_uint4((uint32_t)lo, (uint32_t)(lo >> 32), (uint32_t)hi, (uint32_t)(hi >> 32));
+}
+
+// ---------------------------------------------------------------------------
+// scoring
+// ---------------------------------------------------------------------------
+// The block's texels in the fit space as packed bytes (UNORM input): normal
+// maps read blue and alpha as 255, RGB blocks drop alpha (not scored).
+template <bool ALPHA, bool NORMAL>
+__device__ __forceinline__ uint32_t texel_word(uint32_t px) {
+    const uint32_t t = NORMAL ? (px | 0xFFFF0000u) : px;
+    return ALPHA ? t : (t & 0x00FFFFFFu);
+}
+
+// Squared error of the spec decode of endpoints E0/E1 (0..255) with grid
+// weights W (0..64) against the block's texels.  A decoded UNORM8 channel is
+// ((c0 * (64 - w) + c1 * w + 32) >> 6) >> 8 with c = e * 257 (linear) or
+// (e << 8) | 0x80 (sRGB), i.e. byte 2 of 4 * (64 * c0 + 32) + 4 * (c1 - c0) * w.
+// UNORM input: sum (dec - t)^2 = sum dec.dec - 2 sum dec.t + sum t.t over
+// packed bytes (__dp4a), exact in 32-bit integers (at most 36 * 4 * 255^2);
+// the last sum is per block (t2).  sRGB input: fused multiply-adds of the
+// float differences, texel-major, r g b (a), as the oracle accumulates them.
+template <int DIM, bool ALPHA, bool NORMAL, bool SRGB>
+struct BlockError {
+    typedef typename std::conditional<SRGB, float, uint32_t>::type T;
+
+    static __device__ __forceinline__ uint32_t texel_sq(const uint32_t (&px)[DIM * DIM]) {
+        uint32_t t2 = 0;
+#pragma unroll
+        for (int k = 0; k < DIM * DIM; ++k) {
+            const uint32_t t = texel_word<ALPHA, NORMAL>(px[k]);
+            t2 = __dp4a(t, t, t2);
+        }
+        return t2;
+    }
+
+    static __device__ __forceinline__ T eval(const uint32_t (&px)[DIM * DIM], const float* lut, uint32_t t2,
+                                             const int E0[4], const int E1[4], const int (&W)[16]) {
+        constexpr int NCH = ALPHA ? 4 : 3;
+        int base[NCH], delta[NCH];
+#pragma unroll
+        for (int c = 0; c < NCH; ++c) {
+            const int c0 = SRGB ? ((E0[c] << 8) | 0x80) : E0[c] * 257;
+            const int c1 = SRGB ? ((E1[c] << 8) | 0x80) : E1[c] * 257;
+            base[c] = 4 * (64 * c0 + 32);
+            delta[c] = 4 * (c1 - c0);
+        }
+        uint32_t dd = 0, dt = 0;
+        float errf = 0.0f;
+#pragma unroll
+        for (int k = 0; k < DIM * DIM; ++k) {
+            int w;
+            if constexpr (DIM == 6) {
+                const Infill f = infill_6x6(k);
+                int acc = W[f.v0] * f.w00;
+                if (f.w01) acc += W[f.v0 + 1] * f.w01;
+                if (f.w10) acc += W[f.v0 + 4] * f.w10;
+                if (f.w11) acc += W[f.v0 + 5] * f.w11;
+                w = (acc + 8) >> 4;
+            } else {
+                w = W[k];
+            }
+            uint32_t v[NCH];
+#pragma unroll
+            for (int c = 0; c < NCH; ++c) v[c] = (uint32_t)(base[c] + delta[c] * w);   // decoded in byte 2
+            if constexpr (SRGB) {
+#pragma unroll
+                for (int c = 0; c < NCH; ++c) {
+                    float t;
+                    if (c == 3) t = NORMAL ? 255.0f : (float)(px[k] >> 24);
+                    else if (NORMAL && c == 2) t = 255.0f;
+                    else t = lds_f32_volatile(lut + ((px[k] >> (8 * c)) & 0xFFu));
+                    const float d = __fsub_rn(__int2float_rn((int)((v[c] >> 16) & 0xFFu)), t);
+                    errf = __fmaf_rn(d, d, errf);
+                }
+            } else {
+                uint32_t dec = __byte_perm(v[0], v[1], 0x3362u);             // r, g, 0, 0
+                dec = __byte_perm(dec, v[2], 0x3610u);                       // r, g, b, 0
+                if constexpr (ALPHA) dec = __byte_perm(dec, v[3], 0x6210u);  // r, g, b, a
+                dd = __dp4a(dec, dec, dd);
+                dt = __dp4a(dec, texel_word<ALPHA, NORMAL>(px[k]), dt);
+            }
+        }
+        if constexpr (SRGB) {
+            (void)t2; (void)dd; (void)dt;
+            return errf;
+        } else {
+            (void)errf;
+            return dd - 2u * dt + t2;
+        }
+    }
+};
+
+// One candidate of weight range wq: endpoint symbols / decoded values and the
+// value-order weight indices q (0..levels-1) with their decoded weights W.
+template <bool ALPHA, class G>
+__device__ __forceinline__ void search_trial(int wq, const uint32_t q0[4], const uint32_t q1[4],
+                                             const G& s, const SearchSmem& sm, int slot, int cq,
+                                             int sym0[4], int sym1[4], int E0[4], int E1[4], uint32_t (&q)[16],
+                                             int (&W)[16]) {
+    constexpr int NCH = ALPHA ? 4 : 3;
+#pragma unroll
+    for (int c = 0; c < 4; ++c) { sym0[c] = 0; sym1[c] = 0; E0[c] = 255; E1[c] = 255; }
+#pragma unroll
+    for (int c = 0; c < NCH; ++c) {
+        if (cq == kQuant256) {
+            sym0[c] = E0[c] = (int)q0[c];
+            sym1[c] = E1[c] = (int)q1[c];
+        } else {
+            const uint32_t a = sm.color[slot][q0[c]], b = sm.color[slot][q1[c]];
+            sym0[c] = (int)(a & 0xFFu); E0[c] = (int)(a >> 8);
+            sym1[c] = (int)(b & 0xFFu); E1[c] = (int)(b >> 8);
+        }
+    }
+    if (E1[0] + E1[1] + E1[2] < E0[0] + E0[1] + E0[2]) {
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            int t = sym0[c]; sym0[c] = sym1[c]; sym1[c] = t;
+            t = E0[c]; E0[c] = E1[c]; E1[c] = t;
+        }
+    }
+    const float d0 = (float)(E1[0] - E0[0]), d1 = (float)(E1[1] - E0[1]);
+    const float d2 = (float)(E1[2] - E0[2]), d3 = (float)(E1[3] - E0[3]);
+    const float dd = dot4(d0, d1, d2, d3, d0, d1, d2, d3);
+    const float R = (float)(quant_levels(wq) - 1);
+    if (dd == 0.0f) {
+#pragma unroll
+        for (int g = 0; g < 16; ++g) q[g] = 0u;
+    } else {
+        const float r = __frcp_rn(dd);
+        const float f0 = (float)E0[0], f1 = (float)E0[1], f2 = (float)E0[2], f3 = (float)E0[3];
+#pragma unroll
+        for (int g = 0; g < 16; ++g) {
+            const float4 sg = s.get(g);
+            const float x = dot4(__fsub_rn(sg.x, f0), __fsub_rn(sg.y, f1), __fsub_rn(sg.z, f2),
+                                 __fsub_rn(sg.w, f3), d0, d1, d2, d3);
+            const float w = fminf(fmaxf(__fmul_rn(x, r), 0.0f), 1.0f);
+            q[g] = rint_u32(__fmul_rn(w, R));
+        }
+    }
+#pragma unroll
+    for (int g = 0; g < 16; ++g) W[g] = sm.wval[wq][q[g]];
+}
+
+// The search over one block.  `fixed` is the fixed-mode block with rounded
+// endpoints q0/q1 and weights qw; `grid` holds the 16 grid-point colours
+// (grid_sample of the texels), in registers or shared memory.
+template <int DIM, bool ALPHA, bool NORMAL, bool SRGB, class G>
+__device__ __forceinline__ uint4 search_block(const G& grid, const uint32_t (&px)[DIM * DIM], const uint32_t q0[4],
+                                              const uint32_t q1[4], const uint32_t qw[16], const uint4 fixed,
+                                              const SearchSmem& sm) {
+    typedef BlockError<DIM, ALPHA, NORMAL, SRGB> Err;
+    constexpr int WQ0 = ALPHA ? kQuant6 : kQuant12;
+    int E0[4], E1[4], W[16];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) { E0[c] = (int)q0[c]; E1[c] = (int)q1[c]; }
+#pragma unroll
+    for (int g = 0; g < 16; ++g) W[g] = sm.wval[WQ0][qw[g]];
+    const uint32_t t2 = SRGB ? 0u : Err::texel_sq(px);
+    typename Err::T best = Err::eval(px, sm.lut, t2, E0, E1, W);
+    int best_wq = -1;
+#pragma unroll 1
+    for (int wq = kQuant3; wq <= kQuant32; ++wq) {
+        const int cq = sm.cq[wq];
+        if (cq < 0) continue;
+        int sym0[4], sym1[4];
+        uint32_t q[16];
+        search_trial<ALPHA>(wq, q0, q1, grid, sm, sm.slot[wq], cq, sym0, sym1, E0, E1, q, W);
+        const typename Err::T err = Err::eval(px, sm.lut, t2, E0, E1, W);
+        if (err < best) { best = err; best_wq = wq; }
+    }
+    if (best_wq < 0) return fixed;
+    const int cq = sm.cq[best_wq];
+    int sym0[4], sym1[4];
+    uint32_t q[16];
+    search_trial<ALPHA>(best_wq, q0, q1, grid, sm, sm.slot[best_wq], cq, sym0, sym1, E0, E1, q, W);
+    uint32_t ev[ALPHA ? 8 : 6];
+#pragma unroll
+    for (int c = 0; c < (ALPHA ? 4 : 3); ++c) { ev[2 * c] = (uint32_t)sym0[c]; ev[2 * c + 1] = (uint32_t)sym1[c]; }
+    uint32_t sw[16];
+#pragma unroll
+    for (int g = 0; g < 16; ++g) sw[g] = sm.scramble[best_wq][q[g]];
+    return assemble_search_block<ALPHA>(best_wq, cq, ev, sw, sm);
+}
+
+}  // namespace astc

@@ -226,4 +226,86 @@ constexpr ASTC_HD uint32_t blockmode_4x4_grid(int weight_quant) {
     return ((r >> 1) & 3u) | ((r & 1u) << 4) | (a << 5) | (b << 7) | (h << 9) | (d << 10);
 }
 
+// ---------------------------------------------------------------------------
+// search mode: the single-partition modes with a 4x4 weight grid
+// ---------------------------------------------------------------------------
+// Endpoint quant method of weight quant method wq with nvals endpoint values:
+// the decoder takes the largest range whose ISE fits between bit 17 and the
+// weights; the mode is illegal outside 24..96 weight bits or below QUANT_6.
+constexpr ASTC_HD int endpoint_quant_for(int wq, int nvals) {
+    if (wq < kQuant2 || wq > kQuant32) return -1;
+    const int wbits = ise_bit_count(wq, 16);
+    if (wbits < 24 || wbits > 96) return -1;
+    const int avail = 128 - 17 - wbits;
+    for (int q = kQuant256; q >= kQuant6; --q)
+        if (ise_bit_count(q, nvals) <= avail) return q;
+    return -1;
+}
+
+struct SearchTables {
+    // (unquantised << 8) | symbol of the colour value nearest each byte
+    // (ties: the smaller value), per endpoint range used below QUANT_256
+    uint16_t color[2][8][256];     // [alpha][slot][byte]
+    int8_t slot[2][12];            // [alpha][wq] -> slot, -1 = QUANT_256
+    int8_t cq[2][12];              // [alpha][wq] -> endpoint quant method
+    uint8_t wval[12][32];          // [wq][value-order index] -> weight 0..64
+    uint8_t scramble[12][32];      // [wq][value-order index] -> ISE symbol
+    uint8_t trit_pack[256];
+    uint8_t quint_pack[128];
+    int nslots[2];                 // [alpha] rows of color in use
+};
+
+constexpr SearchTables make_search_tables() {
+    SearchTables s{};
+    const IseTables t = make_ise_tables();
+    for (int a = 0; a < 2; ++a) {
+        int nslots = 0;
+        for (int wq = 0; wq < 12; ++wq) {
+            const int cq = endpoint_quant_for(wq, a ? 8 : 6);
+            s.cq[a][wq] = (int8_t)cq;
+            s.slot[a][wq] = -1;
+            if (cq < 0 || cq == kQuant256) continue;
+            int slot = -1;
+            for (int w2 = 0; w2 < wq; ++w2)
+                if (s.cq[a][w2] == cq) slot = s.slot[a][w2];
+            if (slot < 0) {
+                slot = nslots++;
+                // symbols by value, then each byte's nearest on either side
+                int sym_at[256] = {};
+                for (int v = 0; v < 256; ++v) sym_at[v] = -1;
+                for (int v = 0; v < quant_levels(cq); ++v) sym_at[unquant_color(cq, v)] = v;
+                int below[256] = {}, above[256] = {};
+                int last = 0;
+                for (int v = 0; v < 256; ++v) { if (sym_at[v] >= 0) last = v; below[v] = last; }
+                last = 255;
+                for (int v = 255; v >= 0; --v) { if (sym_at[v] >= 0) last = v; above[v] = last; }
+                for (int v = 0; v < 256; ++v) {
+                    const int u = (v - below[v] <= above[v] - v) ? below[v] : above[v];
+                    s.color[a][slot][v] = (uint16_t)((u << 8) | sym_at[u]);
+                }
+            }
+            s.slot[a][wq] = (int8_t)slot;
+        }
+        s.nslots[a] = nslots;
+    }
+    for (int wq = 0; wq < 12; ++wq)
+        for (int i = 0; i < quant_levels(wq); ++i) {
+            s.scramble[wq][i] = t.scramble[wq][i];
+            s.wval[wq][i] = t.weight_unq[wq][t.scramble[wq][i]];
+        }
+    for (int i = 0; i < 243; ++i) s.trit_pack[i] = t.trit_pack[i];
+    for (int i = 0; i < 125; ++i) s.quint_pack[i] = t.quint_pack[i];
+    return s;
+}
+
+// Spec bilinear infill of a 4x4 weight grid at texel k of a 6x6 block: the
+// grid index of the top-left tap and the four tap weights (sum 16).
+struct Infill { int v0, w00, w01, w10, w11; };
+constexpr ASTC_HD Infill infill_6x6(int k) {
+    const int s = k % 6, t = k / 6, ds = (1024 + 3) / 5;
+    const int gs = (ds * s * 3 + 32) >> 6, gt = (ds * t * 3 + 32) >> 6;
+    const int fs = gs & 15, ft = gt & 15, w11 = (fs * ft + 8) >> 4;
+    return Infill{(gs >> 4) + 4 * (gt >> 4), 16 - fs - ft + w11, fs - w11, ft - w11, w11};
+}
+
 }  // namespace astc

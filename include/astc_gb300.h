@@ -62,6 +62,28 @@ typedef enum astc_memory {
     ASTC_MEMORY_DEVICE = 1       /* input and output are device pointers    */
 } astc_memory;
 
+typedef enum astc_axis {
+    ASTC_AXIS_PCA = 0,           /* principal_component_analysis, the
+                                    reference's fit (ASTC_Encode.hlsl:514)   */
+    ASTC_AXIS_MAX_ACCUMULATION = 1 /* max_accumulation_pixel_direction, the
+                                    reference's alternative fit, defined but
+                                    commented out (170-227, 515)             */
+} astc_axis;
+
+typedef enum astc_quality {
+    ASTC_QUALITY_FAST = 0,       /* the reference's fixed mode (518-522):
+                                    QUANT_12 (RGB) / QUANT_6 (RGBA) weights,
+                                    QUANT_256 endpoints                     */
+    ASTC_QUALITY_SEARCH = 1      /* the fixed-mode block and every single-
+                                    partition 4x4-grid mode (weight ranges
+                                    QUANT_3..QUANT_32, each with the largest
+                                    endpoint range that fits), keeping the
+                                    one whose decode has the least squared
+                                    error; the choose_best_quantmethod the
+                                    reference sketches (524-526).  Never
+                                    worse than FAST; FP32 only              */
+} astc_quality;
+
 /* Encoder options: the reference's encode_option (astc_encode.h:14-28) plus
  * the GPU-side controls.  Use astc_opts_init() for the reference defaults. */
 typedef struct astc_opts {
@@ -78,10 +100,12 @@ typedef struct astc_opts {
                         the result is in `out` (for asynchronous work on
                         the legacy default stream pass cudaStreamLegacy,
                         (void*)0x1, not NULL)                               */
+    int axis;        /* astc_axis (FP32 only)                               */
+    int quality;     /* astc_quality (FP32 only)                            */
 } astc_opts;
 
 /* Fills the reference defaults: 4x4, no alpha, not a normal map, linear,
- * zero border, FP32, host memory, synchronous. */
+ * zero border, FP32, host memory, synchronous, PCA axis, fixed mode. */
 void astc_opts_init(astc_opts* opts);
 
 /* Bytes of ASTC blocks for a w x h image: 16 * ceil(w/dim) * ceil(h/dim). */

@@ -17,6 +17,12 @@
  *   assemble_block         ASTC_Encode.hlsl:400-444
  *   ISE                    ASTC_IntegerSequenceEncoding.hlsl:5-276
  *   scramble tables        ASTC_Table.hlsl:4-66
+ *   max_accumulation_pixel_direction  ASTC_Encode.hlsl:170-227 (the shader's
+ *                          unused alternative to the PCA, opts.axis = 1)
+ *   search mode            the choose_best_quantmethod the shader sketches at
+ *                          ASTC_Encode.hlsl:524-526 (opts.quality = 1): every
+ *                          4x4-grid weight range with the endpoint range the
+ *                          decoder derives, scored by the spec decode
  *
  * The lookup tables are GENERATED here from the ASTC specification's
  * definitions (trit/quint decode, weight unquantisation), never copied; the
@@ -43,6 +49,7 @@
 #include <cstdint>
 #include <cstdlib>
 #include <cstring>
+#include <utility>
 #include <vector>
 
 #ifdef _OPENMP
@@ -444,6 +451,78 @@ void assemble_symbolic(const uint32_t ep_q[8], const uint32_t qw[16], bool alpha
 }
 
 // ---------------------------------------------------------------------------
+// Integer helpers of the search mode (ASTC specification rules)
+// ---------------------------------------------------------------------------
+// Endpoint quant method of a single-partition block with a 4x4 weight grid
+// of quant method wq and nvals endpoint values: the decoder takes the
+// largest range whose ISE fits in the bits between bit 17 and the weights
+// (and the block is illegal below QUANT_6 or outside 24..96 weight bits).
+int endpoint_quant(int wq, int nvals) {
+    if (wq < QUANT_2 || wq > QUANT_32) return -1;
+    const int wbits = ise_bits(wq, 16);
+    if (wbits < 24 || wbits > 96) return -1;
+    const int avail = 128 - 17 - wbits;
+    for (int q = QUANT_256; q >= QUANT_6; --q)
+        if (ise_bits(q, nvals) <= avail) return q;
+    return -1;
+}
+
+// The ISE symbol of colour range cq whose unquantised value is nearest v
+// (ties: the smaller value); *unq receives that value.
+int nearest_color(int cq, int v, int* unq) {
+    const Tables& tb = tables();
+    int best = 0, bu = tb.cunq[cq][0], bd = std::abs(bu - v);
+    for (int s = 1; s < kQuantLevels[cq]; ++s) {
+        const int u = tb.cunq[cq][s], d = std::abs(u - v);
+        if (d < bd || (d == bd && u < bu)) { best = s; bu = u; bd = d; }
+    }
+    *unq = bu;
+    return best;
+}
+
+// One UNORM8 channel of the spec LDR decode: endpoints expanded to 16 bits
+// (x257, or x256 + 0x80 for sRGB), interpolated at weight w of 64, top byte.
+int decode_channel(int e0, int e1, int w, bool srgb) {
+    const int c0 = srgb ? ((e0 << 8) | 0x80) : e0 * 257;
+    const int c1 = srgb ? ((e1 << 8) | 0x80) : e1 * 257;
+    return ((c0 * (64 - w) + c1 * w + 32) >> 6) >> 8;
+}
+
+// Spec bilinear infill of a 4x4 weight grid at texel (s, t) of a 6x6 block.
+int infill_6x6(const int wv[16], int s, int t) {
+    const int ds = (1024 + 3) / 5;
+    const int gs = (ds * s * 3 + 32) >> 6, gt = (ds * t * 3 + 32) >> 6;
+    const int js = gs >> 4, fs = gs & 15, jt = gt >> 4, ft = gt & 15;
+    const int w11 = (fs * ft + 8) >> 4, w10 = ft - w11, w01 = fs - w11, w00 = 16 - fs - ft + w11;
+    const int v0 = js + 4 * jt;
+    int acc = wv[v0] * w00;
+    if (w01) acc += wv[v0 + 1] * w01;
+    if (w10) acc += wv[v0 + 4] * w10;
+    if (w11) acc += wv[v0 + 5] * w11;
+    return (acc + 8) >> 4;
+}
+
+// A single-partition block with a 4x4 weight grid of any range: mode and CEM
+// in bits 0..16, the endpoint ISE from bit 17 up, the weight ISE bit-reversed
+// from bit 127 down (every field ORed, each cut to its ISE length).
+void assemble_general(uint32_t wq, uint32_t cq, uint32_t cem, const uint32_t* ev, int nvals,
+                      const uint32_t* sw, uint8_t out[16]) {
+    Bits128 ep = {{0, 0, 0, 0}}, wt = {{0, 0, 0, 0}};
+    ise_encode((int)cq, nvals, ev, ep);
+    ise_encode((int)wq, 16, sw, wt);
+    const int ebits = ise_bits((int)cq, nvals), wbits = ise_bits((int)wq, 16);
+    std::memset(out, 0, 16);
+    auto set = [&](int pos) { out[pos >> 3] = (uint8_t)(out[pos >> 3] | (1u << (pos & 7))); };
+    const uint32_t head = assemble_blockmode(wq) | ((cem & 0xF) << 13);
+    for (int i = 0; i < 17; ++i)
+        if ((head >> i) & 1) set(i);
+    for (int i = 0; i < ebits; ++i)
+        if ((ep.w[i >> 5] >> (i & 31)) & 1) set(17 + i);
+    for (int i = 0; i < wbits; ++i)
+        if ((wt.w[i >> 5] >> (i & 31)) & 1) set(127 - i);
+}
+
+// ---------------------------------------------------------------------------
 // Arithmetic policies: FP32 (the pinned model), FP64 twin, FP32 op counter
 // ---------------------------------------------------------------------------
 struct F32 {
@@ -584,6 +663,42 @@ struct Pipe {
         find_min_max(tex, n, mean, k, alpha, e0, e1);
     }
 
+    // max_accumulation_pixel_direction (ASTC_Encode.hlsl:170-227): the axis is
+    // the largest of four sums -- of the deviations of the texels whose red,
+    // green, blue (or, with alpha, alpha) lies above the mean.
+    static void max_accumulation(const T (*tex)[4], int n, bool alpha, T e0[4], T e1[4]) {
+        T mean[4] = {0, 0, 0, 0};
+        for (int i = 0; i < n; ++i)
+            for (int c = 0; c < 4; ++c) mean[c] = P::add(mean[c], tex[i][c]);
+        for (int c = 0; c < 4; ++c) mean[c] = div_const(mean[c], n);
+        T sum[4][4];
+        for (int a = 0; a < 4; ++a)
+            for (int c = 0; c < 4; ++c) sum[a][c] = 0;
+        for (int i = 0; i < n; ++i) {
+            T d[4];
+            for (int c = 0; c < 4; ++c) d[c] = P::sub(tex[i][c], mean[c]);
+            for (int a = 0; a < 4; ++a)                   // sum += (dt.a > 0) ? dt : 0
+                for (int c = 0; c < 4; ++c) sum[a][c] = P::add(sum[a][c], d[a] > 0 ? d[c] : (T)0);
+        }
+        T k[4];
+        for (int c = 0; c < 4; ++c) k[c] = sum[0][c];
+        T maxdot = dot4(sum[0], sum[0]);
+        for (int a = 1; a < (alpha ? 4 : 3); ++a) {       // strict >, in r g b a order
+            const T d = dot4(sum[a], sum[a]);
+            if (d > maxdot) {
+                maxdot = d;
+                for (int c = 0; c < 4; ++c) k[c] = sum[a][c];
+            }
+        }
+        if (!(length(k) < P::lit(1e-5f, 1e-5))) normalize(k);   // safe normalize
+        find_min_max(tex, n, mean, k, alpha, e0, e1);
+    }
+
+    static void fit(const T (*tex)[4], int n, bool alpha, int axis, T e0[4], T e1[4]) {
+        if (axis == 1) max_accumulation(tex, n, alpha, e0, e1);
+        else pca(tex, n, alpha, e0, e1);
+    }
+
     // idx_grids / wt_grids (ASTC_Encode.hlsl:268-304): the 4x4 weight grid of
     // a 6x6 block samples 2x2 texel taps at fixed bilinear weights.
     static void grid_taps(int g, int idx[4], T wt[4]) {
@@ -602,6 +717,24 @@ struct Pipe {
             wt[c] = (nearx[c] && neary[c]) ? hi : (nearx[c] || neary[c]) ? mid : lo;
     }
 
+    // the colour at weight-grid point g: the texel itself (4x4) or the 2x2
+    // bilinear sample of sample_texel (ASTC_Encode.hlsl:307-314, 6x6)
+    static void grid_sample(const T (*tex)[4], int dim, int g, T s[4]) {
+        if (dim == 6) {
+            int idx[4]; T cw[4];
+            grid_taps(g, idx, cw);
+            for (int c = 0; c < 4; ++c) {
+                T acc = P::mul(tex[idx[0]][c], cw[0]);
+                acc = P::mad(tex[idx[1]][c], cw[1], acc);
+                acc = P::mad(tex[idx[2]][c], cw[2], acc);
+                acc = P::mad(tex[idx[3]][c], cw[3], acc);
+                s[c] = acc;
+            }
+        } else {
+            for (int c = 0; c < 4; ++c) s[c] = tex[g][c];
+        }
+    }
+
     // calculate_normal_weights + quantize_weights (ASTC_Encode.hlsl:316-393)
     static void weights(const T (*tex)[4], int dim, const T e0[4], const T e1[4],
                         uint32_t range, uint32_t qw[16]) {
@@ -615,19 +748,7 @@ struct Pipe {
             T minw = P::lit(1e31f, 1e31), maxw = P::lit(-1e31f, -1e31);
             for (int i = 0; i < 16; ++i) {
                 T s[4];
-                if (dim == 6) {                             // sample_texel 307-314
-                    int idx[4]; T cw[4];
-                    grid_taps(i, idx, cw);
-                    for (int c = 0; c < 4; ++c) {
-                        T acc = P::mul(tex[idx[0]][c], cw[0]);
-                        acc = P::mad(tex[idx[1]][c], cw[1], acc);
-                        acc = P::mad(tex[idx[2]][c], cw[2], acc);
-                        acc = P::mad(tex[idx[3]][c], cw[3], acc);
-                        s[c] = acc;
-                    }
-                } else {
-                    for (int c = 0; c < 4; ++c) s[c] = tex[i][c];
-                }
+                grid_sample(tex, dim, i, s);
                 T d[4];
                 for (int c = 0; c < 4; ++c) d[c] = P::sub(s[c], e0[c]);
                 const T x = dot4(k, d);
@@ -648,11 +769,9 @@ struct Pipe {
         }
     }
 
-    // encode_block (ASTC_Encode.hlsl:510-550)
-    static void encode(const T (*tex)[4], int dim, bool alpha, uint32_t ep_q[8],
-                       uint32_t qw[16], uint8_t out[16]) {
-        T e0[4], e1[4];
-        pca(tex, dim * dim, alpha, e0, e1);
+    // encode_block (ASTC_Encode.hlsl:510-550) after the endpoint fit
+    static void fixed_mode(const T (*tex)[4], int dim, bool alpha, const T e0[4], const T e1[4],
+                           uint32_t ep_q[8], uint32_t qw[16], uint8_t out[16]) {
         for (int c = 0; c < 4; ++c) {                       // encode_color 233-245
             ep_q[2 * c] = (uint32_t)P::rint(e0[c]);
             ep_q[2 * c + 1] = (uint32_t)P::rint(e1[c]);
@@ -660,6 +779,119 @@ struct Pipe {
         const uint32_t range = alpha ? 5u : 11u;            // weight_range - 1
         weights(tex, dim, e0, e1, range, qw);
         assemble_symbolic(ep_q, qw, alpha, out);
+    }
+
+    // encode_block (ASTC_Encode.hlsl:510-550); axis 1 swaps in the
+    // alternative fit the shader leaves commented out at line 515
+    static void encode(const T (*tex)[4], int dim, bool alpha, uint32_t ep_q[8],
+                       uint32_t qw[16], uint8_t out[16], int axis = 0) {
+        T e0[4], e1[4];
+        fit(tex, dim * dim, alpha, axis, e0, e1);
+        fixed_mode(tex, dim, alpha, e0, e1, ep_q, qw, out);
+    }
+
+    // ---- search mode -----------------------------------------------------
+    // Squared error, in the fit space, of a decoded single-partition block
+    // with endpoints E0/E1 (0..255) and grid weights wv (0..64): texels in
+    // row-major order, channels r g b (a), accumulated with mad.
+    static T block_error(const T (*tex)[4], int dim, int nch, bool srgb, const int E0[4],
+                         const int E1[4], const int wv[16]) {
+        T err = 0;
+        for (int i = 0; i < dim * dim; ++i) {
+            const int w = dim == 4 ? wv[i] : infill_6x6(wv, i % 6, i / 6);
+            for (int c = 0; c < nch; ++c) {
+                const T d = P::sub((T)decode_channel(E0[c], E1[c], w, srgb), tex[i][c]);
+                err = P::mad(d, d, err);
+            }
+        }
+        return err;
+    }
+
+    // One search candidate: weight range wq, endpoint range cq, endpoints
+    // snapped to the nearest representable values (dark one first, so the
+    // decoder neither swaps nor blue-contracts), weights projected onto the
+    // decoded endpoints and rounded to the range.
+    struct Trial {
+        int wq, cq;
+        int sym0[4], sym1[4], E0[4], E1[4];
+        uint32_t q[16];
+    };
+    static void trial(const T (*s)[4], const T e0[4], const T e1[4], bool alpha, int wq, Trial& tr) {
+        const int nch = alpha ? 4 : 3;
+        tr.wq = wq;
+        tr.cq = endpoint_quant(wq, alpha ? 8 : 6);
+        for (int c = 0; c < 4; ++c) { tr.sym0[c] = tr.sym1[c] = 0; tr.E0[c] = tr.E1[c] = 255; }
+        for (int c = 0; c < nch; ++c) {
+            tr.sym0[c] = nearest_color(tr.cq, (int)P::rint(e0[c]), &tr.E0[c]);
+            tr.sym1[c] = nearest_color(tr.cq, (int)P::rint(e1[c]), &tr.E1[c]);
+        }
+        if (tr.E1[0] + tr.E1[1] + tr.E1[2] < tr.E0[0] + tr.E0[1] + tr.E0[2])
+            for (int c = 0; c < 4; ++c) {
+                std::swap(tr.sym0[c], tr.sym1[c]);
+                std::swap(tr.E0[c], tr.E1[c]);
+            }
+        T d[4];
+        for (int c = 0; c < 4; ++c) d[c] = (T)(tr.E1[c] - tr.E0[c]);
+        const T dd = dot4(d, d);
+        const uint32_t R = (uint32_t)kQuantLevels[wq] - 1;
+        if (dd == 0) {
+            for (int g = 0; g < 16; ++g) tr.q[g] = 0;
+            return;
+        }
+        const T r = P::div(P::lit(1.0f, 1.0), dd);
+        for (int g = 0; g < 16; ++g) {
+            T diff[4];
+            for (int c = 0; c < 4; ++c) diff[c] = P::sub(s[g][c], (T)tr.E0[c]);
+            T w = P::mul(dot4(diff, d), r);
+            w = P::min(P::max(w, (T)0), P::lit(1.0f, 1.0));
+            tr.q[g] = (uint32_t)P::rint(P::mul(w, (T)R));
+        }
+    }
+
+    static void trial_weights(int wq, const uint32_t q[16], int wv[16]) {
+        const Tables& tb = tables();
+        for (int g = 0; g < 16; ++g) wv[g] = tb.wunq[wq][tb.scramble[wq][q[g]]];
+    }
+
+    // The fixed-mode block, then every weight range QUANT_3..QUANT_32 with
+    // its endpoint range; the first candidate with the least error is kept.
+    static void search(const T (*tex)[4], int dim, bool alpha, bool srgb, int axis, uint8_t out[16],
+                       int* chosen, T* best_err, T* fixed_err) {
+        const int nch = alpha ? 4 : 3;
+        T e0[4], e1[4];
+        fit(tex, dim * dim, alpha, axis, e0, e1);
+        uint32_t ep_q[8], qw[16];
+        fixed_mode(tex, dim, alpha, e0, e1, ep_q, qw, out);
+        int E0[4], E1[4], wv[16];
+        for (int c = 0; c < 4; ++c) { E0[c] = (int)ep_q[2 * c]; E1[c] = (int)ep_q[2 * c + 1]; }
+        trial_weights(alpha ? QUANT_6 : QUANT_12, qw, wv);
+        T best = block_error(tex, dim, nch, srgb, E0, E1, wv);
+        *fixed_err = best;
+        *chosen = -1;
+        T s[16][4];
+        for (int g = 0; g < 16; ++g) grid_sample(tex, dim, g, s[g]);
+        Trial keep = {};
+        for (int wq = QUANT_3; wq <= QUANT_32; ++wq) {
+            if (endpoint_quant(wq, alpha ? 8 : 6) < 0) continue;
+            Trial tr;
+            trial(s, e0, e1, alpha, wq, tr);
+            trial_weights(wq, tr.q, wv);
+            const T err = block_error(tex, dim, nch, srgb, tr.E0, tr.E1, wv);
+            if (err < best) { best = err; *chosen = wq; keep = tr; }
+        }
+        if (*chosen >= 0) assemble_trial(keep, alpha, out);
+        *best_err = best;
+    }
+
+    static void assemble_trial(const Trial& tr, bool alpha, uint8_t out[16]) {
+        const Tables& tb = tables();
+        const int nvals = alpha ? 8 : 6;
+        const uint32_t ev[8] = {(uint32_t)tr.sym0[0], (uint32_t)tr.sym1[0], (uint32_t)tr.sym0[1],
+                                (uint32_t)tr.sym1[1], (uint32_t)tr.sym0[2], (uint32_t)tr.sym1[2],
+                                (uint32_t)tr.sym0[3], (uint32_t)tr.sym1[3]};
+        uint32_t sw[16];
+        for (int g = 0; g < 16; ++g) sw[g] = (uint32_t)tb.scramble[tr.wq][tr.q[g]];
+        assemble_general((uint32_t)tr.wq, (uint32_t)tr.cq, alpha ? 12u : 8u, ev, nvals, sw, out);
     }
 
     // MainCS texel fetch (ASTC_Encode.hlsl:561-580)
@@ -690,6 +922,8 @@ struct Pipe {
         if (!rgba || !out || !o || w <= 0 || h <= 0) return -1;
         if (o->block_dim != 4 && o->block_dim != 6) return -2;
         if (o->border != 0 && o->border != 1) return -3;
+        if (o->axis != 0 && o->axis != 1) return -4;
+        if (o->quality != 0 && o->quality != 1) return -5;
         tables();
         const int dim = o->block_dim;
         const int nbx = (w + dim - 1) / dim, nby = (h + dim - 1) / dim;
@@ -704,8 +938,15 @@ struct Pipe {
             const int by = (int)(b / nbx), bx = (int)(b - (long long)by * nbx);
             T tex[36][4];
             fetch(rgba, w, h, bx, by, *o, tex);
+            if (o->quality) {
+                int chosen;
+                T err, err_fixed;
+                search(tex, dim, o->has_alpha != 0, o->srgb != 0, o->axis, out + 16 * b, &chosen, &err,
+                       &err_fixed);
+                continue;
+            }
             uint32_t ep[8], qw[16];
-            encode(tex, dim, o->has_alpha != 0, ep, qw, out + 16 * b);
+            encode(tex, dim, o->has_alpha != 0, ep, qw, out + 16 * b, o->axis);
         }
         return 0;
     }
@@ -1113,6 +1354,22 @@ int oracle_unquant_color(int quant, int value) {
 
 void oracle_grid_taps(int g, int idx[4], float wt[4]) {
     Pipe<F32>::grid_taps(g & 15, idx, wt);
+}
+
+int oracle_endpoint_quant(int wq, int nvals) {
+    if (nvals != 6 && nvals != 8) return -1;
+    return endpoint_quant(wq, nvals);
+}
+
+int oracle_search_block_fp32(const float* texels, int block_dim, int has_alpha, int srgb, int axis,
+                             uint8_t out[16], int* chosen_wq, float* err, float* err_fixed) {
+    if (!texels || !out || !chosen_wq || !err || !err_fixed) return -1;
+    if ((block_dim != 4 && block_dim != 6) || (axis != 0 && axis != 1)) return -1;
+    float tex[36][4];
+    for (int i = 0; i < block_dim * block_dim; ++i)
+        for (int c = 0; c < 4; ++c) tex[i][c] = texels[4 * i + c];
+    Pipe<F32>::search(tex, block_dim, has_alpha != 0, srgb != 0, axis, out, chosen_wq, err, err_fixed);
+    return 0;
 }
 
 double oracle_flops_per_block(int block_dim, int has_alpha, int is_normal) {

@@ -32,6 +32,17 @@ typedef struct oracle_opts {
     int srgb;        /* texels are sRGB-decoded before the fit (main.cpp:38)*/
     int border;      /* 0 = zero outside the texture (D3D11 Load rule),
                         1 = clamp to the edge texel                         */
+    int axis;        /* 0 = principal_component_analysis (the shader's
+                        call, ASTC_Encode.hlsl:514), 1 = the shader's
+                        alternative max_accumulation_pixel_direction
+                        (170-227, commented out at 515)                     */
+    int quality;     /* 0 = the shader's fixed mode (518-522); 1 = search:
+                        the fixed-mode block plus every single-partition
+                        4x4-grid weight range QUANT_3..QUANT_32 with the
+                        largest endpoint range that fits, keeping the
+                        candidate with the least decoded error (the
+                        choose_best_quantmethod the shader sketches at
+                        524-526)                                            */
 } oracle_opts;
 
 /* Encode a tightly packed RGBA8 image (row 0 first) into 16-byte blocks in
@@ -87,6 +98,18 @@ void oracle_grid_taps(int g, int idx[4], float wt[4]);
 /* Algorithmic FP32 operation count of one block, counted by running the
  * FP32 pipeline with counting arithmetic (FMA counted as 2). */
 double oracle_flops_per_block(int block_dim, int has_alpha, int is_normal);
+
+/* Search mode introspection.  Endpoint quant method the ASTC decoder derives
+ * for a single-partition 4x4 weight grid of weight quant method `wq` and
+ * `nvals` endpoint values (6 = CEM 8, 8 = CEM 12), or -1 if the mode is
+ * invalid. */
+int oracle_endpoint_quant(int wq, int nvals);
+/* Encode one block (texels: N*4 floats, 0..255, the fit space) in search
+ * mode with FP32 arithmetic.  *chosen_wq = weight quant method of the block
+ * kept (-1 when the fixed-mode block was kept), *err = its squared error in
+ * the fit space, *err_fixed = the fixed-mode block's. */
+int oracle_search_block_fp32(const float* texels, int block_dim, int has_alpha, int srgb, int axis,
+                             uint8_t out[16], int* chosen_wq, float* err, float* err_fixed);
 
 #ifdef __cplusplus
 }

@@ -20,7 +20,8 @@ _lib: ctypes.CDLL | None = None
 
 
 class OracleOpts(ctypes.Structure):
-    _fields_ = [(n, ctypes.c_int) for n in ("block_dim", "has_alpha", "is_normal", "srgb", "border")]
+    _fields_ = [(n, ctypes.c_int) for n in ("block_dim", "has_alpha", "is_normal", "srgb", "border",
+                                            "axis", "quality")]
 
 
 def build(force: bool = False) -> str:
@@ -62,24 +63,31 @@ def lib() -> ctypes.CDLL:
             L.oracle_grid_taps.restype = None
             L.oracle_flops_per_block.argtypes = [ip, ip, ip]
             L.oracle_flops_per_block.restype = ctypes.c_double
+            L.oracle_endpoint_quant.argtypes = [ip, ip]
+            L.oracle_search_block_fp32.argtypes = [vp, ip, ip, ip, ip, vp, vp, vp, vp]
             _lib = L
     return _lib
 
 
-def _opts(block_dim, has_alpha, is_normal, srgb, border) -> OracleOpts:
+def _opts(block_dim, has_alpha, is_normal, srgb, border, axis=0, quality=0) -> OracleOpts:
     return OracleOpts(int(block_dim), int(bool(has_alpha)), int(bool(is_normal)), int(bool(srgb)),
-                      int(border))
+                      int(border), int(axis), int(quality))
 
 
 def encode(rgba: np.ndarray, block_dim: int = 4, has_alpha: bool = False, is_normal: bool = False,
-           srgb: bool = False, border: int = 0, threads: int = 0, fp64: bool = False) -> np.ndarray:
-    """FP32 (or FP64 twin) oracle encode of a (H, W, 4) uint8 image -> (n, 16) uint8."""
+           srgb: bool = False, border: int = 0, threads: int = 0, fp64: bool = False,
+           axis: int = 0, quality: int = 0) -> np.ndarray:
+    """FP32 (or FP64 twin) oracle encode of a (H, W, 4) uint8 image -> (n, 16) uint8.
+
+    axis 1 = max_accumulation_pixel_direction instead of the PCA; quality 1 =
+    search over the single-partition weight/endpoint ranges."""
     a = np.ascontiguousarray(rgba, dtype=np.uint8)
     h, w = a.shape[:2]
     nb = ((w + block_dim - 1) // block_dim) * ((h + block_dim - 1) // block_dim)
     out = np.empty((nb, 16), np.uint8)
     fn = lib().oracle_encode_fp64 if fp64 else lib().oracle_encode_fp32
-    rc = fn(a.ctypes.data, w, h, ctypes.byref(_opts(block_dim, has_alpha, is_normal, srgb, border)),
+    rc = fn(a.ctypes.data, w, h,
+            ctypes.byref(_opts(block_dim, has_alpha, is_normal, srgb, border, axis, quality)),
             out.ctypes.data, threads)
     if rc != 0:
         raise ValueError(f"oracle encode rejected the arguments ({rc})")
@@ -173,3 +181,26 @@ def grid_taps(g: int):
 
 def flops_per_block(block_dim: int, has_alpha: bool, is_normal: bool = False) -> float:
     return float(lib().oracle_flops_per_block(block_dim, int(has_alpha), int(is_normal)))
+
+
+def endpoint_quant(wq: int, nvals: int) -> int:
+    """Endpoint quant method the decoder derives for a 4x4 weight grid of
+    quant method wq (single partition), or -1 for an illegal mode."""
+    return int(lib().oracle_endpoint_quant(wq, nvals))
+
+
+def search_block(texels: np.ndarray, block_dim: int, has_alpha: bool, srgb: bool = False, axis: int = 0):
+    """Search-mode FP32 encode of one block of fit-space texels (N x 4 floats).
+
+    Returns (block bytes, chosen weight quant method or -1 for the fixed-mode
+    block, its squared error, the fixed-mode block's squared error)."""
+    t = np.ascontiguousarray(texels, dtype=np.float32).reshape(-1)
+    out = np.zeros(16, np.uint8)
+    wq = ctypes.c_int(0)
+    err = ctypes.c_float(0)
+    err_fixed = ctypes.c_float(0)
+    rc = lib().oracle_search_block_fp32(t.ctypes.data, block_dim, int(has_alpha), int(srgb), int(axis),
+                                        out.ctypes.data, ctypes.byref(wq), ctypes.byref(err),
+                                        ctypes.byref(err_fixed))
+    assert rc == 0
+    return out, wq.value, err.value, err_fixed.value

@@ -60,7 +60,7 @@ def test_encoded_size(native):
 
 
 @pytest.mark.parametrize("field,value", [("block_dim", 5), ("border", 2), ("precision", 7),
-                                         ("memory", 3)])
+                                         ("memory", 3), ("axis", 2), ("quality", -1)])
 def test_bad_options_rejected(native, field, value):
     lib = native.load_library()
     o = native.make_opts()
@@ -70,6 +70,25 @@ def test_bad_options_rejected(native, field, value):
     st = lib.astc_encode_gpu(buf.ctypes.data, 4, 4, ctypes.byref(o), out.ctypes.data)
     assert st == native.Status.INVALID_ARG
     assert lib.astc_last_error()
+
+
+@pytest.mark.parametrize("axis,quality", [(1, 0), (0, 1), (1, 1)])
+def test_half2_rejects_search_and_axis(native, axis, quality):
+    """The max-accumulation axis and the mode search are FP32 only."""
+    lib = native.load_library()
+    o = native.make_opts(precision=native.Precision.HALF2, axis=axis, quality=quality)
+    buf = np.zeros((4, 4, 4), np.uint8)
+    out = np.zeros(16, np.uint8)
+    st = lib.astc_encode_gpu(buf.ctypes.data, 4, 4, ctypes.byref(o), out.ctypes.data)
+    assert st == native.Status.UNSUPPORTED
+    assert b"FP32" in lib.astc_last_error()
+
+
+def test_opts_init_defaults(native):
+    o = native.AstcOpts()
+    o.axis, o.quality = 7, 7
+    native.load_library().astc_opts_init(ctypes.byref(o))
+    assert (o.block_dim, o.precision, o.axis, o.quality) == (4, 0, native.Axis.PCA, native.Quality.FAST)
 
 
 def test_bad_sizes_and_pointers_rejected(native):

@@ -1,0 +1,166 @@
+"""The oracle's two modes beyond the reference's fixed pipeline.
+
+* axis = 1: max_accumulation_pixel_direction (ASTC_Encode.hlsl:170-227), the
+  endpoint fit the reference defines but leaves commented out at line 515;
+* quality = 1: the search the reference sketches as choose_best_quantmethod
+  (524-526): the fixed-mode block plus every single-partition 4x4-grid mode.
+
+The reference never runs either, so there is no reference output to pin them
+to; these tests pin them to the ASTC rules instead: the endpoint range is the
+one the decoder derives, every search block decodes (spec decoder) to exactly
+the error the search scored it with, the search is never worse than the fixed
+mode, and the max-accumulation fit reproduces a two-colour block exactly.
+"""
+import numpy as np
+import pytest
+
+from astc_encoder_gb300 import synth
+
+QUANT_LEVELS = [2, 3, 4, 5, 6, 8, 10, 12, 16, 20, 24, 32, 40, 48, 64, 80, 96, 128, 160, 192, 256]
+
+
+def _ise_bits(q, n):
+    levels = QUANT_LEVELS[q]
+    b = 0
+    while levels % 2 == 0:
+        levels //= 2
+        b += 1
+    if levels == 3:
+        return ((8 + 5 * b) * n + 4) // 5
+    if levels == 5:
+        return ((7 + 3 * b) * n + 2) // 3
+    return n * b
+
+
+@pytest.mark.parametrize("nvals", [6, 8])
+def test_endpoint_range_is_the_decoders(oracle, nvals):
+    for wq in range(12):
+        wbits = _ise_bits(wq, 16)
+        avail = 128 - 17 - wbits
+        fits = [q for q in range(4, 21) if _ise_bits(q, nvals) <= avail]
+        want = max(fits) if (24 <= wbits <= 96 and fits) else -1
+        assert oracle.endpoint_quant(wq, nvals) == want
+    # QUANT_2 weights (16 bits) are below the 24-bit minimum; QUANT_32 leaves
+    # 31 bits: QUANT_32 endpoints for RGB, QUANT_12 for RGBA
+    assert oracle.endpoint_quant(0, nvals) == -1
+    assert oracle.endpoint_quant(11, nvals) == (11 if nvals == 6 else 7)
+
+
+def _fit_texels(oracle, px, srgb):
+    tex = px.reshape(-1, 4).astype(np.float32)
+    if srgb:
+        tex[:, :3] = oracle.srgb_lut()[px.reshape(-1, 4)[:, :3]]
+    return tex
+
+
+def _decoded_error(oracle, blk, tex, dim, alpha, srgb):
+    """Squared error of the spec decode, accumulated as the search does."""
+    dec, _ = oracle.decode(blk.reshape(1, 16), dim, dim, dim, dim, srgb)
+    dec = dec.reshape(-1, 4).astype(np.float32)
+    err = np.float32(0)
+    for i in range(dim * dim):
+        for c in range(4 if alpha else 3):
+            d = np.float32(dec[i, c] - tex[i, c])
+            # fused multiply-add: d*d is exact in float64, one rounding
+            err = np.float32(np.float64(d) * np.float64(d) + np.float64(err))
+    return err
+
+
+def _random_block(rng, dim, kind):
+    px = rng.integers(0, 256, (dim, dim, 4)).astype(np.uint8)
+    if kind == 1:                                   # flat colour, noisy alpha
+        px[..., :3] = px[:1, :1, :3]
+    elif kind == 2:                                 # gradient with a little noise
+        ramp = np.linspace(0, 255, dim * dim * 4).reshape(dim, dim, 4)
+        px = np.clip(ramp + rng.integers(-6, 7, ramp.shape), 0, 255).astype(np.uint8)
+    elif kind == 3:                                 # two colours
+        a, b = rng.integers(0, 256, 4), rng.integers(0, 256, 4)
+        mask = rng.random((dim, dim)) < 0.5
+        px[mask], px[~mask] = a, b
+    return px
+
+
+@pytest.mark.parametrize("dim", [4, 6])
+@pytest.mark.parametrize("alpha", [False, True])
+@pytest.mark.parametrize("srgb", [False, True])
+@pytest.mark.parametrize("axis", [0, 1])
+def test_search_scores_match_the_spec_decode(oracle, dim, alpha, srgb, axis):
+    rng = np.random.default_rng(1000 * dim + 100 * alpha + 10 * srgb + axis)
+    chosen = set()
+    for trial in range(60):
+        px = _random_block(rng, dim, trial % 4)
+        tex = _fit_texels(oracle, px, srgb)
+        blk, wq, err, err_fixed = oracle.search_block(tex, dim, alpha, srgb, axis)
+        assert err <= err_fixed
+        assert _decoded_error(oracle, blk, tex, dim, alpha, srgb) == np.float32(err)
+        chosen.add(wq)
+    assert len(chosen) >= 3          # several ranges win on mixed content
+
+
+@pytest.mark.parametrize("dim", [4, 6])
+@pytest.mark.parametrize("alpha", [False, True])
+def test_search_image_never_worse_and_decodes(oracle, dim, alpha):
+    """Whole images: no error blocks, and per-block error never above the fixed mode."""
+    rgba = synth.rgb_noise(96, 80, seed=5) if not alpha else synth.rgba_cutout(96, 80, seed=6)
+    fixed = oracle.encode(rgba, block_dim=dim, has_alpha=alpha, border=1)
+    best = oracle.encode(rgba, block_dim=dim, has_alpha=alpha, border=1, quality=1)
+    assert (best != fixed).any(axis=1).mean() > 0.2
+    h, w = rgba.shape[:2]
+    ch = 4 if alpha else 3
+    dfix, e1 = oracle.decode(fixed, w, h, dim)
+    dbest, e2 = oracle.decode(best, w, h, dim)
+    assert e1 == 0 and e2 == 0
+
+    def block_sse(d):
+        diff = (d[..., :ch].astype(np.int64) - rgba[..., :ch]) ** 2
+        nby, nbx = -(-h // dim), -(-w // dim)
+        pad = np.zeros((nby * dim, nbx * dim, ch), np.int64)
+        pad[:h, :w] = diff
+        return pad.reshape(nby, dim, nbx, dim, ch).sum(axis=(1, 3, 4)).ravel()
+
+    # clamp border: edge blocks score replicated texels too, so compare the
+    # interior blocks exactly and the image as a whole
+    nby, nbx = -(-h // dim), -(-w // dim)
+    interior = np.zeros((nby, nbx), bool)
+    interior[: h // dim, : w // dim] = True
+    sf, sb = block_sse(dfix), block_sse(dbest)
+    assert (sb[interior.ravel()] <= sf[interior.ravel()]).all()
+    assert sb.sum() < sf.sum()
+
+
+@pytest.mark.parametrize("dim", [4, 6])
+def test_search_fp64_twin_runs(oracle, dim):
+    rgba = synth.rgb_noise(40, 40, seed=9)
+    a = oracle.encode(rgba, block_dim=dim, quality=1)
+    b = oracle.encode(rgba, block_dim=dim, quality=1, fp64=True)
+    assert (a == b).all(axis=1).mean() > 0.8
+
+
+@pytest.mark.parametrize("alpha", [False, True])
+def test_max_accumulation_two_colour_block(oracle, alpha):
+    """Two colours: every deviation above the mean is the bright colour's, so
+    the axis is (bright - mean) and the endpoints are the two colours."""
+    dark = np.array([10, 20, 30, 40 if alpha else 255], np.uint8)
+    bright = np.array([210, 120, 60, 250 if alpha else 255], np.uint8)
+    px = np.empty((4, 4, 4), np.uint8)
+    pattern = (np.arange(16) % 3 == 0).reshape(4, 4)
+    px[pattern], px[~pattern] = bright, dark
+    blocks = oracle.encode(px, block_dim=4, has_alpha=alpha, axis=1)
+    ep = np.zeros(8, np.uint32)
+    for c in range(4):
+        ep[2 * c], ep[2 * c + 1] = dark[c], bright[c]
+    qw = np.where(pattern.ravel(), 5 if alpha else 11, 0).astype(np.uint32)
+    want = oracle.assemble_symbolic(ep, qw, alpha)
+    assert np.array_equal(blocks[0], want)
+
+
+def test_max_accumulation_constant_block_equals_pca(oracle):
+    px = np.full((6, 6, 4), [90, 140, 200, 255], np.uint8)
+    assert np.array_equal(oracle.encode(px, block_dim=6, axis=1), oracle.encode(px, block_dim=6))
+
+
+def test_bad_axis_and_quality_rejected(oracle):
+    with pytest.raises(ValueError):
+        oracle.encode(np.zeros((4, 4, 4), np.uint8), axis=2)
+    with pytest.raises(ValueError):
+        oracle.encode(np.zeros((4, 4, 4), np.uint8), quality=3)
