@@ -45,11 +45,16 @@ __device__ __forceinline__ void load_search_smem(SearchSmem& sm) {
     for (int i = tid; i < 256; i += nt) {
         sm.trits[i] = g_search.trit_pack[i];
         if (i < 128) sm.quints[i] = g_search.quint_pack[i];
-        if (SRGB) sm.lut[i] = __uint_as_float(g_srgb_bits_s.v[i]);
+        if (SRGB) {
+            const float v = __uint_as_float(g_srgb_bits_s.v[i]);
+            sm.lut[i] = v;
+            sm.tbyte[i] = (uint8_t)rint_u32(v);
+        }
     }
     if (tid < 12) {
         sm.cq[tid] = g_search.cq[ALPHA][tid];
         sm.slot[tid] = g_search.slot[ALPHA][tid];
+        sm.wmax[tid] = (float)(quant_levels(tid) - 1);
     }
 }
 
@@ -79,19 +84,25 @@ __global__ void __launch_bounds__(kSearchThreads, 3) astc_encode_blocks_search(c
         return;
     }
     // the 16 grid-point colours every candidate projects: registers for 4x4,
-    // a [point][thread] shared array for 6x6 (whose 36 packed texels and
-    // the scoring loop already fill the register budget)
+    // a [point][thread] shared array for 6x6 (whose 36 target words and the
+    // scoring loop already fill the register budget); then the texels as
+    // the bytes the scoring compares with
+    uint32_t tw[N];
     if constexpr (DIM == 6) {
         extern __shared__ float4 s_grid[];
         SharedTexels<16> grid{s_grid + threadIdx.x, (int)blockDim.x};
 #pragma unroll
         for (int g = 0; g < 16; ++g) grid.put(g, grid_sample<DIM>(st, g));
-        p.out[b] = search_block<DIM, ALPHA, NORMAL, SRGB>(grid, px, q0, q1, qw, fixed, sm);
+#pragma unroll
+        for (int k = 0; k < N; ++k) tw[k] = target_word<ALPHA, NORMAL, SRGB>(px[k], sm.tbyte);
+        p.out[b] = search_block<DIM, ALPHA, SRGB>(grid, tw, q0, q1, qw, fixed, sm);
     } else {
         RegTexels<16> grid;
 #pragma unroll
         for (int g = 0; g < 16; ++g) grid.put(g, grid_sample<DIM>(st, g));
-        p.out[b] = search_block<DIM, ALPHA, NORMAL, SRGB>(grid, px, q0, q1, qw, fixed, sm);
+#pragma unroll
+        for (int k = 0; k < N; ++k) tw[k] = target_word<ALPHA, NORMAL, SRGB>(px[k], sm.tbyte);
+        p.out[b] = search_block<DIM, ALPHA, SRGB>(grid, tw, q0, q1, qw, fixed, sm);
     }
 }
 

@@ -11,10 +11,12 @@
 // one first, so the decoder neither swaps nor blue-contracts), projects the
 // grid colours onto the decoded endpoints and rounds the weights to the
 // range.  Every candidate is scored by the exact squared error of its spec
-// decode against the fit-space texels -- integers for UNORM input (exact
-// below 2^24), fused multiply-adds in texel-major, r-g-b-a order for sRGB --
-// and the first candidate with the least error is kept.  The oracle's search
-// mode follows the same steps, so blocks are bit-identical to it.
+// decode against the texels rounded to bytes in the fit space (UNORM codes
+// as they are, sRGB codes linearised x255 and rounded), in 32-bit integers,
+// and the first candidate with the least error is kept.  Weight ranges that
+// share an endpoint range share the endpoints and so the projections, which
+// are computed once per endpoint range.  The oracle's search mode follows
+// the same steps, so blocks are bit-identical to it.
 #pragma once
 #include <type_traits>
 
@@ -70,7 +72,9 @@ struct SearchSmem {
     uint8_t quints[128];
     int8_t cq[12];               // weight range -> endpoint range (-1: illegal)
     int8_t slot[12];             // weight range -> row of color (-1: QUANT_256)
-    float lut[256];
+    float wmax[12];              // weight range -> levels - 1
+    float lut[256];              // sRGB code -> linear x255 (fit texels)
+    uint8_t tbyte[256];          // sRGB code -> rint(linear x255) (scoring)
 };
 
 // ---------------------------------------------------------------------------
@@ -166,38 +170,38 @@ __device__ __forceinline__ uint4 assemble_search_block(int wq, int cq, const uin
 // ---------------------------------------------------------------------------
 // scoring
 // ---------------------------------------------------------------------------
-// The block's texels in the fit space as packed bytes (UNORM input): normal
-// maps read blue and alpha as 255, RGB blocks drop alpha (not scored).
-template <bool ALPHA, bool NORMAL>
-__device__ __forceinline__ uint32_t texel_word(uint32_t px) {
-    const uint32_t t = NORMAL ? (px | 0xFFFF0000u) : px;
+// The block's texels rounded to bytes in the fit space, packed r g b a:
+// normal maps read blue and alpha as 255, sRGB codes go through tbyte, RGB
+// blocks drop alpha (not scored).
+template <bool ALPHA, bool NORMAL, bool SRGB>
+__device__ __forceinline__ uint32_t target_word(uint32_t px, const uint8_t* tbyte) {
+    uint32_t t = px;
+    if (SRGB) {
+        t = (uint32_t)tbyte[px & 0xFFu] | ((uint32_t)tbyte[(px >> 8) & 0xFFu] << 8) |
+            ((uint32_t)tbyte[(px >> 16) & 0xFFu] << 16) | (px & 0xFF000000u);
+    }
+    if (NORMAL) t |= 0xFFFF0000u;
     return ALPHA ? t : (t & 0x00FFFFFFu);
 }
 
 // Squared error of the spec decode of endpoints E0/E1 (0..255) with grid
-// weights W (0..64) against the block's texels.  A decoded UNORM8 channel is
-// ((c0 * (64 - w) + c1 * w + 32) >> 6) >> 8 with c = e * 257 (linear) or
+// weights W (0..64) against the target words tw.  A decoded UNORM8 channel
+// is ((c0 * (64 - w) + c1 * w + 32) >> 6) >> 8 with c = e * 257 (linear) or
 // (e << 8) | 0x80 (sRGB), i.e. byte 2 of 4 * (64 * c0 + 32) + 4 * (c1 - c0) * w.
-// UNORM input: sum (dec - t)^2 = sum dec.dec - 2 sum dec.t + sum t.t over
-// packed bytes (__dp4a), exact in 32-bit integers (at most 36 * 4 * 255^2);
-// the last sum is per block (t2).  sRGB input: fused multiply-adds of the
-// float differences, texel-major, r g b (a), as the oracle accumulates them.
-template <int DIM, bool ALPHA, bool NORMAL, bool SRGB>
+// sum (dec - t)^2 = sum dec.dec - 2 sum dec.t + sum t.t over packed bytes
+// (__dp4a), exact in 32-bit integers (at most 36 * 4 * 255^2); the last sum
+// is per block (t2).
+template <int DIM, bool ALPHA, bool SRGB>
 struct BlockError {
-    typedef typename std::conditional<SRGB, float, uint32_t>::type T;
-
-    static __device__ __forceinline__ uint32_t texel_sq(const uint32_t (&px)[DIM * DIM]) {
+    static __device__ __forceinline__ uint32_t target_sq(const uint32_t (&tw)[DIM * DIM]) {
         uint32_t t2 = 0;
 #pragma unroll
-        for (int k = 0; k < DIM * DIM; ++k) {
-            const uint32_t t = texel_word<ALPHA, NORMAL>(px[k]);
-            t2 = __dp4a(t, t, t2);
-        }
+        for (int k = 0; k < DIM * DIM; ++k) t2 = __dp4a(tw[k], tw[k], t2);
         return t2;
     }
 
-    static __device__ __forceinline__ T eval(const uint32_t (&px)[DIM * DIM], const float* lut, uint32_t t2,
-                                             const int E0[4], const int E1[4], const int (&W)[16]) {
+    static __device__ __forceinline__ uint32_t eval(const uint32_t (&tw)[DIM * DIM], uint32_t t2,
+                                                    const int E0[4], const int E1[4], const int (&W)[16]) {
         constexpr int NCH = ALPHA ? 4 : 3;
         int base[NCH], delta[NCH];
 #pragma unroll
@@ -208,7 +212,6 @@ struct BlockError {
             delta[c] = 4 * (c1 - c0);
         }
         uint32_t dd = 0, dt = 0;
-        float errf = 0.0f;
 #pragma unroll
         for (int k = 0; k < DIM * DIM; ++k) {
             int w;
@@ -225,41 +228,23 @@ struct BlockError {
             uint32_t v[NCH];
 #pragma unroll
             for (int c = 0; c < NCH; ++c) v[c] = (uint32_t)(base[c] + delta[c] * w);   // decoded in byte 2
-            if constexpr (SRGB) {
-#pragma unroll
-                for (int c = 0; c < NCH; ++c) {
-                    float t;
-                    if (c == 3) t = NORMAL ? 255.0f : (float)(px[k] >> 24);
-                    else if (NORMAL && c == 2) t = 255.0f;
-                    else t = lds_f32_volatile(lut + ((px[k] >> (8 * c)) & 0xFFu));
-                    const float d = __fsub_rn(__int2float_rn((int)((v[c] >> 16) & 0xFFu)), t);
-                    errf = __fmaf_rn(d, d, errf);
-                }
-            } else {
-                uint32_t dec = __byte_perm(v[0], v[1], 0x3362u);             // r, g, 0, 0
-                dec = __byte_perm(dec, v[2], 0x3610u);                       // r, g, b, 0
-                if constexpr (ALPHA) dec = __byte_perm(dec, v[3], 0x6210u);  // r, g, b, a
-                dd = __dp4a(dec, dec, dd);
-                dt = __dp4a(dec, texel_word<ALPHA, NORMAL>(px[k]), dt);
-            }
+            uint32_t dec = __byte_perm(v[0], v[1], 0x3362u);             // r, g, 0, 0
+            dec = __byte_perm(dec, v[2], 0x3610u);                       // r, g, b, 0
+            if constexpr (ALPHA) dec = __byte_perm(dec, v[3], 0x6210u);  // r, g, b, a
+            dd = __dp4a(dec, dec, dd);
+            dt = __dp4a(dec, tw[k], dt);
         }
-        if constexpr (SRGB) {
-            (void)t2; (void)dd; (void)dt;
-            return errf;
-        } else {
-            (void)errf;
-            return dd - 2u * dt + t2;
-        }
+        return dd - 2u * dt + t2;
     }
 };
 
-// One candidate of weight range wq: endpoint symbols / decoded values and the
-// value-order weight indices q (0..levels-1) with their decoded weights W.
-template <bool ALPHA, class G>
-__device__ __forceinline__ void search_trial(int wq, const uint32_t q0[4], const uint32_t q1[4],
-                                             const G& s, const SearchSmem& sm, int slot, int cq,
-                                             int sym0[4], int sym1[4], int E0[4], int E1[4], uint32_t (&q)[16],
-                                             int (&W)[16]) {
+// Candidate endpoints for endpoint range cq: each rounded endpoint snapped to
+// the nearest representable value (symbols sym, decoded values E), the
+// darker (RGB sum) first.
+template <bool ALPHA>
+__device__ __forceinline__ void snap_endpoints(int cq, int slot, const uint32_t q0[4], const uint32_t q1[4],
+                                               const SearchSmem& sm, int sym0[4], int sym1[4], int E0[4],
+                                               int E1[4]) {
     constexpr int NCH = ALPHA ? 4 : 3;
 #pragma unroll
     for (int c = 0; c < 4; ++c) { sym0[c] = 0; sym1[c] = 0; E0[c] = 255; E1[c] = 255; }
@@ -281,67 +266,76 @@ __device__ __forceinline__ void search_trial(int wq, const uint32_t q0[4], const
             t = E0[c]; E0[c] = E1[c]; E1[c] = t;
         }
     }
+}
+
+// Projections of the grid colours on the decoded endpoints, clamped to [0, 1]
+// (all 0 for equal endpoints).
+template <class G>
+__device__ __forceinline__ void project_weights(const G& s, const int E0[4], const int E1[4], float (&wf)[16]) {
     const float d0 = (float)(E1[0] - E0[0]), d1 = (float)(E1[1] - E0[1]);
     const float d2 = (float)(E1[2] - E0[2]), d3 = (float)(E1[3] - E0[3]);
     const float dd = dot4(d0, d1, d2, d3, d0, d1, d2, d3);
-    const float R = (float)(quant_levels(wq) - 1);
     if (dd == 0.0f) {
 #pragma unroll
-        for (int g = 0; g < 16; ++g) q[g] = 0u;
-    } else {
-        const float r = __frcp_rn(dd);
-        const float f0 = (float)E0[0], f1 = (float)E0[1], f2 = (float)E0[2], f3 = (float)E0[3];
-#pragma unroll
-        for (int g = 0; g < 16; ++g) {
-            const float4 sg = s.get(g);
-            const float x = dot4(__fsub_rn(sg.x, f0), __fsub_rn(sg.y, f1), __fsub_rn(sg.z, f2),
-                                 __fsub_rn(sg.w, f3), d0, d1, d2, d3);
-            const float w = fminf(fmaxf(__fmul_rn(x, r), 0.0f), 1.0f);
-            q[g] = rint_u32(__fmul_rn(w, R));
-        }
+        for (int g = 0; g < 16; ++g) wf[g] = 0.0f;
+        return;
     }
+    const float r = __frcp_rn(dd);
+    const float f0 = (float)E0[0], f1 = (float)E0[1], f2 = (float)E0[2], f3 = (float)E0[3];
 #pragma unroll
-    for (int g = 0; g < 16; ++g) W[g] = sm.wval[wq][q[g]];
+    for (int g = 0; g < 16; ++g) {
+        const float4 sg = s.get(g);
+        const float x = dot4(__fsub_rn(sg.x, f0), __fsub_rn(sg.y, f1), __fsub_rn(sg.z, f2),
+                             __fsub_rn(sg.w, f3), d0, d1, d2, d3);
+        wf[g] = fminf(fmaxf(__fmul_rn(x, r), 0.0f), 1.0f);
+    }
 }
 
 // The search over one block.  `fixed` is the fixed-mode block with rounded
 // endpoints q0/q1 and weights qw; `grid` holds the 16 grid-point colours
-// (grid_sample of the texels), in registers or shared memory.
-template <int DIM, bool ALPHA, bool NORMAL, bool SRGB, class G>
-__device__ __forceinline__ uint4 search_block(const G& grid, const uint32_t (&px)[DIM * DIM], const uint32_t q0[4],
+// (grid_sample of the texels), in registers or shared memory; tw are the
+// target words.
+template <int DIM, bool ALPHA, bool SRGB, class G>
+__device__ __forceinline__ uint4 search_block(const G& grid, const uint32_t (&tw)[DIM * DIM], const uint32_t q0[4],
                                               const uint32_t q1[4], const uint32_t qw[16], const uint4 fixed,
                                               const SearchSmem& sm) {
-    typedef BlockError<DIM, ALPHA, NORMAL, SRGB> Err;
+    typedef BlockError<DIM, ALPHA, SRGB> Err;
     constexpr int WQ0 = ALPHA ? kQuant6 : kQuant12;
-    int E0[4], E1[4], W[16];
+    int E0[4], E1[4], sym0[4], sym1[4], W[16];
 #pragma unroll
     for (int c = 0; c < 4; ++c) { E0[c] = (int)q0[c]; E1[c] = (int)q1[c]; }
 #pragma unroll
     for (int g = 0; g < 16; ++g) W[g] = sm.wval[WQ0][qw[g]];
-    const uint32_t t2 = SRGB ? 0u : Err::texel_sq(px);
-    typename Err::T best = Err::eval(px, sm.lut, t2, E0, E1, W);
-    int best_wq = -1;
+    const uint32_t t2 = Err::target_sq(tw);
+    uint32_t best = Err::eval(tw, t2, E0, E1, W);
+    int best_wq = -1, prev_cq = -1;
+    float wf[16];
 #pragma unroll 1
     for (int wq = kQuant3; wq <= kQuant32; ++wq) {
         const int cq = sm.cq[wq];
         if (cq < 0) continue;
-        int sym0[4], sym1[4];
-        uint32_t q[16];
-        search_trial<ALPHA>(wq, q0, q1, grid, sm, sm.slot[wq], cq, sym0, sym1, E0, E1, q, W);
-        const typename Err::T err = Err::eval(px, sm.lut, t2, E0, E1, W);
+        if (cq != prev_cq) {                      // new endpoints: project again
+            snap_endpoints<ALPHA>(cq, sm.slot[wq], q0, q1, sm, sym0, sym1, E0, E1);
+            project_weights(grid, E0, E1, wf);
+            prev_cq = cq;
+        }
+        const float R = sm.wmax[wq];
+#pragma unroll
+        for (int g = 0; g < 16; ++g) W[g] = sm.wval[wq][rint_u32(__fmul_rn(wf[g], R))];
+        const uint32_t err = Err::eval(tw, t2, E0, E1, W);
         if (err < best) { best = err; best_wq = wq; }
     }
     if (best_wq < 0) return fixed;
     const int cq = sm.cq[best_wq];
-    int sym0[4], sym1[4];
-    uint32_t q[16];
-    search_trial<ALPHA>(best_wq, q0, q1, grid, sm, sm.slot[best_wq], cq, sym0, sym1, E0, E1, q, W);
+    snap_endpoints<ALPHA>(cq, sm.slot[best_wq], q0, q1, sm, sym0, sym1, E0, E1);
+    project_weights(grid, E0, E1, wf);
+    const float R = sm.wmax[best_wq];
     uint32_t ev[ALPHA ? 8 : 6];
 #pragma unroll
     for (int c = 0; c < (ALPHA ? 4 : 3); ++c) { ev[2 * c] = (uint32_t)sym0[c]; ev[2 * c + 1] = (uint32_t)sym1[c]; }
     uint32_t sw[16];
 #pragma unroll
-    for (int g = 0; g < 16; ++g) sw[g] = sm.scramble[best_wq][q[g]];
+    for (int g = 0; g < 16; ++g) sw[g] = sm.scramble[best_wq][rint_u32(__fmul_rn(wf[g], R))];
     return assemble_search_block<ALPHA>(best_wq, cq, ev, sw, sm);
 }
 

@@ -58,6 +58,8 @@ def _parse():
     ap.add_argument("--no-batched", action="store_true", help="skip the mixed batched workload")
     ap.add_argument("--batched-count", type=int, default=256, help="textures in the mixed batch")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving sweep")
+    ap.add_argument("--no-search", action="store_true",
+                    help="skip the search-mode / max-accumulation throughput and PSNR leg")
     ap.add_argument("--serving-rates", default="100,1000,5000,20000,50000,100000",
                     help="offered request rates (req/s)")
     ap.add_argument("--precision", default="fp32", choices=["fp32", "half2"],
@@ -269,6 +271,53 @@ def _time_launches(torch, native, texs, outs, spec, steps):
     launches = native.kernel_launch_count() - l0
     per_step = [a.elapsed_time(b) for a, b in ev]
     return sum(per_step) / max(1, launches), per_step, launches
+
+
+def _psnr_blocks(native, blocks: np.ndarray, tex: np.ndarray, spec: dict) -> float:
+    """Decoded PSNR in the space the encoder fits (GPU decoder, GPU SSE)."""
+    h, w = tex.shape[:2]
+    fitted = native.fitted_reference(tex, spec["srgb"], spec["is_normal"])
+    ch = 4 if spec["has_alpha"] else (2 if spec["is_normal"] else 3)
+    d = native.decode(blocks, w, h, spec["block_dim"])
+    s = native.sse(d, fitted)
+    return native.psnr_from_sse(float(s[:ch].sum()), h * w * ch)
+
+
+def _bench_search(torch, native, headline: str, texs, outs, spec: dict) -> dict:
+    """Throughput and decoded PSNR of the search mode (every single-partition
+    4x4-grid mode, least decoded error) and of the max-accumulation axis,
+    against the fixed mode, on each workload (device-resident inputs above
+    L2 size, as the headline)."""
+    from astc_encoder_gb300 import synth
+    result = {}
+    for name in (headline, "4x4_rgb_512", "4x4_normal_4096", "6x6_rgba_srgb_2048"):
+        if name in result:
+            continue
+        if name == headline:
+            st, so, sspec = texs, outs, dict(spec)
+        else:
+            simg, sspec = synth.workload(name)
+            sh, sw = simg.shape[:2]
+            sd = sspec["block_dim"]
+            snb = ((sw + sd - 1) // sd) * ((sh + sd - 1) // sd)
+            reps = max(1, (268 << 20) // (sh * sw * 4))
+            st = _texture_batch(torch, simg, reps, salt=11)
+            so = [torch.empty((snb, 16), dtype=torch.uint8, device="cuda") for _ in st]
+        sh, sw = st[0].shape[:2]
+        tex0 = st[0].cpu().numpy()
+        entry = {"textures_per_step": len(st)}
+        for label, kw in (("fast", {}), ("search", dict(quality=1)), ("max_accumulation", dict(axis=1))):
+            run = dict(sspec, **kw)
+            _time_launches(torch, native, st, so, run, 2)
+            per, steps, _ = _time_launches(torch, native, st, so, run, 5)
+            entry[label] = {"value": sh * sw * len(st) * 5 / (sum(steps) / 1e3) / 1e6, "unit": "Mtexels/s",
+                            "mean_launch_us": per * 1e3,
+                            "psnr_db": _psnr_blocks(native, so[0].cpu().numpy(), tex0, sspec)}
+        entry["search_gain_db"] = entry["search"]["psnr_db"] - entry["fast"]["psnr_db"]
+        result[name] = entry
+        if name != headline:
+            del st, so
+    return result
 
 
 def _bench_batched(torch, native, oracle, count: int, reps: int = 5) -> dict:
@@ -599,6 +648,7 @@ def run_ours(args) -> None:
                            "textures_per_step": reps}
             del xt, xo
 
+    search = None if args.no_search else _bench_search(torch, native, args.workload, texs, outs, spec)
     batched = None if args.no_batched else _bench_batched(torch, native, oracle, args.batched_count)
     serving = None if args.no_serving else _bench_serving(
         torch, native, [int(r) for r in args.serving_rates.split(",") if r])
@@ -616,7 +666,8 @@ def run_ours(args) -> None:
                    "l2": f"inputs {texels_step * 4 / 2**20:.0f} MiB per step, distinct per texture "
                          "(> 129 MB L2); no flush needed",
                    "parallelism": f"replicas{world}",
-                   "kernel_variant": {"store": "shared" if tuned.store else "registers",
+                   "kernel_variant": {"store": {0: "registers", 1: "shared",
+                                                2: "registers_capped"}.get(tuned.store, tuned.store),
                                       "threads_per_cta": tuned.threads,
                                       "autotune_best_us": tuned.best_us}},
         "e2e": {"value": e2e_value, "unit": "Mtexels/s",
@@ -637,6 +688,7 @@ def run_ours(args) -> None:
         "clocks": clk,
         "wall_s_timed_region": wall,
         "extra_workloads": extra,
+        "search_mode": search,
         "batched_mixed": batched,
         "serving": serving,
     }

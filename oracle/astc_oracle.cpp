@@ -791,17 +791,18 @@ struct Pipe {
     }
 
     // ---- search mode -----------------------------------------------------
-    // Squared error, in the fit space, of a decoded single-partition block
-    // with endpoints E0/E1 (0..255) and grid weights wv (0..64): texels in
-    // row-major order, channels r g b (a), accumulated with mad.
-    static T block_error(const T (*tex)[4], int dim, int nch, bool srgb, const int E0[4],
-                         const int E1[4], const int wv[16]) {
-        T err = 0;
+    // Squared error of a decoded single-partition block with endpoints E0/E1
+    // (0..255) and grid weights wv (0..64) against the texels rounded to
+    // bytes in the fit space (tb: UNORM codes as they are, sRGB codes
+    // linearised x255 and rounded), channels r g b (a).  Exact integers.
+    static uint32_t block_error(const int (*tb)[4], int dim, int nch, bool srgb, const int E0[4],
+                                const int E1[4], const int wv[16]) {
+        uint32_t err = 0;
         for (int i = 0; i < dim * dim; ++i) {
             const int w = dim == 4 ? wv[i] : infill_6x6(wv, i % 6, i / 6);
             for (int c = 0; c < nch; ++c) {
-                const T d = P::sub((T)decode_channel(E0[c], E1[c], w, srgb), tex[i][c]);
-                err = P::mad(d, d, err);
+                const int d = decode_channel(E0[c], E1[c], w, srgb) - tb[i][c];
+                err += (uint32_t)(d * d);
             }
         }
         return err;
@@ -856,8 +857,11 @@ struct Pipe {
     // The fixed-mode block, then every weight range QUANT_3..QUANT_32 with
     // its endpoint range; the first candidate with the least error is kept.
     static void search(const T (*tex)[4], int dim, bool alpha, bool srgb, int axis, uint8_t out[16],
-                       int* chosen, T* best_err, T* fixed_err) {
+                       int* chosen, uint32_t* best_err, uint32_t* fixed_err) {
         const int nch = alpha ? 4 : 3;
+        int tb[36][4];
+        for (int i = 0; i < dim * dim; ++i)
+            for (int c = 0; c < 4; ++c) tb[i][c] = (int)P::rint(tex[i][c]);
         T e0[4], e1[4];
         fit(tex, dim * dim, alpha, axis, e0, e1);
         uint32_t ep_q[8], qw[16];
@@ -865,7 +869,7 @@ struct Pipe {
         int E0[4], E1[4], wv[16];
         for (int c = 0; c < 4; ++c) { E0[c] = (int)ep_q[2 * c]; E1[c] = (int)ep_q[2 * c + 1]; }
         trial_weights(alpha ? QUANT_6 : QUANT_12, qw, wv);
-        T best = block_error(tex, dim, nch, srgb, E0, E1, wv);
+        uint32_t best = block_error(tb, dim, nch, srgb, E0, E1, wv);
         *fixed_err = best;
         *chosen = -1;
         T s[16][4];
@@ -876,7 +880,7 @@ struct Pipe {
             Trial tr;
             trial(s, e0, e1, alpha, wq, tr);
             trial_weights(wq, tr.q, wv);
-            const T err = block_error(tex, dim, nch, srgb, tr.E0, tr.E1, wv);
+            const uint32_t err = block_error(tb, dim, nch, srgb, tr.E0, tr.E1, wv);
             if (err < best) { best = err; *chosen = wq; keep = tr; }
         }
         if (*chosen >= 0) assemble_trial(keep, alpha, out);
@@ -940,7 +944,7 @@ struct Pipe {
             fetch(rgba, w, h, bx, by, *o, tex);
             if (o->quality) {
                 int chosen;
-                T err, err_fixed;
+                uint32_t err, err_fixed;
                 search(tex, dim, o->has_alpha != 0, o->srgb != 0, o->axis, out + 16 * b, &chosen, &err,
                        &err_fixed);
                 continue;
@@ -1362,7 +1366,7 @@ int oracle_endpoint_quant(int wq, int nvals) {
 }
 
 int oracle_search_block_fp32(const float* texels, int block_dim, int has_alpha, int srgb, int axis,
-                             uint8_t out[16], int* chosen_wq, float* err, float* err_fixed) {
+                             uint8_t out[16], int* chosen_wq, uint32_t* err, uint32_t* err_fixed) {
     if (!texels || !out || !chosen_wq || !err || !err_fixed) return -1;
     if ((block_dim != 4 && block_dim != 6) || (axis != 0 && axis != 1)) return -1;
     float tex[36][4];

@@ -40,9 +40,10 @@ typedef struct oracle_opts {
                         the fixed-mode block plus every single-partition
                         4x4-grid weight range QUANT_3..QUANT_32 with the
                         largest endpoint range that fits, keeping the
-                        candidate with the least decoded error (the
-                        choose_best_quantmethod the shader sketches at
-                        524-526)                                            */
+                        candidate whose decode has the least squared error
+                        against the texels rounded to bytes in the fit
+                        space (the choose_best_quantmethod the shader
+                        sketches at 524-526)                                */
 } oracle_opts;
 
 /* Encode a tightly packed RGBA8 image (row 0 first) into 16-byte blocks in
@@ -106,10 +107,11 @@ double oracle_flops_per_block(int block_dim, int has_alpha, int is_normal);
 int oracle_endpoint_quant(int wq, int nvals);
 /* Encode one block (texels: N*4 floats, 0..255, the fit space) in search
  * mode with FP32 arithmetic.  *chosen_wq = weight quant method of the block
- * kept (-1 when the fixed-mode block was kept), *err = its squared error in
- * the fit space, *err_fixed = the fixed-mode block's. */
+ * kept (-1 when the fixed-mode block was kept), *err = the squared error of
+ * its decode against the texels rounded to bytes, *err_fixed = the
+ * fixed-mode block's. */
 int oracle_search_block_fp32(const float* texels, int block_dim, int has_alpha, int srgb, int axis,
-                             uint8_t out[16], int* chosen_wq, float* err, float* err_fixed);
+                             uint8_t out[16], int* chosen_wq, uint32_t* err, uint32_t* err_fixed);
 
 #ifdef __cplusplus
 }

@@ -193,12 +193,13 @@ def search_block(texels: np.ndarray, block_dim: int, has_alpha: bool, srgb: bool
     """Search-mode FP32 encode of one block of fit-space texels (N x 4 floats).
 
     Returns (block bytes, chosen weight quant method or -1 for the fixed-mode
-    block, its squared error, the fixed-mode block's squared error)."""
+    block, the squared error of its decode against the texels rounded to
+    bytes, the fixed-mode block's)."""
     t = np.ascontiguousarray(texels, dtype=np.float32).reshape(-1)
     out = np.zeros(16, np.uint8)
     wq = ctypes.c_int(0)
-    err = ctypes.c_float(0)
-    err_fixed = ctypes.c_float(0)
+    err = ctypes.c_uint32(0)
+    err_fixed = ctypes.c_uint32(0)
     rc = lib().oracle_search_block_fp32(t.ctypes.data, block_dim, int(has_alpha), int(srgb), int(axis),
                                         out.ctypes.data, ctypes.byref(wq), ctypes.byref(err),
                                         ctypes.byref(err_fixed))

@@ -54,16 +54,12 @@ def _fit_texels(oracle, px, srgb):
 
 
 def _decoded_error(oracle, blk, tex, dim, alpha, srgb):
-    """Squared error of the spec decode, accumulated as the search does."""
+    """Squared error of the spec decode against the texels rounded to bytes."""
     dec, _ = oracle.decode(blk.reshape(1, 16), dim, dim, dim, dim, srgb)
-    dec = dec.reshape(-1, 4).astype(np.float32)
-    err = np.float32(0)
-    for i in range(dim * dim):
-        for c in range(4 if alpha else 3):
-            d = np.float32(dec[i, c] - tex[i, c])
-            # fused multiply-add: d*d is exact in float64, one rounding
-            err = np.float32(np.float64(d) * np.float64(d) + np.float64(err))
-    return err
+    dec = dec.reshape(-1, 4).astype(np.int64)
+    target = np.rint(tex).astype(np.int64)
+    ch = 4 if alpha else 3
+    return int(((dec[:, :ch] - target[:, :ch]) ** 2).sum())
 
 
 def _random_block(rng, dim, kind):
@@ -92,7 +88,7 @@ def test_search_scores_match_the_spec_decode(oracle, dim, alpha, srgb, axis):
         tex = _fit_texels(oracle, px, srgb)
         blk, wq, err, err_fixed = oracle.search_block(tex, dim, alpha, srgb, axis)
         assert err <= err_fixed
-        assert _decoded_error(oracle, blk, tex, dim, alpha, srgb) == np.float32(err)
+        assert _decoded_error(oracle, blk, tex, dim, alpha, srgb) == err
         chosen.add(wq)
     assert len(chosen) >= 3          # several ranges win on mixed content
 
