@@ -20,6 +20,7 @@
 //                      unused choose_best_quantmethod; FP32 only)
 //   --max-accumulation fit endpoints with the reference's unused
 //                      max_accumulation_pixel_direction instead of the PCA
+//   --thorough         --search from the better of the two fits
 //   -o PATH            output path
 //   --dump-rgba PATH   write the loaded (flipped) RGBA image as PAM and exit
 //                      without encoding (no GPU needed)
@@ -43,7 +44,7 @@ std::string strip_file_extension(const std::string& path) {
 
 int usage() {
     std::cout << "usage: astc_cs_enc input_texture [-4x4|-6x6] [-alpha] [-norm] [-srgb]"
-                 " [--clamp] [--half2] [--search] [--max-accumulation] [-o out.astc]"
+                 " [--clamp] [--half2] [--search] [--max-accumulation] [--thorough] [-o out.astc]"
                  " [--dump-rgba out.pam]" << std::endl;
     return -1;
 }
@@ -57,7 +58,7 @@ int main(int argc, char** argv) {
     }
     const std::string src = argv[1];
     bool is4x4 = true, alpha = false, norm = false, srgb = false, clamp = false, half2 = false;
-    bool search = false, max_acc = false;
+    bool search = false, max_acc = false, thorough = false;
     std::string out_path, dump_path;
     for (int i = 2; i < argc; ++i) {
         const std::string a = argv[i];
@@ -70,6 +71,7 @@ int main(int argc, char** argv) {
         else if (a == "--half2") half2 = true;
         else if (a == "--search") search = true;
         else if (a == "--max-accumulation") max_acc = true;
+        else if (a == "--thorough") thorough = true;
         else if (a == "-o" && i + 1 < argc) out_path = argv[++i];
         else if (a == "--dump-rgba" && i + 1 < argc) dump_path = argv[++i];
         else std::cerr << "ignoring unknown argument: " << a << std::endl;
@@ -105,7 +107,7 @@ int main(int argc, char** argv) {
     o.srgb = srgb && !norm;                                     // main.cpp:214
     o.border = clamp ? ASTC_BORDER_CLAMP : ASTC_BORDER_ZERO;
     o.precision = half2 ? ASTC_PRECISION_HALF2 : ASTC_PRECISION_FP32;
-    o.quality = search ? ASTC_QUALITY_SEARCH : ASTC_QUALITY_FAST;
+    o.quality = thorough ? ASTC_QUALITY_THOROUGH : (search ? ASTC_QUALITY_SEARCH : ASTC_QUALITY_FAST);
     o.axis = max_acc ? ASTC_AXIS_MAX_ACCUMULATION : ASTC_AXIS_PCA;
     std::vector<uint8_t> blocks(astc_encoded_size(img.width, img.height, o.block_dim));
     astc_status st = astc_encode_gpu(img.rgba.data(), img.width, img.height, &o, blocks.data());

@@ -36,8 +36,10 @@ struct TextureView;
 TextureView make_view(const EncodeJob& job);
 // Packed-half2 pipeline (astc_encode_h2.cu).
 cudaError_t launch_encode_h2(const EncodeJob& job, cudaStream_t stream);
-// FP32 with the max-accumulation axis and/or the mode search (astc_encode_search.cu).
+// FP32 with the max-accumulation axis and/or the mode search (astc_encode_search.cu);
+// the search from the better of both fits (astc_encode_thorough.cu).
 cudaError_t launch_encode_search(const EncodeJob& job, cudaStream_t stream);
+cudaError_t launch_encode_thorough(const EncodeJob& job, cudaStream_t stream);
 
 // Decoder / SSE launchers (astc_decode.cu).
 cudaError_t launch_decode(const uint8_t* blocks, int width, int height, int bw, int bh,

@@ -1,0 +1,216 @@
+// astc_search_kernel.cuh -- the sm_103a kernel of the FP32 encoder's
+// reference-defined alternatives to its fixed pipeline, included by the two
+// translation units that instantiate it (astc_encode_search.cu: fixed mode
+// with the max-accumulation axis, and the search; astc_encode_thorough.cu:
+// the search from the better of both fits), so each compiles in parallel
+// and gets its own register allocation:
+//   axis   = ASTC_AXIS_MAX_ACCUMULATION: the endpoint fit the reference
+//            shader defines but leaves commented out
+//            (max_accumulation_pixel_direction, ASTC_Encode.hlsl:170-227, 515);
+//   quality = ASTC_QUALITY_SEARCH: the choose_best_quantmethod the shader
+//            sketches at 524-526 -- every single-partition 4x4-grid mode,
+//            scored by its exact decode (astc_pipeline_search.cuh);
+//   quality = ASTC_QUALITY_THOROUGH: both fits, the search from the one
+//            whose fixed-mode block decodes with the smaller error (the
+//            PCA on ties).
+// One thread encodes one block.  Texels stay packed (one register each) and
+// are re-decoded per pass, which keeps the 36-texel 6x6 search in registers.
+// Compile including units with --fmad=false: blocks are bit-identical to the
+// FP32 oracle.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "astc_internal.h"
+#include "astc_pipeline_search.cuh"
+
+namespace astc {
+namespace {
+
+constexpr int kSearchThreads = 128;
+
+__device__ const SearchTables g_search = make_search_tables();
+__device__ const SrgbBits g_srgb_bits_s = make_srgb_bits();
+
+struct SearchLaunch {
+    TextureView tex;
+    long long nblocks;
+    uint4* out;
+    int axis;     // 0 = PCA, 1 = max accumulation
+    int search;   // 0 = fixed mode, 1 = search, 2 = search from the better fit
+};
+
+template <bool ALPHA, bool SRGB>
+__device__ __forceinline__ void load_search_smem(SearchSmem& sm) {
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const uint32_t* src = reinterpret_cast<const uint32_t*>(&g_search.color[ALPHA][0][0]);
+    uint32_t* dst = reinterpret_cast<uint32_t*>(&sm.color[0][0]);
+    const int words = g_search.nslots[ALPHA] * 128;
+    for (int i = tid; i < words; i += nt) dst[i] = src[i];
+    for (int i = tid; i < 12 * 32; i += nt) {
+        sm.wval[i >> 5][i & 31] = g_search.wval[i >> 5][i & 31];
+        sm.scramble[i >> 5][i & 31] = g_search.scramble[i >> 5][i & 31];
+    }
+    for (int i = tid; i < 256; i += nt) {
+        sm.trits[i] = g_search.trit_pack[i];
+        if (i < 128) sm.quints[i] = g_search.quint_pack[i];
+        if (SRGB) {
+            const float v = __uint_as_float(g_srgb_bits_s.v[i]);
+            sm.lut[i] = v;
+            sm.tbyte[i] = (uint8_t)rint_u32(v);
+        }
+    }
+    if (tid < 12) {
+        sm.cq[tid] = g_search.cq[ALPHA][tid];
+        sm.slot[tid] = g_search.slot[ALPHA][tid];
+        sm.wmax[tid] = (float)(quant_levels(tid) - 1);
+    }
+}
+
+// Endpoint fit on `axis` and the fixed-mode block (encode_block 510-550).
+template <int DIM, bool ALPHA, class S>
+__device__ __forceinline__ uint4 fit_fixed(const S& st, int axis, uint32_t q0[4], uint32_t q1[4],
+                                           uint32_t qw[16], const uint8_t* trits) {
+    constexpr int N = DIM * DIM;
+    const float4 m = block_mean<N>(st);
+    const float4 v = axis ? max_accumulation_axis<N, ALPHA>(st, m) : pca_axis<N>(st, m);
+    float e0[4], e1[4];
+    find_min_max<N, ALPHA>(st, m, v, e0, e1, q0, q1);
+    reference_weights<DIM, ALPHA>(st, e0, e1, qw);
+    return assemble_block<ALPHA>(q0, q1, qw, trits);
+}
+
+// Keeps, of two fits, the one whose fixed-mode block decodes with the
+// smaller error (the first on ties).  The second fit is carried as its block
+// (its QUANT_256 endpoints are bits 17.. in r0 r1 g0 g1 b0 b1 a0 a1 order)
+// and its weights packed 4 bits each.
+template <int DIM, bool ALPHA, bool SRGB>
+__device__ __forceinline__ void pick_fit(const uint32_t (&tw)[DIM * DIM], const SearchSmem& sm, uint32_t q0[4],
+                                         uint32_t q1[4], uint32_t qw[16], uint4& fixed, const uint4 fixed_b,
+                                         uint64_t rw_packed) {
+    typedef BlockError<DIM, ALPHA, SRGB> Err;
+    constexpr int WQ0 = ALPHA ? kQuant6 : kQuant12;
+    const uint32_t t2 = Err::target_sq(tw);
+    const uint64_t ep = (((uint64_t)fixed_b.y << 32 | fixed_b.x) >> 17) | (((uint64_t)fixed_b.w << 32 | fixed_b.z) << 47);
+    uint32_t r0[4], r1[4], rw[16];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        r0[c] = (ALPHA || c < 3) ? (uint32_t)(ep >> (16 * c)) & 0xFFu : 255u;
+        r1[c] = (ALPHA || c < 3) ? (uint32_t)(ep >> (16 * c + 8)) & 0xFFu : 255u;
+    }
+#pragma unroll
+    for (int g = 0; g < 16; ++g) rw[g] = (uint32_t)(rw_packed >> (4 * g)) & 0xFu;
+    int E0[4], E1[4], W[16];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) { E0[c] = (int)q0[c]; E1[c] = (int)q1[c]; }
+#pragma unroll
+    for (int g = 0; g < 16; ++g) W[g] = sm.wval[WQ0][qw[g]];
+    const uint32_t ea = Err::eval(tw, t2, E0, E1, W);
+#pragma unroll
+    for (int c = 0; c < 4; ++c) { E0[c] = (int)r0[c]; E1[c] = (int)r1[c]; }
+#pragma unroll
+    for (int g = 0; g < 16; ++g) W[g] = sm.wval[WQ0][rw[g]];
+    const uint32_t eb = Err::eval(tw, t2, E0, E1, W);
+    if (eb < ea) {
+#pragma unroll
+        for (int c = 0; c < 4; ++c) { q0[c] = r0[c]; q1[c] = r1[c]; }
+#pragma unroll
+        for (int g = 0; g < 16; ++g) qw[g] = rw[g];
+        fixed = fixed_b;
+    }
+}
+
+template <int DIM, bool ALPHA, bool NORMAL, bool SRGB, bool THOROUGH>
+__global__ void __launch_bounds__(kSearchThreads, 3) astc_encode_blocks_search(const SearchLaunch p) {
+    constexpr int N = DIM * DIM;
+    __shared__ SearchSmem sm;
+    load_search_smem<ALPHA, SRGB>(sm);
+    __syncthreads();
+    const long long b = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= p.nblocks) return;
+    const int by = (int)(b / p.tex.nbx);
+    const int bx = (int)(b - (long long)by * p.tex.nbx);
+    uint32_t px[N];
+    load_block_packed<DIM>(p.tex, bx, by, px);
+    const PackedTexels<N, SRGB, NORMAL> st{px, sm.lut};
+    constexpr bool thorough = THOROUGH;
+    uint32_t q0[4], q1[4], qw[16];
+    uint4 fixed = fit_fixed<DIM, ALPHA>(st, thorough ? 0 : p.axis, q0, q1, qw, sm.trits);
+    if (!THOROUGH && !p.search) {
+        p.out[b] = fixed;
+        return;
+    }
+    uint4 fixed_b = fixed;
+    uint64_t rw_packed = 0;
+    if constexpr (thorough) {
+        uint32_t r0[4], r1[4], rw[16];
+        fixed_b = fit_fixed<DIM, ALPHA>(st, 1, r0, r1, rw, sm.trits);
+#pragma unroll
+        for (int g = 0; g < 16; ++g) rw_packed |= (uint64_t)rw[g] << (4 * g);
+    }
+    // the 16 grid-point colours every candidate projects: registers for 4x4,
+    // a [point][thread] shared array for 6x6 (whose 36 target words and the
+    // scoring loop already fill the register budget); then the texels as
+    // the bytes the scoring compares with
+    uint32_t tw[N];
+    if constexpr (DIM == 6) {
+        extern __shared__ float4 s_grid[];
+        SharedTexels<16> grid{s_grid + threadIdx.x, (int)blockDim.x};
+#pragma unroll
+        for (int g = 0; g < 16; ++g) grid.put(g, grid_sample<DIM>(st, g));
+#pragma unroll
+        for (int k = 0; k < N; ++k) tw[k] = target_word<ALPHA, NORMAL, SRGB>(px[k], sm.tbyte);
+        if constexpr (thorough) pick_fit<DIM, ALPHA, SRGB>(tw, sm, q0, q1, qw, fixed, fixed_b, rw_packed);
+        p.out[b] = search_block<DIM, ALPHA, SRGB>(grid, tw, q0, q1, qw, fixed, sm);
+    } else {
+        RegTexels<16> grid;
+#pragma unroll
+        for (int g = 0; g < 16; ++g) grid.put(g, grid_sample<DIM>(st, g));
+#pragma unroll
+        for (int k = 0; k < N; ++k) tw[k] = target_word<ALPHA, NORMAL, SRGB>(px[k], sm.tbyte);
+        if constexpr (thorough) pick_fit<DIM, ALPHA, SRGB>(tw, sm, q0, q1, qw, fixed, fixed_b, rw_packed);
+        p.out[b] = search_block<DIM, ALPHA, SRGB>(grid, tw, q0, q1, qw, fixed, sm);
+    }
+}
+
+template <int DIM, bool ALPHA, bool NORMAL, bool SRGB, bool THOROUGH>
+cudaError_t launch_t(const SearchLaunch& p, cudaStream_t s) {
+    const long long grid = (p.nblocks + kSearchThreads - 1) / kSearchThreads;
+    const size_t smem = (DIM == 6 && p.search) ? (size_t)16 * kSearchThreads * sizeof(float4) : 0;
+    astc_encode_blocks_search<DIM, ALPHA, NORMAL, SRGB, THOROUGH><<<(unsigned)grid, kSearchThreads, smem, s>>>(p);
+    return cudaGetLastError();
+}
+
+template <bool THOROUGH, int DIM, bool ALPHA, bool NORMAL>
+cudaError_t launch_srgb(const SearchLaunch& p, bool srgb, cudaStream_t s) {
+    return srgb ? launch_t<DIM, ALPHA, NORMAL, true, THOROUGH>(p, s)
+                : launch_t<DIM, ALPHA, NORMAL, false, THOROUGH>(p, s);
+}
+template <bool THOROUGH, int DIM, bool ALPHA>
+cudaError_t launch_norm(const SearchLaunch& p, bool normal, bool srgb, cudaStream_t s) {
+    return normal ? launch_srgb<THOROUGH, DIM, ALPHA, true>(p, srgb, s)
+                  : launch_srgb<THOROUGH, DIM, ALPHA, false>(p, srgb, s);
+}
+template <bool THOROUGH, int DIM>
+cudaError_t launch_alpha(const SearchLaunch& p, bool alpha, bool normal, bool srgb, cudaStream_t s) {
+    return alpha ? launch_norm<THOROUGH, DIM, true>(p, normal, srgb, s)
+                 : launch_norm<THOROUGH, DIM, false>(p, normal, srgb, s);
+}
+
+template <bool THOROUGH>
+cudaError_t launch_search_kernels(const EncodeJob& j, cudaStream_t stream) {
+    SearchLaunch p;
+    p.tex = make_view(j);
+    p.nblocks = (long long)p.tex.nbx * blocks_y(j.height, j.block_dim);
+    p.out = reinterpret_cast<uint4*>(j.out);
+    p.axis = j.axis;
+    p.search = j.quality == ASTC_QUALITY_FAST ? 0 : 1;
+    const bool alpha = j.has_alpha != 0, normal = j.is_normal != 0, srgb = j.srgb != 0;
+    const cudaError_t e = j.block_dim == 4 ? launch_alpha<THOROUGH, 4>(p, alpha, normal, srgb, stream)
+                                           : launch_alpha<THOROUGH, 6>(p, alpha, normal, srgb, stream);
+    if (e == cudaSuccess) count_launches(1);
+    return e;
+}
+
+}  // namespace
+}  // namespace astc

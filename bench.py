@@ -306,7 +306,8 @@ def _bench_search(torch, native, headline: str, texs, outs, spec: dict) -> dict:
         sh, sw = st[0].shape[:2]
         tex0 = st[0].cpu().numpy()
         entry = {"textures_per_step": len(st)}
-        for label, kw in (("fast", {}), ("search", dict(quality=1)), ("max_accumulation", dict(axis=1))):
+        for label, kw in (("fast", {}), ("search", dict(quality=1)), ("max_accumulation", dict(axis=1)),
+                          ("thorough", dict(quality=2))):
             run = dict(sspec, **kw)
             _time_launches(torch, native, st, so, run, 2)
             per, steps, _ = _time_launches(torch, native, st, so, run, 5)
@@ -314,6 +315,7 @@ def _bench_search(torch, native, headline: str, texs, outs, spec: dict) -> dict:
                             "mean_launch_us": per * 1e3,
                             "psnr_db": _psnr_blocks(native, so[0].cpu().numpy(), tex0, sspec)}
         entry["search_gain_db"] = entry["search"]["psnr_db"] - entry["fast"]["psnr_db"]
+        entry["thorough_gain_db"] = entry["thorough"]["psnr_db"] - entry["fast"]["psnr_db"]
         result[name] = entry
         if name != headline:
             del st, so

@@ -74,14 +74,23 @@ typedef enum astc_quality {
     ASTC_QUALITY_FAST = 0,       /* the reference's fixed mode (518-522):
                                     QUANT_12 (RGB) / QUANT_6 (RGBA) weights,
                                     QUANT_256 endpoints                     */
-    ASTC_QUALITY_SEARCH = 1      /* the fixed-mode block and every single-
+    ASTC_QUALITY_SEARCH = 1,     /* the fixed-mode block and every single-
                                     partition 4x4-grid mode (weight ranges
                                     QUANT_3..QUANT_32, each with the largest
                                     endpoint range that fits), keeping the
                                     one whose decode has the least squared
-                                    error; the choose_best_quantmethod the
+                                    error against the texels rounded to
+                                    bytes in the fit space; the
+                                    choose_best_quantmethod the
                                     reference sketches (524-526).  Never
                                     worse than FAST; FP32 only              */
+    ASTC_QUALITY_THOROUGH = 2    /* SEARCH from the better of the two fits:
+                                    PCA and max accumulation both run, the
+                                    one whose fixed-mode block decodes with
+                                    less error is searched from (PCA on
+                                    ties; opts.axis is ignored).  Recovers
+                                    the blocks the reference's PCA collapses
+                                    (flat colour, varying alpha); FP32 only */
 } astc_quality;
 
 /* Encoder options: the reference's encode_option (astc_encode.h:14-28) plus

@@ -856,6 +856,8 @@ struct Pipe {
 
     // The fixed-mode block, then every weight range QUANT_3..QUANT_32 with
     // its endpoint range; the first candidate with the least error is kept.
+    // axis 2 fits both ways and searches from the fit whose fixed-mode block
+    // has the smaller error (the PCA on ties).
     static void search(const T (*tex)[4], int dim, bool alpha, bool srgb, int axis, uint8_t out[16],
                        int* chosen, uint32_t* best_err, uint32_t* fixed_err) {
         const int nch = alpha ? 4 : 3;
@@ -863,13 +865,27 @@ struct Pipe {
         for (int i = 0; i < dim * dim; ++i)
             for (int c = 0; c < 4; ++c) tb[i][c] = (int)P::rint(tex[i][c]);
         T e0[4], e1[4];
-        fit(tex, dim * dim, alpha, axis, e0, e1);
-        uint32_t ep_q[8], qw[16];
-        fixed_mode(tex, dim, alpha, e0, e1, ep_q, qw, out);
-        int E0[4], E1[4], wv[16];
-        for (int c = 0; c < 4; ++c) { E0[c] = (int)ep_q[2 * c]; E1[c] = (int)ep_q[2 * c + 1]; }
-        trial_weights(alpha ? QUANT_6 : QUANT_12, qw, wv);
-        uint32_t best = block_error(tb, dim, nch, srgb, E0, E1, wv);
+        uint32_t ep_q[8], qw[16], best = 0;
+        const int a_first = axis == 2 ? 0 : axis, a_last = axis == 2 ? 1 : axis;
+        for (int a = a_first; a <= a_last; ++a) {
+            T f0[4], f1[4];
+            uint32_t fe[8], fw[16];
+            uint8_t fb[16];
+            fit(tex, dim * dim, alpha, a, f0, f1);
+            fixed_mode(tex, dim, alpha, f0, f1, fe, fw, fb);
+            int E0[4], E1[4], wv[16];
+            for (int c = 0; c < 4; ++c) { E0[c] = (int)fe[2 * c]; E1[c] = (int)fe[2 * c + 1]; }
+            trial_weights(alpha ? QUANT_6 : QUANT_12, fw, wv);
+            const uint32_t err = block_error(tb, dim, nch, srgb, E0, E1, wv);
+            if (a == a_first || err < best) {
+                best = err;
+                for (int c = 0; c < 4; ++c) { e0[c] = f0[c]; e1[c] = f1[c]; }
+                std::memcpy(ep_q, fe, sizeof(ep_q));
+                std::memcpy(qw, fw, sizeof(qw));
+                std::memcpy(out, fb, 16);
+            }
+        }
+        int wv[16];
         *fixed_err = best;
         *chosen = -1;
         T s[16][4];
@@ -927,7 +943,7 @@ struct Pipe {
         if (o->block_dim != 4 && o->block_dim != 6) return -2;
         if (o->border != 0 && o->border != 1) return -3;
         if (o->axis != 0 && o->axis != 1) return -4;
-        if (o->quality != 0 && o->quality != 1) return -5;
+        if (o->quality < 0 || o->quality > 2) return -5;
         tables();
         const int dim = o->block_dim;
         const int nbx = (w + dim - 1) / dim, nby = (h + dim - 1) / dim;
@@ -945,8 +961,8 @@ struct Pipe {
             if (o->quality) {
                 int chosen;
                 uint32_t err, err_fixed;
-                search(tex, dim, o->has_alpha != 0, o->srgb != 0, o->axis, out + 16 * b, &chosen, &err,
-                       &err_fixed);
+                search(tex, dim, o->has_alpha != 0, o->srgb != 0, o->quality == 2 ? 2 : o->axis,
+                       out + 16 * b, &chosen, &err, &err_fixed);
                 continue;
             }
             uint32_t ep[8], qw[16];
@@ -1368,7 +1384,7 @@ int oracle_endpoint_quant(int wq, int nvals) {
 int oracle_search_block_fp32(const float* texels, int block_dim, int has_alpha, int srgb, int axis,
                              uint8_t out[16], int* chosen_wq, uint32_t* err, uint32_t* err_fixed) {
     if (!texels || !out || !chosen_wq || !err || !err_fixed) return -1;
-    if ((block_dim != 4 && block_dim != 6) || (axis != 0 && axis != 1)) return -1;
+    if ((block_dim != 4 && block_dim != 6) || axis < 0 || axis > 2) return -1;
     float tex[36][4];
     for (int i = 0; i < block_dim * block_dim; ++i)
         for (int c = 0; c < 4; ++c) tex[i][c] = texels[4 * i + c];

@@ -43,7 +43,10 @@ typedef struct oracle_opts {
                         candidate whose decode has the least squared error
                         against the texels rounded to bytes in the fit
                         space (the choose_best_quantmethod the shader
-                        sketches at 524-526)                                */
+                        sketches at 524-526); 2 = the same search from the
+                        better of the two fits (both axes tried, the one
+                        whose fixed-mode block has the smaller error kept,
+                        the PCA on ties; axis is then ignored)             */
 } oracle_opts;
 
 /* Encode a tightly packed RGBA8 image (row 0 first) into 16-byte blocks in
@@ -106,7 +109,7 @@ double oracle_flops_per_block(int block_dim, int has_alpha, int is_normal);
  * invalid. */
 int oracle_endpoint_quant(int wq, int nvals);
 /* Encode one block (texels: N*4 floats, 0..255, the fit space) in search
- * mode with FP32 arithmetic.  *chosen_wq = weight quant method of the block
+ * mode with FP32 arithmetic (axis 2: from the better of both fits).  *chosen_wq = weight quant method of the block
  * kept (-1 when the fixed-mode block was kept), *err = the squared error of
  * its decode against the texels rounded to bytes, *err_fixed = the
  * fixed-mode block's. */

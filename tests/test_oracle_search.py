@@ -79,7 +79,7 @@ def _random_block(rng, dim, kind):
 @pytest.mark.parametrize("dim", [4, 6])
 @pytest.mark.parametrize("alpha", [False, True])
 @pytest.mark.parametrize("srgb", [False, True])
-@pytest.mark.parametrize("axis", [0, 1])
+@pytest.mark.parametrize("axis", [0, 1, 2])
 def test_search_scores_match_the_spec_decode(oracle, dim, alpha, srgb, axis):
     rng = np.random.default_rng(1000 * dim + 100 * alpha + 10 * srgb + axis)
     chosen = set()
@@ -125,6 +125,30 @@ def test_search_image_never_worse_and_decodes(oracle, dim, alpha):
 
 
 @pytest.mark.parametrize("dim", [4, 6])
+@pytest.mark.parametrize("alpha", [False, True])
+def test_thorough_picks_the_better_fit(oracle, dim, alpha):
+    """quality 2 searches from whichever fit has the smaller fixed-mode
+    error: on every block its error is at most the min of the two
+    single-fit fixed modes, and it equals a quality-1 encode with the axis
+    that fit came from."""
+    rng = np.random.default_rng(77 + dim + alpha)
+    wins = {0: 0, 1: 0}
+    for trial in range(80):
+        px = _random_block(rng, dim, trial % 4)
+        if trial % 5 == 1:                           # flat colour, alpha cut-out
+            px[..., :3] = 120
+            px[..., 3] = np.where(rng.random((dim, dim)) < 0.5, 0, 255)
+        tex = _fit_texels(oracle, px, False)
+        blk, _, err, err_fixed = oracle.search_block(tex, dim, alpha, False, 2)
+        runs = [oracle.search_block(tex, dim, alpha, False, a) for a in (0, 1)]
+        assert err_fixed == min(runs[0][3], runs[1][3])
+        pick = 1 if runs[1][3] < runs[0][3] else 0
+        wins[pick] += 1
+        assert np.array_equal(blk, runs[pick][0]) and err == runs[pick][2]
+    assert wins[0] and wins[1]
+
+
+@pytest.mark.parametrize("dim", [4, 6])
 def test_search_fp64_twin_runs(oracle, dim):
     rgba = synth.rgb_noise(40, 40, seed=9)
     a = oracle.encode(rgba, block_dim=dim, quality=1)
@@ -160,3 +184,20 @@ def test_bad_axis_and_quality_rejected(oracle):
         oracle.encode(np.zeros((4, 4, 4), np.uint8), axis=2)
     with pytest.raises(ValueError):
         oracle.encode(np.zeros((4, 4, 4), np.uint8), quality=3)
+
+
+def test_thorough_recovers_alpha_cutouts(oracle):
+    """Flat colour with an alpha cut-out: the reference's PCA start vector has
+    no alpha component, so the power iteration exits at once and the block
+    collapses to its mean; the max-accumulation fit keeps the cut-out."""
+    px = np.zeros((8, 8, 4), np.uint8)
+    px[..., :3] = (100, 150, 200)
+    px[..., 3] = np.where((np.arange(8)[:, None] + np.arange(8)[None, :]) % 3 == 0, 0, 255)
+    fast = oracle.encode(px, block_dim=4, has_alpha=True)
+    best = oracle.encode(px, block_dim=4, has_alpha=True, quality=2)
+    dfast, _ = oracle.decode(fast, 8, 8, 4)
+    dbest, _ = oracle.decode(best, 8, 8, 4)
+    for by in (0, 4):                                  # alpha flattened per block
+        for bx in (0, 4):
+            assert len(np.unique(dfast[by:by + 4, bx:bx + 4, 3])) == 1
+    assert np.array_equal(dbest[..., 3], px[..., 3])   # alpha kept exactly
