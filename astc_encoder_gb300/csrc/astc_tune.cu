@@ -7,7 +7,10 @@
 // count near 255 and the SM near 8 warps).  The CTA size trades scheduling
 // slack against shared memory.  astc_autotune times every (store, CTA size)
 // candidate for a format on a synthetic texture of the caller's size on the
-// current device and installs the fastest for that format in this process.
+// current device and installs the fastest for that format in this process --
+// unless it beats the format's current choice by less than 3%, which then
+// stays (timing noise, e.g. under a profiler that serialises launches, does
+// not move the choice).
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -138,6 +141,11 @@ astc_status astc_autotune(int block_dim, int has_alpha, int is_normal, int srgb,
                 if (us < best) { best = us; best_store = stores[si]; best_threads = sizes[ti]; }
             }
         if (st != ASTC_OK) break;
+        if (def_us > 0.0f && best > 0.97f * def_us) {
+            best_store = def_store;
+            best_threads = def_threads;
+            best = def_us;
+        }
         set_encode_choice(block_dim, has_alpha != 0, is_normal != 0, srgb != 0, best_store, best_threads);
         if (result) {
             result->store = best_store;

@@ -524,8 +524,11 @@ def run_ours(args) -> None:
     dim = spec["block_dim"]
     nblocks = ((w + dim - 1) // dim) * ((h + dim - 1) // dim)
     prec = 1 if args.precision == "half2" else 0
-    # the autotuner picks the kernel variant (texel store, CTA size) for this format
-    tuned = native.autotune(dim, spec["has_alpha"], spec["is_normal"], spec["srgb"], w, h)
+    # the autotuner picks the kernel variant (texel store, CTA size) for this
+    # format; the profiling case keeps the built-in default (under a profiler
+    # every launch is serialised and the autotuner's timings are meaningless)
+    tuned = None if args.profile_case else native.autotune(dim, spec["has_alpha"], spec["is_normal"],
+                                                           spec["srgb"], w, h)
     texs = _texture_batch(torch, img, 2 if args.profile_case else TEXTURES_PER_STEP, salt=rank)
     outs = [torch.empty((nblocks, 16), dtype=torch.uint8, device="cuda") for _ in texs]
     spec_run = dict(spec, precision=prec)
@@ -536,8 +539,10 @@ def run_ours(args) -> None:
         spec_prof = dict(spec_run, quality=quality) if quality else spec_run
         _time_launches(torch, native, texs, outs, spec_prof, max(3, args.warmup))
         per, _, launches = _time_launches(torch, native, texs, outs, spec_prof, args.steps)
+        store, threads = native.get_kernel_choice(dim, spec["has_alpha"], spec["is_normal"], spec["srgb"])
         print(json.dumps({"profile_case": args.workload, "quality": args.profile_quality,
-                          "launches": launches, "mean_launch_us": per * 1e3}), flush=True)
+                          "launches": launches, "mean_launch_us": per * 1e3,
+                          "kernel_variant": {"store": store, "threads_per_cta": threads}}), flush=True)
         return
 
     # warm-up (untimed) + a short sustained burn so clocks settle
