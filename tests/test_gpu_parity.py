@@ -241,6 +241,46 @@ def test_host_memory_zero_copy_paths(native, oracle):
         assert st == 0 and np.array_equal(pin_out.numpy(), want)
 
 
+def test_host_memory_upload_ring(native, oracle):
+    """Pinned inputs of 4 MiB and more are uploaded through a ring of device
+    slots (copy engine, events; bands of whole block rows above a slot) while
+    earlier kernels run: blocks equal the oracle's across band seams, with a
+    ragged last band, for pinned and pageable outputs, through synchronous
+    calls and through back-to-back asynchronous calls on one stream."""
+    import torch
+    lib = native.load_library()
+    # 32 MiB slots: 4096 wide 6x6 is 683 block rows of 96 KiB -> two bands
+    # (342 + 341 block rows, the last ragged); 2048 wide inputs of 16 MiB are
+    # one band each
+    cases = [((4093, 4096), dict(block_dim=6, has_alpha=True, srgb=True, border=1)),
+             ((2049, 2048), dict(block_dim=4, has_alpha=False, border=0)),
+             ((2049, 2048), dict(block_dim=4, has_alpha=True, border=1, quality=1))]
+    for (h, w), opts in cases:
+        img = _texture(h, w, seed=h + w + opts["block_dim"])
+        want = oracle.encode(img, **opts)
+        pin_in = torch.from_numpy(img).pin_memory()
+        pin_out = torch.zeros(want.shape, dtype=torch.uint8).pin_memory()
+        page_out = np.zeros_like(want)
+        o = native.make_opts(memory=native.Memory.HOST, **opts)
+        assert lib.astc_encode_gpu(pin_in.data_ptr(), w, h, ctypes.byref(o), pin_out.data_ptr()) == 0
+        assert np.array_equal(pin_out.numpy(), want), opts
+        assert lib.astc_encode_gpu(pin_in.data_ptr(), w, h, ctypes.byref(o), page_out.ctypes.data) == 0
+        assert np.array_equal(page_out, want), opts
+    # asynchronous: six calls in flight on one stream, slots reused across calls
+    img = _texture(2043, 2048, seed=7)
+    opts = dict(block_dim=6, has_alpha=True, srgb=True, border=1)
+    want = oracle.encode(img, **opts)
+    stream = torch.cuda.Stream()
+    ins = [torch.from_numpy(np.roll(img, 13 * i, axis=1)).pin_memory() for i in range(6)]
+    outs = [torch.zeros(want.shape, dtype=torch.uint8).pin_memory() for _ in ins]
+    o = native.make_opts(memory=native.Memory.HOST, stream=stream.cuda_stream, **opts)
+    for a, b in zip(ins, outs):
+        assert lib.astc_encode_gpu(a.data_ptr(), 2048, 2043, ctypes.byref(o), b.data_ptr()) == 0
+    stream.synchronize()
+    for i, b in enumerate(outs):
+        assert np.array_equal(b.numpy(), oracle.encode(np.roll(img, 13 * i, axis=1), **opts)), i
+
+
 def test_server_with_pinned_requests(native):
     import torch
     imgs = [_texture(97 + 13 * i, 61 + 7 * i, seed=i) for i in range(12)]
