@@ -266,6 +266,17 @@ def test_host_memory_upload_ring(native, oracle):
         assert np.array_equal(pin_out.numpy(), want), opts
         assert lib.astc_encode_gpu(pin_in.data_ptr(), w, h, ctypes.byref(o), page_out.ctypes.data) == 0
         assert np.array_equal(page_out, want), opts
+    # a row-pitched view into a wider pinned image (the 2-D band copies)
+    img = _texture(2049, 2048, seed=99)
+    opts = dict(block_dim=4, has_alpha=True, border=1)
+    want = oracle.encode(img, **opts)
+    wide = torch.zeros((2049, 2112, 4), dtype=torch.uint8).pin_memory()
+    wide[:, :2048] = torch.from_numpy(img)
+    pin_out = torch.zeros(want.shape, dtype=torch.uint8).pin_memory()
+    o = native.make_opts(memory=native.Memory.HOST, **opts)
+    assert lib.astc_encode_gpu_pitched(wide.data_ptr(), 2048, 2049, 2112 * 4, ctypes.byref(o),
+                                       pin_out.data_ptr()) == 0
+    assert np.array_equal(pin_out.numpy(), want)
     # asynchronous: six calls in flight on one stream, slots reused across calls
     img = _texture(2043, 2048, seed=7)
     opts = dict(block_dim=6, has_alpha=True, srgb=True, border=1)
