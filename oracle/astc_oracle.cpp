@@ -453,15 +453,16 @@ void assemble_symbolic(const uint32_t ep_q[8], const uint32_t qw[16], bool alpha
 // ---------------------------------------------------------------------------
 // Integer helpers of the search mode (ASTC specification rules)
 // ---------------------------------------------------------------------------
-// Endpoint quant method of a single-partition block with a 4x4 weight grid
-// of quant method wq and nvals endpoint values: the decoder takes the
-// largest range whose ISE fits in the bits between bit 17 and the weights
-// (and the block is illegal below QUANT_6 or outside 24..96 weight bits).
-int endpoint_quant(int wq, int nvals) {
+// Endpoint quant method of a block with a 4x4 weight grid of quant method wq
+// and nvals endpoint values: the decoder takes the largest range whose ISE
+// fits in the bits between the header (17 bits for one partition, 29 for
+// several with one shared CEM) and the weights (and the block is illegal
+// below QUANT_6 or outside 24..96 weight bits).
+int endpoint_quant(int wq, int nvals, int header_bits = 17) {
     if (wq < QUANT_2 || wq > QUANT_32) return -1;
     const int wbits = ise_bits(wq, 16);
     if (wbits < 24 || wbits > 96) return -1;
-    const int avail = 128 - 17 - wbits;
+    const int avail = 128 - header_bits - wbits;
     for (int q = QUANT_256; q >= QUANT_6; --q)
         if (ise_bits(q, nvals) <= avail) return q;
     return -1;
@@ -502,24 +503,49 @@ int infill_6x6(const int wv[16], int s, int t) {
     return (acc + 8) >> 4;
 }
 
-// A single-partition block with a 4x4 weight grid of any range: mode and CEM
-// in bits 0..16, the endpoint ISE from bit 17 up, the weight ISE bit-reversed
-// from bit 127 down (every field ORed, each cut to its ISE length).
-void assemble_general(uint32_t wq, uint32_t cq, uint32_t cem, const uint32_t* ev, int nvals,
-                      const uint32_t* sw, uint8_t out[16]) {
+// A block with a 4x4 weight grid of any range: the header (mode, partition
+// fields, CEM) in bits 0..hbits-1, the endpoint ISE from bit hbits up, the
+// weight ISE bit-reversed from bit 127 down (every field ORed, each cut to
+// its ISE length).
+void assemble_fields(uint32_t head, int hbits, uint32_t wq, uint32_t cq, const uint32_t* ev, int nvals,
+                     const uint32_t* sw, uint8_t out[16]) {
     Bits128 ep = {{0, 0, 0, 0}}, wt = {{0, 0, 0, 0}};
     ise_encode((int)cq, nvals, ev, ep);
     ise_encode((int)wq, 16, sw, wt);
     const int ebits = ise_bits((int)cq, nvals), wbits = ise_bits((int)wq, 16);
     std::memset(out, 0, 16);
     auto set = [&](int pos) { out[pos >> 3] = (uint8_t)(out[pos >> 3] | (1u << (pos & 7))); };
-    const uint32_t head = assemble_blockmode(wq) | ((cem & 0xF) << 13);
-    for (int i = 0; i < 17; ++i)
+    for (int i = 0; i < hbits; ++i)
         if ((head >> i) & 1) set(i);
     for (int i = 0; i < ebits; ++i)
-        if ((ep.w[i >> 5] >> (i & 31)) & 1) set(17 + i);
+        if ((ep.w[i >> 5] >> (i & 31)) & 1) set(hbits + i);
     for (int i = 0; i < wbits; ++i)
         if ((wt.w[i >> 5] >> (i & 31)) & 1) set(127 - i);
+}
+
+// Single partition: mode [10:0], CEM [16:13], endpoints from bit 17.
+void assemble_general(uint32_t wq, uint32_t cq, uint32_t cem, const uint32_t* ev, int nvals,
+                      const uint32_t* sw, uint8_t out[16]) {
+    assemble_fields(assemble_blockmode(wq) | ((cem & 0xF) << 13), 17, wq, cq, ev, nvals, sw, out);
+}
+
+// Two partitions sharing one CEM: mode [10:0], partition count - 1 = 1 at
+// [12:11], partition index [22:13], CEM field [28:23] = CEM << 2 (the low two
+// bits 00 mean "every partition uses this CEM"), endpoints from bit 29.
+void assemble_two_partitions(uint32_t wq, uint32_t cq, uint32_t cem, uint32_t seed, const uint32_t* ev,
+                             int nvals, const uint32_t* sw, uint8_t out[16]) {
+    const uint32_t head = assemble_blockmode(wq) | (1u << 11) | ((seed & 0x3FF) << 13) | ((cem & 0xF) << 25);
+    assemble_fields(head, 29, wq, cq, ev, nvals, sw, out);
+}
+
+// Two-partition patterns (the spec's partition hash, defined with the
+// decoder below): bit i = texel i (row-major) lies in partition 1.
+const uint64_t* partition_masks(int dim);
+
+inline int popcount64(uint64_t v) {
+    int c = 0;
+    while (v) { v &= v - 1; ++c; }
+    return c;
 }
 
 // ---------------------------------------------------------------------------
@@ -619,11 +645,12 @@ struct Pipe {
         }
     }
 
-    // find_min_max (ASTC_Encode.hlsl:108-137)
+    // find_min_max (ASTC_Encode.hlsl:108-137), over the texels in `sel`
     static void find_min_max(const T (*tex)[4], int n, const T mean[4], const T k[4],
-                             bool alpha, T e0[4], T e1[4]) {
+                             bool alpha, T e0[4], T e1[4], uint64_t sel = ~0ull) {
         T a = P::lit(1e31f, 1e31), b = P::lit(-1e31f, -1e31);
         for (int i = 0; i < n; ++i) {
+            if (!((sel >> i) & 1)) continue;
             T d[4];
             for (int c = 0; c < 4; ++c) d[c] = P::sub(tex[i][c], mean[c]);
             const T t = dot4(d, k);
@@ -859,13 +886,13 @@ struct Pipe {
     // axis 2 fits both ways and searches from the fit whose fixed-mode block
     // has the smaller error (the PCA on ties).
     static void search(const T (*tex)[4], int dim, bool alpha, bool srgb, int axis, uint8_t out[16],
-                       int* chosen, uint32_t* best_err, uint32_t* fixed_err) {
+                       int* chosen, uint32_t* best_err, uint32_t* fixed_err, bool partitions = false) {
         const int nch = alpha ? 4 : 3;
         int tb[36][4];
         for (int i = 0; i < dim * dim; ++i)
             for (int c = 0; c < 4; ++c) tb[i][c] = (int)P::rint(tex[i][c]);
-        T e0[4], e1[4];
-        uint32_t ep_q[8], qw[16], best = 0;
+        T e0[4] = {0, 0, 0, 0}, e1[4] = {0, 0, 0, 0};
+        uint32_t ep_q[8] = {}, qw[16] = {}, best = 0;
         const int a_first = axis == 2 ? 0 : axis, a_last = axis == 2 ? 1 : axis;
         for (int a = a_first; a <= a_last; ++a) {
             T f0[4], f1[4];
@@ -900,7 +927,167 @@ struct Pipe {
             if (err < best) { best = err; *chosen = wq; keep = tr; }
         }
         if (*chosen >= 0) assemble_trial(keep, alpha, out);
+        if (partitions) {
+            // two partitions, split along the kept fit's fixed-mode endpoints
+            int PE0[4], PE1[4];
+            for (int c = 0; c < 4; ++c) { PE0[c] = (int)ep_q[2 * c]; PE1[c] = (int)ep_q[2 * c + 1]; }
+            uint8_t pblk[16];
+            int pch = -1;
+            const uint32_t perr = two_partitions(tex, tb, dim, alpha, srgb, PE0, PE1, pblk, &pch);
+            if (perr < best) {
+                best = perr;
+                *chosen = pch;
+                std::memcpy(out, pblk, 16);
+            }
+        }
         *best_err = best;
+    }
+
+    // ---- two partitions (quality 3) ----------------------------------------
+    // The fit of one partition: mean (correctly rounded division by its texel
+    // count), covariance / max(count - 1, 1), the shader's power iteration,
+    // and find_min_max over the partition's texels.
+    static void fit_partition(const T (*tex)[4], int n, uint64_t sel, bool alpha, T e0[4], T e1[4]) {
+        const int cnt = popcount64(sel);
+        T mean[4] = {0, 0, 0, 0};
+        for (int i = 0; i < n; ++i)
+            if ((sel >> i) & 1)
+                for (int c = 0; c < 4; ++c) mean[c] = P::add(mean[c], tex[i][c]);
+        for (int c = 0; c < 4; ++c) mean[c] = P::div(mean[c], (T)cnt);
+        T cov[4][4];
+        for (int i = 0; i < 4; ++i)
+            for (int j = 0; j < 4; ++j) cov[i][j] = 0;
+        for (int t = 0; t < n; ++t) {
+            if (!((sel >> t) & 1)) continue;
+            T d[4];
+            for (int c = 0; c < 4; ++c) d[c] = P::sub(tex[t][c], mean[c]);
+            for (int i = 0; i < 4; ++i)
+                for (int j = 0; j < 4; ++j) cov[i][j] = P::mad(d[i], d[j], cov[i][j]);
+        }
+        const T den = (T)(cnt > 1 ? cnt - 1 : 1);
+        for (int i = 0; i < 4; ++i)
+            for (int j = 0; j < 4; ++j) cov[i][j] = P::div(cov[i][j], den);
+        T k[4];
+        eigen_vector(cov, k);
+        find_min_max(tex, n, mean, k, alpha, e0, e1, sel);
+    }
+
+    // Two-partition candidates from fixed-mode endpoints E0/E1 (rounded): the
+    // texels beyond the endpoints' midpoint form the ideal split; the
+    // partition index whose pattern (or its complement) differs from it in the
+    // fewest texels is taken (the smallest index on ties, one-partition
+    // patterns skipped); each partition is fitted on its own; every weight
+    // range whose endpoint range (12 or 16 values after the 29-bit header) is
+    // legal is scored.  Returns the best error (UINT32_MAX if none) and its
+    // block in out.
+    static uint32_t two_partitions(const T (*tex)[4], const int (*tb)[4], int dim, bool alpha, bool srgb,
+                                   const int E0[4], const int E1[4], uint8_t out[16], int* chosen) {
+        const Tables& tbl = tables();
+        const int n = dim * dim, nch = alpha ? 4 : 3, nv = alpha ? 8 : 6;
+        const uint64_t full = n == 64 ? ~0ull : ((1ull << n) - 1);
+        T d[4];
+        for (int c = 0; c < 4; ++c) d[c] = (T)(E1[c] - E0[c]);
+        const T dd = dot4(d, d);
+        if (dd == 0) return UINT32_MAX;
+        uint64_t ideal = 0;
+        for (int i = 0; i < n; ++i) {
+            T diff[4];
+            for (int c = 0; c < 4; ++c) diff[c] = P::sub(tex[i][c], (T)E0[c]);
+            const T x = dot4(diff, d);
+            if (P::add(x, x) > dd) ideal |= 1ull << i;
+        }
+        if (ideal == 0 || ideal == full) return UINT32_MAX;
+        const uint64_t* pm = partition_masks(dim);
+        int seed = -1, best_m = n + 1;
+        for (int s = 0; s < 1024; ++s) {
+            if (pm[s] == 0 || pm[s] == full) continue;
+            int m = popcount64(pm[s] ^ ideal);
+            if (n - m < m) m = n - m;
+            if (m < best_m) { best_m = m; seed = s; }
+        }
+        const uint64_t sel1 = pm[seed], sel0 = full & ~sel1;
+        T pe0[2][4], pe1[2][4];
+        fit_partition(tex, n, sel0, alpha, pe0[0], pe1[0]);
+        fit_partition(tex, n, sel1, alpha, pe0[1], pe1[1]);
+        uint32_t best = UINT32_MAX;
+        for (int wq = QUANT_3; wq <= QUANT_32; ++wq) {
+            const int cq = endpoint_quant(wq, 2 * nv, 29);
+            if (cq < 0) continue;
+            // snapped endpoints per partition, darker first
+            int sym0[2][4], sym1[2][4], Q0[2][4], Q1[2][4];
+            for (int p = 0; p < 2; ++p) {
+                for (int c = 0; c < 4; ++c) { sym0[p][c] = sym1[p][c] = 0; Q0[p][c] = Q1[p][c] = 255; }
+                for (int c = 0; c < nch; ++c) {
+                    sym0[p][c] = nearest_color(cq, (int)P::rint(pe0[p][c]), &Q0[p][c]);
+                    sym1[p][c] = nearest_color(cq, (int)P::rint(pe1[p][c]), &Q1[p][c]);
+                }
+                if (Q1[p][0] + Q1[p][1] + Q1[p][2] < Q0[p][0] + Q0[p][1] + Q0[p][2])
+                    for (int c = 0; c < 4; ++c) {
+                        std::swap(sym0[p][c], sym1[p][c]);
+                        std::swap(Q0[p][c], Q1[p][c]);
+                    }
+            }
+            // per-texel weights on the texel's own partition, clamped to [0, 1]
+            T pd[2][4], r[2];
+            bool flat[2];
+            for (int p = 0; p < 2; ++p) {
+                for (int c = 0; c < 4; ++c) pd[p][c] = (T)(Q1[p][c] - Q0[p][c]);
+                const T pdd = dot4(pd[p], pd[p]);
+                flat[p] = pdd == 0;
+                r[p] = flat[p] ? (T)0 : P::div(P::lit(1.0f, 1.0), pdd);
+            }
+            T wt[36];
+            for (int i = 0; i < n; ++i) {
+                const int p = (int)((sel1 >> i) & 1);
+                if (flat[p]) { wt[i] = 0; continue; }
+                T diff[4];
+                for (int c = 0; c < 4; ++c) diff[c] = P::sub(tex[i][c], (T)Q0[p][c]);
+                const T w = P::mul(dot4(diff, pd[p]), r[p]);
+                wt[i] = P::min(P::max(w, (T)0), P::lit(1.0f, 1.0));
+            }
+            // grid weights: the texel weights (4x4) or their 2x2 bilinear
+            // sample with the shader's taps (6x6), rounded to the range
+            const uint32_t R = (uint32_t)kQuantLevels[wq] - 1;
+            uint32_t q[16];
+            for (int g = 0; g < 16; ++g) {
+                T w = wt[g];
+                if (dim == 6) {
+                    int idx[4]; T cw[4];
+                    grid_taps(g, idx, cw);
+                    w = P::mul(wt[idx[0]], cw[0]);
+                    w = P::mad(wt[idx[1]], cw[1], w);
+                    w = P::mad(wt[idx[2]], cw[2], w);
+                    w = P::mad(wt[idx[3]], cw[3], w);
+                }
+                const uint32_t v = (uint32_t)P::rint(P::mul(w, (T)R));
+                q[g] = v > R ? R : v;
+            }
+            int wv[16];
+            trial_weights(wq, q, wv);
+            uint32_t err = 0;
+            for (int i = 0; i < n; ++i) {
+                const int p = (int)((sel1 >> i) & 1);
+                const int w = dim == 4 ? wv[i] : infill_6x6(wv, i % 6, i / 6);
+                for (int c = 0; c < nch; ++c) {
+                    const int e = decode_channel(Q0[p][c], Q1[p][c], w, srgb) - tb[i][c];
+                    err += (uint32_t)(e * e);
+                }
+            }
+            if (err < best) {
+                best = err;
+                *chosen = 100 + wq;
+                uint32_t ev[16], sw[16];
+                for (int p = 0; p < 2; ++p)
+                    for (int c = 0; c < nv / 2; ++c) {
+                        ev[p * nv + 2 * c] = (uint32_t)sym0[p][c];
+                        ev[p * nv + 2 * c + 1] = (uint32_t)sym1[p][c];
+                    }
+                for (int g = 0; g < 16; ++g) sw[g] = (uint32_t)tbl.scramble[wq][q[g]];
+                assemble_two_partitions((uint32_t)wq, (uint32_t)cq, alpha ? 12u : 8u, (uint32_t)seed, ev, 2 * nv,
+                                        sw, out);
+            }
+        }
+        return best;
     }
 
     static void assemble_trial(const Trial& tr, bool alpha, uint8_t out[16]) {
@@ -943,7 +1130,7 @@ struct Pipe {
         if (o->block_dim != 4 && o->block_dim != 6) return -2;
         if (o->border != 0 && o->border != 1) return -3;
         if (o->axis != 0 && o->axis != 1) return -4;
-        if (o->quality < 0 || o->quality > 2) return -5;
+        if (o->quality < 0 || o->quality > 3) return -5;
         tables();
         const int dim = o->block_dim;
         const int nbx = (w + dim - 1) / dim, nby = (h + dim - 1) / dim;
@@ -961,8 +1148,8 @@ struct Pipe {
             if (o->quality) {
                 int chosen;
                 uint32_t err, err_fixed;
-                search(tex, dim, o->has_alpha != 0, o->srgb != 0, o->quality == 2 ? 2 : o->axis,
-                       out + 16 * b, &chosen, &err, &err_fixed);
+                search(tex, dim, o->has_alpha != 0, o->srgb != 0, o->quality >= 2 ? 2 : o->axis,
+                       out + 16 * b, &chosen, &err, &err_fixed, o->quality == 3);
                 continue;
             }
             uint32_t ep[8], qw[16];
@@ -1146,6 +1333,26 @@ int select_partition(int seed, int x, int y, int z, int pcount, bool small) {
     if (b >= c && b >= d) return 1;
     if (c >= d) return 2;
     return 3;
+}
+
+const uint64_t* partition_masks(int dim) {
+    struct Masks {
+        uint64_t m[2][1024];
+        Masks() {
+            for (int d = 0; d < 2; ++d) {
+                const int dim = d ? 6 : 4;
+                for (int s = 0; s < 1024; ++s) {
+                    uint64_t v = 0;
+                    for (int y = 0; y < dim; ++y)
+                        for (int x = 0; x < dim; ++x)
+                            if (select_partition(s, x, y, 0, 2, dim * dim < 31) == 1) v |= 1ull << (y * dim + x);
+                    m[d][s] = v;
+                }
+            }
+        }
+    };
+    static const Masks masks;
+    return masks.m[dim == 6 ? 1 : 0];
 }
 
 void error_block(int bw, int bh, uint8_t* out) {
@@ -1382,13 +1589,15 @@ int oracle_endpoint_quant(int wq, int nvals) {
 }
 
 int oracle_search_block_fp32(const float* texels, int block_dim, int has_alpha, int srgb, int axis,
-                             uint8_t out[16], int* chosen_wq, uint32_t* err, uint32_t* err_fixed) {
+                             int partitions, uint8_t out[16], int* chosen_wq, uint32_t* err,
+                             uint32_t* err_fixed) {
     if (!texels || !out || !chosen_wq || !err || !err_fixed) return -1;
     if ((block_dim != 4 && block_dim != 6) || axis < 0 || axis > 2) return -1;
     float tex[36][4];
     for (int i = 0; i < block_dim * block_dim; ++i)
         for (int c = 0; c < 4; ++c) tex[i][c] = texels[4 * i + c];
-    Pipe<F32>::search(tex, block_dim, has_alpha != 0, srgb != 0, axis, out, chosen_wq, err, err_fixed);
+    Pipe<F32>::search(tex, block_dim, has_alpha != 0, srgb != 0, axis, out, chosen_wq, err, err_fixed,
+                      partitions != 0);
     return 0;
 }
 

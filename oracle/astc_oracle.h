@@ -46,7 +46,11 @@ typedef struct oracle_opts {
                         sketches at 524-526); 2 = the same search from the
                         better of the two fits (both axes tried, the one
                         whose fixed-mode block has the smaller error kept,
-                        the PCA on ties; axis is then ignored)             */
+                        the PCA on ties; axis is then ignored); 3 = 2 plus
+                        two-partition candidates (one partition pattern,
+                        matched to the split of the kept fit, each
+                        partition fitted on its own, every legal weight
+                        range scored)                                      */
 } oracle_opts;
 
 /* Encode a tightly packed RGBA8 image (row 0 first) into 16-byte blocks in
@@ -109,12 +113,14 @@ double oracle_flops_per_block(int block_dim, int has_alpha, int is_normal);
  * invalid. */
 int oracle_endpoint_quant(int wq, int nvals);
 /* Encode one block (texels: N*4 floats, 0..255, the fit space) in search
- * mode with FP32 arithmetic (axis 2: from the better of both fits).  *chosen_wq = weight quant method of the block
- * kept (-1 when the fixed-mode block was kept), *err = the squared error of
- * its decode against the texels rounded to bytes, *err_fixed = the
- * fixed-mode block's. */
+ * mode with FP32 arithmetic (axis 2: from the better of both fits; with
+ * partitions, two-partition candidates as well).  *chosen_wq = weight quant
+ * method of the block kept (-1 when the fixed-mode block was kept, 100 + wq
+ * for a two-partition block), *err = the squared error of its decode against
+ * the texels rounded to bytes, *err_fixed = the fixed-mode block's. */
 int oracle_search_block_fp32(const float* texels, int block_dim, int has_alpha, int srgb, int axis,
-                             uint8_t out[16], int* chosen_wq, uint32_t* err, uint32_t* err_fixed);
+                             int partitions, uint8_t out[16], int* chosen_wq, uint32_t* err,
+                             uint32_t* err_fixed);
 
 #ifdef __cplusplus
 }

@@ -64,7 +64,7 @@ def lib() -> ctypes.CDLL:
             L.oracle_flops_per_block.argtypes = [ip, ip, ip]
             L.oracle_flops_per_block.restype = ctypes.c_double
             L.oracle_endpoint_quant.argtypes = [ip, ip]
-            L.oracle_search_block_fp32.argtypes = [vp, ip, ip, ip, ip, vp, vp, vp, vp]
+            L.oracle_search_block_fp32.argtypes = [vp, ip, ip, ip, ip, ip, vp, vp, vp, vp]
             _lib = L
     return _lib
 
@@ -189,19 +189,20 @@ def endpoint_quant(wq: int, nvals: int) -> int:
     return int(lib().oracle_endpoint_quant(wq, nvals))
 
 
-def search_block(texels: np.ndarray, block_dim: int, has_alpha: bool, srgb: bool = False, axis: int = 0):
+def search_block(texels: np.ndarray, block_dim: int, has_alpha: bool, srgb: bool = False, axis: int = 0,
+                 partitions: bool = False):
     """Search-mode FP32 encode of one block of fit-space texels (N x 4 floats).
 
-    Returns (block bytes, chosen weight quant method or -1 for the fixed-mode
-    block, the squared error of its decode against the texels rounded to
-    bytes, the fixed-mode block's)."""
+    Returns (block bytes, chosen weight quant method -- -1 for the fixed-mode
+    block, 100 + wq for a two-partition block --, the squared error of its
+    decode against the texels rounded to bytes, the fixed-mode block's)."""
     t = np.ascontiguousarray(texels, dtype=np.float32).reshape(-1)
     out = np.zeros(16, np.uint8)
     wq = ctypes.c_int(0)
     err = ctypes.c_uint32(0)
     err_fixed = ctypes.c_uint32(0)
     rc = lib().oracle_search_block_fp32(t.ctypes.data, block_dim, int(has_alpha), int(srgb), int(axis),
-                                        out.ctypes.data, ctypes.byref(wq), ctypes.byref(err),
+                                        int(partitions), out.ctypes.data, ctypes.byref(wq), ctypes.byref(err),
                                         ctypes.byref(err_fixed))
     assert rc == 0
     return out, wq.value, err.value, err_fixed.value

@@ -148,6 +148,56 @@ def test_thorough_picks_the_better_fit(oracle, dim, alpha):
     assert wins[0] and wins[1]
 
 
+def _four_colour_block(rng, dim):
+    """Two regions of two colours each: one partition cannot hold the four
+    colours, two can."""
+    cols = rng.integers(0, 256, (4, 4)).astype(np.uint8)
+    yy, xx = np.mgrid[0:dim, 0:dim]
+    region = (xx + rng.integers(-1, 2)) >= dim // 2
+    pick = rng.random((dim, dim)) < 0.5
+    px = np.empty((dim, dim, 4), np.uint8)
+    px[region & pick], px[region & ~pick] = cols[0], cols[1]
+    px[~region & pick], px[~region & ~pick] = cols[2], cols[3]
+    return px
+
+
+@pytest.mark.parametrize("dim", [4, 6])
+@pytest.mark.parametrize("alpha", [False, True])
+@pytest.mark.parametrize("srgb", [False, True])
+def test_two_partitions_score_match_the_spec_decode(oracle, dim, alpha, srgb):
+    rng = np.random.default_rng(500 + 10 * dim + 2 * alpha + srgb)
+    partitioned = 0
+    for trial in range(60):
+        px = _four_colour_block(rng, dim) if trial % 2 else _random_block(rng, dim, trial % 4)
+        tex = _fit_texels(oracle, px, srgb)
+        blk, wq, err, _ = oracle.search_block(tex, dim, alpha, srgb, 2, partitions=True)
+        _, _, err_thorough, _ = oracle.search_block(tex, dim, alpha, srgb, 2)
+        assert err <= err_thorough
+        assert _decoded_error(oracle, blk, tex, dim, alpha, srgb) == err
+        if wq >= 100:
+            partitioned += 1
+            word = int.from_bytes(blk[:4].tobytes(), "little")
+            assert (word >> 11) & 3 == 1                       # two partitions
+            assert (word >> 23) & 3 == 0 and (word >> 25) & 0xF == (12 if alpha else 8)
+    assert partitioned >= 10
+
+
+@pytest.mark.parametrize("dim", [4, 6])
+@pytest.mark.parametrize("alpha", [False, True])
+def test_two_partitions_image(oracle, dim, alpha):
+    rgba = synth.rgb_noise(96, 80, seed=15) if not alpha else synth.rgba_cutout(96, 80, seed=16)
+    thorough = oracle.encode(rgba, block_dim=dim, has_alpha=alpha, border=1, quality=2)
+    best = oracle.encode(rgba, block_dim=dim, has_alpha=alpha, border=1, quality=3)
+    h, w = rgba.shape[:2]
+    ch = 4 if alpha else 3
+    d2, e2 = oracle.decode(thorough, w, h, dim)
+    d3, e3 = oracle.decode(best, w, h, dim)
+    assert e2 == 0 and e3 == 0
+    sse = lambda d: int(((d[..., :ch].astype(np.int64) - rgba[..., :ch]) ** 2).sum())  # noqa: E731
+    assert sse(d3) < sse(d2)
+    assert ((best.view("<u4")[:, 0] >> 11) & 3).astype(bool).mean() > 0.05
+
+
 @pytest.mark.parametrize("dim", [4, 6])
 def test_search_fp64_twin_runs(oracle, dim):
     rgba = synth.rgb_noise(40, 40, seed=9)
@@ -183,7 +233,7 @@ def test_bad_axis_and_quality_rejected(oracle):
     with pytest.raises(ValueError):
         oracle.encode(np.zeros((4, 4, 4), np.uint8), axis=2)
     with pytest.raises(ValueError):
-        oracle.encode(np.zeros((4, 4, 4), np.uint8), quality=3)
+        oracle.encode(np.zeros((4, 4, 4), np.uint8), quality=4)
 
 
 def test_thorough_recovers_alpha_cutouts(oracle):

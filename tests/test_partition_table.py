@@ -1,0 +1,61 @@
+"""The committed two-partition pattern table (csrc/astc_partition_table.h) is
+what the generator computes, and what the oracle's spec decoder does: a
+two-partition block with partition 0 black and partition 1 white (all weights
+zero) decodes to exactly the table's mask, for every partition index and
+both block sizes."""
+import os
+import re
+import sys
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+CSRC = os.path.join(ROOT, "astc_encoder_gb300", "csrc")
+
+
+def _header_tables():
+    text = open(os.path.join(CSRC, "astc_partition_table.h")).read()
+    out = {}
+    for name in ("kPartition2Mask4x4", "kPartition2Mask6x6"):
+        body = re.search(name + r"\[1024\] = \{(.*?)\};", text, re.S).group(1)
+        out[name] = [int(v.rstrip("ul"), 16) for v in re.findall(r"0x[0-9A-Fa-f]+u?l*", body)]
+        assert len(out[name]) == 1024
+    return out["kPartition2Mask4x4"], out["kPartition2Mask6x6"]
+
+
+def test_header_matches_generator():
+    sys.path.insert(0, CSRC)
+    try:
+        import gen_partition_table as gen
+    finally:
+        sys.path.remove(CSRC)
+    m4, m6 = _header_tables()
+    assert m4 == gen.masks(4)
+    assert m6 == gen.masks(6)
+
+
+def _two_partition_block(seed: int) -> np.ndarray:
+    # 4x4 weight grid, QUANT_3 weights (26 bits, all zero), 2 partitions, CEM 8
+    # for both; 12 endpoint values of QUANT_64 (6 bits each) from bit 29:
+    # partition 0 all 0 (black), partition 1 all 63 (white)
+    r = 3  # QUANT_3: R = 3 -> bits [1:0] = 1, bit 4 = 1; A = 2 at bits 5-6
+    mode = ((r >> 1) & 3) | ((r & 1) << 4) | (2 << 5)
+    v = mode | (1 << 11) | (seed << 13) | ((8 << 2) << 23)
+    for i in range(6, 12):
+        v |= 63 << (29 + 6 * i)
+    return np.frombuffer(v.to_bytes(16, "little"), np.uint8).copy()
+
+
+@pytest.mark.parametrize("dim", [4, 6])
+def test_table_matches_spec_decoder(oracle, dim):
+    m4, m6 = _header_tables()
+    table = m4 if dim == 4 else m6
+    for seed in range(1024):
+        rgba, err = oracle.decode_block(_two_partition_block(seed), dim, dim)
+        assert err == 0
+        rgba = rgba.reshape(-1, 4)
+        assert set(np.unique(rgba[:, 0]).tolist()) <= {0, 255}
+        mask = sum(1 << i for i in range(dim * dim) if rgba[i, 0] == 255)
+        assert mask == table[seed], seed
