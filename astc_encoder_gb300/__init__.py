@@ -68,6 +68,7 @@ class Quality(enum.IntEnum):
     FAST = 0                # the reference's fixed mode (518-522)
     SEARCH = 1              # every single-partition 4x4-grid mode, least decoded error
     THOROUGH = 2            # SEARCH from the better of the PCA and max-accumulation fits
+    PARTITIONS = 3          # THOROUGH plus two-partition blocks
 
 
 class AstcError(RuntimeError):

@@ -36,6 +36,7 @@ LIB_SOURCES = [
     ("astc_encode_h2.cu", ["--fmad=false"]),
     ("astc_encode_search.cu", ["--fmad=false"]),
     ("astc_encode_thorough.cu", ["--fmad=false"]),
+    ("astc_encode_partitions.cu", ["--fmad=false"]),
     ("astc_batch.cu", ["--fmad=false"]),
     ("astc_mips.cu", []),
     ("astc_server.cu", []),
@@ -49,7 +50,8 @@ CLI_SOURCES = [
     ("image_load.cpp", []),
 ]
 HEADERS = ["astc_internal.h", "astc_tables.h", "astc_block_common.cuh", "astc_pipeline_fp32.cuh",
-           "astc_pipeline_h2.cuh", "astc_pipeline_search.cuh", "astc_search_kernel.cuh", "astc_srgb_table.h", "image_load.h"]
+           "astc_pipeline_h2.cuh", "astc_pipeline_search.cuh", "astc_pipeline_partition.cuh", "astc_search_kernel.cuh",
+           "astc_partition_table.h", "astc_srgb_table.h", "image_load.h"]
 
 
 def nvcc() -> str:

@@ -1,14 +1,16 @@
 // astc_encode_search.cu -- instantiates the search kernel
 // (astc_search_kernel.cuh) for the fixed mode with the max-accumulation axis
 // and for the search from one fit; hands ASTC_QUALITY_THOROUGH to
-// astc_encode_thorough.cu.  Compiled with --fmad=false.
+// astc_encode_thorough.cu and ASTC_QUALITY_PARTITIONS to
+// astc_encode_partitions.cu.  Compiled with --fmad=false.
 #include "astc_search_kernel.cuh"
 
 namespace astc {
 
 cudaError_t launch_encode_search(const EncodeJob& j, cudaStream_t stream) {
     if (j.quality == ASTC_QUALITY_THOROUGH) return launch_encode_thorough(j, stream);
-    return launch_search_kernels<false>(j, stream);
+    if (j.quality == ASTC_QUALITY_PARTITIONS) return launch_encode_partitions(j, stream);
+    return launch_search_kernels<0>(j, stream);
 }
 
 }  // namespace astc

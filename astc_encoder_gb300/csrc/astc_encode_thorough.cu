@@ -7,7 +7,7 @@
 namespace astc {
 
 cudaError_t launch_encode_thorough(const EncodeJob& j, cudaStream_t stream) {
-    return launch_search_kernels<true>(j, stream);
+    return launch_search_kernels<1>(j, stream);
 }
 
 }  // namespace astc

@@ -40,6 +40,8 @@ cudaError_t launch_encode_h2(const EncodeJob& job, cudaStream_t stream);
 // the search from the better of both fits (astc_encode_thorough.cu).
 cudaError_t launch_encode_search(const EncodeJob& job, cudaStream_t stream);
 cudaError_t launch_encode_thorough(const EncodeJob& job, cudaStream_t stream);
+// THOROUGH plus two-partition candidates (astc_encode_partitions.cu).
+cudaError_t launch_encode_partitions(const EncodeJob& job, cudaStream_t stream);
 
 // Decoder / SSE launchers (astc_decode.cu).
 cudaError_t launch_decode(const uint8_t* blocks, int width, int height, int bw, int bh,

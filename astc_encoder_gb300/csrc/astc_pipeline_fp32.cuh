@@ -24,6 +24,29 @@ __device__ __forceinline__ float4 block_mean(const S& st) {
                        __fmul_rn(m3, kInvN));
 }
 
+// eigen_vector (93-106) of the symmetric 4x4 matrix c: v = M v; stop if
+// |v| < 1e-5 (returning that v); v = normalize(M v); eight rounds
+__device__ __forceinline__ float4 power_iteration(float c00, float c01, float c02, float c03, float c11,
+                                                  float c12, float c13, float c22, float c23, float c33) {
+    float v0 = 0.26726f, v1 = 0.80178f, v2 = 0.53452f, v3 = 0.0f;
+#pragma unroll 1
+    for (int it = 0; it < 8; ++it) {
+        float t0 = dot4(c00, c01, c02, c03, v0, v1, v2, v3);
+        float t1 = dot4(c01, c11, c12, c13, v0, v1, v2, v3);
+        float t2 = dot4(c02, c12, c22, c23, v0, v1, v2, v3);
+        float t3 = dot4(c03, c13, c23, c33, v0, v1, v2, v3);
+        v0 = t0; v1 = t1; v2 = t2; v3 = t3;
+        if (shorter_than_small_value(dot4(v0, v1, v2, v3, v0, v1, v2, v3))) break;
+        t0 = dot4(c00, c01, c02, c03, v0, v1, v2, v3);
+        t1 = dot4(c01, c11, c12, c13, v0, v1, v2, v3);
+        t2 = dot4(c02, c12, c22, c23, v0, v1, v2, v3);
+        t3 = dot4(c03, c13, c23, c33, v0, v1, v2, v3);
+        const float r = rnorm_from_dot(dot4(t0, t1, t2, t3, t0, t1, t2, t3));
+        v0 = __fmul_rn(t0, r); v1 = __fmul_rn(t1, r); v2 = __fmul_rn(t2, r); v3 = __fmul_rn(t3, r);
+    }
+    return make_float4(v0, v1, v2, v3);
+}
+
 // principal axis: covariance (149-162), symmetric, 10 unique terms,
 // x fl(1/(N-1)); power iteration (eigen_vector 93-106): v = M v; stop if
 // |v| < 1e-5; v = normalize(M v)
@@ -47,24 +70,7 @@ __device__ __forceinline__ float4 pca_axis(const S& st, const float4 m) {
     c03 = __fmul_rn(c03, kInvN1); c11 = __fmul_rn(c11, kInvN1); c12 = __fmul_rn(c12, kInvN1);
     c13 = __fmul_rn(c13, kInvN1); c22 = __fmul_rn(c22, kInvN1); c23 = __fmul_rn(c23, kInvN1);
     c33 = __fmul_rn(c33, kInvN1);
-
-    float v0 = 0.26726f, v1 = 0.80178f, v2 = 0.53452f, v3 = 0.0f;
-#pragma unroll 1
-    for (int it = 0; it < 8; ++it) {
-        float t0 = dot4(c00, c01, c02, c03, v0, v1, v2, v3);
-        float t1 = dot4(c01, c11, c12, c13, v0, v1, v2, v3);
-        float t2 = dot4(c02, c12, c22, c23, v0, v1, v2, v3);
-        float t3 = dot4(c03, c13, c23, c33, v0, v1, v2, v3);
-        v0 = t0; v1 = t1; v2 = t2; v3 = t3;
-        if (shorter_than_small_value(dot4(v0, v1, v2, v3, v0, v1, v2, v3))) break;
-        t0 = dot4(c00, c01, c02, c03, v0, v1, v2, v3);
-        t1 = dot4(c01, c11, c12, c13, v0, v1, v2, v3);
-        t2 = dot4(c02, c12, c22, c23, v0, v1, v2, v3);
-        t3 = dot4(c03, c13, c23, c33, v0, v1, v2, v3);
-        const float r = rnorm_from_dot(dot4(t0, t1, t2, t3, t0, t1, t2, t3));
-        v0 = __fmul_rn(t0, r); v1 = __fmul_rn(t1, r); v2 = __fmul_rn(t2, r); v3 = __fmul_rn(t3, r);
-    }
-    return make_float4(v0, v1, v2, v3);
+    return power_iteration(c00, c01, c02, c03, c11, c12, c13, c22, c23, c33);
 }
 
 // max_accumulation_pixel_direction (170-227), the shader's alternative axis:
@@ -110,10 +116,11 @@ __device__ __forceinline__ float4 max_accumulation_axis(const S& st, const float
 // e0/e1 are the float endpoints, q0/q1 their rounded (QUANT_256) values.
 template <int N, bool ALPHA, class S>
 __device__ __forceinline__ void find_min_max(const S& st, const float4 m, const float4 v, float e0[4],
-                                             float e1[4], uint32_t q0[4], uint32_t q1[4]) {
+                                             float e1[4], uint32_t q0[4], uint32_t q1[4], uint64_t sel = ~0ull) {
     float a = 1e31f, b = -1e31f;
 #pragma unroll
     for (int k = 0; k < N; ++k) {
+        if (!((sel >> k) & 1)) continue;                       // texels outside `sel` take no part
         const float4 t = st.get(k);
         const float p = dot4(__fsub_rn(t.x, m.x), __fsub_rn(t.y, m.y), __fsub_rn(t.z, m.z),
                              __fsub_rn(t.w, m.w), v.x, v.y, v.z, v.w);

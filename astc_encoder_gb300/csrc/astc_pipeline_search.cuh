@@ -63,6 +63,15 @@ struct PackedTexels {
     }
 };
 
+// Per-thread floats in a [k][thread] shared array.
+template <int N>
+struct SharedFloats {
+    float* base;
+    int stride;
+    __device__ __forceinline__ void put(int k, float v) { base[k * stride] = v; }
+    __device__ __forceinline__ float get(int k) const { return base[k * stride]; }
+};
+
 // Per-CTA copies of the search tables (shared memory).
 struct SearchSmem {
     uint16_t color[8][256];      // this format's endpoint ranges below QUANT_256
@@ -298,7 +307,7 @@ __device__ __forceinline__ void project_weights(const G& s, const int E0[4], con
 template <int DIM, bool ALPHA, bool SRGB, class G>
 __device__ __forceinline__ uint4 search_block(const G& grid, const uint32_t (&tw)[DIM * DIM], const uint32_t q0[4],
                                               const uint32_t q1[4], const uint32_t qw[16], const uint4 fixed,
-                                              const SearchSmem& sm) {
+                                              const SearchSmem& sm, uint32_t* err_out = nullptr) {
     typedef BlockError<DIM, ALPHA, SRGB> Err;
     constexpr int WQ0 = ALPHA ? kQuant6 : kQuant12;
     int E0[4], E1[4], sym0[4], sym1[4], W[16];
@@ -325,6 +334,7 @@ __device__ __forceinline__ uint4 search_block(const G& grid, const uint32_t (&tw
         const uint32_t err = Err::eval(tw, t2, E0, E1, W);
         if (err < best) { best = err; best_wq = wq; }
     }
+    if (err_out) *err_out = best;
     if (best_wq < 0) return fixed;
     const int cq = sm.cq[best_wq];
     snap_endpoints<ALPHA>(cq, sm.slot[best_wq], q0, q1, sm, sym0, sym1, E0, E1);

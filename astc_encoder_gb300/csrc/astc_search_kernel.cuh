@@ -12,7 +12,9 @@
 //            scored by its exact decode (astc_pipeline_search.cuh);
 //   quality = ASTC_QUALITY_THOROUGH: both fits, the search from the one
 //            whose fixed-mode block decodes with the smaller error (the
-//            PCA on ties).
+//            PCA on ties);
+//   quality = ASTC_QUALITY_PARTITIONS: THOROUGH plus two-partition
+//            candidates (astc_pipeline_partition.cuh; astc_encode_partitions.cu).
 // One thread encodes one block.  Texels stay packed (one register each) and
 // are re-decoded per pass, which keeps the 36-texel 6x6 search in registers.
 // Compile including units with --fmad=false: blocks are bit-identical to the
@@ -22,7 +24,7 @@
 #include <stdint.h>
 
 #include "astc_internal.h"
-#include "astc_pipeline_search.cuh"
+#include "astc_pipeline_partition.cuh"
 
 namespace astc {
 namespace {
@@ -31,6 +33,18 @@ constexpr int kSearchThreads = 128;
 
 __device__ const SearchTables g_search = make_search_tables();
 __device__ const SrgbBits g_srgb_bits_s = make_srgb_bits();
+struct PartitionClasses {
+    uint64_t c4[kPartition2Classes4x4Count];   // (index << 54) | pattern, as in PartSmem
+    uint64_t c6[kPartition2Classes6x6Count];
+};
+constexpr PartitionClasses make_partition_classes() {
+    PartitionClasses p{};
+    for (int i = 0; i < kPartition2Classes4x4Count; ++i)
+        p.c4[i] = ((uint64_t)(kPartition2Classes4x4[i] >> 16) << 54) | (kPartition2Classes4x4[i] & 0xFFFFu);
+    for (int i = 0; i < kPartition2Classes6x6Count; ++i) p.c6[i] = kPartition2Classes6x6[i];
+    return p;
+}
+__device__ const PartitionClasses g_classes = make_partition_classes();
 
 struct SearchLaunch {
     TextureView tex;
@@ -40,12 +54,29 @@ struct SearchLaunch {
     int search;   // 0 = fixed mode, 1 = search, 2 = search from the better fit
 };
 
+template <bool ALPHA>
+__device__ __forceinline__ void load_partition_smem(PartSmem& pm, int dim) {
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const uint32_t* src = reinterpret_cast<const uint32_t*>(&g_search.color[1][ALPHA][0][0]);
+    uint32_t* dst = reinterpret_cast<uint32_t*>(&pm.color[0][0]);
+    const int words = g_search.nslots[1][ALPHA] * 128;
+    for (int i = tid; i < words; i += nt) dst[i] = src[i];
+    const int n = dim == 6 ? kPartition2Classes6x6Count : kPartition2Classes4x4Count;
+    const uint64_t* cls = dim == 6 ? g_classes.c6 : g_classes.c4;
+    for (int i = tid; i < n; i += nt) pm.classes[i] = cls[i];
+    if (tid < 12) {
+        pm.cq[tid] = g_search.cq[1][ALPHA][tid];
+        pm.slot[tid] = g_search.slot[1][ALPHA][tid];
+    }
+    if (tid == 0) pm.nclasses = n;
+}
+
 template <bool ALPHA, bool SRGB>
 __device__ __forceinline__ void load_search_smem(SearchSmem& sm) {
     const int tid = threadIdx.x, nt = blockDim.x;
-    const uint32_t* src = reinterpret_cast<const uint32_t*>(&g_search.color[ALPHA][0][0]);
+    const uint32_t* src = reinterpret_cast<const uint32_t*>(&g_search.color[0][ALPHA][0][0]);
     uint32_t* dst = reinterpret_cast<uint32_t*>(&sm.color[0][0]);
-    const int words = g_search.nslots[ALPHA] * 128;
+    const int words = g_search.nslots[0][ALPHA] * 128;
     for (int i = tid; i < words; i += nt) dst[i] = src[i];
     for (int i = tid; i < 12 * 32; i += nt) {
         sm.wval[i >> 5][i & 31] = g_search.wval[i >> 5][i & 31];
@@ -61,8 +92,8 @@ __device__ __forceinline__ void load_search_smem(SearchSmem& sm) {
         }
     }
     if (tid < 12) {
-        sm.cq[tid] = g_search.cq[ALPHA][tid];
-        sm.slot[tid] = g_search.slot[ALPHA][tid];
+        sm.cq[tid] = g_search.cq[0][ALPHA][tid];
+        sm.slot[tid] = g_search.slot[0][ALPHA][tid];
         sm.wmax[tid] = (float)(quant_levels(tid) - 1);
     }
 }
@@ -120,11 +151,16 @@ __device__ __forceinline__ void pick_fit(const uint32_t (&tw)[DIM * DIM], const 
     }
 }
 
-template <int DIM, bool ALPHA, bool NORMAL, bool SRGB, bool THOROUGH>
+// MODE 0: fixed mode (max-accumulation axis) or SEARCH; 1: THOROUGH;
+// 2: THOROUGH plus two-partition candidates.
+template <int DIM, bool ALPHA, bool NORMAL, bool SRGB, int MODE>
 __global__ void __launch_bounds__(kSearchThreads, 3) astc_encode_blocks_search(const SearchLaunch p) {
     constexpr int N = DIM * DIM;
+    constexpr bool thorough = MODE >= 1;
     __shared__ SearchSmem sm;
+    __shared__ typename std::conditional<MODE == 2, PartSmem, char>::type pm;
     load_search_smem<ALPHA, SRGB>(sm);
+    if constexpr (MODE == 2) load_partition_smem<ALPHA>(pm, DIM);
     __syncthreads();
     const long long b = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= p.nblocks) return;
@@ -133,10 +169,9 @@ __global__ void __launch_bounds__(kSearchThreads, 3) astc_encode_blocks_search(c
     uint32_t px[N];
     load_block_packed<DIM>(p.tex, bx, by, px);
     const PackedTexels<N, SRGB, NORMAL> st{px, sm.lut};
-    constexpr bool thorough = THOROUGH;
     uint32_t q0[4], q1[4], qw[16];
     uint4 fixed = fit_fixed<DIM, ALPHA>(st, thorough ? 0 : p.axis, q0, q1, qw, sm.trits);
-    if (!THOROUGH && !p.search) {
+    if (!thorough && !p.search) {
         p.out[b] = fixed;
         return;
     }
@@ -153,6 +188,8 @@ __global__ void __launch_bounds__(kSearchThreads, 3) astc_encode_blocks_search(c
     // scoring loop already fill the register budget); then the texels as
     // the bytes the scoring compares with
     uint32_t tw[N];
+    uint4 blk;
+    uint32_t err = 0;
     if constexpr (DIM == 6) {
         extern __shared__ float4 s_grid[];
         SharedTexels<16> grid{s_grid + threadIdx.x, (int)blockDim.x};
@@ -161,7 +198,14 @@ __global__ void __launch_bounds__(kSearchThreads, 3) astc_encode_blocks_search(c
 #pragma unroll
         for (int k = 0; k < N; ++k) tw[k] = target_word<ALPHA, NORMAL, SRGB>(px[k], sm.tbyte);
         if constexpr (thorough) pick_fit<DIM, ALPHA, SRGB>(tw, sm, q0, q1, qw, fixed, fixed_b, rw_packed);
-        p.out[b] = search_block<DIM, ALPHA, SRGB>(grid, tw, q0, q1, qw, fixed, sm);
+        blk = search_block<DIM, ALPHA, SRGB>(grid, tw, q0, q1, qw, fixed, sm, &err);
+        if constexpr (MODE == 2) {
+            // the grid colours are done with: the same shared array holds the
+            // partition candidates' per-texel weights
+            SharedFloats<36> tws{reinterpret_cast<float*>(s_grid) + threadIdx.x, (int)blockDim.x};
+            blk = two_partition_block<DIM, ALPHA, SRGB>(st, tw, BlockError<DIM, ALPHA, SRGB>::target_sq(tw), q0,
+                                                        q1, err, blk, sm, pm, tws);
+        }
     } else {
         RegTexels<16> grid;
 #pragma unroll
@@ -169,35 +213,41 @@ __global__ void __launch_bounds__(kSearchThreads, 3) astc_encode_blocks_search(c
 #pragma unroll
         for (int k = 0; k < N; ++k) tw[k] = target_word<ALPHA, NORMAL, SRGB>(px[k], sm.tbyte);
         if constexpr (thorough) pick_fit<DIM, ALPHA, SRGB>(tw, sm, q0, q1, qw, fixed, fixed_b, rw_packed);
-        p.out[b] = search_block<DIM, ALPHA, SRGB>(grid, tw, q0, q1, qw, fixed, sm);
+        blk = search_block<DIM, ALPHA, SRGB>(grid, tw, q0, q1, qw, fixed, sm, &err);
+        if constexpr (MODE == 2) {
+            char none = 0;
+            blk = two_partition_block<DIM, ALPHA, SRGB>(st, tw, BlockError<DIM, ALPHA, SRGB>::target_sq(tw), q0,
+                                                        q1, err, blk, sm, pm, none);
+        }
     }
+    p.out[b] = blk;
 }
 
-template <int DIM, bool ALPHA, bool NORMAL, bool SRGB, bool THOROUGH>
+template <int DIM, bool ALPHA, bool NORMAL, bool SRGB, int MODE>
 cudaError_t launch_t(const SearchLaunch& p, cudaStream_t s) {
     const long long grid = (p.nblocks + kSearchThreads - 1) / kSearchThreads;
     const size_t smem = (DIM == 6 && p.search) ? (size_t)16 * kSearchThreads * sizeof(float4) : 0;
-    astc_encode_blocks_search<DIM, ALPHA, NORMAL, SRGB, THOROUGH><<<(unsigned)grid, kSearchThreads, smem, s>>>(p);
+    astc_encode_blocks_search<DIM, ALPHA, NORMAL, SRGB, MODE><<<(unsigned)grid, kSearchThreads, smem, s>>>(p);
     return cudaGetLastError();
 }
 
-template <bool THOROUGH, int DIM, bool ALPHA, bool NORMAL>
+template <int MODE, int DIM, bool ALPHA, bool NORMAL>
 cudaError_t launch_srgb(const SearchLaunch& p, bool srgb, cudaStream_t s) {
-    return srgb ? launch_t<DIM, ALPHA, NORMAL, true, THOROUGH>(p, s)
-                : launch_t<DIM, ALPHA, NORMAL, false, THOROUGH>(p, s);
+    return srgb ? launch_t<DIM, ALPHA, NORMAL, true, MODE>(p, s)
+                : launch_t<DIM, ALPHA, NORMAL, false, MODE>(p, s);
 }
-template <bool THOROUGH, int DIM, bool ALPHA>
+template <int MODE, int DIM, bool ALPHA>
 cudaError_t launch_norm(const SearchLaunch& p, bool normal, bool srgb, cudaStream_t s) {
-    return normal ? launch_srgb<THOROUGH, DIM, ALPHA, true>(p, srgb, s)
-                  : launch_srgb<THOROUGH, DIM, ALPHA, false>(p, srgb, s);
+    return normal ? launch_srgb<MODE, DIM, ALPHA, true>(p, srgb, s)
+                  : launch_srgb<MODE, DIM, ALPHA, false>(p, srgb, s);
 }
-template <bool THOROUGH, int DIM>
+template <int MODE, int DIM>
 cudaError_t launch_alpha(const SearchLaunch& p, bool alpha, bool normal, bool srgb, cudaStream_t s) {
-    return alpha ? launch_norm<THOROUGH, DIM, true>(p, normal, srgb, s)
-                 : launch_norm<THOROUGH, DIM, false>(p, normal, srgb, s);
+    return alpha ? launch_norm<MODE, DIM, true>(p, normal, srgb, s)
+                 : launch_norm<MODE, DIM, false>(p, normal, srgb, s);
 }
 
-template <bool THOROUGH>
+template <int MODE>
 cudaError_t launch_search_kernels(const EncodeJob& j, cudaStream_t stream) {
     SearchLaunch p;
     p.tex = make_view(j);
@@ -206,8 +256,8 @@ cudaError_t launch_search_kernels(const EncodeJob& j, cudaStream_t stream) {
     p.axis = j.axis;
     p.search = j.quality == ASTC_QUALITY_FAST ? 0 : 1;
     const bool alpha = j.has_alpha != 0, normal = j.is_normal != 0, srgb = j.srgb != 0;
-    const cudaError_t e = j.block_dim == 4 ? launch_alpha<THOROUGH, 4>(p, alpha, normal, srgb, stream)
-                                           : launch_alpha<THOROUGH, 6>(p, alpha, normal, srgb, stream);
+    const cudaError_t e = j.block_dim == 4 ? launch_alpha<MODE, 4>(p, alpha, normal, srgb, stream)
+                                           : launch_alpha<MODE, 6>(p, alpha, normal, srgb, stream);
     if (e == cudaSuccess) count_launches(1);
     return e;
 }

@@ -230,13 +230,14 @@ constexpr ASTC_HD uint32_t blockmode_4x4_grid(int weight_quant) {
 // search mode: the single-partition modes with a 4x4 weight grid
 // ---------------------------------------------------------------------------
 // Endpoint quant method of weight quant method wq with nvals endpoint values:
-// the decoder takes the largest range whose ISE fits between bit 17 and the
-// weights; the mode is illegal outside 24..96 weight bits or below QUANT_6.
-constexpr ASTC_HD int endpoint_quant_for(int wq, int nvals) {
+// the decoder takes the largest range whose ISE fits between the header (17
+// bits for one partition, 29 for two sharing one CEM) and the weights; the
+// mode is illegal outside 24..96 weight bits or below QUANT_6.
+constexpr ASTC_HD int endpoint_quant_for(int wq, int nvals, int header_bits = 17) {
     if (wq < kQuant2 || wq > kQuant32) return -1;
     const int wbits = ise_bit_count(wq, 16);
     if (wbits < 24 || wbits > 96) return -1;
-    const int avail = 128 - 17 - wbits;
+    const int avail = 128 - header_bits - wbits;
     for (int q = kQuant256; q >= kQuant6; --q)
         if (ise_bit_count(q, nvals) <= avail) return q;
     return -1;
@@ -244,30 +245,32 @@ constexpr ASTC_HD int endpoint_quant_for(int wq, int nvals) {
 
 struct SearchTables {
     // (unquantised << 8) | symbol of the colour value nearest each byte
-    // (ties: the smaller value), per endpoint range used below QUANT_256
-    uint16_t color[2][8][256];     // [alpha][slot][byte]
-    int8_t slot[2][12];            // [alpha][wq] -> slot, -1 = QUANT_256
-    int8_t cq[2][12];              // [alpha][wq] -> endpoint quant method
+    // (ties: the smaller value), per endpoint range used below QUANT_256;
+    // [parts - 1] = one partition (6 / 8 values) or two (12 / 16 values)
+    uint16_t color[2][2][8][256];  // [parts - 1][alpha][slot][byte]
+    int8_t slot[2][2][12];         // [parts - 1][alpha][wq] -> slot, -1 = QUANT_256
+    int8_t cq[2][2][12];           // [parts - 1][alpha][wq] -> endpoint quant method
     uint8_t wval[12][32];          // [wq][value-order index] -> weight 0..64
     uint8_t scramble[12][32];      // [wq][value-order index] -> ISE symbol
     uint8_t trit_pack[256];
     uint8_t quint_pack[128];
-    int nslots[2];                 // [alpha] rows of color in use
+    int nslots[2][2];              // [parts - 1][alpha] rows of color in use
 };
 
 constexpr SearchTables make_search_tables() {
     SearchTables s{};
     const IseTables t = make_ise_tables();
+    for (int pt = 0; pt < 2; ++pt)
     for (int a = 0; a < 2; ++a) {
         int nslots = 0;
         for (int wq = 0; wq < 12; ++wq) {
-            const int cq = endpoint_quant_for(wq, a ? 8 : 6);
-            s.cq[a][wq] = (int8_t)cq;
-            s.slot[a][wq] = -1;
+            const int cq = endpoint_quant_for(wq, (a ? 8 : 6) * (pt + 1), pt ? 29 : 17);
+            s.cq[pt][a][wq] = (int8_t)cq;
+            s.slot[pt][a][wq] = -1;
             if (cq < 0 || cq == kQuant256) continue;
             int slot = -1;
             for (int w2 = 0; w2 < wq; ++w2)
-                if (s.cq[a][w2] == cq) slot = s.slot[a][w2];
+                if (s.cq[pt][a][w2] == cq) slot = s.slot[pt][a][w2];
             if (slot < 0) {
                 slot = nslots++;
                 // symbols by value, then each byte's nearest on either side
@@ -281,12 +284,12 @@ constexpr SearchTables make_search_tables() {
                 for (int v = 255; v >= 0; --v) { if (sym_at[v] >= 0) last = v; above[v] = last; }
                 for (int v = 0; v < 256; ++v) {
                     const int u = (v - below[v] <= above[v] - v) ? below[v] : above[v];
-                    s.color[a][slot][v] = (uint16_t)((u << 8) | sym_at[u]);
+                    s.color[pt][a][slot][v] = (uint16_t)((u << 8) | sym_at[u]);
                 }
             }
-            s.slot[a][wq] = (int8_t)slot;
+            s.slot[pt][a][wq] = (int8_t)slot;
         }
-        s.nslots[a] = nslots;
+        s.nslots[pt][a] = nslots;
     }
     for (int wq = 0; wq < 12; ++wq)
         for (int i = 0; i < quant_levels(wq); ++i) {

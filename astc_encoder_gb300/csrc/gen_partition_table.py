@@ -72,8 +72,29 @@ def masks(dim: int) -> list:
     return out
 
 
+def classes(dim: int) -> list:
+    """(seed, mask) of the smallest partition index of every class {pattern,
+    complement} that splits the block, in index order.  Scanning these in
+    order with a strict 'fewer mismatches' test picks the same index as
+    scanning all 1024 (a pattern and its complement score alike, duplicates
+    score alike, and ties go to the smallest index)."""
+    full = (1 << (dim * dim)) - 1
+    seen = set()
+    out = []
+    for seed, m in enumerate(masks(dim)):
+        if m in (0, full):
+            continue
+        key = min(m, full ^ m)
+        if key in seen:
+            continue
+        seen.add(key)
+        out.append((seed, m))
+    return out
+
+
 def main() -> None:
     m4, m6 = masks(4), masks(6)
+    c4, c6 = classes(4), classes(6)
     lines = ["// Generated by gen_partition_table.py -- do not edit.",
              "// Two-partition ASTC blocks: for each partition index 0..1023, the texels",
              "// (bit y * dim + x) that the specification's partition hash puts in partition 1.",
@@ -85,6 +106,19 @@ def main() -> None:
     lines.append("constexpr uint64_t kPartition2Mask6x6[1024] = {")
     for i in range(0, 1024, 6):
         lines.append("    " + ", ".join(f"0x{v:09X}ull" for v in m6[i:i + 6]) + ",")
+    lines.append("};")
+    lines.append("// The smallest partition index of each {pattern, complement} class that")
+    lines.append("// splits the block, in index order: (index << 16) | mask for 4x4, (index << 54) | mask")
+    lines.append("// for 6x6.")
+    lines.append(f"constexpr int kPartition2Classes4x4Count = {len(c4)};")
+    lines.append(f"constexpr uint32_t kPartition2Classes4x4[{len(c4)}] = {{")
+    for i in range(0, len(c4), 8):
+        lines.append("    " + ", ".join(f"0x{(sd << 16) | m:08X}u" for sd, m in c4[i:i + 8]) + ",")
+    lines.append("};")
+    lines.append(f"constexpr int kPartition2Classes6x6Count = {len(c6)};")
+    lines.append(f"constexpr uint64_t kPartition2Classes6x6[{len(c6)}] = {{")
+    for i in range(0, len(c6), 4):
+        lines.append("    " + ", ".join(f"0x{(sd << 54) | m:016X}ull" for sd, m in c6[i:i + 4]) + ",")
     lines += ["};", "}  // namespace astc", ""]
     out = os.path.join(os.path.dirname(os.path.abspath(__file__)), "astc_partition_table.h")
     with open(out, "w") as fh:

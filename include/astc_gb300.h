@@ -84,13 +84,21 @@ typedef enum astc_quality {
                                     choose_best_quantmethod the
                                     reference sketches (524-526).  Never
                                     worse than FAST; FP32 only              */
-    ASTC_QUALITY_THOROUGH = 2    /* SEARCH from the better of the two fits:
+    ASTC_QUALITY_THOROUGH = 2,   /* SEARCH from the better of the two fits:
                                     PCA and max accumulation both run, the
                                     one whose fixed-mode block decodes with
                                     less error is searched from (PCA on
                                     ties; opts.axis is ignored).  Recovers
                                     the blocks the reference's PCA collapses
                                     (flat colour, varying alpha); FP32 only */
+    ASTC_QUALITY_PARTITIONS = 3  /* THOROUGH plus two-partition blocks: the
+                                    partition index whose pattern best
+                                    matches the split along the kept fit,
+                                    each partition fitted on its own, every
+                                    legal weight range scored by its exact
+                                    decode (the reference has only a
+                                    commented-out layout stub for partitions,
+                                    ASTC_Encode.hlsl:422-431); FP32 only    */
 } astc_quality;
 
 /* Encoder options: the reference's encode_option (astc_encode.h:14-28) plus

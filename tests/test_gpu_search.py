@@ -35,8 +35,8 @@ def _psnr(a, b):
     return float("inf") if mse == 0 else 10 * np.log10(255.0 ** 2 / mse)
 
 
-GRID = [g for g in itertools.product([4, 6], [False, True], [False, True], [False, True], [0, 1], [0, 1, 2])
-        if (g[4] or g[5]) and not (g[5] == 2 and g[4] == 1)]
+GRID = [g for g in itertools.product([4, 6], [False, True], [False, True], [False, True], [0, 1], [0, 1, 2, 3])
+        if (g[4] or g[5]) and not (g[5] >= 2 and g[4] == 1)]
 
 
 @pytest.mark.parametrize("dim,alpha,normal,srgb,axis,quality", GRID)
@@ -54,7 +54,7 @@ def test_option_grid_bit_exact(native, oracle, dim, alpha, normal, srgb, axis, q
 def test_ragged_sizes(native, oracle, h, w, dim):
     img = _texture(h, w, seed=h * 1000 + w)
     for border in (0, 1):
-        for quality in (1, 2):
+        for quality in (1, 2, 3):
             opts = dict(block_dim=dim, has_alpha=True, border=border, quality=quality)
             assert np.array_equal(native.encode(img, **opts), oracle.encode(img, **opts))
 
@@ -71,7 +71,7 @@ def test_constant_images(native, oracle):
                 assert np.array_equal(got, native.encode(img, block_dim=dim, has_alpha=alpha))
 
 
-@pytest.mark.parametrize("quality", [1, 2])
+@pytest.mark.parametrize("quality", [1, 2, 3])
 @pytest.mark.parametrize("name", ["4x4_rgb_512", "6x6_rgba_srgb_2048", "4x4_normal_4096"])
 def test_workloads_full_size(native, oracle, name, quality):
     """Full-size workloads: bit-exact, decodes cleanly, never worse than FAST."""

@@ -25,6 +25,45 @@ def _header_tables():
     return out["kPartition2Mask4x4"], out["kPartition2Mask6x6"]
 
 
+def _header_classes():
+    text = open(os.path.join(CSRC, "astc_partition_table.h")).read()
+    out = []
+    for name, shift, mbits in (("kPartition2Classes4x4", 16, 16), ("kPartition2Classes6x6", 54, 36)):
+        body = re.search(name + r"\[\d+\] = \{(.*?)\};", text, re.S).group(1)
+        vals = [int(v.rstrip("ul"), 16) for v in re.findall(r"0x[0-9A-Fa-f]+u?l*", body)]
+        out.append([(v >> shift, v & ((1 << mbits) - 1)) for v in vals])
+    return out
+
+
+def test_classes_pick_the_same_index_as_a_full_scan():
+    """The class lists scanned in order give the full scan's choice for any split."""
+    m4, m6 = _header_tables()
+    c4, c6 = _header_classes()
+    rng = np.random.default_rng(3)
+    for dim, table, cls in ((4, m4, c4), (6, m6, c6)):
+        n = dim * dim
+        full = (1 << n) - 1
+        for s, m in cls:
+            assert table[s] == m and m not in (0, full)
+        for _ in range(300):
+            ideal = int(rng.integers(1, full))
+            best = (n + 1, -1)
+            for s, m in enumerate(table):
+                if m in (0, full):
+                    continue
+                d = bin(m ^ ideal).count("1")
+                d = min(d, n - d)
+                if d < best[0]:
+                    best = (d, s)
+            got = (n + 1, -1)
+            for s, m in cls:
+                d = bin(m ^ ideal).count("1")
+                d = min(d, n - d)
+                if d < got[0]:
+                    got = (d, s)
+            assert got == best
+
+
 def test_header_matches_generator():
     sys.path.insert(0, CSRC)
     try:
@@ -34,6 +73,7 @@ def test_header_matches_generator():
     m4, m6 = _header_tables()
     assert m4 == gen.masks(4)
     assert m6 == gen.masks(6)
+    assert _header_classes() == [gen.classes(4), gen.classes(6)]
 
 
 def _two_partition_block(seed: int) -> np.ndarray:
