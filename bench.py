@@ -68,7 +68,7 @@ def _parse():
                     help="small case for ncu: one FP32 and one HALF2 batched graph launch")
     ap.add_argument("--profile-case", action="store_true",
                     help="small case for ncu: 2 textures per step, encode launches only")
-    ap.add_argument("--profile-quality", default="fast", choices=["fast", "search", "thorough"],
+    ap.add_argument("--profile-quality", default="fast", choices=["fast", "search", "thorough", "partitions"],
                     help="with --profile-case: the quality mode the launches use (FP32)")
     return ap.parse_args()
 
@@ -535,7 +535,7 @@ def run_ours(args) -> None:
 
     if args.profile_case:
         # only the encode launches: warm-up, then the timed steps; no other kernels
-        quality = {"fast": 0, "search": 1, "thorough": 2}[args.profile_quality]
+        quality = {"fast": 0, "search": 1, "thorough": 2, "partitions": 3}[args.profile_quality]
         spec_prof = dict(spec_run, quality=quality) if quality else spec_run
         _time_launches(torch, native, texs, outs, spec_prof, max(3, args.warmup))
         per, _, launches = _time_launches(torch, native, texs, outs, spec_prof, args.steps)
