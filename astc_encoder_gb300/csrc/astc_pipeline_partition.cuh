@@ -20,14 +20,13 @@
 
 namespace astc {
 
-constexpr int kPartitionClassesMax =
-    kPartition2Classes6x6Count > kPartition2Classes4x4Count ? kPartition2Classes6x6Count
-                                                            : kPartition2Classes4x4Count;
-
 // Per-CTA copies of the two-partition tables (shared memory).
 struct PartSmem {
     uint16_t color[8][256];                  // endpoint ranges of two-partition modes
-    uint64_t classes[kPartitionClassesMax];  // (index << 54) | pattern
+    union {
+        uint64_t c6[kPartition2Classes6x6Count];   // (index << 54) | 36-bit pattern
+        uint32_t c4[kPartition2Classes4x4Count];   // (index << 16) | 16-bit pattern
+    } classes;
     int8_t cq[12];                           // weight range -> endpoint range (-1: illegal)
     int8_t slot[12];
     int nclasses;
@@ -69,16 +68,6 @@ __device__ __forceinline__ void fit_partition(const S& st, uint64_t sel, uint32_
     const float4 v = power_iteration(c00, c01, c02, c03, c11, c12, c13, c22, c23, c33);
     float e0[4], e1[4];
     find_min_max<N, ALPHA>(st, m, v, e0, e1, q0, q1, sel);
-}
-
-// Clamped projection of texel t on endpoints e0 -> e0 + d (r = 1 / |d|^2;
-// flat partitions weigh 0), as the oracle computes it.
-__device__ __forceinline__ float part_weight(const float4 t, const float f[4], const float d[4], float r,
-                                             bool flat) {
-    if (flat) return 0.0f;
-    const float x = dot4(__fsub_rn(t.x, f[0]), __fsub_rn(t.y, f[1]), __fsub_rn(t.z, f[2]),
-                         __fsub_rn(t.w, f[3]), d[0], d[1], d[2], d[3]);
-    return fminf(fmaxf(__fmul_rn(x, r), 0.0f), 1.0f);
 }
 
 // The squared error of a two-partition decode: as BlockError::eval with the
@@ -158,33 +147,49 @@ __device__ __forceinline__ void snap_two(int cq, int slot, const uint32_t a0[4],
 // Grid weights (value-order indices q) of a two-partition candidate: texel
 // weights on the texel's own partition; 4x4 rounds them directly, 6x6 keeps
 // them in `tws` ([texel][thread] floats) and samples the shader's 2x2 taps.
+// Each partition's values are held in named registers and chosen with the
+// texel's partition bit (an array indexed by it would live in local memory).
+struct PartLine {
+    float f0, f1, f2, f3;   // decoded low endpoint
+    float d0, d1, d2, d3;   // high - low
+    float r;                // 1 / |d|^2 (0 for a flat partition)
+    bool flat;
+};
+
+__device__ __forceinline__ PartLine part_line(const int E0[4], const int E1[4]) {
+    PartLine l;
+    l.f0 = (float)E0[0]; l.f1 = (float)E0[1]; l.f2 = (float)E0[2]; l.f3 = (float)E0[3];
+    l.d0 = (float)(E1[0] - E0[0]); l.d1 = (float)(E1[1] - E0[1]);
+    l.d2 = (float)(E1[2] - E0[2]); l.d3 = (float)(E1[3] - E0[3]);
+    const float dd = dot4(l.d0, l.d1, l.d2, l.d3, l.d0, l.d1, l.d2, l.d3);
+    l.flat = dd == 0.0f;
+    l.r = l.flat ? 0.0f : __frcp_rn(dd);
+    return l;
+}
+
+__device__ __forceinline__ float part_weight_sel(const float4 t, bool p1, const PartLine& a, const PartLine& b) {
+    const bool flat = p1 ? b.flat : a.flat;
+    const float x = dot4(__fsub_rn(t.x, p1 ? b.f0 : a.f0), __fsub_rn(t.y, p1 ? b.f1 : a.f1),
+                         __fsub_rn(t.z, p1 ? b.f2 : a.f2), __fsub_rn(t.w, p1 ? b.f3 : a.f3),
+                         p1 ? b.d0 : a.d0, p1 ? b.d1 : a.d1, p1 ? b.d2 : a.d2, p1 ? b.d3 : a.d3);
+    const float w = fminf(fmaxf(__fmul_rn(x, p1 ? b.r : a.r), 0.0f), 1.0f);
+    return flat ? 0.0f : w;
+}
+
 template <int DIM, class S, class TW>
 __device__ __forceinline__ void two_partition_weights(const S& st, uint64_t sel1, const int E0[2][4],
                                                       const int E1[2][4], float R, TW& tws, uint32_t (&q)[16]) {
-    float f[2][4], d[2][4], r[2];
-    bool flat[2];
-#pragma unroll
-    for (int p = 0; p < 2; ++p) {
-#pragma unroll
-        for (int c = 0; c < 4; ++c) { f[p][c] = (float)E0[p][c]; d[p][c] = (float)(E1[p][c] - E0[p][c]); }
-        const float dd = dot4(d[p][0], d[p][1], d[p][2], d[p][3], d[p][0], d[p][1], d[p][2], d[p][3]);
-        flat[p] = dd == 0.0f;
-        r[p] = flat[p] ? 0.0f : __frcp_rn(dd);
-    }
+    const PartLine la = part_line(E0[0], E1[0]), lb = part_line(E0[1], E1[1]);
     if constexpr (DIM == 4) {
 #pragma unroll
         for (int k = 0; k < 16; ++k) {
-            const int p = (int)((sel1 >> k) & 1);
-            const float w = part_weight(st.get(k), f[p], d[p], r[p], flat[p]);
+            const float w = part_weight_sel(st.get(k), (sel1 >> k) & 1, la, lb);
             const uint32_t v = rint_u32(__fmul_rn(w, R));
             q[k] = v < (uint32_t)R ? v : (uint32_t)R;
         }
     } else {
 #pragma unroll
-        for (int k = 0; k < 36; ++k) {
-            const int p = (int)((sel1 >> k) & 1);
-            tws.put(k, part_weight(st.get(k), f[p], d[p], r[p], flat[p]));
-        }
+        for (int k = 0; k < 36; ++k) tws.put(k, part_weight_sel(st.get(k), (sel1 >> k) & 1, la, lb));
 #pragma unroll
         for (int g = 0; g < 16; ++g) {
             const int i0 = grid_tap0(g);
@@ -243,16 +248,33 @@ __device__ __forceinline__ uint4 two_partition_block(const S& st, const uint32_t
     if (ideal == 0 || ideal == kFull) return best;
     // the best-matching partition pattern
     int best_m = N + 1;
-    uint64_t pick = 0;
+    uint64_t sel1;
+    int seed;
+    if constexpr (DIM == 4) {
+        const uint32_t ideal32 = (uint32_t)ideal;
+        uint32_t pick = 0;
 #pragma unroll 4
-    for (int i = 0; i < pm.nclasses; ++i) {
-        const uint64_t e = pm.classes[i];
-        int m = __popcll((e & kPatternBits) ^ ideal);
-        m = (N - m < m) ? N - m : m;
-        if (m < best_m) { best_m = m; pick = e; }
+        for (int i = 0; i < pm.nclasses; ++i) {
+            const uint32_t e = pm.classes.c4[i];
+            int m = __popc((e & 0xFFFFu) ^ ideal32);
+            m = (N - m < m) ? N - m : m;
+            if (m < best_m) { best_m = m; pick = e; }
+        }
+        sel1 = pick & 0xFFFFu;
+        seed = (int)(pick >> 16);
+    } else {
+        uint64_t pick = 0;
+#pragma unroll 4
+        for (int i = 0; i < pm.nclasses; ++i) {
+            const uint64_t e = pm.classes.c6[i];
+            int m = __popcll((e & kPatternBits) ^ ideal);
+            m = (N - m < m) ? N - m : m;
+            if (m < best_m) { best_m = m; pick = e; }
+        }
+        sel1 = pick & kPatternBits;
+        seed = (int)(pick >> 54);
     }
-    const uint64_t sel1 = pick & kPatternBits, sel0 = kFull & ~sel1;
-    const int seed = (int)(pick >> 54);
+    const uint64_t sel0 = kFull & ~sel1;
     // one fit per partition (one copy of the code: the loop is not unrolled)
     uint32_t a0[4], a1[4], b0[4], b1[4];
 #pragma unroll 1

@@ -34,13 +34,12 @@ constexpr int kSearchThreads = 128;
 __device__ const SearchTables g_search = make_search_tables();
 __device__ const SrgbBits g_srgb_bits_s = make_srgb_bits();
 struct PartitionClasses {
-    uint64_t c4[kPartition2Classes4x4Count];   // (index << 54) | pattern, as in PartSmem
+    uint32_t c4[kPartition2Classes4x4Count];   // as in PartSmem
     uint64_t c6[kPartition2Classes6x6Count];
 };
 constexpr PartitionClasses make_partition_classes() {
     PartitionClasses p{};
-    for (int i = 0; i < kPartition2Classes4x4Count; ++i)
-        p.c4[i] = ((uint64_t)(kPartition2Classes4x4[i] >> 16) << 54) | (kPartition2Classes4x4[i] & 0xFFFFu);
+    for (int i = 0; i < kPartition2Classes4x4Count; ++i) p.c4[i] = kPartition2Classes4x4[i];
     for (int i = 0; i < kPartition2Classes6x6Count; ++i) p.c6[i] = kPartition2Classes6x6[i];
     return p;
 }
@@ -62,8 +61,10 @@ __device__ __forceinline__ void load_partition_smem(PartSmem& pm, int dim) {
     const int words = g_search.nslots[1][ALPHA] * 128;
     for (int i = tid; i < words; i += nt) dst[i] = src[i];
     const int n = dim == 6 ? kPartition2Classes6x6Count : kPartition2Classes4x4Count;
-    const uint64_t* cls = dim == 6 ? g_classes.c6 : g_classes.c4;
-    for (int i = tid; i < n; i += nt) pm.classes[i] = cls[i];
+    for (int i = tid; i < n; i += nt) {
+        if (dim == 6) pm.classes.c6[i] = g_classes.c6[i];
+        else pm.classes.c4[i] = g_classes.c4[i];
+    }
     if (tid < 12) {
         pm.cq[tid] = g_search.cq[1][ALPHA][tid];
         pm.slot[tid] = g_search.slot[1][ALPHA][tid];
@@ -123,30 +124,32 @@ __device__ __forceinline__ void pick_fit(const uint32_t (&tw)[DIM * DIM], const 
     constexpr int WQ0 = ALPHA ? kQuant6 : kQuant12;
     const uint32_t t2 = Err::target_sq(tw);
     const uint64_t ep = (((uint64_t)fixed_b.y << 32 | fixed_b.x) >> 17) | (((uint64_t)fixed_b.w << 32 | fixed_b.z) << 47);
-    uint32_t r0[4], r1[4], rw[16];
+    uint32_t r0[4], r1[4];
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
         r0[c] = (ALPHA || c < 3) ? (uint32_t)(ep >> (16 * c)) & 0xFFu : 255u;
         r1[c] = (ALPHA || c < 3) ? (uint32_t)(ep >> (16 * c + 8)) & 0xFFu : 255u;
     }
+    // both fits scored by one copy of the scoring code
+    uint32_t ea = 0;
+    bool take_b = false;
+#pragma unroll 1
+    for (int f = 0; f < 2; ++f) {
+        int E0[4], E1[4], W[16];
 #pragma unroll
-    for (int g = 0; g < 16; ++g) rw[g] = (uint32_t)(rw_packed >> (4 * g)) & 0xFu;
-    int E0[4], E1[4], W[16];
+        for (int c = 0; c < 4; ++c) { E0[c] = (int)(f ? r0[c] : q0[c]); E1[c] = (int)(f ? r1[c] : q1[c]); }
 #pragma unroll
-    for (int c = 0; c < 4; ++c) { E0[c] = (int)q0[c]; E1[c] = (int)q1[c]; }
-#pragma unroll
-    for (int g = 0; g < 16; ++g) W[g] = sm.wval[WQ0][qw[g]];
-    const uint32_t ea = Err::eval(tw, t2, E0, E1, W);
-#pragma unroll
-    for (int c = 0; c < 4; ++c) { E0[c] = (int)r0[c]; E1[c] = (int)r1[c]; }
-#pragma unroll
-    for (int g = 0; g < 16; ++g) W[g] = sm.wval[WQ0][rw[g]];
-    const uint32_t eb = Err::eval(tw, t2, E0, E1, W);
-    if (eb < ea) {
+        for (int g = 0; g < 16; ++g)
+            W[g] = sm.wval[WQ0][f ? (uint32_t)(rw_packed >> (4 * g)) & 0xFu : qw[g]];
+        const uint32_t e = Err::eval(tw, t2, E0, E1, W);
+        if (f == 0) ea = e;
+        else take_b = e < ea;
+    }
+    if (take_b) {
 #pragma unroll
         for (int c = 0; c < 4; ++c) { q0[c] = r0[c]; q1[c] = r1[c]; }
 #pragma unroll
-        for (int g = 0; g < 16; ++g) qw[g] = rw[g];
+        for (int g = 0; g < 16; ++g) qw[g] = (uint32_t)(rw_packed >> (4 * g)) & 0xFu;
         fixed = fixed_b;
     }
 }
