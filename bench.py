@@ -286,10 +286,11 @@ def _psnr_blocks(native, blocks: np.ndarray, tex: np.ndarray, spec: dict) -> flo
 
 
 def _bench_search(torch, native, headline: str, texs, outs, spec: dict) -> dict:
-    """Throughput and decoded PSNR of the search mode (every single-partition
-    4x4-grid mode, least decoded error) and of the max-accumulation axis,
-    against the fixed mode, on each workload (device-resident inputs above
-    L2 size, as the headline)."""
+    """Throughput and decoded PSNR of the quality modes -- the search (every
+    single-partition 4x4-grid mode, least decoded error), the max-accumulation
+    axis, THOROUGH (search from the better fit) and PARTITIONS (THOROUGH plus
+    two-partition blocks) -- against the fixed mode, on each workload
+    (device-resident inputs above L2 size, as the headline)."""
     from astc_encoder_gb300 import synth
     result = {}
     for name in (headline, "4x4_rgb_512", "4x4_normal_4096", "6x6_rgba_srgb_2048"):
@@ -309,7 +310,7 @@ def _bench_search(torch, native, headline: str, texs, outs, spec: dict) -> dict:
         tex0 = st[0].cpu().numpy()
         entry = {"textures_per_step": len(st)}
         for label, kw in (("fast", {}), ("search", dict(quality=1)), ("max_accumulation", dict(axis=1)),
-                          ("thorough", dict(quality=2))):
+                          ("thorough", dict(quality=2)), ("partitions", dict(quality=3))):
             run = dict(sspec, **kw)
             _time_launches(torch, native, st, so, run, 2)
             per, steps, _ = _time_launches(torch, native, st, so, run, 5)
@@ -318,6 +319,7 @@ def _bench_search(torch, native, headline: str, texs, outs, spec: dict) -> dict:
                             "psnr_db": _psnr_blocks(native, so[0].cpu().numpy(), tex0, sspec)}
         entry["search_gain_db"] = entry["search"]["psnr_db"] - entry["fast"]["psnr_db"]
         entry["thorough_gain_db"] = entry["thorough"]["psnr_db"] - entry["fast"]["psnr_db"]
+        entry["partitions_gain_db"] = entry["partitions"]["psnr_db"] - entry["fast"]["psnr_db"]
         result[name] = entry
         if name != headline:
             del st, so
