@@ -114,10 +114,11 @@ __device__ __forceinline__ uint32_t eval_two_partitions(const uint32_t (&tw)[DIM
     return dd - 2u * dt + t2;
 }
 
-// Snapped endpoints of both partitions for endpoint range cq (symbols and
-// decoded values, darker first in each partition).
+// Snapped endpoints of both partitions for the endpoint range whose
+// nearest-colour table is row `slot` (symbols and decoded values, darker
+// first in each partition).
 template <bool ALPHA>
-__device__ __forceinline__ void snap_two(int cq, int slot, const uint32_t a0[4], const uint32_t a1[4],
+__device__ __forceinline__ void snap_two(int slot, const uint32_t a0[4], const uint32_t a1[4],
                                          const uint32_t b0[4], const uint32_t b1[4], const PartSmem& pm,
                                          int sym0[2][4], int sym1[2][4], int E0[2][4], int E1[2][4]) {
     constexpr int NCH = ALPHA ? 4 : 3;
@@ -141,7 +142,6 @@ __device__ __forceinline__ void snap_two(int cq, int slot, const uint32_t a0[4],
             }
         }
     }
-    (void)cq;
 }
 
 // Grid weights (value-order indices q) of a two-partition candidate: texel
@@ -301,7 +301,7 @@ __device__ __forceinline__ uint4 two_partition_block(const S& st, const uint32_t
         const int wq = final_pass ? found : it;
         const int cq = pm.cq[wq];
         if (cq < 0) continue;
-        snap_two<ALPHA>(cq, pm.slot[wq], a0, a1, b0, b1, pm, sym0, sym1, E0, E1);
+        snap_two<ALPHA>(pm.slot[wq], a0, a1, b0, b1, pm, sym0, sym1, E0, E1);
         two_partition_weights<DIM>(st, sel1, E0, E1, sm.wmax[wq], tws, q);
         if (!final_pass) {
 #pragma unroll
