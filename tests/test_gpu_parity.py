@@ -292,6 +292,65 @@ def test_host_memory_upload_ring(native, oracle):
         assert np.array_equal(b.numpy(), oracle.encode(np.roll(img, 13 * i, axis=1), **opts)), i
 
 
+def test_concurrent_host_threads(native):
+    """Calls from several host threads at once (the per-device pool and the
+    upload ring are shared): pinned inputs large enough for the ring, small
+    pageable inputs and device buffers, each result equal to the same call
+    made alone."""
+    import threading
+    import torch
+    lib = native.load_library()
+    jobs = []
+    for i in range(12):
+        if i % 3 == 0:
+            img = _texture(1031, 2048, seed=300 + i)                     # 8 MiB pinned -> ring
+            opts = dict(block_dim=6, has_alpha=True, srgb=True, border=1)
+        elif i % 3 == 1:
+            img = _texture(57 + i, 91, seed=300 + i)                     # small, pageable
+            opts = dict(block_dim=4, has_alpha=False)
+        else:
+            img = _texture(300, 257, seed=300 + i)                       # device pointers
+            opts = dict(block_dim=4, has_alpha=True, quality=1)
+        jobs.append((i, img, opts, native.encode(img, **opts)))
+    torch.cuda.synchronize()
+    results = {}
+    errors = []
+
+    def worker(part):
+        try:
+            torch.cuda.set_device(0)
+            for i, img, opts, _ in part:
+                h, w = img.shape[:2]
+                if i % 3 == 0:
+                    src = torch.from_numpy(img).pin_memory()
+                    dst = torch.zeros(encoded_shape(w, h, opts["block_dim"]), dtype=torch.uint8).pin_memory()
+                    o = native.make_opts(memory=native.Memory.HOST, **opts)
+                    st = lib.astc_encode_gpu(src.data_ptr(), w, h, ctypes.byref(o), dst.data_ptr())
+                    results[i] = (st, dst.numpy().copy())
+                elif i % 3 == 1:
+                    results[i] = (0, native.encode(img, **opts))
+                else:
+                    d_in = torch.from_numpy(img).cuda()
+                    d_out = torch.empty(encoded_shape(w, h, opts["block_dim"]), dtype=torch.uint8, device="cuda")
+                    native.encode_device(d_in.data_ptr(), w, h, d_out.data_ptr(), **opts)
+                    results[i] = (0, d_out.cpu().numpy())
+        except Exception as e:                      # noqa: BLE001 -- reported below
+            errors.append(repr(e))
+
+    def encoded_shape(w, h, dim):
+        return (((w + dim - 1) // dim) * ((h + dim - 1) // dim), 16)
+
+    threads = [threading.Thread(target=worker, args=(jobs[k::4],)) for k in range(4)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert not errors, errors
+    for i, _, _, want in jobs:
+        st, got = results[i]
+        assert st == 0 and np.array_equal(got, want), i
+
+
 def test_server_with_pinned_requests(native):
     import torch
     imgs = [_texture(97 + 13 * i, 61 + 7 * i, seed=i) for i in range(12)]
