@@ -332,6 +332,7 @@ def test_concurrent_host_threads(native):
                 else:
                     d_in = torch.from_numpy(img).cuda()
                     d_out = torch.empty(encoded_shape(w, h, opts["block_dim"]), dtype=torch.uint8, device="cuda")
+                    torch.cuda.synchronize()        # the library's own stream does not order after torch's
                     native.encode_device(d_in.data_ptr(), w, h, d_out.data_ptr(), **opts)
                     results[i] = (0, d_out.cpu().numpy())
         except Exception as e:                      # noqa: BLE001 -- reported below
