@@ -100,7 +100,10 @@ astc_status pool_for_current(DevicePool** out, int* dev_out) {
 
 astc_status pool_init_locked(DevicePool& p, int dev) {
     if (p.ready) return ASTC_OK;
-    cudaError_t e = cudaStreamCreateWithFlags(&p.stream, cudaStreamNonBlocking);
+    // a blocking stream: calls without a stream of their own are ordered after
+    // earlier work on the legacy default stream (where callers usually filled
+    // their device buffers)
+    cudaError_t e = cudaStreamCreate(&p.stream);
     if (e != cudaSuccess) return cuda_error(e, "cudaStreamCreateWithFlags");
     (void)dev;
     p.ready = true;

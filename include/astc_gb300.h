@@ -113,9 +113,10 @@ typedef struct astc_opts {
     int precision;   /* astc_precision                                     */
     int memory;      /* astc_memory: where `rgba8` and `out` live          */
     void* stream;    /* cudaStream_t to run on asynchronously; NULL = the
-                        library's own stream, and the call returns when
-                        the result is in `out` (for asynchronous work on
-                        the legacy default stream pass cudaStreamLegacy,
+                        library's own stream (ordered after earlier work on
+                        the legacy default stream), and the call returns
+                        when the result is in `out` (for asynchronous work
+                        on the legacy default stream pass cudaStreamLegacy,
                         (void*)0x1, not NULL)                               */
     int axis;        /* astc_axis (FP32 only)                               */
     int quality;     /* astc_quality (FP32 only)                            */

@@ -124,6 +124,7 @@ def test_device_pointer_api_and_pitch(native, oracle):
     wide = torch.zeros((96, 128, 4), dtype=torch.uint8, device="cuda")
     wide[:, :80] = dev
     out.zero_()
+    torch.cuda.synchronize()        # without a stream the library runs on its own stream
     native.encode_device(wide.data_ptr(), 80, 96, out.data_ptr(), block_dim=4, has_alpha=True,
                          row_pitch=128 * 4)
     assert np.array_equal(out.cpu().numpy(), want)
@@ -131,6 +132,7 @@ def test_device_pointer_api_and_pitch(native, oracle):
     odd = torch.zeros((96, 81, 4), dtype=torch.uint8, device="cuda")
     odd[:, :80] = dev
     out.zero_()
+    torch.cuda.synchronize()
     native.encode_device(odd.data_ptr(), 80, 96, out.data_ptr(), block_dim=4, has_alpha=True,
                          row_pitch=81 * 4)
     assert np.array_equal(out.cpu().numpy(), want)

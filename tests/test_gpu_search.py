@@ -101,6 +101,7 @@ def test_device_pointer_path(native, oracle):
     want = oracle.encode(img, block_dim=6, has_alpha=True, quality=1, axis=1)
     dev = torch.from_numpy(img).cuda()
     out = torch.empty((len(want), 16), dtype=torch.uint8, device="cuda")
+    torch.cuda.synchronize()        # without a stream the library runs on its own stream
     native.encode_device(dev.data_ptr(), 80, 96, out.data_ptr(), block_dim=6, has_alpha=True,
                          quality=1, axis=1)
     assert np.array_equal(out.cpu().numpy(), want)
