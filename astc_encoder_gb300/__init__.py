@@ -169,6 +169,9 @@ def load_library() -> ctypes.CDLL:
     lib.astc_batch_encode.argtypes = [ctypes.c_void_p, ctypes.POINTER(BatchItem), ctypes.c_int,
                                       ctypes.c_int, ctypes.c_void_p]
     lib.astc_batch_encode.restype = ctypes.c_int
+    lib.astc_batch_encode_quality.argtypes = [ctypes.c_void_p, ctypes.POINTER(BatchItem), ctypes.c_int,
+                                              ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
+    lib.astc_batch_encode_quality.restype = ctypes.c_int
     lib.astc_batch_destroy.argtypes = [ctypes.c_void_p]
     lib.astc_batch_destroy.restype = ctypes.c_int
     lib.astc_mip_levels.argtypes = [ctypes.c_int, ctypes.c_int]
@@ -216,7 +219,7 @@ def device_caps() -> dict:
 class ServerConfig(ctypes.Structure):
     """``astc_server_config`` of include/astc_gb300.h."""
     _fields_ = [("pool_bytes", ctypes.c_size_t), ("max_batch", ctypes.c_int), ("inflight", ctypes.c_int),
-                ("precision", ctypes.c_int), ("mode", ctypes.c_int)]
+                ("precision", ctypes.c_int), ("mode", ctypes.c_int), ("quality", ctypes.c_int)]
 
 
 class Request(ctypes.Structure):
@@ -246,9 +249,9 @@ class Server:
     """Continuous-batching request server (astc_server_*) over host buffers."""
 
     def __init__(self, pool_bytes: int = 2 << 30, max_batch: int = 256, inflight: int = 3,
-                 precision: int = Precision.FP32, mode: int = SERVE_BATCHED):
+                 precision: int = Precision.FP32, mode: int = SERVE_BATCHED, quality: int = Quality.FAST):
         self._lib = load_library()
-        cfg = ServerConfig(pool_bytes, max_batch, inflight, int(precision), int(mode))
+        cfg = ServerConfig(pool_bytes, max_batch, inflight, int(precision), int(mode), int(quality))
         h = ctypes.c_void_p()
         _check(self._lib.astc_server_create(ctypes.byref(cfg), ctypes.byref(h)))
         self._h = h
@@ -320,14 +323,19 @@ class Batch:
         _check(self._lib.astc_batch_create(max_textures, max_blocks, ctypes.byref(h)))
         self._h = h
 
-    def encode(self, items: list[dict], precision: int = Precision.FP32, stream: int | None = None) -> None:
+    def encode(self, items: list[dict], precision: int = Precision.FP32, stream: int | None = None,
+               quality: int = Quality.FAST) -> None:
         arr = (BatchItem * max(1, len(items)))()
         for i, it in enumerate(items):
             arr[i] = BatchItem(it["rgba8"], it.get("row_pitch", 0), it["width"], it["height"],
                                it.get("block_dim", 4), int(it.get("has_alpha", False)),
                                int(it.get("is_normal", False)), int(it.get("srgb", False)),
                                int(it.get("border", Border.ZERO)), it["out"])
-        _check(self._lib.astc_batch_encode(self._h, arr, len(items), int(precision), stream or None))
+        if quality == Quality.FAST:
+            _check(self._lib.astc_batch_encode(self._h, arr, len(items), int(precision), stream or None))
+        else:
+            _check(self._lib.astc_batch_encode_quality(self._h, arr, len(items), int(precision), int(quality),
+                                                       stream or None))
 
     def close(self) -> None:
         if self._h:

@@ -186,6 +186,29 @@ astc_status check_ptr(astc_batch* b, const void* p, const char* what) {
     return ASTC_OK;
 }
 
+// Checks item i of a batch call and adds its block count to *blocks.
+astc_status validate_item(astc_batch* b, const astc_batch_item& t, int i, long long* blocks) {
+    if (t.block_dim != 4 && t.block_dim != 6)
+        return set_error(ASTC_ERR_INVALID_ARG, "item " + std::to_string(i) + ": block_dim must be 4 or 6");
+    if (t.width <= 0 || t.height <= 0 || t.width > 0xFFFFFF || t.height > 0xFFFFFF)
+        return set_error(ASTC_ERR_INVALID_ARG, "item " + std::to_string(i) + ": bad size");
+    if (t.border != ASTC_BORDER_ZERO && t.border != ASTC_BORDER_CLAMP)
+        return set_error(ASTC_ERR_INVALID_ARG, "item " + std::to_string(i) + ": bad border");
+    const size_t pitch = t.row_pitch ? t.row_pitch : (size_t)t.width * 4;
+    if (pitch < (size_t)t.width * 4 || pitch % 4)
+        return set_error(ASTC_ERR_INVALID_ARG, "item " + std::to_string(i) + ": bad row_pitch");
+    if (!t.rgba8 || !t.out || reinterpret_cast<uintptr_t>(t.rgba8) % 4 || reinterpret_cast<uintptr_t>(t.out) % 16)
+        return set_error(ASTC_ERR_INVALID_ARG,
+                         "item " + std::to_string(i) + ": rgba8 must be 4-byte and out 16-byte aligned");
+    astc_status st;
+    if ((st = check_ptr(b, t.rgba8, "rgba8")) != ASTC_OK) return st;
+    if ((st = check_ptr(b, t.out, "out")) != ASTC_OK) return st;
+    const long long nb = (long long)blocks_x(t.width, t.block_dim) * blocks_y(t.height, t.block_dim);
+    if (nb > (1LL << 31)) return set_error(ASTC_ERR_INVALID_ARG, "texture has more than 2^31 blocks");
+    *blocks += nb;
+    return ASTC_OK;
+}
+
 // Captures one persistent kernel per format in `mask` (the descriptor upload
 // is issued before the launch with the exact sizes of each batch).
 astc_status build_graph(astc_batch* b, unsigned mask, int prec, cudaGraphExec_t* out) {
@@ -270,27 +293,11 @@ astc_status astc_batch_encode(astc_batch* b, const astc_batch_item* in, int coun
         int per_fmt[kFormats] = {};
         for (int i = 0; i < count; ++i) {
             const astc_batch_item& t = in[i];
-            if (t.block_dim != 4 && t.block_dim != 6)
-                return set_error(ASTC_ERR_INVALID_ARG, "item " + std::to_string(i) + ": block_dim must be 4 or 6");
-            if (t.width <= 0 || t.height <= 0 || t.width > 0xFFFFFF || t.height > 0xFFFFFF)
-                return set_error(ASTC_ERR_INVALID_ARG, "item " + std::to_string(i) + ": bad size");
-            if (t.border != ASTC_BORDER_ZERO && t.border != ASTC_BORDER_CLAMP)
-                return set_error(ASTC_ERR_INVALID_ARG, "item " + std::to_string(i) + ": bad border");
-            const size_t pitch = t.row_pitch ? t.row_pitch : (size_t)t.width * 4;
-            if (pitch < (size_t)t.width * 4 || pitch % 4)
-                return set_error(ASTC_ERR_INVALID_ARG, "item " + std::to_string(i) + ": bad row_pitch");
-            if (!t.rgba8 || !t.out || reinterpret_cast<uintptr_t>(t.rgba8) % 4 ||
-                reinterpret_cast<uintptr_t>(t.out) % 16)
-                return set_error(ASTC_ERR_INVALID_ARG,
-                                 "item " + std::to_string(i) + ": rgba8 must be 4-byte and out 16-byte aligned");
-            astc_status st;
-            if ((st = check_ptr(b, t.rgba8, "rgba8")) != ASTC_OK) return st;
-            if ((st = check_ptr(b, t.out, "out")) != ASTC_OK) return st;
-            const long long nb = (long long)blocks_x(t.width, t.block_dim) * blocks_y(t.height, t.block_dim);
-            if (nb > (1LL << 31)) return set_error(ASTC_ERR_INVALID_ARG, "texture has more than 2^31 blocks");
-            blocks += nb;
+            const long long before = blocks;
+            const astc_status st = validate_item(b, t, i, &blocks);
+            if (st != ASTC_OK) return st;
             per_fmt[format_index(t.block_dim, t.has_alpha, t.is_normal, t.srgb)] +=
-                (int)((nb + kBatchThreads - 1) / kBatchThreads);
+                (int)((blocks - before + kBatchThreads - 1) / kBatchThreads);
         }
         if (blocks > b->max_blocks) return set_error(ASTC_ERR_INVALID_ARG, "batch exceeds max_blocks");
         // the previous batch's upload must have left the pinned staging buffer
@@ -368,6 +375,55 @@ astc_status astc_batch_encode(astc_batch* b, const astc_batch_item* in, int coun
         return ASTC_OK;
     } catch (const std::bad_alloc&) {
         return set_error(ASTC_ERR_OUT_OF_MEMORY, "host allocation failed");
+    } catch (...) {
+        return set_error(ASTC_ERR_CUDA, "unexpected exception");
+    }
+}
+
+astc_status astc_batch_encode_quality(astc_batch* b, const astc_batch_item* in, int count, int precision,
+                                      int quality, void* stream) {
+    if (quality == ASTC_QUALITY_FAST) return astc_batch_encode(b, in, count, precision, stream);
+    if (!b || (!in && count > 0)) return set_error(ASTC_ERR_INVALID_ARG, "NULL argument");
+    if (quality < ASTC_QUALITY_FAST || quality > ASTC_QUALITY_PARTITIONS)
+        return set_error(ASTC_ERR_INVALID_ARG, "bad quality");
+    if (precision != ASTC_PRECISION_FP32)
+        return set_error(ASTC_ERR_UNSUPPORTED, "the quality modes are FP32 only");
+    if (count < 0 || count > b->max_items)
+        return set_error(ASTC_ERR_INVALID_ARG, "count exceeds the batch's max_textures");
+    try {
+        std::lock_guard<std::mutex> lk(b->mu);
+        int dev = 0;
+        cudaError_t e = cudaGetDevice(&dev);
+        if (e != cudaSuccess) return cuda_error(e, "cudaGetDevice");
+        if (dev != b->device) return set_error(ASTC_ERR_INVALID_ARG, "batch was created on another device");
+        long long blocks = 0;
+        for (int i = 0; i < count; ++i) {
+            const astc_status st = validate_item(b, in[i], i, &blocks);
+            if (st != ASTC_OK) return st;
+        }
+        if (blocks > b->max_blocks) return set_error(ASTC_ERR_INVALID_ARG, "batch exceeds max_blocks");
+        // one quality-mode kernel per texture on the stream (these kernels run
+        // for tens of microseconds or more, so launches do not dominate)
+        cudaStream_t s = static_cast<cudaStream_t>(stream);
+        for (int i = 0; i < count; ++i) {
+            const astc_batch_item& t = in[i];
+            EncodeJob j;
+            j.in = t.rgba8;
+            j.pitch = t.row_pitch ? t.row_pitch : (size_t)t.width * 4;
+            j.width = t.width;
+            j.height = t.height;
+            j.block_dim = t.block_dim;
+            j.has_alpha = t.has_alpha;
+            j.is_normal = t.is_normal;
+            j.srgb = t.srgb;
+            j.border = t.border;
+            j.precision = ASTC_PRECISION_FP32;
+            j.quality = quality;
+            j.out = t.out;
+            if ((e = launch_encode_search(j, s)) != cudaSuccess) return cuda_error(e, "quality kernel launch");
+        }
+        if (!stream && (e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_error(e, "batch encode");
+        return ASTC_OK;
     } catch (...) {
         return set_error(ASTC_ERR_CUDA, "unexpected exception");
     }

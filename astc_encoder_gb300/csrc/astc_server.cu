@@ -170,8 +170,8 @@ cudaError_t launch_slot(astc_server* s, Slot& slot) {
         items.push_back(it);
     }
     if (s->cfg.mode == ASTC_SERVE_BATCHED) {
-        const astc_status st = astc_batch_encode(slot.batch, items.data(), (int)items.size(), s->cfg.precision,
-                                                 slot.stream);
+        const astc_status st = astc_batch_encode_quality(slot.batch, items.data(), (int)items.size(),
+                                                         s->cfg.precision, s->cfg.quality, slot.stream);
         if (st != ASTC_OK) return cudaErrorUnknown;
     } else {
         for (const astc_batch_item& it : items) {
@@ -186,9 +186,11 @@ cudaError_t launch_slot(astc_server* s, Slot& slot) {
             j.srgb = it.srgb;
             j.border = it.border;
             j.precision = s->cfg.precision;
+            j.quality = s->cfg.quality;
             j.out = it.out;
-            e = s->cfg.precision == ASTC_PRECISION_HALF2 ? launch_encode_h2(j, slot.stream)
-                                                         : launch_encode(j, slot.stream);
+            e = s->cfg.quality != ASTC_QUALITY_FAST           ? launch_encode_search(j, slot.stream)
+                : s->cfg.precision == ASTC_PRECISION_HALF2 ? launch_encode_h2(j, slot.stream)
+                                                           : launch_encode(j, slot.stream);
             if (e != cudaSuccess) return e;
         }
     }
@@ -285,6 +287,10 @@ astc_status astc_server_create(const astc_server_config* cfg, astc_server** out)
         return set_error(ASTC_ERR_INVALID_ARG, "bad precision");
     if (cfg->mode != ASTC_SERVE_BATCHED && cfg->mode != ASTC_SERVE_PER_REQUEST)
         return set_error(ASTC_ERR_INVALID_ARG, "bad mode");
+    if (cfg->quality < ASTC_QUALITY_FAST || cfg->quality > ASTC_QUALITY_PARTITIONS)
+        return set_error(ASTC_ERR_INVALID_ARG, "bad quality");
+    if (cfg->quality != ASTC_QUALITY_FAST && cfg->precision != ASTC_PRECISION_FP32)
+        return set_error(ASTC_ERR_UNSUPPORTED, "the quality modes are FP32 only");
     std::unique_ptr<astc_server> s(new (std::nothrow) astc_server());
     if (!s) return set_error(ASTC_ERR_OUT_OF_MEMORY, "host allocation failed");
     s->cfg = *cfg;

@@ -173,6 +173,12 @@ astc_status astc_batch_create(int max_textures, long long max_blocks, astc_batch
  * it reuses the staging buffer.  Not thread-safe per handle across streams. */
 astc_status astc_batch_encode(astc_batch* batch, const astc_batch_item* items, int count,
                               int precision, void* stream);
+/* The same with a quality mode (astc_quality).  ASTC_QUALITY_FAST is
+ * astc_batch_encode; the search modes (FP32 only) launch one quality-mode
+ * kernel per item on `stream`; every texture's blocks equal its
+ * astc_encode_gpu result with that quality. */
+astc_status astc_batch_encode_quality(astc_batch* batch, const astc_batch_item* items, int count,
+                                      int precision, int quality, void* stream);
 astc_status astc_batch_destroy(astc_batch* batch);
 
 /* ---- serving: continuous batching of single-texture requests -----------
@@ -198,6 +204,8 @@ typedef struct astc_server_config {
     int inflight;        /* slots (batches or requests) in flight, 1..16        */
     int precision;       /* astc_precision                                      */
     int mode;            /* astc_serve_mode                                     */
+    int quality;         /* astc_quality of every request (FP32 for the search
+                            modes)                                              */
 } astc_server_config;
 
 typedef struct astc_request {

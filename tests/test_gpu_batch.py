@@ -66,6 +66,24 @@ def test_batch_equals_alone_all_formats(native, oracle, precision):
                 assert np.array_equal(got, oracle.encode(img, **opts)), opts
 
 
+@pytest.mark.parametrize("quality", [1, 3])
+def test_batch_quality_modes(native, oracle, quality):
+    """astc_batch_encode_quality: every texture's blocks equal its
+    astc_encode_gpu result with the same quality (and the oracle's)."""
+    import torch
+    cases = _batch_case(torch, seed=10 + quality)
+    torch.cuda.synchronize()
+    with native.Batch(64, 1 << 20) as b:
+        b.encode(_items(cases), quality=quality)
+        for img, opts, dev, out in cases:
+            got = out.cpu().numpy()
+            assert np.array_equal(got, native.encode(img, quality=quality, **opts)), opts
+            assert np.array_equal(got, oracle.encode(img, quality=quality, **opts)), opts
+        with pytest.raises(native.AstcError) as e:
+            b.encode(_items(cases), precision=1, quality=quality)
+        assert e.value.status == native.Status.UNSUPPORTED
+
+
 def test_batch_graph_reuse_and_many_mips(native, oracle):
     import torch
     stream = torch.cuda.Stream()

@@ -66,6 +66,22 @@ def test_alone_equals_in_the_mix(native, oracle, mode, precision):
         assert np.array_equal(alone, oracle.encode(probe.img, **probe.opts))
 
 
+@pytest.mark.parametrize("mode", [0, 1])
+def test_server_quality_mode(native, mode):
+    """A THOROUGH server returns each request's astc_encode_gpu blocks with
+    that quality, batched or per request; HALF2 with it is refused."""
+    with native.Server(pool_bytes=32 << 20, max_batch=8, inflight=2, mode=mode, quality=2) as srv:
+        mix = _mix(native, 16, seed=40 + mode, max_side=120)
+        tickets = [srv.submit(r.req) for r in mix]
+        for t in tickets:
+            srv.wait(t)
+    for r in mix:
+        assert np.array_equal(r.out, native.encode(r.img, quality=2, **r.opts)), r.opts
+    with pytest.raises(native.AstcError) as e:
+        native.Server(pool_bytes=1 << 24, precision=1, quality=2)
+    assert e.value.status == native.Status.UNSUPPORTED
+
+
 def test_admission_by_memory_with_a_small_pool(native):
     # a 2 MiB pool holds only a few of these requests at a time; the rest wait
     mix = _mix(native, 40, seed=11, max_side=400)
