@@ -144,9 +144,47 @@ __device__ __forceinline__ void snap_two(int slot, const uint32_t a0[4], const u
     }
 }
 
+// Integer projections (UNORM input, where every fit-space texel value is an
+// integer): for a texel's packed bytes t (the target word: blue and alpha
+// 255 for normal maps, alpha 0 for RGB blocks, whose endpoint alpha
+// difference is 0), dot(t - E0, E1 - E0) = t.dpos - t.dneg - E0.d with the
+// difference split into its positive and negative parts, exactly; the FP32
+// dot product of the same integers is exact too (below 2^24), so the two are
+// equal.
+struct IntLine {
+    uint32_t dpos, dneg;   // max(d, 0), max(-d, 0) per channel, packed bytes
+    int e0d;               // E0 . d
+    float r;               // 1 / |d|^2 (0 for equal endpoints)
+    bool flat;
+};
+
+__device__ __forceinline__ IntLine int_line(const int E0[4], const int E1[4]) {
+    IntLine l;
+    l.dpos = 0; l.dneg = 0; l.e0d = 0;
+    int dd = 0;
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        const int d = E1[c] - E0[c];
+        l.dpos |= (uint32_t)(d > 0 ? d : 0) << (8 * c);
+        l.dneg |= (uint32_t)(d < 0 ? -d : 0) << (8 * c);
+        l.e0d += E0[c] * d;
+        dd += d * d;
+    }
+    l.flat = dd == 0;
+    l.r = l.flat ? 0.0f : __frcp_rn((float)dd);
+    return l;
+}
+
+__device__ __forceinline__ float int_weight(uint32_t t, uint32_t dpos, uint32_t dneg, int e0d, float r) {
+    const int x = (int)__dp4a(t, dpos, 0u) - (int)__dp4a(t, dneg, 0u) - e0d;
+    return fminf(fmaxf(__fmul_rn((float)x, r), 0.0f), 1.0f);
+}
+
 // Grid weights (value-order indices q) of a two-partition candidate: texel
-// weights on the texel's own partition; 4x4 rounds them directly, 6x6 keeps
-// them in `tws` ([texel][thread] floats) and samples the shader's 2x2 taps.
+// weights on the texel's own partition (integer projections for UNORM input,
+// equal to the FP32 ones there; on GB300 this trims the normal-map
+// candidates by a few per cent); 4x4 rounds them directly, 6x6 keeps them in
+// `tws` ([texel][thread] floats) and samples the shader's 2x2 taps.
 // Each partition's values are held in named registers and chosen with the
 // texel's partition bit (an array indexed by it would live in local memory).
 struct PartLine {
@@ -176,20 +214,39 @@ __device__ __forceinline__ float part_weight_sel(const float4 t, bool p1, const 
     return flat ? 0.0f : w;
 }
 
-template <int DIM, class S, class TW>
-__device__ __forceinline__ void two_partition_weights(const S& st, uint64_t sel1, const int E0[2][4],
-                                                      const int E1[2][4], float R, TW& tws, uint32_t (&q)[16]) {
-    const PartLine la = part_line(E0[0], E1[0]), lb = part_line(E0[1], E1[1]);
+template <int DIM, bool SRGB, class S, class TW>
+__device__ __forceinline__ void two_partition_weights(const S& st, const uint32_t (&tw)[DIM * DIM], uint64_t sel1,
+                                                      const int E0[2][4], const int E1[2][4], float R, TW& tws,
+                                                      uint32_t (&q)[16]) {
+    // texel weight k: integer projections for UNORM input, FP32 for sRGB
+    auto weight = [&](int k, bool p1, const auto& la, const auto& lb) -> float {
+        if constexpr (SRGB) {
+            return part_weight_sel(st.get(k), p1, la, lb);
+        } else {
+            const float w = int_weight(tw[k], p1 ? lb.dpos : la.dpos, p1 ? lb.dneg : la.dneg, p1 ? lb.e0d : la.e0d,
+                                       p1 ? lb.r : la.r);
+            return (p1 ? lb.flat : la.flat) ? 0.0f : w;
+        }
+    };
+    using Line = typename std::conditional<SRGB, PartLine, IntLine>::type;
+    Line la, lb;
+    if constexpr (SRGB) {
+        la = part_line(E0[0], E1[0]);
+        lb = part_line(E0[1], E1[1]);
+    } else {
+        la = int_line(E0[0], E1[0]);
+        lb = int_line(E0[1], E1[1]);
+    }
     if constexpr (DIM == 4) {
 #pragma unroll
         for (int k = 0; k < 16; ++k) {
-            const float w = part_weight_sel(st.get(k), (sel1 >> k) & 1, la, lb);
+            const float w = weight(k, (sel1 >> k) & 1, la, lb);
             const uint32_t v = rint_u32(__fmul_rn(w, R));
             q[k] = v < (uint32_t)R ? v : (uint32_t)R;
         }
     } else {
 #pragma unroll
-        for (int k = 0; k < 36; ++k) tws.put(k, part_weight_sel(st.get(k), (sel1 >> k) & 1, la, lb));
+        for (int k = 0; k < 36; ++k) tws.put(k, weight(k, (sel1 >> k) & 1, la, lb));
 #pragma unroll
         for (int g = 0; g < 16; ++g) {
             const int i0 = grid_tap0(g);
@@ -302,7 +359,7 @@ __device__ __forceinline__ uint4 two_partition_block(const S& st, const uint32_t
         const int cq = pm.cq[wq];
         if (cq < 0) continue;
         snap_two<ALPHA>(pm.slot[wq], a0, a1, b0, b1, pm, sym0, sym1, E0, E1);
-        two_partition_weights<DIM>(st, sel1, E0, E1, sm.wmax[wq], tws, q);
+        two_partition_weights<DIM, SRGB>(st, tw, sel1, E0, E1, sm.wmax[wq], tws, q);
         if (!final_pass) {
 #pragma unroll
             for (int g = 0; g < 16; ++g) W[g] = sm.wval[wq][q[g]];
