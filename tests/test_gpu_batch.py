@@ -4,7 +4,7 @@ GPU mip chains.
 * A texture's blocks are identical whether it is encoded alone (plain kernel,
   astc_encode_gpu) or inside a batch of textures of other sizes and formats,
   for both precisions; FP32 is also identical to the oracle.
-* HALF2 is held to the benchmark spec's quality gate: PSNR at most 0.05 dB below
+* HALF2 is held to its quality gate: PSNR at most 0.05 dB below
   the FP64 oracle's on the same texture (decoded with the spec decoder, in
   the space the encoder fits).
 """

@@ -2,7 +2,7 @@
 
 Bar: every block bit-identical to the oracle (the kernels follow the oracle's
 FP32 model operation by operation; the integer stages are exact by
-construction).  The acceptance floor from the benchmark spec (>= 99.9% identical
+construction).  The acceptance floor of the FP32 path (>= 99.9% identical
 blocks, PSNR within 0.01 dB) is also asserted separately so a regression
 shows up as the right failure.
 """
