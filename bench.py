@@ -275,6 +275,23 @@ def _time_launches(torch, native, texs, outs, spec, steps):
     return sum(per_step) / max(1, launches), per_step, launches
 
 
+# DRAM bytes (read + write) of one launch of the production kernel, from the
+# ncu capture summarised in profiles/ (the capture's command is given there):
+# (workload, precision, texel store) -> bytes, capture
+_NCU_TRAFFIC = {
+    ("6x6_rgba_srgb_2048", 0, 2): (16_834_816, "astc_encode_blocks_fp32_6x6_rgba_srgb_2048.md: "
+                                               "16.83 MB read, 0 B written (blocks still in L2)"),
+}
+
+
+def _traffic(workload: str, prec: int, tuned) -> dict:
+    key = (workload, prec, getattr(tuned, "store", None))
+    if key not in _NCU_TRAFFIC:
+        return {"traffic": None, "traffic_source": "no ncu capture of this kernel variant"}
+    b, src = _NCU_TRAFFIC[key]
+    return {"traffic": b, "traffic_unit": "bytes per launch", "traffic_source": "profiles/" + src}
+
+
 def _psnr_blocks(native, blocks: np.ndarray, tex: np.ndarray, spec: dict) -> float:
     """Decoded PSNR in the space the encoder fits (GPU decoder, GPU SSE)."""
     h, w = tex.shape[:2]
@@ -691,7 +708,8 @@ def run_ours(args) -> None:
         "roofline": {"bound": "hbm", "kernel": kernel, "achieved": achieved_gbs,
                      "peak": hbm_peak, "unit": "GB/s",
                      "frac": (achieved_gbs / hbm_peak) if hbm_peak else None,
-                     "traffic": None, "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)",
+                     **_traffic(args.workload, prec, tuned),
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)",
                      "alg_bytes_per_launch": alg_bytes, "mean_launch_us": mean_launch_s * 1e6},
         "roofline_fp32": {"bound": "fp32_issue", "achieved": achieved_tf, "peak": fp32_peak,
                           "unit": "TFLOP/s", "frac": achieved_tf / fp32_peak,
