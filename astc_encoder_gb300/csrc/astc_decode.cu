@@ -51,9 +51,24 @@ struct Bits {
     }
 };
 
-__device__ void ise_decode(const DecodeTables& T, int quant, int count, const Bits& b, int pos,
+// Bits at or past the end of the sequence (pos + its ISE length) read as
+// zero: the last trit or quint group is stored cut to the sequence's length,
+// and whatever follows in the block (endpoints, a dual-plane selector) is not
+// part of it.
+struct BoundedBits {
+    const Bits& b;
+    int end;
+    __device__ uint32_t read(int pos, int count) const {
+        if (pos >= end) return 0;
+        const int n = pos + count > end ? end - pos : count;
+        return b.read(pos, n);
+    }
+};
+
+__device__ void ise_decode(const DecodeTables& T, int quant, int count, const Bits& bits, int pos,
                            uint8_t* out) {
     const RangeShape s = range_shape(quant);
+    const BoundedBits b{bits, pos + ise_bit_count(quant, count)};
     if (s.trits) {
         for (int g = 0; g < count; g += 5) {
             uint32_t m[5], tb = 0;

@@ -1,0 +1,210 @@
+// astc_pipeline_dual.cuh -- dual-plane candidates of the FP32 encoder's
+// ASTC_QUALITY_THOROUGH and ASTC_QUALITY_PARTITIONS modes.  The reference
+// shader writes the dual-plane bit of its block mode as a constant 0
+// (assemble_blockmode, ASTC_Encode.hlsl:446-473).
+//
+// For each channel pc that varies over the block, plane 2 carries pc alone:
+// the other channels are fitted on the axis the shader's power iteration finds
+// for the block's covariance with pc's row and column zeroed (the PCA of the
+// block with pc held constant; the axis's pc component is then exactly 0, so
+// pc takes no part in find_min_max's projections), pc's endpoints are its
+// minimum and maximum.  Every weight range whose 32 weights (plane 1, plane 2
+// per grid point; 24..96 bits) leave a legal endpoint range after the 2-bit
+// plane selector is scored by the exact decode, each channel taking its
+// plane's weight.  Plane-1 weights project the grid colours on the decoded
+// endpoints without pc, plane-2 weights are (c_pc - E0_pc) / (E1_pc - E0_pc),
+// both clamped to [0, 1] and rounded to the range.  The oracle's dual_plane
+// follows the same steps.
+#pragma once
+#include "astc_pipeline_search.cuh"
+
+namespace astc {
+
+// Per-CTA copies of the dual-plane endpoint tables (shared memory).
+struct DualSmem {
+    uint16_t color[8][256];
+    int8_t cq[12];       // weight range -> endpoint range (-1: illegal)
+    int8_t slot[12];
+};
+
+__device__ __forceinline__ float comp(const float4 t, int c) {
+    return c == 0 ? t.x : c == 1 ? t.y : c == 2 ? t.z : t.w;
+}
+
+// The squared error of a dual-plane decode (channel pc on plane-2 weights).
+// P[g]: grid point g's unquantised plane-1 weight in the low half, its plane-2
+// weight in the high half (each 0..64, so the 6x6 infill sums, at most
+// 64 * 16, stay inside their halves and are computed on both at once).
+template <int DIM, bool ALPHA, bool SRGB>
+__device__ __forceinline__ uint32_t eval_dual(const uint32_t (&tw)[DIM * DIM], uint32_t t2, int pc, const int E0[4],
+                                              const int E1[4], const uint32_t (&P)[16]) {
+    constexpr int NCH = ALPHA ? 4 : 3;
+    int base[NCH], delta[NCH];
+#pragma unroll
+    for (int c = 0; c < NCH; ++c) {
+        const int c0 = SRGB ? ((E0[c] << 8) | 0x80) : E0[c] * 257;
+        const int c1 = SRGB ? ((E1[c] << 8) | 0x80) : E1[c] * 257;
+        base[c] = 4 * (64 * c0 + 32);
+        delta[c] = 4 * (c1 - c0);
+    }
+    uint32_t dd = 0, dt = 0;
+#pragma unroll
+    for (int k = 0; k < DIM * DIM; ++k) {
+        int w1, w2;
+        if constexpr (DIM == 6) {
+            const Infill f = infill_6x6(k);
+            uint32_t a = P[f.v0] * (uint32_t)f.w00 + 0x00080008u;
+            if (f.w01) a += P[f.v0 + 1] * (uint32_t)f.w01;
+            if (f.w10) a += P[f.v0 + 4] * (uint32_t)f.w10;
+            if (f.w11) a += P[f.v0 + 5] * (uint32_t)f.w11;
+            w1 = (int)((a & 0xFFFFu) >> 4);
+            w2 = (int)(a >> 20);
+        } else {
+            w1 = (int)(P[k] & 0xFFFFu);
+            w2 = (int)(P[k] >> 16);
+        }
+        uint32_t v[NCH];
+#pragma unroll
+        for (int c = 0; c < NCH; ++c) v[c] = (uint32_t)(base[c] + delta[c] * (c == pc ? w2 : w1));
+        uint32_t dec = __byte_perm(v[0], v[1], 0x3362u);
+        dec = __byte_perm(dec, v[2], 0x3610u);
+        if constexpr (ALPHA) dec = __byte_perm(dec, v[3], 0x6210u);
+        dd = __dp4a(dec, dec, dd);
+        dt = __dp4a(dec, tw[k], dt);
+    }
+    return dd - 2u * dt + t2;
+}
+
+// One dual-plane block: mode with D (bit 10) set, CEM [16:13], endpoints from
+// bit 17, the plane selector right below the weights, 32 interleaved weights
+// bit-reversed from bit 127.
+template <bool ALPHA>
+__device__ __forceinline__ uint4 assemble_dual(int wq, int cq, int pc, const uint32_t (&ev)[ALPHA ? 8 : 6],
+                                               const uint32_t (&sw)[32], const SearchSmem& sm) {
+    const Bits128 ep = ise_encode<ALPHA ? 8 : 6>(cq, ev, sm.trits, sm.quints);
+    const Bits128 wt = ise_encode<32>(wq, sw, sm.trits, sm.quints);
+    const int sel = 128 - ise_bit_count(wq, 32) - 2;       // 32..102: never straddles the words
+    const uint64_t head = (uint64_t)blockmode_4x4_grid(wq) | (1ull << 10) | ((uint64_t)(ALPHA ? 12u : 8u) << 13);
+    uint64_t lo = head | (ep.lo << 17) | __brevll(wt.hi);
+    uint64_t hi = (ep.lo >> 47) | (ep.hi << 17) | __brevll(wt.lo);
+    if (sel < 64) lo |= (uint64_t)pc << sel;
+    else hi |= (uint64_t)pc << (sel - 64);
+    return make_uint4((uint32_t)lo, (uint32_t)(lo >> 32), (uint32_t)hi, (uint32_t)(hi >> 32));
+}
+
+// Dual-plane candidates of one block; returns `best` unless one decodes with
+// less error than best_err (which it then lowers).  st: the fit-space texels,
+// grid: the 16 grid-point colours, tw/t2: the scoring targets.
+template <int DIM, bool ALPHA, bool SRGB, class S, class G>
+__device__ __forceinline__ uint4 dual_plane_block(const S& st, const G& grid, const uint32_t (&tw)[DIM * DIM],
+                                                  uint32_t t2, uint32_t& best_err, uint4 best, const SearchSmem& sm,
+                                                  const DualSmem& ds) {
+    constexpr int N = DIM * DIM;
+    constexpr int NCH = ALPHA ? 4 : 3;
+    int found_pc = -1, found_wq = -1;
+    uint4 out = best;
+    // the block's mean and covariance, shared by every channel
+    const float4 m = block_mean<N>(st);
+    const Covariance cv = block_covariance<N>(st, m);
+    // every channel, then one more pass over the best (pc, range) to assemble it
+#pragma unroll 1
+    for (int it = 0; it <= NCH; ++it) {
+        const bool final_pass = it == NCH;
+        if (final_pass && found_pc < 0) break;
+        const int pc = final_pass ? found_pc : it;
+        float lo = 1e31f, hi = -1e31f;
+#pragma unroll
+        for (int k = 0; k < N; ++k) {
+            const float v = comp(st.get(k), pc);
+            lo = fminf(lo, v);
+            hi = fmaxf(hi, v);
+        }
+        if (lo == hi) continue;                    // a constant channel: nothing to split off
+        uint32_t q0[4], q1[4];
+        {
+            // entry (i, j) is zeroed when i or j is pc
+            const bool z0 = pc == 0, z1 = pc == 1, z2 = pc == 2, z3 = pc == 3;
+            const float4 v = power_iteration(z0 ? 0.0f : cv.c00, (z0 || z1) ? 0.0f : cv.c01,
+                                             (z0 || z2) ? 0.0f : cv.c02, (z0 || z3) ? 0.0f : cv.c03,
+                                             z1 ? 0.0f : cv.c11, (z1 || z2) ? 0.0f : cv.c12,
+                                             (z1 || z3) ? 0.0f : cv.c13, z2 ? 0.0f : cv.c22,
+                                             (z2 || z3) ? 0.0f : cv.c23, z3 ? 0.0f : cv.c33);
+            float e0[4], e1[4];
+            find_min_max<N, ALPHA>(st, m, v, e0, e1, q0, q1);
+        }
+        const uint32_t lq = rint_u32(lo), hq = rint_u32(hi);
+        q0[0] = pc == 0 ? lq : q0[0]; q0[1] = pc == 1 ? lq : q0[1]; q0[2] = pc == 2 ? lq : q0[2];
+        q0[3] = pc == 3 ? lq : q0[3];
+        q1[0] = pc == 0 ? hq : q1[0]; q1[1] = pc == 1 ? hq : q1[1]; q1[2] = pc == 2 ? hq : q1[2];
+        q1[3] = pc == 3 ? hq : q1[3];
+#pragma unroll 1
+        for (int wq = kQuant2; wq <= kQuant32; ++wq) {
+            if (final_pass && wq != found_wq) continue;
+            const int cq = ds.cq[wq];
+            if (cq < 0) continue;
+            int sym0[4], sym1[4], E0[4], E1[4];
+#pragma unroll
+            for (int c = 0; c < 4; ++c) { sym0[c] = 0; sym1[c] = 0; E0[c] = 255; E1[c] = 255; }
+#pragma unroll
+            for (int c = 0; c < NCH; ++c) {
+                if (cq == kQuant256) {
+                    sym0[c] = E0[c] = (int)q0[c];
+                    sym1[c] = E1[c] = (int)q1[c];
+                } else {
+                    const uint32_t a = ds.color[ds.slot[wq]][q0[c]], b = ds.color[ds.slot[wq]][q1[c]];
+                    sym0[c] = (int)(a & 0xFFu); E0[c] = (int)(a >> 8);
+                    sym1[c] = (int)(b & 0xFFu); E1[c] = (int)(b >> 8);
+                }
+            }
+            if (E1[0] + E1[1] + E1[2] < E0[0] + E0[1] + E0[2]) {
+#pragma unroll
+                for (int c = 0; c < 4; ++c) {
+                    int t = sym0[c]; sym0[c] = sym1[c]; sym1[c] = t;
+                    t = E0[c]; E0[c] = E1[c]; E1[c] = t;
+                }
+            }
+            float d[4], f[4];
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                f[c] = (float)E0[c];
+                d[c] = c == pc ? 0.0f : (float)(E1[c] - E0[c]);
+            }
+            const float dd = dot4(d[0], d[1], d[2], d[3], d[0], d[1], d[2], d[3]);
+            const float r = dd == 0.0f ? 0.0f : __frcp_rn(dd);
+            // selects, not E[pc]: a runtime index would put E0/E1 in local memory
+            const int e0p = pc == 0 ? E0[0] : pc == 1 ? E0[1] : pc == 2 ? E0[2] : E0[3];
+            const int e1p = pc == 0 ? E1[0] : pc == 1 ? E1[1] : pc == 2 ? E1[2] : E1[3];
+            const float dp = (float)(e1p - e0p);
+            const float rp = dp == 0.0f ? 0.0f : __frcp_rn(dp);
+            const float R = sm.wmax[wq];
+            // scoring passes: the weights' values; the final pass: their ISE symbols
+            const uint8_t* tab = final_pass ? sm.scramble[wq] : sm.wval[wq];
+            uint32_t P[16];
+#pragma unroll
+            for (int g = 0; g < 16; ++g) {
+                const float4 sg = grid.get(g);
+                const float x0 = __fsub_rn(sg.x, f[0]), x1 = __fsub_rn(sg.y, f[1]);
+                const float x2 = __fsub_rn(sg.z, f[2]), x3 = __fsub_rn(sg.w, f[3]);
+                const float w1 = fminf(fmaxf(__fmul_rn(dot4(x0, x1, x2, x3, d[0], d[1], d[2], d[3]), r), 0.0f), 1.0f);
+                const float xp = pc == 0 ? x0 : pc == 1 ? x1 : pc == 2 ? x2 : x3;
+                const float w2 = fminf(fmaxf(__fmul_rn(xp, rp), 0.0f), 1.0f);
+                P[g] = (uint32_t)tab[rint_u32(__fmul_rn(w1, R))] | ((uint32_t)tab[rint_u32(__fmul_rn(w2, R))] << 16);
+            }
+            if (!final_pass) {
+                const uint32_t err = eval_dual<DIM, ALPHA, SRGB>(tw, t2, pc, E0, E1, P);
+                if (err < best_err) { best_err = err; found_pc = pc; found_wq = wq; }
+                continue;
+            }
+            uint32_t ev[ALPHA ? 8 : 6];
+#pragma unroll
+            for (int c = 0; c < NCH; ++c) { ev[2 * c] = (uint32_t)sym0[c]; ev[2 * c + 1] = (uint32_t)sym1[c]; }
+            uint32_t sw[32];
+#pragma unroll
+            for (int g = 0; g < 16; ++g) { sw[2 * g] = P[g] & 0xFFFFu; sw[2 * g + 1] = P[g] >> 16; }
+            out = assemble_dual<ALPHA>(wq, cq, pc, ev, sw, sm);
+        }
+    }
+    return out;
+}
+
+}  // namespace astc

@@ -47,11 +47,13 @@ __device__ __forceinline__ float4 power_iteration(float c00, float c01, float c0
     return make_float4(v0, v1, v2, v3);
 }
 
-// principal axis: covariance (149-162), symmetric, 10 unique terms,
-// x fl(1/(N-1)); power iteration (eigen_vector 93-106): v = M v; stop if
-// |v| < 1e-5; v = normalize(M v)
+// covariance (149-162): symmetric, 10 unique terms, x fl(1/(N-1))
+struct Covariance {
+    float c00, c01, c02, c03, c11, c12, c13, c22, c23, c33;
+};
+
 template <int N, class S>
-__device__ __forceinline__ float4 pca_axis(const S& st, const float4 m) {
+__device__ __forceinline__ Covariance block_covariance(const S& st, const float4 m) {
     float c00 = 0.f, c01 = 0.f, c02 = 0.f, c03 = 0.f, c11 = 0.f, c12 = 0.f, c13 = 0.f,
           c22 = 0.f, c23 = 0.f, c33 = 0.f;
 #pragma unroll
@@ -66,11 +68,18 @@ __device__ __forceinline__ float4 pca_axis(const S& st, const float4 m) {
         c23 = __fmaf_rn(d2, d3, c23); c33 = __fmaf_rn(d3, d3, c33);
     }
     constexpr float kInvN1 = 1.0f / (float)(N - 1);
-    c00 = __fmul_rn(c00, kInvN1); c01 = __fmul_rn(c01, kInvN1); c02 = __fmul_rn(c02, kInvN1);
-    c03 = __fmul_rn(c03, kInvN1); c11 = __fmul_rn(c11, kInvN1); c12 = __fmul_rn(c12, kInvN1);
-    c13 = __fmul_rn(c13, kInvN1); c22 = __fmul_rn(c22, kInvN1); c23 = __fmul_rn(c23, kInvN1);
-    c33 = __fmul_rn(c33, kInvN1);
-    return power_iteration(c00, c01, c02, c03, c11, c12, c13, c22, c23, c33);
+    return Covariance{__fmul_rn(c00, kInvN1), __fmul_rn(c01, kInvN1), __fmul_rn(c02, kInvN1),
+                      __fmul_rn(c03, kInvN1), __fmul_rn(c11, kInvN1), __fmul_rn(c12, kInvN1),
+                      __fmul_rn(c13, kInvN1), __fmul_rn(c22, kInvN1), __fmul_rn(c23, kInvN1),
+                      __fmul_rn(c33, kInvN1)};
+}
+
+// principal axis: the covariance, then the power iteration (eigen_vector
+// 93-106): v = M v; stop if |v| < 1e-5; v = normalize(M v)
+template <int N, class S>
+__device__ __forceinline__ float4 pca_axis(const S& st, const float4 m) {
+    const Covariance c = block_covariance<N>(st, m);
+    return power_iteration(c.c00, c.c01, c.c02, c.c03, c.c11, c.c12, c.c13, c.c22, c.c23, c.c33);
 }
 
 // max_accumulation_pixel_direction (170-227), the shader's alternative axis:

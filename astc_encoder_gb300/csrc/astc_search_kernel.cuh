@@ -24,6 +24,7 @@
 #include <stdint.h>
 
 #include "astc_internal.h"
+#include "astc_pipeline_dual.cuh"
 #include "astc_pipeline_partition.cuh"
 
 namespace astc {
@@ -52,6 +53,19 @@ struct SearchLaunch {
     int axis;     // 0 = PCA, 1 = max accumulation
     int search;   // 0 = fixed mode, 1 = search, 2 = search from the better fit
 };
+
+template <bool ALPHA>
+__device__ __forceinline__ void load_dual_smem(DualSmem& ds) {
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const uint32_t* src = reinterpret_cast<const uint32_t*>(&g_search.color[2][ALPHA][0][0]);
+    uint32_t* dst = reinterpret_cast<uint32_t*>(&ds.color[0][0]);
+    const int words = g_search.nslots[2][ALPHA] * 128;
+    for (int i = tid; i < words; i += nt) dst[i] = src[i];
+    if (tid < 12) {
+        ds.cq[tid] = g_search.cq[2][ALPHA][tid];
+        ds.slot[tid] = g_search.slot[2][ALPHA][tid];
+    }
+}
 
 template <bool ALPHA>
 __device__ __forceinline__ void load_partition_smem(PartSmem& pm, int dim) {
@@ -154,15 +168,18 @@ __device__ __forceinline__ void pick_fit(const uint32_t (&tw)[DIM * DIM], const 
     }
 }
 
-// MODE 0: fixed mode (max-accumulation axis) or SEARCH; 1: THOROUGH;
-// 2: THOROUGH plus two-partition candidates.
+// MODE 0: fixed mode (max-accumulation axis) or SEARCH; 1: THOROUGH (both
+// fits, the search, dual-plane candidates); 2: THOROUGH plus two-partition
+// candidates.
 template <int DIM, bool ALPHA, bool NORMAL, bool SRGB, int MODE>
 __global__ void __launch_bounds__(kSearchThreads, 3) astc_encode_blocks_search(const SearchLaunch p) {
     constexpr int N = DIM * DIM;
     constexpr bool thorough = MODE >= 1;
     __shared__ SearchSmem sm;
     __shared__ typename std::conditional<MODE == 2, PartSmem, char>::type pm;
+    __shared__ typename std::conditional<(MODE >= 1), DualSmem, char>::type ds;
     load_search_smem<ALPHA, SRGB>(sm);
+    if constexpr (MODE >= 1) load_dual_smem<ALPHA>(ds);
     if constexpr (MODE == 2) load_partition_smem<ALPHA>(pm, DIM);
     __syncthreads();
     const long long b = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -202,10 +219,15 @@ __global__ void __launch_bounds__(kSearchThreads, 3) astc_encode_blocks_search(c
         for (int k = 0; k < N; ++k) tw[k] = target_word<ALPHA, NORMAL, SRGB>(px[k], sm.tbyte);
         if constexpr (thorough) pick_fit<DIM, ALPHA, SRGB>(tw, sm, q0, q1, qw, fixed, fixed_b, rw_packed);
         blk = search_block<DIM, ALPHA, SRGB>(grid, tw, q0, q1, qw, fixed, sm, &err);
+        if constexpr (thorough)
+            blk = dual_plane_block<DIM, ALPHA, SRGB>(st, grid, tw, BlockError<DIM, ALPHA, SRGB>::target_sq(tw), err,
+                                                     blk, sm, ds);
         if constexpr (MODE == 2) {
-            // the grid colours are done with: the same shared array holds the
-            // partition candidates' per-texel weights
-            SharedFloats<36> tws{reinterpret_cast<float*>(s_grid) + threadIdx.x, (int)blockDim.x};
+            // the partition candidates' per-texel weights, [texel][thread],
+            // after the grid colours: a region of their own, since their float
+            // columns would cross other threads' float4 grid columns (other
+            // warps can still be reading theirs)
+            SharedFloats<36> tws{reinterpret_cast<float*>(s_grid + 16 * blockDim.x) + threadIdx.x, (int)blockDim.x};
             blk = two_partition_block<DIM, ALPHA, SRGB>(st, tw, BlockError<DIM, ALPHA, SRGB>::target_sq(tw), q0,
                                                         q1, err, blk, sm, pm, tws);
         }
@@ -217,6 +239,9 @@ __global__ void __launch_bounds__(kSearchThreads, 3) astc_encode_blocks_search(c
         for (int k = 0; k < N; ++k) tw[k] = target_word<ALPHA, NORMAL, SRGB>(px[k], sm.tbyte);
         if constexpr (thorough) pick_fit<DIM, ALPHA, SRGB>(tw, sm, q0, q1, qw, fixed, fixed_b, rw_packed);
         blk = search_block<DIM, ALPHA, SRGB>(grid, tw, q0, q1, qw, fixed, sm, &err);
+        if constexpr (thorough)
+            blk = dual_plane_block<DIM, ALPHA, SRGB>(st, grid, tw, BlockError<DIM, ALPHA, SRGB>::target_sq(tw), err,
+                                                     blk, sm, ds);
         if constexpr (MODE == 2) {
             char none = 0;
             blk = two_partition_block<DIM, ALPHA, SRGB>(st, tw, BlockError<DIM, ALPHA, SRGB>::target_sq(tw), q0,
@@ -229,8 +254,19 @@ __global__ void __launch_bounds__(kSearchThreads, 3) astc_encode_blocks_search(c
 template <int DIM, bool ALPHA, bool NORMAL, bool SRGB, int MODE>
 cudaError_t launch_t(const SearchLaunch& p, cudaStream_t s) {
     const long long grid = (p.nblocks + kSearchThreads - 1) / kSearchThreads;
-    const size_t smem = (DIM == 6 && p.search) ? (size_t)16 * kSearchThreads * sizeof(float4) : 0;
-    astc_encode_blocks_search<DIM, ALPHA, NORMAL, SRGB, MODE><<<(unsigned)grid, kSearchThreads, smem, s>>>(p);
+    // 6x6: the grid colours, and for two partitions their per-texel weights
+    const size_t per_thread = 16 * sizeof(float4) + (MODE == 2 ? 36 * sizeof(float) : 0);
+    const size_t smem = (DIM == 6 && p.search) ? per_thread * kSearchThreads : 0;
+    auto* kernel = astc_encode_blocks_search<DIM, ALPHA, NORMAL, SRGB, MODE>;
+    if (smem) {
+        // with the dual-plane and two-partition tables the total passes the
+        // 48 KB default (68.6 KB for two partitions: 3 CTAs still fit an SM);
+        // the attribute is per device, so it is set on every launch (a
+        // host-side call, against launches of 100+ us)
+        const cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    kernel<<<(unsigned)grid, kSearchThreads, smem, s>>>(p);
     return cudaGetLastError();
 }
 

@@ -356,9 +356,22 @@ int ise_bits(int quant, int count) {
 }
 
 // Spec ISE decode from a little-endian bit stream starting at bit `pos`.
+// Bits at or past the end of the sequence (pos + ise_bits) read as zero: the
+// last trit or quint group of a sequence is stored cut to the sequence's
+// length, and whatever follows in the block (endpoints, a dual-plane
+// selector) is not part of it.
 void ise_decode(int quant, int count, const uint8_t* p, int pos, uint32_t* out) {
     const Tables& tb = tables();
     const int b = tb.btq[quant][0];
+    const int end = pos + ise_bits(quant, count);
+    auto read_bits = [&](const uint8_t* q, int at, int n) -> uint32_t {
+        uint32_t v = 0;
+        for (int i = 0; i < n; ++i) {
+            const int bit = at + i;
+            if (bit >= 0 && bit < 128 && bit < end) v |= (uint32_t)((q[bit >> 3] >> (bit & 7)) & 1) << i;
+        }
+        return v;
+    };
     if (tb.btq[quant][1]) {
         for (int g = 0; g < count; g += 5) {
             uint32_t m[5] = {0, 0, 0, 0, 0};
@@ -458,9 +471,9 @@ void assemble_symbolic(const uint32_t ep_q[8], const uint32_t qw[16], bool alpha
 // fits in the bits between the header (17 bits for one partition, 29 for
 // several with one shared CEM) and the weights (and the block is illegal
 // below QUANT_6 or outside 24..96 weight bits).
-int endpoint_quant(int wq, int nvals, int header_bits = 17) {
+int endpoint_quant(int wq, int nvals, int header_bits = 17, int nweights = 16) {
     if (wq < QUANT_2 || wq > QUANT_32) return -1;
-    const int wbits = ise_bits(wq, 16);
+    const int wbits = ise_bits(wq, nweights);
     if (wbits < 24 || wbits > 96) return -1;
     const int avail = 128 - header_bits - wbits;
     for (int q = QUANT_256; q >= QUANT_6; --q)
@@ -536,6 +549,30 @@ void assemble_two_partitions(uint32_t wq, uint32_t cq, uint32_t cem, uint32_t se
                              int nvals, const uint32_t* sw, uint8_t out[16]) {
     const uint32_t head = assemble_blockmode(wq) | (1u << 11) | ((seed & 0x3FF) << 13) | ((cem & 0xF) << 25);
     assemble_fields(head, 29, wq, cq, ev, nvals, sw, out);
+}
+
+// Single partition, dual plane: mode [10:0] with D (bit 10) set, CEM [16:13],
+// endpoints from bit 17, the 2-bit plane-2 component selector right below
+// the weights, 32 weights (plane 1, plane 2 per grid point) bit-reversed from
+// bit 127 down.
+void assemble_dual_plane(uint32_t wq, uint32_t cq, uint32_t cem, uint32_t pc, const uint32_t* ev, int nvals,
+                         const uint32_t* sw, uint8_t out[16]) {
+    Bits128 ep = {{0, 0, 0, 0}}, wt = {{0, 0, 0, 0}};
+    ise_encode((int)cq, nvals, ev, ep);
+    ise_encode((int)wq, 32, sw, wt);
+    const int ebits = ise_bits((int)cq, nvals), wbits = ise_bits((int)wq, 32);
+    std::memset(out, 0, 16);
+    auto set = [&](int pos) { out[pos >> 3] = (uint8_t)(out[pos >> 3] | (1u << (pos & 7))); };
+    const uint32_t head = assemble_blockmode(wq) | (1u << 10) | ((cem & 0xF) << 13);
+    for (int i = 0; i < 17; ++i)
+        if ((head >> i) & 1) set(i);
+    for (int i = 0; i < ebits; ++i)
+        if ((ep.w[i >> 5] >> (i & 31)) & 1) set(17 + i);
+    const int sel = 128 - wbits - 2;
+    if (pc & 1) set(sel);
+    if (pc & 2) set(sel + 1);
+    for (int i = 0; i < wbits; ++i)
+        if ((wt.w[i >> 5] >> (i & 31)) & 1) set(127 - i);
 }
 
 // Two-partition patterns (the spec's partition hash, defined with the
@@ -668,13 +705,13 @@ struct Pipe {
         if (!alpha) { e0[3] = P::lit(255.0f, 255.0); e1[3] = P::lit(255.0f, 255.0); }
     }
 
-    // principal_component_analysis (ASTC_Encode.hlsl:139-168)
-    static void pca(const T (*tex)[4], int n, bool alpha, T e0[4], T e1[4]) {
-        T mean[4] = {0, 0, 0, 0};
+    // the mean and covariance of principal_component_analysis
+    // (ASTC_Encode.hlsl:139-162)
+    static void covariance(const T (*tex)[4], int n, T mean[4], T cov[4][4]) {
+        for (int c = 0; c < 4; ++c) mean[c] = 0;
         for (int i = 0; i < n; ++i)
             for (int c = 0; c < 4; ++c) mean[c] = P::add(mean[c], tex[i][c]);
         for (int c = 0; c < 4; ++c) mean[c] = div_const(mean[c], n);
-        T cov[4][4];
         for (int i = 0; i < 4; ++i)
             for (int j = 0; j < 4; ++j) cov[i][j] = 0;
         for (int k = 0; k < n; ++k) {
@@ -685,6 +722,12 @@ struct Pipe {
         }
         for (int i = 0; i < 4; ++i)
             for (int j = 0; j < 4; ++j) cov[i][j] = div_const(cov[i][j], n - 1);
+    }
+
+    // principal_component_analysis (ASTC_Encode.hlsl:139-168)
+    static void pca(const T (*tex)[4], int n, bool alpha, T e0[4], T e1[4]) {
+        T mean[4], cov[4][4];
+        covariance(tex, n, mean, cov);
         T k[4];
         eigen_vector(cov, k);
         find_min_max(tex, n, mean, k, alpha, e0, e1);
@@ -927,6 +970,17 @@ struct Pipe {
             if (err < best) { best = err; *chosen = wq; keep = tr; }
         }
         if (*chosen >= 0) assemble_trial(keep, alpha, out);
+        if (axis == 2) {
+            // dual-plane blocks (THOROUGH and above)
+            uint8_t dblk[16];
+            int dch = -1;
+            const uint32_t derr = dual_plane(tex, tb, dim, alpha, srgb, dblk, &dch);
+            if (derr < best) {
+                best = derr;
+                *chosen = dch;
+                std::memcpy(out, dblk, 16);
+            }
+        }
         if (partitions) {
             // two partitions, split along the kept fit's fixed-mode endpoints
             int PE0[4], PE1[4];
@@ -1085,6 +1139,106 @@ struct Pipe {
                 for (int g = 0; g < 16; ++g) sw[g] = (uint32_t)tbl.scramble[wq][q[g]];
                 assemble_two_partitions((uint32_t)wq, (uint32_t)cq, alpha ? 12u : 8u, (uint32_t)seed, ev, 2 * nv,
                                         sw, out);
+            }
+        }
+        return best;
+    }
+
+    // ---- dual plane (qualities 2 and 3) ------------------------------------
+    // For each channel pc that varies over the block (plane 2), the other
+    // channels are fitted on the axis the shader's power iteration finds for
+    // the block's covariance with pc's row and column zeroed (the PCA of the
+    // block with pc held constant), projected by the shader's find_min_max;
+    // pc's endpoints are its min and max.  Every weight range QUANT_2.. whose
+    // 32 weights (24..96 bits) leave a
+    // legal endpoint range after the plane selector is scored.  Plane-1
+    // weights project the grid colours on the decoded endpoints without pc,
+    // plane-2 weights are (c_pc - E0_pc) / (E1_pc - E0_pc), both clamped to
+    // [0, 1] and rounded to the range.  Returns the best error (UINT32_MAX if
+    // none) and its block in out; *chosen = 200 + 16 * pc + wq.
+    static uint32_t dual_plane(const T (*tex)[4], const int (*tb)[4], int dim, bool alpha, bool srgb,
+                               uint8_t out[16], int* chosen) {
+        const Tables& tbl = tables();
+        const int n = dim * dim, nch = alpha ? 4 : 3, nv = alpha ? 8 : 6;
+        uint32_t best = UINT32_MAX;
+        T mean[4], cov[4][4];
+        covariance(tex, n, mean, cov);
+        for (int pc = 0; pc < nch; ++pc) {
+            T lo = P::lit(1e31f, 1e31), hi = P::lit(-1e31f, -1e31);
+            for (int i = 0; i < n; ++i) {
+                lo = P::min(lo, tex[i][pc]);
+                hi = P::max(hi, tex[i][pc]);
+            }
+            if (lo == hi) continue;                          // a constant channel: nothing to split off
+            // the other channels' axis: the power iteration on the covariance
+            // without pc's row and column (pc's component of the axis is then
+            // exactly 0, so pc takes no part in the projections)
+            T cp[4][4];
+            for (int i = 0; i < 4; ++i)
+                for (int j = 0; j < 4; ++j) cp[i][j] = (i == pc || j == pc) ? (T)0 : cov[i][j];
+            T k[4];
+            eigen_vector(cp, k);
+            T e0[4], e1[4];
+            find_min_max(tex, n, mean, k, alpha, e0, e1);
+            e0[pc] = lo;
+            e1[pc] = hi;
+            T s[16][4];
+            for (int g = 0; g < 16; ++g) grid_sample(tex, dim, g, s[g]);
+            for (int wq = QUANT_2; wq <= QUANT_32; ++wq) {
+                const int cq = endpoint_quant(wq, nv, 19, 32);
+                if (cq < 0) continue;
+                int sym0[4], sym1[4], Q0[4], Q1[4];
+                for (int c = 0; c < 4; ++c) { sym0[c] = sym1[c] = 0; Q0[c] = Q1[c] = 255; }
+                for (int c = 0; c < nch; ++c) {
+                    sym0[c] = nearest_color(cq, (int)P::rint(e0[c]), &Q0[c]);
+                    sym1[c] = nearest_color(cq, (int)P::rint(e1[c]), &Q1[c]);
+                }
+                if (Q1[0] + Q1[1] + Q1[2] < Q0[0] + Q0[1] + Q0[2])
+                    for (int c = 0; c < 4; ++c) {
+                        std::swap(sym0[c], sym1[c]);
+                        std::swap(Q0[c], Q1[c]);
+                    }
+                T d[4];
+                for (int c = 0; c < 4; ++c) d[c] = c == pc ? (T)0 : (T)(Q1[c] - Q0[c]);
+                const T dd = dot4(d, d);
+                const T r = dd == 0 ? (T)0 : P::div(P::lit(1.0f, 1.0), dd);
+                const T dp = (T)(Q1[pc] - Q0[pc]);
+                const T rp = dp == 0 ? (T)0 : P::div(P::lit(1.0f, 1.0), dp);
+                const uint32_t R = (uint32_t)kQuantLevels[wq] - 1;
+                uint32_t q1[16], q2[16];
+                for (int g = 0; g < 16; ++g) {
+                    T diff[4];
+                    for (int c = 0; c < 4; ++c) diff[c] = P::sub(s[g][c], (T)Q0[c]);
+                    T w1 = P::mul(dot4(diff, d), r);
+                    w1 = P::min(P::max(w1, (T)0), P::lit(1.0f, 1.0));
+                    T w2 = P::mul(diff[pc], rp);
+                    w2 = P::min(P::max(w2, (T)0), P::lit(1.0f, 1.0));
+                    q1[g] = (uint32_t)P::rint(P::mul(w1, (T)R));
+                    q2[g] = (uint32_t)P::rint(P::mul(w2, (T)R));
+                }
+                int wv1[16], wv2[16];
+                trial_weights(wq, q1, wv1);
+                trial_weights(wq, q2, wv2);
+                uint32_t err = 0;
+                for (int i = 0; i < n; ++i) {
+                    const int w1 = dim == 4 ? wv1[i] : infill_6x6(wv1, i % 6, i / 6);
+                    const int w2 = dim == 4 ? wv2[i] : infill_6x6(wv2, i % 6, i / 6);
+                    for (int c = 0; c < nch; ++c) {
+                        const int e = decode_channel(Q0[c], Q1[c], c == pc ? w2 : w1, srgb) - tb[i][c];
+                        err += (uint32_t)(e * e);
+                    }
+                }
+                if (err < best) {
+                    best = err;
+                    *chosen = 200 + 16 * pc + wq;
+                    uint32_t ev[8], sw[32];
+                    for (int c = 0; c < nv / 2; ++c) { ev[2 * c] = (uint32_t)sym0[c]; ev[2 * c + 1] = (uint32_t)sym1[c]; }
+                    for (int g = 0; g < 16; ++g) {
+                        sw[2 * g] = (uint32_t)tbl.scramble[wq][q1[g]];
+                        sw[2 * g + 1] = (uint32_t)tbl.scramble[wq][q2[g]];
+                    }
+                    assemble_dual_plane((uint32_t)wq, (uint32_t)cq, alpha ? 12u : 8u, (uint32_t)pc, ev, nv, sw, out);
+                }
             }
         }
         return best;
