@@ -49,7 +49,7 @@ CLI_SOURCES = [
     ("astc_cs_enc.cpp", []),
     ("image_load.cpp", []),
 ]
-HEADERS = ["astc_internal.h", "astc_tables.h", "astc_block_common.cuh", "astc_pipeline_fp32.cuh",
+HEADERS = ["astc_internal.h", "astc_tables.h", "astc_ise.h", "astc_block_common.cuh", "astc_pipeline_fp32.cuh",
            "astc_pipeline_h2.cuh", "astc_pipeline_search.cuh", "astc_pipeline_dual.cuh", "astc_pipeline_partition.cuh", "astc_search_kernel.cuh",
            "astc_partition_table.h", "astc_srgb_table.h", "image_load.h"]
 

@@ -3,12 +3,14 @@
 // shader writes the dual-plane bit of its block mode as a constant 0
 // (assemble_blockmode, ASTC_Encode.hlsl:446-473).
 //
-// For each channel pc that varies over the block, plane 2 carries pc alone:
-// the other channels are fitted on the axis the shader's power iteration finds
-// for the block's covariance with pc's row and column zeroed (the PCA of the
-// block with pc held constant; the axis's pc component is then exactly 0, so
-// pc takes no part in find_min_max's projections), pc's endpoints are its
-// minimum and maximum.  Every weight range whose 32 weights (plane 1, plane 2
+// Plane 2 carries one channel pc.  For each channel that varies over the
+// block, the shader's power iteration runs on the block's covariance with that
+// channel's row and column zeroed (the PCA of the block with the channel held
+// constant; the axis's component on the channel is then exactly 0, so it takes
+// no part in find_min_max's projections).  pc is the channel whose zeroed
+// covariance keeps the least off-axis variance: its trace minus the Rayleigh
+// quotient v.Cv / v.v (the first channel on ties).  The other channels are
+// fitted on pc's axis, pc's endpoints are its minimum and maximum.  Every weight range whose 32 weights (plane 1, plane 2
 // per grid point; 24..96 bits) leave a legal endpoint range after the 2-bit
 // plane selector is scored by the exact decode, each channel taking its
 // plane's weight.  Plane-1 weights project the grid colours on the decoded
@@ -101,108 +103,125 @@ __device__ __forceinline__ uint4 dual_plane_block(const S& st, const G& grid, co
                                                   const DualSmem& ds) {
     constexpr int N = DIM * DIM;
     constexpr int NCH = ALPHA ? 4 : 3;
-    int found_pc = -1, found_wq = -1;
-    uint4 out = best;
-    // the block's mean and covariance, shared by every channel
     const float4 m = block_mean<N>(st);
     const Covariance cv = block_covariance<N>(st, m);
-    // every channel, then one more pass over the best (pc, range) to assemble it
+    // the plane-2 channel: of the channels that vary, the one whose zeroed
+    // covariance keeps the least off-axis variance (first on ties)
+    int pc = -1;
+    float least = 0.0f, plo = 0.0f, phi = 0.0f;
+    float4 pv = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 #pragma unroll 1
-    for (int it = 0; it <= NCH; ++it) {
-        const bool final_pass = it == NCH;
-        if (final_pass && found_pc < 0) break;
-        const int pc = final_pass ? found_pc : it;
+    for (int c = 0; c < NCH; ++c) {
         float lo = 1e31f, hi = -1e31f;
 #pragma unroll
         for (int k = 0; k < N; ++k) {
-            const float v = comp(st.get(k), pc);
+            const float v = comp(st.get(k), c);
             lo = fminf(lo, v);
             hi = fmaxf(hi, v);
         }
         if (lo == hi) continue;                    // a constant channel: nothing to split off
-        uint32_t q0[4], q1[4];
-        {
-            // entry (i, j) is zeroed when i or j is pc
-            const bool z0 = pc == 0, z1 = pc == 1, z2 = pc == 2, z3 = pc == 3;
-            const float4 v = power_iteration(z0 ? 0.0f : cv.c00, (z0 || z1) ? 0.0f : cv.c01,
-                                             (z0 || z2) ? 0.0f : cv.c02, (z0 || z3) ? 0.0f : cv.c03,
-                                             z1 ? 0.0f : cv.c11, (z1 || z2) ? 0.0f : cv.c12,
-                                             (z1 || z3) ? 0.0f : cv.c13, z2 ? 0.0f : cv.c22,
-                                             (z2 || z3) ? 0.0f : cv.c23, z3 ? 0.0f : cv.c33);
-            float e0[4], e1[4];
-            find_min_max<N, ALPHA>(st, m, v, e0, e1, q0, q1);
-        }
-        const uint32_t lq = rint_u32(lo), hq = rint_u32(hi);
-        q0[0] = pc == 0 ? lq : q0[0]; q0[1] = pc == 1 ? lq : q0[1]; q0[2] = pc == 2 ? lq : q0[2];
-        q0[3] = pc == 3 ? lq : q0[3];
-        q1[0] = pc == 0 ? hq : q1[0]; q1[1] = pc == 1 ? hq : q1[1]; q1[2] = pc == 2 ? hq : q1[2];
-        q1[3] = pc == 3 ? hq : q1[3];
+        // entry (i, j) is zeroed when i or j is c
+        const bool z0 = c == 0, z1 = c == 1, z2 = c == 2, z3 = c == 3;
+        const float a00 = z0 ? 0.0f : cv.c00, a01 = (z0 || z1) ? 0.0f : cv.c01;
+        const float a02 = (z0 || z2) ? 0.0f : cv.c02, a03 = (z0 || z3) ? 0.0f : cv.c03;
+        const float a11 = z1 ? 0.0f : cv.c11, a12 = (z1 || z2) ? 0.0f : cv.c12;
+        const float a13 = (z1 || z3) ? 0.0f : cv.c13, a22 = z2 ? 0.0f : cv.c22;
+        const float a23 = (z2 || z3) ? 0.0f : cv.c23, a33 = z3 ? 0.0f : cv.c33;
+        const float4 v = power_iteration(a00, a01, a02, a03, a11, a12, a13, a22, a23, a33);
+        // trace minus the Rayleigh quotient v.Cv / v.v
+        const float k0 = dot4(a00, a01, a02, a03, v.x, v.y, v.z, v.w);
+        const float k1 = dot4(a01, a11, a12, a13, v.x, v.y, v.z, v.w);
+        const float k2 = dot4(a02, a12, a22, a23, v.x, v.y, v.z, v.w);
+        const float k3 = dot4(a03, a13, a23, a33, v.x, v.y, v.z, v.w);
+        const float vv = dot4(v.x, v.y, v.z, v.w, v.x, v.y, v.z, v.w);
+        const float lam = vv > 0.0f ? __fdiv_rn(dot4(v.x, v.y, v.z, v.w, k0, k1, k2, k3), vv) : 0.0f;
+        const float resid = __fsub_rn(__fadd_rn(__fadd_rn(__fadd_rn(a00, a11), a22), a33), lam);
+        if (pc < 0 || resid < least) { pc = c; least = resid; plo = lo; phi = hi; pv = v; }
+    }
+    if (pc < 0) return best;
+    // the other channels on pc's axis (its pc component is exactly 0), pc on
+    // its range
+    uint32_t q0[4], q1[4];
+    {
+        float e0[4], e1[4];
+        find_min_max<N, ALPHA>(st, m, pv, e0, e1, q0, q1);
+    }
+    const uint32_t lq = rint_u32(plo), hq = rint_u32(phi);
+    q0[0] = pc == 0 ? lq : q0[0]; q0[1] = pc == 1 ? lq : q0[1]; q0[2] = pc == 2 ? lq : q0[2];
+    q0[3] = pc == 3 ? lq : q0[3];
+    q1[0] = pc == 0 ? hq : q1[0]; q1[1] = pc == 1 ? hq : q1[1]; q1[2] = pc == 2 ? hq : q1[2];
+    q1[3] = pc == 3 ? hq : q1[3];
+    // every legal weight range, then one more pass over the best to assemble it
+    int found = -1;
+    uint4 out = best;
 #pragma unroll 1
-        for (int wq = kQuant2; wq <= kQuant32; ++wq) {
-            if (final_pass && wq != found_wq) continue;
-            const int cq = ds.cq[wq];
-            if (cq < 0) continue;
-            int sym0[4], sym1[4], E0[4], E1[4];
+    for (int it = kQuant2; it <= kQuant32 + 1; ++it) {
+        const bool final_pass = it > kQuant32;
+        if (final_pass && found < 0) break;
+        const int wq = final_pass ? found : it;
+        const int cq = ds.cq[wq];
+        if (cq < 0) continue;
+        int sym0[4], sym1[4], E0[4], E1[4];
 #pragma unroll
-            for (int c = 0; c < 4; ++c) { sym0[c] = 0; sym1[c] = 0; E0[c] = 255; E1[c] = 255; }
+        for (int c = 0; c < 4; ++c) { sym0[c] = 0; sym1[c] = 0; E0[c] = 255; E1[c] = 255; }
 #pragma unroll
-            for (int c = 0; c < NCH; ++c) {
-                if (cq == kQuant256) {
-                    sym0[c] = E0[c] = (int)q0[c];
-                    sym1[c] = E1[c] = (int)q1[c];
-                } else {
-                    const uint32_t a = ds.color[ds.slot[wq]][q0[c]], b = ds.color[ds.slot[wq]][q1[c]];
-                    sym0[c] = (int)(a & 0xFFu); E0[c] = (int)(a >> 8);
-                    sym1[c] = (int)(b & 0xFFu); E1[c] = (int)(b >> 8);
-                }
+        for (int c = 0; c < NCH; ++c) {
+            if (cq == kQuant256) {
+                sym0[c] = E0[c] = (int)q0[c];
+                sym1[c] = E1[c] = (int)q1[c];
+            } else {
+                const uint32_t a = ds.color[ds.slot[wq]][q0[c]], b = ds.color[ds.slot[wq]][q1[c]];
+                sym0[c] = (int)(a & 0xFFu); E0[c] = (int)(a >> 8);
+                sym1[c] = (int)(b & 0xFFu); E1[c] = (int)(b >> 8);
             }
-            if (E1[0] + E1[1] + E1[2] < E0[0] + E0[1] + E0[2]) {
-#pragma unroll
-                for (int c = 0; c < 4; ++c) {
-                    int t = sym0[c]; sym0[c] = sym1[c]; sym1[c] = t;
-                    t = E0[c]; E0[c] = E1[c]; E1[c] = t;
-                }
-            }
-            float d[4], f[4];
+        }
+        if (E1[0] + E1[1] + E1[2] < E0[0] + E0[1] + E0[2]) {
 #pragma unroll
             for (int c = 0; c < 4; ++c) {
-                f[c] = (float)E0[c];
-                d[c] = c == pc ? 0.0f : (float)(E1[c] - E0[c]);
+                int t = sym0[c]; sym0[c] = sym1[c]; sym1[c] = t;
+                t = E0[c]; E0[c] = E1[c]; E1[c] = t;
             }
-            const float dd = dot4(d[0], d[1], d[2], d[3], d[0], d[1], d[2], d[3]);
-            const float r = dd == 0.0f ? 0.0f : __frcp_rn(dd);
-            // selects, not E[pc]: a runtime index would put E0/E1 in local memory
-            const int e0p = pc == 0 ? E0[0] : pc == 1 ? E0[1] : pc == 2 ? E0[2] : E0[3];
-            const int e1p = pc == 0 ? E1[0] : pc == 1 ? E1[1] : pc == 2 ? E1[2] : E1[3];
-            const float dp = (float)(e1p - e0p);
-            const float rp = dp == 0.0f ? 0.0f : __frcp_rn(dp);
-            const float R = sm.wmax[wq];
-            // scoring passes: the weights' values; the final pass: their ISE symbols
-            const uint8_t* tab = final_pass ? sm.scramble[wq] : sm.wval[wq];
-            uint32_t P[16];
-#pragma unroll
-            for (int g = 0; g < 16; ++g) {
-                const float4 sg = grid.get(g);
-                const float x0 = __fsub_rn(sg.x, f[0]), x1 = __fsub_rn(sg.y, f[1]);
-                const float x2 = __fsub_rn(sg.z, f[2]), x3 = __fsub_rn(sg.w, f[3]);
-                const float w1 = fminf(fmaxf(__fmul_rn(dot4(x0, x1, x2, x3, d[0], d[1], d[2], d[3]), r), 0.0f), 1.0f);
-                const float xp = pc == 0 ? x0 : pc == 1 ? x1 : pc == 2 ? x2 : x3;
-                const float w2 = fminf(fmaxf(__fmul_rn(xp, rp), 0.0f), 1.0f);
-                P[g] = (uint32_t)tab[rint_u32(__fmul_rn(w1, R))] | ((uint32_t)tab[rint_u32(__fmul_rn(w2, R))] << 16);
-            }
-            if (!final_pass) {
-                const uint32_t err = eval_dual<DIM, ALPHA, SRGB>(tw, t2, pc, E0, E1, P);
-                if (err < best_err) { best_err = err; found_pc = pc; found_wq = wq; }
-                continue;
-            }
-            uint32_t ev[ALPHA ? 8 : 6];
-#pragma unroll
-            for (int c = 0; c < NCH; ++c) { ev[2 * c] = (uint32_t)sym0[c]; ev[2 * c + 1] = (uint32_t)sym1[c]; }
-            uint32_t sw[32];
-#pragma unroll
-            for (int g = 0; g < 16; ++g) { sw[2 * g] = P[g] & 0xFFFFu; sw[2 * g + 1] = P[g] >> 16; }
-            out = assemble_dual<ALPHA>(wq, cq, pc, ev, sw, sm);
         }
+        float d[4], f[4];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            f[c] = (float)E0[c];
+            d[c] = c == pc ? 0.0f : (float)(E1[c] - E0[c]);
+        }
+        const float dd = dot4(d[0], d[1], d[2], d[3], d[0], d[1], d[2], d[3]);
+        const float r = dd == 0.0f ? 0.0f : __frcp_rn(dd);
+        // selects, not E[pc]: a runtime index would put E0/E1 in local memory
+        const int e0p = pc == 0 ? E0[0] : pc == 1 ? E0[1] : pc == 2 ? E0[2] : E0[3];
+        const int e1p = pc == 0 ? E1[0] : pc == 1 ? E1[1] : pc == 2 ? E1[2] : E1[3];
+        const float dp = (float)(e1p - e0p);
+        const float rp = dp == 0.0f ? 0.0f : __frcp_rn(dp);
+        const float R = sm.wmax[wq];
+        // scoring passes: the weights' values; the final pass: their ISE symbols
+        const uint8_t* tab = final_pass ? sm.scramble[wq] : sm.wval[wq];
+        uint32_t P[16];
+#pragma unroll
+        for (int g = 0; g < 16; ++g) {
+            const float4 sg = grid.get(g);
+            const float x0 = __fsub_rn(sg.x, f[0]), x1 = __fsub_rn(sg.y, f[1]);
+            const float x2 = __fsub_rn(sg.z, f[2]), x3 = __fsub_rn(sg.w, f[3]);
+            const float w1 = fminf(fmaxf(__fmul_rn(dot4(x0, x1, x2, x3, d[0], d[1], d[2], d[3]), r), 0.0f), 1.0f);
+            const float xp = pc == 0 ? x0 : pc == 1 ? x1 : pc == 2 ? x2 : x3;
+            const float w2 = fminf(fmaxf(__fmul_rn(xp, rp), 0.0f), 1.0f);
+            P[g] = (uint32_t)tab[rint_u32(__fmul_rn(w1, R))] | ((uint32_t)tab[rint_u32(__fmul_rn(w2, R))] << 16);
+        }
+        if (!final_pass) {
+            const uint32_t err = eval_dual<DIM, ALPHA, SRGB>(tw, t2, pc, E0, E1, P);
+            if (err < best_err) { best_err = err; found = wq; }
+            continue;
+        }
+        uint32_t ev[ALPHA ? 8 : 6];
+#pragma unroll
+        for (int c = 0; c < NCH; ++c) { ev[2 * c] = (uint32_t)sym0[c]; ev[2 * c + 1] = (uint32_t)sym1[c]; }
+        uint32_t sw[32];
+#pragma unroll
+        for (int g = 0; g < 16; ++g) { sw[2 * g] = P[g] & 0xFFFFu; sw[2 * g + 1] = P[g] >> 16; }
+        out = assemble_dual<ALPHA>(wq, cq, pc, ev, sw, sm);
+        break;
     }
     return out;
 }

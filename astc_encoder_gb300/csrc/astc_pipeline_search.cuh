@@ -21,6 +21,7 @@
 #include <type_traits>
 
 #include "astc_pipeline_fp32.cuh"
+#include "astc_ise.h"
 
 namespace astc {
 
@@ -89,77 +90,16 @@ struct SearchSmem {
 // ---------------------------------------------------------------------------
 // general bounded integer sequence encoding (ISE) into a 128-bit field
 // ---------------------------------------------------------------------------
-struct Bits128 { uint64_t lo, hi; };
-
-__device__ __forceinline__ void put_bits(Bits128& b, int& pos, uint32_t v, int n) {
-    if (n > 0) {
-        const uint64_t x = v;
-        if (pos < 64) {
-            b.lo |= x << pos;
-            if (pos > 0 && pos + n > 64) b.hi |= x >> (64 - pos);
-        } else {
-            b.hi |= x << (pos - 64);
-        }
-    }
-    pos += n;
-}
-
-__device__ __forceinline__ void keep_low_bits(Bits128& b, int n) {
-    if (n < 64) { b.lo &= (n ? (~0ull >> (64 - n)) : 0ull); b.hi = 0; }
-    else if (n < 128) { b.hi &= (n > 64 ? (~0ull >> (128 - n)) : 0ull); }
-}
-
-// COUNT symbols of quant method `quant` (runtime), LSB first: groups of five
-// (trits: m0 T[1:0] m1 T[3:2] m2 T[4] m3 T[6:5] m4 T[7]) or three (quints:
-// m0 Q[2:0] m1 Q[4:3] m2 Q[6:5]) padded with zeros, or plain bit fields
-// (ASTC_IntegerSequenceEncoding.hlsl encode_trits 142-176, encode_quints
+// COUNT symbols of quant method `quant` (runtime) as an integer sequence
+// (astc_ise.h: one rolled loop, the same bits as the reference's
+// ASTC_IntegerSequenceEncoding.hlsl encode_trits 142-176, encode_quints
 // 181-205, bise_* 207-276), cut to the ISE length of COUNT values.
 template <int COUNT>
 __device__ __forceinline__ Bits128 ise_encode(int quant, const uint32_t (&v)[COUNT], const uint8_t* trits,
                                               const uint8_t* quints) {
-    const RangeShape sh = range_shape(quant);
-    const int b = sh.bits;
-    const uint32_t mask = (1u << b) - 1u;
-    Bits128 o{0ull, 0ull};
-    int pos = 0;
-    if (sh.trits) {
-#pragma unroll
-        for (int g = 0; g < (COUNT + 4) / 5; ++g) {
-            uint32_t m[5], t[5];
-#pragma unroll
-            for (int j = 0; j < 5; ++j) {
-                const uint32_t x = (g * 5 + j < COUNT) ? v[(g * 5 + j < COUNT) ? g * 5 + j : 0] : 0u;
-                m[j] = x & mask;
-                t[j] = x >> b;
-            }
-            const uint32_t T = trits[t[4] * 81 + t[3] * 27 + t[2] * 9 + t[1] * 3 + t[0]];
-            put_bits(o, pos, m[0], b); put_bits(o, pos, T & 3u, 2);
-            put_bits(o, pos, m[1], b); put_bits(o, pos, (T >> 2) & 3u, 2);
-            put_bits(o, pos, m[2], b); put_bits(o, pos, (T >> 4) & 1u, 1);
-            put_bits(o, pos, m[3], b); put_bits(o, pos, (T >> 5) & 3u, 2);
-            put_bits(o, pos, m[4], b); put_bits(o, pos, (T >> 7) & 1u, 1);
-        }
-    } else if (sh.quints) {
-#pragma unroll
-        for (int g = 0; g < (COUNT + 2) / 3; ++g) {
-            uint32_t m[3], q[3];
-#pragma unroll
-            for (int j = 0; j < 3; ++j) {
-                const uint32_t x = (g * 3 + j < COUNT) ? v[(g * 3 + j < COUNT) ? g * 3 + j : 0] : 0u;
-                m[j] = x & mask;
-                q[j] = x >> b;
-            }
-            const uint32_t Q = quints[q[2] * 25 + q[1] * 5 + q[0]];
-            put_bits(o, pos, m[0], b); put_bits(o, pos, Q & 7u, 3);
-            put_bits(o, pos, m[1], b); put_bits(o, pos, (Q >> 3) & 3u, 2);
-            put_bits(o, pos, m[2], b); put_bits(o, pos, (Q >> 5) & 3u, 2);
-        }
-    } else {
-#pragma unroll
-        for (int i = 0; i < COUNT; ++i) put_bits(o, pos, v[i], b);
-    }
-    keep_low_bits(o, ise_bit_count(quant, COUNT));
-    return o;
+    uint32_t w[(COUNT + 3) / 4];
+    pack_bytes<COUNT>(v, w);
+    return ise_encode_packed<(COUNT + 3) / 4>(quant, COUNT, w, trits, quints);
 }
 
 // Single-partition block, 4x4 weight grid of range wq, endpoint range cq:

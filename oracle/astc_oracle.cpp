@@ -1145,12 +1145,15 @@ struct Pipe {
     }
 
     // ---- dual plane (qualities 2 and 3) ------------------------------------
-    // For each channel pc that varies over the block (plane 2), the other
-    // channels are fitted on the axis the shader's power iteration finds for
-    // the block's covariance with pc's row and column zeroed (the PCA of the
-    // block with pc held constant), projected by the shader's find_min_max;
-    // pc's endpoints are its min and max.  Every weight range QUANT_2.. whose
-    // 32 weights (24..96 bits) leave a
+    // Plane 2 carries one channel pc.  For each channel that varies over the
+    // block, the shader's power iteration runs on the block's covariance with
+    // that channel's row and column zeroed (the PCA of the block with the
+    // channel held constant); pc is the channel whose zeroed covariance keeps
+    // the least off-axis variance (its trace minus the Rayleigh quotient
+    // k.Ck / k.k; the first channel on ties).  The other channels are fitted
+    // on pc's axis by the shader's find_min_max, pc's endpoints are its min
+    // and max.  Every weight range QUANT_2.. whose 32 weights (24..96 bits)
+    // leave a
     // legal endpoint range after the plane selector is scored.  Plane-1
     // weights project the grid colours on the decoded endpoints without pc,
     // plane-2 weights are (c_pc - E0_pc) / (E1_pc - E0_pc), both clamped to
@@ -1163,21 +1166,36 @@ struct Pipe {
         uint32_t best = UINT32_MAX;
         T mean[4], cov[4][4];
         covariance(tex, n, mean, cov);
-        for (int pc = 0; pc < nch; ++pc) {
-            T lo = P::lit(1e31f, 1e31), hi = P::lit(-1e31f, -1e31);
+        int pc = -1;
+        T lo = 0, hi = 0, k[4] = {0, 0, 0, 0}, least = 0;
+        for (int c = 0; c < nch; ++c) {
+            T clo = P::lit(1e31f, 1e31), chi = P::lit(-1e31f, -1e31);
             for (int i = 0; i < n; ++i) {
-                lo = P::min(lo, tex[i][pc]);
-                hi = P::max(hi, tex[i][pc]);
+                clo = P::min(clo, tex[i][c]);
+                chi = P::max(chi, tex[i][c]);
             }
-            if (lo == hi) continue;                          // a constant channel: nothing to split off
+            if (clo == chi) continue;                        // a constant channel: nothing to split off
             // the other channels' axis: the power iteration on the covariance
-            // without pc's row and column (pc's component of the axis is then
-            // exactly 0, so pc takes no part in the projections)
+            // without c's row and column (c's component of the axis is then
+            // exactly 0, so c takes no part in the projections)
             T cp[4][4];
             for (int i = 0; i < 4; ++i)
-                for (int j = 0; j < 4; ++j) cp[i][j] = (i == pc || j == pc) ? (T)0 : cov[i][j];
-            T k[4];
-            eigen_vector(cp, k);
+                for (int j = 0; j < 4; ++j) cp[i][j] = (i == c || j == c) ? (T)0 : cov[i][j];
+            T kc[4];
+            eigen_vector(cp, kc);
+            T ck[4];
+            for (int r = 0; r < 4; ++r) ck[r] = dot4(cp[r], kc);
+            const T kk = dot4(kc, kc);
+            const T lam = kk > 0 ? P::div(dot4(kc, ck), kk) : (T)0;
+            T tr = 0;
+            for (int r = 0; r < 4; ++r) tr = P::add(tr, cp[r][r]);
+            const T resid = P::sub(tr, lam);
+            if (pc < 0 || resid < least) {
+                pc = c; least = resid; lo = clo; hi = chi;
+                for (int r = 0; r < 4; ++r) k[r] = kc[r];
+            }
+        }
+        if (pc >= 0) {
             T e0[4], e1[4];
             find_min_max(tex, n, mean, k, alpha, e0, e1);
             e0[pc] = lo;
