@@ -67,7 +67,7 @@ class Axis(enum.IntEnum):
 class Quality(enum.IntEnum):
     FAST = 0                # the reference's fixed mode (518-522)
     SEARCH = 1              # every single-partition 4x4-grid mode, least decoded error
-    THOROUGH = 2            # SEARCH from the better of the PCA and max-accumulation fits
+    THOROUGH = 2            # SEARCH from the better of the PCA and max-accumulation fits, plus dual-plane blocks
     PARTITIONS = 3          # THOROUGH plus two-partition blocks
 
 

@@ -21,11 +21,13 @@
 namespace astc {
 
 // Unroll factor of the candidates' per-texel loops: rolled loops keep the
-// candidate loop short (the kernel is otherwise bound by instruction fetch);
-// on GB300, 4x4 ran best fully rolled (normal map: 1.78 ms against 1.96 at 2
-// and 2.36 fully unrolled) and 6x6 at 2 (0.47 ms; 0.54 rolled).
+// candidate loop short (instruction fetch), unrolled ones keep the texels in
+// registers (a rolled loop indexes them, so they live in local memory).  On
+// GB300 with the rolled ISE encoder, PARTITIONS launches: 4x4 normal map
+// 4096^2 1.63 ms rolled, 1.66 at 4, 1.75 unrolled (4x4 RGB 512^2: 90, 86,
+// 84 us); 6x6 RGBA sRGB 2048^2 615 us at 2, 560 unrolled.
 template <int DIM>
-constexpr int kPartTexelUnroll = DIM == 4 ? 1 : 2;
+constexpr int kPartTexelUnroll = DIM == 4 ? 1 : 36;
 
 // Per-CTA copies of the two-partition tables (shared memory).
 struct PartSmem {

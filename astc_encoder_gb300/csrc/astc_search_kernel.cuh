@@ -219,6 +219,11 @@ __global__ void __launch_bounds__(kSearchThreads, 3) astc_encode_blocks_search(c
         for (int k = 0; k < N; ++k) tw[k] = target_word<ALPHA, NORMAL, SRGB>(px[k], sm.tbyte);
         if constexpr (thorough) pick_fit<DIM, ALPHA, SRGB>(tw, sm, q0, q1, qw, fixed, fixed_b, rw_packed);
         blk = search_block<DIM, ALPHA, SRGB>(grid, tw, q0, q1, qw, fixed, sm, &err);
+        // an exact block stays: later candidates must decode with less error
+        if (err == 0) {
+            p.out[b] = blk;
+            return;
+        }
         if constexpr (thorough)
             blk = dual_plane_block<DIM, ALPHA, SRGB>(st, grid, tw, BlockError<DIM, ALPHA, SRGB>::target_sq(tw), err,
                                                      blk, sm, ds);
@@ -239,6 +244,10 @@ __global__ void __launch_bounds__(kSearchThreads, 3) astc_encode_blocks_search(c
         for (int k = 0; k < N; ++k) tw[k] = target_word<ALPHA, NORMAL, SRGB>(px[k], sm.tbyte);
         if constexpr (thorough) pick_fit<DIM, ALPHA, SRGB>(tw, sm, q0, q1, qw, fixed, fixed_b, rw_packed);
         blk = search_block<DIM, ALPHA, SRGB>(grid, tw, q0, q1, qw, fixed, sm, &err);
+        if (err == 0) {
+            p.out[b] = blk;
+            return;
+        }
         if constexpr (thorough)
             blk = dual_plane_block<DIM, ALPHA, SRGB>(st, grid, tw, BlockError<DIM, ALPHA, SRGB>::target_sq(tw), err,
                                                      blk, sm, ds);

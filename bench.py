@@ -305,9 +305,9 @@ def _psnr_blocks(native, blocks: np.ndarray, tex: np.ndarray, spec: dict) -> flo
 def _bench_search(torch, native, headline: str, texs, outs, spec: dict) -> dict:
     """Throughput and decoded PSNR of the quality modes -- the search (every
     single-partition 4x4-grid mode, least decoded error), the max-accumulation
-    axis, THOROUGH (search from the better fit) and PARTITIONS (THOROUGH plus
-    two-partition blocks) -- against the fixed mode, on each workload
-    (device-resident inputs above L2 size, as the headline)."""
+    axis, THOROUGH (search from the better fit, plus dual-plane blocks) and
+    PARTITIONS (THOROUGH plus two-partition blocks) -- against the fixed mode,
+    on each workload (device-resident inputs above L2 size, as the headline)."""
     from astc_encoder_gb300 import synth
     result = {}
     for name in (headline, "4x4_rgb_512", "4x4_normal_4096", "6x6_rgba_srgb_2048"):

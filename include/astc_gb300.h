@@ -84,13 +84,21 @@ typedef enum astc_quality {
                                     choose_best_quantmethod the
                                     reference sketches (524-526).  Never
                                     worse than FAST; FP32 only              */
-    ASTC_QUALITY_THOROUGH = 2,   /* SEARCH from the better of the two fits:
-                                    PCA and max accumulation both run, the
+    ASTC_QUALITY_THOROUGH = 2,   /* SEARCH from the better of the two fits
+                                    (PCA and max accumulation both run; the
                                     one whose fixed-mode block decodes with
-                                    less error is searched from (PCA on
-                                    ties; opts.axis is ignored).  Recovers
-                                    the blocks the reference's PCA collapses
-                                    (flat colour, varying alpha); FP32 only */
+                                    less error is searched from, PCA on
+                                    ties; opts.axis is ignored), plus
+                                    single-partition dual-plane blocks: one
+                                    channel on its own weight plane (the one
+                                    whose removal leaves the least off-axis
+                                    variance), the others fitted without it,
+                                    every legal weight range scored (the
+                                    reference writes the dual-plane bit as 0,
+                                    ASTC_Encode.hlsl:446-473).  Recovers the
+                                    blocks the reference's PCA collapses
+                                    (flat colour, varying alpha) and
+                                    decorrelated channels; FP32 only        */
     ASTC_QUALITY_PARTITIONS = 3  /* THOROUGH plus two-partition blocks: the
                                     partition index whose pattern best
                                     matches the split along the kept fit,

@@ -22,7 +22,12 @@
  *   search mode            the choose_best_quantmethod the shader sketches at
  *                          ASTC_Encode.hlsl:524-526 (opts.quality = 1): every
  *                          4x4-grid weight range with the endpoint range the
- *                          decoder derives, scored by the spec decode
+ *                          decoder derives, scored by the spec decode;
+ *                          quality 2 adds the other fit and dual-plane
+ *                          blocks, quality 3 two-partition blocks (modes
+ *                          the shader leaves out: its dual-plane bit is 0,
+ *                          ASTC_Encode.hlsl:446-473; its partition layout a
+ *                          commented-out stub, 422-431)
  *
  * The lookup tables are GENERATED here from the ASTC specification's
  * definitions (trit/quint decode, weight unquantisation), never copied; the

@@ -46,7 +46,10 @@ typedef struct oracle_opts {
                         sketches at 524-526); 2 = the same search from the
                         better of the two fits (both axes tried, the one
                         whose fixed-mode block has the smaller error kept,
-                        the PCA on ties; axis is then ignored); 3 = 2 plus
+                        the PCA on ties; axis is then ignored) plus
+                        dual-plane candidates (one channel on plane 2,
+                        chosen by the residual of the covariance without
+                        it; every legal weight range scored); 3 = 2 plus
                         two-partition candidates (one partition pattern,
                         matched to the split of the kept fit, each
                         partition fitted on its own, every legal weight

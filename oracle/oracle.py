@@ -80,7 +80,9 @@ def encode(rgba: np.ndarray, block_dim: int = 4, has_alpha: bool = False, is_nor
     """FP32 (or FP64 twin) oracle encode of a (H, W, 4) uint8 image -> (n, 16) uint8.
 
     axis 1 = max_accumulation_pixel_direction instead of the PCA; quality 1 =
-    search over the single-partition weight/endpoint ranges."""
+    search over the single-partition weight/endpoint ranges; 2 = the search
+    from the better of both fits plus dual-plane blocks; 3 = 2 plus
+    two-partition blocks."""
     a = np.ascontiguousarray(rgba, dtype=np.uint8)
     h, w = a.shape[:2]
     nb = ((w + block_dim - 1) // block_dim) * ((h + block_dim - 1) // block_dim)
