@@ -2,7 +2,8 @@
 of a two-partition ASTC block, the texels the specification's partition hash
 puts in partition 1, as a bit mask over the block's texels in row-major order
 (bit y * dim + x), for 4x4 blocks (16 bits; "small block" rule: fewer than 31
-texels doubles the coordinates) and 6x6 blocks (36 bits).
+texels doubles the coordinates) and 6x6 blocks (36 bits); the two-partition
+pattern classes; and the three-partition pattern classes.
 Run: python astc_encoder_gb300/csrc/gen_partition_table.py
 """
 import os
@@ -92,6 +93,32 @@ def classes(dim: int) -> list:
     return out
 
 
+def classes3(dim: int) -> list:
+    """(seed, m1, m2) of the smallest partition index of every distinct way a
+    three-partition block splits its texels into three non-empty sets (two
+    indices that split alike up to the partitions' order are one class), in
+    index order; m1 / m2 = the texels in partitions 1 / 2 of that index."""
+    small = dim * dim < 31
+    seen = set()
+    out = []
+    for seed in range(1024):
+        part = [select_partition(seed, i % dim, i // dim, 0, 3, small) for i in range(dim * dim)]
+        if len(set(part)) < 3:
+            continue
+        order = []
+        for v in part:
+            if v not in order:
+                order.append(v)
+        canon = tuple(order.index(v) for v in part)          # relabelled in order of first texel
+        if canon in seen:
+            continue
+        seen.add(canon)
+        m1 = sum(1 << i for i, v in enumerate(part) if v == 1)
+        m2 = sum(1 << i for i, v in enumerate(part) if v == 2)
+        out.append((seed, m1, m2))
+    return out
+
+
 def main() -> None:
     m4, m6 = masks(4), masks(6)
     c4, c6 = classes(4), classes(6)
@@ -119,6 +146,25 @@ def main() -> None:
     lines.append(f"constexpr uint64_t kPartition2Classes6x6[{len(c6)}] = {{")
     for i in range(0, len(c6), 4):
         lines.append("    " + ", ".join(f"0x{(sd << 54) | m:016X}ull" for sd, m in c6[i:i + 4]) + ",")
+    t4, t6 = classes3(4), classes3(6)
+    lines.append("};")
+    lines.append("// Three-partition pattern classes: the smallest partition index of each")
+    lines.append("// distinct split of the block into three non-empty sets, in index order.")
+    lines.append("// 4x4: m1 | (m2 << 16) | (index << 32); 6x6: A = m1 | (index << 54), B = m2")
+    lines.append("// (m1 / m2: the texels in partitions 1 / 2).")
+    lines.append(f"constexpr int kPartition3Classes4x4Count = {len(t4)};")
+    lines.append(f"constexpr uint64_t kPartition3Classes4x4[{len(t4)}] = {{")
+    for i in range(0, len(t4), 4):
+        lines.append("    " + ", ".join(f"0x{m1 | (m2 << 16) | (sd << 32):012X}ull" for sd, m1, m2 in t4[i:i + 4]) + ",")
+    lines.append("};")
+    lines.append(f"constexpr int kPartition3Classes6x6Count = {len(t6)};")
+    lines.append(f"constexpr uint64_t kPartition3Classes6x6A[{len(t6)}] = {{")
+    for i in range(0, len(t6), 4):
+        lines.append("    " + ", ".join(f"0x{m1 | (sd << 54):016X}ull" for sd, m1, m2 in t6[i:i + 4]) + ",")
+    lines.append("};")
+    lines.append(f"constexpr uint64_t kPartition3Classes6x6B[{len(t6)}] = {{")
+    for i in range(0, len(t6), 4):
+        lines.append("    " + ", ".join(f"0x{m2:09X}ull" for sd, m1, m2 in t6[i:i + 4]) + ",")
     lines += ["};", "}  // namespace astc", ""]
     out = os.path.join(os.path.dirname(os.path.abspath(__file__)), "astc_partition_table.h")
     with open(out, "w") as fh:

@@ -111,6 +111,27 @@ def normal_map(h: int = 4096, w: int = 4096, seed: int = SEED_BASE + 2) -> np.nd
     return out
 
 
+def ui_shapes(h: int = 512, w: int = 512, seed: int = SEED_BASE + 5) -> np.ndarray:
+    """Flat-colour graphics (UI, sprites): a background and 400 hard-edged
+    rectangles and discs of random colours and sizes 2..40 px, A = 255.
+    Blocks where three colours meet are where three-partition blocks pay."""
+    rng = np.random.default_rng(seed)
+    out = np.empty((h, w, 4), np.uint8)
+    out[..., :3] = rng.integers(0, 256, 3)
+    out[..., 3] = 255
+    yy, xx = np.mgrid[0:h, 0:w]
+    for _ in range(400):
+        c = rng.integers(0, 256, 3)
+        y0, x0 = int(rng.integers(0, h)), int(rng.integers(0, w))
+        sh, sw = (int(v) for v in rng.integers(2, 40, 2))
+        if rng.random() < 0.5:
+            out[y0:y0 + sh, x0:x0 + sw, :3] = c
+        else:
+            r = max(sh, sw) / 2
+            out[(yy - y0) ** 2 + (xx - x0) ** 2 < r * r, :3] = c
+    return out
+
+
 WORKLOADS = {
     "4x4_rgb_512": dict(gen=rgb_noise, shape=(512, 512), block_dim=4, has_alpha=False,
                         is_normal=False, srgb=False, border=0),

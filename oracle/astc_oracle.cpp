@@ -547,12 +547,14 @@ void assemble_general(uint32_t wq, uint32_t cq, uint32_t cem, const uint32_t* ev
     assemble_fields(assemble_blockmode(wq) | ((cem & 0xF) << 13), 17, wq, cq, ev, nvals, sw, out);
 }
 
-// Two partitions sharing one CEM: mode [10:0], partition count - 1 = 1 at
-// [12:11], partition index [22:13], CEM field [28:23] = CEM << 2 (the low two
-// bits 00 mean "every partition uses this CEM"), endpoints from bit 29.
-void assemble_two_partitions(uint32_t wq, uint32_t cq, uint32_t cem, uint32_t seed, const uint32_t* ev,
-                             int nvals, const uint32_t* sw, uint8_t out[16]) {
-    const uint32_t head = assemble_blockmode(wq) | (1u << 11) | ((seed & 0x3FF) << 13) | ((cem & 0xF) << 25);
+// pcount (2 or 3) partitions sharing one CEM: mode [10:0], partition count -
+// 1 at [12:11], partition index [22:13], CEM field [28:23] = CEM << 2 (the
+// low two bits 00 mean "every partition uses this CEM"), endpoints from bit
+// 29, partition 0's first.
+void assemble_partitions(uint32_t pcount, uint32_t wq, uint32_t cq, uint32_t cem, uint32_t seed,
+                         const uint32_t* ev, int nvals, const uint32_t* sw, uint8_t out[16]) {
+    const uint32_t head = assemble_blockmode(wq) | ((pcount - 1) << 11) | ((seed & 0x3FF) << 13) |
+                          ((cem & 0xF) << 25);
     assemble_fields(head, 29, wq, cq, ev, nvals, sw, out);
 }
 
@@ -583,6 +585,13 @@ void assemble_dual_plane(uint32_t wq, uint32_t cq, uint32_t cem, uint32_t pc, co
 // Two-partition patterns (the spec's partition hash, defined with the
 // decoder below): bit i = texel i (row-major) lies in partition 1.
 const uint64_t* partition_masks(int dim);
+
+// Three-partition pattern classes of a block size: one per distinct way the
+// partition index splits the block's texels into three non-empty sets (two
+// indices that split alike up to the partitions' order are one class, kept
+// as the smaller index), in index order; m1 / m2 = texels in partitions 1 / 2.
+struct ThreeClass { int seed; uint64_t m1, m2; };
+const std::vector<ThreeClass>& three_partition_classes(int dim);
 
 inline int popcount64(uint64_t v) {
     int c = 0;
@@ -934,7 +943,7 @@ struct Pipe {
     // axis 2 fits both ways and searches from the fit whose fixed-mode block
     // has the smaller error (the PCA on ties).
     static void search(const T (*tex)[4], int dim, bool alpha, bool srgb, int axis, uint8_t out[16],
-                       int* chosen, uint32_t* best_err, uint32_t* fixed_err, bool partitions = false) {
+                       int* chosen, uint32_t* best_err, uint32_t* fixed_err, int partitions = 0) {
         const int nch = alpha ? 4 : 3;
         int tb[36][4];
         for (int i = 0; i < dim * dim; ++i)
@@ -986,7 +995,7 @@ struct Pipe {
                 std::memcpy(out, dblk, 16);
             }
         }
-        if (partitions) {
+        if (partitions >= 1) {
             // two partitions, split along the kept fit's fixed-mode endpoints
             int PE0[4], PE1[4];
             for (int c = 0; c < 4; ++c) { PE0[c] = (int)ep_q[2 * c]; PE1[c] = (int)ep_q[2 * c + 1]; }
@@ -997,6 +1006,17 @@ struct Pipe {
                 best = perr;
                 *chosen = pch;
                 std::memcpy(out, pblk, 16);
+            }
+        }
+        if (partitions >= 2 && best > 0) {
+            // three partitions (no candidate can beat an exact block)
+            uint8_t tblk[16];
+            int tch = -1;
+            const uint32_t terr = three_partitions(tex, tb, dim, alpha, srgb, tblk, &tch);
+            if (terr < best) {
+                best = terr;
+                *chosen = tch;
+                std::memcpy(out, tblk, 16);
             }
         }
         *best_err = best;
@@ -1142,8 +1162,169 @@ struct Pipe {
                         ev[p * nv + 2 * c + 1] = (uint32_t)sym1[p][c];
                     }
                 for (int g = 0; g < 16; ++g) sw[g] = (uint32_t)tbl.scramble[wq][q[g]];
-                assemble_two_partitions((uint32_t)wq, (uint32_t)cq, alpha ? 12u : 8u, (uint32_t)seed, ev, 2 * nv,
-                                        sw, out);
+                assemble_partitions(2, (uint32_t)wq, (uint32_t)cq, alpha ? 12u : 8u, (uint32_t)seed, ev, 2 * nv,
+                                    sw, out);
+            }
+        }
+        return best;
+    }
+
+    // ---- three partitions (quality 4) --------------------------------------
+    // Integer labels of the texels (rounded bytes, nch channels): k0 = the
+    // texel farthest from texel 0, k1 the one farthest from k0, k2 the one
+    // farthest from both (first on ties); every texel takes the nearest of
+    // the three (lowest on ties).  Returns false if a label is left empty.
+    static int byte_dist(const int* a, const int* b, int nch) {
+        int d = 0;
+        for (int c = 0; c < nch; ++c) d += (a[c] - b[c]) * (a[c] - b[c]);
+        return d;
+    }
+    static bool three_labels(const int (*tb)[4], int n, int nch, uint64_t L[3]) {
+        int k0 = 0, k1 = 0, k2 = 0, far = -1;
+        for (int i = 0; i < n; ++i) {
+            const int d = byte_dist(tb[i], tb[0], nch);
+            if (d > far) { far = d; k0 = i; }
+        }
+        far = -1;
+        for (int i = 0; i < n; ++i) {
+            const int d = byte_dist(tb[i], tb[k0], nch);
+            if (d > far) { far = d; k1 = i; }
+        }
+        far = -1;
+        for (int i = 0; i < n; ++i) {
+            const int d0 = byte_dist(tb[i], tb[k0], nch), d1 = byte_dist(tb[i], tb[k1], nch);
+            const int d = d0 < d1 ? d0 : d1;
+            if (d > far) { far = d; k2 = i; }
+        }
+        L[0] = L[1] = L[2] = 0;
+        for (int i = 0; i < n; ++i) {
+            const int a = byte_dist(tb[i], tb[k0], nch), b = byte_dist(tb[i], tb[k1], nch);
+            const int c = byte_dist(tb[i], tb[k2], nch);
+            L[(a <= b && a <= c) ? 0 : (b <= c ? 1 : 2)] |= 1ull << i;
+        }
+        return L[0] && L[1] && L[2];
+    }
+
+    // Texels of a pattern class that disagree with the labels under the best
+    // matching of labels to partitions.
+    static int three_mismatch(const uint64_t L[3], const ThreeClass& k, uint64_t full, int n) {
+        const uint64_t pm[3] = {full & ~(k.m1 | k.m2), k.m1, k.m2};
+        int M[3][3];
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b) M[a][b] = popcount64(L[a] & pm[b]);
+        static const int perm[6][3] = {{0, 1, 2}, {0, 2, 1}, {1, 0, 2}, {1, 2, 0}, {2, 0, 1}, {2, 1, 0}};
+        int most = 0;
+        for (const auto& q : perm) {
+            const int m = M[0][q[0]] + M[1][q[1]] + M[2][q[2]];
+            if (m > most) most = m;
+        }
+        return n - most;
+    }
+
+    // Three-partition candidates (RGB only: a block carries at most 18 colour
+    // endpoint integers, three RGBA partitions would need 24): the four
+    // pattern classes that best match the labels (fewest mismatches, then
+    // smallest index), each partition fitted on its own (fit_partition),
+    // every weight range whose endpoint range (18 values after the 29-bit
+    // header) is legal scored with each texel decoded on its partition.
+    // Returns the best error (UINT32_MAX if none) and its block; *chosen =
+    // 300 + 16 * rank + wq.
+    static uint32_t three_partitions(const T (*tex)[4], const int (*tb)[4], int dim, bool alpha, bool srgb,
+                                     uint8_t out[16], int* chosen) {
+        const Tables& tbl = tables();
+        const int n = dim * dim, nch = alpha ? 4 : 3, nv = alpha ? 8 : 6;
+        const uint64_t full = n == 64 ? ~0ull : ((1ull << n) - 1);
+        if (alpha) return UINT32_MAX;
+        uint64_t L[3];
+        if (!three_labels(tb, n, nch, L)) return UINT32_MAX;
+        uint32_t key[4] = {UINT32_MAX, UINT32_MAX, UINT32_MAX, UINT32_MAX};
+        const std::vector<ThreeClass>& cls = three_partition_classes(dim);
+        for (int c = 0; c < (int)cls.size(); ++c) {
+            uint32_t k = (uint32_t)three_mismatch(L, cls[c], full, n) << 16 | (uint32_t)c;
+            for (int r = 0; r < 4; ++r)
+                if (k < key[r]) std::swap(k, key[r]);
+        }
+        uint32_t best = UINT32_MAX;
+        for (int rank = 0; rank < 4; ++rank) {
+            if (key[rank] == UINT32_MAX) break;
+            const ThreeClass& pc = cls[key[rank] & 0xFFFF];
+            const uint64_t pm[3] = {full & ~(pc.m1 | pc.m2), pc.m1, pc.m2};
+            T pe0[3][4], pe1[3][4];
+            for (int p = 0; p < 3; ++p) fit_partition(tex, n, pm[p], alpha, pe0[p], pe1[p]);
+            for (int wq = QUANT_3; wq <= QUANT_32; ++wq) {
+                const int cq = endpoint_quant(wq, 3 * nv, 29);
+                if (cq < 0) continue;
+                int sym0[3][4], sym1[3][4], Q0[3][4], Q1[3][4];
+                for (int p = 0; p < 3; ++p) {
+                    for (int c = 0; c < 4; ++c) { sym0[p][c] = sym1[p][c] = 0; Q0[p][c] = Q1[p][c] = 255; }
+                    for (int c = 0; c < nch; ++c) {
+                        sym0[p][c] = nearest_color(cq, (int)P::rint(pe0[p][c]), &Q0[p][c]);
+                        sym1[p][c] = nearest_color(cq, (int)P::rint(pe1[p][c]), &Q1[p][c]);
+                    }
+                    if (Q1[p][0] + Q1[p][1] + Q1[p][2] < Q0[p][0] + Q0[p][1] + Q0[p][2])
+                        for (int c = 0; c < 4; ++c) {
+                            std::swap(sym0[p][c], sym1[p][c]);
+                            std::swap(Q0[p][c], Q1[p][c]);
+                        }
+                }
+                T pd[3][4], r[3];
+                bool flat[3];
+                for (int p = 0; p < 3; ++p) {
+                    for (int c = 0; c < 4; ++c) pd[p][c] = (T)(Q1[p][c] - Q0[p][c]);
+                    const T pdd = dot4(pd[p], pd[p]);
+                    flat[p] = pdd == 0;
+                    r[p] = flat[p] ? (T)0 : P::div(P::lit(1.0f, 1.0), pdd);
+                }
+                int part[36];
+                for (int i = 0; i < n; ++i) part[i] = ((pc.m1 >> i) & 1) ? 1 : ((pc.m2 >> i) & 1) ? 2 : 0;
+                T wt[36];
+                for (int i = 0; i < n; ++i) {
+                    const int p = part[i];
+                    if (flat[p]) { wt[i] = 0; continue; }
+                    T diff[4];
+                    for (int c = 0; c < 4; ++c) diff[c] = P::sub(tex[i][c], (T)Q0[p][c]);
+                    const T w = P::mul(dot4(diff, pd[p]), r[p]);
+                    wt[i] = P::min(P::max(w, (T)0), P::lit(1.0f, 1.0));
+                }
+                const uint32_t R = (uint32_t)kQuantLevels[wq] - 1;
+                uint32_t q[16];
+                for (int g = 0; g < 16; ++g) {
+                    T w = wt[g];
+                    if (dim == 6) {
+                        int idx[4]; T cw[4];
+                        grid_taps(g, idx, cw);
+                        w = P::mul(wt[idx[0]], cw[0]);
+                        w = P::mad(wt[idx[1]], cw[1], w);
+                        w = P::mad(wt[idx[2]], cw[2], w);
+                        w = P::mad(wt[idx[3]], cw[3], w);
+                    }
+                    const uint32_t v = (uint32_t)P::rint(P::mul(w, (T)R));
+                    q[g] = v > R ? R : v;
+                }
+                int wv[16];
+                trial_weights(wq, q, wv);
+                uint32_t err = 0;
+                for (int i = 0; i < n; ++i) {
+                    const int p = part[i];
+                    const int w = dim == 4 ? wv[i] : infill_6x6(wv, i % 6, i / 6);
+                    for (int c = 0; c < nch; ++c) {
+                        const int e = decode_channel(Q0[p][c], Q1[p][c], w, srgb) - tb[i][c];
+                        err += (uint32_t)(e * e);
+                    }
+                }
+                if (err < best) {
+                    best = err;
+                    *chosen = 300 + 16 * rank + wq;
+                    uint32_t ev[24], sw[16];
+                    for (int p = 0; p < 3; ++p)
+                        for (int c = 0; c < nv / 2; ++c) {
+                            ev[p * nv + 2 * c] = (uint32_t)sym0[p][c];
+                            ev[p * nv + 2 * c + 1] = (uint32_t)sym1[p][c];
+                        }
+                    for (int g = 0; g < 16; ++g) sw[g] = (uint32_t)tbl.scramble[wq][q[g]];
+                    assemble_partitions(3, (uint32_t)wq, (uint32_t)cq, alpha ? 12u : 8u, (uint32_t)pc.seed, ev,
+                                        3 * nv, sw, out);
+                }
             }
         }
         return best;
@@ -1307,7 +1488,7 @@ struct Pipe {
         if (o->block_dim != 4 && o->block_dim != 6) return -2;
         if (o->border != 0 && o->border != 1) return -3;
         if (o->axis != 0 && o->axis != 1) return -4;
-        if (o->quality < 0 || o->quality > 3) return -5;
+        if (o->quality < 0 || o->quality > 4) return -5;
         tables();
         const int dim = o->block_dim;
         const int nbx = (w + dim - 1) / dim, nby = (h + dim - 1) / dim;
@@ -1326,7 +1507,7 @@ struct Pipe {
                 int chosen;
                 uint32_t err, err_fixed;
                 search(tex, dim, o->has_alpha != 0, o->srgb != 0, o->quality >= 2 ? 2 : o->axis,
-                       out + 16 * b, &chosen, &err, &err_fixed, o->quality == 3);
+                       out + 16 * b, &chosen, &err, &err_fixed, o->quality >= 3 ? o->quality - 2 : 0);
                 continue;
             }
             uint32_t ep[8], qw[16];
@@ -1530,6 +1711,36 @@ const uint64_t* partition_masks(int dim) {
     };
     static const Masks masks;
     return masks.m[dim == 6 ? 1 : 0];
+}
+
+const std::vector<ThreeClass>& three_partition_classes(int dim) {
+    struct Classes {
+        std::vector<ThreeClass> c[2];
+        Classes() {
+            for (int d = 0; d < 2; ++d) {
+                const int dim = d ? 6 : 4, n = dim * dim;
+                std::vector<std::pair<uint64_t, uint64_t>> seen;
+                for (int s = 0; s < 1024; ++s) {
+                    int part[36], first[3] = {-1, -1, -1}, order = 0;
+                    uint64_t m[3] = {0, 0, 0}, cm[3] = {0, 0, 0};
+                    for (int i = 0; i < n; ++i) {
+                        part[i] = select_partition(s, i % dim, i / dim, 0, 3, n < 31);
+                        m[part[i]] |= 1ull << i;
+                        if (first[part[i]] < 0) first[part[i]] = order++;
+                        cm[first[part[i]]] |= 1ull << i;      // relabelled in order of first texel
+                    }
+                    if (!m[0] || !m[1] || !m[2]) continue;
+                    bool dup = false;
+                    for (const auto& q : seen) dup = dup || (q.first == cm[1] && q.second == cm[2]);
+                    if (dup) continue;
+                    seen.emplace_back(cm[1], cm[2]);
+                    c[d].push_back(ThreeClass{s, m[1], m[2]});
+                }
+            }
+        }
+    };
+    static const Classes cl;
+    return cl.c[dim == 6 ? 1 : 0];
 }
 
 void error_block(int bw, int bh, uint8_t* out) {
@@ -1760,6 +1971,18 @@ void oracle_grid_taps(int g, int idx[4], float wt[4]) {
     Pipe<F32>::grid_taps(g & 15, idx, wt);
 }
 
+int oracle_three_classes(int dim, int* seeds, uint64_t* m1, uint64_t* m2, int cap) {
+    if (dim != 4 && dim != 6) return -1;
+    const std::vector<ThreeClass>& cls = three_partition_classes(dim);
+    const int n = (int)cls.size();
+    for (int i = 0; i < n && i < cap; ++i) {
+        seeds[i] = cls[i].seed;
+        m1[i] = cls[i].m1;
+        m2[i] = cls[i].m2;
+    }
+    return n;
+}
+
 int oracle_endpoint_quant(int wq, int nvals) {
     if (nvals != 6 && nvals != 8) return -1;
     return endpoint_quant(wq, nvals);
@@ -1773,8 +1996,9 @@ int oracle_search_block_fp32(const float* texels, int block_dim, int has_alpha, 
     float tex[36][4];
     for (int i = 0; i < block_dim * block_dim; ++i)
         for (int c = 0; c < 4; ++c) tex[i][c] = texels[4 * i + c];
+    if (partitions < 0 || partitions > 2) return -1;
     Pipe<F32>::search(tex, block_dim, has_alpha != 0, srgb != 0, axis, out, chosen_wq, err, err_fixed,
-                      partitions != 0);
+                      partitions);
     return 0;
 }
 

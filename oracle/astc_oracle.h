@@ -53,7 +53,9 @@ typedef struct oracle_opts {
                         two-partition candidates (one partition pattern,
                         matched to the split of the kept fit, each
                         partition fitted on its own, every legal weight
-                        range scored)                                      */
+                        range scored); 4 = 3 plus three-partition
+                        candidates (the four pattern classes that best
+                        match an integer three-colour labelling)          */
 } oracle_opts;
 
 /* Encode a tightly packed RGBA8 image (row 0 first) into 16-byte blocks in
@@ -115,12 +117,20 @@ double oracle_flops_per_block(int block_dim, int has_alpha, int is_normal);
  * `nvals` endpoint values (6 = CEM 8, 8 = CEM 12), or -1 if the mode is
  * invalid. */
 int oracle_endpoint_quant(int wq, int nvals);
+/* The three-partition pattern classes of a block size (4 or 6): the smallest
+ * partition index of each distinct split of the block into three non-empty
+ * sets, in index order, with the texels of its partitions 1 and 2 (bit
+ * y * dim + x).  Writes up to cap entries; returns the class count. */
+int oracle_three_classes(int dim, int* seeds, uint64_t* m1, uint64_t* m2, int cap);
 /* Encode one block (texels: N*4 floats, 0..255, the fit space) in search
- * mode with FP32 arithmetic (axis 2: from the better of both fits; with
- * partitions, two-partition candidates as well).  *chosen_wq = weight quant
- * method of the block kept (-1 when the fixed-mode block was kept, 100 + wq
- * for a two-partition block), *err = the squared error of its decode against
- * the texels rounded to bytes, *err_fixed = the fixed-mode block's. */
+ * mode with FP32 arithmetic (axis 2: from the better of both fits, with
+ * dual-plane candidates; partitions 1: two-partition candidates as well, 2:
+ * two- and three-partition candidates).  *chosen_wq = weight quant method of
+ * the block kept (-1 when the fixed-mode block was kept, 100 + wq for a
+ * two-partition block, 200 + 16 * plane-2 channel + wq for a dual-plane
+ * block, 300 + 16 * class rank + wq for a three-partition block), *err = the
+ * squared error of its decode against the texels rounded to bytes,
+ * *err_fixed = the fixed-mode block's. */
 int oracle_search_block_fp32(const float* texels, int block_dim, int has_alpha, int srgb, int axis,
                              int partitions, uint8_t out[16], int* chosen_wq, uint32_t* err,
                              uint32_t* err_fixed);

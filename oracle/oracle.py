@@ -49,6 +49,7 @@ def lib() -> ctypes.CDLL:
             L.oracle_encode_block_fp32.argtypes = [vp, ip, ip, vp, vp, vp]
             L.oracle_assemble_symbolic.argtypes = [vp, vp, ip, vp]
             L.oracle_ise_encode.argtypes = [ip, ip, vp, vp]
+            L.oracle_three_classes.argtypes = [ip, vp, vp, vp, ip]
             L.oracle_ise_decode.argtypes = [ip, ip, vp, ip, vp]
             L.oracle_ise_bits.argtypes = [ip, ip]
             for n in ("oracle_table_trits", "oracle_table_quints", "oracle_table_btq",
@@ -82,7 +83,7 @@ def encode(rgba: np.ndarray, block_dim: int = 4, has_alpha: bool = False, is_nor
     axis 1 = max_accumulation_pixel_direction instead of the PCA; quality 1 =
     search over the single-partition weight/endpoint ranges; 2 = the search
     from the better of both fits plus dual-plane blocks; 3 = 2 plus
-    two-partition blocks."""
+    two-partition blocks; 4 = 3 plus three-partition blocks."""
     a = np.ascontiguousarray(rgba, dtype=np.uint8)
     h, w = a.shape[:2]
     nb = ((w + block_dim - 1) // block_dim) * ((h + block_dim - 1) // block_dim)
@@ -191,13 +192,27 @@ def endpoint_quant(wq: int, nvals: int) -> int:
     return int(lib().oracle_endpoint_quant(wq, nvals))
 
 
+def three_classes(dim: int) -> list:
+    """[(seed, m1, m2)] -- the oracle's three-partition pattern classes."""
+    seeds = np.zeros(1024, np.int32)
+    m1 = np.zeros(1024, np.uint64)
+    m2 = np.zeros(1024, np.uint64)
+    n = lib().oracle_three_classes(dim, seeds.ctypes.data, m1.ctypes.data, m2.ctypes.data, 1024)
+    assert n > 0
+    return [(int(seeds[i]), int(m1[i]), int(m2[i])) for i in range(n)]
+
+
 def search_block(texels: np.ndarray, block_dim: int, has_alpha: bool, srgb: bool = False, axis: int = 0,
-                 partitions: bool = False):
-    """Search-mode FP32 encode of one block of fit-space texels (N x 4 floats).
+                 partitions: int = 0):
+    """Search-mode FP32 encode of one block of fit-space texels (N x 4 floats);
+    partitions: 0 = single partition only, 1 = also two-partition blocks, 2 =
+    also three-partition blocks.
 
     Returns (block bytes, chosen weight quant method -- -1 for the fixed-mode
-    block, 100 + wq for a two-partition block --, the squared error of its
-    decode against the texels rounded to bytes, the fixed-mode block's)."""
+    block, 100 + wq for a two-partition block, 200 + 16 * pc + wq for a
+    dual-plane block, 300 + 16 * rank + wq for a three-partition block --, the
+    squared error of its decode against the texels rounded to bytes, the
+    fixed-mode block's)."""
     t = np.ascontiguousarray(texels, dtype=np.float32).reshape(-1)
     out = np.zeros(16, np.uint8)
     wq = ctypes.c_int(0)

@@ -1,9 +1,11 @@
-"""The oracle's two modes beyond the reference's fixed pipeline.
+"""The oracle's modes beyond the reference's fixed pipeline.
 
 * axis = 1: max_accumulation_pixel_direction (ASTC_Encode.hlsl:170-227), the
   endpoint fit the reference defines but leaves commented out at line 515;
 * quality = 1: the search the reference sketches as choose_best_quantmethod
-  (524-526): the fixed-mode block plus every single-partition 4x4-grid mode.
+  (524-526): the fixed-mode block plus every single-partition 4x4-grid mode;
+* quality 2-4: the search from the better of both fits with dual-plane
+  blocks, then two- and three-partition blocks.
 
 The reference never runs either, so there is no reference output to pin them
 to; these tests pin them to the ASTC rules instead: the endpoint range is the
@@ -274,11 +276,69 @@ def test_dual_plane_normal_map_gain(oracle):
     assert sse(two) * 2 < sse(one)
 
 
+def _three_colour_block(rng, dim):
+    """Three flat colours in three regions cut by two straight edges, with
+    +-2 noise: two partitions cannot hold them, three can."""
+    cols = rng.integers(0, 256, (3, 4)).astype(np.int64)
+    cols[:, 3] = 255
+    yy, xx = np.mgrid[0:dim, 0:dim]
+    a = xx * int(rng.integers(1, 4)) + yy * int(rng.integers(-2, 3)) >= int(rng.integers(2, 2 * dim))
+    b = yy * int(rng.integers(1, 4)) - xx >= int(rng.integers(0, dim))
+    region = np.where(a, 0, np.where(b, 1, 2))
+    px = cols[region] + rng.integers(-2, 3, (dim, dim, 4)) * np.array([1, 1, 1, 0])
+    return np.clip(px, 0, 255).astype(np.uint8)
+
+
+@pytest.mark.parametrize("dim", [4, 6])
+@pytest.mark.parametrize("alpha", [False, True])
+@pytest.mark.parametrize("srgb", [False, True])
+def test_three_partitions_score_match_the_spec_decode(oracle, dim, alpha, srgb):
+    """Quality 4's three-partition blocks (RGB only: three RGBA partitions
+    would need 24 colour endpoint integers, above the format's 18): three
+    partitions in the header, one shared CEM, exact scored error, never worse
+    than quality 3."""
+    rng = np.random.default_rng(700 + 10 * dim + 2 * alpha + srgb)
+    three = 0
+    for trial in range(60):
+        px = _three_colour_block(rng, dim) if trial % 4 else _random_block(rng, dim, trial % 4)
+        tex = _fit_texels(oracle, px, srgb)
+        blk, wq, err, _ = oracle.search_block(tex, dim, alpha, srgb, 2, partitions=2)
+        _, _, err_two, _ = oracle.search_block(tex, dim, alpha, srgb, 2, partitions=1)
+        assert err <= err_two
+        assert _decoded_error(oracle, blk, tex, dim, alpha, srgb) == err
+        if 300 <= wq < 400:
+            three += 1
+            word = int.from_bytes(blk[:4].tobytes(), "little")
+            assert (word >> 11) & 3 == 2                       # three partitions
+            assert (word >> 23) & 3 == 0 and (word >> 25) & 0xF == 8
+    if alpha:
+        assert three == 0
+    else:
+        assert three >= 6, three
+
+
+@pytest.mark.parametrize("dim", [4, 6])
+def test_three_partitions_image(oracle, dim):
+    """Flat-colour graphics: quality 4 decodes cleanly and beats quality 3;
+    RGBA input keeps quality 3's blocks."""
+    rgba = synth.ui_shapes(96, 96, seed=21)
+    q3 = oracle.encode(rgba, block_dim=dim, quality=3)
+    q4 = oracle.encode(rgba, block_dim=dim, quality=4)
+    d3, e3 = oracle.decode(q3, 96, 96, dim)
+    d4, e4 = oracle.decode(q4, 96, 96, dim)
+    assert e3 == 0 and e4 == 0
+    sse = lambda d: int(((d[..., :3].astype(np.int64) - rgba[..., :3]) ** 2).sum())  # noqa: E731
+    assert sse(d4) < sse(d3)
+    assert (((q4.view("<u4")[:, 0] >> 11) & 3) == 2).any()
+    a3 = oracle.encode(rgba, block_dim=dim, has_alpha=True, quality=3)
+    assert np.array_equal(oracle.encode(rgba, block_dim=dim, has_alpha=True, quality=4), a3)
+
+
 def test_bad_axis_and_quality_rejected(oracle):
     with pytest.raises(ValueError):
         oracle.encode(np.zeros((4, 4, 4), np.uint8), axis=2)
     with pytest.raises(ValueError):
-        oracle.encode(np.zeros((4, 4, 4), np.uint8), quality=4)
+        oracle.encode(np.zeros((4, 4, 4), np.uint8), quality=5)
 
 
 def test_thorough_recovers_alpha_cutouts(oracle):

@@ -1,8 +1,10 @@
-"""The committed two-partition pattern table (csrc/astc_partition_table.h) is
+"""The committed partition pattern tables (csrc/astc_partition_table.h) are
 what the generator computes, and what the oracle's spec decoder does: a
 two-partition block with partition 0 black and partition 1 white (all weights
 zero) decodes to exactly the table's mask, for every partition index and
-both block sizes."""
+both block sizes; the three-partition class lists equal the oracle's, are
+distinct splits into three non-empty sets, and a three-partition block with
+partitions black / grey / white decodes to exactly each class's sets."""
 import os
 import re
 import sys
@@ -99,3 +101,61 @@ def test_table_matches_spec_decoder(oracle, dim):
         assert set(np.unique(rgba[:, 0]).tolist()) <= {0, 255}
         mask = sum(1 << i for i in range(dim * dim) if rgba[i, 0] == 255)
         assert mask == table[seed], seed
+
+
+def _header_three_classes():
+    text = open(os.path.join(CSRC, "astc_partition_table.h")).read()
+
+    def arr(name):
+        body = re.search(name + r"\[\d+\] = \{(.*?)\};", text, re.S).group(1)
+        return [int(v.rstrip("ul"), 16) for v in re.findall(r"0x[0-9A-Fa-f]+u?l*", body)]
+
+    c4 = [(v >> 32, v & 0xFFFF, (v >> 16) & 0xFFFF) for v in arr("kPartition3Classes4x4")]
+    a, b = arr("kPartition3Classes6x6A"), arr("kPartition3Classes6x6B")
+    c6 = [(x >> 54, x & ((1 << 36) - 1), y) for x, y in zip(a, b)]
+    return c4, c6
+
+
+def test_three_partition_classes_match_generator_and_oracle(oracle):
+    sys.path.insert(0, CSRC)
+    try:
+        import gen_partition_table as gen
+    finally:
+        sys.path.remove(CSRC)
+    c4, c6 = _header_three_classes()
+    assert c4 == gen.classes3(4) and c6 == gen.classes3(6)
+    assert c4 == oracle.three_classes(4) and c6 == oracle.three_classes(6)
+    for dim, cls in ((4, c4), (6, c6)):
+        full = (1 << (dim * dim)) - 1
+        seeds = [s for s, _, _ in cls]
+        assert seeds == sorted(seeds)
+        for s, m1, m2 in cls:
+            assert m1 and m2 and not (m1 & m2) and (full & ~(m1 | m2))
+        # distinct as splits: no two classes are the same three sets
+        keys = {frozenset([m1, m2, full & ~(m1 | m2)]) for _, m1, m2 in cls}
+        assert len(keys) == len(cls)
+
+
+def _three_partition_block(seed: int) -> np.ndarray:
+    # 4x4 weight grid, QUANT_3 weights (26 bits, all zero), 3 partitions, CEM 8
+    # for all; 18 endpoint values of QUANT_16 (4 bits each) from bit 29:
+    # partition 0 all 0 (black), partition 1 all 8 (136), partition 2 all 15 (255)
+    r = 3
+    mode = ((r >> 1) & 3) | ((r & 1) << 4) | (2 << 5)
+    v = mode | (2 << 11) | (seed << 13) | ((8 << 2) << 23)
+    for i in range(6, 18):
+        v |= (8 if i < 12 else 15) << (29 + 4 * i)
+    return np.frombuffer(v.to_bytes(16, "little"), np.uint8).copy()
+
+
+@pytest.mark.parametrize("dim", [4, 6])
+def test_three_partition_classes_match_spec_decoder(oracle, dim):
+    c4, c6 = _header_three_classes()
+    for seed, m1, m2 in (c4 if dim == 4 else c6):
+        rgba, err = oracle.decode_block(_three_partition_block(seed), dim, dim)
+        assert err == 0
+        r = rgba.reshape(-1, 4)[:, 0]
+        assert set(np.unique(r).tolist()) <= {0, 136, 255}
+        got1 = sum(1 << i for i in range(dim * dim) if r[i] == 136)
+        got2 = sum(1 << i for i in range(dim * dim) if r[i] == 255)
+        assert (got1, got2) == (m1, m2), seed
