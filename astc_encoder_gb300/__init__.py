@@ -69,6 +69,7 @@ class Quality(enum.IntEnum):
     SEARCH = 1              # every single-partition 4x4-grid mode, least decoded error
     THOROUGH = 2            # SEARCH from the better of the PCA and max-accumulation fits, plus dual-plane blocks
     PARTITIONS = 3          # THOROUGH plus two-partition blocks
+    THREE_PARTITIONS = 4    # PARTITIONS plus three-partition blocks (RGB input)
 
 
 class AstcError(RuntimeError):

@@ -37,6 +37,7 @@ LIB_SOURCES = [
     ("astc_encode_search.cu", ["--fmad=false"]),
     ("astc_encode_thorough.cu", ["--fmad=false"]),
     ("astc_encode_partitions.cu", ["--fmad=false"]),
+    ("astc_encode_three.cu", ["--fmad=false"]),
     ("astc_batch.cu", ["--fmad=false"]),
     ("astc_mips.cu", []),
     ("astc_server.cu", []),
@@ -50,7 +51,7 @@ CLI_SOURCES = [
     ("image_load.cpp", []),
 ]
 HEADERS = ["astc_internal.h", "astc_tables.h", "astc_ise.h", "astc_block_common.cuh", "astc_pipeline_fp32.cuh",
-           "astc_pipeline_h2.cuh", "astc_pipeline_search.cuh", "astc_pipeline_dual.cuh", "astc_pipeline_partition.cuh", "astc_search_kernel.cuh",
+           "astc_pipeline_h2.cuh", "astc_pipeline_search.cuh", "astc_pipeline_dual.cuh", "astc_pipeline_partition.cuh", "astc_pipeline_partition3.cuh", "astc_search_kernel.cuh",
            "astc_partition_table.h", "astc_srgb_table.h", "image_load.h"]
 
 

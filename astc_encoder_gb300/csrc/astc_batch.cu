@@ -384,7 +384,7 @@ astc_status astc_batch_encode_quality(astc_batch* b, const astc_batch_item* in, 
                                       int quality, void* stream) {
     if (quality == ASTC_QUALITY_FAST) return astc_batch_encode(b, in, count, precision, stream);
     if (!b || (!in && count > 0)) return set_error(ASTC_ERR_INVALID_ARG, "NULL argument");
-    if (quality < ASTC_QUALITY_FAST || quality > ASTC_QUALITY_PARTITIONS)
+    if (quality < ASTC_QUALITY_FAST || quality > ASTC_QUALITY_THREE_PARTITIONS)
         return set_error(ASTC_ERR_INVALID_ARG, "bad quality");
     if (precision != ASTC_PRECISION_FP32)
         return set_error(ASTC_ERR_UNSUPPORTED, "the quality modes are FP32 only");

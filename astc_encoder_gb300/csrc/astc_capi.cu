@@ -203,7 +203,7 @@ astc_status validate_opts(const astc_opts* o, int w, int h) {
         return set_error(ASTC_ERR_INVALID_ARG, "memory must be ASTC_MEMORY_HOST or ASTC_MEMORY_DEVICE");
     if (o->axis != ASTC_AXIS_PCA && o->axis != ASTC_AXIS_MAX_ACCUMULATION)
         return set_error(ASTC_ERR_INVALID_ARG, "axis must be ASTC_AXIS_PCA or ASTC_AXIS_MAX_ACCUMULATION");
-    if (o->quality < ASTC_QUALITY_FAST || o->quality > ASTC_QUALITY_PARTITIONS)
+    if (o->quality < ASTC_QUALITY_FAST || o->quality > ASTC_QUALITY_THREE_PARTITIONS)
         return set_error(ASTC_ERR_INVALID_ARG,
                          "quality must be ASTC_QUALITY_FAST, _SEARCH, _THOROUGH or _PARTITIONS");
     if (o->precision == ASTC_PRECISION_HALF2 && (o->axis != ASTC_AXIS_PCA || o->quality != ASTC_QUALITY_FAST))

@@ -22,6 +22,7 @@
 //                      max_accumulation_pixel_direction instead of the PCA
 //   --thorough         --search from the better of the two fits
 //   --partitions       --thorough plus two-partition blocks
+//   --three-partitions --partitions plus three-partition blocks (RGB input)
 //   -o PATH            output path
 //   --dump-rgba PATH   write the loaded (flipped) RGBA image as PAM and exit
 //                      without encoding (no GPU needed)
@@ -46,6 +47,7 @@ std::string strip_file_extension(const std::string& path) {
 int usage() {
     std::cout << "usage: astc_cs_enc input_texture [-4x4|-6x6] [-alpha] [-norm] [-srgb]"
                  " [--clamp] [--half2] [--search] [--max-accumulation] [--thorough] [--partitions]"
+                 " [--three-partitions]"
                  " [-o out.astc]"
                  " [--dump-rgba out.pam]" << std::endl;
     return -1;
@@ -60,7 +62,7 @@ int main(int argc, char** argv) {
     }
     const std::string src = argv[1];
     bool is4x4 = true, alpha = false, norm = false, srgb = false, clamp = false, half2 = false;
-    bool search = false, max_acc = false, thorough = false, partitions = false;
+    bool search = false, max_acc = false, thorough = false, partitions = false, three = false;
     std::string out_path, dump_path;
     for (int i = 2; i < argc; ++i) {
         const std::string a = argv[i];
@@ -75,6 +77,7 @@ int main(int argc, char** argv) {
         else if (a == "--max-accumulation") max_acc = true;
         else if (a == "--thorough") thorough = true;
         else if (a == "--partitions") partitions = true;
+        else if (a == "--three-partitions") three = true;
         else if (a == "-o" && i + 1 < argc) out_path = argv[++i];
         else if (a == "--dump-rgba" && i + 1 < argc) dump_path = argv[++i];
         else std::cerr << "ignoring unknown argument: " << a << std::endl;
@@ -110,7 +113,8 @@ int main(int argc, char** argv) {
     o.srgb = srgb && !norm;                                     // main.cpp:214
     o.border = clamp ? ASTC_BORDER_CLAMP : ASTC_BORDER_ZERO;
     o.precision = half2 ? ASTC_PRECISION_HALF2 : ASTC_PRECISION_FP32;
-    o.quality = partitions ? ASTC_QUALITY_PARTITIONS
+    o.quality = three ? ASTC_QUALITY_THREE_PARTITIONS
+                : partitions ? ASTC_QUALITY_PARTITIONS
                 : thorough ? ASTC_QUALITY_THOROUGH : (search ? ASTC_QUALITY_SEARCH : ASTC_QUALITY_FAST);
     o.axis = max_acc ? ASTC_AXIS_MAX_ACCUMULATION : ASTC_AXIS_PCA;
     std::vector<uint8_t> blocks(astc_encoded_size(img.width, img.height, o.block_dim));

@@ -10,6 +10,7 @@ namespace astc {
 cudaError_t launch_encode_search(const EncodeJob& j, cudaStream_t stream) {
     if (j.quality == ASTC_QUALITY_THOROUGH) return launch_encode_thorough(j, stream);
     if (j.quality == ASTC_QUALITY_PARTITIONS) return launch_encode_partitions(j, stream);
+    if (j.quality == ASTC_QUALITY_THREE_PARTITIONS) return launch_encode_three(j, stream);
     return launch_search_kernels<0>(j, stream);
 }
 

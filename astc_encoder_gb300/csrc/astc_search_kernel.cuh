@@ -14,7 +14,10 @@
 //            whose fixed-mode block decodes with the smaller error (the
 //            PCA on ties);
 //   quality = ASTC_QUALITY_PARTITIONS: THOROUGH plus two-partition
-//            candidates (astc_pipeline_partition.cuh; astc_encode_partitions.cu).
+//            candidates (astc_pipeline_partition.cuh; astc_encode_partitions.cu);
+//   quality = ASTC_QUALITY_THREE_PARTITIONS: PARTITIONS plus three-partition
+//            candidates for RGB blocks (astc_pipeline_partition3.cuh;
+//            astc_encode_three.cu).
 // One thread encodes one block.  Texels stay packed (one register each) and
 // are re-decoded per pass, which keeps the 36-texel 6x6 search in registers.
 // Compile including units with --fmad=false: blocks are bit-identical to the
@@ -26,6 +29,7 @@
 #include "astc_internal.h"
 #include "astc_pipeline_dual.cuh"
 #include "astc_pipeline_partition.cuh"
+#include "astc_pipeline_partition3.cuh"
 
 namespace astc {
 namespace {
@@ -45,6 +49,16 @@ constexpr PartitionClasses make_partition_classes() {
     return p;
 }
 __device__ const PartitionClasses g_classes = make_partition_classes();
+constexpr Partition3Classes make_partition3_classes() {
+    Partition3Classes p{};
+    for (int i = 0; i < kPartition3Classes4x4Count; ++i) p.c4[i] = kPartition3Classes4x4[i];
+    for (int i = 0; i < kPartition3Classes6x6Count; ++i) {
+        p.c6a[i] = kPartition3Classes6x6A[i];
+        p.c6b[i] = kPartition3Classes6x6B[i];
+    }
+    return p;
+}
+__device__ const Partition3Classes g_classes3 = make_partition3_classes();
 
 struct SearchLaunch {
     TextureView tex;
@@ -64,6 +78,18 @@ __device__ __forceinline__ void load_dual_smem(DualSmem& ds) {
     if (tid < 12) {
         ds.cq[tid] = g_search.cq[2][ALPHA][tid];
         ds.slot[tid] = g_search.slot[2][ALPHA][tid];
+    }
+}
+
+__device__ __forceinline__ void load_part3_smem(Part3Smem& p3) {
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const uint32_t* src = reinterpret_cast<const uint32_t*>(&g_search.color[3][0][0][0]);
+    uint32_t* dst = reinterpret_cast<uint32_t*>(&p3.color[0][0]);
+    const int words = g_search.nslots[3][0] * 128;
+    for (int i = tid; i < words; i += nt) dst[i] = src[i];
+    if (tid < 12) {
+        p3.cq[tid] = g_search.cq[3][0][tid];
+        p3.slot[tid] = g_search.slot[3][0][tid];
     }
 }
 
@@ -170,17 +196,20 @@ __device__ __forceinline__ void pick_fit(const uint32_t (&tw)[DIM * DIM], const 
 
 // MODE 0: fixed mode (max-accumulation axis) or SEARCH; 1: THOROUGH (both
 // fits, the search, dual-plane candidates); 2: THOROUGH plus two-partition
-// candidates.
+// candidates; 3 (RGB only): 2 plus three-partition candidates.
 template <int DIM, bool ALPHA, bool NORMAL, bool SRGB, int MODE>
 __global__ void __launch_bounds__(kSearchThreads, 3) astc_encode_blocks_search(const SearchLaunch p) {
     constexpr int N = DIM * DIM;
     constexpr bool thorough = MODE >= 1;
     __shared__ SearchSmem sm;
-    __shared__ typename std::conditional<MODE == 2, PartSmem, char>::type pm;
+    static_assert(MODE != 3 || !ALPHA, "three RGBA partitions exceed the format's 18 endpoint values");
+    __shared__ typename std::conditional<(MODE >= 2), PartSmem, char>::type pm;
     __shared__ typename std::conditional<(MODE >= 1), DualSmem, char>::type ds;
+    __shared__ typename std::conditional<MODE == 3, Part3Smem, char>::type p3;
     load_search_smem<ALPHA, SRGB>(sm);
     if constexpr (MODE >= 1) load_dual_smem<ALPHA>(ds);
-    if constexpr (MODE == 2) load_partition_smem<ALPHA>(pm, DIM);
+    if constexpr (MODE >= 2) load_partition_smem<ALPHA>(pm, DIM);
+    if constexpr (MODE == 3) load_part3_smem(p3);
     __syncthreads();
     const long long b = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= p.nblocks) return;
@@ -227,7 +256,7 @@ __global__ void __launch_bounds__(kSearchThreads, 3) astc_encode_blocks_search(c
         if constexpr (thorough)
             blk = dual_plane_block<DIM, ALPHA, SRGB>(st, grid, tw, BlockError<DIM, ALPHA, SRGB>::target_sq(tw), err,
                                                      blk, sm, ds);
-        if constexpr (MODE == 2) {
+        if constexpr (MODE >= 2) {
             // the partition candidates' per-texel weights, [texel][thread],
             // after the grid colours: a region of their own, since their float
             // columns would cross other threads' float4 grid columns (other
@@ -235,6 +264,10 @@ __global__ void __launch_bounds__(kSearchThreads, 3) astc_encode_blocks_search(c
             SharedFloats<36> tws{reinterpret_cast<float*>(s_grid + 16 * blockDim.x) + threadIdx.x, (int)blockDim.x};
             blk = two_partition_block<DIM, ALPHA, SRGB>(st, tw, BlockError<DIM, ALPHA, SRGB>::target_sq(tw), q0,
                                                         q1, err, blk, sm, pm, tws);
+            if constexpr (MODE == 3)
+                if (err != 0)
+                    blk = three_partition_block<DIM, SRGB>(st, tw, BlockError<DIM, ALPHA, SRGB>::target_sq(tw), err,
+                                                           blk, sm, p3, g_classes3, tws);
         }
     } else {
         RegTexels<16> grid;
@@ -251,10 +284,14 @@ __global__ void __launch_bounds__(kSearchThreads, 3) astc_encode_blocks_search(c
         if constexpr (thorough)
             blk = dual_plane_block<DIM, ALPHA, SRGB>(st, grid, tw, BlockError<DIM, ALPHA, SRGB>::target_sq(tw), err,
                                                      blk, sm, ds);
-        if constexpr (MODE == 2) {
+        if constexpr (MODE >= 2) {
             char none = 0;
             blk = two_partition_block<DIM, ALPHA, SRGB>(st, tw, BlockError<DIM, ALPHA, SRGB>::target_sq(tw), q0,
                                                         q1, err, blk, sm, pm, none);
+            if constexpr (MODE == 3)
+                if (err != 0)
+                    blk = three_partition_block<DIM, SRGB>(st, tw, BlockError<DIM, ALPHA, SRGB>::target_sq(tw), err,
+                                                           blk, sm, p3, g_classes3, none);
         }
     }
     p.out[b] = blk;
@@ -263,8 +300,8 @@ __global__ void __launch_bounds__(kSearchThreads, 3) astc_encode_blocks_search(c
 template <int DIM, bool ALPHA, bool NORMAL, bool SRGB, int MODE>
 cudaError_t launch_t(const SearchLaunch& p, cudaStream_t s) {
     const long long grid = (p.nblocks + kSearchThreads - 1) / kSearchThreads;
-    // 6x6: the grid colours, and for two partitions their per-texel weights
-    const size_t per_thread = 16 * sizeof(float4) + (MODE == 2 ? 36 * sizeof(float) : 0);
+    // 6x6: the grid colours, and for partitions their per-texel weights
+    const size_t per_thread = 16 * sizeof(float4) + (MODE >= 2 ? 36 * sizeof(float) : 0);
     const size_t smem = (DIM == 6 && p.search) ? per_thread * kSearchThreads : 0;
     auto* kernel = astc_encode_blocks_search<DIM, ALPHA, NORMAL, SRGB, MODE>;
     if (smem) {
@@ -295,7 +332,9 @@ cudaError_t launch_alpha(const SearchLaunch& p, bool alpha, bool normal, bool sr
                  : launch_norm<MODE, DIM, false>(p, normal, srgb, s);
 }
 
-template <int MODE>
+// RGB_ONLY: instantiate the kernels without alpha only (the caller routes
+// alpha elsewhere).
+template <int MODE, bool RGB_ONLY = false>
 cudaError_t launch_search_kernels(const EncodeJob& j, cudaStream_t stream) {
     SearchLaunch p;
     p.tex = make_view(j);
@@ -304,8 +343,15 @@ cudaError_t launch_search_kernels(const EncodeJob& j, cudaStream_t stream) {
     p.axis = j.axis;
     p.search = j.quality == ASTC_QUALITY_FAST ? 0 : 1;
     const bool alpha = j.has_alpha != 0, normal = j.is_normal != 0, srgb = j.srgb != 0;
-    const cudaError_t e = j.block_dim == 4 ? launch_alpha<MODE, 4>(p, alpha, normal, srgb, stream)
-                                           : launch_alpha<MODE, 6>(p, alpha, normal, srgb, stream);
+    cudaError_t e;
+    if constexpr (RGB_ONLY) {
+        if (alpha) return cudaErrorInvalidValue;
+        e = j.block_dim == 4 ? launch_norm<MODE, 4, false>(p, normal, srgb, stream)
+                             : launch_norm<MODE, 6, false>(p, normal, srgb, stream);
+    } else {
+        e = j.block_dim == 4 ? launch_alpha<MODE, 4>(p, alpha, normal, srgb, stream)
+                             : launch_alpha<MODE, 6>(p, alpha, normal, srgb, stream);
+    }
     if (e == cudaSuccess) count_launches(1);
     return e;
 }

@@ -287,7 +287,7 @@ astc_status astc_server_create(const astc_server_config* cfg, astc_server** out)
         return set_error(ASTC_ERR_INVALID_ARG, "bad precision");
     if (cfg->mode != ASTC_SERVE_BATCHED && cfg->mode != ASTC_SERVE_PER_REQUEST)
         return set_error(ASTC_ERR_INVALID_ARG, "bad mode");
-    if (cfg->quality < ASTC_QUALITY_FAST || cfg->quality > ASTC_QUALITY_PARTITIONS)
+    if (cfg->quality < ASTC_QUALITY_FAST || cfg->quality > ASTC_QUALITY_THREE_PARTITIONS)
         return set_error(ASTC_ERR_INVALID_ARG, "bad quality");
     if (cfg->quality != ASTC_QUALITY_FAST && cfg->precision != ASTC_PRECISION_FP32)
         return set_error(ASTC_ERR_UNSUPPORTED, "the quality modes are FP32 only");

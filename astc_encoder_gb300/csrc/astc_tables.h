@@ -231,12 +231,12 @@ constexpr ASTC_HD uint32_t blockmode_4x4_grid(int weight_quant) {
 // ---------------------------------------------------------------------------
 // Endpoint quant method of weight quant method wq with nvals endpoint values:
 // the decoder takes the largest range whose ISE fits between the header (17
-// bits for one partition, 29 for two sharing one CEM, 19 for one dual-plane
-// partition: its 2-bit plane selector sits below the weights) and the
-// nweights weights (32 for dual plane); the mode is illegal outside 24..96
-// weight bits or below QUANT_6.
+// bits for one partition, 29 for two or three sharing one CEM, 19 for one
+// dual-plane partition: its 2-bit plane selector sits below the weights) and
+// the nweights weights (32 for dual plane); the mode is illegal outside 24..96
+// weight bits, below QUANT_6, or above 18 endpoint values.
 constexpr ASTC_HD int endpoint_quant_for(int wq, int nvals, int header_bits = 17, int nweights = 16) {
-    if (wq < kQuant2 || wq > kQuant32) return -1;
+    if (wq < kQuant2 || wq > kQuant32 || nvals > 18) return -1;
     const int wbits = ise_bit_count(wq, nweights);
     if (wbits < 24 || wbits > 96) return -1;
     const int avail = 128 - header_bits - wbits;
@@ -249,26 +249,28 @@ struct SearchTables {
     // (unquantised << 8) | symbol of the colour value nearest each byte
     // (ties: the smaller value), per endpoint range used below QUANT_256;
     // kind 0 = one partition (6 / 8 values), 1 = two partitions (12 / 16
-    // values), 2 = one dual-plane partition (6 / 8 values, 32 weights)
-    uint16_t color[3][2][8][256];  // [kind][alpha][slot][byte]
-    int8_t slot[3][2][12];         // [kind][alpha][wq] -> slot, -1 = QUANT_256
-    int8_t cq[3][2][12];           // [kind][alpha][wq] -> endpoint quant method
+    // values), 2 = one dual-plane partition (6 / 8 values, 32 weights), 3 =
+    // three partitions (18 values; none with alpha: 24 exceed the format's 18)
+    uint16_t color[4][2][8][256];  // [kind][alpha][slot][byte]
+    int8_t slot[4][2][12];         // [kind][alpha][wq] -> slot, -1 = QUANT_256
+    int8_t cq[4][2][12];           // [kind][alpha][wq] -> endpoint quant method
     uint8_t wval[12][32];          // [wq][value-order index] -> weight 0..64
     uint8_t scramble[12][32];      // [wq][value-order index] -> ISE symbol
     uint8_t trit_pack[256];
     uint8_t quint_pack[128];
-    int nslots[3][2];              // [kind][alpha] rows of color in use
+    int nslots[4][2];              // [kind][alpha] rows of color in use
 };
 
 constexpr SearchTables make_search_tables() {
     SearchTables s{};
     const IseTables t = make_ise_tables();
-    for (int pt = 0; pt < 3; ++pt)
+    for (int pt = 0; pt < 4; ++pt)
     for (int a = 0; a < 2; ++a) {
         int nslots = 0;
         for (int wq = 0; wq < 12; ++wq) {
+            const int parts = pt == 3 ? 3 : pt == 1 ? 2 : 1;
             const int cq = pt == 2 ? endpoint_quant_for(wq, a ? 8 : 6, 19, 32)
-                                   : endpoint_quant_for(wq, (a ? 8 : 6) * (pt + 1), pt ? 29 : 17);
+                                   : endpoint_quant_for(wq, (a ? 8 : 6) * parts, parts > 1 ? 29 : 17);
             s.cq[pt][a][wq] = (int8_t)cq;
             s.slot[pt][a][wq] = -1;
             if (cq < 0 || cq == kQuant256) continue;

@@ -99,7 +99,7 @@ typedef enum astc_quality {
                                     blocks the reference's PCA collapses
                                     (flat colour, varying alpha) and
                                     decorrelated channels; FP32 only        */
-    ASTC_QUALITY_PARTITIONS = 3  /* THOROUGH plus two-partition blocks: the
+    ASTC_QUALITY_PARTITIONS = 3, /* THOROUGH plus two-partition blocks: the
                                     partition index whose pattern best
                                     matches the split along the kept fit,
                                     each partition fitted on its own, every
@@ -107,6 +107,17 @@ typedef enum astc_quality {
                                     decode (the reference has only a
                                     commented-out layout stub for partitions,
                                     ASTC_Encode.hlsl:422-431); FP32 only    */
+    ASTC_QUALITY_THREE_PARTITIONS = 4  /* PARTITIONS plus three-partition
+                                    blocks for RGB input (three RGBA
+                                    partitions would need 24 colour endpoint
+                                    values, above the format's 18): the
+                                    four pattern classes that best match an
+                                    integer three-colour labelling of the
+                                    texels, each partition fitted on its own,
+                                    every legal weight range scored.  For
+                                    flat-colour graphics (UI, sprites);
+                                    RGBA input is encoded as PARTITIONS;
+                                    FP32 only                               */
 } astc_quality;
 
 /* Encoder options: the reference's encode_option (astc_encode.h:14-28) plus

@@ -145,6 +145,7 @@ def test_cli_reads_reference_leaf(native, tmp_path, reference_dir):
     (["--max-accumulation", "--search"], dict(block_dim=4, axis=1, quality=1)),
     (["-6x6", "-alpha", "-srgb", "--thorough"], dict(block_dim=6, has_alpha=True, srgb=True, quality=2)),
     (["--partitions"], dict(block_dim=4, quality=3)),
+    (["-6x6", "--three-partitions"], dict(block_dim=6, quality=4)),
 ])
 def test_cli_encode_matches_library(native, oracle, tmp_path, flags, opts):
     rng = np.random.default_rng(len(flags))

@@ -66,7 +66,7 @@ def test_batch_equals_alone_all_formats(native, oracle, precision):
                 assert np.array_equal(got, oracle.encode(img, **opts)), opts
 
 
-@pytest.mark.parametrize("quality", [1, 3])
+@pytest.mark.parametrize("quality", [1, 3, 4])
 def test_batch_quality_modes(native, oracle, quality):
     """astc_batch_encode_quality: every texture's blocks equal its
     astc_encode_gpu result with the same quality (and the oracle's)."""

@@ -1,4 +1,5 @@
-"""CUDA search mode and max-accumulation axis vs the FP32 oracle, through the C ABI.
+"""CUDA quality modes (search, THOROUGH, PARTITIONS, THREE_PARTITIONS) and the
+max-accumulation axis vs the FP32 oracle, through the C ABI.
 
 Bar: every block bit-identical to the oracle's search / max-accumulation
 encode (the kernels follow the oracle's FP32 model and its integer scoring
@@ -35,7 +36,7 @@ def _psnr(a, b):
     return float("inf") if mse == 0 else 10 * np.log10(255.0 ** 2 / mse)
 
 
-GRID = [g for g in itertools.product([4, 6], [False, True], [False, True], [False, True], [0, 1], [0, 1, 2, 3])
+GRID = [g for g in itertools.product([4, 6], [False, True], [False, True], [False, True], [0, 1], [0, 1, 2, 3, 4])
         if (g[4] or g[5]) and not (g[5] >= 2 and g[4] == 1)]
 
 
@@ -54,9 +55,10 @@ def test_option_grid_bit_exact(native, oracle, dim, alpha, normal, srgb, axis, q
 def test_ragged_sizes(native, oracle, h, w, dim):
     img = _texture(h, w, seed=h * 1000 + w)
     for border in (0, 1):
-        for quality in (1, 2, 3):
-            opts = dict(block_dim=dim, has_alpha=True, border=border, quality=quality)
-            assert np.array_equal(native.encode(img, **opts), oracle.encode(img, **opts))
+        for quality in (1, 2, 3, 4):
+            for alpha in (False, True):
+                opts = dict(block_dim=dim, has_alpha=alpha, border=border, quality=quality)
+                assert np.array_equal(native.encode(img, **opts), oracle.encode(img, **opts))
 
 
 def test_constant_images(native, oracle):
@@ -71,7 +73,7 @@ def test_constant_images(native, oracle):
                 assert np.array_equal(got, native.encode(img, block_dim=dim, has_alpha=alpha))
 
 
-@pytest.mark.parametrize("quality", [1, 2, 3])
+@pytest.mark.parametrize("quality", [1, 2, 3, 4])
 @pytest.mark.parametrize("name", ["4x4_rgb_512", "6x6_rgba_srgb_2048", "4x4_normal_4096"])
 def test_workloads_full_size(native, oracle, name, quality):
     """Full-size workloads: bit-exact, decodes cleanly, never worse than FAST."""
@@ -93,6 +95,29 @@ def test_workloads_full_size(native, oracle, name, quality):
     p_search = _psnr(d_search[..., :ch], ref[..., :ch])
     p_fast = _psnr(d_fast[..., :ch], ref[..., :ch])
     assert p_search >= p_fast, (p_search, p_fast)
+
+
+@pytest.mark.parametrize("dim,srgb,normal", [(4, False, False), (6, False, False), (4, True, False),
+                                             (6, True, False), (4, False, True)])
+def test_three_partitions_flat_graphics(native, oracle, dim, srgb, normal):
+    """Flat-colour graphics, where three-partition blocks win: bit-exact with
+    the oracle, some blocks carry three partitions, and the decode beats
+    PARTITIONS'."""
+    from astc_encoder_gb300 import synth
+    img = synth.ui_shapes(160, 144, seed=40 + dim + 2 * srgb + 4 * normal)
+    opts = dict(block_dim=dim, srgb=srgb, is_normal=normal, border=1)
+    got = native.encode(img, quality=4, **opts)
+    want = oracle.encode(img, quality=4, **opts)
+    same = np.all(got == want, axis=1)
+    assert np.array_equal(got, want), f"{(~same).sum()} of {len(same)} blocks differ"
+    three = ((got.view("<u4")[:, 0] >> 11) & 3) == 2
+    assert three.any()
+    two = native.encode(img, quality=3, **opts)
+    ref = native.fitted_reference(img, srgb, normal)
+    ch = 2 if normal else 3
+    d3 = native.decode(got, 144, 160, dim, srgb=srgb)
+    d2 = native.decode(two, 144, 160, dim, srgb=srgb)
+    assert _psnr(d3[..., :ch], ref[..., :ch]) >= _psnr(d2[..., :ch], ref[..., :ch])
 
 
 def test_device_pointer_path(native, oracle):
