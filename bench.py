@@ -11,9 +11,10 @@ no step reads its inputs from L2), each through the C ABI
                 event pair around each step on the launching stream (a dedicated
                 non-default torch stream passed to the C ABI; max over ranks).
 * e2e        -- the same metric through the same entry point with pinned
-                HOST buffers: the kernels read each texture from host memory
-                and write its blocks back over NVLink-C2C (zero-copy), all inside
-                the timed region, one stream synchronize per step.
+                HOST buffers: each texture goes up through the library's upload
+                ring (copy engine, 32 MiB slots overlapped with the encode) and
+                the kernels write its blocks back in place over NVLink-C2C, all
+                inside the timed region, one stream synchronize per step.
 * roofline   -- the dominant kernel's algorithmic bytes (4 B/texel read +
                 16 B/block written) per launch over its mean launch time,
                 against the measured HBM copy bandwidth; roofline_fp32 gives
@@ -68,7 +69,8 @@ def _parse():
                     help="small case for ncu: one FP32 and one HALF2 batched graph launch")
     ap.add_argument("--profile-case", action="store_true",
                     help="small case for ncu: 2 textures per step, encode launches only")
-    ap.add_argument("--profile-quality", default="fast", choices=["fast", "search", "thorough", "partitions"],
+    ap.add_argument("--profile-quality", default="fast",
+                    choices=["fast", "search", "thorough", "partitions", "three_partitions"],
                     help="with --profile-case: the quality mode the launches use (FP32)")
     return ap.parse_args()
 
@@ -305,18 +307,25 @@ def _psnr_blocks(native, blocks: np.ndarray, tex: np.ndarray, spec: dict) -> flo
 def _bench_search(torch, native, headline: str, texs, outs, spec: dict) -> dict:
     """Throughput and decoded PSNR of the quality modes -- the search (every
     single-partition 4x4-grid mode, least decoded error), the max-accumulation
-    axis, THOROUGH (search from the better fit, plus dual-plane blocks) and
-    PARTITIONS (THOROUGH plus two-partition blocks) -- against the fixed mode,
-    on each workload (device-resident inputs above L2 size, as the headline)."""
+    axis, THOROUGH (search from the better fit, plus dual-plane blocks),
+    PARTITIONS (THOROUGH plus two-partition blocks) and THREE_PARTITIONS
+    (PARTITIONS plus three-partition RGB blocks) -- against the fixed mode, on
+    each workload and on flat-colour graphics (synth.ui_shapes, 4x4 RGB, where
+    three partitions pay), device-resident inputs above L2 size as the
+    headline."""
     from astc_encoder_gb300 import synth
     result = {}
-    for name in (headline, "4x4_rgb_512", "4x4_normal_4096", "6x6_rgba_srgb_2048"):
+    for name in (headline, "4x4_rgb_512", "4x4_normal_4096", "6x6_rgba_srgb_2048", "ui_shapes_4x4_1024"):
         if name in result:
             continue
         if name == headline:
             st, so, sspec = texs, outs, dict(spec)
         else:
-            simg, sspec = synth.workload(name)
+            if name == "ui_shapes_4x4_1024":
+                simg = synth.ui_shapes(1024, 1024)
+                sspec = dict(block_dim=4, has_alpha=False, is_normal=False, srgb=False, border=0)
+            else:
+                simg, sspec = synth.workload(name)
             sh, sw = simg.shape[:2]
             sd = sspec["block_dim"]
             snb = ((sw + sd - 1) // sd) * ((sh + sd - 1) // sd)
@@ -327,7 +336,8 @@ def _bench_search(torch, native, headline: str, texs, outs, spec: dict) -> dict:
         tex0 = st[0].cpu().numpy()
         entry = {"textures_per_step": len(st)}
         for label, kw in (("fast", {}), ("search", dict(quality=1)), ("max_accumulation", dict(axis=1)),
-                          ("thorough", dict(quality=2)), ("partitions", dict(quality=3))):
+                          ("thorough", dict(quality=2)), ("partitions", dict(quality=3)),
+                          ("three_partitions", dict(quality=4))):
             run = dict(sspec, **kw)
             _time_launches(torch, native, st, so, run, 2)
             per, steps, _ = _time_launches(torch, native, st, so, run, 5)
@@ -337,6 +347,7 @@ def _bench_search(torch, native, headline: str, texs, outs, spec: dict) -> dict:
         entry["search_gain_db"] = entry["search"]["psnr_db"] - entry["fast"]["psnr_db"]
         entry["thorough_gain_db"] = entry["thorough"]["psnr_db"] - entry["fast"]["psnr_db"]
         entry["partitions_gain_db"] = entry["partitions"]["psnr_db"] - entry["fast"]["psnr_db"]
+        entry["three_partitions_gain_db"] = entry["three_partitions"]["psnr_db"] - entry["fast"]["psnr_db"]
         result[name] = entry
         if name != headline:
             del st, so
@@ -555,7 +566,8 @@ def run_ours(args) -> None:
 
     if args.profile_case:
         # only the encode launches: warm-up, then the timed steps; no other kernels
-        quality = {"fast": 0, "search": 1, "thorough": 2, "partitions": 3}[args.profile_quality]
+        quality = {"fast": 0, "search": 1, "thorough": 2, "partitions": 3,
+                   "three_partitions": 4}[args.profile_quality]
         spec_prof = dict(spec_run, quality=quality) if quality else spec_run
         _time_launches(torch, native, texs, outs, spec_prof, max(3, args.warmup))
         per, _, launches = _time_launches(torch, native, texs, outs, spec_prof, args.steps)
@@ -703,7 +715,7 @@ def run_ours(args) -> None:
                                       "autotune_best_us": tuned.best_us}},
         "e2e": {"value": e2e_value, "unit": "Mtexels/s",
                 "h2d_bytes_per_step": texels_step * 4, "d2h_bytes_per_step": nblocks * 16 * len(texs),
-                "entry_point": "astc_encode_gpu (ASTC_MEMORY_HOST, pinned buffers read and written in place over NVLink-C2C, one stream sync per step)",
+                "entry_point": "astc_encode_gpu (ASTC_MEMORY_HOST, pinned buffers: inputs through the upload ring, blocks written in place over NVLink-C2C; one stream sync per step)",
                 "steps": e2e_steps},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "kernel": kernel, "achieved": achieved_gbs,
