@@ -61,6 +61,17 @@ def test_ragged_sizes(native, oracle, h, w, dim):
                 assert np.array_equal(native.encode(img, **opts), oracle.encode(img, **opts))
 
 
+@pytest.mark.parametrize("h,w", [(4, 20000), (20001, 6)])
+def test_extreme_aspect_ratios(native, oracle, h, w):
+    """One block row of 5000 blocks, and one block column of 3334-5001: the
+    block index arithmetic at the widths and heights the grid spans."""
+    img = _texture(h, w, seed=h + w)
+    for dim in (4, 6):
+        for quality in (1, 2, 3, 4):
+            opts = dict(block_dim=dim, border=1, quality=quality)
+            assert np.array_equal(native.encode(img, **opts), oracle.encode(img, **opts)), (dim, quality)
+
+
 def test_constant_images(native, oracle):
     for val in (0, 1, 127, 255):
         img = np.full((24, 24, 4), val, np.uint8)
