@@ -83,8 +83,8 @@ __device__ __forceinline__ uint32_t eval_dual(const uint32_t (&tw)[DIM * DIM], u
 template <bool ALPHA>
 __device__ __forceinline__ uint4 assemble_dual(int wq, int cq, int pc, const uint32_t (&ev)[ALPHA ? 8 : 6],
                                                const uint32_t (&sw)[32], const SearchSmem& sm) {
-    const Bits128 ep = ise_encode<ALPHA ? 8 : 6>(cq, ev, sm.trits, sm.quints);
-    const Bits128 wt = ise_encode<32>(wq, sw, sm.trits, sm.quints);
+    const Bits128 ep = ise_encode_endpoints<ALPHA ? 8 : 6>(cq, ev, sm.trits, sm.quints);
+    const Bits128 wt = ise_encode_weights<32, kQuant2, kQuant6>(wq, sw, sm.trits, sm.quints);
     const int sel = 128 - ise_bit_count(wq, 32) - 2;       // 32..102: never straddles the words
     const uint64_t head = (uint64_t)blockmode_4x4_grid(wq) | (1ull << 10) | ((uint64_t)(ALPHA ? 12u : 8u) << 13);
     uint64_t lo = head | (ep.lo << 17) | __brevll(wt.hi);

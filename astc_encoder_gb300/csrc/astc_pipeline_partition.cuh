@@ -278,8 +278,8 @@ template <bool ALPHA>
 __device__ __forceinline__ uint4 assemble_two_partitions(int wq, int cq, int seed,
                                                          const uint32_t (&ev)[ALPHA ? 16 : 12],
                                                          const uint32_t (&sw)[16], const SearchSmem& sm) {
-    const Bits128 ep = ise_encode<ALPHA ? 16 : 12>(cq, ev, sm.trits, sm.quints);
-    const Bits128 wt = ise_encode<16>(wq, sw, sm.trits, sm.quints);
+    const Bits128 ep = ise_encode_endpoints<ALPHA ? 16 : 12>(cq, ev, sm.trits, sm.quints);
+    const Bits128 wt = ise_encode_weights<16, kQuant3, kQuant16>(wq, sw, sm.trits, sm.quints);
     const uint64_t head = (uint64_t)blockmode_4x4_grid(wq) | (1ull << 11) | ((uint64_t)(seed & 0x3FF) << 13) |
                           ((uint64_t)(ALPHA ? 12u : 8u) << 25);
     const uint64_t lo = head | (ep.lo << 29) | __brevll(wt.hi);

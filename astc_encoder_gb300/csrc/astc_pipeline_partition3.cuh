@@ -205,8 +205,8 @@ __device__ __forceinline__ void three_partition_weights(const S& st, uint64_t m1
 // bit 29, weight ISE bit-reversed from bit 127.
 __device__ __forceinline__ uint4 assemble_three_partitions(int wq, int cq, int seed, const uint32_t (&ev)[18],
                                                            const uint32_t (&sw)[16], const SearchSmem& sm) {
-    const Bits128 ep = ise_encode<18>(cq, ev, sm.trits, sm.quints);
-    const Bits128 wt = ise_encode<16>(wq, sw, sm.trits, sm.quints);
+    const Bits128 ep = ise_encode_endpoints<18>(cq, ev, sm.trits, sm.quints);
+    const Bits128 wt = ise_encode_weights<16, kQuant3, kQuant8>(wq, sw, sm.trits, sm.quints);
     const uint64_t head = (uint64_t)blockmode_4x4_grid(wq) | (2ull << 11) | ((uint64_t)(seed & 0x3FF) << 13) |
                           (8ull << 25);
     const uint64_t lo = head | (ep.lo << 29) | __brevll(wt.hi);

@@ -90,26 +90,14 @@ struct SearchSmem {
 // ---------------------------------------------------------------------------
 // general bounded integer sequence encoding (ISE) into a 128-bit field
 // ---------------------------------------------------------------------------
-// COUNT symbols of quant method `quant` (runtime) as an integer sequence
-// (astc_ise.h: one rolled loop, the same bits as the reference's
-// ASTC_IntegerSequenceEncoding.hlsl encode_trits 142-176, encode_quints
-// 181-205, bise_* 207-276), cut to the ISE length of COUNT values.
-template <int COUNT>
-__device__ __forceinline__ Bits128 ise_encode(int quant, const uint32_t (&v)[COUNT], const uint8_t* trits,
-                                              const uint8_t* quints) {
-    uint32_t w[(COUNT + 3) / 4];
-    pack_bytes<COUNT>(v, w);
-    return ise_encode_packed<(COUNT + 3) / 4>(quant, COUNT, w, trits, quints);
-}
-
 // Single-partition block, 4x4 weight grid of range wq, endpoint range cq:
 // mode [10:0], CEM [16:13], endpoint ISE from bit 17 up, weight ISE
 // bit-reversed from bit 127 down.
 template <bool ALPHA>
 __device__ __forceinline__ uint4 assemble_search_block(int wq, int cq, const uint32_t (&ev)[ALPHA ? 8 : 6],
                                                        const uint32_t (&sw)[16], const SearchSmem& sm) {
-    const Bits128 ep = ise_encode<ALPHA ? 8 : 6>(cq, ev, sm.trits, sm.quints);
-    const Bits128 wt = ise_encode<16>(wq, sw, sm.trits, sm.quints);
+    const Bits128 ep = ise_encode_endpoints<ALPHA ? 8 : 6>(cq, ev, sm.trits, sm.quints);
+    const Bits128 wt = ise_encode_weights<16, kQuant3, kQuant32>(wq, sw, sm.trits, sm.quints);
     const uint64_t head = (uint64_t)blockmode_4x4_grid(wq) | ((uint64_t)(ALPHA ? 12u : 8u) << 13);
     const uint64_t lo = head | (ep.lo << 17) | __brevll(wt.hi);
     const uint64_t hi = (ep.lo >> 47) | (ep.hi << 17) | __brevll(wt.lo);

@@ -1,10 +1,11 @@
-"""The rolled ISE encoder of the search-mode assemblers (csrc/astc_ise.h),
-compiled for the host, against the oracle's integer sequence encoder
+"""The ISE encoders of the search-mode assemblers (csrc/astc_ise.h: the rolled
+loop for any range, the compile-time form of each range), compiled for the
+host, against the oracle's integer sequence encoder
 (ASTC_IntegerSequenceEncoding.hlsl encode_trits / encode_quints / bise_*):
-every range QUANT_2..QUANT_256, every length the assemblers use (6, 8, 12,
-16 endpoint values; 16 and 32 weights) and the ragged lengths in between,
-random and extreme values.  Bar: all 16 bytes identical (the oracle's
-sequence is zero past its length)."""
+every range QUANT_2..QUANT_256; the rolled loop at every length 1..32, the
+compile-time forms at the lengths the assemblers use (6, 8, 12, 16, 18
+endpoint values; 16 and 32 weights); random and extreme values.  Bar: all 16
+bytes identical (the oracle's sequence is zero past its length)."""
 import os
 import shutil
 import subprocess
@@ -30,11 +31,12 @@ def harness(tmp_path_factory):
     return exe
 
 
-def test_rolled_encoder_matches_oracle(harness):
-    rng = np.random.default_rng(11)
+@pytest.mark.parametrize("form", [0, 1])
+def test_encoders_match_oracle(harness, form):
+    rng = np.random.default_rng(11 + form)
     cases = []
     for quant, levels in enumerate(LEVELS):
-        for count in range(1, 33):
+        for count in (range(1, 33) if form == 0 else (6, 8, 12, 16, 18, 32)):
             if oracle.ise_bits(quant, count) > 128:
                 continue
             for kind in range(4):
@@ -47,7 +49,7 @@ def test_rolled_encoder_matches_oracle(harness):
                 else:
                     v = rng.choice([0, levels - 1], count)
                 cases.append((quant, count, [int(x) for x in v]))
-    text = "".join(f"{q} {c} {' '.join(map(str, v))}\n" for q, c, v in cases)
+    text = "".join(f"{form} {q} {c} {' '.join(map(str, v))}\n" for q, c, v in cases)
     got = subprocess.run([harness], input=text, capture_output=True, text=True, check=True).stdout.split()
     assert len(got) == len(cases)
     for (q, c, v), hexbytes in zip(cases, got):
