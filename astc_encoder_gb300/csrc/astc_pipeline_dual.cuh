@@ -9,8 +9,10 @@
 // constant; the axis's component on the channel is then exactly 0, so it takes
 // no part in find_min_max's projections).  pc is the channel whose zeroed
 // covariance keeps the least off-axis variance: its trace minus the Rayleigh
-// quotient v.Cv / v.v (the first channel on ties).  The other channels are
-// fitted on pc's axis, pc's endpoints are its minimum and maximum.  Every weight range whose 32 weights (plane 1, plane 2
+// quotient v.Cv / v.v (the first channel on ties) -- or, when fewer than
+// three channels vary (a normal map's x and y), the first varying channel.
+// The other channels are fitted on pc's axis, pc's endpoints are its minimum
+// and maximum.  Every weight range whose 32 weights (plane 1, plane 2
 // per grid point; 24..96 bits) leave a legal endpoint range after the 2-bit
 // plane selector is scored by the exact decode, each channel taking its
 // plane's weight.  Plane-1 weights project the grid colours on the decoded
@@ -28,10 +30,6 @@ struct DualSmem {
     int8_t cq[12];       // weight range -> endpoint range (-1: illegal)
     int8_t slot[12];
 };
-
-__device__ __forceinline__ float comp(const float4 t, int c) {
-    return c == 0 ? t.x : c == 1 ? t.y : c == 2 ? t.z : t.w;
-}
 
 // The squared error of a dual-plane decode (channel pc on plane-2 weights).
 // P[g]: grid point g's unquantised plane-1 weight in the low half, its plane-2
@@ -105,21 +103,35 @@ __device__ __forceinline__ uint4 dual_plane_block(const S& st, const G& grid, co
     constexpr int NCH = ALPHA ? 4 : 3;
     const float4 m = block_mean<N>(st);
     const Covariance cv = block_covariance<N>(st, m);
-    // the plane-2 channel: of the channels that vary, the one whose zeroed
-    // covariance keeps the least off-axis variance (first on ties)
-    int pc = -1;
-    float least = 0.0f, plo = 0.0f, phi = 0.0f;
-    float4 pv = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-#pragma unroll 1
-    for (int c = 0; c < NCH; ++c) {
-        float lo = 1e31f, hi = -1e31f;
+    // each channel's range (one pass); constant channels have nothing to split off
+    float lo[4] = {1e31f, 1e31f, 1e31f, 1e31f}, hi[4] = {-1e31f, -1e31f, -1e31f, -1e31f};
 #pragma unroll
-        for (int k = 0; k < N; ++k) {
-            const float v = comp(st.get(k), c);
-            lo = fminf(lo, v);
-            hi = fmaxf(hi, v);
+    for (int k = 0; k < N; ++k) {
+        const float4 t = st.get(k);
+        lo[0] = fminf(lo[0], t.x); hi[0] = fmaxf(hi[0], t.x);
+        lo[1] = fminf(lo[1], t.y); hi[1] = fmaxf(hi[1], t.y);
+        lo[2] = fminf(lo[2], t.z); hi[2] = fmaxf(hi[2], t.z);
+        if constexpr (ALPHA) { lo[3] = fminf(lo[3], t.w); hi[3] = fmaxf(hi[3], t.w); }
+    }
+    int nvary = 0, first = -1;
+#pragma unroll
+    for (int c = 0; c < NCH; ++c)
+        if (lo[c] != hi[c]) {
+            ++nvary;
+            if (first < 0) first = c;
         }
-        if (lo == hi) continue;                    // a constant channel: nothing to split off
+    if (nvary == 0) return best;
+    // the plane-2 channel: with three or more varying, the one whose zeroed
+    // covariance keeps the least off-axis variance (first on ties); with fewer
+    // (a normal map's x and y), the first varying channel
+    int pc = first;
+    float4 pv = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    float least = 0.0f;
+#pragma unroll 1
+    for (int c = nvary < 3 ? first : 0; c < (nvary < 3 ? first + 1 : NCH); ++c) {
+        const float clo = c == 0 ? lo[0] : c == 1 ? lo[1] : c == 2 ? lo[2] : lo[3];
+        const float chi = c == 0 ? hi[0] : c == 1 ? hi[1] : c == 2 ? hi[2] : hi[3];
+        if (clo == chi) continue;
         // entry (i, j) is zeroed when i or j is c
         const bool z0 = c == 0, z1 = c == 1, z2 = c == 2, z3 = c == 3;
         const float a00 = z0 ? 0.0f : cv.c00, a01 = (z0 || z1) ? 0.0f : cv.c01;
@@ -128,6 +140,10 @@ __device__ __forceinline__ uint4 dual_plane_block(const S& st, const G& grid, co
         const float a13 = (z1 || z3) ? 0.0f : cv.c13, a22 = z2 ? 0.0f : cv.c22;
         const float a23 = (z2 || z3) ? 0.0f : cv.c23, a33 = z3 ? 0.0f : cv.c33;
         const float4 v = power_iteration(a00, a01, a02, a03, a11, a12, a13, a22, a23, a33);
+        if (nvary < 3) {
+            pv = v;
+            break;
+        }
         // trace minus the Rayleigh quotient v.Cv / v.v
         const float k0 = dot4(a00, a01, a02, a03, v.x, v.y, v.z, v.w);
         const float k1 = dot4(a01, a11, a12, a13, v.x, v.y, v.z, v.w);
@@ -136,9 +152,10 @@ __device__ __forceinline__ uint4 dual_plane_block(const S& st, const G& grid, co
         const float vv = dot4(v.x, v.y, v.z, v.w, v.x, v.y, v.z, v.w);
         const float lam = vv > 0.0f ? __fdiv_rn(dot4(v.x, v.y, v.z, v.w, k0, k1, k2, k3), vv) : 0.0f;
         const float resid = __fsub_rn(__fadd_rn(__fadd_rn(__fadd_rn(a00, a11), a22), a33), lam);
-        if (pc < 0 || resid < least) { pc = c; least = resid; plo = lo; phi = hi; pv = v; }
+        if (c == first || resid < least) { pc = c; least = resid; pv = v; }
     }
-    if (pc < 0) return best;
+    const float plo = pc == 0 ? lo[0] : pc == 1 ? lo[1] : pc == 2 ? lo[2] : lo[3];
+    const float phi = pc == 0 ? hi[0] : pc == 1 ? hi[1] : pc == 2 ? hi[2] : hi[3];
     // the other channels on pc's axis (its pc component is exactly 0), pc on
     // its range
     uint32_t q0[4], q1[4];

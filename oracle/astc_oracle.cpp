@@ -1336,7 +1336,8 @@ struct Pipe {
     // that channel's row and column zeroed (the PCA of the block with the
     // channel held constant); pc is the channel whose zeroed covariance keeps
     // the least off-axis variance (its trace minus the Rayleigh quotient
-    // k.Ck / k.k; the first channel on ties).  The other channels are fitted
+    // k.Ck / k.k; the first channel on ties) -- or, when fewer than three
+    // channels vary (a normal map's x and y), the first varying channel.  The other channels are fitted
     // on pc's axis by the shader's find_min_max, pc's endpoints are its min
     // and max.  Every weight range QUANT_2.. whose 32 weights (24..96 bits)
     // leave a
@@ -1352,35 +1353,57 @@ struct Pipe {
         uint32_t best = UINT32_MAX;
         T mean[4], cov[4][4];
         covariance(tex, n, mean, cov);
-        int pc = -1;
-        T lo = 0, hi = 0, k[4] = {0, 0, 0, 0}, least = 0;
+        // each channel's range; constant channels have nothing to split off
+        T clo[4], chi[4];
+        int nvary = 0, first = -1;
         for (int c = 0; c < nch; ++c) {
-            T clo = P::lit(1e31f, 1e31), chi = P::lit(-1e31f, -1e31);
+            clo[c] = P::lit(1e31f, 1e31);
+            chi[c] = P::lit(-1e31f, -1e31);
             for (int i = 0; i < n; ++i) {
-                clo = P::min(clo, tex[i][c]);
-                chi = P::max(chi, tex[i][c]);
+                clo[c] = P::min(clo[c], tex[i][c]);
+                chi[c] = P::max(chi[c], tex[i][c]);
             }
-            if (clo == chi) continue;                        // a constant channel: nothing to split off
-            // the other channels' axis: the power iteration on the covariance
-            // without c's row and column (c's component of the axis is then
-            // exactly 0, so c takes no part in the projections)
-            T cp[4][4];
-            for (int i = 0; i < 4; ++i)
-                for (int j = 0; j < 4; ++j) cp[i][j] = (i == c || j == c) ? (T)0 : cov[i][j];
-            T kc[4];
-            eigen_vector(cp, kc);
-            T ck[4];
-            for (int r = 0; r < 4; ++r) ck[r] = dot4(cp[r], kc);
-            const T kk = dot4(kc, kc);
-            const T lam = kk > 0 ? P::div(dot4(kc, ck), kk) : (T)0;
-            T tr = 0;
-            for (int r = 0; r < 4; ++r) tr = P::add(tr, cp[r][r]);
-            const T resid = P::sub(tr, lam);
-            if (pc < 0 || resid < least) {
-                pc = c; least = resid; lo = clo; hi = chi;
-                for (int r = 0; r < 4; ++r) k[r] = kc[r];
+            if (clo[c] != chi[c]) {
+                ++nvary;
+                if (first < 0) first = c;
             }
         }
+        // the other channels' axis for channel c: the power iteration on the
+        // covariance without c's row and column (c's component of the axis is
+        // then exactly 0, so c takes no part in the projections)
+        auto axis_without = [&](int c, T kc[4], T cp[4][4]) {
+            for (int i = 0; i < 4; ++i)
+                for (int j = 0; j < 4; ++j) cp[i][j] = (i == c || j == c) ? (T)0 : cov[i][j];
+            eigen_vector(cp, kc);
+        };
+        int pc = -1;
+        T k[4] = {0, 0, 0, 0};
+        if (nvary > 0 && nvary < 3) {
+            // two varying channels (or one): each plane carries one, so plane 2
+            // takes the first
+            T cp[4][4];
+            pc = first;
+            axis_without(pc, k, cp);
+        } else if (nvary >= 3) {
+            T least = 0;
+            for (int c = 0; c < nch; ++c) {
+                if (clo[c] == chi[c]) continue;
+                T kc[4], cp[4][4];
+                axis_without(c, kc, cp);
+                T ck[4];
+                for (int r = 0; r < 4; ++r) ck[r] = dot4(cp[r], kc);
+                const T kk = dot4(kc, kc);
+                const T lam = kk > 0 ? P::div(dot4(kc, ck), kk) : (T)0;
+                T tr = 0;
+                for (int r = 0; r < 4; ++r) tr = P::add(tr, cp[r][r]);
+                const T resid = P::sub(tr, lam);
+                if (pc < 0 || resid < least) {
+                    pc = c; least = resid;
+                    for (int r = 0; r < 4; ++r) k[r] = kc[r];
+                }
+            }
+        }
+        const T lo = pc >= 0 ? clo[pc] : (T)0, hi = pc >= 0 ? chi[pc] : (T)0;
         if (pc >= 0) {
             T e0[4], e1[4];
             find_min_max(tex, n, mean, k, alpha, e0, e1);
