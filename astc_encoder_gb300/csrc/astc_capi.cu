@@ -205,7 +205,7 @@ astc_status validate_opts(const astc_opts* o, int w, int h) {
         return set_error(ASTC_ERR_INVALID_ARG, "axis must be ASTC_AXIS_PCA or ASTC_AXIS_MAX_ACCUMULATION");
     if (o->quality < ASTC_QUALITY_FAST || o->quality > ASTC_QUALITY_THREE_PARTITIONS)
         return set_error(ASTC_ERR_INVALID_ARG,
-                         "quality must be ASTC_QUALITY_FAST, _SEARCH, _THOROUGH or _PARTITIONS");
+                         "quality must be ASTC_QUALITY_FAST, _SEARCH, _THOROUGH, _PARTITIONS or _THREE_PARTITIONS");
     if (o->precision == ASTC_PRECISION_HALF2 && (o->axis != ASTC_AXIS_PCA || o->quality != ASTC_QUALITY_FAST))
         return set_error(ASTC_ERR_UNSUPPORTED, "the max-accumulation axis and the mode search are FP32 only");
     if (w <= 0 || h <= 0) return set_error(ASTC_ERR_INVALID_ARG, "width and height must be positive");
