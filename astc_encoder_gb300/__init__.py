@@ -62,6 +62,7 @@ class Memory(enum.IntEnum):
 class Axis(enum.IntEnum):
     PCA = 0                 # principal_component_analysis (ASTC_Encode.hlsl:514)
     MAX_ACCUMULATION = 1    # max_accumulation_pixel_direction (170-227, unused there)
+    BEST = 2                # both fits, the better fixed-mode block (PCA on ties)
 
 
 class Quality(enum.IntEnum):

@@ -201,13 +201,13 @@ astc_status validate_opts(const astc_opts* o, int w, int h) {
         return set_error(ASTC_ERR_INVALID_ARG, "precision must be FP32 or HALF2");
     if (o->memory != ASTC_MEMORY_HOST && o->memory != ASTC_MEMORY_DEVICE)
         return set_error(ASTC_ERR_INVALID_ARG, "memory must be ASTC_MEMORY_HOST or ASTC_MEMORY_DEVICE");
-    if (o->axis != ASTC_AXIS_PCA && o->axis != ASTC_AXIS_MAX_ACCUMULATION)
-        return set_error(ASTC_ERR_INVALID_ARG, "axis must be ASTC_AXIS_PCA or ASTC_AXIS_MAX_ACCUMULATION");
+    if (o->axis != ASTC_AXIS_PCA && o->axis != ASTC_AXIS_MAX_ACCUMULATION && o->axis != ASTC_AXIS_BEST)
+        return set_error(ASTC_ERR_INVALID_ARG, "axis must be ASTC_AXIS_PCA, _MAX_ACCUMULATION or _BEST");
     if (o->quality < ASTC_QUALITY_FAST || o->quality > ASTC_QUALITY_THREE_PARTITIONS)
         return set_error(ASTC_ERR_INVALID_ARG,
                          "quality must be ASTC_QUALITY_FAST, _SEARCH, _THOROUGH, _PARTITIONS or _THREE_PARTITIONS");
     if (o->precision == ASTC_PRECISION_HALF2 && (o->axis != ASTC_AXIS_PCA || o->quality != ASTC_QUALITY_FAST))
-        return set_error(ASTC_ERR_UNSUPPORTED, "the max-accumulation axis and the mode search are FP32 only");
+        return set_error(ASTC_ERR_UNSUPPORTED, "the other axes and the quality modes are FP32 only");
     if (w <= 0 || h <= 0) return set_error(ASTC_ERR_INVALID_ARG, "width and height must be positive");
     if (w > 0xFFFFFF || h > 0xFFFFFF)
         return set_error(ASTC_ERR_INVALID_ARG, "width and height must fit the 24-bit .astc size fields");

@@ -23,6 +23,7 @@
 //   --thorough         --search from the better of the two fits
 //   --partitions       --thorough plus two-partition blocks
 //   --three-partitions --partitions plus three-partition blocks (RGB input)
+//   --best-fit         both fits, the better fixed-mode block (or --search from it)
 //   -o PATH            output path
 //   --dump-rgba PATH   write the loaded (flipped) RGBA image as PAM and exit
 //                      without encoding (no GPU needed)
@@ -47,7 +48,7 @@ std::string strip_file_extension(const std::string& path) {
 int usage() {
     std::cout << "usage: astc_cs_enc input_texture [-4x4|-6x6] [-alpha] [-norm] [-srgb]"
                  " [--clamp] [--half2] [--search] [--max-accumulation] [--thorough] [--partitions]"
-                 " [--three-partitions]"
+                 " [--three-partitions] [--best-fit]"
                  " [-o out.astc]"
                  " [--dump-rgba out.pam]" << std::endl;
     return -1;
@@ -63,6 +64,7 @@ int main(int argc, char** argv) {
     const std::string src = argv[1];
     bool is4x4 = true, alpha = false, norm = false, srgb = false, clamp = false, half2 = false;
     bool search = false, max_acc = false, thorough = false, partitions = false, three = false;
+    bool best_fit = false;
     std::string out_path, dump_path;
     for (int i = 2; i < argc; ++i) {
         const std::string a = argv[i];
@@ -78,6 +80,7 @@ int main(int argc, char** argv) {
         else if (a == "--thorough") thorough = true;
         else if (a == "--partitions") partitions = true;
         else if (a == "--three-partitions") three = true;
+        else if (a == "--best-fit") best_fit = true;
         else if (a == "-o" && i + 1 < argc) out_path = argv[++i];
         else if (a == "--dump-rgba" && i + 1 < argc) dump_path = argv[++i];
         else std::cerr << "ignoring unknown argument: " << a << std::endl;
@@ -116,7 +119,7 @@ int main(int argc, char** argv) {
     o.quality = three ? ASTC_QUALITY_THREE_PARTITIONS
                 : partitions ? ASTC_QUALITY_PARTITIONS
                 : thorough ? ASTC_QUALITY_THOROUGH : (search ? ASTC_QUALITY_SEARCH : ASTC_QUALITY_FAST);
-    o.axis = max_acc ? ASTC_AXIS_MAX_ACCUMULATION : ASTC_AXIS_PCA;
+    o.axis = best_fit ? ASTC_AXIS_BEST : max_acc ? ASTC_AXIS_MAX_ACCUMULATION : ASTC_AXIS_PCA;
     std::vector<uint8_t> blocks(astc_encoded_size(img.width, img.height, o.block_dim));
     astc_status st = astc_encode_gpu(img.rgba.data(), img.width, img.height, &o, blocks.data());
     if (st != ASTC_OK) {

@@ -8,7 +8,9 @@
 namespace astc {
 
 cudaError_t launch_encode_search(const EncodeJob& j, cudaStream_t stream) {
-    if (j.quality == ASTC_QUALITY_THOROUGH) return launch_encode_thorough(j, stream);
+    // both fits: THOROUGH, and the fixed mode or the search with ASTC_AXIS_BEST
+    if (j.quality == ASTC_QUALITY_THOROUGH || (j.quality <= ASTC_QUALITY_SEARCH && j.axis == ASTC_AXIS_BEST))
+        return launch_encode_thorough(j, stream);
     if (j.quality == ASTC_QUALITY_PARTITIONS) return launch_encode_partitions(j, stream);
     if (j.quality == ASTC_QUALITY_THREE_PARTITIONS) return launch_encode_three(j, stream);
     return launch_search_kernels<0>(j, stream);

@@ -64,8 +64,9 @@ struct SearchLaunch {
     TextureView tex;
     long long nblocks;
     uint4* out;
-    int axis;     // 0 = PCA, 1 = max accumulation
-    int search;   // 0 = fixed mode, 1 = search, 2 = search from the better fit
+    int axis;     // 0 = PCA, 1 = max accumulation (the kernels with both fits ignore it)
+    int search;   // 0 = fixed mode, 1 = the weight-range search
+    int dual;     // dual-plane candidates (THOROUGH and above)
 };
 
 template <bool ALPHA>
@@ -194,9 +195,10 @@ __device__ __forceinline__ void pick_fit(const uint32_t (&tw)[DIM * DIM], const 
     }
 }
 
-// MODE 0: fixed mode (max-accumulation axis) or SEARCH; 1: THOROUGH (both
-// fits, the search, dual-plane candidates); 2: THOROUGH plus two-partition
-// candidates; 3 (RGB only): 2 plus three-partition candidates.
+// MODE 0: fixed mode (max-accumulation axis) or SEARCH from one fit; 1: both
+// fits (ASTC_AXIS_BEST: the fixed mode or the search from the better;
+// THOROUGH: the search and dual-plane candidates); 2: THOROUGH plus
+// two-partition candidates; 3 (RGB only): 2 plus three-partition candidates.
 template <int DIM, bool ALPHA, bool NORMAL, bool SRGB, int MODE>
 __global__ void __launch_bounds__(kSearchThreads, 3) astc_encode_blocks_search(const SearchLaunch p) {
     constexpr int N = DIM * DIM;
@@ -240,13 +242,19 @@ __global__ void __launch_bounds__(kSearchThreads, 3) astc_encode_blocks_search(c
     uint4 blk;
     uint32_t err = 0;
     if constexpr (DIM == 6) {
+#pragma unroll
+        for (int k = 0; k < N; ++k) tw[k] = target_word<ALPHA, NORMAL, SRGB>(px[k], sm.tbyte);
+        if constexpr (thorough) {
+            pick_fit<DIM, ALPHA, SRGB>(tw, sm, q0, q1, qw, fixed, fixed_b, rw_packed);
+            if (!p.search) {                       // ASTC_AXIS_BEST, fixed mode
+                p.out[b] = fixed;
+                return;
+            }
+        }
         extern __shared__ float4 s_grid[];
         SharedTexels<16> grid{s_grid + threadIdx.x, (int)blockDim.x};
 #pragma unroll
         for (int g = 0; g < 16; ++g) grid.put(g, grid_sample<DIM>(st, g));
-#pragma unroll
-        for (int k = 0; k < N; ++k) tw[k] = target_word<ALPHA, NORMAL, SRGB>(px[k], sm.tbyte);
-        if constexpr (thorough) pick_fit<DIM, ALPHA, SRGB>(tw, sm, q0, q1, qw, fixed, fixed_b, rw_packed);
         blk = search_block<DIM, ALPHA, SRGB>(grid, tw, q0, q1, qw, fixed, sm, &err);
         // an exact block stays: later candidates must decode with less error
         if (err == 0) {
@@ -254,8 +262,9 @@ __global__ void __launch_bounds__(kSearchThreads, 3) astc_encode_blocks_search(c
             return;
         }
         if constexpr (thorough)
-            blk = dual_plane_block<DIM, ALPHA, SRGB>(st, grid, tw, BlockError<DIM, ALPHA, SRGB>::target_sq(tw), err,
-                                                     blk, sm, ds);
+            if (p.dual)
+                blk = dual_plane_block<DIM, ALPHA, SRGB>(st, grid, tw, BlockError<DIM, ALPHA, SRGB>::target_sq(tw),
+                                                         err, blk, sm, ds);
         if constexpr (MODE >= 2) {
             // the partition candidates' per-texel weights, [texel][thread],
             // after the grid colours: a region of their own, since their float
@@ -270,20 +279,27 @@ __global__ void __launch_bounds__(kSearchThreads, 3) astc_encode_blocks_search(c
                                                            blk, sm, p3, g_classes3, tws);
         }
     } else {
+#pragma unroll
+        for (int k = 0; k < N; ++k) tw[k] = target_word<ALPHA, NORMAL, SRGB>(px[k], sm.tbyte);
+        if constexpr (thorough) {
+            pick_fit<DIM, ALPHA, SRGB>(tw, sm, q0, q1, qw, fixed, fixed_b, rw_packed);
+            if (!p.search) {                       // ASTC_AXIS_BEST, fixed mode
+                p.out[b] = fixed;
+                return;
+            }
+        }
         RegTexels<16> grid;
 #pragma unroll
         for (int g = 0; g < 16; ++g) grid.put(g, grid_sample<DIM>(st, g));
-#pragma unroll
-        for (int k = 0; k < N; ++k) tw[k] = target_word<ALPHA, NORMAL, SRGB>(px[k], sm.tbyte);
-        if constexpr (thorough) pick_fit<DIM, ALPHA, SRGB>(tw, sm, q0, q1, qw, fixed, fixed_b, rw_packed);
         blk = search_block<DIM, ALPHA, SRGB>(grid, tw, q0, q1, qw, fixed, sm, &err);
         if (err == 0) {
             p.out[b] = blk;
             return;
         }
         if constexpr (thorough)
-            blk = dual_plane_block<DIM, ALPHA, SRGB>(st, grid, tw, BlockError<DIM, ALPHA, SRGB>::target_sq(tw), err,
-                                                     blk, sm, ds);
+            if (p.dual)
+                blk = dual_plane_block<DIM, ALPHA, SRGB>(st, grid, tw, BlockError<DIM, ALPHA, SRGB>::target_sq(tw),
+                                                         err, blk, sm, ds);
         if constexpr (MODE >= 2) {
             char none = 0;
             blk = two_partition_block<DIM, ALPHA, SRGB>(st, tw, BlockError<DIM, ALPHA, SRGB>::target_sq(tw), q0,
@@ -342,6 +358,7 @@ cudaError_t launch_search_kernels(const EncodeJob& j, cudaStream_t stream) {
     p.out = reinterpret_cast<uint4*>(j.out);
     p.axis = j.axis;
     p.search = j.quality == ASTC_QUALITY_FAST ? 0 : 1;
+    p.dual = j.quality >= ASTC_QUALITY_THOROUGH ? 1 : 0;
     const bool alpha = j.has_alpha != 0, normal = j.is_normal != 0, srgb = j.srgb != 0;
     cudaError_t e;
     if constexpr (RGB_ONLY) {

@@ -307,7 +307,7 @@ def _psnr_blocks(native, blocks: np.ndarray, tex: np.ndarray, spec: dict) -> flo
 def _bench_search(torch, native, headline: str, texs, outs, spec: dict) -> dict:
     """Throughput and decoded PSNR of the quality modes -- the search (every
     single-partition 4x4-grid mode, least decoded error), the max-accumulation
-    axis, THOROUGH (search from the better fit, plus dual-plane blocks),
+    axis, the better of both fits (ASTC_AXIS_BEST), THOROUGH (search from the better fit, plus dual-plane blocks),
     PARTITIONS (THOROUGH plus two-partition blocks) and THREE_PARTITIONS
     (PARTITIONS plus three-partition RGB blocks) -- against the fixed mode, on
     each workload and on flat-colour graphics (synth.ui_shapes, 4x4 RGB, where
@@ -336,6 +336,7 @@ def _bench_search(torch, native, headline: str, texs, outs, spec: dict) -> dict:
         tex0 = st[0].cpu().numpy()
         entry = {"textures_per_step": len(st)}
         for label, kw in (("fast", {}), ("search", dict(quality=1)), ("max_accumulation", dict(axis=1)),
+                          ("best_fit", dict(axis=2)),
                           ("thorough", dict(quality=2)), ("partitions", dict(quality=3)),
                           ("three_partitions", dict(quality=4))):
             run = dict(sspec, **kw)

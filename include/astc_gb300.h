@@ -65,9 +65,18 @@ typedef enum astc_memory {
 typedef enum astc_axis {
     ASTC_AXIS_PCA = 0,           /* principal_component_analysis, the
                                     reference's fit (ASTC_Encode.hlsl:514)   */
-    ASTC_AXIS_MAX_ACCUMULATION = 1 /* max_accumulation_pixel_direction, the
-                                    reference's alternative fit, defined but
-                                    commented out (170-227, 515)             */
+    ASTC_AXIS_MAX_ACCUMULATION = 1, /* max_accumulation_pixel_direction,
+                                    the reference's alternative fit, defined
+                                    but commented out (170-227, 515)         */
+    ASTC_AXIS_BEST = 2           /* both fits; the one whose fixed-mode
+                                    block decodes with the smaller squared
+                                    error against the texels rounded to
+                                    bytes (the PCA on ties) is kept, or with
+                                    ASTC_QUALITY_SEARCH searched from.  Most
+                                    of THOROUGH's gain on alpha cut-outs at
+                                    about three times THOROUGH's speed; FP32
+                                    only (THOROUGH and above use both fits
+                                    whatever the axis)                      */
 } astc_axis;
 
 typedef enum astc_quality {

@@ -938,12 +938,14 @@ struct Pipe {
         for (int g = 0; g < 16; ++g) wv[g] = tb.wunq[wq][tb.scramble[wq][q[g]]];
     }
 
-    // The fixed-mode block, then every weight range QUANT_3..QUANT_32 with
-    // its endpoint range; the first candidate with the least error is kept.
-    // axis 2 fits both ways and searches from the fit whose fixed-mode block
-    // has the smaller error (the PCA on ties).
+    // The fixed-mode block, then (ranges) every weight range QUANT_3..QUANT_32
+    // with its endpoint range; the first candidate with the least error is
+    // kept.  axis 2 fits both ways and keeps the fit whose fixed-mode block has
+    // the smaller error (the PCA on ties); dual adds dual-plane candidates,
+    // partitions 1 / 2 two- / two- and three-partition candidates.
     static void search(const T (*tex)[4], int dim, bool alpha, bool srgb, int axis, uint8_t out[16],
-                       int* chosen, uint32_t* best_err, uint32_t* fixed_err, int partitions = 0) {
+                       int* chosen, uint32_t* best_err, uint32_t* fixed_err, int partitions, bool ranges,
+                       bool dual) {
         const int nch = alpha ? 4 : 3;
         int tb[36][4];
         for (int i = 0; i < dim * dim; ++i)
@@ -972,6 +974,10 @@ struct Pipe {
         int wv[16];
         *fixed_err = best;
         *chosen = -1;
+        if (!ranges) {
+            *best_err = best;
+            return;
+        }
         T s[16][4];
         for (int g = 0; g < 16; ++g) grid_sample(tex, dim, g, s[g]);
         Trial keep = {};
@@ -984,7 +990,7 @@ struct Pipe {
             if (err < best) { best = err; *chosen = wq; keep = tr; }
         }
         if (*chosen >= 0) assemble_trial(keep, alpha, out);
-        if (axis == 2) {
+        if (dual) {
             // dual-plane blocks (THOROUGH and above)
             uint8_t dblk[16];
             int dch = -1;
@@ -1510,7 +1516,7 @@ struct Pipe {
         if (!rgba || !out || !o || w <= 0 || h <= 0) return -1;
         if (o->block_dim != 4 && o->block_dim != 6) return -2;
         if (o->border != 0 && o->border != 1) return -3;
-        if (o->axis != 0 && o->axis != 1) return -4;
+        if (o->axis < 0 || o->axis > 2) return -4;
         if (o->quality < 0 || o->quality > 4) return -5;
         tables();
         const int dim = o->block_dim;
@@ -1526,11 +1532,13 @@ struct Pipe {
             const int by = (int)(b / nbx), bx = (int)(b - (long long)by * nbx);
             T tex[36][4];
             fetch(rgba, w, h, bx, by, *o, tex);
-            if (o->quality) {
+            if (o->quality || o->axis == 2) {
+                // quality 0 with axis 2: the better of the two fixed-mode blocks
                 int chosen;
                 uint32_t err, err_fixed;
                 search(tex, dim, o->has_alpha != 0, o->srgb != 0, o->quality >= 2 ? 2 : o->axis,
-                       out + 16 * b, &chosen, &err, &err_fixed, o->quality >= 3 ? o->quality - 2 : 0);
+                       out + 16 * b, &chosen, &err, &err_fixed, o->quality >= 3 ? o->quality - 2 : 0,
+                       o->quality >= 1, o->quality >= 2);
                 continue;
             }
             uint32_t ep[8], qw[16];
@@ -2021,7 +2029,7 @@ int oracle_search_block_fp32(const float* texels, int block_dim, int has_alpha, 
         for (int c = 0; c < 4; ++c) tex[i][c] = texels[4 * i + c];
     if (partitions < 0 || partitions > 2) return -1;
     Pipe<F32>::search(tex, block_dim, has_alpha != 0, srgb != 0, axis, out, chosen_wq, err, err_fixed,
-                      partitions);
+                      partitions, true, axis == 2);
     return 0;
 }
 

@@ -35,7 +35,9 @@ typedef struct oracle_opts {
     int axis;        /* 0 = principal_component_analysis (the shader's
                         call, ASTC_Encode.hlsl:514), 1 = the shader's
                         alternative max_accumulation_pixel_direction
-                        (170-227, commented out at 515)                     */
+                        (170-227, commented out at 515), 2 = both, keeping
+                        the fit whose fixed-mode block decodes with the
+                        smaller squared error (the PCA on ties)             */
     int quality;     /* 0 = the shader's fixed mode (518-522); 1 = search:
                         the fixed-mode block plus every single-partition
                         4x4-grid weight range QUANT_3..QUANT_32 with the

@@ -80,7 +80,8 @@ def encode(rgba: np.ndarray, block_dim: int = 4, has_alpha: bool = False, is_nor
            axis: int = 0, quality: int = 0) -> np.ndarray:
     """FP32 (or FP64 twin) oracle encode of a (H, W, 4) uint8 image -> (n, 16) uint8.
 
-    axis 1 = max_accumulation_pixel_direction instead of the PCA; quality 1 =
+    axis 1 = max_accumulation_pixel_direction instead of the PCA, axis 2 = both,
+    the fit whose fixed-mode block decodes better (the PCA on ties); quality 1 =
     search over the single-partition weight/endpoint ranges; 2 = the search
     from the better of both fits plus dual-plane blocks; 3 = 2 plus
     two-partition blocks; 4 = 3 plus three-partition blocks."""

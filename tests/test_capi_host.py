@@ -60,7 +60,7 @@ def test_encoded_size(native):
 
 
 @pytest.mark.parametrize("field,value", [("block_dim", 5), ("border", 2), ("precision", 7),
-                                         ("memory", 3), ("axis", 2), ("quality", -1),
+                                         ("memory", 3), ("axis", 3), ("quality", -1),
                                          ("quality", 5)])
 def test_bad_options_rejected(native, field, value):
     lib = native.load_library()
@@ -73,7 +73,7 @@ def test_bad_options_rejected(native, field, value):
     assert lib.astc_last_error()
 
 
-@pytest.mark.parametrize("axis,quality", [(1, 0), (0, 1), (1, 1), (0, 2), (0, 3), (0, 4)])
+@pytest.mark.parametrize("axis,quality", [(1, 0), (2, 0), (0, 1), (1, 1), (2, 1), (0, 2), (0, 3), (0, 4)])
 def test_half2_rejects_search_and_axis(native, axis, quality):
     """The max-accumulation axis and the mode search are FP32 only."""
     lib = native.load_library()

@@ -146,6 +146,9 @@ def test_cli_reads_reference_leaf(native, tmp_path, reference_dir):
     (["-6x6", "-alpha", "-srgb", "--thorough"], dict(block_dim=6, has_alpha=True, srgb=True, quality=2)),
     (["--partitions"], dict(block_dim=4, quality=3)),
     (["-6x6", "--three-partitions"], dict(block_dim=6, quality=4)),
+    (["-alpha", "--best-fit"], dict(block_dim=4, has_alpha=True, axis=2)),
+    (["-6x6", "-alpha", "-srgb", "--best-fit", "--search"], dict(block_dim=6, has_alpha=True, srgb=True, axis=2,
+                                                               quality=1)),
 ])
 def test_cli_encode_matches_library(native, oracle, tmp_path, flags, opts):
     rng = np.random.default_rng(len(flags))

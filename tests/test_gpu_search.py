@@ -36,8 +36,8 @@ def _psnr(a, b):
     return float("inf") if mse == 0 else 10 * np.log10(255.0 ** 2 / mse)
 
 
-GRID = [g for g in itertools.product([4, 6], [False, True], [False, True], [False, True], [0, 1], [0, 1, 2, 3, 4])
-        if (g[4] or g[5]) and not (g[5] >= 2 and g[4] == 1)]
+GRID = [g for g in itertools.product([4, 6], [False, True], [False, True], [False, True], [0, 1, 2], [0, 1, 2, 3, 4])
+        if (g[4] or g[5]) and not (g[5] >= 2 and g[4] != 0)]
 
 
 @pytest.mark.parametrize("dim,alpha,normal,srgb,axis,quality", GRID)

@@ -334,9 +334,41 @@ def test_three_partitions_image(oracle, dim):
     assert np.array_equal(oracle.encode(rgba, block_dim=dim, has_alpha=True, quality=4), a3)
 
 
+@pytest.mark.parametrize("dim", [4, 6])
+@pytest.mark.parametrize("alpha", [False, True])
+def test_best_fit_fast_mode(oracle, dim, alpha):
+    """axis 2 with the fixed mode: every block is the PCA block or the
+    max-accumulation block, whichever decodes with the smaller squared error
+    (the PCA on ties)."""
+    rgba = synth.rgb_noise(96, 96, seed=31) if not alpha else synth.rgba_cutout(96, 96, seed=32)
+    blocks = [oracle.encode(rgba, block_dim=dim, has_alpha=alpha, axis=a) for a in (0, 1, 2)]
+    ch = 4 if alpha else 3
+    nb = -(-96 // dim)
+
+    def block_sse(blk):
+        d, errors = oracle.decode(blk, 96, 96, dim)
+        assert errors == 0
+        diff = (d[..., :ch].astype(np.int64) - rgba[..., :ch]) ** 2
+        pad = np.zeros((nb * dim, nb * dim, ch), np.int64)
+        pad[:96, :96] = diff
+        return pad.reshape(nb, dim, nb, dim, ch).sum(axis=(1, 3, 4)).ravel()
+
+    e0, e1, e2 = (block_sse(b) for b in blocks)
+    # zero border: blocks cut by the image edge score their padded texels, so
+    # compare the blocks inside the image
+    inside = np.zeros((nb, nb), bool)
+    inside[: 96 // dim, : 96 // dim] = True
+    inside = inside.ravel()
+    pick1 = e1 < e0
+    want = np.where(pick1[:, None], blocks[1], blocks[0])
+    assert np.array_equal(blocks[2][inside], want[inside])
+    assert np.array_equal(e2[inside], np.minimum(e0, e1)[inside])
+    assert pick1[inside].any() and (~pick1[inside]).any()
+
+
 def test_bad_axis_and_quality_rejected(oracle):
     with pytest.raises(ValueError):
-        oracle.encode(np.zeros((4, 4, 4), np.uint8), axis=2)
+        oracle.encode(np.zeros((4, 4, 4), np.uint8), axis=3)
     with pytest.raises(ValueError):
         oracle.encode(np.zeros((4, 4, 4), np.uint8), quality=5)
 
