@@ -8,7 +8,9 @@
 namespace astc {
 
 cudaError_t launch_encode_search(const EncodeJob& j, cudaStream_t stream) {
-    // both fits: THOROUGH, and the fixed mode or the search with ASTC_AXIS_BEST
+    // ASTC_AXIS_BEST with the fixed mode: its own register-resident kernel
+    if (j.quality == ASTC_QUALITY_FAST && j.axis == ASTC_AXIS_BEST) return launch_encode_best(j, stream);
+    // both fits: THOROUGH, and the search with ASTC_AXIS_BEST
     if (j.quality == ASTC_QUALITY_THOROUGH || (j.quality <= ASTC_QUALITY_SEARCH && j.axis == ASTC_AXIS_BEST))
         return launch_encode_thorough(j, stream);
     if (j.quality == ASTC_QUALITY_PARTITIONS) return launch_encode_partitions(j, stream);

@@ -43,6 +43,7 @@ cudaError_t launch_encode_thorough(const EncodeJob& job, cudaStream_t stream);
 // THOROUGH plus two-partition candidates (astc_encode_partitions.cu).
 cudaError_t launch_encode_partitions(const EncodeJob& job, cudaStream_t stream);
 cudaError_t launch_encode_three(const EncodeJob& job, cudaStream_t stream);
+cudaError_t launch_encode_best(const EncodeJob& job, cudaStream_t stream);
 
 // Decoder / SSE launchers (astc_decode.cu).
 cudaError_t launch_decode(const uint8_t* blocks, int width, int height, int bw, int bh,
