@@ -74,9 +74,10 @@ typedef enum astc_axis {
                                     bytes (the PCA on ties) is kept, or with
                                     ASTC_QUALITY_SEARCH searched from.  Most
                                     of THOROUGH's gain on alpha cut-outs at
-                                    about three times THOROUGH's speed; FP32
-                                    only (THOROUGH and above use both fits
-                                    whatever the axis)                      */
+                                    4-5 times THOROUGH's speed (40-45% of
+                                    the fixed mode's); FP32 only (THOROUGH
+                                    and above use both fits whatever the
+                                    axis)                                   */
 } astc_axis;
 
 typedef enum astc_quality {
