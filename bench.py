@@ -70,7 +70,7 @@ def _parse():
     ap.add_argument("--profile-case", action="store_true",
                     help="small case for ncu: 2 textures per step, encode launches only")
     ap.add_argument("--profile-quality", default="fast",
-                    choices=["fast", "search", "thorough", "partitions", "three_partitions"],
+                    choices=["fast", "best_fit", "search", "thorough", "partitions", "three_partitions"],
                     help="with --profile-case: the quality mode the launches use (FP32)")
     return ap.parse_args()
 
@@ -567,9 +567,9 @@ def run_ours(args) -> None:
 
     if args.profile_case:
         # only the encode launches: warm-up, then the timed steps; no other kernels
-        quality = {"fast": 0, "search": 1, "thorough": 2, "partitions": 3,
-                   "three_partitions": 4}[args.profile_quality]
-        spec_prof = dict(spec_run, quality=quality) if quality else spec_run
+        quality, axis = {"fast": (0, 0), "best_fit": (0, 2), "search": (1, 0), "thorough": (2, 0),
+                         "partitions": (3, 0), "three_partitions": (4, 0)}[args.profile_quality]
+        spec_prof = dict(spec_run, quality=quality, axis=axis) if (quality or axis) else spec_run
         _time_launches(torch, native, texs, outs, spec_prof, max(3, args.warmup))
         per, _, launches = _time_launches(torch, native, texs, outs, spec_prof, args.steps)
         store, threads = native.get_kernel_choice(dim, spec["has_alpha"], spec["is_normal"], spec["srgb"])
