@@ -4,6 +4,7 @@
 // PNG chunk layout, filters 0-4 and colour types the PNG specification.
 #include "image_load.h"
 
+#include <ctype.h>
 #include <stdio.h>
 #include <string.h>
 
@@ -342,6 +343,112 @@ bool decode_pnm(const uint8_t* d, size_t n, Image& img, std::string& err) {
     return true;
 }
 
+// Truevision TGA: image types 2 / 10 (true colour, 24 or 32 bit BGR(A)), 3 / 11
+// (8-bit grey), raw or run-length encoded; bit 5 of the descriptor says the
+// rows run top-down, otherwise bottom-up.
+bool decode_tga(const uint8_t* d, size_t n, Image& img, std::string& err) {
+    if (n < 18) { err = "TGA header too short"; return false; }
+    const int idlen = d[0], cmap = d[1], type = d[2];
+    const int w = d[12] | (d[13] << 8), h = d[14] | (d[15] << 8), bpp = d[16], desc = d[17];
+    const bool rle = type == 10 || type == 11, grey = type == 3 || type == 11;
+    if (cmap != 0 || !(type == 2 || type == 3 || type == 10 || type == 11)) {
+        err = "unsupported TGA type (colour-mapped or not an image)";
+        return false;
+    }
+    if (w <= 0 || h <= 0 || (grey ? bpp != 8 : (bpp != 24 && bpp != 32))) {
+        err = "unsupported TGA pixel depth";
+        return false;
+    }
+    const int px = bpp / 8;
+    size_t pos = 18 + (size_t)idlen;
+    std::vector<uint8_t> raw((size_t)w * h * px);
+    if (!rle) {
+        if (pos + raw.size() > n) { err = "TGA data too short"; return false; }
+        std::copy(d + pos, d + pos + raw.size(), raw.begin());
+    } else {
+        size_t o = 0;
+        while (o < raw.size()) {
+            if (pos >= n) { err = "TGA data too short"; return false; }
+            const int c = d[pos++], count = (c & 0x7F) + 1;
+            if (o + (size_t)count * px > raw.size()) { err = "TGA run past the image"; return false; }
+            if (c & 0x80) {                               // one pixel repeated
+                if (pos + px > n) { err = "TGA data too short"; return false; }
+                for (int i = 0; i < count; ++i, o += px) std::copy(d + pos, d + pos + px, raw.begin() + o);
+                pos += px;
+            } else {                                      // count literal pixels
+                if (pos + (size_t)count * px > n) { err = "TGA data too short"; return false; }
+                std::copy(d + pos, d + pos + (size_t)count * px, raw.begin() + o);
+                pos += (size_t)count * px;
+                o += (size_t)count * px;
+            }
+        }
+    }
+    img.width = w;
+    img.height = h;
+    img.rgba.assign((size_t)w * h * 4, 255);
+    const bool top_down = (desc >> 5) & 1;
+    for (int y = 0; y < h; ++y) {
+        const uint8_t* s = raw.data() + (size_t)(top_down ? y : h - 1 - y) * w * px;
+        uint8_t* o = img.rgba.data() + (size_t)y * w * 4;
+        for (int x = 0; x < w; ++x, s += px, o += 4) {
+            if (grey) { o[0] = o[1] = o[2] = s[0]; continue; }
+            o[0] = s[2]; o[1] = s[1]; o[2] = s[0];
+            if (px == 4) o[3] = s[3];
+        }
+    }
+    return true;
+}
+
+// Windows BMP with a BITMAPINFOHEADER (or later): 24-bit BGR and 32-bit BGRA,
+// uncompressed or 32-bit with bit-field masks; rows bottom-up unless the
+// height is negative; 24-bit rows padded to 4 bytes.
+bool decode_bmp(const uint8_t* d, size_t n, Image& img, std::string& err) {
+    auto u16 = [&](size_t o) { return (uint32_t)d[o] | ((uint32_t)d[o + 1] << 8); };
+    auto u32 = [&](size_t o) { return u16(o) | (u16(o + 2) << 16); };
+    if (n < 54 || d[0] != 'B' || d[1] != 'M') { err = "not a BMP file"; return false; }
+    const uint32_t off = u32(10), hdr = u32(14);
+    if (hdr < 40) { err = "unsupported BMP header"; return false; }
+    const int w = (int)u32(18), hraw = (int)u32(22), bpp = (int)u16(28), comp = (int)u32(30);
+    const bool top_down = hraw < 0;
+    const int h = top_down ? -hraw : hraw;
+    if (w <= 0 || h <= 0 || (bpp != 24 && bpp != 32) || !(comp == 0 || (comp == 3 && bpp == 32))) {
+        err = "unsupported BMP format (24/32-bit uncompressed or 32-bit bit fields only)";
+        return false;
+    }
+    uint32_t mask[4] = {0x00FF0000u, 0x0000FF00u, 0x000000FFu, bpp == 32 ? 0xFF000000u : 0u};
+    if (comp == 3) {
+        if (14 + 40 + 12 > n) { err = "BMP masks missing"; return false; }
+        for (int c = 0; c < 3; ++c) mask[c] = u32(54 + 4 * c);
+        mask[3] = hdr >= 56 && 14 + 56 <= n ? u32(54 + 12) : 0u;
+    }
+    const size_t stride = ((size_t)w * (bpp / 8) + 3) & ~(size_t)3;
+    if ((size_t)off + stride * h > n) { err = "BMP data too short"; return false; }
+    img.width = w;
+    img.height = h;
+    img.rgba.assign((size_t)w * h * 4, 255);
+    auto channel = [](uint32_t v, uint32_t m) -> uint8_t {
+        if (!m) return 255;
+        int shift = 0;
+        while (!((m >> shift) & 1)) ++shift;
+        const uint32_t x = (v & m) >> shift, top = m >> shift;
+        return (uint8_t)(top == 255 ? x : (x * 255 + top / 2) / top);
+    };
+    for (int y = 0; y < h; ++y) {
+        const uint8_t* s = d + off + (size_t)(top_down ? y : h - 1 - y) * stride;
+        uint8_t* o = img.rgba.data() + (size_t)y * w * 4;
+        for (int x = 0; x < w; ++x, o += 4) {
+            if (bpp == 24) {
+                o[0] = s[3 * x + 2]; o[1] = s[3 * x + 1]; o[2] = s[3 * x];
+            } else {
+                const uint32_t v = (uint32_t)s[4 * x] | ((uint32_t)s[4 * x + 1] << 8) |
+                                   ((uint32_t)s[4 * x + 2] << 16) | ((uint32_t)s[4 * x + 3] << 24);
+                for (int c = 0; c < 4; ++c) o[c] = channel(v, mask[c]);
+            }
+        }
+    }
+    return true;
+}
+
 bool load_image(const std::string& path, Image& img, std::string& err) {
     FILE* f = fopen(path.c_str(), "rb");
     if (!f) { err = "cannot open " + path; return false; }
@@ -351,7 +458,15 @@ bool load_image(const std::string& path, Image& img, std::string& err) {
     while ((got = fread(buf, 1, sizeof(buf), f)) > 0) data.insert(data.end(), buf, buf + got);
     fclose(f);
     if (data.size() >= 8 && data[0] == 0x89 && data[1] == 'P') return decode_png(data.data(), data.size(), img, err);
-    return decode_pnm(data.data(), data.size(), img, err);
+    if (data.size() >= 2 && data[0] == 'P' && data[1] >= '5' && data[1] <= '7')
+        return decode_pnm(data.data(), data.size(), img, err);
+    if (data.size() >= 2 && data[0] == 'B' && data[1] == 'M') return decode_bmp(data.data(), data.size(), img, err);
+    const size_t dot = path.find_last_of('.');
+    std::string ext = dot == std::string::npos ? "" : path.substr(dot + 1);
+    for (auto& c : ext) c = (char)tolower((unsigned char)c);
+    if (ext == "tga") return decode_tga(data.data(), data.size(), img, err);   // TGA has no magic number
+    err = "unsupported image format (PNG, PAM/PPM/PGM, BMP and TGA are read)";
+    return false;
 }
 
 bool save_pam(const std::string& path, const Image& img, std::string& err) {

@@ -1,7 +1,9 @@
 """The drop-in command line tool astc_cs_enc (reference: main.cpp:140-258).
 
 CPU tests exercise its image reader through --dump-rgba (no GPU): PNGs of
-every colour type and all five row filters written here with zlib, and PAM.
+every colour type and all five row filters written here with zlib, PAM, TGA
+(grey / BGR / BGRA, raw and run-length encoded, either row order) and BMP
+(24-bit padded rows, 32-bit, bit fields, either row order).
 GPU tests run the full encode and compare the written .astc with the
 library's blocks for the flipped image, and the reference's own leaf.astc.
 """
@@ -114,6 +116,97 @@ def test_cli_reads_16bit_png_and_pam(native, tmp_path):
     img = rng.integers(0, 256, (11, 13, 4), dtype=np.uint8)
     pam.write_bytes(b"P7\nWIDTH 13\nHEIGHT 11\nDEPTH 4\nMAXVAL 255\nTUPLTYPE RGB_ALPHA\nENDHDR\n" + img.tobytes())
     assert np.array_equal(_dump(native, str(pam), tmp_path), img[::-1])
+
+
+def _tga(path, arr, rle=False, top_down=False):
+    """Writes a TGA: (h, w) grey, (h, w, 3) BGR or (h, w, 4) BGRA from RGB(A)."""
+    h, w = arr.shape[:2]
+    grey = arr.ndim == 2
+    px = arr if grey else arr[..., [2, 1, 0] + ([3] if arr.shape[2] == 4 else [])]
+    bpp = 8 if grey else 8 * arr.shape[2]
+    rows = px if top_down else px[::-1]
+    flat = rows.reshape(h * w, -1).astype(np.uint8)
+    body = bytearray()
+    if not rle:
+        body += flat.tobytes()
+    else:
+        i = 0
+        while i < len(flat):
+            run = 1
+            while i + run < len(flat) and run < 128 and np.array_equal(flat[i + run], flat[i]):
+                run += 1
+            if run > 1:
+                body.append(0x80 | (run - 1))
+                body += flat[i].tobytes()
+                i += run
+                continue
+            lit = 1
+            while i + lit < len(flat) and lit < 128 and not (
+                    i + lit + 1 < len(flat) and np.array_equal(flat[i + lit], flat[i + lit + 1])):
+                lit += 1
+            body.append(lit - 1)
+            body += flat[i:i + lit].tobytes()
+            i += lit
+    itype = (11 if rle else 3) if grey else (10 if rle else 2)
+    head = struct.pack("<BBBHHBHHHHBB", 3, 0, itype, 0, 0, 0, 0, 0, w, h, bpp, 0x20 if top_down else 0)
+    with open(path, "wb") as fh:
+        fh.write(head + b"abc" + bytes(body))
+
+
+def _bmp(path, arr, top_down=False, bitfields=False):
+    """Writes a BMP from (h, w, 3) RGB (24-bit) or (h, w, 4) RGBA (32-bit)."""
+    h, w, c = arr.shape
+    bpp = 8 * c
+    stride = (w * c + 3) & ~3
+    rows = arr if top_down else arr[::-1]
+    data = bytearray()
+    for r in rows:
+        line = r[:, [2, 1, 0] + ([3] if c == 4 else [])].astype(np.uint8).tobytes()
+        data += line + b"\0" * (stride - len(line))
+    masks = struct.pack("<IIII", 0x00FF0000, 0x0000FF00, 0x000000FF, 0xFF000000) if bitfields else b""
+    hdr_size = 56 if bitfields else 40
+    off = 14 + hdr_size
+    info = struct.pack("<IiiHHIIiiII", hdr_size, w, -h if top_down else h, 1, bpp, 3 if bitfields else 0,
+                       len(data), 2835, 2835, 0, 0) + masks
+    with open(path, "wb") as fh:
+        fh.write(b"BM" + struct.pack("<IHHI", off + len(data), 0, 0, off) + info + bytes(data))
+
+
+@pytest.mark.parametrize("channels", [1, 3, 4])
+@pytest.mark.parametrize("rle", [False, True])
+@pytest.mark.parametrize("top_down", [False, True])
+def test_cli_reads_tga(native, tmp_path, channels, rle, top_down):
+    rng = np.random.default_rng(17 + channels)
+    shape = (19, 23) if channels == 1 else (19, 23, channels)
+    arr = rng.integers(0, 256, shape, dtype=np.uint8)
+    arr[3:9, 2:15] = arr[3, 2]                          # runs for the RLE encoder
+    path = str(tmp_path / "in.tga")
+    _tga(path, arr, rle=rle, top_down=top_down)
+    want = np.full((19, 23, 4), 255, np.uint8)
+    if channels == 1:
+        want[..., :3] = arr[..., None]
+    else:
+        want[..., :channels] = arr
+    assert np.array_equal(_dump(native, path, tmp_path), want[::-1])
+
+
+@pytest.mark.parametrize("channels,bitfields", [(3, False), (4, False), (4, True)])
+@pytest.mark.parametrize("top_down", [False, True])
+def test_cli_reads_bmp(native, tmp_path, channels, bitfields, top_down):
+    rng = np.random.default_rng(29 + channels)
+    arr = rng.integers(0, 256, (13, 21, channels), dtype=np.uint8)     # 21 * 3 rows need padding
+    path = str(tmp_path / "in.bmp")
+    _bmp(path, arr, top_down=top_down, bitfields=bitfields)
+    want = np.full((13, 21, 4), 255, np.uint8)
+    want[..., :channels] = arr
+    assert np.array_equal(_dump(native, path, tmp_path), want[::-1])
+
+
+def test_cli_rejects_unknown_format(native, tmp_path):
+    path = tmp_path / "in.xyz"
+    path.write_bytes(b"\x00\x01garbage")
+    r = subprocess.run([CLI, str(path)], capture_output=True, text=True)
+    assert r.returncode != 0 and "unsupported image format" in r.stdout
 
 
 def test_cli_argument_errors(native, tmp_path):
