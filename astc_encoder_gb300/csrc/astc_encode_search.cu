@@ -1,8 +1,10 @@
 // astc_encode_search.cu -- instantiates the search kernel
 // (astc_search_kernel.cuh) for the fixed mode with the max-accumulation axis
-// and for the search from one fit; hands ASTC_QUALITY_THOROUGH to
-// astc_encode_thorough.cu and ASTC_QUALITY_PARTITIONS to
-// astc_encode_partitions.cu.  Compiled with --fmad=false.
+// and for the search from one fit, and routes the other quality modes:
+// ASTC_AXIS_BEST with the fixed mode to astc_encode_best.cu, the both-fits
+// modes to astc_encode_thorough.cu, ASTC_QUALITY_PARTITIONS to
+// astc_encode_partitions.cu, ASTC_QUALITY_THREE_PARTITIONS to
+// astc_encode_three.cu.  Compiled with --fmad=false.
 #include "astc_search_kernel.cuh"
 
 namespace astc {

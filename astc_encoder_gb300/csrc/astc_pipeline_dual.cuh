@@ -1,5 +1,5 @@
 // astc_pipeline_dual.cuh -- dual-plane candidates of the FP32 encoder's
-// ASTC_QUALITY_THOROUGH and ASTC_QUALITY_PARTITIONS modes.  The reference
+// quality modes from ASTC_QUALITY_THOROUGH up.  The reference
 // shader writes the dual-plane bit of its block mode as a constant 0
 // (assemble_blockmode, ASTC_Encode.hlsl:446-473).
 //
