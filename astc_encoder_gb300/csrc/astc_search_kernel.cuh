@@ -1,23 +1,27 @@
 // astc_search_kernel.cuh -- the sm_103a kernel of the FP32 encoder's
-// reference-defined alternatives to its fixed pipeline, included by the two
-// translation units that instantiate it (astc_encode_search.cu: fixed mode
-// with the max-accumulation axis, and the search; astc_encode_thorough.cu:
-// the search from the better of both fits), so each compiles in parallel
-// and gets its own register allocation:
+// reference-defined alternatives to its fixed pipeline, included by the
+// translation units that instantiate it (astc_encode_search.cu: the fixed
+// mode with the max-accumulation axis, and the search from one fit;
+// astc_encode_thorough.cu: both fits; astc_encode_partitions.cu and
+// astc_encode_three.cu: the partition modes), so each compiles in parallel and
+// gets its own register allocation:
 //   axis   = ASTC_AXIS_MAX_ACCUMULATION: the endpoint fit the reference
 //            shader defines but leaves commented out
 //            (max_accumulation_pixel_direction, ASTC_Encode.hlsl:170-227, 515);
+//   axis   = ASTC_AXIS_BEST with ASTC_QUALITY_SEARCH: both fits, the search
+//            from the one whose fixed-mode block decodes with the smaller
+//            error (the fixed mode with it has a kernel of its own,
+//            astc_encode_best.cu);
 //   quality = ASTC_QUALITY_SEARCH: the choose_best_quantmethod the shader
 //            sketches at 524-526 -- every single-partition 4x4-grid mode,
 //            scored by its exact decode (astc_pipeline_search.cuh);
 //   quality = ASTC_QUALITY_THOROUGH: both fits, the search from the one
 //            whose fixed-mode block decodes with the smaller error (the
-//            PCA on ties);
+//            PCA on ties), dual-plane candidates (astc_pipeline_dual.cuh);
 //   quality = ASTC_QUALITY_PARTITIONS: THOROUGH plus two-partition
-//            candidates (astc_pipeline_partition.cuh; astc_encode_partitions.cu);
+//            candidates (astc_pipeline_partition.cuh);
 //   quality = ASTC_QUALITY_THREE_PARTITIONS: PARTITIONS plus three-partition
-//            candidates for RGB blocks (astc_pipeline_partition3.cuh;
-//            astc_encode_three.cu).
+//            candidates for RGB blocks (astc_pipeline_partition3.cuh).
 // One thread encodes one block.  Texels stay packed (one register each) and
 // are re-decoded per pass, which keeps the 36-texel 6x6 search in registers.
 // Compile including units with --fmad=false: blocks are bit-identical to the
