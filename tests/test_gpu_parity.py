@@ -312,7 +312,12 @@ def test_concurrent_host_threads(native):
             opts = dict(block_dim=4, has_alpha=False)
         else:
             img = _texture(300, 257, seed=300 + i)                       # device pointers
-            opts = dict(block_dim=4, has_alpha=True, quality=1)
+            # the quality kernels, including the 6x6 partition kernel that
+            # raises its shared-memory limit on every launch
+            opts = [dict(block_dim=4, has_alpha=True, quality=1),
+                    dict(block_dim=6, has_alpha=True, srgb=True, border=1, quality=3),
+                    dict(block_dim=4, quality=4),
+                    dict(block_dim=6, has_alpha=True, srgb=True, border=1, axis=2)][i // 3]
         jobs.append((i, img, opts, native.encode(img, **opts)))
     torch.cuda.synchronize()
     results = {}
