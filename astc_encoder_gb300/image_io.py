@@ -1,11 +1,14 @@
-"""Image loading for the encoder's command line (PNG, PAM/PPM/PGM).
+"""Image loading for the encoder's command line (PNG, PAM/PPM/PGM, BMP, TGA).
 
 The reference loads images with stb_image forced to RGBA and flipped
 vertically (main.cpp:24-25).  This module is a small self-contained reader:
 PNG (8-bit greyscale / grey+alpha / RGB / RGBA / palette, non-interlaced,
-all five row filters, zlib from the Python standard library) and Netpbm
-P5/P6/P7.  It always returns a (H, W, 4) uint8 array, row 0 first; the caller
-flips when it wants the reference's orientation.
+all five row filters, zlib from the Python standard library), Netpbm
+P5/P6/P7, Windows BMP (24/32-bit, uncompressed or bit fields) and Truevision
+TGA (8-bit grey, 24/32-bit true colour, raw or run-length encoded) -- the
+same formats as the C++ reader of the command line tool.  It always returns
+a (H, W, 4) uint8 array, row 0 first; the caller flips when it wants the
+reference's orientation.
 """
 from __future__ import annotations
 
@@ -146,9 +149,93 @@ def load_pnm(path: str) -> np.ndarray:
     return out
 
 
+def load_bmp(path: str) -> np.ndarray:
+    with open(path, "rb") as fh:
+        data = fh.read()
+    if data[:2] != b"BM" or len(data) < 54:
+        raise ValueError("not a BMP file")
+    off, hdr = struct.unpack_from("<I", data, 10)[0], struct.unpack_from("<I", data, 14)[0]
+    w, hraw, _, bpp, comp = struct.unpack_from("<iiHHI", data, 18)
+    if hdr < 40 or w <= 0 or hraw == 0 or bpp not in (24, 32) or not (comp == 0 or (comp == 3 and bpp == 32)):
+        raise ValueError("unsupported BMP format (24/32-bit uncompressed or 32-bit bit fields only)")
+    h = abs(hraw)
+    masks = [0x00FF0000, 0x0000FF00, 0x000000FF, 0xFF000000 if bpp == 32 else 0]
+    if comp == 3:
+        masks[:3] = struct.unpack_from("<III", data, 54)
+        masks[3] = struct.unpack_from("<I", data, 66)[0] if hdr >= 56 else 0
+    c = bpp // 8
+    stride = (w * c + 3) & ~3
+    rows = np.frombuffer(data, np.uint8, stride * h, off).reshape(h, stride)[:, :w * c].reshape(h, w, c)
+    if hraw > 0:
+        rows = rows[::-1]
+    out = np.full((h, w, 4), 255, np.uint8)
+    if bpp == 24:
+        out[..., :3] = rows[..., [2, 1, 0]]
+        return out
+    v = rows.astype(np.uint32)
+    v = v[..., 0] | (v[..., 1] << 8) | (v[..., 2] << 16) | (v[..., 3] << 24)
+    for ch, m in enumerate(masks):
+        if not m:
+            continue
+        shift = (m & -m).bit_length() - 1
+        top = m >> shift
+        x = (v & m) >> shift
+        out[..., ch] = x if top == 255 else (x * 255 + top // 2) // top
+    return out
+
+
+def load_tga(path: str) -> np.ndarray:
+    with open(path, "rb") as fh:
+        data = fh.read()
+    if len(data) < 18:
+        raise ValueError("TGA header too short")
+    idlen, cmap, itype = data[0], data[1], data[2]
+    w, h = struct.unpack_from("<HH", data, 12)
+    bpp, desc = data[16], data[17]
+    grey = itype in (3, 11)
+    if cmap != 0 or itype not in (2, 3, 10, 11) or w == 0 or h == 0 or bpp != (8 if grey else bpp) or \
+            (not grey and bpp not in (24, 32)):
+        raise ValueError("unsupported TGA file")
+    px = bpp // 8
+    pos = 18 + idlen
+    n = w * h * px
+    if itype in (2, 3):
+        raw = np.frombuffer(data, np.uint8, n, pos)
+    else:
+        buf = bytearray()
+        while len(buf) < n:
+            c = data[pos]
+            pos += 1
+            count = (c & 0x7F) + 1
+            if c & 0x80:
+                buf += data[pos:pos + px] * count
+                pos += px
+            else:
+                buf += data[pos:pos + count * px]
+                pos += count * px
+        raw = np.frombuffer(bytes(buf[:n]), np.uint8)
+    raw = raw.reshape(h, w, px)
+    if not (desc >> 5) & 1:
+        raw = raw[::-1]
+    out = np.full((h, w, 4), 255, np.uint8)
+    if grey:
+        out[..., :3] = raw[..., :1]
+    else:
+        out[..., :3] = raw[..., [2, 1, 0]]
+        if px == 4:
+            out[..., 3] = raw[..., 3]
+    return out
+
+
 def load_image(path: str) -> np.ndarray:
     with open(path, "rb") as fh:
         head = fh.read(8)
     if head == PNG_SIG:
         return load_png(path)
-    return load_pnm(path)
+    if head[:1] == b"P" and head[1:2] in (b"5", b"6", b"7"):
+        return load_pnm(path)
+    if head[:2] == b"BM":
+        return load_bmp(path)
+    if path.lower().endswith(".tga"):                  # TGA has no magic number
+        return load_tga(path)
+    raise ValueError("unsupported image format (PNG, PAM/PPM/PGM, BMP and TGA are read)")

@@ -188,6 +188,8 @@ def test_cli_reads_tga(native, tmp_path, channels, rle, top_down):
     else:
         want[..., :channels] = arr
     assert np.array_equal(_dump(native, path, tmp_path), want[::-1])
+    from astc_encoder_gb300 import image_io                 # the Python reader agrees
+    assert np.array_equal(image_io.load_image(path), want)
 
 
 @pytest.mark.parametrize("channels,bitfields", [(3, False), (4, False), (4, True)])
@@ -200,6 +202,8 @@ def test_cli_reads_bmp(native, tmp_path, channels, bitfields, top_down):
     want = np.full((13, 21, 4), 255, np.uint8)
     want[..., :channels] = arr
     assert np.array_equal(_dump(native, path, tmp_path), want[::-1])
+    from astc_encoder_gb300 import image_io                 # the Python reader agrees
+    assert np.array_equal(image_io.load_image(path), want)
 
 
 def test_cli_rejects_unknown_format(native, tmp_path):
