@@ -1,10 +1,12 @@
-// image_load.cpp -- PNG / Netpbm reader for the command line tool.
+// image_load.cpp -- PNG / JPEG / Netpbm / BMP / TGA reader for the command
+// line tool.
 // Inflate follows RFC 1951 (stored, fixed and dynamic Huffman blocks,
 // canonical codes decoded one bit at a time); the zlib wrapper RFC 1950;
 // PNG chunk layout, filters 0-4 and colour types the PNG specification.
 #include "image_load.h"
 
 #include <ctype.h>
+#include <math.h>
 #include <stdio.h>
 #include <string.h>
 
@@ -449,6 +451,271 @@ bool decode_bmp(const uint8_t* d, size_t n, Image& img, std::string& err) {
     return true;
 }
 
+// Baseline sequential JPEG (ITU-T T.81: SOF0 / SOF1, 8-bit samples, Huffman
+// coding, one grey or three YCbCr components with sampling factors 1..2,
+// restart intervals).  Coefficients are dequantised and taken through a
+// separable floating-point inverse DCT (+128, rounded, clamped); chroma is
+// upsampled by replication and converted with the JFIF equations.
+// Progressive, arithmetic-coded, 12-bit and CMYK files are refused.
+namespace {
+
+struct JpegHuff {
+    uint8_t count[17] = {};                  // codes of each length 1..16
+    uint8_t sym[256] = {};
+    int mincode[17] = {}, maxcode[18] = {}, valptr[17] = {};
+    bool present = false;
+    void build() {
+        int code = 0, k = 0;
+        for (int l = 1; l <= 16; ++l) {
+            valptr[l] = k;
+            mincode[l] = code;
+            code += count[l];
+            k += count[l];
+            maxcode[l] = count[l] ? code - 1 : -1;
+            code <<= 1;
+        }
+        maxcode[17] = 0x7FFFFFFF;
+    }
+};
+
+struct JpegBits {
+    const uint8_t* d;
+    size_t n, pos;
+    uint32_t acc = 0;
+    int bits = 0;
+    bool marker = false;                     // hit a marker: only zero bits follow
+    int fill_byte() {
+        if (marker || pos >= n) return 0;
+        uint8_t b = d[pos];
+        if (b == 0xFF) {
+            const uint8_t nx = pos + 1 < n ? d[pos + 1] : 0;
+            if (nx == 0x00) { pos += 2; return 0xFF; }
+            marker = true;                   // RSTn or another marker: stop here
+            return 0;
+        }
+        ++pos;
+        return b;
+    }
+    int bit() {
+        if (bits == 0) { acc = (uint32_t)fill_byte(); bits = 8; }
+        --bits;
+        return (int)((acc >> bits) & 1u);
+    }
+    int get(int k) {
+        int v = 0;
+        for (int i = 0; i < k; ++i) v = (v << 1) | bit();
+        return v;
+    }
+    void reset() { bits = 0; }
+};
+
+int jpeg_decode_sym(JpegBits& b, const JpegHuff& h) {
+    int code = 0;
+    for (int l = 1; l <= 16; ++l) {
+        code = (code << 1) | b.bit();
+        if (h.count[l] && code <= h.maxcode[l]) return h.sym[h.valptr[l] + code - h.mincode[l]];
+    }
+    return -1;
+}
+
+int jpeg_extend(int v, int t) { return t == 0 ? 0 : (v < (1 << (t - 1)) ? v - (1 << t) + 1 : v); }
+
+const uint8_t kZigzag[64] = {0,  1,  8,  16, 9,  2,  3,  10, 17, 24, 32, 25, 18, 11, 4,  5,
+                             12, 19, 26, 33, 40, 48, 41, 34, 27, 20, 13, 6,  7,  14, 21, 28,
+                             35, 42, 49, 56, 57, 50, 43, 36, 29, 22, 15, 23, 30, 37, 44, 51,
+                             58, 59, 52, 45, 38, 31, 39, 46, 53, 60, 61, 54, 47, 55, 62, 63};
+
+void jpeg_idct(const float in[64], uint8_t* out, int stride) {
+    static float cosv[8][8];
+    static bool init = false;
+    if (!init) {
+        for (int x = 0; x < 8; ++x)
+            for (int u = 0; u < 8; ++u)
+                cosv[x][u] = (float)((u == 0 ? std::sqrt(0.5) : 1.0) * std::cos((2 * x + 1) * u * 3.14159265358979323846 / 16.0));
+        init = true;
+    }
+    float tmp[64];
+    for (int y = 0; y < 8; ++y)                       // rows: over u
+        for (int x = 0; x < 8; ++x) {
+            float s = 0.0f;
+            for (int u = 0; u < 8; ++u) s += cosv[x][u] * in[y * 8 + u];
+            tmp[y * 8 + x] = s * 0.5f;
+        }
+    for (int x = 0; x < 8; ++x)                       // columns: over v
+        for (int y = 0; y < 8; ++y) {
+            float s = 0.0f;
+            for (int v = 0; v < 8; ++v) s += cosv[y][v] * tmp[v * 8 + x];
+            const float r = std::floor(s * 0.5f + 128.5f);
+            out[y * stride + x] = (uint8_t)(r < 0.0f ? 0 : r > 255.0f ? 255 : r);
+        }
+}
+
+}  // namespace
+
+bool decode_jpeg(const uint8_t* d, size_t n, Image& img, std::string& err) {
+    if (n < 4 || d[0] != 0xFF || d[1] != 0xD8) { err = "not a JPEG file"; return false; }
+    uint16_t qt[4][64] = {};
+    JpegHuff hdc[4], hac[4];
+    struct Comp { int id, h, v, tq, td = 0, ta = 0; std::vector<uint8_t> plane; int pw = 0, ph = 0; int dc = 0; };
+    std::vector<Comp> comps;
+    int width = 0, height = 0, restart = 0, hmax = 1, vmax = 1;
+    bool frame = false, done = false;
+    size_t pos = 2;
+    auto u16 = [&](size_t o) { return (int)((d[o] << 8) | d[o + 1]); };
+    while (pos + 4 <= n && !done) {
+        if (d[pos] != 0xFF) { ++pos; continue; }
+        const int m = d[pos + 1];
+        if (m == 0xFF) { ++pos; continue; }
+        if (m == 0xD8 || (m >= 0xD0 && m <= 0xD7) || m == 0x01) { pos += 2; continue; }
+        if (m == 0xD9) break;
+        const int len = u16(pos + 2);
+        const size_t seg = pos + 4, end = pos + 2 + (size_t)len;
+        if (len < 2 || end > n) { err = "JPEG segment past the end"; return false; }
+        if (m == 0xDB) {                                          // DQT
+            for (size_t o = seg; o < end;) {
+                const int pq = d[o] >> 4, tq = d[o] & 15;
+                ++o;
+                if (tq > 3 || o + (pq ? 128 : 64) > end) { err = "bad JPEG quantisation table"; return false; }
+                for (int i = 0; i < 64; ++i) qt[tq][kZigzag[i]] = pq ? (uint16_t)u16(o + 2 * i) : d[o + i];
+                o += pq ? 128 : 64;
+            }
+        } else if (m == 0xC4) {                                   // DHT
+            for (size_t o = seg; o < end;) {
+                const int tc = d[o] >> 4, th = d[o] & 15;
+                if (tc > 1 || th > 3 || o + 17 > end) { err = "bad JPEG Huffman table"; return false; }
+                JpegHuff& h = tc ? hac[th] : hdc[th];
+                int total = 0;
+                for (int l = 1; l <= 16; ++l) { h.count[l] = d[o + l]; total += h.count[l]; }
+                if (total > 256 || o + 17 + total > end) { err = "bad JPEG Huffman table"; return false; }
+                for (int i = 0; i < total; ++i) h.sym[i] = d[o + 17 + i];
+                h.build();
+                h.present = true;
+                o += 17 + total;
+            }
+        } else if (m == 0xC0 || m == 0xC1) {                      // SOF0 / SOF1
+            if (d[seg] != 8) { err = "only 8-bit JPEG is read"; return false; }
+            height = u16(seg + 1);
+            width = u16(seg + 3);
+            const int nc = d[seg + 5];
+            if (width <= 0 || height <= 0 || (nc != 1 && nc != 3) || seg + 6 + 3 * (size_t)nc > end) {
+                err = "unsupported JPEG frame (grey or YCbCr only)";
+                return false;
+            }
+            for (int i = 0; i < nc; ++i) {
+                Comp c;
+                c.id = d[seg + 6 + 3 * i];
+                c.h = d[seg + 7 + 3 * i] >> 4;
+                c.v = d[seg + 7 + 3 * i] & 15;
+                c.tq = d[seg + 8 + 3 * i] & 3;
+                if (c.h < 1 || c.h > 2 || c.v < 1 || c.v > 2) { err = "unsupported JPEG sampling"; return false; }
+                hmax = std::max(hmax, c.h);
+                vmax = std::max(vmax, c.v);
+                comps.push_back(c);
+            }
+            if (nc == 1) comps[0].h = comps[0].v = hmax = vmax = 1;   // one component: blocks in raster order
+            frame = true;
+        } else if ((m >= 0xC2 && m <= 0xCF) && m != 0xC4 && m != 0xC8 && m != 0xCC) {
+            err = "progressive, lossless or arithmetic-coded JPEG is not read";
+            return false;
+        } else if (m == 0xDD) {                                   // DRI
+            restart = u16(seg);
+        } else if (m == 0xDA) {                                   // SOS: one interleaved scan
+            if (!frame) { err = "JPEG scan before the frame header"; return false; }
+            const int ns = d[seg];
+            if (ns != (int)comps.size()) { err = "non-interleaved JPEG scans are not read"; return false; }
+            for (int i = 0; i < ns; ++i) {
+                const int id = d[seg + 1 + 2 * i], t = d[seg + 2 + 2 * i];
+                bool found = false;
+                for (auto& c : comps)
+                    if (c.id == id) { c.td = t >> 4; c.ta = t & 15; found = true; }
+                if (!found) { err = "JPEG scan names an unknown component"; return false; }
+            }
+            for (auto& c : comps)
+                if (c.td > 3 || c.ta > 3 || !hdc[c.td].present || !hac[c.ta].present) {
+                    err = "JPEG Huffman table missing";
+                    return false;
+                }
+            const int mcux = (width + 8 * hmax - 1) / (8 * hmax), mcuy = (height + 8 * vmax - 1) / (8 * vmax);
+            for (auto& c : comps) {
+                c.pw = mcux * c.h * 8;
+                c.ph = mcuy * c.v * 8;
+                c.plane.assign((size_t)c.pw * c.ph, 0);
+                c.dc = 0;
+            }
+            JpegBits bits{d, n, end};
+            float blk[64];
+            int mcus = 0;
+            for (int my = 0; my < mcuy; ++my)
+                for (int mx = 0; mx < mcux; ++mx) {
+                    if (restart && mcus > 0 && mcus % restart == 0) {
+                        // the RSTn marker ends the interval: realign, reset predictors
+                        bits.reset();
+                        while (bits.pos + 1 < n && !(d[bits.pos] == 0xFF && d[bits.pos + 1] >= 0xD0 &&
+                                                     d[bits.pos + 1] <= 0xD7))
+                            ++bits.pos;
+                        bits.pos += 2;
+                        bits.marker = false;
+                        for (auto& c : comps) c.dc = 0;
+                    }
+                    ++mcus;
+                    for (auto& c : comps)
+                        for (int by = 0; by < c.v; ++by)
+                            for (int bx = 0; bx < c.h; ++bx) {
+                                for (int i = 0; i < 64; ++i) blk[i] = 0.0f;
+                                const int t = jpeg_decode_sym(bits, hdc[c.td]);
+                                if (t < 0 || t > 11) { err = "corrupt JPEG data"; return false; }
+                                c.dc += jpeg_extend(bits.get(t), t);
+                                blk[0] = (float)(c.dc * (int)qt[c.tq][0]);
+                                for (int k = 1; k < 64;) {
+                                    const int rs = jpeg_decode_sym(bits, hac[c.ta]);
+                                    if (rs < 0) { err = "corrupt JPEG data"; return false; }
+                                    const int r = rs >> 4, sz = rs & 15;
+                                    if (sz == 0) {
+                                        if (r != 15) break;           // EOB
+                                        k += 16;                      // ZRL
+                                        continue;
+                                    }
+                                    k += r;
+                                    if (k > 63) { err = "corrupt JPEG data"; return false; }
+                                    const int z = kZigzag[k];
+                                    blk[z] = (float)(jpeg_extend(bits.get(sz), sz) * (int)qt[c.tq][z]);
+                                    ++k;
+                                }
+                                const int ox = (mx * c.h + bx) * 8, oy = (my * c.v + by) * 8;
+                                jpeg_idct(blk, c.plane.data() + (size_t)oy * c.pw + ox, c.pw);
+                            }
+                }
+            done = true;
+        }
+        pos = end;
+    }
+    if (!done) { err = "JPEG has no image scan"; return false; }
+    img.width = width;
+    img.height = height;
+    img.rgba.assign((size_t)width * height * 4, 255);
+    for (int y = 0; y < height; ++y)
+        for (int x = 0; x < width; ++x) {
+            float v[3];
+            for (size_t c = 0; c < comps.size(); ++c) {
+                const Comp& k = comps[c];
+                const int sx = x * k.h / hmax, sy = y * k.v / vmax;   // replication
+                v[c] = k.plane[(size_t)sy * k.pw + sx];
+            }
+            uint8_t* o = img.rgba.data() + ((size_t)y * width + x) * 4;
+            if (comps.size() == 1) {
+                o[0] = o[1] = o[2] = (uint8_t)v[0];
+                continue;
+            }
+            const float cb = v[1] - 128.0f, cr = v[2] - 128.0f;
+            const float rgb[3] = {v[0] + 1.402f * cr, v[0] - 0.344136f * cb - 0.714136f * cr, v[0] + 1.772f * cb};
+            for (int c = 0; c < 3; ++c) {
+                const float r = std::floor(rgb[c] + 0.5f);
+                o[c] = (uint8_t)(r < 0.0f ? 0 : r > 255.0f ? 255 : r);
+            }
+        }
+    return true;
+}
+
 bool load_image(const std::string& path, Image& img, std::string& err) {
     FILE* f = fopen(path.c_str(), "rb");
     if (!f) { err = "cannot open " + path; return false; }
@@ -461,11 +728,13 @@ bool load_image(const std::string& path, Image& img, std::string& err) {
     if (data.size() >= 2 && data[0] == 'P' && data[1] >= '5' && data[1] <= '7')
         return decode_pnm(data.data(), data.size(), img, err);
     if (data.size() >= 2 && data[0] == 'B' && data[1] == 'M') return decode_bmp(data.data(), data.size(), img, err);
+    if (data.size() >= 3 && data[0] == 0xFF && data[1] == 0xD8 && data[2] == 0xFF)
+        return decode_jpeg(data.data(), data.size(), img, err);
     const size_t dot = path.find_last_of('.');
     std::string ext = dot == std::string::npos ? "" : path.substr(dot + 1);
     for (auto& c : ext) c = (char)tolower((unsigned char)c);
     if (ext == "tga") return decode_tga(data.data(), data.size(), img, err);   // TGA has no magic number
-    err = "unsupported image format (PNG, PAM/PPM/PGM, BMP and TGA are read)";
+    err = "unsupported image format (PNG, JPEG, PAM/PPM/PGM, BMP and TGA are read)";
     return false;
 }
 

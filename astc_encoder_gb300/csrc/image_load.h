@@ -1,8 +1,9 @@
 // image_load.h -- image reader for the command line tool: PNG (own inflate,
 // RFC 1950/1951; 8-bit grey, grey+alpha, RGB, RGBA and palette; 16-bit
 // channels reduced to their high byte; non-interlaced), Netpbm P5/P6/P7,
-// Windows BMP (24/32-bit, uncompressed or bit fields) and Truevision TGA
-// (24/32-bit true colour and 8-bit grey, raw or run-length encoded).
+// Windows BMP (24/32-bit, uncompressed or bit fields), Truevision TGA
+// (24/32-bit true colour and 8-bit grey, raw or run-length encoded) and
+// baseline JPEG (8-bit grey or YCbCr, Huffman coded, one interleaved scan).
 // Output is always RGBA8, row 0 first (the caller flips for the reference's
 // orientation, main.cpp:24).  Written for this project; the reference uses
 // the third-party stb_image for the same job.
@@ -25,6 +26,7 @@ bool decode_png(const uint8_t* data, size_t size, Image& out, std::string& err);
 bool decode_pnm(const uint8_t* data, size_t size, Image& out, std::string& err);
 bool decode_bmp(const uint8_t* data, size_t size, Image& out, std::string& err);
 bool decode_tga(const uint8_t* data, size_t size, Image& out, std::string& err);
+bool decode_jpeg(const uint8_t* data, size_t size, Image& out, std::string& err);
 // zlib stream (2-byte header, deflate blocks, Adler-32) -> raw bytes.
 bool zlib_inflate(const uint8_t* data, size_t size, std::vector<uint8_t>& out, std::string& err);
 // Writes RGBA8 as a P7 (PAM) file.

@@ -1,11 +1,12 @@
-"""Image loading for the encoder's command line (PNG, PAM/PPM/PGM, BMP, TGA).
+"""Image loading for the encoder's command line (PNG, JPEG, PAM/PPM/PGM, BMP, TGA).
 
 The reference loads images with stb_image forced to RGBA and flipped
 vertically (main.cpp:24-25).  This module is a small self-contained reader:
 PNG (8-bit greyscale / grey+alpha / RGB / RGBA / palette, non-interlaced,
 all five row filters, zlib from the Python standard library), Netpbm
-P5/P6/P7, Windows BMP (24/32-bit, uncompressed or bit fields) and Truevision
-TGA (8-bit grey, 24/32-bit true colour, raw or run-length encoded) -- the
+P5/P6/P7, Windows BMP (24/32-bit, uncompressed or bit fields), Truevision
+TGA (8-bit grey, 24/32-bit true colour, raw or run-length encoded) and
+baseline JPEG (8-bit grey or YCbCr, Huffman coded, one interleaved scan) -- the
 same formats as the C++ reader of the command line tool.  It always returns
 a (H, W, 4) uint8 array, row 0 first; the caller flips when it wants the
 reference's orientation.
@@ -227,6 +228,200 @@ def load_tga(path: str) -> np.ndarray:
     return out
 
 
+_ZIGZAG = np.array([0, 1, 8, 16, 9, 2, 3, 10, 17, 24, 32, 25, 18, 11, 4, 5, 12, 19, 26, 33, 40, 48,
+                    41, 34, 27, 20, 13, 6, 7, 14, 21, 28, 35, 42, 49, 56, 57, 50, 43, 36, 29, 22,
+                    15, 23, 30, 37, 44, 51, 58, 59, 52, 45, 38, 31, 39, 46, 53, 60, 61, 54, 47, 55,
+                    62, 63])
+
+
+def _jpeg_huffman(counts, syms):
+    """(code length, code) -> symbol, as a 16-bit peek table of (symbol, length)."""
+    table = np.full((1 << 16, 2), -1, np.int32)
+    code, k = 0, 0
+    for length in range(1, 17):
+        for _ in range(counts[length - 1]):
+            lo = code << (16 - length)
+            table[lo:lo + (1 << (16 - length))] = (syms[k], length)
+            code += 1
+            k += 1
+        code <<= 1
+    return table
+
+
+def load_jpeg(path: str) -> np.ndarray:
+    """Baseline sequential JPEG (ITU-T T.81 SOF0/SOF1, 8-bit, Huffman, grey or
+    YCbCr with sampling factors 1..2, one interleaved scan, restart intervals):
+    the same decoding as the command line tool's reader, in float64."""
+    with open(path, "rb") as fh:
+        d = fh.read()
+    if d[:2] != b"\xff\xd8":
+        raise ValueError("not a JPEG file")
+    qt = np.zeros((4, 64), np.int64)
+    huff = {}
+    comps, restart, pos = [], 0, 2
+    width = height = 0
+    while pos + 4 <= len(d):
+        if d[pos] != 0xFF:
+            pos += 1
+            continue
+        m = d[pos + 1]
+        if m == 0xFF:
+            pos += 1
+            continue
+        if m == 0xD8 or 0xD0 <= m <= 0xD7 or m == 0x01:
+            pos += 2
+            continue
+        if m == 0xD9:
+            break
+        length = struct.unpack_from(">H", d, pos + 2)[0]
+        seg, end = pos + 4, pos + 2 + length
+        if m == 0xDB:
+            o = seg
+            while o < end:
+                pq, tq = d[o] >> 4, d[o] & 15
+                vals = struct.unpack_from(">64H", d, o + 1) if pq else list(d[o + 1:o + 65])
+                qt[tq, _ZIGZAG] = vals
+                o += 129 if pq else 65
+        elif m == 0xC4:
+            o = seg
+            while o < end:
+                counts = d[o + 1:o + 17]
+                total = sum(counts)
+                huff[(d[o] >> 4, d[o] & 15)] = _jpeg_huffman(counts, d[o + 17:o + 17 + total])
+                o += 17 + total
+        elif m in (0xC0, 0xC1):
+            if d[seg] != 8:
+                raise ValueError("only 8-bit JPEG is read")
+            height, width = struct.unpack_from(">HH", d, seg + 1)
+            nc = d[seg + 5]
+            if nc not in (1, 3):
+                raise ValueError("unsupported JPEG frame (grey or YCbCr only)")
+            for i in range(nc):
+                c = d[seg + 6 + 3 * i:seg + 9 + 3 * i]
+                comps.append({"id": c[0], "h": c[1] >> 4, "v": c[1] & 15, "tq": c[2] & 3})
+            if nc == 1:
+                comps[0]["h"] = comps[0]["v"] = 1
+        elif 0xC2 <= m <= 0xCF and m not in (0xC4, 0xC8, 0xCC):
+            raise ValueError("progressive, lossless or arithmetic-coded JPEG is not read")
+        elif m == 0xDD:
+            restart = struct.unpack_from(">H", d, seg)[0]
+        elif m == 0xDA:
+            ns = d[seg]
+            if ns != len(comps):
+                raise ValueError("non-interleaved JPEG scans are not read")
+            for i in range(ns):
+                cid, t = d[seg + 1 + 2 * i], d[seg + 2 + 2 * i]
+                for c in comps:
+                    if c["id"] == cid:
+                        c["td"], c["ta"] = t >> 4, t & 15
+            return _jpeg_scan(d, end, width, height, comps, qt, huff, restart)
+        pos = end
+    raise ValueError("JPEG has no image scan")
+
+
+def _jpeg_segments(d, pos):
+    """The entropy-coded data from pos, split at RSTn markers, unstuffed."""
+    segs, cur = [], bytearray()
+    while pos < len(d):
+        b = d[pos]
+        if b == 0xFF and pos + 1 < len(d):
+            nx = d[pos + 1]
+            if nx == 0x00:
+                cur.append(0xFF)
+                pos += 2
+                continue
+            if 0xD0 <= nx <= 0xD7:
+                segs.append(bytes(cur))
+                cur = bytearray()
+                pos += 2
+                continue
+            break
+        cur.append(b)
+        pos += 1
+    segs.append(bytes(cur))
+    return segs
+
+
+def _jpeg_scan(d, pos, width, height, comps, qt, huff, restart):
+    hmax = max(c["h"] for c in comps)
+    vmax = max(c["v"] for c in comps)
+    mcux, mcuy = -(-width // (8 * hmax)), -(-height // (8 * vmax))
+    nmcu = mcux * mcuy
+    segs = _jpeg_segments(d, pos)
+    coef = [np.zeros((mcuy * c["v"], mcux * c["h"], 64), np.float64) for c in comps]
+    seg_i, data, bitpos, dc = -1, b"", 0, [0] * len(comps)
+
+    def bits(k):
+        nonlocal bitpos
+        v = 0
+        for _ in range(k):
+            byte = bitpos >> 3
+            b = data[byte] if byte < len(data) else 0
+            v = (v << 1) | ((b >> (7 - (bitpos & 7))) & 1)
+            bitpos += 1
+        return v
+
+    def sym(table):
+        nonlocal bitpos
+        byte = bitpos >> 3
+        w = int.from_bytes((data[byte:byte + 3] + b"\0\0\0")[:3], "big")
+        peek = (w >> (8 - (bitpos & 7))) & 0xFFFF
+        s, length = table[peek]
+        if length < 0:
+            raise ValueError("corrupt JPEG data")
+        bitpos += int(length)
+        return int(s)
+
+    def extend(v, t):
+        return 0 if t == 0 else (v - (1 << t) + 1 if v < (1 << (t - 1)) else v)
+
+    for n in range(nmcu):
+        if n == 0 or (restart and n % restart == 0):
+            seg_i += 1
+            data = segs[seg_i] if seg_i < len(segs) else b""
+            bitpos, dc = 0, [0] * len(comps)
+        my, mx = divmod(n, mcux)
+        for ci, c in enumerate(comps):
+            dct, act = huff[(0, c["td"])], huff[(1, c["ta"])]
+            for by in range(c["v"]):
+                for bx in range(c["h"]):
+                    blk = coef[ci][my * c["v"] + by, mx * c["h"] + bx]
+                    t = sym(dct)
+                    dc[ci] += extend(bits(t), t)
+                    blk[0] = dc[ci]
+                    k = 1
+                    while k < 64:
+                        rs = sym(act)
+                        r, sz = rs >> 4, rs & 15
+                        if sz == 0:
+                            if r != 15:
+                                break
+                            k += 16
+                            continue
+                        k += r
+                        blk[_ZIGZAG[k]] = extend(bits(sz), sz)
+                        k += 1
+    xs = np.arange(8)
+    cosv = np.cos((2 * xs[:, None] + 1) * xs[None, :] * np.pi / 16) * np.where(xs == 0, np.sqrt(0.5), 1.0)
+    planes = []
+    for ci, c in enumerate(comps):
+        blocks = (coef[ci] * qt[c["tq"]]).reshape(coef[ci].shape[:2] + (8, 8))
+        pix = np.einsum("xu,abvu,yv->abyx", cosv, blocks, cosv) * 0.25
+        pix = np.clip(np.floor(pix + 128.5), 0, 255)
+        plane = pix.transpose(0, 2, 1, 3).reshape(blocks.shape[0] * 8, blocks.shape[1] * 8)
+        ys = np.arange(height) * c["v"] // vmax
+        xs_ = np.arange(width) * c["h"] // hmax
+        planes.append(plane[ys][:, xs_])
+    out = np.full((height, width, 4), 255, np.uint8)
+    if len(comps) == 1:
+        out[..., :3] = planes[0][..., None].astype(np.uint8)
+        return out
+    y, cb, cr = planes[0], planes[1] - 128.0, planes[2] - 128.0
+    rgb = np.stack([y + 1.402 * cr, y - 0.344136 * cb - 0.714136 * cr, y + 1.772 * cb], -1)
+    out[..., :3] = np.clip(np.floor(rgb + 0.5), 0, 255).astype(np.uint8)
+    return out
+
+
 def load_image(path: str) -> np.ndarray:
     with open(path, "rb") as fh:
         head = fh.read(8)
@@ -236,6 +431,8 @@ def load_image(path: str) -> np.ndarray:
         return load_pnm(path)
     if head[:2] == b"BM":
         return load_bmp(path)
+    if head[:3] == b"\xff\xd8\xff":
+        return load_jpeg(path)
     if path.lower().endswith(".tga"):                  # TGA has no magic number
         return load_tga(path)
-    raise ValueError("unsupported image format (PNG, PAM/PPM/PGM, BMP and TGA are read)")
+    raise ValueError("unsupported image format (PNG, JPEG, PAM/PPM/PGM, BMP and TGA are read)")

@@ -3,7 +3,11 @@
 CPU tests exercise its image reader through --dump-rgba (no GPU): PNGs of
 every colour type and all five row filters written here with zlib, PAM, TGA
 (grey / BGR / BGRA, raw and run-length encoded, either row order) and BMP
-(24-bit padded rows, 32-bit, bit fields, either row order).
+(24-bit padded rows, 32-bit, bit fields, either row order), and baseline
+JPEG (grey and YCbCr at 4:4:4 / 4:2:2 / 4:4:0 / 4:2:0, restart intervals,
+8- and 16-bit quantisation tables) written here with scipy's orthonormal DCT
+and Huffman tables built from the data, plus a third-party JPEG where one is
+installed.
 GPU tests run the full encode and compare the written .astc with the
 library's blocks for the flipped image, and the reference's own leaf.astc.
 """
@@ -204,6 +208,227 @@ def test_cli_reads_bmp(native, tmp_path, channels, bitfields, top_down):
     assert np.array_equal(_dump(native, path, tmp_path), want[::-1])
     from astc_encoder_gb300 import image_io                 # the Python reader agrees
     assert np.array_equal(image_io.load_image(path), want)
+
+
+# T.81 zig-zag: anti-diagonals in turn, odd ones walked down, even ones up
+ZIGZAG = np.array(sorted(range(64), key=lambda i: (i // 8 + i % 8,
+                                                    (i // 8) if (i // 8 + i % 8) % 2 else (i % 8))))
+
+
+def _huffman_table(freq):
+    """Canonical Huffman code (lengths <= 16) for {symbol: count}; a dummy
+    symbol of count 0 takes the all-ones code, which T.81 reserves."""
+    import heapq
+    freq = dict(freq)
+    while True:
+        heap = [(f, i, [s]) for i, (s, f) in enumerate(sorted(freq.items()))] + [(0, -1, [256])]
+        heapq.heapify(heap)
+        length = {s: 0 for s in list(freq) + [256]}
+        n = len(heap)
+        while len(heap) > 1:
+            fa, _, a = heapq.heappop(heap)
+            fb, _, b = heapq.heappop(heap)
+            for s in a + b:
+                length[s] += 1
+            heapq.heappush(heap, (fa + fb, n, a + b))
+            n += 1
+        if max(length.values()) <= 16:
+            break
+        freq = {s: f // 2 + 1 for s, f in freq.items()}
+    order = sorted(length, key=lambda s: (length[s], s))
+    codes, code, prev = {}, 0, length[order[0]]
+    for s in order:
+        code <<= length[s] - prev
+        prev = length[s]
+        codes[s] = (code, length[s])
+        code += 1
+    counts = [sum(1 for s in order if length[s] == n and s != 256) for n in range(1, 17)]
+    return codes, bytes(counts) + bytes(s for s in order if s != 256)
+
+
+def _jpeg(path, img, sampling=(1, 1), restart=0, q16=False):
+    """Writes a baseline JPEG of img ((H, W) grey or (H, W, 3) RGB) and returns
+    the decoded image a conforming decoder gives (float64, rounded), as RGBA."""
+    from scipy.fft import dctn, idctn
+    h, w = img.shape[:2]
+    x = img.astype(np.float64)
+    if img.ndim == 2:
+        planes, samp = [x], [(1, 1)]
+        sampling = (1, 1)
+    else:
+        r, g, b = x[..., 0], x[..., 1], x[..., 2]
+        planes = [0.299 * r + 0.587 * g + 0.114 * b,
+                  -0.168736 * r - 0.331264 * g + 0.5 * b + 128.0,
+                  0.5 * r - 0.418688 * g - 0.081312 * b + 128.0]
+        samp = [sampling, (1, 1), (1, 1)]
+    hmax, vmax = sampling
+    mcux, mcuy = -(-w // (8 * hmax)), -(-h // (8 * vmax))
+    u = np.arange(8)
+    qts = [2 + (u[:, None] + u[None, :]) // 2, 3 + (u[:, None] + u[None, :])]   # luma, chroma
+    coefs, recon = [], []
+    for ci, (p, (sh, sv)) in enumerate(zip(planes, samp)):
+        full = np.pad(p, ((0, mcuy * 8 * vmax - h), (0, mcux * 8 * hmax - w)), mode="edge")
+        fy, fx = vmax // sv, hmax // sh
+        sub = full.reshape(full.shape[0] // fy, fy, full.shape[1] // fx, fx).mean(axis=(1, 3))
+        bl = (sub - 128.0).reshape(sub.shape[0] // 8, 8, sub.shape[1] // 8, 8).transpose(0, 2, 1, 3)
+        q = qts[min(ci, 1)]
+        c = np.rint(dctn(bl, axes=(2, 3), norm="ortho") / q).astype(np.int64)
+        coefs.append(c)
+        pix = np.clip(np.floor(idctn(c * q, axes=(2, 3), norm="ortho") + 128.5), 0, 255)
+        plane = pix.transpose(0, 2, 1, 3).reshape(sub.shape)
+        recon.append(plane[np.arange(h) * sv // vmax][:, np.arange(w) * sh // hmax])
+    want = np.full((h, w, 4), 255, np.uint8)
+    if img.ndim == 2:
+        want[..., :3] = recon[0][..., None]
+    else:
+        yy, cb, cr = recon[0], recon[1] - 128.0, recon[2] - 128.0
+        rgb = np.stack([yy + 1.402 * cr, yy - 0.344136 * cb - 0.714136 * cr, yy + 1.772 * cb], -1)
+        want[..., :3] = np.clip(np.floor(rgb + 0.5), 0, 255)
+
+    def cat(v):
+        return 0 if v == 0 else abs(int(v)).bit_length()
+
+    def extra(v, t):
+        return v if v >= 0 else v + (1 << t) - 1
+
+    # symbol streams, in MCU order: (table, symbol, extra bits, extra length)
+    segs, stream, pred = [], [], [0] * len(planes)
+    for n in range(mcux * mcuy):
+        if restart and n and n % restart == 0:
+            segs.append(stream)
+            stream, pred = [], [0] * len(planes)
+        my, mx = divmod(n, mcux)
+        for ci, (sh, sv) in enumerate(samp):
+            t = min(ci, 1)
+            for by in range(sv):
+                for bx in range(sh):
+                    zz = coefs[ci][my * sv + by, mx * sh + bx].reshape(64)[ZIGZAG]
+                    diff = int(zz[0]) - pred[ci]
+                    pred[ci] = int(zz[0])
+                    stream.append(((0, t), cat(diff), extra(diff, cat(diff)), cat(diff)))
+                    run, last = 0, max([k for k in range(1, 64) if zz[k]] or [0])
+                    for k in range(1, last + 1):
+                        if zz[k] == 0:
+                            run += 1
+                            continue
+                        while run > 15:
+                            stream.append(((1, t), 0xF0, 0, 0))
+                            run -= 16
+                        sz = cat(zz[k])
+                        stream.append(((1, t), (run << 4) | sz, extra(int(zz[k]), sz), sz))
+                        run = 0
+                    if last < 63:
+                        stream.append(((1, t), 0x00, 0, 0))
+    segs.append(stream)
+    freq = {}
+    for st in segs:
+        for key, sym, _, _ in st:
+            freq.setdefault(key, {}).setdefault(sym, 0)
+            freq[key][sym] += 1
+    tables = {key: _huffman_table(f) for key, f in freq.items()}
+
+    def seg(marker, body):
+        return b"\xff" + bytes([marker]) + struct.pack(">H", len(body) + 2) + body
+    out = b"\xff\xd8" + seg(0xE0, b"JFIF\x00\x01\x01\x00\x00\x01\x00\x01\x00\x00")
+    out += seg(0xFE, b"written by the test suite")
+    for t, q in enumerate(qts[:len(set(min(i, 1) for i in range(len(planes))))]):
+        zq = q.reshape(64)[ZIGZAG]
+        out += seg(0xDB, bytes([(16 if q16 else 0) | t]) +
+                   (struct.pack(">64H", *zq) if q16 else bytes(zq.astype(np.uint8))))
+    out += seg(0xC0, struct.pack(">BHHB", 8, h, w, len(planes)) +
+               b"".join(bytes([ci + 1, (sh << 4) | sv, min(ci, 1)]) for ci, (sh, sv) in enumerate(samp)))
+    for (cls, t), (codes, spec) in sorted(tables.items()):
+        out += seg(0xC4, bytes([(cls << 4) | t]) + spec)
+    if restart:
+        out += seg(0xDD, struct.pack(">H", restart))
+    out += seg(0xDA, bytes([len(planes)]) +
+               b"".join(bytes([ci + 1, (min(ci, 1) << 4) | min(ci, 1)]) for ci in range(len(planes))) +
+               b"\x00\x3f\x00")
+    for i, st in enumerate(segs):
+        bitstr = "".join(format(tables[key][0][sym][0], "0%db" % tables[key][0][sym][1]) +
+                         (format(ev, "0%db" % el) if el else "") for key, sym, ev, el in st)
+        bitstr += "1" * (-len(bitstr) % 8)
+        data = int(bitstr, 2).to_bytes(len(bitstr) // 8, "big") if bitstr else b""
+        out += data.replace(b"\xff", b"\xff\x00")
+        if i + 1 < len(segs):
+            out += bytes([0xFF, 0xD0 + i % 8])
+    out += b"\xff\xd9"
+    with open(path, "wb") as fh:
+        fh.write(out)
+    return want
+
+
+def _smooth(h, w, channels, seed):
+    rng = np.random.default_rng(seed)
+    yy, xx = np.mgrid[0:h, 0:w].astype(np.float64)
+    chans = [128 + 90 * np.sin(xx / (5 + 3 * c) + yy / (7 + c) + c) + rng.normal(0, 4, (h, w))
+             for c in range(channels)]
+    arr = np.clip(np.rint(np.stack(chans, -1)), 0, 255).astype(np.uint8)
+    return arr[..., 0] if channels == 1 else arr
+
+
+def test_jpeg_zigzag_tables():
+    """The readers' zig-zag order against the anti-diagonal walk of T.81 Figure 5."""
+    from astc_encoder_gb300 import image_io
+    assert np.array_equal(image_io._ZIGZAG, ZIGZAG)
+    src = open(os.path.join(ROOT, "astc_encoder_gb300", "csrc", "image_load.cpp")).read()
+    body = src[src.index("kZigzag[64] = {") + 15:]
+    table = [int(v) for v in body[:body.index("}")].replace("\n", " ").split(",")]
+    assert table == list(ZIGZAG)
+
+
+@pytest.mark.parametrize("kind,sampling,restart,q16", [
+    ("grey", (1, 1), 0, False), ("grey", (1, 1), 5, True), ("rgb", (1, 1), 0, False),
+    ("rgb", (2, 2), 0, False), ("rgb", (2, 1), 3, False), ("rgb", (1, 2), 1, True),
+    ("rgb", (2, 2), 2, False)])
+def test_cli_reads_jpeg(native, tmp_path, kind, sampling, restart, q16):
+    img = _smooth(37, 29, 1 if kind == "grey" else 3, seed=sum(sampling) + restart)
+    path = str(tmp_path / "in.jpg")
+    want = _jpeg(path, img, sampling=sampling, restart=restart, q16=q16)
+    got = _dump(native, path, tmp_path)[::-1]
+    assert np.abs(got.astype(int) - want).max() <= 1          # float32 against float64 rounding
+    assert np.mean(got != want) < 0.01
+    from astc_encoder_gb300 import image_io                 # the Python reader agrees
+    py = image_io.load_image(path)
+    assert np.abs(py.astype(int) - want).max() <= 1 and np.mean(py != want) < 0.01
+    ref = np.dstack([img] * 3) if kind == "grey" else img   # and the picture is the input's
+    mse = np.mean((got[..., :3].astype(float) - ref) ** 2)
+    assert 10 * np.log10(255.0 ** 2 / mse) > (33 if sampling == (1, 1) else 25)
+
+
+def test_cli_reads_third_party_jpeg(native, tmp_path):
+    """A baseline JPEG from another encoder (APPn segments, its own tables)."""
+    sample = None
+    try:
+        import sklearn
+        sample = os.path.join(os.path.dirname(sklearn.__file__), "datasets", "images", "china.jpg")
+    except ImportError:
+        pass
+    if sample is None or not os.path.exists(sample):
+        pytest.skip("no third-party JPEG sample here")
+    got = _dump(native, sample, tmp_path)[::-1]
+    from astc_encoder_gb300 import image_io
+    py = image_io.load_image(sample)
+    assert got.shape == (427, 640, 4) and np.abs(py.astype(int) - got).max() <= 1
+    assert np.mean(py != got) < 0.01 and (got[..., 3] == 255).all()
+    # a coherent decode: neighbours agree far better than chance, and the 8x8
+    # block boundaries are no rougher than block interiors (a misplaced
+    # coefficient or a wrong transform shows as block edges)
+    dx = np.abs(np.diff(got[..., :3].astype(int), axis=1)).mean(axis=(0, 2))
+    edges, inner = dx[7::8].mean(), np.delete(dx, np.arange(7, dx.size, 8)).mean()
+    assert dx.mean() < 0.3 * got[..., :3].std() and edges < 1.15 * inner
+
+
+def test_cli_refuses_progressive_jpeg(native, tmp_path):
+    path = str(tmp_path / "in.jpg")
+    _jpeg(path, _smooth(16, 16, 3, 0))
+    data = open(path, "rb").read().replace(b"\xff\xc0", b"\xff\xc2", 1)
+    open(path, "wb").write(data)
+    r = subprocess.run([CLI, path, "--dump-rgba", str(tmp_path / "o.pam")], capture_output=True, text=True)
+    assert r.returncode != 0 and "progressive" in r.stdout
+    from astc_encoder_gb300 import image_io
+    with pytest.raises(ValueError, match="progressive"):
+        image_io.load_image(path)
 
 
 def test_cli_rejects_unknown_format(native, tmp_path):
