@@ -31,6 +31,7 @@
 #include <string.h>
 
 #include <iostream>
+#include <new>
 #include <string>
 #include <vector>
 
@@ -94,7 +95,13 @@ int main(int argc, char** argv) {
 
     astc::Image img;
     std::string err;
-    if (!astc::load_image(src, img, err)) {
+    bool loaded = false;
+    try {
+        loaded = astc::load_image(src, img, err);
+    } catch (const std::bad_alloc&) {
+        err = "out of host memory";
+    }
+    if (!loaded) {
         std::cout << "load source texture failed! [" << src << "] " << err << std::endl;
         return -1;
     }

@@ -15,6 +15,13 @@
 namespace astc {
 namespace {
 
+// Images up to 2^30 texels (4 GiB of RGBA8); larger or empty headers are refused
+// before anything is allocated.
+bool dims_ok(long long w, long long h, std::string& err) {
+    if (w <= 0 || h <= 0 || w * h > (1ll << 30)) { err = "bad image size"; return false; }
+    return true;
+}
+
 struct Bits {
     const uint8_t* p;
     size_t n, pos = 0;
@@ -223,7 +230,7 @@ bool decode_png(const uint8_t* d, size_t n, Image& img, std::string& err) {
         }
         pos += 12 + (size_t)len;
     }
-    if (w == 0 || h == 0 || w > (1u << 24) || h > (1u << 24)) { err = "bad PNG size"; return false; }
+    if (!dims_ok(w, h, err)) return false;
     if (interlace != 0) { err = "interlaced PNG is not supported"; return false; }
     int chans = 0;
     switch (ctype) {
@@ -331,7 +338,8 @@ bool decode_pnm(const uint8_t* d, size_t n, Image& img, std::string& err) {
         return false;
     }
     ++pos;                                               // one whitespace byte before the data
-    if (w <= 0 || h <= 0 || depth < 1 || depth > 4 || maxv != 255) { err = "unsupported PNM header"; return false; }
+    if (depth < 1 || depth > 4 || maxv != 255) { err = "unsupported PNM header"; return false; }
+    if (!dims_ok(w, h, err)) return false;
     if (pos + (size_t)w * h * depth > n) { err = "PNM data too short"; return false; }
     img.width = w;
     img.height = h;
@@ -357,12 +365,15 @@ bool decode_tga(const uint8_t* d, size_t n, Image& img, std::string& err) {
         err = "unsupported TGA type (colour-mapped or not an image)";
         return false;
     }
-    if (w <= 0 || h <= 0 || (grey ? bpp != 8 : (bpp != 24 && bpp != 32))) {
+    if (grey ? bpp != 8 : (bpp != 24 && bpp != 32)) {
         err = "unsupported TGA pixel depth";
         return false;
     }
+    if (!dims_ok(w, h, err)) return false;
     const int px = bpp / 8;
     size_t pos = 18 + (size_t)idlen;
+    // raw data holds every byte; a run-length packet of 1 + px bytes at most 128 pixels
+    if ((size_t)w * h * px > (rle ? 128 * n : n)) { err = "TGA data too short"; return false; }
     std::vector<uint8_t> raw((size_t)w * h * px);
     if (!rle) {
         if (pos + raw.size() > n) { err = "TGA data too short"; return false; }
@@ -412,8 +423,10 @@ bool decode_bmp(const uint8_t* d, size_t n, Image& img, std::string& err) {
     if (hdr < 40) { err = "unsupported BMP header"; return false; }
     const int w = (int)u32(18), hraw = (int)u32(22), bpp = (int)u16(28), comp = (int)u32(30);
     const bool top_down = hraw < 0;
-    const int h = top_down ? -hraw : hraw;
-    if (w <= 0 || h <= 0 || (bpp != 24 && bpp != 32) || !(comp == 0 || (comp == 3 && bpp == 32))) {
+    const long long h64 = top_down ? -(long long)hraw : (long long)hraw;
+    if (!dims_ok(w, h64, err)) return false;
+    const int h = (int)h64;
+    if ((bpp != 24 && bpp != 32) || !(comp == 0 || (comp == 3 && bpp == 32))) {
         err = "unsupported BMP format (24/32-bit uncompressed or 32-bit bit fields only)";
         return false;
     }
@@ -484,13 +497,15 @@ struct JpegBits {
     uint32_t acc = 0;
     int bits = 0;
     bool marker = false;                     // hit a marker: only zero bits follow
+    int past = 0;                            // bytes supplied after the data ran out
     int fill_byte() {
-        if (marker || pos >= n) return 0;
+        if (marker || pos >= n) { ++past; return 0; }
         uint8_t b = d[pos];
         if (b == 0xFF) {
             const uint8_t nx = pos + 1 < n ? d[pos + 1] : 0;
             if (nx == 0x00) { pos += 2; return 0xFF; }
             marker = true;                   // RSTn or another marker: stop here
+            ++past;
             return 0;
         }
         ++pos;
@@ -506,7 +521,7 @@ struct JpegBits {
         for (int i = 0; i < k; ++i) v = (v << 1) | bit();
         return v;
     }
-    void reset() { bits = 0; }
+    void reset() { bits = 0; past = 0; }
 };
 
 int jpeg_decode_sym(JpegBits& b, const JpegHuff& h) {
@@ -556,7 +571,12 @@ bool decode_jpeg(const uint8_t* d, size_t n, Image& img, std::string& err) {
     if (n < 4 || d[0] != 0xFF || d[1] != 0xD8) { err = "not a JPEG file"; return false; }
     uint16_t qt[4][64] = {};
     JpegHuff hdc[4], hac[4];
-    struct Comp { int id, h, v, tq, td = 0, ta = 0; std::vector<uint8_t> plane; int pw = 0, ph = 0; int dc = 0; };
+    struct Comp {
+        int id, h, v, tq, td = 0, ta = 0;
+        std::vector<uint8_t> plane;
+        int pw = 0, ph = 0;
+        long long dc = 0;                                   // DC predictor (no overflow on corrupt data)
+    };
     std::vector<Comp> comps;
     int width = 0, height = 0, restart = 0, hmax = 1, vmax = 1;
     bool frame = false, done = false;
@@ -571,6 +591,8 @@ bool decode_jpeg(const uint8_t* d, size_t n, Image& img, std::string& err) {
         const int len = u16(pos + 2);
         const size_t seg = pos + 4, end = pos + 2 + (size_t)len;
         if (len < 2 || end > n) { err = "JPEG segment past the end"; return false; }
+        const size_t need = m == 0xC0 || m == 0xC1 ? 6 : m == 0xDD ? 2 : m == 0xDA ? 1 : 0;
+        if (seg + need > end) { err = "JPEG segment too short"; return false; }
         if (m == 0xDB) {                                          // DQT
             for (size_t o = seg; o < end;) {
                 const int pq = d[o] >> 4, tq = d[o] & 15;
@@ -597,7 +619,8 @@ bool decode_jpeg(const uint8_t* d, size_t n, Image& img, std::string& err) {
             height = u16(seg + 1);
             width = u16(seg + 3);
             const int nc = d[seg + 5];
-            if (width <= 0 || height <= 0 || (nc != 1 && nc != 3) || seg + 6 + 3 * (size_t)nc > end) {
+            if (!dims_ok(width, height, err)) return false;
+            if ((nc != 1 && nc != 3) || seg + 6 + 3 * (size_t)nc > end) {
                 err = "unsupported JPEG frame (grey or YCbCr only)";
                 return false;
             }
@@ -623,6 +646,7 @@ bool decode_jpeg(const uint8_t* d, size_t n, Image& img, std::string& err) {
             if (!frame) { err = "JPEG scan before the frame header"; return false; }
             const int ns = d[seg];
             if (ns != (int)comps.size()) { err = "non-interleaved JPEG scans are not read"; return false; }
+            if (seg + 1 + 2 * (size_t)ns > end) { err = "JPEG segment too short"; return false; }
             for (int i = 0; i < ns; ++i) {
                 const int id = d[seg + 1 + 2 * i], t = d[seg + 2 + 2 * i];
                 bool found = false;
@@ -636,6 +660,13 @@ bool decode_jpeg(const uint8_t* d, size_t n, Image& img, std::string& err) {
                     return false;
                 }
             const int mcux = (width + 8 * hmax - 1) / (8 * hmax), mcuy = (height + 8 * vmax - 1) / (8 * vmax);
+            // every block codes at least a DC and an AC symbol of one bit or more
+            int per_mcu = 0;
+            for (auto& c : comps) per_mcu += c.h * c.v;
+            if ((long long)mcux * mcuy * per_mcu > 4ll * (long long)(n - end) + 64) {
+                err = "JPEG data too short for its size";
+                return false;
+            }
             for (auto& c : comps) {
                 c.pw = mcux * c.h * 8;
                 c.ph = mcuy * c.v * 8;
@@ -665,7 +696,7 @@ bool decode_jpeg(const uint8_t* d, size_t n, Image& img, std::string& err) {
                                 const int t = jpeg_decode_sym(bits, hdc[c.td]);
                                 if (t < 0 || t > 11) { err = "corrupt JPEG data"; return false; }
                                 c.dc += jpeg_extend(bits.get(t), t);
-                                blk[0] = (float)(c.dc * (int)qt[c.tq][0]);
+                                blk[0] = (float)c.dc * (float)qt[c.tq][0];
                                 for (int k = 1; k < 64;) {
                                     const int rs = jpeg_decode_sym(bits, hac[c.ta]);
                                     if (rs < 0) { err = "corrupt JPEG data"; return false; }
@@ -678,9 +709,10 @@ bool decode_jpeg(const uint8_t* d, size_t n, Image& img, std::string& err) {
                                     k += r;
                                     if (k > 63) { err = "corrupt JPEG data"; return false; }
                                     const int z = kZigzag[k];
-                                    blk[z] = (float)(jpeg_extend(bits.get(sz), sz) * (int)qt[c.tq][z]);
+                                    blk[z] = (float)jpeg_extend(bits.get(sz), sz) * (float)qt[c.tq][z];
                                     ++k;
                                 }
+                                if (bits.past > 8) { err = "JPEG data too short"; return false; }
                                 const int ox = (mx * c.h + bx) * 8, oy = (my * c.v + by) * 8;
                                 jpeg_idct(blk, c.plane.data() + (size_t)oy * c.pw + ox, c.pw);
                             }

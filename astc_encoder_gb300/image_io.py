@@ -347,6 +347,8 @@ def _jpeg_scan(d, pos, width, height, comps, qt, huff, restart):
     vmax = max(c["v"] for c in comps)
     mcux, mcuy = -(-width // (8 * hmax)), -(-height // (8 * vmax))
     nmcu = mcux * mcuy
+    if nmcu * sum(c["h"] * c["v"] for c in comps) > 4 * (len(d) - pos) + 64:
+        raise ValueError("JPEG data too short for its size")   # >= 2 bits per block
     segs = _jpeg_segments(d, pos)
     coef = [np.zeros((mcuy * c["v"], mcux * c["h"], 64), np.float64) for c in comps]
     seg_i, data, bitpos, dc = -1, b"", 0, [0] * len(comps)
@@ -385,6 +387,8 @@ def _jpeg_scan(d, pos, width, height, comps, qt, huff, restart):
             dct, act = huff[(0, c["td"])], huff[(1, c["ta"])]
             for by in range(c["v"]):
                 for bx in range(c["h"]):
+                    if bitpos > 8 * len(data) + 64:
+                        raise ValueError("JPEG data too short")
                     blk = coef[ci][my * c["v"] + by, mx * c["h"] + bx]
                     t = sym(dct)
                     dc[ci] += extend(bits(t), t)

@@ -431,6 +431,49 @@ def test_cli_refuses_progressive_jpeg(native, tmp_path):
         image_io.load_image(path)
 
 
+@pytest.mark.parametrize("fmt", ["png", "jpg", "bmp", "tga", "pam"])
+def test_cli_survives_corrupt_images(native, tmp_path, fmt):
+    """Mutated, truncated and extended files: the reader returns an image or an
+    error, never a crash, and never spends more than the file's size on work."""
+    rng = np.random.default_rng(["png", "jpg", "bmp", "tga", "pam"].index(fmt))
+    arr = _smooth(21, 27, 3, 5)
+    rgba = np.dstack([arr, np.full(arr.shape[:2], 200, np.uint8)])
+    path = str(tmp_path / ("in." + fmt))
+    if fmt == "png":
+        _png(path, rgba, 6)
+    elif fmt == "jpg":
+        _jpeg(path, arr, sampling=(2, 2), restart=2)
+    elif fmt == "bmp":
+        _bmp(path, rgba)
+    elif fmt == "tga":
+        _tga(path, rgba, rle=True)
+    else:
+        with open(path, "wb") as fh:
+            fh.write(b"P7\nWIDTH 27\nHEIGHT 21\nDEPTH 4\nMAXVAL 255\nTUPLTYPE RGB_ALPHA\nENDHDR\n" + rgba.tobytes())
+    good = open(path, "rb").read()
+    for trial in range(60):
+        data = bytearray(good)
+        kind = trial % 4
+        if kind == 0:                                   # flip bytes anywhere
+            for i in rng.integers(0, len(data), 1 + trial % 5):
+                data[i] = int(rng.integers(0, 256))
+        elif kind == 1:                                 # flip bytes in the header
+            for i in rng.integers(0, min(len(data), 64), 1 + trial % 3):
+                data[i] = int(rng.integers(0, 256))
+        elif kind == 2:                                 # truncate
+            data = data[:int(rng.integers(1, len(data)))]
+        else:                                           # splice in garbage
+            i = int(rng.integers(0, len(data)))
+            data[i:i] = rng.integers(0, 256, int(rng.integers(1, 40)), dtype=np.uint8).tobytes()
+        bad = str(tmp_path / ("bad." + fmt))
+        with open(bad, "wb") as fh:
+            fh.write(bytes(data))
+        r = subprocess.run([CLI, bad, "--dump-rgba", str(tmp_path / "o.pam")], capture_output=True,
+                           text=True, timeout=60)
+        assert r.returncode in (0, 255), (trial, r.returncode, r.stdout[-300:], r.stderr[-300:])
+        assert r.returncode == 0 or "load source texture failed" in r.stdout
+
+
 def test_cli_rejects_unknown_format(native, tmp_path):
     path = tmp_path / "in.xyz"
     path.write_bytes(b"\x00\x01garbage")
