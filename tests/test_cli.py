@@ -474,6 +474,64 @@ def test_cli_survives_corrupt_images(native, tmp_path, fmt):
         assert r.returncode == 0 or "load source texture failed" in r.stdout
 
 
+def test_image_reader_under_sanitizers(tmp_path):
+    """The reader built with ASan + UBSan over 400 mutated files of every format."""
+    import shutil
+    if shutil.which("g++") is None:
+        pytest.skip("no g++")
+    exe = str(tmp_path / "fuzz")
+    csrc = os.path.join(ROOT, "astc_encoder_gb300", "csrc")
+    r = subprocess.run(["g++", "-std=c++17", "-O1", "-g", "-fsanitize=address,undefined",
+                        "-fno-sanitize-recover=undefined", "-I", csrc,
+                        os.path.join(ROOT, "tests", "image_fuzz_main.cpp"), os.path.join(csrc, "image_load.cpp"),
+                        "-o", exe], capture_output=True, text=True)
+    if r.returncode != 0:
+        pytest.skip("sanitizer runtime unavailable: " + r.stderr[-200:])
+    arr = _smooth(21, 27, 3, 5)
+    rgba = np.dstack([arr, np.full(arr.shape[:2], 200, np.uint8)])
+    seeds = []
+    for name, write in [("a.png", lambda p: _png(p, rgba, 6)), ("b.png", lambda p: _png(p, arr[..., 0], 3,
+                                                                                         palette=np.arange(768) % 256)),
+                        ("c.jpg", lambda p: _jpeg(p, arr, sampling=(2, 2), restart=2)),
+                        ("d.jpg", lambda p: _jpeg(p, arr[..., 0])), ("e.bmp", lambda p: _bmp(p, rgba, bitfields=True)),
+                        ("f.bmp", lambda p: _bmp(p, arr)), ("g.tga", lambda p: _tga(p, rgba, rle=True)),
+                        ("h.tga", lambda p: _tga(p, arr[..., 0], rle=True))]:
+        path = str(tmp_path / name)
+        write(path)
+        seeds.append(path)
+    pam = str(tmp_path / "i.pam")
+    with open(pam, "wb") as fh:
+        fh.write(b"P7\nWIDTH 27\nHEIGHT 21\nDEPTH 4\nMAXVAL 255\nTUPLTYPE RGB_ALPHA\nENDHDR\n" + rgba.tobytes())
+    seeds.append(pam)
+    rng = np.random.default_rng(11)
+    for batch in range(10):
+        files = []
+        for j in range(40):
+            src = seeds[int(rng.integers(len(seeds)))]
+            data = bytearray(open(src, "rb").read())
+            kind = int(rng.integers(5))
+            if kind == 0:
+                for i in rng.integers(0, len(data), 1 + int(rng.integers(8))):
+                    data[i] = int(rng.integers(256))
+            elif kind == 1:
+                for i in rng.integers(0, min(len(data), 80), 1 + int(rng.integers(4))):
+                    data[i] = int(rng.integers(256))
+            elif kind == 2:
+                data = data[:int(rng.integers(1, len(data)))]
+            elif kind == 3:
+                i = int(rng.integers(0, len(data)))
+                data[i:i] = rng.integers(0, 256, int(rng.integers(1, 60)), dtype=np.uint8).tobytes()
+            else:                                       # a stray marker / tag byte pair
+                i = int(rng.integers(0, len(data) - 4))
+                data[i:i + 2] = bytes([0xFF, int(rng.integers(256))])
+            path = str(tmp_path / ("m%d%s" % (j, os.path.splitext(src)[1])))
+            with open(path, "wb") as fh:
+                fh.write(bytes(data))
+            files.append(path)
+        r = subprocess.run([exe] + files, capture_output=True, text=True, timeout=300)
+        assert r.returncode == 0, r.stderr[-2000:]
+
+
 def test_cli_rejects_unknown_format(native, tmp_path):
     path = tmp_path / "in.xyz"
     path.write_bytes(b"\x00\x01garbage")
