@@ -178,6 +178,13 @@ constexpr SrgbBits make_srgb_bits() {
     return s;
 }
 
+// Programmatic dependent launch (launch_pdl): allow the next kernel on the
+// stream to be launched (every CTA calls this first), and wait until the
+// previous kernel has completed with its writes visible (called after the
+// constant-table set-up, before the first global load or store).
+__device__ __forceinline__ void pdl_allow_next() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void pdl_wait_prior() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 // Per-CTA copies of the constant tables (trit packing, sRGB texel values).
 template <bool SRGB>
 __device__ __forceinline__ void load_cta_tables(const TritPack& tp, const SrgbBits& sb, uint8_t* s_trits,

@@ -16,7 +16,9 @@
 // keeps the register count (and so the occupancy) of the 36-texel block in
 // check; the length tests compare against an exact threshold instead of
 // taking a square root; the ISE of the fixed weight range is unrolled into
-// 64-bit shifts and the weight bit reversal is one __brevll.
+// 64-bit shifts and the weight bit reversal is one __brevll.  Launches use
+// programmatic dependent launch (launch_pdl): in a stream of encodes the next
+// kernel's CTAs are resident and have their tables loaded when this one ends.
 //
 // Floating point follows the FP32 oracle's model operation by operation:
 // mad = fused (__fmaf_rn), dot(a,b) = a.x*b.x then fused over y, z, w,
@@ -57,8 +59,10 @@ astc_encode_blocks_fp32(const Launch p) {
     extern __shared__ float4 s_texels[];                  // kStoreShared only
     __shared__ uint8_t s_trits[256];
     __shared__ float s_lut[SRGB ? 256 : 1];
+    pdl_allow_next();
     load_cta_tables<SRGB>(c_trit_pack, c_srgb_bits, s_trits, s_lut);
     __syncthreads();
+    pdl_wait_prior();
     const long long b = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= p.nblocks) return;
     const int by = (int)(b / p.tex.nbx);
@@ -107,8 +111,7 @@ cudaError_t launch_t(const Launch& p, int threads, cudaStream_t s) {
         if (e != cudaSuccess) return e;
     }
     const long long grid = (p.nblocks + threads - 1) / threads;
-    kern<<<(unsigned)grid, threads, smem, s>>>(p);
-    return cudaGetLastError();
+    return launch_pdl(kern, (unsigned)grid, (unsigned)threads, smem, s, p);
 }
 
 template <int DIM, bool ALPHA, bool NORMAL, bool SRGB>

@@ -94,8 +94,10 @@ __global__ void __launch_bounds__(128, 3) astc_encode_blocks_best(const BestLaun
     constexpr int N = DIM * DIM;
     __shared__ uint8_t s_trits[256];
     __shared__ float s_lut[SRGB ? 256 : 1];
+    pdl_allow_next();
     load_cta_tables<SRGB>(c_trit_pack_best, c_srgb_bits_best, s_trits, s_lut);
     __syncthreads();
+    pdl_wait_prior();
     const long long b = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= p.nblocks) return;
     const int by = (int)(b / p.tex.nbx);
@@ -127,8 +129,7 @@ __global__ void __launch_bounds__(128, 3) astc_encode_blocks_best(const BestLaun
 template <int DIM, bool ALPHA, bool NORMAL, bool SRGB>
 cudaError_t launch_t(const BestLaunch& p, cudaStream_t s) {
     const long long grid = (p.nblocks + 127) / 128;
-    astc_encode_blocks_best<DIM, ALPHA, NORMAL, SRGB><<<(unsigned)grid, 128, 0, s>>>(p);
-    return cudaGetLastError();
+    return launch_pdl(astc_encode_blocks_best<DIM, ALPHA, NORMAL, SRGB>, (unsigned)grid, 128u, 0, s, p);
 }
 
 template <int DIM, bool ALPHA, bool NORMAL>

@@ -21,6 +21,31 @@ struct EncodeJob {
     uint8_t* out;         // 16 * nblocks bytes, 16-byte aligned
 };
 
+// Launch with programmatic dependent launch (PDL): the kernel may be started
+// while the previous kernel on the stream is still finishing, once every CTA
+// of that kernel has started and allowed it (pdl_allow_next); it loads its
+// constant tables and then waits in pdl_wait_prior until the previous kernel
+// has completed and its writes are visible, before it reads or writes any
+// global memory.  Stream order is unchanged for every caller; what overlaps is
+// the launch gap and the table set-up (a kernel that does not allow it, or a
+// copy, delays the launch to its completion as usual).  On GB300 this took a
+// 2048x2048 6x6 launch from 23.9 to 20.2 us in a stream of encodes.
+template <class... P, class... A>
+cudaError_t launch_pdl(void (*kern)(P...), unsigned grid, unsigned threads, size_t smem, cudaStream_t s,
+                       A&&... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(threads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kern, static_cast<A&&>(args)...);
+}
+
 inline int blocks_x(int w, int dim) { return (w + dim - 1) / dim; }
 inline int blocks_y(int h, int dim) { return (h + dim - 1) / dim; }
 

@@ -67,6 +67,9 @@ def _parse():
                     help="precision of the main workload")
     ap.add_argument("--profile-batched", action="store_true",
                     help="small case for ncu: one FP32 and one HALF2 batched graph launch")
+    ap.add_argument("--wave-sweep", action="store_true",
+                    help="fixed-mode launch time against the number of full waves (6x6 RGBA sRGB); "
+                         "prints one JSON line per texture size and exits")
     ap.add_argument("--profile-case", action="store_true",
                     help="small case for ncu: 2 textures per step, encode launches only")
     ap.add_argument("--profile-quality", default="fast",
@@ -275,6 +278,28 @@ def _time_launches(torch, native, texs, outs, spec, steps):
     launches = native.kernel_launch_count() - l0
     per_step = [a.elapsed_time(b) for a, b in ev]
     return sum(per_step) / max(1, launches), per_step, launches
+
+
+def _wave_sweep(torch, native, synth, warmup: int, steps: int) -> None:
+    """Mean launch time of the fixed-mode 6x6 RGBA sRGB kernel for textures of
+    0.5 to 4 full waves (12 resident warps per SM: 152 x 384 blocks per wave)
+    and the 2048x2048 texture (2.004 waves): separates the per-launch cost
+    (ramp-up and drain) from the cost of a further full wave."""
+    spec = dict(block_dim=6, has_alpha=True, is_normal=False, srgb=True, border=1)
+    per_wave = torch.cuda.get_device_properties(0).multi_processor_count * 384
+    src = synth.rgba_cutout(3648, 2304)
+    for h, w in [(456, 2304), (912, 2304), (1368, 2304), (1824, 2304), (1830, 2304), (2048, 2048),
+                 (2736, 2304), (3648, 2304)]:
+        img = np.ascontiguousarray(src[:h, :w]) if (h, w) != (2048, 2048) else synth.rgba_cutout(2048, 2048)
+        texs = _texture_batch(torch, img, TEXTURES_PER_STEP, salt=0)
+        nb = ((w + 5) // 6) * ((h + 5) // 6)
+        outs = [torch.empty((nb, 16), dtype=torch.uint8, device="cuda") for _ in texs]
+        _time_launches(torch, native, texs, outs, spec, warmup)
+        per, _, _ = _time_launches(torch, native, texs, outs, spec, steps)
+        print(json.dumps({"wave_sweep": f"{w}x{h}", "blocks": nb, "waves": round(nb / per_wave, 3),
+                          "mean_launch_us": round(per * 1e3, 2),
+                          "Mtexels_s": round(w * h / (per * 1e3), 1)}), flush=True)
+        del texs, outs
 
 
 # DRAM bytes (read + write) of one launch of the production kernel, from the
@@ -549,6 +574,10 @@ def run_ours(args) -> None:
                 b.encode(items, precision=prec, stream=work_stream.cuda_stream)
             torch.cuda.synchronize()
         print(json.dumps({"profile_batched": len(items), "blocks": n_blocks}), flush=True)
+        return
+
+    if args.wave_sweep:
+        _wave_sweep(torch, native, synth, max(3, args.warmup), max(5, min(args.steps, 20)))
         return
 
     img, spec = synth.workload(args.workload)
