@@ -3,7 +3,8 @@
 Every CUDA translation unit is compiled for sm_103a only
 (``-gencode arch=compute_103a,code=sm_103a``) in parallel, then linked into
 ``astc_encoder_gb300/_lib/libastc_gb300.so`` (static CUDA runtime) and the
-drop-in command line tool ``astc_encoder_gb300/_lib/astc_cs_enc``.  Objects go
+drop-in command line tool ``astc_encoder_gb300/_lib/astc_cs_enc`` (plus the
+benchmark's FP32 throughput probe ``libastc_fp32_peak.so``).  Objects go
 to ``astc_encoder_gb300/_build/``.  Nothing is installed outside the tree.
 
 Usage: ``python -m astc_encoder_gb300.build [--force] [--verbose]``
@@ -23,6 +24,7 @@ BUILD = os.path.join(PKG, "_build")
 LIBDIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(LIBDIR, "libastc_gb300.so")
 CLI = os.path.join(LIBDIR, "astc_cs_enc")
+PEAK_LIB = os.path.join(LIBDIR, "libastc_fp32_peak.so")      # FP32 FMA throughput, for the benchmark
 INCLUDE = os.path.join(os.path.dirname(PKG), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -101,7 +103,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
     os.makedirs(LIBDIR, exist_ok=True)
     jobs = [(s, f) for s, f in LIB_SOURCES] + [(s, f) for s, f in CLI_SOURCES
-                                               if os.path.exists(os.path.join(CSRC, s))]
+                                               if os.path.exists(os.path.join(CSRC, s))] + [("fp32_peak.cu", [])]
     with cf.ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 4)) as ex:
         futs = {s: ex.submit(_compile, s, f, force, verbose) for s, f in jobs}
         objs = {s: fu.result() for s, fu in futs.items()}
@@ -112,6 +114,9 @@ def build(force: bool = False, verbose: bool = False) -> str:
     if len(cli_objs) == len(CLI_SOURCES) and (force or _stale(CLI, cli_objs + [LIB])):
         _run([nvcc(), *ARCH, "-o", CLI, *cli_objs, "-L", LIBDIR, "-lastc_gb300",
               "-Xlinker", "-rpath,$ORIGIN"], verbose)
+    peak_obj = objs["fp32_peak.cu"]
+    if force or _stale(PEAK_LIB, [peak_obj]):
+        _run([nvcc(), *ARCH, "-shared", "-Xcompiler", "-fPIC", "-o", PEAK_LIB, peak_obj], verbose)
     return LIB
 
 

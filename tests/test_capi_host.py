@@ -35,6 +35,15 @@ def test_library_exports_every_declared_symbol(native):
     assert not missing, missing
 
 
+def test_fp32_peak_probe_is_built_apart(native):
+    """The benchmark's FP32 FMA probe is its own library, not part of the encoder's."""
+    import ctypes
+    from astc_encoder_gb300 import build
+    peak = ctypes.CDLL(build.PEAK_LIB)
+    assert hasattr(peak, "astc_fp32_fma_peak")
+    assert not hasattr(native.load_library(), "astc_fp32_fma_peak")
+
+
 def test_library_links_no_oracle(native):
     # the product library must not carry the oracle's code
     data = open(native.library_path(), "rb").read()

@@ -210,6 +210,22 @@ def test_sse_matches_numpy(native):
     assert native.sse(a, b).tolist() == want.tolist()
 
 
+def test_fp32_peak_probe_is_plausible(native):
+    """The FMA probe used as the FP32 roofline denominator: between half and 1.1x
+    of SMs x 128 lanes x 2 FLOPs x the SM clock."""
+    import ctypes
+    import torch
+    from astc_encoder_gb300 import build
+    lib = ctypes.CDLL(build.PEAK_LIB)
+    lib.astc_fp32_fma_peak.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
+    out = ctypes.c_double(0.0)
+    assert lib.astc_fp32_fma_peak(3, ctypes.byref(out)) == 0
+    props = torch.cuda.get_device_properties(0)
+    clock_ghz = getattr(props, "clock_rate", 0) / 1e6 or 2.07           # kHz when torch reports it
+    nominal = props.multi_processor_count * 128 * 2 * clock_ghz / 1e3
+    assert 0.5 * nominal < out.value < 1.1 * nominal, (out.value, nominal)
+
+
 def test_launch_counter_moves(native):
     before = native.kernel_launch_count()
     native.encode(np.zeros((8, 8, 4), np.uint8))
