@@ -212,11 +212,14 @@ __global__ void __launch_bounds__(kSearchThreads, 3) astc_encode_blocks_search(c
     __shared__ typename std::conditional<(MODE >= 2), PartSmem, char>::type pm;
     __shared__ typename std::conditional<(MODE >= 1), DualSmem, char>::type ds;
     __shared__ typename std::conditional<MODE == 3, Part3Smem, char>::type p3;
+    pdl_allow_next();
+    // the tables are read-only device constants: loaded before the wait
     load_search_smem<ALPHA, SRGB>(sm);
     if constexpr (MODE >= 1) load_dual_smem<ALPHA>(ds);
     if constexpr (MODE >= 2) load_partition_smem<ALPHA>(pm, DIM);
     if constexpr (MODE == 3) load_part3_smem(p3);
     __syncthreads();
+    pdl_wait_prior();
     const long long b = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= p.nblocks) return;
     const int by = (int)(b / p.tex.nbx);
@@ -332,8 +335,7 @@ cudaError_t launch_t(const SearchLaunch& p, cudaStream_t s) {
         const cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
     }
-    kernel<<<(unsigned)grid, kSearchThreads, smem, s>>>(p);
-    return cudaGetLastError();
+    return launch_pdl(kernel, (unsigned)grid, (unsigned)kSearchThreads, smem, s, p);
 }
 
 template <int MODE, int DIM, bool ALPHA, bool NORMAL>

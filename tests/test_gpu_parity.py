@@ -138,9 +138,9 @@ def test_device_pointer_api_and_pitch(native, oracle):
     assert np.array_equal(out.cpu().numpy(), want)
 
 
-@pytest.mark.parametrize("precision,axis", [(0, 0), (1, 0), (0, 2)])
-def test_back_to_back_launches_keep_stream_order(native, precision, axis):
-    """The plain FP32, HALF2 and best-fit kernels are launched with programmatic
+@pytest.mark.parametrize("precision,axis,quality", [(0, 0, 0), (1, 0, 0), (0, 2, 0), (0, 0, 1), (0, 0, 3)])
+def test_back_to_back_launches_keep_stream_order(native, precision, axis, quality):
+    """The plain FP32, HALF2, best-fit and quality kernels are launched with programmatic
     dependent launch: each may start while the previous kernel on the stream
     finishes.  Stream order must still hold: a producer kernel right before an
     encode (read after write), an overwrite of the input right after it (write
@@ -148,7 +148,7 @@ def test_back_to_back_launches_keep_stream_order(native, precision, axis):
     an encode whose input is the previous encode's output."""
     import torch
     h = w = 384                                    # 64 x 64 blocks of 6x6 = 65,536 bytes = 128 x 128 texels
-    opts = dict(block_dim=6, has_alpha=True, srgb=True, precision=precision, axis=axis)
+    opts = dict(block_dim=6, has_alpha=True, srgb=True, precision=precision, axis=axis, quality=quality)
     imgs = [_texture(h, w, seed=40 + i) for i in range(3)]
     want = [native.encode(im, **opts) for im in imgs]
     nb = want[0].shape[0]
@@ -166,13 +166,13 @@ def test_back_to_back_launches_keep_stream_order(native, precision, axis):
                                  **opts)
         # the last blocks, read as a 128 x 128 RGBA image by the next encode
         native.encode_device(same.data_ptr(), 128, 128, chained.data_ptr(), stream=s.cuda_stream,
-                             block_dim=4, has_alpha=True, precision=precision)
+                             block_dim=4, has_alpha=True, precision=precision, quality=quality)
     s.synchronize()
     for i in range(12):
         assert np.array_equal(outs[i].cpu().numpy(), want[i % 3]), i
     assert np.array_equal(same.cpu().numpy(), want[0])
     again = native.encode(np.ascontiguousarray(want[0].reshape(128, 128, 4)), block_dim=4, has_alpha=True,
-                          precision=precision)
+                          precision=precision, quality=quality)
     assert np.array_equal(chained.cpu().numpy(), again)
 
 
