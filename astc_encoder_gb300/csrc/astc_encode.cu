@@ -59,10 +59,10 @@ astc_encode_blocks_fp32(const Launch p) {
     extern __shared__ float4 s_texels[];                  // kStoreShared only
     __shared__ uint8_t s_trits[256];
     __shared__ float s_lut[SRGB ? 256 : 1];
-    pdl_allow_next();
     load_cta_tables<SRGB>(c_trit_pack, c_srgb_bits, s_trits, s_lut);
     __syncthreads();
     pdl_wait_prior();
+    pdl_allow_next();
     const long long b = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= p.nblocks) return;
     const int by = (int)(b / p.tex.nbx);

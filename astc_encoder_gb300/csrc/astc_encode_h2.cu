@@ -27,10 +27,10 @@ __global__ void __launch_bounds__(kH2Threads) astc_encode_blocks_h2(const Launch
     constexpr int N = DIM * DIM;
     __shared__ uint8_t s_trits[256];
     __shared__ float s_lut[SRGB ? 256 : 1];
-    pdl_allow_next();
     load_cta_tables<SRGB>(c_trit_pack_h2, c_srgb_bits_h2, s_trits, s_lut);
     __syncthreads();
     pdl_wait_prior();
+    pdl_allow_next();
     const long long b = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= p.nblocks) return;
     const int by = (int)(b / p.tex.nbx);

@@ -23,10 +23,10 @@ struct EncodeJob {
 
 // Launch with programmatic dependent launch (PDL): the kernel may be started
 // while the previous kernel on the stream is still finishing, once every CTA
-// of that kernel has started and allowed it (pdl_allow_next); it loads its
-// constant tables and then waits in pdl_wait_prior until the previous kernel
-// has completed and its writes are visible, before it reads or writes any
-// global memory.  Stream order is unchanged for every caller; what overlaps is
+// of that kernel has passed its own wait and allowed it (pdl_allow_next); it
+// loads its constant tables and then waits in pdl_wait_prior until the
+// previous kernel has completed and its writes are visible, before it reads
+// or writes any global memory.  Stream order is unchanged for every caller; what overlaps is
 // the launch gap and the table set-up (a kernel that does not allow it, or a
 // copy, delays the launch to its completion as usual).  On GB300 this took a
 // 2048x2048 6x6 launch from 23.9 to 20.2 us in a stream of encodes.

@@ -212,7 +212,6 @@ __global__ void __launch_bounds__(kSearchThreads, 3) astc_encode_blocks_search(c
     __shared__ typename std::conditional<(MODE >= 2), PartSmem, char>::type pm;
     __shared__ typename std::conditional<(MODE >= 1), DualSmem, char>::type ds;
     __shared__ typename std::conditional<MODE == 3, Part3Smem, char>::type p3;
-    pdl_allow_next();
     // the tables are read-only device constants: loaded before the wait
     load_search_smem<ALPHA, SRGB>(sm);
     if constexpr (MODE >= 1) load_dual_smem<ALPHA>(ds);
@@ -220,6 +219,7 @@ __global__ void __launch_bounds__(kSearchThreads, 3) astc_encode_blocks_search(c
     if constexpr (MODE == 3) load_part3_smem(p3);
     __syncthreads();
     pdl_wait_prior();
+    pdl_allow_next();
     const long long b = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= p.nblocks) return;
     const int by = (int)(b / p.tex.nbx);
