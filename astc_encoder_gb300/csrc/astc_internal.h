@@ -26,10 +26,12 @@ struct EncodeJob {
 // of that kernel has passed its own wait and allowed it (pdl_allow_next); it
 // loads its constant tables and then waits in pdl_wait_prior until the
 // previous kernel has completed and its writes are visible, before it reads
-// or writes any global memory.  Stream order is unchanged for every caller; what overlaps is
-// the launch gap and the table set-up (a kernel that does not allow it, or a
-// copy, delays the launch to its completion as usual).  On GB300 this took a
-// 2048x2048 6x6 launch from 23.9 to 20.2 us in a stream of encodes.
+// or writes any global memory.  Stream order is unchanged for every caller;
+// what overlaps is the launch gap and the table set-up (a kernel that does not
+// allow it, or a copy, delays the launch to its completion as usual).  On
+// GB300 this took a 2048x2048 6x6 launch from 23.9 to 20.0 us in a stream of
+// encodes.  While the stream is being captured into a graph the launch is a
+// plain one (the waits then return at once).
 template <class... P, class... A>
 cudaError_t launch_pdl(void (*kern)(P...), unsigned grid, unsigned threads, size_t smem, cudaStream_t s,
                        A&&... args) {
@@ -41,8 +43,11 @@ cudaError_t launch_pdl(void (*kern)(P...), unsigned grid, unsigned threads, size
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
     attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
+    const cudaError_t e = cudaStreamIsCapturing(s, &capture);
+    if (e != cudaSuccess) return e;
     cfg.attrs = attr;
-    cfg.numAttrs = 1;
+    cfg.numAttrs = capture == cudaStreamCaptureStatusNone ? 1 : 0;
     return cudaLaunchKernelEx(&cfg, kern, static_cast<A&&>(args)...);
 }
 

@@ -176,6 +176,31 @@ def test_back_to_back_launches_keep_stream_order(native, precision, axis, qualit
     assert np.array_equal(chained.cpu().numpy(), again)
 
 
+@pytest.mark.parametrize("quality", [0, 1])
+def test_encode_captured_in_a_cuda_graph(native, quality):
+    """A device-memory encode captured into a CUDA graph (as an engine's frame
+    graph would) replays with whatever the input buffer holds at replay time."""
+    import torch
+    h = w = 192
+    opts = dict(block_dim=4, has_alpha=True, quality=quality)
+    imgs = [_texture(h, w, seed=60 + i) for i in range(3)]
+    want = [native.encode(im, **opts) for im in imgs]
+    tex = torch.from_numpy(imgs[0]).cuda()
+    out = torch.empty((want[0].shape[0], 16), dtype=torch.uint8, device="cuda")
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):                       # warm the library's state outside the capture
+        native.encode_device(tex.data_ptr(), w, h, out.data_ptr(), stream=s.cuda_stream, **opts)
+    s.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s):
+        native.encode_device(tex.data_ptr(), w, h, out.data_ptr(), stream=s.cuda_stream, **opts)
+    for i in (1, 2, 0):
+        tex.copy_(torch.from_numpy(imgs[i]))
+        g.replay()
+        torch.cuda.synchronize()
+        assert np.array_equal(out.cpu().numpy(), want[i]), i
+
+
 def test_device_api_rejects_host_pointers(native):
     img = np.zeros((8, 8, 4), np.uint8)
     out = np.zeros((4, 16), np.uint8)
