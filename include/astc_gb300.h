@@ -74,7 +74,7 @@ typedef enum astc_axis {
                                     bytes (the PCA on ties) is kept, or with
                                     ASTC_QUALITY_SEARCH searched from.  Most
                                     of THOROUGH's gain on alpha cut-outs at
-                                    4-5 times THOROUGH's speed (40-45% of
+                                    4-6 times THOROUGH's speed (40-55% of
                                     the fixed mode's); FP32 only (THOROUGH
                                     and above use both fits whatever the
                                     axis)                                   */
