@@ -103,12 +103,12 @@ astc_encode_persistent(const BatchJob* __restrict__ jobs, const WorkItem* __rest
                 SharedTexels<N> st{s_texels + threadIdx.x, kBatchThreads};
 #pragma unroll
                 for (int k = 0; k < N; ++k) st.put(k, decode_texel<SRGB, NORMAL>(px[k], s_lut));
-                r = encode_block_fp32<DIM, ALPHA>(st, s_trits);
+                r = encode_block_fp32<DIM, ALPHA, NORMAL>(st, s_trits);
             } else {
                 RegTexels<N> st;
 #pragma unroll
                 for (int k = 0; k < N; ++k) st.put(k, decode_texel<SRGB, NORMAL>(px[k], s_lut));
-                r = encode_block_fp32<DIM, ALPHA>(st, s_trits);
+                r = encode_block_fp32<DIM, ALPHA, NORMAL>(st, s_trits);
             }
             j.out[b] = r;
         }

@@ -73,12 +73,12 @@ astc_encode_blocks_fp32(const Launch p) {
         SharedTexels<N> st{s_texels + threadIdx.x, (int)blockDim.x};
 #pragma unroll
         for (int k = 0; k < N; ++k) st.put(k, decode_texel<SRGB, NORMAL>(px[k], s_lut));
-        p.out[b] = encode_block_fp32<DIM, ALPHA>(st, s_trits);
+        p.out[b] = encode_block_fp32<DIM, ALPHA, NORMAL>(st, s_trits);
     } else {
         RegTexels<N> st;
 #pragma unroll
         for (int k = 0; k < N; ++k) st.put(k, decode_texel<SRGB, NORMAL>(px[k], s_lut));
-        p.out[b] = encode_block_fp32<DIM, ALPHA>(st, s_trits);
+        p.out[b] = encode_block_fp32<DIM, ALPHA, NORMAL>(st, s_trits);
     }
 }
 

@@ -9,9 +9,35 @@
 
 namespace astc {
 
+// ZW forms (normal maps): the blue and alpha of every texel are the constant
+// 255 (ASTC_Encode.hlsl:575-578), so their deviations from the mean are +0
+// and every product with them is a zero.  The ZW forms leave those terms out;
+// a result then differs from the full form's at most in the sign of a zero,
+// which no comparison, clamp or rounding downstream distinguishes (blocks stay
+// bit-identical to the oracle, which computes every term).
+
+// the mean of N texels whose channel is 255, computed as block_mean does
+template <int N>
+constexpr float mean_of_255() {
+    float s = 0.0f;
+    for (int k = 0; k < N; ++k) s = s + 255.0f;
+    return s * (1.0f / (float)N);
+}
+static_assert(mean_of_255<16>() == 255.0f && mean_of_255<36>() == 255.0f, "constant channel mean");
+
 // mean (ASTC_Encode.hlsl:143-147, 172-178): sum, then x fl(1/N)
-template <int N, class S>
+template <int N, bool ZW = false, class S>
 __device__ __forceinline__ float4 block_mean(const S& st) {
+    if constexpr (ZW) {
+        float m0 = 0.f, m1 = 0.f;
+#pragma unroll
+        for (int k = 0; k < N; ++k) {
+            const float4 t = st.get(k);
+            m0 = __fadd_rn(m0, t.x); m1 = __fadd_rn(m1, t.y);
+        }
+        constexpr float kInvN = 1.0f / (float)N;
+        return make_float4(__fmul_rn(m0, kInvN), __fmul_rn(m1, kInvN), 255.0f, 255.0f);
+    }
     float m0 = 0.f, m1 = 0.f, m2 = 0.f, m3 = 0.f;
 #pragma unroll
     for (int k = 0; k < N; ++k) {
@@ -47,13 +73,42 @@ __device__ __forceinline__ float4 power_iteration(float c00, float c01, float c0
     return make_float4(v0, v1, v2, v3);
 }
 
+// power_iteration for a matrix whose rows and columns 2 and 3 are zero (ZW)
+__device__ __forceinline__ float4 power_iteration_zw(float c00, float c01, float c11) {
+    float v0 = 0.26726f, v1 = 0.80178f;
+#pragma unroll 1
+    for (int it = 0; it < 8; ++it) {
+        float t0 = __fmaf_rn(c01, v1, __fmul_rn(c00, v0));
+        float t1 = __fmaf_rn(c11, v1, __fmul_rn(c01, v0));
+        v0 = t0; v1 = t1;
+        if (shorter_than_small_value(__fmaf_rn(v1, v1, __fmul_rn(v0, v0)))) break;
+        t0 = __fmaf_rn(c01, v1, __fmul_rn(c00, v0));
+        t1 = __fmaf_rn(c11, v1, __fmul_rn(c01, v0));
+        const float r = rnorm_from_dot(__fmaf_rn(t1, t1, __fmul_rn(t0, t0)));
+        v0 = __fmul_rn(t0, r); v1 = __fmul_rn(t1, r);
+    }
+    return make_float4(v0, v1, 0.0f, 0.0f);
+}
+
 // covariance (149-162): symmetric, 10 unique terms, x fl(1/(N-1))
 struct Covariance {
     float c00, c01, c02, c03, c11, c12, c13, c22, c23, c33;
 };
 
-template <int N, class S>
+template <int N, bool ZW = false, class S>
 __device__ __forceinline__ Covariance block_covariance(const S& st, const float4 m) {
+    constexpr float kInvN1 = 1.0f / (float)(N - 1);
+    if constexpr (ZW) {
+        float c00 = 0.f, c01 = 0.f, c11 = 0.f;
+#pragma unroll
+        for (int k = 0; k < N; ++k) {
+            const float4 t = st.get(k);
+            const float d0 = __fsub_rn(t.x, m.x), d1 = __fsub_rn(t.y, m.y);
+            c00 = __fmaf_rn(d0, d0, c00); c01 = __fmaf_rn(d0, d1, c01); c11 = __fmaf_rn(d1, d1, c11);
+        }
+        return Covariance{__fmul_rn(c00, kInvN1), __fmul_rn(c01, kInvN1), 0.f, 0.f, __fmul_rn(c11, kInvN1),
+                          0.f, 0.f, 0.f, 0.f, 0.f};
+    }
     float c00 = 0.f, c01 = 0.f, c02 = 0.f, c03 = 0.f, c11 = 0.f, c12 = 0.f, c13 = 0.f,
           c22 = 0.f, c23 = 0.f, c33 = 0.f;
 #pragma unroll
@@ -67,7 +122,6 @@ __device__ __forceinline__ Covariance block_covariance(const S& st, const float4
         c13 = __fmaf_rn(d1, d3, c13); c22 = __fmaf_rn(d2, d2, c22);
         c23 = __fmaf_rn(d2, d3, c23); c33 = __fmaf_rn(d3, d3, c33);
     }
-    constexpr float kInvN1 = 1.0f / (float)(N - 1);
     return Covariance{__fmul_rn(c00, kInvN1), __fmul_rn(c01, kInvN1), __fmul_rn(c02, kInvN1),
                       __fmul_rn(c03, kInvN1), __fmul_rn(c11, kInvN1), __fmul_rn(c12, kInvN1),
                       __fmul_rn(c13, kInvN1), __fmul_rn(c22, kInvN1), __fmul_rn(c23, kInvN1),
@@ -76,9 +130,10 @@ __device__ __forceinline__ Covariance block_covariance(const S& st, const float4
 
 // principal axis: the covariance, then the power iteration (eigen_vector
 // 93-106): v = M v; stop if |v| < 1e-5; v = normalize(M v)
-template <int N, class S>
+template <int N, bool ZW = false, class S>
 __device__ __forceinline__ float4 pca_axis(const S& st, const float4 m) {
-    const Covariance c = block_covariance<N>(st, m);
+    const Covariance c = block_covariance<N, ZW>(st, m);
+    if constexpr (ZW) return power_iteration_zw(c.c00, c.c01, c.c11);
     return power_iteration(c.c00, c.c01, c.c02, c.c03, c.c11, c.c12, c.c13, c.c22, c.c23, c.c33);
 }
 
@@ -123,7 +178,7 @@ __device__ __forceinline__ float4 max_accumulation_axis(const S& st, const float
 // find_min_max (108-137): extreme projections on the axis, clamped
 // endpoints, the darker (rounded RGB sum) first; !ALPHA forces alpha 255.
 // e0/e1 are the float endpoints, q0/q1 their rounded (QUANT_256) values.
-template <int N, bool ALPHA, class S>
+template <int N, bool ALPHA, bool ZW = false, class S>
 __device__ __forceinline__ void find_min_max(const S& st, const float4 m, const float4 v, float e0[4],
                                              float e1[4], uint32_t q0[4], uint32_t q1[4], uint64_t sel = ~0ull) {
     float a = 1e31f, b = -1e31f;
@@ -131,8 +186,9 @@ __device__ __forceinline__ void find_min_max(const S& st, const float4 m, const 
     for (int k = 0; k < N; ++k) {
         if (!((sel >> k) & 1)) continue;                       // texels outside `sel` take no part
         const float4 t = st.get(k);
-        const float p = dot4(__fsub_rn(t.x, m.x), __fsub_rn(t.y, m.y), __fsub_rn(t.z, m.z),
-                             __fsub_rn(t.w, m.w), v.x, v.y, v.z, v.w);
+        const float p = ZW ? __fmaf_rn(__fsub_rn(t.y, m.y), v.y, __fmul_rn(__fsub_rn(t.x, m.x), v.x))
+                           : dot4(__fsub_rn(t.x, m.x), __fsub_rn(t.y, m.y), __fsub_rn(t.z, m.z),
+                                  __fsub_rn(t.w, m.w), v.x, v.y, v.z, v.w);
         a = fminf(a, p);
         b = fmaxf(b, p);
     }
@@ -156,7 +212,7 @@ __device__ __forceinline__ void find_min_max(const S& st, const float4 m, const 
 
 // the colour at weight-grid point g: the texel (4x4) or sample_texel's 2x2
 // bilinear tap sum (307-314, 6x6)
-template <int DIM, class S>
+template <int DIM, bool ZW = false, class S>
 __device__ __forceinline__ float4 grid_sample(const S& st, int g) {
     if constexpr (DIM == 6) {
         const int i0 = grid_tap0(g);
@@ -166,6 +222,11 @@ __device__ __forceinline__ float4 grid_sample(const S& st, int g) {
         float4 s;
         s.x = __fmaf_rn(t11.x, w11, __fmaf_rn(t10.x, w10, __fmaf_rn(t01.x, w01, __fmul_rn(t00.x, w00))));
         s.y = __fmaf_rn(t11.y, w11, __fmaf_rn(t10.y, w10, __fmaf_rn(t01.y, w01, __fmul_rn(t00.y, w00))));
+        if constexpr (ZW) {                 // blue and alpha are multiplied by k2 = k3 = +0
+            s.z = 0.0f;
+            s.w = 0.0f;
+            return s;
+        }
         s.z = __fmaf_rn(t11.z, w11, __fmaf_rn(t10.z, w10, __fmaf_rn(t01.z, w01, __fmul_rn(t00.z, w00))));
         s.w = __fmaf_rn(t11.w, w11, __fmaf_rn(t10.w, w10, __fmaf_rn(t01.w, w01, __fmul_rn(t00.w, w00))));
         return s;
@@ -177,13 +238,14 @@ __device__ __forceinline__ float4 grid_sample(const S& st, int g) {
 // weights on the 4x4 grid (calculate_normal_weights 316-372): projections on
 // normalize(e1 - e0) rescaled to [min, max], quantised (256-260, 374-393)
 // to 0..R, R = 5 (QUANT_6, alpha) or 11 (QUANT_12)
-template <int DIM, bool ALPHA, class S>
+template <int DIM, bool ALPHA, bool ZW = false, class S>
 __device__ __forceinline__ void reference_weights(const S& st, const float e0[4], const float e1[4],
                                                   uint32_t qw[16]) {
     constexpr uint32_t R = ALPHA ? 5u : 11u;
     float k0 = __fsub_rn(e1[0], e0[0]), k1 = __fsub_rn(e1[1], e0[1]);
     float k2 = __fsub_rn(e1[2], e0[2]), k3 = __fsub_rn(e1[3], e0[3]);
-    const float kk = dot4(k0, k1, k2, k3, k0, k1, k2, k3);
+    // ZW: both endpoints' blue and alpha are 255, so k2 = k3 = +0
+    const float kk = ZW ? __fmaf_rn(k1, k1, __fmul_rn(k0, k0)) : dot4(k0, k1, k2, k3, k0, k1, k2, k3);
     if (shorter_than_small_value(kk)) {
 #pragma unroll
         for (int i = 0; i < 16; ++i) qw[i] = 0u;
@@ -195,9 +257,10 @@ __device__ __forceinline__ void reference_weights(const S& st, const float e0[4]
     float minw = 1e31f, maxw = -1e31f;
 #pragma unroll
     for (int i = 0; i < 16; ++i) {
-        const float4 s = grid_sample<DIM>(st, i);
-        const float x = dot4(k0, k1, k2, k3, __fsub_rn(s.x, e0[0]), __fsub_rn(s.y, e0[1]),
-                             __fsub_rn(s.z, e0[2]), __fsub_rn(s.w, e0[3]));
+        const float4 s = grid_sample<DIM, ZW>(st, i);
+        const float x = ZW ? __fmaf_rn(k1, __fsub_rn(s.y, e0[1]), __fmul_rn(k0, __fsub_rn(s.x, e0[0])))
+                           : dot4(k0, k1, k2, k3, __fsub_rn(s.x, e0[0]), __fsub_rn(s.y, e0[1]),
+                                  __fsub_rn(s.z, e0[2]), __fsub_rn(s.w, e0[3]));
         minw = fminf(x, minw);
         maxw = fmaxf(x, maxw);
         w[i] = x;
@@ -212,16 +275,17 @@ __device__ __forceinline__ void reference_weights(const S& st, const float e0[4]
 }
 
 // per-block pipeline (encode_block 510-550) over a texel store S
-template <int DIM, bool ALPHA, class S>
+// (NORMAL: the ZW forms)
+template <int DIM, bool ALPHA, bool NORMAL = false, class S>
 __device__ __forceinline__ uint4 encode_block_fp32(const S& st, const uint8_t* trits) {
     constexpr int N = DIM * DIM;
-    const float4 m = block_mean<N>(st);
-    const float4 v = pca_axis<N>(st, m);
+    const float4 m = block_mean<N, NORMAL>(st);
+    const float4 v = pca_axis<N, NORMAL>(st, m);
     float e0[4], e1[4];
     uint32_t q0[4], q1[4];
-    find_min_max<N, ALPHA>(st, m, v, e0, e1, q0, q1);
+    find_min_max<N, ALPHA, NORMAL>(st, m, v, e0, e1, q0, q1);
     uint32_t qw[16];
-    reference_weights<DIM, ALPHA>(st, e0, e1, qw);
+    reference_weights<DIM, ALPHA, NORMAL>(st, e0, e1, qw);
     return assemble_block<ALPHA>(q0, q1, qw, trits);
 }
 

@@ -138,6 +138,38 @@ def test_device_pointer_api_and_pitch(native, oracle):
     assert np.array_equal(out.cpu().numpy(), want)
 
 
+@pytest.mark.parametrize("dim", [4, 6])
+@pytest.mark.parametrize("alpha", [False, True])
+def test_normal_map_zero_terms(native, oracle, dim, alpha):
+    """Normal maps skip every term of the constant blue and alpha channels.
+    Blocks built to make the skipped terms matter if they could: constant
+    blocks (zero covariance), one varying channel, mirror-symmetric blocks
+    (projections and sums exactly zero), extremes, and noise."""
+    rng = np.random.default_rng(90 + dim + alpha)
+    h = w = dim * 24
+    img = rng.integers(0, 256, (h, w, 4), dtype=np.uint8)
+    yy, xx = np.mgrid[0:h, 0:w]
+    by, bx = yy // dim, xx // dim
+    kind = (by * 24 + bx) % 8
+    lx, ly = xx % dim, yy % dim
+    img[kind == 0] = [128, 128, 7, 200]                                   # constant
+    img[..., 0] = np.where(kind == 1, (lx * 40) % 256, img[..., 0])       # x only
+    img[..., 1] = np.where(kind == 1, 64, img[..., 1])
+    img[..., 1] = np.where(kind == 2, (ly * 40) % 256, img[..., 1])       # y only
+    img[..., 0] = np.where(kind == 2, 200, img[..., 0])
+    sym = 128 + np.where(lx < dim // 2, -1, 1) * 50                       # mirror pairs about the mean
+    img[..., 0] = np.where(kind == 3, sym, img[..., 0])
+    img[..., 1] = np.where(kind == 3, 256 - sym, img[..., 1])
+    img[..., 0] = np.where(kind == 4, np.where((lx + ly) % 2 == 0, 0, 255), img[..., 0])
+    img[..., 1] = np.where(kind == 4, np.where((lx + ly) % 2 == 0, 255, 0), img[..., 1])
+    img[..., 0] = np.where(kind == 5, 128, img[..., 0])                   # x at the mean, y symmetric
+    img[..., 1] = np.where(kind == 5, 128 + np.where(ly < dim // 2, -3, 3), img[..., 1])
+    opts = dict(block_dim=dim, has_alpha=alpha, is_normal=True, border=1)
+    want = oracle.encode(img, **opts)
+    assert np.array_equal(native.encode(img, **opts), want)
+    assert np.array_equal(native.encode(img, precision=0, **opts), want)
+
+
 @pytest.mark.parametrize("precision,axis,quality", [(0, 0, 0), (1, 0, 0), (0, 2, 0), (0, 0, 1), (0, 0, 3)])
 def test_back_to_back_launches_keep_stream_order(native, precision, axis, quality):
     """The plain FP32, HALF2, best-fit and quality kernels are launched with programmatic
@@ -258,7 +290,8 @@ def test_launch_counter_moves(native):
 
 
 @pytest.mark.parametrize("dim,alpha,normal,srgb", [(4, False, False, False), (4, True, False, True),
-                                                   (6, True, False, True), (6, False, True, False)])
+                                                   (6, True, False, True), (6, False, True, False),
+                                                   (4, False, True, False), (6, True, True, False)])
 def test_every_kernel_variant_bit_exact(native, oracle, dim, alpha, normal, srgb):
     img = _texture(97, 61, seed=dim * 5 + alpha + srgb)
     opts = dict(block_dim=dim, has_alpha=alpha, is_normal=normal, srgb=srgb, border=1)
