@@ -89,14 +89,18 @@ Choice g_choice[2][2][2][2] = {};     // [dim6][alpha][normal][srgb]
 bool g_choice_init = false;
 std::mutex g_choice_mu;
 
-// GB300 sweep over 2048x2048 textures (us per launch at 128 threads;
-// registers / shared / capped registers): 4x4 RGB 29.0 / 27.1 / 28.9,
-// 4x4 RGBA sRGB 29.0 / 29.0 / 29.0, 4x4 normal 20.8 / 20.9 / 20.8,
-// 6x6 RGBA sRGB 26.8 / 39.1 / 24.0, 6x6 RGB 24.9 / 41.0 / 22.9.  The
-// shared-memory store loses for 6x6 (its re-reads cost more than the
-// occupancy it gains); capping the register store at 168 (no spills) lifts
-// 6x6 from 8 to 12 warps per SM.
-Choice default_choice(int dim, bool /*alpha*/, bool /*normal*/, bool /*srgb*/) {
+// GB300 sweep, launches overlapped, 8 distinct textures per step (us per
+// launch; store/threads): 2048x2048 4x4 RGB shared/128 23.4, registers/128
+// 24.9; 4x4 RGBA sRGB shared/128 23.8, registers/128 24.7; 4096x4096 4x4
+// normal map registers/128 50.9, capped/128 50.9, shared/128 53.4; 2048x2048
+// 6x6 RGBA sRGB capped/128 19.6, registers/128 23.0, shared/128 34.5; 6x6 RGB
+// capped/128 19.2, registers/128 21.6; 4096x4096 6x6 normal map
+// registers/128 41.1, capped/128 41.6.  The shared-memory store loses for 6x6
+// (its re-reads cost more than the occupancy it gains); capping the register
+// store at 168 (no spills) lifts 6x6 from 8 to 12 warps per SM.  Normal maps
+// (two varying channels) fit in registers without the cap.
+Choice default_choice(int dim, bool /*alpha*/, bool normal, bool /*srgb*/) {
+    if (normal) return Choice{kStoreRegisters, 128};
     return dim == 6 ? Choice{kStoreRegistersCapped, 128} : Choice{kStoreShared, 128};
 }
 
