@@ -212,7 +212,9 @@ __device__ __forceinline__ void find_min_max(const S& st, const float4 m, const 
 
 // the colour at weight-grid point g: the texel (4x4) or sample_texel's 2x2
 // bilinear tap sum (307-314, 6x6)
-template <int DIM, bool ZW = false, class S>
+// NCH: the channels the caller uses (2: red and green, 3: no alpha, 4: all);
+// the others are left as 0
+template <int DIM, int NCH = 4, class S>
 __device__ __forceinline__ float4 grid_sample(const S& st, int g) {
     if constexpr (DIM == 6) {
         const int i0 = grid_tap0(g);
@@ -222,13 +224,12 @@ __device__ __forceinline__ float4 grid_sample(const S& st, int g) {
         float4 s;
         s.x = __fmaf_rn(t11.x, w11, __fmaf_rn(t10.x, w10, __fmaf_rn(t01.x, w01, __fmul_rn(t00.x, w00))));
         s.y = __fmaf_rn(t11.y, w11, __fmaf_rn(t10.y, w10, __fmaf_rn(t01.y, w01, __fmul_rn(t00.y, w00))));
-        if constexpr (ZW) {                 // blue and alpha are multiplied by k2 = k3 = +0
-            s.z = 0.0f;
-            s.w = 0.0f;
-            return s;
-        }
-        s.z = __fmaf_rn(t11.z, w11, __fmaf_rn(t10.z, w10, __fmaf_rn(t01.z, w01, __fmul_rn(t00.z, w00))));
-        s.w = __fmaf_rn(t11.w, w11, __fmaf_rn(t10.w, w10, __fmaf_rn(t01.w, w01, __fmul_rn(t00.w, w00))));
+        s.z = 0.0f;
+        s.w = 0.0f;
+        if constexpr (NCH >= 3)
+            s.z = __fmaf_rn(t11.z, w11, __fmaf_rn(t10.z, w10, __fmaf_rn(t01.z, w01, __fmul_rn(t00.z, w00))));
+        if constexpr (NCH >= 4)
+            s.w = __fmaf_rn(t11.w, w11, __fmaf_rn(t10.w, w10, __fmaf_rn(t01.w, w01, __fmul_rn(t00.w, w00))));
         return s;
     } else {
         return st.get(g);
@@ -244,8 +245,12 @@ __device__ __forceinline__ void reference_weights(const S& st, const float e0[4]
     constexpr uint32_t R = ALPHA ? 5u : 11u;
     float k0 = __fsub_rn(e1[0], e0[0]), k1 = __fsub_rn(e1[1], e0[1]);
     float k2 = __fsub_rn(e1[2], e0[2]), k3 = __fsub_rn(e1[3], e0[3]);
-    // ZW: both endpoints' blue and alpha are 255, so k2 = k3 = +0
-    const float kk = ZW ? __fmaf_rn(k1, k1, __fmul_rn(k0, k0)) : dot4(k0, k1, k2, k3, k0, k1, k2, k3);
+    // the terms whose k component is exactly +0 are left out: ZW (normal
+    // maps): both endpoints' blue and alpha are 255, k2 = k3 = +0; without
+    // alpha both endpoints' alpha is forced to 255 (find_min_max), k3 = +0
+    constexpr int NCH = ZW ? 2 : (ALPHA ? 4 : 3);
+    const float kk2 = __fmaf_rn(k1, k1, __fmul_rn(k0, k0));
+    const float kk = NCH == 2 ? kk2 : NCH == 3 ? __fmaf_rn(k2, k2, kk2) : dot4(k0, k1, k2, k3, k0, k1, k2, k3);
     if (shorter_than_small_value(kk)) {
 #pragma unroll
         for (int i = 0; i < 16; ++i) qw[i] = 0u;
@@ -257,10 +262,12 @@ __device__ __forceinline__ void reference_weights(const S& st, const float e0[4]
     float minw = 1e31f, maxw = -1e31f;
 #pragma unroll
     for (int i = 0; i < 16; ++i) {
-        const float4 s = grid_sample<DIM, ZW>(st, i);
-        const float x = ZW ? __fmaf_rn(k1, __fsub_rn(s.y, e0[1]), __fmul_rn(k0, __fsub_rn(s.x, e0[0])))
-                           : dot4(k0, k1, k2, k3, __fsub_rn(s.x, e0[0]), __fsub_rn(s.y, e0[1]),
-                                  __fsub_rn(s.z, e0[2]), __fsub_rn(s.w, e0[3]));
+        const float4 s = grid_sample<DIM, NCH>(st, i);
+        const float x2 = __fmaf_rn(k1, __fsub_rn(s.y, e0[1]), __fmul_rn(k0, __fsub_rn(s.x, e0[0])));
+        const float x = NCH == 2   ? x2
+                        : NCH == 3 ? __fmaf_rn(k2, __fsub_rn(s.z, e0[2]), x2)
+                                   : dot4(k0, k1, k2, k3, __fsub_rn(s.x, e0[0]), __fsub_rn(s.y, e0[1]),
+                                          __fsub_rn(s.z, e0[2]), __fsub_rn(s.w, e0[3]));
         minw = fminf(x, minw);
         maxw = fmaxf(x, maxw);
         w[i] = x;
