@@ -107,16 +107,16 @@ __global__ void __launch_bounds__(128, 3) astc_encode_blocks_best(const BestLaun
     RegTexels<N> st;
 #pragma unroll
     for (int k = 0; k < N; ++k) st.put(k, decode_texel<SRGB, NORMAL>(px[k], s_lut));
-    const float4 m = block_mean<N>(st);
+    const float4 m = block_mean<N, NORMAL>(st);
     uint4 best = make_uint4(0u, 0u, 0u, 0u);
     uint32_t best_err = 0;
 #pragma unroll 1
     for (int axis = 0; axis < 2; ++axis) {
-        const float4 v = axis ? max_accumulation_axis<N, ALPHA>(st, m) : pca_axis<N>(st, m);
+        const float4 v = axis ? max_accumulation_axis<N, ALPHA>(st, m) : pca_axis<N, NORMAL>(st, m);
         float e0[4], e1[4];
         uint32_t q0[4], q1[4], qw[16];
-        find_min_max<N, ALPHA>(st, m, v, e0, e1, q0, q1);
-        reference_weights<DIM, ALPHA>(st, e0, e1, qw);
+        find_min_max<N, ALPHA, NORMAL>(st, m, v, e0, e1, q0, q1);
+        reference_weights<DIM, ALPHA, NORMAL>(st, e0, e1, qw);
         const uint32_t err = fixed_error<DIM, ALPHA, SRGB>(st, q0, q1, qw);
         if (axis == 0 || err < best_err) {
             best_err = err;

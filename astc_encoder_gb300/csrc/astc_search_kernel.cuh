@@ -144,16 +144,17 @@ __device__ __forceinline__ void load_search_smem(SearchSmem& sm) {
     }
 }
 
-// Endpoint fit on `axis` and the fixed-mode block (encode_block 510-550).
-template <int DIM, bool ALPHA, class S>
+// Endpoint fit on `axis` and the fixed-mode block (encode_block 510-550);
+// normal maps take the ZW forms (both axes have zero blue and alpha).
+template <int DIM, bool ALPHA, bool NORMAL, class S>
 __device__ __forceinline__ uint4 fit_fixed(const S& st, int axis, uint32_t q0[4], uint32_t q1[4],
                                            uint32_t qw[16], const uint8_t* trits) {
     constexpr int N = DIM * DIM;
-    const float4 m = block_mean<N>(st);
-    const float4 v = axis ? max_accumulation_axis<N, ALPHA>(st, m) : pca_axis<N>(st, m);
+    const float4 m = block_mean<N, NORMAL>(st);
+    const float4 v = axis ? max_accumulation_axis<N, ALPHA>(st, m) : pca_axis<N, NORMAL>(st, m);
     float e0[4], e1[4];
-    find_min_max<N, ALPHA>(st, m, v, e0, e1, q0, q1);
-    reference_weights<DIM, ALPHA>(st, e0, e1, qw);
+    find_min_max<N, ALPHA, NORMAL>(st, m, v, e0, e1, q0, q1);
+    reference_weights<DIM, ALPHA, NORMAL>(st, e0, e1, qw);
     return assemble_block<ALPHA>(q0, q1, qw, trits);
 }
 
@@ -228,7 +229,7 @@ __global__ void __launch_bounds__(kSearchThreads, 3) astc_encode_blocks_search(c
     load_block_packed<DIM>(p.tex, bx, by, px);
     const PackedTexels<N, SRGB, NORMAL> st{px, sm.lut};
     uint32_t q0[4], q1[4], qw[16];
-    uint4 fixed = fit_fixed<DIM, ALPHA>(st, thorough ? 0 : p.axis, q0, q1, qw, sm.trits);
+    uint4 fixed = fit_fixed<DIM, ALPHA, NORMAL>(st, thorough ? 0 : p.axis, q0, q1, qw, sm.trits);
     if (!thorough && !p.search) {
         p.out[b] = fixed;
         return;
@@ -237,7 +238,7 @@ __global__ void __launch_bounds__(kSearchThreads, 3) astc_encode_blocks_search(c
     uint64_t rw_packed = 0;
     if constexpr (thorough) {
         uint32_t r0[4], r1[4], rw[16];
-        fixed_b = fit_fixed<DIM, ALPHA>(st, 1, r0, r1, rw, sm.trits);
+        fixed_b = fit_fixed<DIM, ALPHA, NORMAL>(st, 1, r0, r1, rw, sm.trits);
 #pragma unroll
         for (int g = 0; g < 16; ++g) rw_packed |= (uint64_t)rw[g] << (4 * g);
     }
