@@ -291,7 +291,8 @@ astc_status astc_save_file(const char* path, int block_dim_x, int block_dim_y,
                            size_t blocks_size);
 
 /* Read a .astc file written by astc_save_file (or any 2-D .astc).  On
- * ASTC_OK *width/*height/*block_dim_x/*block_dim_y are set; when `blocks` is
+ * ASTC_OK the width, height and block dimensions are stored through their
+ * pointers; when `blocks` is
  * non-NULL up to `capacity` block bytes are copied.  *blocks_size receives
  * the block byte count.  (No counterpart in the reference, which only
  * writes.) */
