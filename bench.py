@@ -325,6 +325,30 @@ _NCU_TRAFFIC = {
 }
 
 
+# Warp instructions of one launch of the production kernel, from the same ncu
+# capture: (workload, precision, texel store) -> instructions, capture
+_NCU_INSTRUCTIONS = {
+    ("6x6_rgba_srgb_2048", 0, 2): (11_260_000, "astc_encode_blocks_fp32_6x6_rgba_srgb_2048.md: "
+                                               "11.26 M warp-instructions per launch"),
+}
+
+
+def _issue_roofline(workload: str, prec: int, tuned, mean_launch_s: float, sm_mhz, sms: int) -> dict | None:
+    """Warp instructions issued per second against the SMs' issue ceiling (4
+    schedulers per SM, one warp-instruction per cycle each, at the SM clock
+    sampled during the timed region); None without a capture of this kernel."""
+    key = (workload, prec, getattr(tuned, "store", None))
+    if key not in _NCU_INSTRUCTIONS or not sm_mhz:
+        return None
+    n, src = _NCU_INSTRUCTIONS[key]
+    achieved = n / mean_launch_s / 1e9
+    peak = sms * 4 * float(sm_mhz) / 1e3
+    return {"bound": "instruction_issue", "achieved": achieved, "peak": peak,
+            "unit": "G warp-instructions/s", "frac": achieved / peak, "instructions_per_launch": n,
+            "peak_source": f"{sms} SMs x 4 schedulers x {sm_mhz} MHz (median SM clock in the timed region)",
+            "instructions_source": "profiles/" + src}
+
+
 def _traffic(workload: str, prec: int, tuned) -> dict:
     key = (workload, prec, getattr(tuned, "store", None))
     if key not in _NCU_TRAFFIC:
@@ -780,6 +804,8 @@ def run_ours(args) -> None:
                           "peak_fma_microbenchmark": fma_peak, "peak_sgemm": sgemm_peak,
                           "peak_source": "max of an FP32 FMA microbenchmark (libastc_fp32_peak.so) and an "
                                          "8192^3 SGEMM (TF32 off), both measured in this run"},
+        "roofline_issue": _issue_roofline(args.workload, prec, tuned, mean_launch_s, clk.get("sm_mhz"),
+                                          torch.cuda.get_device_properties(local).multi_processor_count),
         "quality": quality,
         "clocks": clk,
         "wall_s_timed_region": wall,

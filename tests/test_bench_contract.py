@@ -45,3 +45,21 @@ def test_help_lists_the_contract_flags():
     assert r.returncode == 0
     for flag in ("--gpus", "--steps", "--warmup", "--impl", "--wave-sweep"):
         assert flag in r.stdout
+
+
+def test_issue_roofline_arithmetic():
+    """roofline_issue: instructions per launch from the committed capture over
+    the launch time, against 4 warp-instructions per SM per cycle."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("bench_mod", BENCH)
+    bench = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bench)
+
+    class Tuned:
+        store = 2
+    r = bench._issue_roofline("6x6_rgba_srgb_2048", 0, Tuned(), 20e-6, 2000, 150)
+    assert abs(r["peak"] - 150 * 4 * 2.0) < 1e-9
+    assert abs(r["achieved"] - r["instructions_per_launch"] / 20e-6 / 1e9) < 1e-6
+    assert abs(r["frac"] - r["achieved"] / r["peak"]) < 1e-12
+    assert bench._issue_roofline("4x4_rgb_512", 0, Tuned(), 20e-6, 2000, 150) is None
+    assert bench._issue_roofline("6x6_rgba_srgb_2048", 0, Tuned(), 20e-6, None, 150) is None
