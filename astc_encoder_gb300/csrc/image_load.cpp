@@ -464,12 +464,15 @@ bool decode_bmp(const uint8_t* d, size_t n, Image& img, std::string& err) {
     return true;
 }
 
-// Baseline sequential JPEG (ITU-T T.81: SOF0 / SOF1, 8-bit samples, Huffman
-// coding, one grey or three YCbCr components with sampling factors 1..2,
-// restart intervals).  Coefficients are dequantised and taken through a
-// separable floating-point inverse DCT (+128, rounded, clamped); chroma is
-// upsampled by replication and converted with the JFIF equations.
-// Progressive, arithmetic-coded, 12-bit and CMYK files are refused.
+// Baseline and progressive JPEG (ITU-T T.81: SOF0 / SOF1 / SOF2, 8-bit
+// samples, Huffman coding; one grey or three YCbCr components with sampling
+// factors 1..2; interleaved and single-component scans; spectral selection and
+// successive approximation (Annex G); restart intervals).  The scans fill each
+// component's quantised coefficients; then every block is dequantised and
+// taken through a separable floating-point inverse DCT (+128, rounded,
+// clamped), chroma is upsampled by replication and converted with the JFIF
+// equations.  Arithmetic-coded, lossless, hierarchical, 12-bit and CMYK files
+// are refused.
 namespace {
 
 struct JpegHuff {
@@ -565,24 +568,139 @@ void jpeg_idct(const float in[64], uint8_t* out, int stride) {
         }
 }
 
+int16_t clamp16(long long v) { return (int16_t)(v < -32768 ? -32768 : v > 32767 ? 32767 : v); }
+
+// One component: its quantised coefficients, natural order, on the block grid
+// of the MCU-padded image (bh x bw blocks of 64).
+struct JpegComp {
+    int id = 0, h = 1, v = 1, tq = 0, td = 0, ta = 0;
+    int bw = 0, bh = 0;          // MCU-padded block grid
+    int cbw = 0, cbh = 0;        // blocks a single-component scan covers
+    std::vector<int16_t> coef;
+    long long pred = 0;          // DC predictor
+    bool dc_seen = false;
+};
+
+struct JpegScanParams {
+    int ss, se, ah, al;
+    bool progressive;
+};
+
+// One block of a scan (Annex F for sequential, G.1.2 for progressive).
+bool jpeg_block(JpegBits& b, const JpegHuff* dc, const JpegHuff* ac, const JpegScanParams& sp, JpegComp& c,
+                int16_t* blk, int& eobrun) {
+    if (!sp.progressive) {
+        const int t = jpeg_decode_sym(b, *dc);
+        if (t < 0 || t > 11) return false;
+        c.pred += jpeg_extend(b.get(t), t);
+        blk[0] = clamp16(c.pred);
+        for (int k = 1; k < 64;) {
+            const int rs = jpeg_decode_sym(b, *ac);
+            if (rs < 0) return false;
+            const int r = rs >> 4, sz = rs & 15;
+            if (sz == 0) {
+                if (r != 15) break;               // EOB
+                k += 16;                          // ZRL
+                continue;
+            }
+            k += r;
+            if (k > 63) return false;
+            blk[kZigzag[k]] = (int16_t)jpeg_extend(b.get(sz), sz);
+            ++k;
+        }
+        return true;
+    }
+    if (sp.ss == 0) {                               // DC scans
+        if (sp.ah == 0) {
+            const int t = jpeg_decode_sym(b, *dc);
+            if (t < 0 || t > 11) return false;
+            c.pred += jpeg_extend(b.get(t), t);
+            blk[0] = clamp16(c.pred * (1ll << sp.al));
+        } else if (b.bit()) {
+            blk[0] = (int16_t)(blk[0] | (1 << sp.al));
+        }
+        return true;
+    }
+    if (sp.ah == 0) {                               // AC first scan
+        if (eobrun > 0) { --eobrun; return true; }
+        for (int k = sp.ss; k <= sp.se;) {
+            const int rs = jpeg_decode_sym(b, *ac);
+            if (rs < 0) return false;
+            const int r = rs >> 4, sz = rs & 15;
+            if (sz == 0) {
+                if (r < 15) {                       // EOB run
+                    eobrun = (1 << r) - 1;
+                    if (r) eobrun += b.get(r);
+                    break;
+                }
+                k += 16;                            // ZRL
+                continue;
+            }
+            k += r;
+            if (k > sp.se) return false;
+            blk[kZigzag[k]] = clamp16((long long)jpeg_extend(b.get(sz), sz) * (1ll << sp.al));
+            ++k;
+        }
+        return true;
+    }
+    // AC refinement: a correction bit for every coefficient already nonzero,
+    // and newly nonzero coefficients of magnitude 1 << al
+    const int p1 = 1 << sp.al, m1 = -p1;
+    auto refine = [&](int z) {
+        if (b.bit() && (blk[z] & p1) == 0) blk[z] = (int16_t)(blk[z] + (blk[z] >= 0 ? p1 : m1));
+    };
+    int k = sp.ss;
+    if (eobrun == 0) {
+        for (; k <= sp.se; ++k) {
+            const int rs = jpeg_decode_sym(b, *ac);
+            if (rs < 0) return false;
+            int r = rs >> 4;
+            const int sz = rs & 15;
+            int val = 0;
+            if (sz) {
+                if (sz != 1) return false;
+                val = b.bit() ? p1 : m1;
+            } else if (r != 15) {                   // EOB run: this block's rest is refined below
+                eobrun = 1 << r;
+                if (r) eobrun += b.get(r);
+                break;
+            }
+            // skip r coefficients that are still zero, refining the nonzero ones on the way
+            for (; k <= sp.se; ++k) {
+                const int z = kZigzag[k];
+                if (blk[z] != 0) {
+                    refine(z);
+                } else {
+                    if (r == 0) break;
+                    --r;
+                }
+            }
+            if (val) {
+                if (k > sp.se) return false;
+                blk[kZigzag[k]] = (int16_t)val;
+            }
+        }
+    }
+    if (eobrun > 0) {
+        for (; k <= sp.se; ++k)
+            if (blk[kZigzag[k]] != 0) refine(kZigzag[k]);
+        --eobrun;
+    }
+    return true;
+}
+
 }  // namespace
 
 bool decode_jpeg(const uint8_t* d, size_t n, Image& img, std::string& err) {
     if (n < 4 || d[0] != 0xFF || d[1] != 0xD8) { err = "not a JPEG file"; return false; }
     uint16_t qt[4][64] = {};
     JpegHuff hdc[4], hac[4];
-    struct Comp {
-        int id, h, v, tq, td = 0, ta = 0;
-        std::vector<uint8_t> plane;
-        int pw = 0, ph = 0;
-        long long dc = 0;                                   // DC predictor (no overflow on corrupt data)
-    };
-    std::vector<Comp> comps;
-    int width = 0, height = 0, restart = 0, hmax = 1, vmax = 1;
-    bool frame = false, done = false;
+    std::vector<JpegComp> comps;
+    int width = 0, height = 0, restart = 0, hmax = 1, vmax = 1, mcux = 0, mcuy = 0, scans = 0;
+    bool frame = false, progressive = false;
     size_t pos = 2;
     auto u16 = [&](size_t o) { return (int)((d[o] << 8) | d[o + 1]); };
-    while (pos + 4 <= n && !done) {
+    while (pos + 4 <= n) {
         if (d[pos] != 0xFF) { ++pos; continue; }
         const int m = d[pos + 1];
         if (m == 0xFF) { ++pos; continue; }
@@ -591,7 +709,7 @@ bool decode_jpeg(const uint8_t* d, size_t n, Image& img, std::string& err) {
         const int len = u16(pos + 2);
         const size_t seg = pos + 4, end = pos + 2 + (size_t)len;
         if (len < 2 || end > n) { err = "JPEG segment past the end"; return false; }
-        const size_t need = m == 0xC0 || m == 0xC1 ? 6 : m == 0xDD ? 2 : m == 0xDA ? 1 : 0;
+        const size_t need = m == 0xC0 || m == 0xC1 || m == 0xC2 ? 6 : m == 0xDD ? 2 : m == 0xDA ? 1 : 0;
         if (seg + need > end) { err = "JPEG segment too short"; return false; }
         if (m == 0xDB) {                                          // DQT
             for (size_t o = seg; o < end;) {
@@ -614,8 +732,10 @@ bool decode_jpeg(const uint8_t* d, size_t n, Image& img, std::string& err) {
                 h.present = true;
                 o += 17 + total;
             }
-        } else if (m == 0xC0 || m == 0xC1) {                      // SOF0 / SOF1
+        } else if (m == 0xC0 || m == 0xC1 || m == 0xC2) {         // SOF0 / SOF1 / SOF2
+            if (frame) { err = "JPEG with more than one frame"; return false; }
             if (d[seg] != 8) { err = "only 8-bit JPEG is read"; return false; }
+            progressive = m == 0xC2;
             height = u16(seg + 1);
             width = u16(seg + 3);
             const int nc = d[seg + 5];
@@ -625,7 +745,7 @@ bool decode_jpeg(const uint8_t* d, size_t n, Image& img, std::string& err) {
                 return false;
             }
             for (int i = 0; i < nc; ++i) {
-                Comp c;
+                JpegComp c;
                 c.id = d[seg + 6 + 3 * i];
                 c.h = d[seg + 7 + 3 * i] >> 4;
                 c.v = d[seg + 7 + 3 * i] & 15;
@@ -636,92 +756,122 @@ bool decode_jpeg(const uint8_t* d, size_t n, Image& img, std::string& err) {
                 comps.push_back(c);
             }
             if (nc == 1) comps[0].h = comps[0].v = hmax = vmax = 1;   // one component: blocks in raster order
+            mcux = (width + 8 * hmax - 1) / (8 * hmax);
+            mcuy = (height + 8 * vmax - 1) / (8 * vmax);
+            for (auto& c : comps) {
+                c.bw = mcux * c.h;
+                c.bh = mcuy * c.v;
+                c.cbw = ((width * c.h + hmax - 1) / hmax + 7) / 8;
+                c.cbh = ((height * c.v + vmax - 1) / vmax + 7) / 8;
+            }
             frame = true;
-        } else if ((m >= 0xC2 && m <= 0xCF) && m != 0xC4 && m != 0xC8 && m != 0xCC) {
-            err = "progressive, lossless or arithmetic-coded JPEG is not read";
+        } else if ((m >= 0xC3 && m <= 0xCF) && m != 0xC4 && m != 0xC8 && m != 0xCC) {
+            err = "lossless, hierarchical or arithmetic-coded JPEG is not read";
             return false;
         } else if (m == 0xDD) {                                   // DRI
             restart = u16(seg);
-        } else if (m == 0xDA) {                                   // SOS: one interleaved scan
+        } else if (m == 0xDA) {                                   // SOS
             if (!frame) { err = "JPEG scan before the frame header"; return false; }
+            if (++scans > 256) { err = "too many JPEG scans"; return false; }
             const int ns = d[seg];
-            if (ns != (int)comps.size()) { err = "non-interleaved JPEG scans are not read"; return false; }
-            if (seg + 1 + 2 * (size_t)ns > end) { err = "JPEG segment too short"; return false; }
+            if (ns < 1 || ns > (int)comps.size() || seg + 4 + 2 * (size_t)ns > end) {
+                err = "bad JPEG scan header";
+                return false;
+            }
+            std::vector<JpegComp*> sc;
             for (int i = 0; i < ns; ++i) {
                 const int id = d[seg + 1 + 2 * i], t = d[seg + 2 + 2 * i];
-                bool found = false;
+                JpegComp* found = nullptr;
                 for (auto& c : comps)
-                    if (c.id == id) { c.td = t >> 4; c.ta = t & 15; found = true; }
+                    if (c.id == id) found = &c;
                 if (!found) { err = "JPEG scan names an unknown component"; return false; }
+                found->td = t >> 4;
+                found->ta = t & 15;
+                sc.push_back(found);
             }
-            for (auto& c : comps)
-                if (c.td > 3 || c.ta > 3 || !hdc[c.td].present || !hac[c.ta].present) {
+            const size_t q = seg + 1 + 2 * (size_t)ns;
+            const JpegScanParams sp{d[q], d[q + 1], d[q + 2] >> 4, d[q + 2] & 15, progressive};
+            if (!progressive ? (sp.ss != 0 || sp.se != 63 || sp.ah || sp.al)
+                             : (sp.se > 63 || sp.ss > sp.se || (sp.ss == 0 && sp.se != 0) || (sp.ss > 0 && ns != 1) ||
+                                sp.ah > 13 || sp.al > 13)) {
+                err = "bad JPEG scan parameters";
+                return false;
+            }
+            const bool dc_first = sp.ss == 0 && sp.ah == 0;
+            for (JpegComp* c : sc) {
+                if ((dc_first || sp.ss == 0) ? (c->td > 3 || (dc_first && !hdc[c->td].present))
+                                             : (c->ta > 3 || !hac[c->ta].present)) {
                     err = "JPEG Huffman table missing";
                     return false;
                 }
-            const int mcux = (width + 8 * hmax - 1) / (8 * hmax), mcuy = (height + 8 * vmax - 1) / (8 * vmax);
-            // every block codes at least a DC and an AC symbol of one bit or more
-            int per_mcu = 0;
-            for (auto& c : comps) per_mcu += c.h * c.v;
-            if ((long long)mcux * mcuy * per_mcu > 4ll * (long long)(n - end) + 64) {
-                err = "JPEG data too short for its size";
-                return false;
-            }
-            for (auto& c : comps) {
-                c.pw = mcux * c.h * 8;
-                c.ph = mcuy * c.v * 8;
-                c.plane.assign((size_t)c.pw * c.ph, 0);
-                c.dc = 0;
+                if (!progressive && (c->ta > 3 || !hac[c->ta].present)) { err = "JPEG Huffman table missing"; return false; }
+                if (c->coef.empty()) {
+                    // a component's first scan codes its DC: at least one bit per block (two in a
+                    // sequential scan), which bounds the work by the file's size
+                    if (!dc_first) { err = "JPEG AC scan before the DC scan"; return false; }
+                    const long long blocks = ns == 1 ? (long long)c->cbw * c->cbh : (long long)c->bw * c->bh;
+                    if (blocks > 8ll * (long long)(n - end) + 64) { err = "JPEG data too short for its size"; return false; }
+                    c->coef.assign((size_t)c->bw * c->bh * 64, 0);
+                }
+                c->pred = 0;
             }
             JpegBits bits{d, n, end};
-            float blk[64];
-            int mcus = 0;
-            for (int my = 0; my < mcuy; ++my)
-                for (int mx = 0; mx < mcux; ++mx) {
-                    if (restart && mcus > 0 && mcus % restart == 0) {
-                        // the RSTn marker ends the interval: realign, reset predictors
-                        bits.reset();
-                        while (bits.pos + 1 < n && !(d[bits.pos] == 0xFF && d[bits.pos + 1] >= 0xD0 &&
-                                                     d[bits.pos + 1] <= 0xD7))
-                            ++bits.pos;
-                        bits.pos += 2;
-                        bits.marker = false;
-                        for (auto& c : comps) c.dc = 0;
-                    }
-                    ++mcus;
-                    for (auto& c : comps)
-                        for (int by = 0; by < c.v; ++by)
-                            for (int bx = 0; bx < c.h; ++bx) {
-                                for (int i = 0; i < 64; ++i) blk[i] = 0.0f;
-                                const int t = jpeg_decode_sym(bits, hdc[c.td]);
-                                if (t < 0 || t > 11) { err = "corrupt JPEG data"; return false; }
-                                c.dc += jpeg_extend(bits.get(t), t);
-                                blk[0] = (float)c.dc * (float)qt[c.tq][0];
-                                for (int k = 1; k < 64;) {
-                                    const int rs = jpeg_decode_sym(bits, hac[c.ta]);
-                                    if (rs < 0) { err = "corrupt JPEG data"; return false; }
-                                    const int r = rs >> 4, sz = rs & 15;
-                                    if (sz == 0) {
-                                        if (r != 15) break;           // EOB
-                                        k += 16;                      // ZRL
-                                        continue;
-                                    }
-                                    k += r;
-                                    if (k > 63) { err = "corrupt JPEG data"; return false; }
-                                    const int z = kZigzag[k];
-                                    blk[z] = (float)jpeg_extend(bits.get(sz), sz) * (float)qt[c.tq][z];
-                                    ++k;
-                                }
-                                if (bits.past > 8) { err = "JPEG data too short"; return false; }
-                                const int ox = (mx * c.h + bx) * 8, oy = (my * c.v + by) * 8;
-                                jpeg_idct(blk, c.plane.data() + (size_t)oy * c.pw + ox, c.pw);
-                            }
+            int eobrun = 0, units = 0;
+            const long long nunits = ns == 1 ? (long long)sc[0]->cbw * sc[0]->cbh : (long long)mcux * mcuy;
+            for (long long u = 0; u < nunits; ++u) {
+                if (restart && units > 0 && units % restart == 0) {
+                    // the RSTn marker ends the interval: realign, reset predictors and EOB runs
+                    bits.reset();
+                    while (bits.pos + 1 < n && !(d[bits.pos] == 0xFF && d[bits.pos + 1] >= 0xD0 &&
+                                                 d[bits.pos + 1] <= 0xD7))
+                        ++bits.pos;
+                    bits.pos += 2;
+                    bits.marker = false;
+                    eobrun = 0;
+                    for (JpegComp* c : sc) c->pred = 0;
                 }
-            done = true;
+                ++units;
+                for (JpegComp* c : sc) {
+                    const int nby = ns == 1 ? 1 : c->v, nbx = ns == 1 ? 1 : c->h;
+                    for (int by = 0; by < nby; ++by)
+                        for (int bx = 0; bx < nbx; ++bx) {
+                            const long long row = ns == 1 ? u / c->cbw : (u / mcux) * c->v + by;
+                            const long long col = ns == 1 ? u % c->cbw : (u % mcux) * c->h + bx;
+                            int16_t* blk = c->coef.data() + ((size_t)row * c->bw + (size_t)col) * 64;
+                            if (!jpeg_block(bits, &hdc[c->td & 3], &hac[c->ta & 3], sp, *c, blk, eobrun)) {
+                                err = "corrupt JPEG data";
+                                return false;
+                            }
+                        }
+                    if (dc_first) c->dc_seen = true;
+                }
+                if (bits.past > 8) { err = "JPEG data too short"; return false; }
+            }
+            // continue after the entropy-coded data, at the next marker that is not RSTn
+            size_t p = bits.pos;
+            while (p + 1 < n && !(d[p] == 0xFF && d[p + 1] != 0x00 && !(d[p + 1] >= 0xD0 && d[p + 1] <= 0xD7))) ++p;
+            pos = p;
+            continue;
         }
         pos = end;
     }
-    if (!done) { err = "JPEG has no image scan"; return false; }
+    if (!frame || scans == 0) { err = "JPEG has no image scan"; return false; }
+    for (auto& c : comps)
+        if (!c.dc_seen) { err = "JPEG component without a scan"; return false; }
+    // dequantise and inverse-transform every block into the component planes
+    std::vector<std::vector<uint8_t>> planes(comps.size());
+    for (size_t ci = 0; ci < comps.size(); ++ci) {
+        const JpegComp& c = comps[ci];
+        const int pw = c.bw * 8;
+        planes[ci].assign((size_t)pw * c.bh * 8, 0);
+        float blk[64];
+        for (int by = 0; by < c.bh; ++by)
+            for (int bx = 0; bx < c.bw; ++bx) {
+                const int16_t* q = c.coef.data() + ((size_t)by * c.bw + bx) * 64;
+                for (int i = 0; i < 64; ++i) blk[i] = (float)q[i] * (float)qt[c.tq][i];
+                jpeg_idct(blk, planes[ci].data() + (size_t)by * 8 * pw + bx * 8, pw);
+            }
+    }
     img.width = width;
     img.height = height;
     img.rgba.assign((size_t)width * height * 4, 255);
@@ -729,9 +879,9 @@ bool decode_jpeg(const uint8_t* d, size_t n, Image& img, std::string& err) {
         for (int x = 0; x < width; ++x) {
             float v[3];
             for (size_t c = 0; c < comps.size(); ++c) {
-                const Comp& k = comps[c];
+                const JpegComp& k = comps[c];
                 const int sx = x * k.h / hmax, sy = y * k.v / vmax;   // replication
-                v[c] = k.plane[(size_t)sy * k.pw + sx];
+                v[c] = planes[c][(size_t)sy * k.bw * 8 + sx];
             }
             uint8_t* o = img.rgba.data() + ((size_t)y * width + x) * 4;
             if (comps.size() == 1) {

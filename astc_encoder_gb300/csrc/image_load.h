@@ -3,7 +3,7 @@
 // channels reduced to their high byte; non-interlaced), Netpbm P5/P6/P7,
 // Windows BMP (24/32-bit, uncompressed or bit fields), Truevision TGA
 // (24/32-bit true colour and 8-bit grey, raw or run-length encoded) and
-// baseline JPEG (8-bit grey or YCbCr, Huffman coded, one interleaved scan).
+// JPEG (8-bit grey or YCbCr, Huffman coded, baseline or progressive).
 // Output is always RGBA8, row 0 first (the caller flips for the reference's
 // orientation, main.cpp:24).  Written for this project; the reference uses
 // the third-party stb_image for the same job.

@@ -6,7 +6,7 @@ PNG (8-bit greyscale / grey+alpha / RGB / RGBA / palette, non-interlaced,
 all five row filters, zlib from the Python standard library), Netpbm
 P5/P6/P7, Windows BMP (24/32-bit, uncompressed or bit fields), Truevision
 TGA (8-bit grey, 24/32-bit true colour, raw or run-length encoded) and
-baseline JPEG (8-bit grey or YCbCr, Huffman coded, one interleaved scan) -- the
+JPEG (8-bit grey or YCbCr, Huffman coded, baseline or progressive) -- the
 same formats as the C++ reader of the command line tool.  It always returns
 a (H, W, 4) uint8 array, row 0 first; the caller flips when it wants the
 reference's orientation.
@@ -249,17 +249,19 @@ def _jpeg_huffman(counts, syms):
 
 
 def load_jpeg(path: str) -> np.ndarray:
-    """Baseline sequential JPEG (ITU-T T.81 SOF0/SOF1, 8-bit, Huffman, grey or
-    YCbCr with sampling factors 1..2, one interleaved scan, restart intervals):
-    the same decoding as the command line tool's reader, in float64."""
+    """Baseline and progressive JPEG (ITU-T T.81 SOF0/SOF1/SOF2, 8-bit, Huffman,
+    grey or YCbCr with sampling factors 1..2, interleaved and single-component
+    scans, spectral selection and successive approximation, restart
+    intervals): the same decoding as the command line tool's reader, in
+    float64."""
     with open(path, "rb") as fh:
         d = fh.read()
     if d[:2] != b"\xff\xd8":
         raise ValueError("not a JPEG file")
     qt = np.zeros((4, 64), np.int64)
     huff = {}
-    comps, restart, pos = [], 0, 2
-    width = height = 0
+    comps, restart, pos, frame = [], 0, 2, None
+    scans = 0
     while pos + 4 <= len(d):
         if d[pos] != 0xFF:
             pos += 1
@@ -289,7 +291,7 @@ def load_jpeg(path: str) -> np.ndarray:
                 total = sum(counts)
                 huff[(d[o] >> 4, d[o] & 15)] = _jpeg_huffman(counts, d[o + 17:o + 17 + total])
                 o += 17 + total
-        elif m in (0xC0, 0xC1):
+        elif m in (0xC0, 0xC1, 0xC2):
             if d[seg] != 8:
                 raise ValueError("only 8-bit JPEG is read")
             height, width = struct.unpack_from(">HH", d, seg + 1)
@@ -301,118 +303,243 @@ def load_jpeg(path: str) -> np.ndarray:
                 comps.append({"id": c[0], "h": c[1] >> 4, "v": c[1] & 15, "tq": c[2] & 3})
             if nc == 1:
                 comps[0]["h"] = comps[0]["v"] = 1
-        elif 0xC2 <= m <= 0xCF and m not in (0xC4, 0xC8, 0xCC):
-            raise ValueError("progressive, lossless or arithmetic-coded JPEG is not read")
+            hmax = max(c["h"] for c in comps)
+            vmax = max(c["v"] for c in comps)
+            mcux, mcuy = -(-width // (8 * hmax)), -(-height // (8 * vmax))
+            for c in comps:
+                c["bw"], c["bh"] = mcux * c["h"], mcuy * c["v"]
+                c["cbw"] = (-(-width * c["h"] // hmax) + 7) // 8
+                c["cbh"] = (-(-height * c["v"] // vmax) + 7) // 8
+                c["coef"] = None
+            frame = dict(width=width, height=height, hmax=hmax, vmax=vmax, mcux=mcux, mcuy=mcuy,
+                         progressive=m == 0xC2)
+        elif 0xC3 <= m <= 0xCF and m not in (0xC4, 0xC8, 0xCC):
+            raise ValueError("lossless, hierarchical or arithmetic-coded JPEG is not read")
         elif m == 0xDD:
             restart = struct.unpack_from(">H", d, seg)[0]
         elif m == 0xDA:
+            if frame is None:
+                raise ValueError("JPEG scan before the frame header")
+            scans += 1
             ns = d[seg]
-            if ns != len(comps):
-                raise ValueError("non-interleaved JPEG scans are not read")
+            sc = []
             for i in range(ns):
                 cid, t = d[seg + 1 + 2 * i], d[seg + 2 + 2 * i]
-                for c in comps:
-                    if c["id"] == cid:
-                        c["td"], c["ta"] = t >> 4, t & 15
-            return _jpeg_scan(d, end, width, height, comps, qt, huff, restart)
+                c = next((c for c in comps if c["id"] == cid), None)
+                if c is None:
+                    raise ValueError("JPEG scan names an unknown component")
+                c["td"], c["ta"] = t >> 4, t & 15
+                sc.append(c)
+            q = seg + 1 + 2 * ns
+            ss, se, ah, al = d[q], d[q + 1], d[q + 2] >> 4, d[q + 2] & 15
+            prog = frame["progressive"]
+            if (not prog and (ss, se, ah, al) != (0, 63, 0, 0)) or \
+                    (prog and (se > 63 or ss > se or (ss == 0 and se != 0) or (ss > 0 and ns != 1))):
+                raise ValueError("bad JPEG scan parameters")
+            for c in sc:
+                if c["coef"] is None:
+                    if not (ss == 0 and ah == 0):
+                        raise ValueError("JPEG AC scan before the DC scan")
+                    c["coef"] = np.zeros((c["bh"], c["bw"], 64), np.int64)
+            pos = _jpeg_scan(d, end, frame, sc, ss, se, ah, al, huff, restart)
+            continue
         pos = end
-    raise ValueError("JPEG has no image scan")
+    if frame is None or scans == 0:
+        raise ValueError("JPEG has no image scan")
+    if any(c["coef"] is None for c in comps):
+        raise ValueError("JPEG component without a scan")
+    return _jpeg_image(frame, comps, qt)
 
 
-def _jpeg_segments(d, pos):
-    """The entropy-coded data from pos, split at RSTn markers, unstuffed."""
-    segs, cur = [], bytearray()
-    while pos < len(d):
-        b = d[pos]
-        if b == 0xFF and pos + 1 < len(d):
-            nx = d[pos + 1]
-            if nx == 0x00:
-                cur.append(0xFF)
-                pos += 2
-                continue
-            if 0xD0 <= nx <= 0xD7:
-                segs.append(bytes(cur))
-                cur = bytearray()
-                pos += 2
-                continue
-            break
-        cur.append(b)
-        pos += 1
-    segs.append(bytes(cur))
-    return segs
+class _JpegBits:
+    """Entropy-coded data from `pos`: unstuffed bytes, with the positions of
+    the RSTn markers; reads past the data (or a marker) give zero bits."""
 
+    def __init__(self, d, pos):
+        out, rst = bytearray(), []
+        while pos < len(d):
+            b = d[pos]
+            if b == 0xFF and pos + 1 < len(d):
+                nx = d[pos + 1]
+                if nx == 0x00:
+                    out.append(0xFF)
+                    pos += 2
+                    continue
+                if 0xD0 <= nx <= 0xD7:
+                    rst.append(len(out))
+                    pos += 2
+                    continue
+                break
+            out.append(b)
+            pos += 1
+        self.data, self.rst, self.end = bytes(out) + b"\0\0\0\0", rst, pos
+        self.limit, self.bitpos, self.seg = len(out) if not rst else rst[0], 0, 0
 
-def _jpeg_scan(d, pos, width, height, comps, qt, huff, restart):
-    hmax = max(c["h"] for c in comps)
-    vmax = max(c["v"] for c in comps)
-    mcux, mcuy = -(-width // (8 * hmax)), -(-height // (8 * vmax))
-    nmcu = mcux * mcuy
-    if nmcu * sum(c["h"] * c["v"] for c in comps) > 4 * (len(d) - pos) + 64:
-        raise ValueError("JPEG data too short for its size")   # >= 2 bits per block
-    segs = _jpeg_segments(d, pos)
-    coef = [np.zeros((mcuy * c["v"], mcux * c["h"], 64), np.float64) for c in comps]
-    seg_i, data, bitpos, dc = -1, b"", 0, [0] * len(comps)
+    def restart(self):
+        self.bitpos = 8 * self.rst[self.seg] if self.seg < len(self.rst) else 8 * (len(self.data) - 4)
+        self.seg += 1
+        self.limit = self.rst[self.seg] if self.seg < len(self.rst) else len(self.data) - 4
 
-    def bits(k):
-        nonlocal bitpos
-        v = 0
-        for _ in range(k):
-            byte = bitpos >> 3
-            b = data[byte] if byte < len(data) else 0
-            v = (v << 1) | ((b >> (7 - (bitpos & 7))) & 1)
-            bitpos += 1
+    def bit(self):
+        byte = self.bitpos >> 3
+        v = (self.data[byte] >> (7 - (self.bitpos & 7))) & 1 if byte < self.limit else 0
+        self.bitpos += 1
         return v
 
-    def sym(table):
-        nonlocal bitpos
-        byte = bitpos >> 3
-        w = int.from_bytes((data[byte:byte + 3] + b"\0\0\0")[:3], "big")
-        peek = (w >> (8 - (bitpos & 7))) & 0xFFFF
+    def get(self, k):
+        v = 0
+        for _ in range(k):
+            v = (v << 1) | self.bit()
+        return v
+
+    def sym(self, table):
+        byte = self.bitpos >> 3
+        w = int.from_bytes(self.data[byte:byte + 3], "big") if byte + 3 <= self.limit else \
+            int.from_bytes((self.data[byte:self.limit] + b"\0\0\0")[:3], "big")
+        peek = (w >> (8 - (self.bitpos & 7))) & 0xFFFF
         s, length = table[peek]
         if length < 0:
             raise ValueError("corrupt JPEG data")
-        bitpos += int(length)
+        self.bitpos += int(length)
         return int(s)
 
-    def extend(v, t):
-        return 0 if t == 0 else (v - (1 << t) + 1 if v < (1 << (t - 1)) else v)
+    def overrun(self):
+        return self.bitpos > 8 * self.limit + 64
 
-    for n in range(nmcu):
-        if n == 0 or (restart and n % restart == 0):
-            seg_i += 1
-            data = segs[seg_i] if seg_i < len(segs) else b""
-            bitpos, dc = 0, [0] * len(comps)
-        my, mx = divmod(n, mcux)
-        for ci, c in enumerate(comps):
-            dct, act = huff[(0, c["td"])], huff[(1, c["ta"])]
+
+def _extend(v, t):
+    return 0 if t == 0 else (v - (1 << t) + 1 if v < (1 << (t - 1)) else v)
+
+
+def _jpeg_scan(d, pos, frame, sc, ss, se, ah, al, huff, restart):
+    """Decodes one scan into the components' coefficients; returns the
+    position of the next marker."""
+    bits = _JpegBits(d, pos)
+    prog = frame["progressive"]
+    single = len(sc) == 1
+    units = sc[0]["cbw"] * sc[0]["cbh"] if single else frame["mcux"] * frame["mcuy"]
+    eobrun = [0]
+    for c in sc:
+        c["pred"] = 0
+    p1, m1 = 1 << al, -(1 << al)
+
+    def refine(blk, z):
+        if bits.bit() and (blk[z] & p1) == 0:
+            blk[z] += p1 if blk[z] >= 0 else m1
+
+    def block(c, blk):
+        if not prog or ss == 0:
+            if ah == 0:
+                t = bits.sym(huff[(0, c["td"])])
+                if t > 11:
+                    raise ValueError("corrupt JPEG data")
+                c["pred"] += _extend(bits.get(t), t)
+                blk[0] = c["pred"] << al
+            elif bits.bit():
+                blk[0] |= p1
+            if prog:
+                return
+            k = 1
+            act = huff[(1, c["ta"])]
+            while k < 64:
+                rs = bits.sym(act)
+                r, sz = rs >> 4, rs & 15
+                if sz == 0:
+                    if r != 15:
+                        break
+                    k += 16
+                    continue
+                k += r
+                if k > 63:
+                    raise ValueError("corrupt JPEG data")
+                blk[_ZIGZAG[k]] = _extend(bits.get(sz), sz)
+                k += 1
+            return
+        act = huff[(1, c["ta"])]
+        if ah == 0:                                      # AC first
+            if eobrun[0] > 0:
+                eobrun[0] -= 1
+                return
+            k = ss
+            while k <= se:
+                rs = bits.sym(act)
+                r, sz = rs >> 4, rs & 15
+                if sz == 0:
+                    if r < 15:
+                        eobrun[0] = (1 << r) - 1 + (bits.get(r) if r else 0)
+                        break
+                    k += 16
+                    continue
+                k += r
+                if k > se:
+                    raise ValueError("corrupt JPEG data")
+                blk[_ZIGZAG[k]] = _extend(bits.get(sz), sz) << al
+                k += 1
+            return
+        k = ss                                           # AC refinement
+        if eobrun[0] == 0:
+            while k <= se:
+                rs = bits.sym(act)
+                r, sz = rs >> 4, rs & 15
+                val = 0
+                if sz:
+                    if sz != 1:
+                        raise ValueError("corrupt JPEG data")
+                    val = p1 if bits.bit() else m1
+                elif r != 15:
+                    eobrun[0] = (1 << r) + (bits.get(r) if r else 0)
+                    break
+                while k <= se:
+                    z = _ZIGZAG[k]
+                    if blk[z] != 0:
+                        refine(blk, z)
+                    else:
+                        if r == 0:
+                            break
+                        r -= 1
+                    k += 1
+                if val:
+                    if k > se:
+                        raise ValueError("corrupt JPEG data")
+                    blk[_ZIGZAG[k]] = val
+                k += 1
+        if eobrun[0] > 0:
+            while k <= se:
+                if blk[_ZIGZAG[k]] != 0:
+                    refine(blk, _ZIGZAG[k])
+                k += 1
+            eobrun[0] -= 1
+
+    mcux = frame["mcux"]
+    for u in range(units):
+        if restart and u and u % restart == 0:
+            bits.restart()
+            eobrun[0] = 0
+            for c in sc:
+                c["pred"] = 0
+        for c in sc:
+            if single:
+                block(c, c["coef"][u // c["cbw"], u % c["cbw"]])
+                continue
+            my, mx = divmod(u, mcux)
             for by in range(c["v"]):
                 for bx in range(c["h"]):
-                    if bitpos > 8 * len(data) + 64:
-                        raise ValueError("JPEG data too short")
-                    blk = coef[ci][my * c["v"] + by, mx * c["h"] + bx]
-                    t = sym(dct)
-                    dc[ci] += extend(bits(t), t)
-                    blk[0] = dc[ci]
-                    k = 1
-                    while k < 64:
-                        rs = sym(act)
-                        r, sz = rs >> 4, rs & 15
-                        if sz == 0:
-                            if r != 15:
-                                break
-                            k += 16
-                            continue
-                        k += r
-                        blk[_ZIGZAG[k]] = extend(bits(sz), sz)
-                        k += 1
+                    block(c, c["coef"][my * c["v"] + by, mx * c["h"] + bx])
+        if bits.overrun():
+            raise ValueError("JPEG data too short")
+    return bits.end
+
+
+def _jpeg_image(frame, comps, qt):
+    width, height, hmax, vmax = frame["width"], frame["height"], frame["hmax"], frame["vmax"]
     xs = np.arange(8)
     cosv = np.cos((2 * xs[:, None] + 1) * xs[None, :] * np.pi / 16) * np.where(xs == 0, np.sqrt(0.5), 1.0)
     planes = []
-    for ci, c in enumerate(comps):
-        blocks = (coef[ci] * qt[c["tq"]]).reshape(coef[ci].shape[:2] + (8, 8))
+    for c in comps:
+        blocks = (c["coef"] * qt[c["tq"]]).reshape(c["bh"], c["bw"], 8, 8).astype(np.float64)
         pix = np.einsum("xu,abvu,yv->abyx", cosv, blocks, cosv) * 0.25
         pix = np.clip(np.floor(pix + 128.5), 0, 255)
-        plane = pix.transpose(0, 2, 1, 3).reshape(blocks.shape[0] * 8, blocks.shape[1] * 8)
+        plane = pix.transpose(0, 2, 1, 3).reshape(c["bh"] * 8, c["bw"] * 8)
         ys = np.arange(height) * c["v"] // vmax
         xs_ = np.arange(width) * c["h"] // hmax
         planes.append(plane[ys][:, xs_])

@@ -5,8 +5,10 @@ every colour type and all five row filters written here with zlib, PAM, TGA
 (grey / BGR / BGRA, raw and run-length encoded, either row order) and BMP
 (24-bit padded rows, 32-bit, bit fields, either row order), and baseline
 JPEG (grey and YCbCr at 4:4:4 / 4:2:2 / 4:4:0 / 4:2:0, restart intervals,
-8- and 16-bit quantisation tables) written here with scipy's orthonormal DCT
-and Huffman tables built from the data, plus a third-party JPEG where one is
+8- and 16-bit quantisation tables; baseline with one interleaved scan or one
+scan per component, and progressive with spectral selection, successive
+approximation and EOB runs) written here with scipy's orthonormal DCT and
+Huffman tables built from the data, plus a third-party JPEG where one is
 installed.
 GPU tests run the full encode and compare the written .astc with the
 library's blocks for the flipped image, and the reference's own leaf.astc.
@@ -246,9 +248,9 @@ def _huffman_table(freq):
     return codes, bytes(counts) + bytes(s for s in order if s != 256)
 
 
-def _jpeg(path, img, sampling=(1, 1), restart=0, q16=False):
-    """Writes a baseline JPEG of img ((H, W) grey or (H, W, 3) RGB) and returns
-    the decoded image a conforming decoder gives (float64, rounded), as RGBA."""
+def _jpeg_coefs(img, sampling=(1, 1)):
+    """Quantised DCT coefficients of img ((H, W) grey or (H, W, 3) RGB) and the
+    decoded image a conforming decoder gives (float64, rounded), as RGBA."""
     from scipy.fft import dctn, idctn
     h, w = img.shape[:2]
     x = img.astype(np.float64)
@@ -273,7 +275,7 @@ def _jpeg(path, img, sampling=(1, 1), restart=0, q16=False):
         bl = (sub - 128.0).reshape(sub.shape[0] // 8, 8, sub.shape[1] // 8, 8).transpose(0, 2, 1, 3)
         q = qts[min(ci, 1)]
         c = np.rint(dctn(bl, axes=(2, 3), norm="ortho") / q).astype(np.int64)
-        coefs.append(c)
+        coefs.append(c.reshape(c.shape[0], c.shape[1], 64))
         pix = np.clip(np.floor(idctn(c * q, axes=(2, 3), norm="ortho") + 128.5), 0, 255)
         plane = pix.transpose(0, 2, 1, 3).reshape(sub.shape)
         recon.append(plane[np.arange(h) * sv // vmax][:, np.arange(w) * sh // hmax])
@@ -284,78 +286,221 @@ def _jpeg(path, img, sampling=(1, 1), restart=0, q16=False):
         yy, cb, cr = recon[0], recon[1] - 128.0, recon[2] - 128.0
         rgb = np.stack([yy + 1.402 * cr, yy - 0.344136 * cb - 0.714136 * cr, yy + 1.772 * cb], -1)
         want[..., :3] = np.clip(np.floor(rgb + 0.5), 0, 255)
+    cbw = [(-(-w * sh // hmax) + 7) // 8 for sh, _ in samp]
+    cbh = [(-(-h * sv // vmax) + 7) // 8 for _, sv in samp]
+    return dict(h=h, w=w, samp=samp, coefs=coefs, qts=qts, want=want, mcux=mcux, mcuy=mcuy, cbw=cbw, cbh=cbh)
 
-    def cat(v):
-        return 0 if v == 0 else abs(int(v)).bit_length()
 
-    def extra(v, t):
-        return v if v >= 0 else v + (1 << t) - 1
+def _cat(v):
+    return 0 if v == 0 else abs(int(v)).bit_length()
 
-    # symbol streams, in MCU order: (table, symbol, extra bits, extra length)
-    segs, stream, pred = [], [], [0] * len(planes)
-    for n in range(mcux * mcuy):
-        if restart and n and n % restart == 0:
-            segs.append(stream)
-            stream, pred = [], [0] * len(planes)
-        my, mx = divmod(n, mcux)
-        for ci, (sh, sv) in enumerate(samp):
-            t = min(ci, 1)
+
+def _extra(v, t):
+    return v if v >= 0 else v + (1 << t) - 1
+
+
+class _ScanEvents:
+    """The symbols and raw bits of one scan, in stream order: ('s', table, symbol),
+    ('b', value, nbits) or ('rst',)."""
+
+    def __init__(self):
+        self.ev, self.eobrun, self.be = [], 0, []
+
+    def sym(self, tab, v):
+        self.ev.append(("s", tab, v))
+
+    def bits(self, v, n):
+        if n:
+            self.ev.append(("b", v, n))
+
+    def flush_eobrun(self, tab):
+        if self.eobrun:
+            nb = self.eobrun.bit_length() - 1
+            self.sym(tab, nb << 4)
+            self.bits(self.eobrun - (1 << nb), nb)
+            for bit in self.be:
+                self.bits(bit, 1)
+            self.eobrun, self.be = 0, []
+
+
+def _scan_events(J, comps, ss, se, ah, al, progressive, restart):
+    """One scan over `comps` (indices) in the decoder's block order."""
+    sc = _ScanEvents()
+    single = len(comps) == 1
+    units = J["cbw"][comps[0]] * J["cbh"][comps[0]] if single else J["mcux"] * J["mcuy"]
+    pred = {ci: 0 for ci in comps}
+    act = ("ac", min(comps[0], 1))
+
+    def blocks(u):
+        for ci in comps:
+            if single:
+                yield ci, J["coefs"][ci][u // J["cbw"][ci], u % J["cbw"][ci]]
+                continue
+            sh, sv = J["samp"][ci]
+            my, mx = divmod(u, J["mcux"])
             for by in range(sv):
                 for bx in range(sh):
-                    zz = coefs[ci][my * sv + by, mx * sh + bx].reshape(64)[ZIGZAG]
-                    diff = int(zz[0]) - pred[ci]
-                    pred[ci] = int(zz[0])
-                    stream.append(((0, t), cat(diff), extra(diff, cat(diff)), cat(diff)))
-                    run, last = 0, max([k for k in range(1, 64) if zz[k]] or [0])
-                    for k in range(1, last + 1):
-                        if zz[k] == 0:
-                            run += 1
-                            continue
-                        while run > 15:
-                            stream.append(((1, t), 0xF0, 0, 0))
-                            run -= 16
-                        sz = cat(zz[k])
-                        stream.append(((1, t), (run << 4) | sz, extra(int(zz[k]), sz), sz))
-                        run = 0
-                    if last < 63:
-                        stream.append(((1, t), 0x00, 0, 0))
-    segs.append(stream)
-    freq = {}
-    for st in segs:
-        for key, sym, _, _ in st:
-            freq.setdefault(key, {}).setdefault(sym, 0)
-            freq[key][sym] += 1
-    tables = {key: _huffman_table(f) for key, f in freq.items()}
+                    yield ci, J["coefs"][ci][my * sv + by, mx * sh + bx]
+
+    for u in range(units):
+        if restart and u and u % restart == 0:
+            sc.flush_eobrun(act)
+            sc.ev.append(("rst",))
+            pred = {ci: 0 for ci in comps}
+        for ci, blk in blocks(u):
+            zz = [int(v) for v in blk[ZIGZAG]]
+            dct = ("dc", min(ci, 1))
+            if not progressive or ss == 0:
+                if ah == 0:                                   # DC (sequential or first)
+                    v = zz[0] >> al
+                    diff = v - pred[ci]
+                    pred[ci] = v
+                    sc.sym(dct, _cat(diff))
+                    sc.bits(_extra(diff, _cat(diff)), _cat(diff))
+                else:                                         # DC refinement
+                    sc.bits((zz[0] >> al) & 1, 1)
+                if progressive:
+                    continue
+                run, acti = 0, ("ac", min(ci, 1))
+                last = max([k for k in range(1, 64) if zz[k]] or [0])
+                for k in range(1, last + 1):
+                    if zz[k] == 0:
+                        run += 1
+                        continue
+                    while run > 15:
+                        sc.sym(acti, 0xF0)
+                        run -= 16
+                    sz = _cat(zz[k])
+                    sc.sym(acti, (run << 4) | sz)
+                    sc.bits(_extra(zz[k], sz), sz)
+                    run = 0
+                if last < 63:
+                    sc.sym(acti, 0x00)
+                continue
+            band = range(ss, se + 1)
+            if ah == 0:                                       # AC first: magnitudes >> al
+                vals = [(abs(zz[k]) >> al) * (1 if zz[k] >= 0 else -1) for k in band]
+                run = 0
+                for v in vals:
+                    if v == 0:
+                        run += 1
+                        continue
+                    sc.flush_eobrun(act)
+                    while run > 15:
+                        sc.sym(act, 0xF0)
+                        run -= 16
+                    sz = _cat(v)
+                    sc.sym(act, (run << 4) | sz)
+                    sc.bits(_extra(v, sz), sz)
+                    run = 0
+                if run:
+                    sc.eobrun += 1
+                    if sc.eobrun == 0x7FFF:
+                        sc.flush_eobrun(act)
+                continue
+            # AC refinement (T.81 G.1.2.3, figure G.7)
+            absv = [abs(zz[k]) >> al for k in band]
+            eob = max([i for i, a in enumerate(absv) if a == 1] or [-1])
+            run, br = 0, []
+            for i, a in enumerate(absv):
+                if a == 0:
+                    run += 1
+                    continue
+                while run > 15 and i <= eob:
+                    sc.flush_eobrun(act)
+                    sc.sym(act, 0xF0)
+                    run -= 16
+                    for bit in br:
+                        sc.bits(bit, 1)
+                    br = []
+                if a > 1:                                     # already nonzero: a correction bit
+                    br.append(a & 1)
+                    continue
+                sc.flush_eobrun(act)
+                sc.sym(act, (run << 4) | 1)
+                sc.bits(1 if zz[ss + i] > 0 else 0, 1)
+                for bit in br:
+                    sc.bits(bit, 1)
+                br, run = [], 0
+            if run or br:
+                sc.eobrun += 1
+                sc.be += br
+                if sc.eobrun == 0x7FFF:
+                    sc.flush_eobrun(act)
+    sc.flush_eobrun(act)
+    return sc.ev
+
+
+def _jpeg_write(path, J, mode="baseline", restart=0, q16=False):
+    """Writes the coefficients of _jpeg_coefs as a JPEG: 'baseline' (one
+    interleaved scan), 'baseline_split' (one scan per component) or
+    'progressive' (spectral selection and successive approximation, with
+    DC and AC refinement scans)."""
+    ncomp = len(J["coefs"])
+    if mode == "baseline":
+        script = [(list(range(ncomp)), 0, 63, 0, 0)]
+    elif mode == "baseline_split":
+        script = [([ci], 0, 63, 0, 0) for ci in range(ncomp)]
+    else:
+        allc = list(range(ncomp))
+        script = [(allc, 0, 0, 0, 1)]                                 # DC first, point transform 1
+        script += [([0], 1, 5, 0, 2), ([0], 6, 63, 0, 2)]              # luma AC bands, two bits dropped
+        script += [([ci], 1, 63, 0, 1) for ci in range(1, ncomp)]      # chroma AC, one bit dropped
+        script += [([0], 1, 63, 2, 1)]                                # luma AC refinement, bit 1
+        script += [(allc, 0, 0, 1, 0)]                                # DC refinement
+        script += [([ci], 1, 63, 1, 0) for ci in range(ncomp)]        # AC refinement, bit 0
+    progressive = mode == "progressive"
 
     def seg(marker, body):
         return b"\xff" + bytes([marker]) + struct.pack(">H", len(body) + 2) + body
     out = b"\xff\xd8" + seg(0xE0, b"JFIF\x00\x01\x01\x00\x00\x01\x00\x01\x00\x00")
     out += seg(0xFE, b"written by the test suite")
-    for t, q in enumerate(qts[:len(set(min(i, 1) for i in range(len(planes))))]):
+    for t, q in enumerate(J["qts"][:min(ncomp, 2)]):
         zq = q.reshape(64)[ZIGZAG]
         out += seg(0xDB, bytes([(16 if q16 else 0) | t]) +
                    (struct.pack(">64H", *zq) if q16 else bytes(zq.astype(np.uint8))))
-    out += seg(0xC0, struct.pack(">BHHB", 8, h, w, len(planes)) +
-               b"".join(bytes([ci + 1, (sh << 4) | sv, min(ci, 1)]) for ci, (sh, sv) in enumerate(samp)))
-    for (cls, t), (codes, spec) in sorted(tables.items()):
-        out += seg(0xC4, bytes([(cls << 4) | t]) + spec)
+    out += seg(0xC2 if progressive else 0xC0, struct.pack(">BHHB", 8, J["h"], J["w"], ncomp) +
+               b"".join(bytes([ci + 1, (sh << 4) | sv, min(ci, 1)]) for ci, (sh, sv) in enumerate(J["samp"])))
     if restart:
         out += seg(0xDD, struct.pack(">H", restart))
-    out += seg(0xDA, bytes([len(planes)]) +
-               b"".join(bytes([ci + 1, (min(ci, 1) << 4) | min(ci, 1)]) for ci in range(len(planes))) +
-               b"\x00\x3f\x00")
-    for i, st in enumerate(segs):
-        bitstr = "".join(format(tables[key][0][sym][0], "0%db" % tables[key][0][sym][1]) +
-                         (format(ev, "0%db" % el) if el else "") for key, sym, ev, el in st)
-        bitstr += "1" * (-len(bitstr) % 8)
-        data = int(bitstr, 2).to_bytes(len(bitstr) // 8, "big") if bitstr else b""
-        out += data.replace(b"\xff", b"\xff\x00")
-        if i + 1 < len(segs):
-            out += bytes([0xFF, 0xD0 + i % 8])
+    for comps, ss, se, ah, al in script:
+        ev = _scan_events(J, comps, ss, se, ah, al, progressive, restart)
+        freq = {}
+        for e in ev:
+            if e[0] == "s":
+                freq.setdefault(e[1], {}).setdefault(e[2], 0)
+                freq[e[1]][e[2]] += 1
+        tables = {key: _huffman_table(f) for key, f in freq.items()}
+        for (cls, t), (codes, spec) in sorted(tables.items()):
+            out += seg(0xC4, bytes([(1 if cls == "ac" else 0) << 4 | t]) + spec)
+        out += seg(0xDA, bytes([len(comps)]) + b"".join(bytes([ci + 1, (min(ci, 1) << 4) | min(ci, 1)])
+                                                         for ci in comps) + bytes([ss, se, (ah << 4) | al]))
+        parts, cur, nrst = [], [], 0
+        for e in ev + [("rst",)]:
+            if e[0] == "rst":
+                bitstr = "".join(cur)
+                bitstr += "1" * (-len(bitstr) % 8)
+                parts.append(int(bitstr, 2).to_bytes(len(bitstr) // 8, "big") if bitstr else b"")
+                cur = []
+            elif e[0] == "s":
+                code, n = tables[e[1]][0][e[2]]
+                cur.append(format(code, "0%db" % n))
+            else:
+                cur.append(format(e[1], "0%db" % e[2]))
+        for i, data in enumerate(parts):
+            out += data.replace(b"\xff", b"\xff\x00")
+            if i + 1 < len(parts):
+                out += bytes([0xFF, 0xD0 + i % 8])
     out += b"\xff\xd9"
     with open(path, "wb") as fh:
         fh.write(out)
-    return want
+
+
+def _jpeg(path, img, sampling=(1, 1), restart=0, q16=False, mode="baseline"):
+    """Writes img as a JPEG and returns what a conforming decoder gives."""
+    J = _jpeg_coefs(img, sampling)
+    _jpeg_write(path, J, mode=mode, restart=restart, q16=q16)
+    return J["want"]
 
 
 def _smooth(h, w, channels, seed):
@@ -419,16 +564,56 @@ def test_cli_reads_third_party_jpeg(native, tmp_path):
     assert dx.mean() < 0.3 * got[..., :3].std() and edges < 1.15 * inner
 
 
-def test_cli_refuses_progressive_jpeg(native, tmp_path):
+@pytest.mark.parametrize("kind,sampling,restart,mode", [
+    ("rgb", (2, 2), 0, "progressive"), ("rgb", (1, 1), 0, "progressive"), ("rgb", (2, 1), 3, "progressive"),
+    ("grey", (1, 1), 4, "progressive"), ("rgb", (1, 2), 1, "progressive"), ("rgb", (2, 2), 2, "baseline_split"),
+    ("rgb", (1, 1), 0, "baseline_split")])
+def test_cli_reads_progressive_and_single_component_scans(native, tmp_path, kind, sampling, restart, mode):
+    """The same coefficients written as one interleaved baseline scan and as
+    `mode` (progressive: DC and AC first scans with point transforms, band
+    splits, AC and DC refinement scans, EOB runs; or one baseline scan per
+    component) decode to the same pixels."""
+    img = _smooth(45, 38, 1 if kind == "grey" else 3, seed=7 + restart + sampling[0])
+    J = _jpeg_coefs(img, sampling)
+    base, other = str(tmp_path / "base.jpg"), str(tmp_path / "other.jpg")
+    _jpeg_write(base, J, mode="baseline")
+    _jpeg_write(other, J, mode=mode, restart=restart)
+    got_base = _dump(native, base, tmp_path)
+    got = _dump(native, other, tmp_path)
+    assert np.array_equal(got, got_base)
+    assert np.abs(got[::-1].astype(int) - J["want"]).max() <= 1
+    from astc_encoder_gb300 import image_io                 # the Python reader agrees
+    assert np.array_equal(image_io.load_image(other), image_io.load_image(base))
+
+
+@pytest.mark.parametrize("restart", [0, 7])
+def test_cli_reads_progressive_long_eob_runs(native, tmp_path, restart):
+    """A smooth image: whole AC bands are zero, so EOB runs span the scan
+    (run-length symbols up to 2^8 with appended bits)."""
+    yy, xx = np.mgrid[0:160, 0:192].astype(np.float64)
+    img = np.clip(np.rint(np.stack([40 + xx * 0.5, 60 + yy * 0.4, 200 - xx * 0.3], -1)), 0, 255).astype(np.uint8)
+    img[40:56, 64:96] = [250, 20, 20]
+    J = _jpeg_coefs(img, (2, 2))
+    base, prog = str(tmp_path / "base.jpg"), str(tmp_path / "prog.jpg")
+    _jpeg_write(base, J, mode="baseline")
+    _jpeg_write(prog, J, mode="progressive", restart=restart)
+    assert np.array_equal(_dump(native, prog, tmp_path), _dump(native, base, tmp_path))
+    from astc_encoder_gb300 import image_io
+    assert np.array_equal(image_io.load_image(prog), image_io.load_image(base))
+
+
+def test_cli_refuses_unsupported_jpeg(native, tmp_path):
     path = str(tmp_path / "in.jpg")
     _jpeg(path, _smooth(16, 16, 3, 0))
-    data = open(path, "rb").read().replace(b"\xff\xc0", b"\xff\xc2", 1)
-    open(path, "wb").write(data)
-    r = subprocess.run([CLI, path, "--dump-rgba", str(tmp_path / "o.pam")], capture_output=True, text=True)
-    assert r.returncode != 0 and "progressive" in r.stdout
+    good = open(path, "rb").read()
     from astc_encoder_gb300 import image_io
-    with pytest.raises(ValueError, match="progressive"):
-        image_io.load_image(path)
+    # a progressive frame whose scan carries sequential parameters; an arithmetic-coded frame
+    for marker, msg in ((b"\xff\xc2", "bad JPEG scan parameters"), (b"\xff\xc9", "arithmetic")):
+        open(path, "wb").write(good.replace(b"\xff\xc0", marker, 1))
+        r = subprocess.run([CLI, path, "--dump-rgba", str(tmp_path / "o.pam")], capture_output=True, text=True)
+        assert r.returncode != 0 and msg in r.stdout
+        with pytest.raises(ValueError, match=msg):
+            image_io.load_image(path)
 
 
 @pytest.mark.parametrize("fmt", ["png", "jpg", "bmp", "tga", "pam"])
@@ -493,7 +678,9 @@ def test_image_reader_under_sanitizers(tmp_path):
     for name, write in [("a.png", lambda p: _png(p, rgba, 6)), ("b.png", lambda p: _png(p, arr[..., 0], 3,
                                                                                          palette=np.arange(768) % 256)),
                         ("c.jpg", lambda p: _jpeg(p, arr, sampling=(2, 2), restart=2)),
-                        ("d.jpg", lambda p: _jpeg(p, arr[..., 0])), ("e.bmp", lambda p: _bmp(p, rgba, bitfields=True)),
+                        ("d.jpg", lambda p: _jpeg(p, arr[..., 0])),
+                        ("j.jpg", lambda p: _jpeg(p, arr, sampling=(2, 1), restart=3, mode="progressive")),
+                        ("e.bmp", lambda p: _bmp(p, rgba, bitfields=True)),
                         ("f.bmp", lambda p: _bmp(p, arr)), ("g.tga", lambda p: _tga(p, rgba, rle=True)),
                         ("h.tga", lambda p: _tga(p, arr[..., 0], rle=True))]:
         path = str(tmp_path / name)
