@@ -1,5 +1,5 @@
-// image_load.cpp -- PNG / JPEG / Netpbm / BMP / TGA reader for the command
-// line tool.
+// image_load.cpp -- PNG / JPEG / PSD / Netpbm / BMP / TGA reader for the
+// command line tool.
 // Inflate follows RFC 1951 (stored, fixed and dynamic Huffman blocks,
 // canonical codes decoded one bit at a time); the zlib wrapper RFC 1950;
 // PNG chunk layout, filters 0-4 and colour types the PNG specification.
@@ -18,7 +18,10 @@ namespace {
 // Images up to 2^30 texels (4 GiB of RGBA8); larger or empty headers are refused
 // before anything is allocated.
 bool dims_ok(long long w, long long h, std::string& err) {
-    if (w <= 0 || h <= 0 || w * h > (1ll << 30)) { err = "bad image size"; return false; }
+    if (w <= 0 || h <= 0 || w > (1ll << 30) || h > (1ll << 30) || w * h > (1ll << 30)) {
+        err = "bad image size";
+        return false;
+    }
     return true;
 }
 
@@ -898,6 +901,92 @@ bool decode_jpeg(const uint8_t* d, size_t n, Image& img, std::string& err) {
     return true;
 }
 
+// Photoshop PSD (version 1), the merged image that follows the layer section:
+// greyscale or RGB colour mode, 8 or 16 bits per channel (16-bit channels keep
+// their high byte), grey(+alpha) or RGB(+alpha) from the first channels (extra
+// channels ignored), raw or PackBits run-length planes.  Photoshop mattes the
+// merged image's partly transparent pixels against white (c = a x + (1 - a)
+// 255); the matte is removed, x = 255 (c - 255 + A) / A for alpha A in 1..254,
+// rounded and clamped.
+bool decode_psd(const uint8_t* d, size_t n, Image& img, std::string& err) {
+    auto be16 = [&](size_t o) { return (uint32_t)((d[o] << 8) | d[o + 1]); };
+    auto be32 = [&](size_t o) { return (be16(o) << 16) | be16(o + 2); };
+    if (n < 26 || memcmp(d, "8BPS", 4) != 0) { err = "not a PSD file"; return false; }
+    if (be16(4) != 1) { err = "only version-1 PSD is read"; return false; }
+    const int channels = (int)be16(12), depth = (int)be16(22), mode = (int)be16(24);
+    const uint32_t h = be32(14), w = be32(18);
+    if (mode != 1 && mode != 3) { err = "PSD colour mode not read (greyscale and RGB are)"; return false; }
+    if (depth != 8 && depth != 16) { err = "only 8- and 16-bit PSD is read"; return false; }
+    if (channels < 1 || channels > 56) { err = "bad PSD channel count"; return false; }
+    if (!dims_ok(w, h, err)) return false;
+    size_t pos = 26;
+    for (int sec = 0; sec < 3; ++sec) {                   // colour mode data, resources, layers
+        if (pos + 4 > n) { err = "PSD truncated"; return false; }
+        pos += 4 + (size_t)be32(pos);
+    }
+    if (pos + 2 > n) { err = "PSD truncated"; return false; }
+    const uint32_t comp = be16(pos);
+    pos += 2;
+    const int bps = depth / 8, used = std::min(channels, mode == 3 ? 4 : 2);
+    const size_t row = (size_t)w * bps, plane = row * h;
+    std::vector<std::vector<uint8_t>> ch(used, std::vector<uint8_t>((size_t)w * h));
+    if (comp == 0) {
+        if (pos + plane * used > n) { err = "PSD data too short"; return false; }
+        for (int c = 0; c < used; ++c)
+            for (size_t i = 0; i < (size_t)w * h; ++i) ch[c][i] = d[pos + c * plane + i * bps];
+    } else if (comp == 1) {
+        const size_t counts = pos, rows = (size_t)channels * h;
+        size_t p = pos + 2 * rows;
+        if (p > n) { err = "PSD data too short"; return false; }
+        std::vector<uint8_t> line(row);
+        for (int c = 0; c < used; ++c)
+            for (uint32_t y = 0; y < h; ++y) {
+                const size_t len = be16(counts + 2 * ((size_t)c * h + y)), stop = p + len;
+                if (stop > n) { err = "PSD data too short"; return false; }
+                size_t o = 0;
+                while (p < stop && o < row) {                 // PackBits
+                    const int k = (int8_t)d[p++];
+                    if (k >= 0) {
+                        const size_t cnt = (size_t)k + 1;
+                        if (p + cnt > stop || o + cnt > row) { err = "bad PSD run"; return false; }
+                        memcpy(line.data() + o, d + p, cnt);
+                        p += cnt;
+                        o += cnt;
+                    } else if (k != -128) {
+                        const size_t cnt = (size_t)(1 - k);
+                        if (p >= stop || o + cnt > row) { err = "bad PSD run"; return false; }
+                        memset(line.data() + o, d[p++], cnt);
+                        o += cnt;
+                    }
+                }
+                if (o != row) { err = "bad PSD run"; return false; }
+                p = stop;
+                for (uint32_t x = 0; x < w; ++x) ch[c][(size_t)y * w + x] = line[(size_t)x * bps];
+            }
+    } else {
+        err = "PSD compression not read (raw and run-length are)";
+        return false;
+    }
+    img.width = (int)w;
+    img.height = (int)h;
+    img.rgba.assign((size_t)w * h * 4, 255);
+    const bool has_alpha = used == (mode == 3 ? 4 : 2);
+    const int nc = mode == 3 ? std::min(used, 3) : 1;
+    for (size_t i = 0; i < (size_t)w * h; ++i) {
+        uint8_t* o = img.rgba.data() + i * 4;
+        for (int c = 0; c < 3; ++c) o[c] = mode == 3 ? (c < nc ? ch[c][i] : 0) : ch[0][i];
+        if (!has_alpha) continue;
+        const int a = ch[used - 1][i];
+        o[3] = (uint8_t)a;
+        if (a == 0 || a == 255) continue;
+        for (int c = 0; c < 3; ++c) {
+            const int v = 255 * ((int)o[c] - 255 + a);
+            o[c] = (uint8_t)(v <= 0 ? 0 : std::min(255, (v + a / 2) / a));
+        }
+    }
+    return true;
+}
+
 bool load_image(const std::string& path, Image& img, std::string& err) {
     FILE* f = fopen(path.c_str(), "rb");
     if (!f) { err = "cannot open " + path; return false; }
@@ -912,11 +1001,12 @@ bool load_image(const std::string& path, Image& img, std::string& err) {
     if (data.size() >= 2 && data[0] == 'B' && data[1] == 'M') return decode_bmp(data.data(), data.size(), img, err);
     if (data.size() >= 3 && data[0] == 0xFF && data[1] == 0xD8 && data[2] == 0xFF)
         return decode_jpeg(data.data(), data.size(), img, err);
+    if (data.size() >= 4 && memcmp(data.data(), "8BPS", 4) == 0) return decode_psd(data.data(), data.size(), img, err);
     const size_t dot = path.find_last_of('.');
     std::string ext = dot == std::string::npos ? "" : path.substr(dot + 1);
     for (auto& c : ext) c = (char)tolower((unsigned char)c);
     if (ext == "tga") return decode_tga(data.data(), data.size(), img, err);   // TGA has no magic number
-    err = "unsupported image format (PNG, JPEG, PAM/PPM/PGM, BMP and TGA are read)";
+    err = "unsupported image format (PNG, JPEG, PSD, PAM/PPM/PGM, BMP and TGA are read)";
     return false;
 }
 

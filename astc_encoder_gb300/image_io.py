@@ -1,12 +1,13 @@
-"""Image loading for the encoder's command line (PNG, JPEG, PAM/PPM/PGM, BMP, TGA).
+"""Image loading for the encoder's command line (PNG, JPEG, PSD, PAM/PPM/PGM, BMP, TGA).
 
 The reference loads images with stb_image forced to RGBA and flipped
 vertically (main.cpp:24-25).  This module is a small self-contained reader:
 PNG (8-bit greyscale / grey+alpha / RGB / RGBA / palette, non-interlaced,
 all five row filters, zlib from the Python standard library), Netpbm
 P5/P6/P7, Windows BMP (24/32-bit, uncompressed or bit fields), Truevision
-TGA (8-bit grey, 24/32-bit true colour, raw or run-length encoded) and
-JPEG (8-bit grey or YCbCr, Huffman coded, baseline or progressive) -- the
+TGA (8-bit grey, 24/32-bit true colour, raw or run-length encoded),
+JPEG (8-bit grey or YCbCr, Huffman coded, baseline or progressive) and
+Photoshop PSD (the merged image; 8/16-bit grey or RGB, optional alpha) -- the
 same formats as the C++ reader of the command line tool.  It always returns
 a (H, W, 4) uint8 array, row 0 first; the caller flips when it wants the
 reference's orientation.
@@ -553,6 +554,77 @@ def _jpeg_image(frame, comps, qt):
     return out
 
 
+def load_psd(path: str) -> np.ndarray:
+    """Photoshop PSD (version 1), the merged image: greyscale or RGB, 8 or 16
+    bits per channel (high byte kept), optional alpha, raw or PackBits; the
+    white matte of partly transparent pixels removed (as the command line
+    tool's reader)."""
+    with open(path, "rb") as fh:
+        d = fh.read()
+    if len(d) < 26 or d[:4] != b"8BPS":
+        raise ValueError("not a PSD file")
+    version, channels, h, w, depth, mode = struct.unpack_from(">H6xHIIHH", d, 4)
+    if version != 1:
+        raise ValueError("only version-1 PSD is read")
+    if mode not in (1, 3):
+        raise ValueError("PSD colour mode not read (greyscale and RGB are)")
+    if depth not in (8, 16):
+        raise ValueError("only 8- and 16-bit PSD is read")
+    if not (0 < w <= 1 << 30 and 0 < h <= 1 << 30 and w * h <= 1 << 30):
+        raise ValueError("bad image size")
+    pos = 26
+    for _ in range(3):
+        pos += 4 + struct.unpack_from(">I", d, pos)[0]
+    comp = struct.unpack_from(">H", d, pos)[0]
+    pos += 2
+    bps, used = depth // 8, min(channels, 4 if mode == 3 else 2)
+    row = w * bps
+    chans = []
+    if comp == 0:
+        for c in range(used):
+            raw = np.frombuffer(d, np.uint8, row * h, pos + c * row * h)
+            chans.append(raw.reshape(h, w, bps)[..., 0])
+    elif comp == 1:
+        counts = struct.unpack_from(">%dH" % (channels * h), d, pos)
+        p = pos + 2 * channels * h
+        for c in range(used):
+            plane = np.zeros((h, row), np.uint8)
+            for y in range(h):
+                stop, line, q = p + counts[c * h + y], bytearray(), p
+                while q < stop and len(line) < row:
+                    k = d[q] - 256 if d[q] > 127 else d[q]
+                    q += 1
+                    if k >= 0:
+                        line += d[q:q + k + 1]
+                        q += k + 1
+                    elif k != -128:
+                        line += bytes([d[q]]) * (1 - k)
+                        q += 1
+                if len(line) != row:
+                    raise ValueError("bad PSD run")
+                plane[y] = np.frombuffer(bytes(line), np.uint8)
+                p = stop
+            chans.append(plane.reshape(h, w, bps)[..., 0])
+    else:
+        raise ValueError("PSD compression not read (raw and run-length are)")
+    out = np.full((h, w, 4), 255, np.uint8)
+    if mode == 3:
+        for c in range(min(used, 3)):
+            out[..., c] = chans[c]
+        if used < 3:
+            out[..., used:3] = 0
+    else:
+        out[..., :3] = chans[0][..., None]
+    if used == (4 if mode == 3 else 2):
+        a = chans[-1].astype(np.int64)
+        out[..., 3] = a
+        part = (a > 0) & (a < 255)
+        v = 255 * (out[..., :3].astype(np.int64) - 255 + a[..., None])
+        x = np.where(v <= 0, 0, np.minimum(255, (v + a[..., None] // 2) // np.maximum(a[..., None], 1)))
+        out[..., :3] = np.where(part[..., None], x, out[..., :3])
+    return out
+
+
 def load_image(path: str) -> np.ndarray:
     with open(path, "rb") as fh:
         head = fh.read(8)
@@ -564,6 +636,8 @@ def load_image(path: str) -> np.ndarray:
         return load_bmp(path)
     if head[:3] == b"\xff\xd8\xff":
         return load_jpeg(path)
+    if head[:4] == b"8BPS":
+        return load_psd(path)
     if path.lower().endswith(".tga"):                  # TGA has no magic number
         return load_tga(path)
-    raise ValueError("unsupported image format (PNG, JPEG, PAM/PPM/PGM, BMP and TGA are read)")
+    raise ValueError("unsupported image format (PNG, JPEG, PSD, PAM/PPM/PGM, BMP and TGA are read)")

@@ -9,7 +9,8 @@ JPEG (grey and YCbCr at 4:4:4 / 4:2:2 / 4:4:0 / 4:2:0, restart intervals,
 scan per component, and progressive with spectral selection, successive
 approximation and EOB runs) written here with scipy's orthonormal DCT and
 Huffman tables built from the data, plus a third-party JPEG where one is
-installed.
+installed, and PSD merged images (grey / RGB, alpha, 8 / 16 bits, raw and
+PackBits, extra channels).
 GPU tests run the full encode and compare the written .astc with the
 library's blocks for the flipped image, and the reference's own leaf.astc.
 """
@@ -680,6 +681,8 @@ def test_image_reader_under_sanitizers(tmp_path):
                         ("c.jpg", lambda p: _jpeg(p, arr, sampling=(2, 2), restart=2)),
                         ("d.jpg", lambda p: _jpeg(p, arr[..., 0])),
                         ("j.jpg", lambda p: _jpeg(p, arr, sampling=(2, 1), restart=3, mode="progressive")),
+                        ("k.psd", lambda p: _psd(p, rgba.transpose(2, 0, 1).copy(), 3, 16, True, 1)),
+                        ("l.psd", lambda p: _psd(p, rgba[..., :2].transpose(2, 0, 1).copy(), 1, 8, False)),
                         ("e.bmp", lambda p: _bmp(p, rgba, bitfields=True)),
                         ("f.bmp", lambda p: _bmp(p, arr)), ("g.tga", lambda p: _tga(p, rgba, rle=True)),
                         ("h.tga", lambda p: _tga(p, arr[..., 0], rle=True))]:
@@ -717,6 +720,88 @@ def test_image_reader_under_sanitizers(tmp_path):
             files.append(path)
         r = subprocess.run([exe] + files, capture_output=True, text=True, timeout=300)
         assert r.returncode == 0, r.stderr[-2000:]
+
+
+def _packbits(row):
+    """PackBits: runs of 3+ equal bytes as repeats, the rest as literals."""
+    out, i = bytearray(), 0
+    while i < len(row):
+        j = i
+        while j + 1 < len(row) and row[j + 1] == row[i] and j - i < 127:
+            j += 1
+        if j - i >= 2:
+            out += bytes([257 - (j - i + 1)]) + bytes([row[i]])
+            i = j + 1
+            continue
+        k = i
+        while k < len(row) and k - i < 128 and not (k + 2 < len(row) and row[k] == row[k + 1] == row[k + 2]):
+            k += 1
+        out += bytes([k - i - 1]) + bytes(row[i:k])
+        i = k
+    return bytes(out)
+
+
+def _psd(path, planes, mode, depth=8, rle=False, extra=0):
+    """Writes a PSD whose merged image holds `planes` ((C, H, W) uint8 values,
+    written as the high byte of 16-bit channels when depth is 16) plus
+    `extra` unused channels."""
+    c, h, w = planes.shape
+    chans = list(planes) + [np.full((h, w), 77, np.uint8)] * extra
+    data = []
+    for p in chans:
+        px = p if depth == 8 else np.stack([p, (p * 7) & 255], -1).reshape(h, w * 2)   # low bytes are noise
+        data.append(px.reshape(h, -1))
+    head = b"8BPS" + struct.pack(">H6xHIIHH", 1, len(chans), h, w, depth, mode)
+    body = struct.pack(">I", 0) + struct.pack(">I", 4) + b"\x00\x01\x02\x03" + struct.pack(">I", 0)
+    if not rle:
+        img = struct.pack(">H", 0) + b"".join(p.astype(np.uint8).tobytes() for p in data)
+    else:
+        rows = [_packbits(bytes(r.astype(np.uint8))) for p in data for r in p]
+        img = struct.pack(">H", 1) + struct.pack(">%dH" % len(rows), *[len(r) for r in rows]) + b"".join(rows)
+    with open(path, "wb") as fh:
+        fh.write(head + body + img)
+
+
+@pytest.mark.parametrize("mode,nch,extra", [(3, 3, 0), (3, 4, 0), (3, 4, 2), (1, 1, 0), (1, 2, 1)])
+@pytest.mark.parametrize("depth", [8, 16])
+@pytest.mark.parametrize("rle", [False, True])
+def test_cli_reads_psd(native, tmp_path, mode, nch, extra, depth, rle):
+    rng = np.random.default_rng(nch * 10 + depth + rle)
+    h, w = 23, 31
+    color = rng.integers(0, 256, (nch, h, w), dtype=np.uint8)
+    color[:, 5:12, 3:20] = color[:, 5, 3][:, None, None]                # runs for PackBits
+    has_alpha = nch == (4 if mode == 3 else 2)
+    planes = color.copy()
+    if has_alpha:
+        a = color[-1].astype(np.int64)
+        a[0] = 0
+        a[1] = 255
+        planes[-1] = a
+        # the merged image is matted against white: c = a x + (1 - a) 255
+        x = color[:-1].astype(np.int64)
+        planes[:-1] = np.clip(np.rint((a * x + (255 - a) * 255) / 255.0), 0, 255)
+    path = str(tmp_path / "in.psd")
+    _psd(path, planes, mode, depth, rle, extra)
+    got = _dump(native, path, tmp_path)[::-1]
+    want = np.full((h, w, 4), 255, np.uint8)
+    if mode == 3:
+        want[..., :3] = planes[:3].transpose(1, 2, 0)
+    else:
+        want[..., :3] = planes[0][..., None]
+    if has_alpha:
+        a = planes[-1].astype(np.int64)
+        want[..., 3] = a
+        part = (a > 0) & (a < 255)
+        v = 255 * (want[..., :3].astype(np.int64) - 255 + a[..., None])
+        x = np.where(v <= 0, 0, np.minimum(255, (v + a[..., None] // 2) // np.maximum(a[..., None], 1)))
+        want[..., :3] = np.where(part[..., None], x, want[..., :3])
+        # the un-matted colour is the original within the matte's rounding
+        orig = color[:-1].transpose(1, 2, 0).astype(int) if mode == 3 else color[0][..., None].astype(int)
+        sel = part & (a >= 32)
+        assert np.abs(want[..., :3].astype(int) - orig)[sel].max() <= 5
+    assert np.array_equal(got, want)
+    from astc_encoder_gb300 import image_io                 # the Python reader agrees
+    assert np.array_equal(image_io.load_image(path), want)
 
 
 def test_cli_rejects_unknown_format(native, tmp_path):
