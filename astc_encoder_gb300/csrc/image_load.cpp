@@ -1,5 +1,5 @@
-// image_load.cpp -- PNG / JPEG / PSD / Netpbm / BMP / TGA reader for the
-// command line tool.
+// image_load.cpp -- PNG / JPEG / PSD / GIF / Netpbm / BMP / TGA reader for
+// the command line tool.
 // Inflate follows RFC 1951 (stored, fixed and dynamic Huffman blocks,
 // canonical codes decoded one bit at a time); the zlib wrapper RFC 1950;
 // PNG chunk layout, filters 0-4 and colour types the PNG specification.
@@ -987,6 +987,144 @@ bool decode_psd(const uint8_t* d, size_t n, Image& img, std::string& err) {
     return true;
 }
 
+// GIF (87a / 89a), the first image: composed on the logical screen, which
+// starts as transparent black (0, 0, 0, 0); global or local palette; the
+// graphic control extension's transparent index leaves its pixels at the
+// screen's (0, 0, 0, 0); interlaced rows in the format's four passes; LZW with
+// variable code width up to 12 bits, clear and end codes.
+bool decode_gif(const uint8_t* d, size_t n, Image& img, std::string& err) {
+    auto le16 = [&](size_t o) { return (int)(d[o] | (d[o + 1] << 8)); };
+    if (n < 13 || memcmp(d, "GIF8", 4) != 0 || (d[4] != '7' && d[4] != '9') || d[5] != 'a') {
+        err = "not a GIF file";
+        return false;
+    }
+    const int sw = le16(6), sh = le16(8), flags = d[10];
+    if (!dims_ok(sw, sh, err)) return false;
+    size_t pos = 13;
+    uint8_t gpal[768] = {}, lpal[768] = {};
+    int gsize = 0, transparent = -1;
+    if (flags & 0x80) {
+        gsize = 2 << (flags & 7);
+        if (pos + 3 * (size_t)gsize > n) { err = "GIF truncated"; return false; }
+        memcpy(gpal, d + pos, 3 * (size_t)gsize);
+        pos += 3 * (size_t)gsize;
+    }
+    while (pos < n) {
+        const int b = d[pos++];
+        if (b == 0x3B) break;                                   // trailer
+        if (b == 0x21) {                                        // extension
+            if (pos >= n) break;
+            const int label = d[pos++];
+            bool first = true;
+            while (pos < n && d[pos] != 0) {
+                const size_t len = d[pos];
+                if (pos + 1 + len > n) { err = "GIF truncated"; return false; }
+                if (label == 0xF9 && first && len >= 4) transparent = (d[pos + 1] & 1) ? d[pos + 4] : -1;
+                first = false;
+                pos += 1 + len;
+            }
+            ++pos;
+            continue;
+        }
+        if (b != 0x2C) { err = "bad GIF block"; return false; }
+        if (pos + 9 > n) { err = "GIF truncated"; return false; }
+        const int fx = le16(pos), fy = le16(pos + 2), fw = le16(pos + 4), fh = le16(pos + 6), ff = d[pos + 8];
+        pos += 9;
+        const uint8_t* pal = gpal;
+        int psize = gsize;
+        if (ff & 0x80) {
+            psize = 2 << (ff & 7);
+            if (pos + 3 * (size_t)psize > n) { err = "GIF truncated"; return false; }
+            memcpy(lpal, d + pos, 3 * (size_t)psize);
+            pos += 3 * (size_t)psize;
+            pal = lpal;
+        }
+        if (pos >= n) { err = "GIF truncated"; return false; }
+        const int minsize = d[pos++];
+        if (minsize < 2 || minsize > 11) { err = "bad GIF code size"; return false; }
+        std::vector<uint8_t> data;                               // the sub-blocks, joined
+        while (pos < n && d[pos] != 0) {
+            const size_t len = d[pos];
+            if (pos + 1 + len > n) { err = "GIF truncated"; return false; }
+            data.insert(data.end(), d + pos + 1, d + pos + 1 + len);
+            pos += 1 + len;
+        }
+        // LZW: prefix / suffix tables, strings written backwards into a stack
+        const size_t npix = (size_t)fw * fh;
+        std::vector<uint8_t> idx;
+        idx.reserve(npix);
+        const int clear = 1 << minsize, stop = clear + 1;
+        std::vector<int> prefix(4096, -1);
+        std::vector<uint8_t> suffix(4096, 0), stack(4097);
+        for (int i = 0; i < clear; ++i) suffix[i] = (uint8_t)i;
+        int width = minsize + 1, next = clear + 2, prev = -1;
+        uint8_t firstc = 0;
+        size_t bitpos = 0;
+        while (idx.size() < npix) {
+            if (bitpos + width > data.size() * 8) break;
+            int code = 0;
+            for (int i = 0; i < width; ++i, ++bitpos) code |= ((data[bitpos >> 3] >> (bitpos & 7)) & 1) << i;
+            if (code == clear) { width = minsize + 1; next = clear + 2; prev = -1; continue; }
+            if (code == stop) break;
+            if (prev < 0) {
+                if (code >= clear) { err = "corrupt GIF data"; return false; }
+                idx.push_back((uint8_t)code);
+                firstc = (uint8_t)code;
+                prev = code;
+                continue;
+            }
+            int cur = code, sp = 0;
+            if (code > next || (code >= clear && code < clear + 2)) { err = "corrupt GIF data"; return false; }
+            if (code == next) { stack[sp++] = firstc; cur = prev; }  // the KwKwK case
+            while (cur >= clear) {
+                if (sp >= 4096) { err = "corrupt GIF data"; return false; }
+                stack[sp++] = suffix[cur];
+                cur = prefix[cur];
+            }
+            stack[sp++] = (uint8_t)cur;
+            firstc = (uint8_t)cur;
+            while (sp > 0 && idx.size() < npix) idx.push_back(stack[--sp]);
+            if (next < 4096) {
+                prefix[next] = prev;
+                suffix[next] = firstc;
+                ++next;
+                if (next == (1 << width) && width < 12) ++width;
+            }
+            prev = code;
+        }
+        idx.resize(npix, 0);                                     // a short stream leaves index 0
+        img.width = sw;
+        img.height = sh;
+        img.rgba.assign((size_t)sw * sh * 4, 0);
+        // row order: interlaced frames store rows 0, 8, 16.., 4, 12.., 2, 6.., 1, 3..
+        std::vector<int> rows;
+        if (ff & 0x40) {
+            const int start[4] = {0, 4, 2, 1}, step[4] = {8, 8, 4, 2};
+            for (int p = 0; p < 4; ++p)
+                for (int y = start[p]; y < fh; y += step[p]) rows.push_back(y);
+        } else {
+            for (int y = 0; y < fh; ++y) rows.push_back(y);
+        }
+        for (int r = 0; r < fh; ++r) {
+            const int y = fy + rows[r];
+            if (y >= sh) continue;
+            for (int x = 0; x < fw; ++x) {
+                if (fx + x >= sw) continue;
+                const int c = idx[(size_t)r * fw + x];
+                if (c == transparent || c >= psize) continue;
+                uint8_t* o = img.rgba.data() + ((size_t)y * sw + fx + x) * 4;
+                o[0] = pal[3 * c];
+                o[1] = pal[3 * c + 1];
+                o[2] = pal[3 * c + 2];
+                o[3] = 255;
+            }
+        }
+        return true;
+    }
+    err = "GIF has no image";
+    return false;
+}
+
 bool load_image(const std::string& path, Image& img, std::string& err) {
     FILE* f = fopen(path.c_str(), "rb");
     if (!f) { err = "cannot open " + path; return false; }
@@ -1002,11 +1140,12 @@ bool load_image(const std::string& path, Image& img, std::string& err) {
     if (data.size() >= 3 && data[0] == 0xFF && data[1] == 0xD8 && data[2] == 0xFF)
         return decode_jpeg(data.data(), data.size(), img, err);
     if (data.size() >= 4 && memcmp(data.data(), "8BPS", 4) == 0) return decode_psd(data.data(), data.size(), img, err);
+    if (data.size() >= 4 && memcmp(data.data(), "GIF8", 4) == 0) return decode_gif(data.data(), data.size(), img, err);
     const size_t dot = path.find_last_of('.');
     std::string ext = dot == std::string::npos ? "" : path.substr(dot + 1);
     for (auto& c : ext) c = (char)tolower((unsigned char)c);
     if (ext == "tga") return decode_tga(data.data(), data.size(), img, err);   // TGA has no magic number
-    err = "unsupported image format (PNG, JPEG, PSD, PAM/PPM/PGM, BMP and TGA are read)";
+    err = "unsupported image format (PNG, JPEG, PSD, GIF, PAM/PPM/PGM, BMP and TGA are read)";
     return false;
 }
 

@@ -1,4 +1,4 @@
-"""Image loading for the encoder's command line (PNG, JPEG, PSD, PAM/PPM/PGM, BMP, TGA).
+"""Image loading for the encoder's command line (PNG, JPEG, PSD, GIF, PAM/PPM/PGM, BMP, TGA).
 
 The reference loads images with stb_image forced to RGBA and flipped
 vertically (main.cpp:24-25).  This module is a small self-contained reader:
@@ -6,8 +6,9 @@ PNG (8-bit greyscale / grey+alpha / RGB / RGBA / palette, non-interlaced,
 all five row filters, zlib from the Python standard library), Netpbm
 P5/P6/P7, Windows BMP (24/32-bit, uncompressed or bit fields), Truevision
 TGA (8-bit grey, 24/32-bit true colour, raw or run-length encoded),
-JPEG (8-bit grey or YCbCr, Huffman coded, baseline or progressive) and
-Photoshop PSD (the merged image; 8/16-bit grey or RGB, optional alpha) -- the
+JPEG (8-bit grey or YCbCr, Huffman coded, baseline or progressive),
+Photoshop PSD (the merged image; 8/16-bit grey or RGB, optional alpha) and
+GIF (the first image; transparency as (0, 0, 0, 0)) -- the
 same formats as the C++ reader of the command line tool.  It always returns
 a (H, W, 4) uint8 array, row 0 first; the caller flips when it wants the
 reference's orientation.
@@ -625,6 +626,107 @@ def load_psd(path: str) -> np.ndarray:
     return out
 
 
+def load_gif(path: str) -> np.ndarray:
+    """GIF 87a / 89a, the first image on its logical screen (transparent black
+    where the image or its transparent index leaves it), as the command line
+    tool's reader."""
+    with open(path, "rb") as fh:
+        d = fh.read()
+    if len(d) < 13 or d[:4] != b"GIF8" or d[4:6] not in (b"7a", b"9a"):
+        raise ValueError("not a GIF file")
+    sw, sh, flags = struct.unpack_from("<HHB", d, 6)
+    pos, gpal, transparent = 13, None, -1
+    if flags & 0x80:
+        n = 2 << (flags & 7)
+        gpal = np.frombuffer(d, np.uint8, 3 * n, pos).reshape(n, 3)
+        pos += 3 * n
+    while pos < len(d):
+        b = d[pos]
+        pos += 1
+        if b == 0x3B:
+            break
+        if b == 0x21:
+            label, first = d[pos], True
+            pos += 1
+            while d[pos] != 0:
+                ln = d[pos]
+                if label == 0xF9 and first and ln >= 4:
+                    transparent = d[pos + 4] if d[pos + 1] & 1 else -1
+                first = False
+                pos += 1 + ln
+            pos += 1
+            continue
+        if b != 0x2C:
+            raise ValueError("bad GIF block")
+        fx, fy, fw, fh, ff = struct.unpack_from("<HHHHB", d, pos)
+        pos += 9
+        pal = gpal
+        if ff & 0x80:
+            n = 2 << (ff & 7)
+            pal = np.frombuffer(d, np.uint8, 3 * n, pos).reshape(n, 3)
+            pos += 3 * n
+        minsize = d[pos]
+        pos += 1
+        data = bytearray()
+        while d[pos] != 0:
+            data += d[pos + 1:pos + 1 + d[pos]]
+            pos += 1 + d[pos]
+        clear, stop = 1 << minsize, (1 << minsize) + 1
+        table, width, out, prev = None, minsize + 1, [], None
+        npix, bitpos, nbits = fw * fh, 0, len(data) * 8
+        bits = int.from_bytes(bytes(data), "little")
+        while len(out) < npix and bitpos + width <= nbits:
+            code = (bits >> bitpos) & ((1 << width) - 1)
+            bitpos += width
+            if code == clear:
+                table = [bytes([i]) for i in range(clear)] + [b"", b""]
+                width, prev = minsize + 1, None
+                continue
+            if code == stop:
+                break
+            if table is None:
+                table = [bytes([i]) for i in range(clear)] + [b"", b""]
+            if prev is None:
+                if code >= clear:
+                    raise ValueError("corrupt GIF data")
+                out.extend(table[code])
+                prev = code
+                continue
+            if code < len(table):
+                cur = table[code]
+            elif code == len(table):
+                cur = table[prev] + table[prev][:1]
+            else:
+                raise ValueError("corrupt GIF data")
+            out.extend(cur)
+            if len(table) < 4096:
+                table.append(table[prev] + cur[:1])
+                if len(table) == (1 << width) and width < 12:
+                    width += 1
+            prev = code
+        idx = np.zeros(npix, np.int64)
+        idx[:min(npix, len(out))] = out[:npix]
+        idx = idx.reshape(fh, fw)
+        if ff & 0x40:
+            order = [y for start, step in ((0, 8), (4, 8), (2, 4), (1, 2)) for y in range(start, fh, step)]
+            rows = np.zeros_like(idx)
+            rows[order] = idx
+            idx = rows
+        img = np.zeros((sh, sw, 4), np.uint8)
+        psize = 0 if pal is None else len(pal)
+        for y in range(fh):
+            if fy + y >= sh:
+                continue
+            for x in range(fw):
+                c = idx[y, x]
+                if fx + x >= sw or c == transparent or c >= psize:
+                    continue
+                img[fy + y, fx + x, :3] = pal[c]
+                img[fy + y, fx + x, 3] = 255
+        return img
+    raise ValueError("GIF has no image")
+
+
 def load_image(path: str) -> np.ndarray:
     with open(path, "rb") as fh:
         head = fh.read(8)
@@ -638,6 +740,8 @@ def load_image(path: str) -> np.ndarray:
         return load_jpeg(path)
     if head[:4] == b"8BPS":
         return load_psd(path)
+    if head[:4] == b"GIF8":
+        return load_gif(path)
     if path.lower().endswith(".tga"):                  # TGA has no magic number
         return load_tga(path)
-    raise ValueError("unsupported image format (PNG, JPEG, PSD, PAM/PPM/PGM, BMP and TGA are read)")
+    raise ValueError("unsupported image format (PNG, JPEG, PSD, GIF, PAM/PPM/PGM, BMP and TGA are read)")

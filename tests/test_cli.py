@@ -9,8 +9,10 @@ JPEG (grey and YCbCr at 4:4:4 / 4:2:2 / 4:4:0 / 4:2:0, restart intervals,
 scan per component, and progressive with spectral selection, successive
 approximation and EOB runs) written here with scipy's orthonormal DCT and
 Huffman tables built from the data, plus a third-party JPEG where one is
-installed, and PSD merged images (grey / RGB, alpha, 8 / 16 bits, raw and
-PackBits, extra channels).
+installed, PSD merged images (grey / RGB, alpha, 8 / 16 bits, raw and
+PackBits, extra channels) and GIF first images (palettes, transparency,
+interlacing, offset frames, a full 12-bit LZW table) with an LZW encoder
+written here.
 GPU tests run the full encode and compare the written .astc with the
 library's blocks for the flipped image, and the reference's own leaf.astc.
 """
@@ -683,6 +685,9 @@ def test_image_reader_under_sanitizers(tmp_path):
                         ("j.jpg", lambda p: _jpeg(p, arr, sampling=(2, 1), restart=3, mode="progressive")),
                         ("k.psd", lambda p: _psd(p, rgba.transpose(2, 0, 1).copy(), 3, 16, True, 1)),
                         ("l.psd", lambda p: _psd(p, rgba[..., :2].transpose(2, 0, 1).copy(), 1, 8, False)),
+                        ("m.gif", lambda p: _gif(p, (arr[..., 0] // 16).astype(np.int64),
+                                                 np.arange(48, dtype=np.uint8).reshape(16, 3) * 5,
+                                                 transparent=3, interlace=True)),
                         ("e.bmp", lambda p: _bmp(p, rgba, bitfields=True)),
                         ("f.bmp", lambda p: _bmp(p, arr)), ("g.tga", lambda p: _tga(p, rgba, rle=True)),
                         ("h.tga", lambda p: _tga(p, arr[..., 0], rle=True))]:
@@ -800,6 +805,106 @@ def test_cli_reads_psd(native, tmp_path, mode, nch, extra, depth, rle):
         sel = part & (a >= 32)
         assert np.abs(want[..., :3].astype(int) - orig)[sel].max() <= 5
     assert np.array_equal(got, want)
+    from astc_encoder_gb300 import image_io                 # the Python reader agrees
+    assert np.array_equal(image_io.load_image(path), want)
+
+
+def _lzw(indices, minsize):
+    """GIF LZW, codes packed least-significant bit first; a clear code first
+    and whenever the 4096-entry table is full."""
+    clear, stop = 1 << minsize, (1 << minsize) + 1
+    acc, nacc, out = 0, 0, bytearray()
+
+    def emit(code, width):
+        nonlocal acc, nacc
+        acc |= code << nacc
+        nacc += width
+        while nacc >= 8:
+            out.append(acc & 255)
+            acc >>= 8
+            nacc -= 8
+
+    def fresh():
+        return {bytes([i]): i for i in range(clear)}, clear + 2, minsize + 1
+    table, nxt, width = fresh()
+    emit(clear, width)
+    w = b""
+    for k in indices:
+        wk = w + bytes([int(k)])
+        if wk in table:
+            w = wk
+            continue
+        emit(table[w], width)
+        if nxt < 4096:
+            table[wk] = nxt
+            nxt += 1
+            if nxt > (1 << width) and width < 12:
+                width += 1
+        else:
+            emit(clear, width)
+            table, nxt, width = fresh()
+        w = bytes([int(k)])
+    emit(table[w], width)
+    emit(stop, width)
+    if nacc:
+        out.append(acc & 255)
+    return bytes(out)
+
+
+def _gif(path, idx, pal, screen=None, offset=(0, 0), transparent=None, interlace=False, local=False):
+    fh, fw = idx.shape
+    sh, sw = screen or (fh, fw)
+    nbits = max(1, int(np.ceil(np.log2(len(pal)))))
+    size = 1 << nbits
+    ptab = np.zeros((size, 3), np.uint8)
+    ptab[:len(pal)] = pal
+    minsize = max(2, nbits)
+    out = b"GIF89a" + struct.pack("<HHBBB", sw, sh, 0 if local else 0x80 | (nbits - 1), 0, 0)
+    if not local:
+        out += ptab.tobytes()
+    if transparent is not None:
+        out += b"\x21\xf9\x04" + struct.pack("<BHB", 1, 0, transparent) + b"\x00"
+    out += b"\x21\xfe\x05hello\x00"                        # a comment extension
+    out += b"\x2c" + struct.pack("<HHHHB", offset[1], offset[0], fw, fh,
+                                  (0x80 | (nbits - 1) if local else 0) | (0x40 if interlace else 0))
+    if local:
+        out += ptab.tobytes()
+    rows = idx
+    if interlace:
+        rows = idx[[y for start, step in ((0, 8), (4, 8), (2, 4), (1, 2)) for y in range(start, fh, step)]]
+    data = _lzw(rows.reshape(-1), minsize)
+    out += bytes([minsize]) + b"".join(bytes([len(data[i:i + 255])]) + data[i:i + 255]
+                                      for i in range(0, len(data), 255)) + b"\x00\x3b"
+    with open(path, "wb") as fh_:
+        fh_.write(out)
+
+
+@pytest.mark.parametrize("case", ["plain", "transparent", "interlaced", "offset_local", "big_table", "two_colour"])
+def test_cli_reads_gif(native, tmp_path, case):
+    rng = np.random.default_rng(["plain", "transparent", "interlaced", "offset_local", "big_table",
+                                 "two_colour"].index(case))
+    ncol = 2 if case == "two_colour" else 256 if case == "big_table" else 37
+    h, w = (96, 128) if case == "big_table" else (29, 41)
+    pal = rng.integers(0, 256, (ncol, 3), dtype=np.uint8)
+    idx = rng.integers(0, ncol, (h, w))
+    idx[4:12, 5:30] = 3 % ncol                                      # repeats for the string table
+    kw, screen, offset = {}, None, (0, 0)
+    if case == "transparent":
+        kw["transparent"] = 5
+    if case == "interlaced":
+        kw["interlace"] = True
+    if case == "offset_local":
+        screen, offset, kw["local"] = (40, 50), (6, 4), True
+    path = str(tmp_path / "in.gif")
+    _gif(path, idx, pal, screen=screen, offset=offset, **kw)
+    sh, sw = screen or (h, w)
+    want = np.zeros((sh, sw, 4), np.uint8)
+    region = want[offset[0]:offset[0] + h, offset[1]:offset[1] + w]
+    region[..., :3] = pal[idx]
+    region[..., 3] = 255
+    if case == "transparent":
+        region[idx == 5] = 0
+    assert np.array_equal(_dump(native, path, tmp_path)[::-1], want)
     from astc_encoder_gb300 import image_io                 # the Python reader agrees
     assert np.array_equal(image_io.load_image(path), want)
 
