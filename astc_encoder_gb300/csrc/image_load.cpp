@@ -1,5 +1,5 @@
-// image_load.cpp -- PNG / JPEG / PSD / GIF / Netpbm / BMP / TGA reader for
-// the command line tool.
+// image_load.cpp -- PNG / JPEG / PSD / GIF / HDR / Netpbm / BMP / TGA reader
+// for the command line tool.
 // Inflate follows RFC 1951 (stored, fixed and dynamic Huffman blocks,
 // canonical codes decoded one bit at a time); the zlib wrapper RFC 1950;
 // PNG chunk layout, filters 0-4 and colour types the PNG specification.
@@ -1125,6 +1125,82 @@ bool decode_gif(const uint8_t* d, size_t n, Image& img, std::string& err) {
     return false;
 }
 
+// Radiance HDR (RGBE): "#?RADIANCE" / "#?RGBE" header with
+// FORMAT=32-bit_rle_rgbe, resolution "-Y h +X w", flat or run-length
+// scanlines (the 2 2 hi lo form, channels coded apart).  Texel (m, e) is
+// m x 2^(e - 136) (0 when e = 0); the 8-bit image is what an 8-bit load of the
+// reference's image library gives: 255 x v^(1/2.2) + 0.5, clamped and
+// truncated, alpha 255.
+bool decode_hdr(const uint8_t* d, size_t n, Image& img, std::string& err) {
+    size_t pos = 0;
+    auto line = [&](std::string& out) {
+        out.clear();
+        while (pos < n && d[pos] != '\n') out.push_back((char)d[pos++]);
+        if (pos >= n) return false;
+        ++pos;
+        return true;
+    };
+    std::string l;
+    if (!line(l) || (l != "#?RADIANCE" && l != "#?RGBE")) { err = "not a Radiance HDR file"; return false; }
+    while (true) {
+        if (!line(l)) { err = "HDR header truncated"; return false; }
+        if (l.empty()) break;
+        if (l.rfind("FORMAT=", 0) == 0) {
+            if (l != "FORMAT=32-bit_rle_rgbe") { err = "HDR format not read (32-bit_rle_rgbe is)"; return false; }
+        }
+    }
+    if (!line(l)) { err = "HDR resolution missing"; return false; }
+    int h = 0, w = 0;
+    char ax[3] = {}, ay[3] = {};
+    if (sscanf(l.c_str(), "%2s %d %2s %d", ay, &h, ax, &w) != 4 || strcmp(ay, "-Y") != 0 || strcmp(ax, "+X") != 0) {
+        err = "HDR orientation not read (-Y h +X w is)";
+        return false;
+    }
+    if (!dims_ok(w, h, err)) return false;
+    if ((size_t)w * h > 64 * (n - pos) + 64) { err = "HDR data too short for its size"; return false; }
+    std::vector<uint8_t> rgbe((size_t)w * h * 4);
+    for (int y = 0; y < h; ++y) {
+        uint8_t* row = rgbe.data() + (size_t)y * w * 4;
+        if (w >= 8 && w < 32768 && pos + 4 <= n && d[pos] == 2 && d[pos + 1] == 2 && !(d[pos + 2] & 0x80)) {
+            if (((d[pos + 2] << 8) | d[pos + 3]) != w) { err = "bad HDR scanline"; return false; }
+            pos += 4;
+            for (int c = 0; c < 4; ++c)
+                for (int x = 0; x < w;) {
+                    if (pos >= n) { err = "HDR data too short"; return false; }
+                    int k = d[pos++];
+                    if (k > 128) {                               // run
+                        k -= 128;
+                        if (pos >= n || x + k > w) { err = "bad HDR run"; return false; }
+                        for (int i = 0; i < k; ++i) row[(size_t)(x + i) * 4 + c] = d[pos];
+                        ++pos;
+                    } else {                                     // literal
+                        if (k == 0 || pos + k > n || x + k > w) { err = "bad HDR run"; return false; }
+                        for (int i = 0; i < k; ++i) row[(size_t)(x + i) * 4 + c] = d[pos + i];
+                        pos += k;
+                    }
+                    x += k;
+                }
+        } else {
+            if (pos + (size_t)w * 4 > n) { err = "HDR data too short"; return false; }
+            memcpy(row, d + pos, (size_t)w * 4);
+            pos += (size_t)w * 4;
+        }
+    }
+    img.width = w;
+    img.height = h;
+    img.rgba.assign((size_t)w * h * 4, 255);
+    for (size_t i = 0; i < (size_t)w * h; ++i) {
+        const uint8_t* p = rgbe.data() + i * 4;
+        const float f = p[3] ? ldexpf(1.0f, (int)p[3] - 136) : 0.0f;
+        for (int c = 0; c < 3; ++c) {
+            float z = powf((float)p[c] * f, 1.0f / 2.2f) * 255.0f + 0.5f;
+            z = z < 0.0f ? 0.0f : z > 255.0f ? 255.0f : z;
+            img.rgba[i * 4 + c] = (uint8_t)(int)z;
+        }
+    }
+    return true;
+}
+
 bool load_image(const std::string& path, Image& img, std::string& err) {
     FILE* f = fopen(path.c_str(), "rb");
     if (!f) { err = "cannot open " + path; return false; }
@@ -1141,11 +1217,14 @@ bool load_image(const std::string& path, Image& img, std::string& err) {
         return decode_jpeg(data.data(), data.size(), img, err);
     if (data.size() >= 4 && memcmp(data.data(), "8BPS", 4) == 0) return decode_psd(data.data(), data.size(), img, err);
     if (data.size() >= 4 && memcmp(data.data(), "GIF8", 4) == 0) return decode_gif(data.data(), data.size(), img, err);
+    if (data.size() >= 6 && memcmp(data.data(), "#?RGBE", 6) == 0) return decode_hdr(data.data(), data.size(), img, err);
+    if (data.size() >= 10 && memcmp(data.data(), "#?RADIANCE", 10) == 0)
+        return decode_hdr(data.data(), data.size(), img, err);
     const size_t dot = path.find_last_of('.');
     std::string ext = dot == std::string::npos ? "" : path.substr(dot + 1);
     for (auto& c : ext) c = (char)tolower((unsigned char)c);
     if (ext == "tga") return decode_tga(data.data(), data.size(), img, err);   // TGA has no magic number
-    err = "unsupported image format (PNG, JPEG, PSD, GIF, PAM/PPM/PGM, BMP and TGA are read)";
+    err = "unsupported image format (PNG, JPEG, PSD, GIF, HDR, PAM/PPM/PGM, BMP and TGA are read)";
     return false;
 }
 

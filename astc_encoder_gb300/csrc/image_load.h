@@ -5,7 +5,8 @@
 // (24/32-bit true colour and 8-bit grey, raw or run-length encoded) and
 // JPEG (8-bit grey or YCbCr, Huffman coded, baseline or progressive) and
 // Photoshop PSD (the merged image; 8/16-bit grey or RGB, optional alpha) and
-// GIF (the first image, transparency as (0, 0, 0, 0)).
+// GIF (the first image, transparency as (0, 0, 0, 0)) and Radiance HDR
+// (RGBE, taken to 8 bits with gamma 1/2.2).
 // Output is always RGBA8, row 0 first (the caller flips for the reference's
 // orientation, main.cpp:24).  Written for this project; the reference uses
 // the third-party stb_image for the same job.
@@ -31,6 +32,7 @@ bool decode_tga(const uint8_t* data, size_t size, Image& out, std::string& err);
 bool decode_jpeg(const uint8_t* data, size_t size, Image& out, std::string& err);
 bool decode_psd(const uint8_t* data, size_t size, Image& out, std::string& err);
 bool decode_gif(const uint8_t* data, size_t size, Image& out, std::string& err);
+bool decode_hdr(const uint8_t* data, size_t size, Image& out, std::string& err);
 // zlib stream (2-byte header, deflate blocks, Adler-32) -> raw bytes.
 bool zlib_inflate(const uint8_t* data, size_t size, std::vector<uint8_t>& out, std::string& err);
 // Writes RGBA8 as a P7 (PAM) file.

@@ -1,4 +1,4 @@
-"""Image loading for the encoder's command line (PNG, JPEG, PSD, GIF, PAM/PPM/PGM, BMP, TGA).
+"""Image loading for the encoder's command line (PNG, JPEG, PSD, GIF, HDR, PAM/PPM/PGM, BMP, TGA).
 
 The reference loads images with stb_image forced to RGBA and flipped
 vertically (main.cpp:24-25).  This module is a small self-contained reader:
@@ -7,8 +7,9 @@ all five row filters, zlib from the Python standard library), Netpbm
 P5/P6/P7, Windows BMP (24/32-bit, uncompressed or bit fields), Truevision
 TGA (8-bit grey, 24/32-bit true colour, raw or run-length encoded),
 JPEG (8-bit grey or YCbCr, Huffman coded, baseline or progressive),
-Photoshop PSD (the merged image; 8/16-bit grey or RGB, optional alpha) and
-GIF (the first image; transparency as (0, 0, 0, 0)) -- the
+Photoshop PSD (the merged image; 8/16-bit grey or RGB, optional alpha),
+GIF (the first image; transparency as (0, 0, 0, 0)) and Radiance HDR (taken
+to 8 bits with gamma 1/2.2) -- the
 same formats as the C++ reader of the command line tool.  It always returns
 a (H, W, 4) uint8 array, row 0 first; the caller flips when it wants the
 reference's orientation.
@@ -727,6 +728,58 @@ def load_gif(path: str) -> np.ndarray:
     raise ValueError("GIF has no image")
 
 
+def load_hdr(path: str) -> np.ndarray:
+    """Radiance HDR (RGBE; flat or run-length scanlines, -Y h +X w), taken to
+    8 bits as the command line tool's reader does: 255 v^(1/2.2) + 0.5,
+    clamped and truncated (float32)."""
+    with open(path, "rb") as fh:
+        d = fh.read()
+    lines, pos = [], 0
+    while True:
+        e = d.index(b"\n", pos)
+        lines.append(d[pos:e].decode("latin-1"))
+        pos = e + 1
+        if len(lines) > 1 and lines[-1] == "":
+            break
+    if lines[0] not in ("#?RADIANCE", "#?RGBE"):
+        raise ValueError("not a Radiance HDR file")
+    for ln in lines:
+        if ln.startswith("FORMAT=") and ln != "FORMAT=32-bit_rle_rgbe":
+            raise ValueError("HDR format not read (32-bit_rle_rgbe is)")
+    e = d.index(b"\n", pos)
+    parts = d[pos:e].decode("latin-1").split()
+    pos = e + 1
+    if len(parts) != 4 or parts[0] != "-Y" or parts[2] != "+X":
+        raise ValueError("HDR orientation not read (-Y h +X w is)")
+    h, w = int(parts[1]), int(parts[3])
+    rgbe = np.zeros((h, w, 4), np.uint8)
+    for y in range(h):
+        if 8 <= w < 32768 and d[pos] == 2 and d[pos + 1] == 2 and not d[pos + 2] & 0x80:
+            pos += 4
+            for c in range(4):
+                x = 0
+                while x < w:
+                    k = d[pos]
+                    pos += 1
+                    if k > 128:
+                        rgbe[y, x:x + k - 128, c] = d[pos]
+                        pos += 1
+                        x += k - 128
+                    else:
+                        rgbe[y, x:x + k, c] = np.frombuffer(d, np.uint8, k, pos)
+                        pos += k
+                        x += k
+        else:
+            rgbe[y] = np.frombuffer(d, np.uint8, 4 * w, pos).reshape(w, 4)
+            pos += 4 * w
+    f = np.where(rgbe[..., 3] > 0, np.ldexp(np.float32(1.0), rgbe[..., 3].astype(np.int32) - 136), 0).astype(np.float32)
+    v = rgbe[..., :3].astype(np.float32) * f[..., None]
+    z = np.power(v, np.float32(1.0 / 2.2)) * np.float32(255.0) + np.float32(0.5)
+    out = np.full((h, w, 4), 255, np.uint8)
+    out[..., :3] = np.clip(z, 0, 255).astype(np.int32)
+    return out
+
+
 def load_image(path: str) -> np.ndarray:
     with open(path, "rb") as fh:
         head = fh.read(8)
@@ -742,6 +795,8 @@ def load_image(path: str) -> np.ndarray:
         return load_psd(path)
     if head[:4] == b"GIF8":
         return load_gif(path)
+    if head[:6] == b"#?RGBE" or head[:8] == b"#?RADIAN":
+        return load_hdr(path)
     if path.lower().endswith(".tga"):                  # TGA has no magic number
         return load_tga(path)
-    raise ValueError("unsupported image format (PNG, JPEG, PSD, GIF, PAM/PPM/PGM, BMP and TGA are read)")
+    raise ValueError("unsupported image format (PNG, JPEG, PSD, GIF, HDR, PAM/PPM/PGM, BMP and TGA are read)")

@@ -12,7 +12,7 @@ Huffman tables built from the data, plus a third-party JPEG where one is
 installed, PSD merged images (grey / RGB, alpha, 8 / 16 bits, raw and
 PackBits, extra channels) and GIF first images (palettes, transparency,
 interlacing, offset frames, a full 12-bit LZW table) with an LZW encoder
-written here.
+written here, and Radiance HDR (flat and run-length scanlines).
 GPU tests run the full encode and compare the written .astc with the
 library's blocks for the flipped image, and the reference's own leaf.astc.
 """
@@ -688,6 +688,7 @@ def test_image_reader_under_sanitizers(tmp_path):
                         ("m.gif", lambda p: _gif(p, (arr[..., 0] // 16).astype(np.int64),
                                                  np.arange(48, dtype=np.uint8).reshape(16, 3) * 5,
                                                  transparent=3, interlace=True)),
+                        ("n.hdr", lambda p: _hdr(p, np.dstack([arr, np.full(arr.shape[:2], 130, np.uint8)]))),
                         ("e.bmp", lambda p: _bmp(p, rgba, bitfields=True)),
                         ("f.bmp", lambda p: _bmp(p, arr)), ("g.tga", lambda p: _tga(p, rgba, rle=True)),
                         ("h.tga", lambda p: _tga(p, arr[..., 0], rle=True))]:
@@ -907,6 +908,56 @@ def test_cli_reads_gif(native, tmp_path, case):
     assert np.array_equal(_dump(native, path, tmp_path)[::-1], want)
     from astc_encoder_gb300 import image_io                 # the Python reader agrees
     assert np.array_equal(image_io.load_image(path), want)
+
+
+def _hdr(path, rgbe, rle=True):
+    """Radiance HDR: run-length scanlines (runs of 3+ as 128 + n, else literals)."""
+    h, w = rgbe.shape[:2]
+    out = b"#?RADIANCE\n# written by the test suite\nFORMAT=32-bit_rle_rgbe\nEXPOSURE=1.0\n\n"
+    out += ("-Y %d +X %d\n" % (h, w)).encode()
+    for y in range(h):
+        if not rle:
+            out += rgbe[y].tobytes()
+            continue
+        out += bytes([2, 2, w >> 8, w & 255])
+        for c in range(4):
+            ch, x = rgbe[y, :, c], 0
+            while x < w:
+                r = x
+                while r + 1 < w and ch[r + 1] == ch[x] and r - x < 126:
+                    r += 1
+                if r - x >= 2:
+                    out += bytes([128 + r - x + 1, int(ch[x])])
+                    x = r + 1
+                    continue
+                k = x
+                while k < w and k - x < 128 and not (k + 2 < w and ch[k] == ch[k + 1] == ch[k + 2]):
+                    k += 1
+                out += bytes([k - x]) + ch[x:k].tobytes()
+                x = k
+    with open(path, "wb") as fh:
+        fh.write(out)
+
+
+@pytest.mark.parametrize("rle", [False, True])
+def test_cli_reads_hdr(native, tmp_path, rle):
+    rng = np.random.default_rng(3 + rle)
+    h, w = 19, 37
+    rgbe = rng.integers(0, 256, (h, w, 4), dtype=np.uint8)
+    rgbe[..., 3] = rng.integers(120, 140, (h, w))                       # values around 2^-16 .. 2^4
+    rgbe[2, :, 3] = 0                                                    # zero texels
+    rgbe[5:9, 4:30] = rgbe[5, 4]                                         # runs
+    path = str(tmp_path / "in.hdr")
+    _hdr(path, rgbe, rle)
+    v = rgbe[..., :3].astype(np.float64) * np.where(rgbe[..., 3] > 0, 2.0 ** (rgbe[..., 3].astype(np.float64) - 136), 0)[..., None]
+    want = np.floor(np.clip(v ** (1 / 2.2) * 255 + 0.5, 0, 255))
+    got = _dump(native, path, tmp_path)[::-1]
+    assert (got[..., 3] == 255).all()
+    diff = np.abs(got[..., :3].astype(int) - want)
+    assert diff.max() <= 1 and (diff > 0).mean() < 0.01                 # float32 pow against float64
+    from astc_encoder_gb300 import image_io
+    py = image_io.load_image(path)
+    assert np.abs(py.astype(int) - got).max() <= 1 and (py != got).mean() < 0.01
 
 
 def test_cli_rejects_unknown_format(native, tmp_path):
