@@ -2,7 +2,8 @@
 // for the command line tool.
 // Inflate follows RFC 1951 (stored, fixed and dynamic Huffman blocks,
 // canonical codes decoded one bit at a time); the zlib wrapper RFC 1950;
-// PNG chunk layout, filters 0-4 and colour types the PNG specification.
+// PNG chunk layout, filters 0-4, colour types, bit depths, Adam7 and tRNS the
+// PNG specification.
 #include "image_load.h"
 
 #include <ctype.h>
@@ -234,7 +235,7 @@ bool decode_png(const uint8_t* d, size_t n, Image& img, std::string& err) {
         pos += 12 + (size_t)len;
     }
     if (!dims_ok(w, h, err)) return false;
-    if (interlace != 0) { err = "interlaced PNG is not supported"; return false; }
+    if (interlace > 1) { err = "bad PNG interlace method"; return false; }
     int chans = 0;
     switch (ctype) {
     case 0: chans = 1; break;
@@ -244,61 +245,93 @@ bool decode_png(const uint8_t* d, size_t n, Image& img, std::string& err) {
     case 6: chans = 4; break;
     default: err = "bad PNG colour type"; return false;
     }
-    if (!(depth == 8 || (depth == 16 && ctype != 3))) { err = "only 8- and 16-bit PNG is supported"; return false; }
-    const int bps = depth / 8;
-    const size_t bpp = (size_t)chans * bps, stride = (size_t)w * bpp;
+    const bool low_ok = ctype == 0 || ctype == 3;              // 1/2/4-bit: grey and palette only
+    if (!(depth == 8 || (depth == 16 && ctype != 3) || (low_ok && (depth == 1 || depth == 2 || depth == 4)))) {
+        err = "bad PNG bit depth";
+        return false;
+    }
     std::vector<uint8_t> raw;
     if (!zlib_inflate(idat.data(), idat.size(), raw, err)) return false;
-    if (raw.size() < (stride + 1) * h) { err = "PNG image data too short"; return false; }
-    std::vector<uint8_t> cur(stride), prev(stride, 0);
+    // Adam7 passes (x0, y0, dx, dy), or the whole image as one pass
+    static const int kAdam7[7][4] = {{0, 0, 8, 8}, {4, 0, 8, 8}, {0, 4, 4, 8}, {2, 0, 4, 4},
+                                     {0, 2, 2, 4}, {1, 0, 2, 2}, {0, 1, 1, 2}};
+    static const int kWhole[1][4] = {{0, 0, 1, 1}};
+    const int npass = interlace ? 7 : 1;
+    const int(*passes)[4] = interlace ? kAdam7 : kWhole;
+    const size_t fbpp = std::max<size_t>(1, (size_t)chans * depth / 8);   // filter unit in bytes
+    const uint32_t maxv = (1u << depth) - 1;
+    // tRNS key colour of grey / RGB images, in sample units
+    int key[3] = {-1, -1, -1};
+    if (ctype == 0 && trns.size() >= 2) key[0] = (trns[0] << 8) | trns[1];
+    if (ctype == 2 && trns.size() >= 6)
+        for (int c = 0; c < 3; ++c) key[c] = (trns[2 * c] << 8) | trns[2 * c + 1];
     img.width = (int)w;
     img.height = (int)h;
     img.rgba.assign((size_t)w * h * 4, 0);
-    for (uint32_t y = 0; y < h; ++y) {
-        const uint8_t* line = raw.data() + y * (stride + 1);
-        const int f = line[0];
-        for (size_t x = 0; x < stride; ++x) {
-            const int a = x >= bpp ? cur[x - bpp] : 0, b = prev[x], c = x >= bpp ? prev[x - bpp] : 0;
-            int p = 0;
-            switch (f) {
-            case 0: p = 0; break;
-            case 1: p = a; break;
-            case 2: p = b; break;
-            case 3: p = (a + b) >> 1; break;
-            case 4: {
-                const int e = a + b - c, pa = abs(e - a), pb = abs(e - b), pc = abs(e - c);
-                p = (pa <= pb && pa <= pc) ? a : (pb <= pc ? b : c);
-                break;
-            }
-            default: err = "bad PNG filter type"; return false;
-            }
-            cur[x] = (uint8_t)(line[1 + x] + p);
-        }
-        uint8_t* o = img.rgba.data() + (size_t)y * w * 4;
-        for (uint32_t x = 0; x < w; ++x) {
-            const uint8_t* s = cur.data() + x * bpp;
-            auto ch = [&](int i) { return s[i * bps]; };             // high byte of 16-bit
-            uint8_t r, g, bl, al = 255;
-            if (ctype == 3) {
-                const int idx = ch(0);
-                if ((size_t)idx * 3 + 2 >= plte.size()) {
-                    err = "palette index out of range";
-                    return false;
+    size_t off = 0;
+    for (int p = 0; p < npass; ++p) {
+        const uint32_t x0 = passes[p][0], y0 = passes[p][1], dx = passes[p][2], dy = passes[p][3];
+        const uint32_t pw = w > x0 ? (w - x0 + dx - 1) / dx : 0, ph = h > y0 ? (h - y0 + dy - 1) / dy : 0;
+        if (pw == 0 || ph == 0) continue;
+        const size_t stride = ((size_t)pw * chans * depth + 7) / 8;
+        if (raw.size() < off + (stride + 1) * ph) { err = "PNG image data too short"; return false; }
+        std::vector<uint8_t> cur(stride), prev(stride, 0);
+        for (uint32_t y = 0; y < ph; ++y, off += stride + 1) {
+            const uint8_t* line = raw.data() + off;
+            const int f = line[0];
+            for (size_t x = 0; x < stride; ++x) {
+                const int a = x >= fbpp ? cur[x - fbpp] : 0, b = prev[x], c = x >= fbpp ? prev[x - fbpp] : 0;
+                int pr = 0;
+                switch (f) {
+                case 0: pr = 0; break;
+                case 1: pr = a; break;
+                case 2: pr = b; break;
+                case 3: pr = (a + b) >> 1; break;
+                case 4: {
+                    const int e = a + b - c, pa = abs(e - a), pb = abs(e - b), pc = abs(e - c);
+                    pr = (pa <= pb && pa <= pc) ? a : (pb <= pc ? b : c);
+                    break;
                 }
-                r = plte[idx * 3];
-                g = plte[idx * 3 + 1];
-                bl = plte[idx * 3 + 2];
-                if ((size_t)idx < trns.size()) al = trns[idx];
-            } else if (chans >= 3) {
-                r = ch(0); g = ch(1); bl = ch(2);
-                if (chans == 4) al = ch(3);
-            } else {
-                r = g = bl = ch(0);
-                if (chans == 2) al = ch(1);
+                default: err = "bad PNG filter type"; return false;
+                }
+                cur[x] = (uint8_t)(line[1 + x] + pr);
             }
-            o[4 * x] = r; o[4 * x + 1] = g; o[4 * x + 2] = bl; o[4 * x + 3] = al;
+            // sample i of this row, in its own bit depth
+            auto sample = [&](size_t i) -> uint32_t {
+                if (depth == 16) return ((uint32_t)cur[2 * i] << 8) | cur[2 * i + 1];
+                if (depth == 8) return cur[i];
+                const size_t bit = i * depth;
+                return (cur[bit >> 3] >> (8 - depth - (bit & 7))) & maxv;
+            };
+            auto to8 = [&](uint32_t v) -> uint8_t {
+                return (uint8_t)(depth == 16 ? v >> 8 : depth == 8 ? v : v * (255 / maxv));
+            };
+            uint8_t* orow = img.rgba.data() + (size_t)(y0 + y * dy) * w * 4;
+            for (uint32_t x = 0; x < pw; ++x) {
+                uint8_t* o = orow + (size_t)(x0 + x * dx) * 4;
+                const size_t i = (size_t)x * chans;
+                if (ctype == 3) {
+                    const uint32_t idx = sample(i);
+                    if ((size_t)idx * 3 + 2 >= plte.size()) { err = "palette index out of range"; return false; }
+                    o[0] = plte[idx * 3];
+                    o[1] = plte[idx * 3 + 1];
+                    o[2] = plte[idx * 3 + 2];
+                    o[3] = idx < trns.size() ? trns[idx] : 255;
+                } else if (chans >= 3) {
+                    const uint32_t r = sample(i), g = sample(i + 1), bl = sample(i + 2);
+                    o[0] = to8(r);
+                    o[1] = to8(g);
+                    o[2] = to8(bl);
+                    o[3] = chans == 4 ? to8(sample(i + 3))
+                                      : ((int)r == key[0] && (int)g == key[1] && (int)bl == key[2] ? 0 : 255);
+                } else {
+                    const uint32_t v = sample(i);
+                    o[0] = o[1] = o[2] = to8(v);
+                    o[3] = chans == 2 ? to8(sample(i + 1)) : ((int)v == key[0] ? 0 : 255);
+                }
+            }
+            std::swap(cur, prev);
         }
-        std::swap(cur, prev);
     }
     return true;
 }

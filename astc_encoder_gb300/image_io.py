@@ -2,8 +2,9 @@
 
 The reference loads images with stb_image forced to RGBA and flipped
 vertically (main.cpp:24-25).  This module is a small self-contained reader:
-PNG (8-bit greyscale / grey+alpha / RGB / RGBA / palette, non-interlaced,
-all five row filters, zlib from the Python standard library), Netpbm
+PNG (greyscale / grey+alpha / RGB / RGBA / palette at every bit depth the
+format allows, 16-bit channels reduced to their high byte, Adam7 interlacing,
+tRNS, all five row filters, zlib from the Python standard library), Netpbm
 P5/P6/P7, Windows BMP (24/32-bit, uncompressed or bit fields), Truevision
 TGA (8-bit grey, 24/32-bit true colour, raw or run-length encoded),
 JPEG (8-bit grey or YCbCr, Huffman coded, baseline or progressive),
@@ -85,32 +86,58 @@ def load_png(path: str) -> np.ndarray:
     if hdr is None:
         raise ValueError("PNG without IHDR")
     w, h, depth, ctype, _, _, interlace = hdr
-    if depth != 8 or interlace != 0:
-        raise ValueError("only 8-bit non-interlaced PNG is supported")
     chans = {0: 1, 2: 3, 3: 1, 4: 2, 6: 4}[ctype]
+    if not (depth == 8 or (depth == 16 and ctype != 3) or (ctype in (0, 3) and depth in (1, 2, 4))):
+        raise ValueError("bad PNG bit depth")
     raw = zlib.decompress(b"".join(idat))
-    px = _unfilter(raw, h, w * chans, chans).reshape(h, w, chans)
+    passes = [(0, 0, 8, 8), (4, 0, 8, 8), (0, 4, 4, 8), (2, 0, 4, 4), (0, 2, 2, 4), (1, 0, 2, 2),
+              (0, 1, 1, 2)] if interlace else [(0, 0, 1, 1)]
+    samples = np.zeros((h, w, chans), np.int64)               # in the image's own bit depth
+    off = 0
+    for x0, y0, dx, dy in passes:
+        pw, ph = max(0, -(-(w - x0) // dx)), max(0, -(-(h - y0) // dy))
+        if pw == 0 or ph == 0:
+            continue
+        stride = (pw * chans * depth + 7) // 8
+        rows = _unfilter(raw[off:off + (stride + 1) * ph], ph, stride, max(1, chans * depth // 8))
+        off += (stride + 1) * ph
+        if depth == 16:
+            v = rows.reshape(ph, pw * chans, 2).astype(np.int64)
+            v = (v[..., 0] << 8) | v[..., 1]
+        elif depth == 8:
+            v = rows.astype(np.int64)
+        else:
+            bits = np.unpackbits(rows, axis=1)[:, :pw * chans * depth].reshape(ph, pw * chans, depth)
+            v = (bits.astype(np.int64) << np.arange(depth - 1, -1, -1)).sum(-1)
+        samples[y0::dy, x0::dx] = v.reshape(ph, pw, chans)
+    maxv = (1 << depth) - 1
+    to8 = (lambda x: x >> 8) if depth == 16 else (lambda x: x * (255 // maxv))
     out = np.empty((h, w, 4), np.uint8)
-    if ctype == 6:
-        out[:] = px
-    elif ctype == 2:
-        out[..., :3] = px
-        out[..., 3] = 255
-    elif ctype == 0:
-        out[..., :3] = px
-        out[..., 3] = 255
-    elif ctype == 4:
-        out[..., :3] = px[..., :1]
-        out[..., 3] = px[..., 1]
-    else:
+    if ctype == 3:
         if plte is None:
             raise ValueError("palette PNG without PLTE")
-        idx = px[..., 0]
+        idx = samples[..., 0]
+        if idx.max(initial=0) >= len(plte):
+            raise ValueError("palette index out of range")
         out[..., :3] = plte[idx]
         alpha = np.full(256, 255, np.uint8)
         if trns is not None:
-            alpha[:len(trns)] = trns
+            alpha[:len(trns)] = trns[:256]
         out[..., 3] = alpha[idx]
+        return out
+    key = None
+    if trns is not None and ctype in (0, 2) and len(trns) >= 2 * (1 if ctype == 0 else 3):
+        key = [(int(trns[2 * c]) << 8) | int(trns[2 * c + 1]) for c in range(1 if ctype == 0 else 3)]
+    if ctype in (2, 6):
+        out[..., :3] = to8(samples[..., :3])
+    else:
+        out[..., :3] = to8(samples[..., :1])
+    if ctype in (4, 6):
+        out[..., 3] = to8(samples[..., -1])
+    else:
+        out[..., 3] = 255
+        if key is not None:
+            out[..., 3] = np.where((samples[..., :len(key)] == key).all(-1), 0, 255)
     return out
 
 

@@ -29,48 +29,61 @@ from conftest import GOLDEN, ROOT
 CLI = os.path.join(ROOT, "astc_encoder_gb300", "_lib", "astc_cs_enc")
 
 
-def _png(path, arr, ctype, depth=8, palette=None, trns=None):
-    """Writes a PNG, cycling the row filter through 0..4."""
+def _png(path, arr, ctype, depth=8, palette=None, trns=None, interlace=False):
+    """Writes a PNG of sample values `arr` (in the image's bit depth), cycling
+    the row filter through 0..4; Adam7 passes when `interlace`."""
     h, w = arr.shape[:2]
     chans = {0: 1, 2: 3, 3: 1, 4: 2, 6: 4}[ctype]
-    bps = depth // 8
-    data = arr.reshape(h, w * chans).astype(np.uint16 if depth == 16 else np.uint8)
-    if depth == 16:
-        rows = data.astype(">u2").view(np.uint8).reshape(h, w * chans * 2)
-    else:
-        rows = data
-    bpp = chans * bps
-    out = bytearray()
-    prev = np.zeros(rows.shape[1], np.int32)
-    for y in range(h):
-        f = y % 5
-        cur = rows[y].astype(np.int32)
-        left = np.concatenate([np.zeros(bpp, np.int32), cur[:-bpp]])
-        upleft = np.concatenate([np.zeros(bpp, np.int32), prev[:-bpp]])
-        if f == 0:
-            enc = cur
-        elif f == 1:
-            enc = cur - left
-        elif f == 2:
-            enc = cur - prev
-        elif f == 3:
-            enc = cur - ((left + prev) >> 1)
+    data = arr.reshape(h, w, chans).astype(np.int64)
+    passes = [(0, 0, 8, 8), (4, 0, 8, 8), (0, 4, 4, 8), (2, 0, 4, 4), (0, 2, 2, 4), (1, 0, 2, 2),
+              (0, 1, 1, 2)] if interlace else [(0, 0, 1, 1)]
+    bpp = max(1, chans * depth // 8)
+    out, nrow = bytearray(), 0
+    for x0, y0, dx, dy in passes:
+        sub = data[y0::dy, x0::dx]
+        if sub.size == 0:
+            continue
+        ph, pw = sub.shape[:2]
+        flat = sub.reshape(ph, pw * chans)
+        if depth == 16:
+            rows = flat.astype(">u2").view(np.uint8).reshape(ph, pw * chans * 2).astype(np.int32)
+        elif depth == 8:
+            rows = flat.astype(np.int32)
         else:
-            p = left + prev - upleft
-            pa, pb, pc = abs(p - left), abs(p - prev), abs(p - upleft)
-            pred = np.where((pa <= pb) & (pa <= pc), left, np.where(pb <= pc, prev, upleft))
-            enc = cur - pred
-        out.append(f)
-        out += (enc & 255).astype(np.uint8).tobytes()
-        prev = cur
+            bits = ((flat[..., None] >> np.arange(depth - 1, -1, -1)) & 1).astype(np.uint8)
+            rows = np.packbits(bits.reshape(ph, -1), axis=1).astype(np.int32)
+        prev = np.zeros(rows.shape[1], np.int32)
+        for y in range(ph):
+            f = nrow % 5
+            nrow += 1
+            cur = rows[y]
+            left = np.concatenate([np.zeros(bpp, np.int32), cur[:-bpp]])
+            upleft = np.concatenate([np.zeros(bpp, np.int32), prev[:-bpp]])
+            if f == 0:
+                enc = cur
+            elif f == 1:
+                enc = cur - left
+            elif f == 2:
+                enc = cur - prev
+            elif f == 3:
+                enc = cur - ((left + prev) >> 1)
+            else:
+                pp = left + prev - upleft
+                pa, pb, pc = abs(pp - left), abs(pp - prev), abs(pp - upleft)
+                pred = np.where((pa <= pb) & (pa <= pc), left, np.where(pb <= pc, prev, upleft))
+                enc = cur - pred
+            out.append(f)
+            out += (enc & 255).astype(np.uint8).tobytes()
+            prev = cur
 
     def chunk(t, b):
         return struct.pack(">I", len(b)) + t + b + struct.pack(">I", zlib.crc32(t + b) & 0xFFFFFFFF)
-    png = b"\x89PNG\r\n\x1a\n" + chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, depth, ctype, 0, 0, 0))
+    png = b"\x89PNG\r\n\x1a\n" + chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, depth, ctype, 0, 0,
+                                                               1 if interlace else 0))
     if palette is not None:
         png += chunk(b"PLTE", palette.astype(np.uint8).tobytes())
     if trns is not None:
-        png += chunk(b"tRNS", trns.astype(np.uint8).tobytes())
+        png += chunk(b"tRNS", bytes(trns) if isinstance(trns, (bytes, bytearray)) else trns.astype(np.uint8).tobytes())
     png += chunk(b"IDAT", zlib.compress(bytes(out), 6)) + chunk(b"IEND", b"")
     with open(path, "wb") as fh:
         fh.write(png)
@@ -112,6 +125,73 @@ def test_cli_reads_every_png_colour_type(native, tmp_path, ctype):
         want[..., 3] = arr[..., 1] if chans == 2 else 255
     got = _dump(native, path, tmp_path)
     assert np.array_equal(got, want[::-1])            # flipped like main.cpp:24
+
+
+@pytest.mark.parametrize("ctype,depth", [(0, 1), (0, 2), (0, 4), (3, 1), (3, 2), (3, 4)])
+@pytest.mark.parametrize("interlace", [False, True])
+def test_cli_reads_low_depth_png(native, tmp_path, ctype, depth, interlace):
+    rng = np.random.default_rng(ctype * 10 + depth + 100 * interlace)
+    h, w = 13, 19                                           # rows end mid-byte
+    vals = rng.integers(0, 1 << depth, (h, w))
+    path = str(tmp_path / "in.png")
+    want = np.full((h, w, 4), 255, np.uint8)
+    if ctype == 3:
+        pal = rng.integers(0, 256, ((1 << depth), 3))
+        trns = rng.integers(0, 256, max(1, (1 << depth) - 1))   # the last entry stays opaque
+        _png(path, vals, 3, depth, palette=pal, trns=trns, interlace=interlace)
+        want[..., :3] = pal[vals]
+        alpha = np.full(1 << depth, 255)
+        alpha[:len(trns)] = trns
+        want[..., 3] = alpha[vals]
+    else:
+        _png(path, vals, 0, depth, interlace=interlace)
+        want[..., :3] = (vals * (255 // ((1 << depth) - 1)))[..., None]
+    assert np.array_equal(_dump(native, path, tmp_path), want[::-1])
+    from astc_encoder_gb300 import image_io                 # the Python reader agrees
+    assert np.array_equal(image_io.load_image(path), want)
+
+
+@pytest.mark.parametrize("ctype,depth", [(0, 8), (2, 8), (3, 8), (4, 8), (6, 8), (2, 16), (6, 16)])
+@pytest.mark.parametrize("h,w", [(13, 11), (1, 1), (3, 9), (8, 8)])
+def test_cli_reads_interlaced_png(native, tmp_path, ctype, depth, h, w):
+    rng = np.random.default_rng(ctype + depth + h * w)
+    chans = {0: 1, 2: 3, 3: 1, 4: 2, 6: 4}[ctype]
+    vals = rng.integers(0, 256 if ctype == 3 else 1 << depth, (h, w, chans))
+    path = str(tmp_path / "in.png")
+    want = np.full((h, w, 4), 255, np.uint8)
+    hi = vals >> 8 if depth == 16 else vals
+    if ctype == 3:
+        pal = rng.integers(0, 256, (256, 3))
+        _png(path, vals, 3, 8, palette=pal, interlace=True)
+        want[..., :3] = pal[vals[..., 0]]
+    else:
+        _png(path, vals, ctype, depth, interlace=True)
+        want[..., :3] = hi[..., :3] if chans >= 3 else hi[..., :1]
+        if chans in (2, 4):
+            want[..., 3] = hi[..., -1]
+    assert np.array_equal(_dump(native, path, tmp_path), want[::-1])
+    from astc_encoder_gb300 import image_io
+    assert np.array_equal(image_io.load_image(path), want)
+
+
+@pytest.mark.parametrize("ctype,depth", [(0, 8), (0, 2), (2, 8), (2, 16)])
+def test_cli_png_transparency_key(native, tmp_path, ctype, depth):
+    """tRNS for grey and RGB images: pixels equal to the key colour (in the
+    image's own bit depth) are transparent."""
+    rng = np.random.default_rng(ctype + depth)
+    h, w, chans = 11, 14, 1 if ctype == 0 else 3
+    vals = rng.integers(0, 1 << depth, (h, w, chans))
+    key = vals[3, 4].copy()
+    vals[7, 2:9] = key
+    path = str(tmp_path / "in.png")
+    _png(path, vals, ctype, depth, trns=b"".join(struct.pack(">H", int(k)) for k in key))
+    want = np.full((h, w, 4), 255, np.uint8)
+    scale = (lambda v: v >> 8) if depth == 16 else (lambda v: v * (255 // ((1 << depth) - 1)))
+    want[..., :3] = scale(vals) if chans == 3 else scale(vals[..., :1])
+    want[..., 3] = np.where((vals == key).all(-1), 0, 255)
+    assert np.array_equal(_dump(native, path, tmp_path), want[::-1])
+    from astc_encoder_gb300 import image_io
+    assert np.array_equal(image_io.load_image(path), want)
 
 
 def test_cli_reads_16bit_png_and_pam(native, tmp_path):
@@ -689,6 +769,11 @@ def test_image_reader_under_sanitizers(tmp_path):
                                                  np.arange(48, dtype=np.uint8).reshape(16, 3) * 5,
                                                  transparent=3, interlace=True)),
                         ("n.hdr", lambda p: _hdr(p, np.dstack([arr, np.full(arr.shape[:2], 130, np.uint8)]))),
+                        ("o.png", lambda p: _png(p, (arr[..., 0] // 64).astype(np.int64), 3, 2,
+                                                 palette=np.arange(12).reshape(4, 3) * 20,
+                                                 trns=np.array([0, 128]), interlace=True)),
+                        ("q.png", lambda p: _png(p, arr.astype(np.int64) * 257, 2, 16,
+                                                 trns=b"\x00\x01\x00\x02\x00\x03", interlace=True)),
                         ("e.bmp", lambda p: _bmp(p, rgba, bitfields=True)),
                         ("f.bmp", lambda p: _bmp(p, arr)), ("g.tga", lambda p: _tga(p, rgba, rle=True)),
                         ("h.tga", lambda p: _tga(p, arr[..., 0], rle=True))]:
