@@ -448,9 +448,9 @@ bool decode_tga(const uint8_t* d, size_t n, Image& img, std::string& err) {
     return true;
 }
 
-// Windows BMP with a BITMAPINFOHEADER (or later): 24-bit BGR and 32-bit BGRA,
-// uncompressed or 32-bit with bit-field masks; rows bottom-up unless the
-// height is negative; 24-bit rows padded to 4 bytes.
+// Windows BMP with a BITMAPINFOHEADER (or later): 1/4/8-bit palettes, 16-bit
+// (5:5:5 or bit fields), 24-bit BGR and 32-bit BGRA (or bit fields); rows
+// bottom-up unless the height is negative, padded to 4 bytes.
 bool decode_bmp(const uint8_t* d, size_t n, Image& img, std::string& err) {
     auto u16 = [&](size_t o) { return (uint32_t)d[o] | ((uint32_t)d[o + 1] << 8); };
     auto u32 = [&](size_t o) { return u16(o) | (u16(o + 2) << 16); };
@@ -462,17 +462,31 @@ bool decode_bmp(const uint8_t* d, size_t n, Image& img, std::string& err) {
     const long long h64 = top_down ? -(long long)hraw : (long long)hraw;
     if (!dims_ok(w, h64, err)) return false;
     const int h = (int)h64;
-    if ((bpp != 24 && bpp != 32) || !(comp == 0 || (comp == 3 && bpp == 32))) {
-        err = "unsupported BMP format (24/32-bit uncompressed or 32-bit bit fields only)";
+    const bool pal = bpp == 1 || bpp == 4 || bpp == 8;
+    if (!(pal || bpp == 16 || bpp == 24 || bpp == 32) ||
+        !(comp == 0 || (comp == 3 && (bpp == 16 || bpp == 32)))) {
+        err = "unsupported BMP format (1/4/8/16/24/32-bit uncompressed or 16/32-bit bit fields)";
         return false;
     }
     uint32_t mask[4] = {0x00FF0000u, 0x0000FF00u, 0x000000FFu, bpp == 32 ? 0xFF000000u : 0u};
+    if (bpp == 16) { mask[0] = 0x7C00u; mask[1] = 0x03E0u; mask[2] = 0x001Fu; mask[3] = 0u; }   // 5:5:5
     if (comp == 3) {
         if (14 + 40 + 12 > n) { err = "BMP masks missing"; return false; }
         for (int c = 0; c < 3; ++c) mask[c] = u32(54 + 4 * c);
         mask[3] = hdr >= 56 && 14 + 56 <= n ? u32(54 + 12) : 0u;
     }
-    const size_t stride = ((size_t)w * (bpp / 8) + 3) & ~(size_t)3;
+    // palette: after the header (and the masks of a 40-byte header with bit fields), B G R x
+    uint8_t palette[256][3] = {};
+    int ncolors = 0;
+    if (pal) {
+        const uint32_t used = u32(46);
+        ncolors = used == 0 || used > (1u << bpp) ? 1 << bpp : (int)used;
+        const size_t at = 14 + (size_t)hdr;
+        if (at + 4 * (size_t)ncolors > n) { err = "BMP palette missing"; return false; }
+        for (int i = 0; i < ncolors; ++i)
+            for (int c = 0; c < 3; ++c) palette[i][c] = d[at + 4 * i + 2 - c];
+    }
+    const size_t stride = (((size_t)w * bpp + 31) / 32) * 4;
     if ((size_t)off + stride * h > n) { err = "BMP data too short"; return false; }
     img.width = w;
     img.height = h;
@@ -482,17 +496,23 @@ bool decode_bmp(const uint8_t* d, size_t n, Image& img, std::string& err) {
         int shift = 0;
         while (!((m >> shift) & 1)) ++shift;
         const uint32_t x = (v & m) >> shift, top = m >> shift;
-        return (uint8_t)(top == 255 ? x : (x * 255 + top / 2) / top);
+        return (uint8_t)(top == 255 ? x : (uint32_t)(((uint64_t)x * 255 + top / 2) / top));
     };
     for (int y = 0; y < h; ++y) {
         const uint8_t* s = d + off + (size_t)(top_down ? y : h - 1 - y) * stride;
         uint8_t* o = img.rgba.data() + (size_t)y * w * 4;
         for (int x = 0; x < w; ++x, o += 4) {
-            if (bpp == 24) {
+            if (pal) {
+                const size_t bit = (size_t)x * bpp;
+                const int idx = (s[bit >> 3] >> (8 - bpp - (bit & 7))) & ((1 << bpp) - 1);
+                if (idx >= ncolors) { err = "BMP palette index out of range"; return false; }
+                o[0] = palette[idx][0]; o[1] = palette[idx][1]; o[2] = palette[idx][2];
+            } else if (bpp == 24) {
                 o[0] = s[3 * x + 2]; o[1] = s[3 * x + 1]; o[2] = s[3 * x];
             } else {
-                const uint32_t v = (uint32_t)s[4 * x] | ((uint32_t)s[4 * x + 1] << 8) |
-                                   ((uint32_t)s[4 * x + 2] << 16) | ((uint32_t)s[4 * x + 3] << 24);
+                const uint32_t v = bpp == 16 ? (uint32_t)s[2 * x] | ((uint32_t)s[2 * x + 1] << 8)
+                                             : (uint32_t)s[4 * x] | ((uint32_t)s[4 * x + 1] << 8) |
+                                                   ((uint32_t)s[4 * x + 2] << 16) | ((uint32_t)s[4 * x + 3] << 24);
                 for (int c = 0; c < 4; ++c) o[c] = channel(v, mask[c]);
             }
         }

@@ -2,7 +2,7 @@
 // RFC 1950/1951; grey, grey+alpha, RGB, RGBA and palette at every bit depth;
 // 16-bit channels reduced to their high byte, 1/2/4-bit grey scaled to 8;
 // Adam7 interlacing; tRNS), Netpbm P5/P6/P7,
-// Windows BMP (24/32-bit, uncompressed or bit fields), Truevision TGA
+// Windows BMP (1/4/8-bit palettes, 16/24/32-bit, bit fields), Truevision TGA
 // (24/32-bit true colour and 8-bit grey, raw or run-length encoded) and
 // JPEG (8-bit grey or YCbCr, Huffman coded, baseline or progressive) and
 // Photoshop PSD (the merged image; 8/16-bit grey or RGB, optional alpha) and

@@ -5,7 +5,7 @@ vertically (main.cpp:24-25).  This module is a small self-contained reader:
 PNG (greyscale / grey+alpha / RGB / RGBA / palette at every bit depth the
 format allows, 16-bit channels reduced to their high byte, Adam7 interlacing,
 tRNS, all five row filters, zlib from the Python standard library), Netpbm
-P5/P6/P7, Windows BMP (24/32-bit, uncompressed or bit fields), Truevision
+P5/P6/P7, Windows BMP (1/4/8-bit palettes, 16/24/32-bit, bit fields), Truevision
 TGA (8-bit grey, 24/32-bit true colour, raw or run-length encoded),
 JPEG (8-bit grey or YCbCr, Huffman coded, baseline or progressive),
 Photoshop PSD (the merged image; 8/16-bit grey or RGB, optional alpha),
@@ -187,24 +187,39 @@ def load_bmp(path: str) -> np.ndarray:
         raise ValueError("not a BMP file")
     off, hdr = struct.unpack_from("<I", data, 10)[0], struct.unpack_from("<I", data, 14)[0]
     w, hraw, _, bpp, comp = struct.unpack_from("<iiHHI", data, 18)
-    if hdr < 40 or w <= 0 or hraw == 0 or bpp not in (24, 32) or not (comp == 0 or (comp == 3 and bpp == 32)):
-        raise ValueError("unsupported BMP format (24/32-bit uncompressed or 32-bit bit fields only)")
+    pal = bpp in (1, 4, 8)
+    if hdr < 40 or w <= 0 or hraw == 0 or not (pal or bpp in (16, 24, 32)) or \
+            not (comp == 0 or (comp == 3 and bpp in (16, 32))):
+        raise ValueError("unsupported BMP format (1/4/8/16/24/32-bit uncompressed or 16/32-bit bit fields)")
     h = abs(hraw)
     masks = [0x00FF0000, 0x0000FF00, 0x000000FF, 0xFF000000 if bpp == 32 else 0]
+    if bpp == 16:
+        masks = [0x7C00, 0x03E0, 0x001F, 0]
     if comp == 3:
         masks[:3] = struct.unpack_from("<III", data, 54)
         masks[3] = struct.unpack_from("<I", data, 66)[0] if hdr >= 56 else 0
-    c = bpp // 8
-    stride = (w * c + 3) & ~3
-    rows = np.frombuffer(data, np.uint8, stride * h, off).reshape(h, stride)[:, :w * c].reshape(h, w, c)
+    stride = ((w * bpp + 31) // 32) * 4
+    rows = np.frombuffer(data, np.uint8, stride * h, off).reshape(h, stride)
     if hraw > 0:
         rows = rows[::-1]
     out = np.full((h, w, 4), 255, np.uint8)
-    if bpp == 24:
-        out[..., :3] = rows[..., [2, 1, 0]]
+    if pal:
+        used = struct.unpack_from("<I", data, 46)[0]
+        n = 1 << bpp if used == 0 or used > 1 << bpp else used
+        table = np.frombuffer(data, np.uint8, 4 * n, 14 + hdr).reshape(n, 4)[:, [2, 1, 0]]
+        bits = np.unpackbits(rows, axis=1)[:, :w * bpp].reshape(h, w, bpp).astype(np.int64)
+        idx = (bits << np.arange(bpp - 1, -1, -1)).sum(-1)
+        if idx.max() >= n:
+            raise ValueError("BMP palette index out of range")
+        out[..., :3] = table[idx]
         return out
-    v = rows.astype(np.uint32)
-    v = v[..., 0] | (v[..., 1] << 8) | (v[..., 2] << 16) | (v[..., 3] << 24)
+    c = bpp // 8
+    px = rows[:, :w * c].reshape(h, w, c)
+    if bpp == 24:
+        out[..., :3] = px[..., [2, 1, 0]]
+        return out
+    v = px.astype(np.uint64)
+    v = sum(v[..., i] << (8 * i) for i in range(c))
     for ch, m in enumerate(masks):
         if not m:
             continue

@@ -3,7 +3,8 @@
 CPU tests exercise its image reader through --dump-rgba (no GPU): PNGs of
 every colour type and all five row filters written here with zlib, PAM, TGA
 (grey / BGR / BGRA, raw and run-length encoded, either row order) and BMP
-(24-bit padded rows, 32-bit, bit fields, either row order), and baseline
+(1/4/8-bit palettes, 16-bit 5:5:5 and bit fields, 24-bit padded rows, 32-bit,
+bit fields, either row order), and baseline
 JPEG (grey and YCbCr at 4:4:4 / 4:2:2 / 4:4:0 / 4:2:0, restart intervals,
 8- and 16-bit quantisation tables; baseline with one interleaved scan or one
 scan per component, and progressive with spectral selection, successive
@@ -259,6 +260,74 @@ def _bmp(path, arr, top_down=False, bitfields=False):
                        len(data), 2835, 2835, 0, 0) + masks
     with open(path, "wb") as fh:
         fh.write(b"BM" + struct.pack("<IHHI", off + len(data), 0, 0, off) + info + bytes(data))
+
+
+def _bmp_indexed(path, idx, palette, bpp, used=0, top_down=False):
+    """Writes a 1/4/8-bit palette BMP (indices MSB-first, rows padded to 4 bytes)."""
+    h, w = idx.shape
+    stride = ((w * bpp + 31) // 32) * 4
+    rows = idx if top_down else idx[::-1]
+    data = bytearray()
+    for r in rows:
+        bits = ((r[:, None] >> np.arange(bpp - 1, -1, -1)) & 1).astype(np.uint8).reshape(-1)
+        line = np.packbits(bits).tobytes()
+        data += line + b"\0" * (stride - len(line))
+    n = used or (1 << bpp)
+    pal = b"".join(bytes([int(c[2]), int(c[1]), int(c[0]), 0]) for c in palette[:n])
+    off = 14 + 40 + len(pal)
+    info = struct.pack("<IiiHHIIiiII", 40, w, -h if top_down else h, 1, bpp, 0, len(data), 2835, 2835, used, 0)
+    with open(path, "wb") as fh:
+        fh.write(b"BM" + struct.pack("<IHHI", off + len(data), 0, 0, off) + info + pal + bytes(data))
+
+
+def _bmp16(path, v, masks=None):
+    """Writes a 16-bit BMP of raw 16-bit pixel values (5:5:5, or bit fields)."""
+    h, w = v.shape
+    stride = ((w * 16 + 31) // 32) * 4
+    data = bytearray()
+    for r in v[::-1]:
+        line = r.astype("<u2").tobytes()
+        data += line + b"\0" * (stride - len(line))
+    extra = struct.pack("<III", *masks) if masks else b""
+    off = 14 + 40 + len(extra)
+    info = struct.pack("<IiiHHIIiiII", 40, w, h, 1, 16, 3 if masks else 0, len(data), 2835, 2835, 0, 0) + extra
+    with open(path, "wb") as fh:
+        fh.write(b"BM" + struct.pack("<IHHI", off + len(data), 0, 0, off) + info + bytes(data))
+
+
+@pytest.mark.parametrize("bpp,used,top_down", [(1, 0, False), (4, 0, True), (4, 11, False), (8, 0, False),
+                                               (8, 200, True)])
+def test_cli_reads_palette_bmp(native, tmp_path, bpp, used, top_down):
+    rng = np.random.default_rng(bpp * 7 + used)
+    h, w = 13, 21                                           # odd widths: padded, partial bytes
+    n = used or (1 << bpp)
+    palette = rng.integers(0, 256, (n, 3))
+    idx = rng.integers(0, n, (h, w))
+    path = str(tmp_path / "in.bmp")
+    _bmp_indexed(path, idx, palette, bpp, used, top_down)
+    want = np.full((h, w, 4), 255, np.uint8)
+    want[..., :3] = palette[idx]
+    assert np.array_equal(_dump(native, path, tmp_path), want[::-1])
+    from astc_encoder_gb300 import image_io
+    assert np.array_equal(image_io.load_image(path), want)
+
+
+@pytest.mark.parametrize("masks", [None, (0xF800, 0x07E0, 0x001F)])
+def test_cli_reads_16bit_bmp(native, tmp_path, masks):
+    rng = np.random.default_rng(16 + (masks is not None))
+    h, w = 9, 15
+    v = rng.integers(0, 1 << 16, (h, w))
+    path = str(tmp_path / "in.bmp")
+    _bmp16(path, v, masks)
+    want = np.full((h, w, 4), 255, np.uint8)
+    for c, m in enumerate(masks or (0x7C00, 0x03E0, 0x001F)):
+        shift = (m & -m).bit_length() - 1
+        top = m >> shift
+        x = (v & m) >> shift
+        want[..., c] = (x * 255 + top // 2) // top
+    assert np.array_equal(_dump(native, path, tmp_path), want[::-1])
+    from astc_encoder_gb300 import image_io
+    assert np.array_equal(image_io.load_image(path), want)
 
 
 @pytest.mark.parametrize("channels", [1, 3, 4])
@@ -774,6 +843,9 @@ def test_image_reader_under_sanitizers(tmp_path):
                                                  trns=np.array([0, 128]), interlace=True)),
                         ("q.png", lambda p: _png(p, arr.astype(np.int64) * 257, 2, 16,
                                                  trns=b"\x00\x01\x00\x02\x00\x03", interlace=True)),
+                        ("r.bmp", lambda p: _bmp_indexed(p, (arr[..., 1] // 16).astype(np.int64),
+                                                         np.arange(48).reshape(16, 3) * 5, 4)),
+                        ("s.bmp", lambda p: _bmp16(p, arr[..., 0].astype(np.int64) * 200, (0xF800, 0x07E0, 0x1F))),
                         ("e.bmp", lambda p: _bmp(p, rgba, bitfields=True)),
                         ("f.bmp", lambda p: _bmp(p, arr)), ("g.tga", lambda p: _tga(p, rgba, rle=True)),
                         ("h.tga", lambda p: _tga(p, arr[..., 0], rle=True))]:
