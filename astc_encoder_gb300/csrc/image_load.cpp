@@ -389,25 +389,55 @@ bool decode_pnm(const uint8_t* d, size_t n, Image& img, std::string& err) {
     return true;
 }
 
-// Truevision TGA: image types 2 / 10 (true colour, 24 or 32 bit BGR(A)), 3 / 11
-// (8-bit grey), raw or run-length encoded; bit 5 of the descriptor says the
-// rows run top-down, otherwise bottom-up.
+// Truevision TGA: image types 1 / 9 (8-bit indices into a 15/16/24/32-bit
+// colour map), 2 / 10 (true colour: 15/16-bit x RRRRR GGGGG BBBBB without
+// alpha, 24 or 32 bit BGR(A)), 3 / 11 (8-bit grey), raw or run-length
+// encoded; bit 5 of the descriptor says the rows run top-down, otherwise
+// bottom-up.
 bool decode_tga(const uint8_t* d, size_t n, Image& img, std::string& err) {
     if (n < 18) { err = "TGA header too short"; return false; }
     const int idlen = d[0], cmap = d[1], type = d[2];
+    const int cfirst = d[3] | (d[4] << 8), clen = d[5] | (d[6] << 8), cbits = d[7];
     const int w = d[12] | (d[13] << 8), h = d[14] | (d[15] << 8), bpp = d[16], desc = d[17];
-    const bool rle = type == 10 || type == 11, grey = type == 3 || type == 11;
-    if (cmap != 0 || !(type == 2 || type == 3 || type == 10 || type == 11)) {
-        err = "unsupported TGA type (colour-mapped or not an image)";
+    const bool rle = type >= 9, grey = type == 3 || type == 11, mapped = type == 1 || type == 9;
+    if (!(type == 1 || type == 2 || type == 3 || type == 9 || type == 10 || type == 11) || (mapped && cmap != 1)) {
+        err = "unsupported TGA type";
         return false;
     }
-    if (grey ? bpp != 8 : (bpp != 24 && bpp != 32)) {
+    if (grey ? bpp != 8 : mapped ? bpp != 8 : (bpp != 15 && bpp != 16 && bpp != 24 && bpp != 32)) {
         err = "unsupported TGA pixel depth";
         return false;
     }
     if (!dims_ok(w, h, err)) return false;
-    const int px = bpp / 8;
+    // 15/16-bit colours: x RRRRR GGGGG BBBBB, each channel x 255 / 31 (no alpha)
+    auto rgb16 = [](const uint8_t* q, uint8_t* o) {
+        const int v = q[0] | (q[1] << 8);
+        o[0] = (uint8_t)(((v >> 10) & 31) * 255 / 31);
+        o[1] = (uint8_t)(((v >> 5) & 31) * 255 / 31);
+        o[2] = (uint8_t)((v & 31) * 255 / 31);
+        o[3] = 255;
+    };
+    const int px = (bpp + 7) / 8;
     size_t pos = 18 + (size_t)idlen;
+    // colour map (present in any type when cmap == 1): clen entries of cbits
+    std::vector<uint8_t> colours;                        // RGBA per entry
+    if (cmap == 1) {
+        const int cb = (cbits + 7) / 8;
+        if (!(cbits == 15 || cbits == 16 || cbits == 24 || cbits == 32)) { err = "bad TGA colour map"; return false; }
+        if (pos + (size_t)clen * cb > n) { err = "TGA colour map truncated"; return false; }
+        colours.assign((size_t)clen * 4, 255);
+        for (int i = 0; i < clen; ++i) {
+            const uint8_t* q = d + pos + (size_t)i * cb;
+            uint8_t* o = colours.data() + (size_t)i * 4;
+            if (cb == 2) {
+                rgb16(q, o);
+            } else {
+                o[0] = q[2]; o[1] = q[1]; o[2] = q[0];
+                if (cb == 4) o[3] = q[3];
+            }
+        }
+        pos += (size_t)clen * cb;
+    }
     // raw data holds every byte; a run-length packet of 1 + px bytes at most 128 pixels
     if ((size_t)w * h * px > (rle ? 128 * n : n)) { err = "TGA data too short"; return false; }
     std::vector<uint8_t> raw((size_t)w * h * px);
@@ -441,6 +471,13 @@ bool decode_tga(const uint8_t* d, size_t n, Image& img, std::string& err) {
         uint8_t* o = img.rgba.data() + (size_t)y * w * 4;
         for (int x = 0; x < w; ++x, s += px, o += 4) {
             if (grey) { o[0] = o[1] = o[2] = s[0]; continue; }
+            if (mapped) {
+                const int i = s[0] - cfirst;
+                if (i < 0 || i >= clen) { err = "TGA colour index out of range"; return false; }
+                memcpy(o, colours.data() + (size_t)i * 4, 4);
+                continue;
+            }
+            if (px == 2) { rgb16(s, o); continue; }
             o[0] = s[2]; o[1] = s[1]; o[2] = s[0];
             if (px == 4) o[3] = s[3];
         }

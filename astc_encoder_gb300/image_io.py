@@ -6,7 +6,8 @@ PNG (greyscale / grey+alpha / RGB / RGBA / palette at every bit depth the
 format allows, 16-bit channels reduced to their high byte, Adam7 interlacing,
 tRNS, all five row filters, zlib from the Python standard library), Netpbm
 P5/P6/P7, Windows BMP (1/4/8-bit palettes, 16/24/32-bit, bit fields), Truevision
-TGA (8-bit grey, 24/32-bit true colour, raw or run-length encoded),
+TGA (colour-mapped, 8-bit grey, 15/16/24/32-bit true colour, raw or
+run-length encoded),
 JPEG (8-bit grey or YCbCr, Huffman coded, baseline or progressive),
 Photoshop PSD (the merged image; 8/16-bit grey or RGB, optional alpha),
 GIF (the first image; transparency as (0, 0, 0, 0)) and Radiance HDR (taken
@@ -230,22 +231,46 @@ def load_bmp(path: str) -> np.ndarray:
     return out
 
 
+def _rgb16(v):
+    """15/16-bit TGA colours x RRRRR GGGGG BBBBB -> RGBA (x 255 / 31, alpha 255)."""
+    v = v.astype(np.int64)
+    out = np.full(v.shape + (4,), 255, np.uint8)
+    for c, sh in enumerate((10, 5, 0)):
+        out[..., c] = ((v >> sh) & 31) * 255 // 31
+    return out
+
+
 def load_tga(path: str) -> np.ndarray:
     with open(path, "rb") as fh:
         data = fh.read()
     if len(data) < 18:
         raise ValueError("TGA header too short")
     idlen, cmap, itype = data[0], data[1], data[2]
+    cfirst, clen, cbits = struct.unpack_from("<HHB", data, 3)
     w, h = struct.unpack_from("<HH", data, 12)
     bpp, desc = data[16], data[17]
-    grey = itype in (3, 11)
-    if cmap != 0 or itype not in (2, 3, 10, 11) or w == 0 or h == 0 or bpp != (8 if grey else bpp) or \
-            (not grey and bpp not in (24, 32)):
+    grey, mapped = itype in (3, 11), itype in (1, 9)
+    if itype not in (1, 2, 3, 9, 10, 11) or (mapped and cmap != 1) or w == 0 or h == 0 or \
+            not (bpp == 8 if (grey or mapped) else bpp in (15, 16, 24, 32)):
         raise ValueError("unsupported TGA file")
-    px = bpp // 8
+    px = (bpp + 7) // 8
     pos = 18 + idlen
+    colours = None
+    if cmap == 1:
+        cb = (cbits + 7) // 8
+        if cbits not in (15, 16, 24, 32):
+            raise ValueError("bad TGA colour map")
+        table = np.frombuffer(data, np.uint8, clen * cb, pos).reshape(clen, cb)
+        pos += clen * cb
+        if cb == 2:
+            colours = _rgb16(table[:, 0].astype(np.int64) | (table[:, 1].astype(np.int64) << 8))
+        else:
+            colours = np.full((clen, 4), 255, np.uint8)
+            colours[:, :3] = table[:, [2, 1, 0]]
+            if cb == 4:
+                colours[:, 3] = table[:, 3]
     n = w * h * px
-    if itype in (2, 3):
+    if itype in (1, 2, 3):
         raw = np.frombuffer(data, np.uint8, n, pos)
     else:
         buf = bytearray()
@@ -266,6 +291,13 @@ def load_tga(path: str) -> np.ndarray:
     out = np.full((h, w, 4), 255, np.uint8)
     if grey:
         out[..., :3] = raw[..., :1]
+    elif mapped:
+        idx = raw[..., 0].astype(np.int64) - cfirst
+        if idx.min() < 0 or idx.max() >= clen:
+            raise ValueError("TGA colour index out of range")
+        out[:] = colours[idx]
+    elif px == 2:
+        out[:] = _rgb16(raw[..., 0].astype(np.int64) | (raw[..., 1].astype(np.int64) << 8))
     else:
         out[..., :3] = raw[..., [2, 1, 0]]
         if px == 4:

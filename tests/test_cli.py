@@ -2,7 +2,8 @@
 
 CPU tests exercise its image reader through --dump-rgba (no GPU): PNGs of
 every colour type and all five row filters written here with zlib, PAM, TGA
-(grey / BGR / BGRA, raw and run-length encoded, either row order) and BMP
+(grey / BGR / BGRA / 16-bit / colour-mapped, raw and run-length encoded,
+either row order) and BMP
 (1/4/8-bit palettes, 16-bit 5:5:5 and bit fields, 24-bit padded rows, 32-bit,
 bit fields, either row order), and baseline
 JPEG (grey and YCbCr at 4:4:4 / 4:2:2 / 4:4:0 / 4:2:0, restart intervals,
@@ -260,6 +261,66 @@ def _bmp(path, arr, top_down=False, bitfields=False):
                        len(data), 2835, 2835, 0, 0) + masks
     with open(path, "wb") as fh:
         fh.write(b"BM" + struct.pack("<IHHI", off + len(data), 0, 0, off) + info + bytes(data))
+
+
+def _tga_mapped(path, idx, colours, cbits, first=0, rle=False):
+    """Writes a colour-mapped TGA: 8-bit indices (offset by `first`) into a
+    15/16/24/32-bit colour map (`colours` holds the stored entries)."""
+    h, w = idx.shape
+    cb = (cbits + 7) // 8
+    head = struct.pack("<BBBHHBHHHHBB", 0, 1, 9 if rle else 1, first, len(colours), cbits, 0, 0, w, h, 8, 0x20)
+    cmap = b"".join(bytes(int(x) for x in c[:cb]) for c in colours)
+    body = bytearray()
+    for r in (idx + first).astype(np.uint8):
+        if rle:
+            for v in r:                                     # one-pixel packets: raw (count 1)
+                body += bytes([0, int(v)])
+        else:
+            body += r.tobytes()
+    with open(path, "wb") as fh:
+        fh.write(head + cmap + bytes(body))
+
+
+def _tga16(path, v):
+    h, w = v.shape
+    head = struct.pack("<BBBHHBHHHHBB", 0, 0, 2, 0, 0, 0, 0, 0, w, h, 16, 0x20)
+    with open(path, "wb") as fh:
+        fh.write(head + v.astype("<u2").tobytes())
+
+
+@pytest.mark.parametrize("cbits,rle,first", [(24, False, 0), (32, True, 5), (16, False, 2), (15, True, 0)])
+def test_cli_reads_colour_mapped_tga(native, tmp_path, cbits, rle, first):
+    rng = np.random.default_rng(cbits + rle)
+    h, w, n = 11, 17, 40
+    cb = (cbits + 7) // 8
+    stored = rng.integers(0, 256, (n, cb))
+    idx = rng.integers(0, n, (h, w))
+    path = str(tmp_path / "in.tga")
+    _tga_mapped(path, idx, stored, cbits, first, rle)
+    if cb == 2:
+        v = stored[:, 0] | (stored[:, 1] << 8)
+        table = np.stack([((v >> s) & 31) * 255 // 31 for s in (10, 5, 0)] + [np.full(n, 255)], -1)
+    else:
+        table = np.full((n, 4), 255)
+        table[:, :3] = stored[:, [2, 1, 0]]
+        if cb == 4:
+            table[:, 3] = stored[:, 3]
+    want = table[idx].astype(np.uint8)
+    assert np.array_equal(_dump(native, path, tmp_path), want[::-1])
+    from astc_encoder_gb300 import image_io
+    assert np.array_equal(image_io.load_image(path), want)
+
+
+def test_cli_reads_16bit_tga(native, tmp_path):
+    v = np.random.default_rng(9).integers(0, 1 << 16, (7, 13))
+    path = str(tmp_path / "in.tga")
+    _tga16(path, v)
+    want = np.full((7, 13, 4), 255, np.uint8)
+    for c, sh in enumerate((10, 5, 0)):
+        want[..., c] = ((v >> sh) & 31) * 255 // 31
+    assert np.array_equal(_dump(native, path, tmp_path), want[::-1])
+    from astc_encoder_gb300 import image_io
+    assert np.array_equal(image_io.load_image(path), want)
 
 
 def _bmp_indexed(path, idx, palette, bpp, used=0, top_down=False):
@@ -843,6 +904,8 @@ def test_image_reader_under_sanitizers(tmp_path):
                                                  trns=np.array([0, 128]), interlace=True)),
                         ("q.png", lambda p: _png(p, arr.astype(np.int64) * 257, 2, 16,
                                                  trns=b"\x00\x01\x00\x02\x00\x03", interlace=True)),
+                        ("t.tga", lambda p: _tga_mapped(p, (arr[..., 2] // 8).astype(np.int64),
+                                                        np.arange(96).reshape(32, 3), 24, 3, True)),
                         ("r.bmp", lambda p: _bmp_indexed(p, (arr[..., 1] // 16).astype(np.int64),
                                                          np.arange(48).reshape(16, 3) * 5, 4)),
                         ("s.bmp", lambda p: _bmp16(p, arr[..., 0].astype(np.int64) * 200, (0xF800, 0x07E0, 0x1F))),
