@@ -1,13 +1,12 @@
-// image_load.h -- image reader for the command line tool: PNG (own inflate,
-// RFC 1950/1951; grey, grey+alpha, RGB, RGBA and palette at every bit depth;
-// 16-bit channels reduced to their high byte, 1/2/4-bit grey scaled to 8;
-// Adam7 interlacing; tRNS), Netpbm P5/P6/P7,
-// Windows BMP (1/4/8-bit palettes, 16/24/32-bit, bit fields), Truevision TGA
-// (24/32-bit true colour and 8-bit grey, raw or run-length encoded) and
-// JPEG (8-bit grey or YCbCr, Huffman coded, baseline or progressive) and
-// Photoshop PSD (the merged image; 8/16-bit grey or RGB, optional alpha) and
-// GIF (the first image, transparency as (0, 0, 0, 0)) and Radiance HDR
-// (RGBE, taken to 8 bits with gamma 1/2.2).
+// image_load.h -- image reader for the command line tool.  PNG (own inflate,
+// RFC 1950/1951; every colour type and bit depth, 16-bit channels reduced to
+// their high byte, 1/2/4-bit grey scaled to 8; Adam7; tRNS), JPEG (8-bit grey
+// or YCbCr, Huffman coded, baseline or progressive), Photoshop PSD (the merged
+// image; 8/16-bit grey or RGB, optional alpha), GIF (the first image;
+// transparency as (0, 0, 0, 0)), Radiance HDR (RGBE, taken to 8 bits with
+// gamma 1/2.2), Windows BMP (1/4/8-bit palettes, 16/24/32-bit, bit fields),
+// Truevision TGA (colour-mapped, 15/16/24/32-bit true colour, 8-bit grey; raw
+// or run-length) and Netpbm P5/P6/P7.
 // Output is always RGBA8, row 0 first (the caller flips for the reference's
 // orientation, main.cpp:24).  Written for this project; the reference uses
 // the third-party stb_image for the same job.
