@@ -1,5 +1,5 @@
-// image_load.cpp -- PNG / JPEG / PSD / GIF / HDR / Netpbm / BMP / TGA reader
-// for the command line tool.
+// image_load.cpp -- PNG / JPEG / PSD / GIF / HDR / PIC / Netpbm / BMP / TGA
+// reader for the command line tool.
 // Inflate follows RFC 1951 (stored, fixed and dynamic Huffman blocks,
 // canonical codes decoded one bit at a time); the zlib wrapper RFC 1950;
 // PNG chunk layout, filters 0-4, colour types, bit depths, Adam7 and tRNS the
@@ -1291,6 +1291,87 @@ bool decode_hdr(const uint8_t* d, size_t n, Image& img, std::string& err) {
     return true;
 }
 
+// Softimage PIC: a 104-byte header (magic 0x5380F634, "PICT" at 88, width
+// and height big-endian at 92), chained channel packets (8-bit channels, a
+// mask of red 0x80, green 0x40, blue 0x20, alpha 0x10; uncompressed, pure
+// run-length or mixed run-length), then each scanline top to bottom, packet
+// by packet.  Channels no packet carries are 255.
+bool decode_pic(const uint8_t* d, size_t n, Image& img, std::string& err) {
+    if (n < 104 || !(d[0] == 0x53 && d[1] == 0x80 && d[2] == 0xF6 && d[3] == 0x34) || memcmp(d + 88, "PICT", 4) != 0) {
+        err = "not a Softimage PIC file";
+        return false;
+    }
+    const int w = (d[92] << 8) | d[93], h = (d[94] << 8) | d[95];
+    if (!dims_ok(w, h, err)) return false;
+    size_t pos = 104;
+    struct Packet { int type, mask; };
+    std::vector<Packet> packets;
+    int all = 0;
+    for (bool chained = true; chained;) {
+        if (pos + 4 > n || packets.size() >= 10) { err = "bad PIC packets"; return false; }
+        chained = d[pos] != 0;
+        if (d[pos + 1] != 8 || d[pos + 2] > 2) { err = "PIC packet not read (8-bit channels are)"; return false; }
+        packets.push_back({d[pos + 2], d[pos + 3]});
+        all |= d[pos + 3];
+        pos += 4;
+    }
+    if (!(all & 0xF0)) { err = "PIC without colour channels"; return false; }
+    // every pixel of every packet needs a byte at least once per 65535 pixels
+    if ((size_t)w * h > 65535ull * (n - pos) + 65535) { err = "PIC data too short for its size"; return false; }
+    img.width = w;
+    img.height = h;
+    img.rgba.assign((size_t)w * h * 4, 255);
+    auto put = [&](uint8_t* px, int mask, const uint8_t* vals) {   // vals in channel order R G B A
+        int k = 0;
+        for (int c = 0; c < 4; ++c)
+            if (mask & (0x80 >> c)) px[c] = vals[k++];
+    };
+    for (int y = 0; y < h; ++y) {
+        uint8_t* row = img.rgba.data() + (size_t)y * w * 4;
+        for (const Packet& p : packets) {
+            int nch = 0;
+            for (int c = 0; c < 4; ++c) nch += (p.mask >> (7 - c)) & 1;
+            uint8_t vals[4];
+            auto read_vals = [&]() {
+                if (pos + nch > n) return false;
+                memcpy(vals, d + pos, nch);
+                pos += nch;
+                return true;
+            };
+            for (int x = 0; x < w;) {
+                int count = 0;
+                bool literal = false;
+                if (p.type == 0) {
+                    count = 1;
+                    literal = true;
+                } else {
+                    if (pos >= n) { err = "PIC data too short"; return false; }
+                    const int c = d[pos++];
+                    if (p.type == 1) {
+                        count = c;
+                    } else if (c < 128) {
+                        count = c + 1;
+                        literal = true;
+                    } else if (c == 128) {
+                        if (pos + 2 > n) { err = "PIC data too short"; return false; }
+                        count = (d[pos] << 8) | d[pos + 1];
+                        pos += 2;
+                    } else {
+                        count = c - 127;
+                    }
+                }
+                if (count <= 0 || x + count > w) { err = "bad PIC run"; return false; }
+                if (!literal && !read_vals()) { err = "PIC data too short"; return false; }
+                for (int i = 0; i < count; ++i, ++x) {
+                    if (literal && !read_vals()) { err = "PIC data too short"; return false; }
+                    put(row + (size_t)x * 4, p.mask, vals);
+                }
+            }
+        }
+    }
+    return true;
+}
+
 bool load_image(const std::string& path, Image& img, std::string& err) {
     FILE* f = fopen(path.c_str(), "rb");
     if (!f) { err = "cannot open " + path; return false; }
@@ -1308,13 +1389,15 @@ bool load_image(const std::string& path, Image& img, std::string& err) {
     if (data.size() >= 4 && memcmp(data.data(), "8BPS", 4) == 0) return decode_psd(data.data(), data.size(), img, err);
     if (data.size() >= 4 && memcmp(data.data(), "GIF8", 4) == 0) return decode_gif(data.data(), data.size(), img, err);
     if (data.size() >= 6 && memcmp(data.data(), "#?RGBE", 6) == 0) return decode_hdr(data.data(), data.size(), img, err);
+    if (data.size() >= 4 && data[0] == 0x53 && data[1] == 0x80 && data[2] == 0xF6 && data[3] == 0x34)
+        return decode_pic(data.data(), data.size(), img, err);
     if (data.size() >= 10 && memcmp(data.data(), "#?RADIANCE", 10) == 0)
         return decode_hdr(data.data(), data.size(), img, err);
     const size_t dot = path.find_last_of('.');
     std::string ext = dot == std::string::npos ? "" : path.substr(dot + 1);
     for (auto& c : ext) c = (char)tolower((unsigned char)c);
     if (ext == "tga") return decode_tga(data.data(), data.size(), img, err);   // TGA has no magic number
-    err = "unsupported image format (PNG, JPEG, PSD, GIF, HDR, PAM/PPM/PGM, BMP and TGA are read)";
+    err = "unsupported image format (PNG, JPEG, PSD, GIF, HDR, PIC, PAM/PPM/PGM, BMP and TGA are read)";
     return false;
 }
 

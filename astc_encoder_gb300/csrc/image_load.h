@@ -6,7 +6,7 @@
 // transparency as (0, 0, 0, 0)), Radiance HDR (RGBE, taken to 8 bits with
 // gamma 1/2.2), Windows BMP (1/4/8-bit palettes, 16/24/32-bit, bit fields),
 // Truevision TGA (colour-mapped, 15/16/24/32-bit true colour, 8-bit grey; raw
-// or run-length) and Netpbm P5/P6/P7.
+// or run-length), Softimage PIC and Netpbm P5/P6/P7.
 // Output is always RGBA8, row 0 first (the caller flips for the reference's
 // orientation, main.cpp:24).  Written for this project; the reference uses
 // the third-party stb_image for the same job.
@@ -33,6 +33,7 @@ bool decode_jpeg(const uint8_t* data, size_t size, Image& out, std::string& err)
 bool decode_psd(const uint8_t* data, size_t size, Image& out, std::string& err);
 bool decode_gif(const uint8_t* data, size_t size, Image& out, std::string& err);
 bool decode_hdr(const uint8_t* data, size_t size, Image& out, std::string& err);
+bool decode_pic(const uint8_t* data, size_t size, Image& out, std::string& err);
 // zlib stream (2-byte header, deflate blocks, Adler-32) -> raw bytes.
 bool zlib_inflate(const uint8_t* data, size_t size, std::vector<uint8_t>& out, std::string& err);
 // Writes RGBA8 as a P7 (PAM) file.

@@ -1,4 +1,4 @@
-"""Image loading for the encoder's command line (PNG, JPEG, PSD, GIF, HDR, PAM/PPM/PGM, BMP, TGA).
+"""Image loading for the encoder's command line (PNG, JPEG, PSD, GIF, HDR, PIC, PNM, BMP, TGA).
 
 The reference loads images with stb_image forced to RGBA and flipped
 vertically (main.cpp:24-25).  This module is a small self-contained reader:
@@ -10,8 +10,8 @@ TGA (colour-mapped, 8-bit grey, 15/16/24/32-bit true colour, raw or
 run-length encoded),
 JPEG (8-bit grey or YCbCr, Huffman coded, baseline or progressive),
 Photoshop PSD (the merged image; 8/16-bit grey or RGB, optional alpha),
-GIF (the first image; transparency as (0, 0, 0, 0)) and Radiance HDR (taken
-to 8 bits with gamma 1/2.2) -- the
+GIF (the first image; transparency as (0, 0, 0, 0)), Radiance HDR (taken
+to 8 bits with gamma 1/2.2) and Softimage PIC -- the
 same formats as the C++ reader of the command line tool.  It always returns
 a (H, W, 4) uint8 array, row 0 first; the caller flips when it wants the
 reference's orientation.
@@ -854,6 +854,55 @@ def load_hdr(path: str) -> np.ndarray:
     return out
 
 
+def load_pic(path: str) -> np.ndarray:
+    """Softimage PIC (8-bit channel packets; uncompressed, pure or mixed
+    run-length), as the command line tool's reader."""
+    with open(path, "rb") as fh:
+        d = fh.read()
+    if len(d) < 104 or d[:4] != b"\x53\x80\xf6\x34" or d[88:92] != b"PICT":
+        raise ValueError("not a Softimage PIC file")
+    w, h = struct.unpack_from(">HH", d, 92)
+    pos, packets, chained = 104, [], True
+    while chained:
+        chained, size, typ, mask = d[pos:pos + 4]
+        if size != 8 or typ > 2:
+            raise ValueError("PIC packet not read (8-bit channels are)")
+        packets.append((typ, mask))
+        pos += 4
+    out = np.full((h, w, 4), 255, np.uint8)
+    for y in range(h):
+        for typ, mask in packets:
+            chans = [c for c in range(4) if mask & (0x80 >> c)]
+            nch = len(chans)
+            x = 0
+            while x < w:
+                if typ == 0:
+                    count, literal = 1, True
+                else:
+                    c = d[pos]
+                    pos += 1
+                    if typ == 1:
+                        count, literal = c, False
+                    elif c < 128:
+                        count, literal = c + 1, True
+                    elif c == 128:
+                        count, literal = struct.unpack_from(">H", d, pos)[0], False
+                        pos += 2
+                    else:
+                        count, literal = c - 127, False
+                if count <= 0 or x + count > w:
+                    raise ValueError("bad PIC run")
+                seg = out[y, x:x + count]
+                if literal:
+                    seg[:, chans] = np.frombuffer(d, np.uint8, count * nch, pos).reshape(count, nch)
+                    pos += count * nch
+                else:
+                    seg[:, chans] = np.frombuffer(d, np.uint8, nch, pos)
+                    pos += nch
+                x += count
+    return out
+
+
 def load_image(path: str) -> np.ndarray:
     with open(path, "rb") as fh:
         head = fh.read(8)
@@ -871,6 +920,8 @@ def load_image(path: str) -> np.ndarray:
         return load_gif(path)
     if head[:6] == b"#?RGBE" or head[:8] == b"#?RADIAN":
         return load_hdr(path)
+    if head[:4] == b"\x53\x80\xf6\x34":
+        return load_pic(path)
     if path.lower().endswith(".tga"):                  # TGA has no magic number
         return load_tga(path)
-    raise ValueError("unsupported image format (PNG, JPEG, PSD, GIF, HDR, PAM/PPM/PGM, BMP and TGA are read)")
+    raise ValueError("unsupported image format (PNG, JPEG, PSD, GIF, HDR, PIC, PAM/PPM/PGM, BMP and TGA are read)")

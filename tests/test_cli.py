@@ -14,7 +14,8 @@ Huffman tables built from the data, plus a third-party JPEG where one is
 installed, PSD merged images (grey / RGB, alpha, 8 / 16 bits, raw and
 PackBits, extra channels) and GIF first images (palettes, transparency,
 interlacing, offset frames, a full 12-bit LZW table) with an LZW encoder
-written here, and Radiance HDR (flat and run-length scanlines).
+written here, Radiance HDR (flat and run-length scanlines) and Softimage PIC
+(uncompressed, pure and mixed run-length packets).
 GPU tests run the full encode and compare the written .astc with the
 library's blocks for the flipped image, and the reference's own leaf.astc.
 """
@@ -318,6 +319,64 @@ def test_cli_reads_16bit_tga(native, tmp_path):
     want = np.full((7, 13, 4), 255, np.uint8)
     for c, sh in enumerate((10, 5, 0)):
         want[..., c] = ((v >> sh) & 31) * 255 // 31
+    assert np.array_equal(_dump(native, path, tmp_path), want[::-1])
+    from astc_encoder_gb300 import image_io
+    assert np.array_equal(image_io.load_image(path), want)
+
+
+def _pic(path, rgba, packets):
+    """Writes a Softimage PIC; packets: (type, channel mask) with type 0
+    uncompressed, 1 pure run-length, 2 mixed run-length."""
+    h, w = rgba.shape[:2]
+    head = b"\x53\x80\xf6\x34" + struct.pack(">f", 3.71) + b"written by the test suite".ljust(80, b"\0")
+    head += b"PICT" + struct.pack(">HHfHH", w, h, 1.0, 3, 0)
+    head += b"".join(bytes([1 if i + 1 < len(packets) else 0, 8, t, m]) for i, (t, m) in enumerate(packets))
+    body = bytearray()
+    for y in range(h):
+        for t, m in packets:
+            chans = [c for c in range(4) if m & (0x80 >> c)]
+            px = [bytes(int(v) for v in rgba[y, x, chans]) for x in range(w)]
+            x = 0
+            while x < w:
+                run = 1
+                while x + run < w and px[x + run] == px[x] and run < 300:
+                    run += 1
+                if t == 0:
+                    body += px[x]
+                    x += 1
+                elif t == 1:
+                    run = min(run, 255)
+                    body += bytes([run]) + px[x]
+                    x += run
+                elif run >= 2:
+                    body += (bytes([128]) + struct.pack(">H", run) if run > 128 else bytes([run + 127])) + px[x]
+                    x += run
+                else:
+                    k = x
+                    while k < w and k - x < 128 and not (k + 1 < w and px[k + 1] == px[k]):
+                        k += 1
+                    k = max(k, x + 1)
+                    body += bytes([k - x - 1]) + b"".join(px[x:k])
+                    x = k
+    with open(path, "wb") as fh:
+        fh.write(head + bytes(body))
+
+
+@pytest.mark.parametrize("packets", [[(0, 0xF0)], [(2, 0xE0), (1, 0x10)], [(1, 0xE0)], [(2, 0xF0)],
+                                     [(0, 0x80), (2, 0x40), (1, 0x30)]])
+def test_cli_reads_pic(native, tmp_path, packets):
+    rng = np.random.default_rng(len(packets) * 7 + packets[0][0])
+    h, w = 9, 310                                           # a run longer than 128 takes the 16-bit count
+    rgba = rng.integers(0, 256, (h, w, 4), dtype=np.uint8)
+    rgba[2:6, 10:200] = rgba[2, 10]
+    rgba[7, :] = (9, 8, 7, 6)
+    path = str(tmp_path / "in.pic")
+    _pic(path, rgba, packets)
+    want = np.full((h, w, 4), 255, np.uint8)
+    for _, m in packets:
+        for c in range(4):
+            if m & (0x80 >> c):
+                want[..., c] = rgba[..., c]
     assert np.array_equal(_dump(native, path, tmp_path), want[::-1])
     from astc_encoder_gb300 import image_io
     assert np.array_equal(image_io.load_image(path), want)
@@ -906,6 +965,7 @@ def test_image_reader_under_sanitizers(tmp_path):
                                                  trns=b"\x00\x01\x00\x02\x00\x03", interlace=True)),
                         ("t.tga", lambda p: _tga_mapped(p, (arr[..., 2] // 8).astype(np.int64),
                                                         np.arange(96).reshape(32, 3), 24, 3, True)),
+                        ("u.pic", lambda p: _pic(p, rgba, [(2, 0xE0), (1, 0x10)])),
                         ("r.bmp", lambda p: _bmp_indexed(p, (arr[..., 1] // 16).astype(np.int64),
                                                          np.arange(48).reshape(16, 3) * 5, 4)),
                         ("s.bmp", lambda p: _bmp16(p, arr[..., 0].astype(np.int64) * 200, (0xF800, 0x07E0, 0x1F))),
