@@ -657,6 +657,15 @@ struct F32Count : F32 {
 // ---------------------------------------------------------------------------
 // The FP pipeline (templated on the arithmetic policy)
 // ---------------------------------------------------------------------------
+// Optional record of the fixed-mode pipeline's intermediate values (FP32 runs
+// only; filled when a non-null pointer is passed).
+typedef oracle_trace Trace;
+
+template <class T>
+inline void trace_put(float* dst, const T* src, int n) {
+    for (int i = 0; i < n; ++i) dst[i] = (float)src[i];
+}
+
 template <class P>
 struct Pipe {
     typedef typename P::T T;
@@ -682,14 +691,21 @@ struct Pipe {
     }
 
     // eigen_vector (ASTC_Encode.hlsl:93-106)
-    static void eigen_vector(const T m[4][4], T v[4]) {
+    static void eigen_vector(const T m[4][4], T v[4], Trace* tr = nullptr) {
         v[0] = P::lit(0.26726f, 0.26726); v[1] = P::lit(0.80178f, 0.80178);
         v[2] = P::lit(0.53452f, 0.53452); v[3] = 0;
+        if (tr) v[3] = (T)tr->start_w;      // a trace may seed the start vector's alpha
+        if (tr) { tr->early_exit = 0; tr->min_len = 1e31f; }
         for (int it = 0; it < 8; ++it) {
             T t[4];
             for (int r = 0; r < 4; ++r) t[r] = dot4(m[r], v);
             for (int r = 0; r < 4; ++r) v[r] = t[r];
-            if (length(v) < P::lit(1e-5f, 1e-5)) return;
+            const T len = length(v);
+            if (tr && (float)len < tr->min_len) tr->min_len = (float)len;
+            if (len < P::lit(1e-5f, 1e-5)) {
+                if (tr) tr->early_exit = 1 + it;
+                return;
+            }
             for (int r = 0; r < 4; ++r) t[r] = dot4(m[r], v);
             for (int r = 0; r < 4; ++r) v[r] = t[r];
             normalize(v);
@@ -698,7 +714,8 @@ struct Pipe {
 
     // find_min_max (ASTC_Encode.hlsl:108-137), over the texels in `sel`
     static void find_min_max(const T (*tex)[4], int n, const T mean[4], const T k[4],
-                             bool alpha, T e0[4], T e1[4], uint64_t sel = ~0ull) {
+                             bool alpha, T e0[4], T e1[4], uint64_t sel = ~0ull,
+                             Trace* tr = nullptr) {
         T a = P::lit(1e31f, 1e31), b = P::lit(-1e31f, -1e31);
         for (int i = 0; i < n; ++i) {
             if (!((sel >> i) & 1)) continue;
@@ -714,6 +731,11 @@ struct Pipe {
         }
         const T s0 = P::add(P::add(P::rint(e0[0]), P::rint(e0[1])), P::rint(e0[2]));
         const T s1 = P::add(P::add(P::rint(e1[0]), P::rint(e1[1])), P::rint(e1[2]));
+        if (tr) {
+            tr->tmin = (float)a; tr->tmax = (float)b;
+            trace_put(tr->e0_fit, e0, 4); trace_put(tr->e1_fit, e1, 4);
+            tr->s0 = (float)s0; tr->s1 = (float)s1; tr->swapped = s0 > s1;
+        }
         if (s0 > s1)
             for (int c = 0; c < 4; ++c) { T t = e0[c]; e0[c] = e1[c]; e1[c] = t; }
         if (!alpha) { e0[3] = P::lit(255.0f, 255.0); e1[3] = P::lit(255.0f, 255.0); }
@@ -739,12 +761,17 @@ struct Pipe {
     }
 
     // principal_component_analysis (ASTC_Encode.hlsl:139-168)
-    static void pca(const T (*tex)[4], int n, bool alpha, T e0[4], T e1[4]) {
+    static void pca(const T (*tex)[4], int n, bool alpha, T e0[4], T e1[4], Trace* tr = nullptr) {
         T mean[4], cov[4][4];
         covariance(tex, n, mean, cov);
         T k[4];
-        eigen_vector(cov, k);
-        find_min_max(tex, n, mean, k, alpha, e0, e1);
+        eigen_vector(cov, k, tr);
+        if (tr) {
+            trace_put(tr->mean, mean, 4);
+            for (int i = 0; i < 4; ++i) trace_put(tr->cov + 4 * i, cov[i], 4);
+            trace_put(tr->axis, k, 4);
+        }
+        find_min_max(tex, n, mean, k, alpha, e0, e1, ~0ull, tr);
     }
 
     // max_accumulation_pixel_direction (ASTC_Encode.hlsl:170-227): the axis is
@@ -821,10 +848,11 @@ struct Pipe {
 
     // calculate_normal_weights + quantize_weights (ASTC_Encode.hlsl:316-393)
     static void weights(const T (*tex)[4], int dim, const T e0[4], const T e1[4],
-                        uint32_t range, uint32_t qw[16]) {
+                        uint32_t range, uint32_t qw[16], Trace* tr = nullptr) {
         T k[4];
         for (int c = 0; c < 4; ++c) k[c] = P::sub(e1[c], e0[c]);
         T w[16];
+        if (tr) { tr->wlen = (float)length(k); tr->minw = tr->maxw = tr->inv = 0; }
         if (length(k) < P::lit(1e-5f, 1e-5)) {
             for (int i = 0; i < 16; ++i) w[i] = 0;
         } else {
@@ -843,10 +871,15 @@ struct Pipe {
             T inv = P::sub(maxw, minw);
             inv = P::max(P::lit(1e-5f, 1e-5), inv);
             inv = P::div(P::lit(1.0f, 1.0), inv);
+            if (tr) {
+                trace_put(tr->wproj, w, 16);
+                tr->minw = (float)minw; tr->maxw = (float)maxw; tr->inv = (float)inv;
+            }
             for (int i = 0; i < 16; ++i) w[i] = P::mul(P::sub(w[i], minw), inv);
         }
         const T rf = (T)range;
         for (int i = 0; i < 16; ++i) {
+            if (tr) tr->wR[i] = (float)P::mul(w[i], rf);
             const T r = P::rint(P::mul(w[i], rf));
             uint32_t q = r <= 0 ? 0u : (uint32_t)r;
             qw[i] = q > range ? range : q;
@@ -1915,6 +1948,38 @@ int oracle_encode_block_fp32(const float* texels, int block_dim, int has_alpha, 
         for (int c = 0; c < 4; ++c) tex[i][c] = texels[4 * i + c];
     Pipe<F32>::encode(tex, block_dim, has_alpha != 0, ep, qw, out);
     return 0;
+}
+
+int oracle_trace_block_fp32(const float* texels, int block_dim, int has_alpha, float start_w,
+                            oracle_trace* tr) {
+    if (!texels || !tr || (block_dim != 4 && block_dim != 6)) return -1;
+    float tex[36][4];
+    for (int i = 0; i < block_dim * block_dim; ++i)
+        for (int c = 0; c < 4; ++c) tex[i][c] = texels[4 * i + c];
+    std::memset(tr, 0, sizeof(*tr));
+    tr->start_w = start_w;
+    float e0[4], e1[4];
+    Pipe<F32>::pca(tex, block_dim * block_dim, has_alpha != 0, e0, e1, tr);
+    trace_put(tr->e0, e0, 4);
+    trace_put(tr->e1, e1, 4);
+    for (int c = 0; c < 4; ++c) {                           // encode_color 233-245
+        tr->ep[2 * c] = (uint32_t)std::rint(e0[c]);
+        tr->ep[2 * c + 1] = (uint32_t)std::rint(e1[c]);
+    }
+    Pipe<F32>::weights(tex, block_dim, e0, e1, has_alpha ? 5u : 11u, tr->qw, tr);
+    assemble_symbolic(tr->ep, tr->qw, has_alpha != 0, tr->block);
+    return 0;
+}
+
+int oracle_find_seed(const float* texels, int block_dim, int has_alpha, const uint8_t target[16],
+                     const float* seeds, int n_seeds) {
+    if (!texels || !target || !seeds || n_seeds < 0) return -2;
+    oracle_trace tr;
+    for (int i = 0; i < n_seeds; ++i) {
+        if (oracle_trace_block_fp32(texels, block_dim, has_alpha, seeds[i], &tr) != 0) return -2;
+        if (std::memcmp(tr.block, target, 16) == 0) return i;
+    }
+    return -1;
 }
 
 int oracle_assemble_symbolic(const uint32_t ep[8], const uint32_t qw[16], int has_alpha,

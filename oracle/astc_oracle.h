@@ -76,6 +76,37 @@ int oracle_encode_block_fp32(const float* texels, int block_dim, int has_alpha,
 
 /* Integer stages only: assemble a block from symbolic endpoints and weights
  * (weight quant method QUANT_6 when has_alpha, QUANT_12 otherwise). */
+/* The intermediate values of the FP32 fixed-mode pipeline for one block, for
+ * the tests that explain each block where the oracle and the reference's own
+ * output differ (which rounding or comparison decided it, and by how much). */
+typedef struct oracle_trace {
+    float start_w;              /* alpha of the power iteration's start vector:
+                                   0 in the shader (ASTC_Encode.hlsl:96); a
+                                   trace may seed it to model rounding noise  */
+    float mean[4], cov[16];     /* principal_component_analysis 139-162       */
+    int early_exit;             /* eigen_vector iteration (1..8) that returned
+                                   early on length(v) < 1e-5, else 0 (93-106) */
+    float min_len;              /* the smallest length(v) the test saw        */
+    float axis[4];              /* eigen_vector's result                      */
+    float tmin, tmax;           /* find_min_max projections (108-118)         */
+    float e0_fit[4], e1_fit[4]; /* clamped endpoints before the swap (120-121) */
+    float s0, s1;               /* rounded RGB sums compared for the swap     */
+    int swapped;                /* s0 > s1 (125-129)                          */
+    float e0[4], e1[4];         /* final endpoints (alpha forced without -alpha)*/
+    float wlen;                 /* length(e1 - e0) in calculate_normal_weights */
+    float wproj[16];            /* dot(k, texel - e0) before scaling (316-356) */
+    float minw, maxw, inv;      /* the scaling (358-366)                      */
+    float wR[16];               /* scaled weight x range, before round (256-260)*/
+    uint32_t ep[8], qw[16];     /* quantised endpoints r0 r1 g0 g1 ..., weights */
+    uint8_t block[16];          /* the assembled block                        */
+} oracle_trace;
+int oracle_trace_block_fp32(const float* texels, int block_dim, int has_alpha, float start_w,
+                            oracle_trace* tr);
+/* The first of n_seeds start-vector alpha seeds under which the FP32
+ * fixed-mode pipeline assembles exactly `target`; -1 if none does. */
+int oracle_find_seed(const float* texels, int block_dim, int has_alpha, const uint8_t target[16],
+                     const float* seeds, int n_seeds);
+
 int oracle_assemble_symbolic(const uint32_t ep[8], const uint32_t qw[16],
                              int has_alpha, uint8_t out[16]);
 

@@ -24,6 +24,15 @@ class OracleOpts(ctypes.Structure):
                                             "axis", "quality")]
 
 
+class OracleTrace(ctypes.Structure):
+    f, i, u = ctypes.c_float, ctypes.c_int, ctypes.c_uint32
+    _fields_ = [("start_w", f), ("mean", f * 4), ("cov", f * 16), ("early_exit", i), ("min_len", f), ("axis", f * 4),
+                ("tmin", f), ("tmax", f), ("e0_fit", f * 4), ("e1_fit", f * 4), ("s0", f), ("s1", f),
+                ("swapped", i), ("e0", f * 4), ("e1", f * 4), ("wlen", f), ("wproj", f * 16),
+                ("minw", f), ("maxw", f), ("inv", f), ("wR", f * 16), ("ep", u * 8), ("qw", u * 16),
+                ("block", ctypes.c_uint8 * 16)]
+
+
 def build(force: bool = False) -> str:
     """Compile the oracle with its Makefile (g++, OpenMP)."""
     src = os.path.join(HERE, "astc_oracle.cpp")
@@ -66,6 +75,8 @@ def lib() -> ctypes.CDLL:
             L.oracle_flops_per_block.restype = ctypes.c_double
             L.oracle_endpoint_quant.argtypes = [ip, ip]
             L.oracle_search_block_fp32.argtypes = [vp, ip, ip, ip, ip, ip, vp, vp, vp, vp]
+            L.oracle_find_seed.argtypes = [vp, ip, ip, vp, vp, ip]
+            L.oracle_trace_block_fp32.argtypes = [vp, ip, ip, ctypes.c_float, ctypes.POINTER(OracleTrace)]
             _lib = L
     return _lib
 
@@ -107,6 +118,39 @@ def encode_block(texels: np.ndarray, block_dim: int, has_alpha: bool):
                                         qw.ctypes.data, out.ctypes.data)
     assert rc == 0
     return ep, qw, out
+
+
+def trace_block(texels: np.ndarray, block_dim: int, has_alpha: bool, start_w: float = 0.0) -> dict:
+    """Intermediate values of the FP32 fixed-mode pipeline for one block
+    (texels: N x 4 floats, 0..255): scalars as floats/ints, vectors as float32
+    arrays; ep / qw the quantised endpoints and weights, block the assembled
+    block.  start_w seeds the alpha of the power iteration's start vector
+    (0 in the shader)."""
+    t = np.ascontiguousarray(texels, dtype=np.float32).reshape(-1)
+    tr = OracleTrace()
+    rc = lib().oracle_trace_block_fp32(t.ctypes.data, block_dim, int(has_alpha), float(start_w),
+                                       ctypes.byref(tr))
+    if rc != 0:
+        raise ValueError("bad trace arguments")
+    out = {}
+    for name, _ in OracleTrace._fields_:
+        v = getattr(tr, name)
+        out[name] = np.array(v[:], dtype=np.uint32 if name in ("ep", "qw") else np.uint8 if name == "block"
+                 else np.float32) \
+            if hasattr(v, "_length_") else v
+    return out
+
+
+def find_seed(texels: np.ndarray, block_dim: int, has_alpha: bool, target: np.ndarray, seeds) -> float | None:
+    """The first start-vector alpha seed (of `seeds`) under which the FP32
+    fixed-mode pipeline assembles exactly the block `target`, or None."""
+    t = np.ascontiguousarray(texels, dtype=np.float32).reshape(-1)
+    tg = np.ascontiguousarray(target, dtype=np.uint8).reshape(16)
+    sd = np.ascontiguousarray(seeds, dtype=np.float32)
+    i = lib().oracle_find_seed(t.ctypes.data, block_dim, int(has_alpha), tg.ctypes.data, sd.ctypes.data, len(sd))
+    if i < -1:
+        raise ValueError("bad seed-search arguments")
+    return None if i < 0 else float(sd[i])
 
 
 def assemble_symbolic(ep, qw, has_alpha: bool) -> np.ndarray:

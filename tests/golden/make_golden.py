@@ -1,7 +1,7 @@
 """Regenerates the golden fixtures in tests/golden/ from the reference tree.
 
-Run in a checkout that has the reference mounted (its path is the first
-argument, default /root/reference).  Writes:
+Run in a checkout that has the reference tree (its path is the one required
+argument).  Writes:
 
 * reference_tables.json -- the reference's literal tables, parsed from its
   HLSL sources as text: bits_trits_quints_table, integer_from_trits,
@@ -15,6 +15,10 @@ argument, default /root/reference).  Writes:
   start on block boundaries so every block lies inside the image.
 * leaf_full_stats.json -- whole-image facts of leaf.astc used by the
   fixture-only tests (block count, mode words, constant-block count).
+* leaf_differing_blocks.npz -- every block of textures/leaf.astc that the
+  FP32 oracle does not reproduce bit for bit: its block index, its 16 texels
+  (flipped as above) and the reference's 16 bytes.  The tests explain each
+  one by the decision that differs (tests/test_oracle_leaf_classes.py).
 
 The reference's texture is 1024x1024; the crops keep the committed fixture
 small (about 100 KB) while covering constant, opaque and cut-out blocks.
@@ -98,10 +102,23 @@ def main(ref: str) -> None:
         "constant_blocks": int(const.sum()),
         "source": "niepp/astc_encoder textures/leaf.png, textures/leaf.astc",
     }
+    from oracle import oracle
+    got = oracle.encode(flipped, block_dim=4, has_alpha=True)
+    differ = np.where(~np.all(got == flat, axis=1))[0].astype(np.int32)
+    np.savez_compressed(os.path.join(HERE, "leaf_differing_blocks.npz"), index=differ,
+                        texels=tex[differ].astype(np.uint8), reference=flat[differ].copy())
+    stats["oracle_identical_blocks"] = int(flat.shape[0] - len(differ))
+    # whole-image squared error (RGBA, 8-bit) of each decode against the source
+    for key, blocks in (("reference_sse", flat), ("oracle_sse", got)):
+        dec, errors = oracle.decode(blocks, 1024, 1024, 4)
+        assert errors == 0
+        stats[key] = float(np.sum((dec.astype(np.float64) - flipped.astype(np.float64)) ** 2))
     with open(os.path.join(HERE, "leaf_full_stats.json"), "w") as fh:
         json.dump(stats, fh, indent=1)
     print("wrote", sorted(os.listdir(HERE)))
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_golden.py <path of the niepp/astc_encoder tree>")
+    main(sys.argv[1])

@@ -4,9 +4,11 @@ leaf.astc was produced by the reference shader on unknown D3D11 hardware with
 -alpha -4x4 in linear space from the vertically flipped leaf.png.  Its integer
 fields (block mode, partition bits, CEM, endpoint layout, ISE of constant
 blocks) pin the integer stages exactly.  The float stages can only be pinned
-statistically: the GPU's approximate rsq/rcp decide ties where a weight lands
-exactly on .5 after scaling (collinear texels), so the oracle reproduces about
-98% of blocks bit-for-bit and the same PSNR.
+statistically: the oracle reproduces 98.16% of the blocks bit for bit, and
+tests/test_oracle_leaf_classes.py explains each of the others (weight and
+endpoint ties, and the alpha axis that the reference's rounding noise finds
+in RGB-alpha decoupled blocks).  The oracle is deterministic, so the counts
+below are exact: any change of its arithmetic shows here.
 """
 import json
 import os
@@ -40,6 +42,11 @@ def test_header_of_reference_file():
     assert STATS["mode_words"] == [0x043] and STATS["cem_values"] == [12]
 
 
+# per crop: blocks that differ, blocks whose endpoint field differs, and the
+# oracle's decoded PSNR minus the reference's (dB)
+CROP_FIGURES = {0: (17, 7, -0.0765), 1: (10, 0, -0.0002)}
+
+
 @pytest.mark.parametrize("crop", [0, 1])
 def test_oracle_matches_leaf_crop(oracle, crop):
     rgba = CROPS[f"crop{crop}_rgba"]
@@ -55,13 +62,14 @@ def test_oracle_matches_leaf_crop(oracle, crop):
     const = np.all(tex == tex[:, :1, :], axis=(1, 2))
     assert const.sum() > 100
     assert same[const].all()
-    # statistical pin of the float stages
-    assert same.mean() >= 0.97, same.mean()
-    # quality: decoded PSNR of the oracle's blocks matches the reference's
+    # the float stages: exact counts of the deterministic oracle
+    n_diff, n_ep, gap = CROP_FIGURES[crop]
+    assert int((~same).sum()) == n_diff
+    assert int((_endpoint_field(got) != _endpoint_field(ref)).sum()) == n_ep
     d_ref, e1 = oracle.decode(ref, 128, 128, 4)
     d_got, e2 = oracle.decode(got, 128, 128, 4)
     assert e1 == 0 and e2 == 0
-    assert abs(_psnr(d_got, rgba) - _psnr(d_ref, rgba)) < 0.1
+    assert abs((_psnr(d_got, rgba) - _psnr(d_ref, rgba)) - gap) < 0.001
 
 
 def test_oracle_matches_full_leaf(oracle, reference_dir):
@@ -77,12 +85,13 @@ def test_oracle_matches_full_leaf(oracle, reference_dir):
     const = np.all(tex == tex[:, :1, :], axis=(1, 2))
     assert const.sum() == STATS["constant_blocks"] == 18340
     assert same[const].all()
-    assert same.mean() >= 0.98, same.mean()
+    assert int(same.sum()) == STATS["oracle_identical_blocks"] == 64332        # 98.16%
     ep_same = _endpoint_field(got) == _endpoint_field(ref)     # 64 bits from bit 17
-    assert ep_same.mean() >= 0.995
+    assert int((~ep_same).sum()) == 118                                        # 99.82%
     d_ref, _ = oracle.decode(ref, 1024, 1024, 4)
     d_got, _ = oracle.decode(got, 1024, 1024, 4)
-    assert abs(_psnr(d_got, flipped) - _psnr(d_ref, flipped)) < 0.1
+    gap = _psnr(d_ref, flipped) - _psnr(d_got, flipped)
+    assert 0.047 < gap < 0.048, gap
     # the reference's constant blocks decode back to their exact colour
     db = d_ref.reshape(256, 4, 256, 4, 4).transpose(0, 2, 1, 3, 4).reshape(-1, 16, 4)
     assert np.array_equal(db[const], tex[const])
