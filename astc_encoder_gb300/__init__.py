@@ -152,6 +152,8 @@ def load_library() -> ctypes.CDLL:
     lib.astc_decode_gpu.restype = ctypes.c_int
     lib.astc_sse_gpu.argtypes = [u8p, u8p, sz, ctypes.c_int, vp, ctypes.POINTER(ctypes.c_uint64)]
     lib.astc_sse_gpu.restype = ctypes.c_int
+    lib.astc_normal_sse_gpu.argtypes = [u8p, u8p, sz, ctypes.c_int, vp, ctypes.POINTER(ctypes.c_double)]
+    lib.astc_normal_sse_gpu.restype = ctypes.c_int
     lib.astc_last_error.argtypes = []
     lib.astc_last_error.restype = ctypes.c_char_p
     lib.astc_status_string.argtypes = [ctypes.c_int]
@@ -166,6 +168,8 @@ def load_library() -> ctypes.CDLL:
     lib.astc_set_kernel_choice.restype = ctypes.c_int
     lib.astc_get_kernel_choice.argtypes = [ctypes.c_int] * 4 + [ip, ip]
     lib.astc_get_kernel_choice.restype = ctypes.c_int
+    lib.astc_get_kernel_choice_for_size.argtypes = [ctypes.c_int] * 6 + [ip, ip]
+    lib.astc_get_kernel_choice_for_size.restype = ctypes.c_int
     lib.astc_batch_create.argtypes = [ctypes.c_int, ctypes.c_longlong, ctypes.POINTER(ctypes.c_void_p)]
     lib.astc_batch_create.restype = ctypes.c_int
     lib.astc_batch_encode.argtypes = [ctypes.c_void_p, ctypes.POINTER(BatchItem), ctypes.c_int,
@@ -199,6 +203,8 @@ def load_library() -> ctypes.CDLL:
     dp = ctypes.POINTER(ctypes.c_double)
     lib.astc_server_replay.argtypes = [ctypes.c_void_p, ctypes.POINTER(Request), dp, ctypes.c_int, dp, dp]
     lib.astc_server_replay.restype = ctypes.c_int
+    lib.astc_server_get_stats.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ServerStats)]
+    lib.astc_server_get_stats.restype = ctypes.c_int
     lib.astc_server_destroy.argtypes = [ctypes.c_void_p]
     lib.astc_server_destroy.restype = ctypes.c_int
     _LIB = lib
@@ -235,6 +241,14 @@ class Request(ctypes.Structure):
 class RequestStats(ctypes.Structure):
     _fields_ = [("submit_us", ctypes.c_double), ("admit_us", ctypes.c_double), ("done_us", ctypes.c_double),
                 ("status", ctypes.c_int)]
+
+
+class ServerStats(ctypes.Structure):
+    """``astc_server_stats`` of include/astc_gb300.h."""
+    _fields_ = [("launches", ctypes.c_longlong), ("requests", ctypes.c_longlong),
+                ("max_requests_per_launch", ctypes.c_int), ("device_busy_s", ctypes.c_double),
+                ("device_overlap_s", ctypes.c_double), ("device_slot_s", ctypes.c_double),
+                ("device_span_s", ctypes.c_double)]
 
 
 SERVE_BATCHED, SERVE_PER_REQUEST = 0, 1
@@ -286,6 +300,12 @@ class Server:
         _check(self._lib.astc_server_replay(self._h, arr, arrival.ctypes.data_as(dp), n,
                                             lat.ctypes.data_as(dp), ctypes.byref(wall)))
         return lat, wall.value
+
+    def stats(self, reset: bool = False) -> dict:
+        """Device-side record of the launches retired since the last reset."""
+        st = ServerStats()
+        _check(self._lib.astc_server_get_stats(self._h, int(reset), ctypes.byref(st)))
+        return {name: getattr(st, name) for name, _ in ServerStats._fields_}
 
     def close(self) -> None:
         if self._h:
@@ -406,6 +426,15 @@ def get_kernel_choice(block_dim: int, has_alpha: bool, is_normal: bool, srgb: bo
     s, t = ctypes.c_int(), ctypes.c_int()
     _check(load_library().astc_get_kernel_choice(block_dim, int(has_alpha), int(is_normal), int(srgb),
                                                  ctypes.byref(s), ctypes.byref(t)))
+    return s.value, t.value
+
+
+def get_kernel_choice_for_size(block_dim: int, has_alpha: bool, is_normal: bool, srgb: bool, width: int,
+                               height: int) -> tuple[int, int]:
+    """(store, threads) astc_encode_gpu uses for a texture of this size."""
+    s, t = ctypes.c_int(), ctypes.c_int()
+    _check(load_library().astc_get_kernel_choice_for_size(block_dim, int(has_alpha), int(is_normal), int(srgb),
+                                                          width, height, ctypes.byref(s), ctypes.byref(t)))
     return s.value, t.value
 
 
@@ -537,6 +566,30 @@ def sse(a: np.ndarray, b: np.ndarray) -> np.ndarray:
     _check(load_library().astc_sse_gpu(x.ctypes.data, y.ctypes.data, x.size // 4, Memory.HOST, None,
                                        res))
     return np.array(list(res), dtype=np.uint64)
+
+
+def normal_sse(a: np.ndarray, b: np.ndarray) -> float:
+    """Squared error of two -norm layout RGBA8 normal maps on their rebuilt
+    unit normals (z = sqrt(max(0, 1 - x^2 - y^2))), components scaled by 127.5;
+    PSNR over 3 values per texel with peak 255.  On the GPU."""
+    x = np.ascontiguousarray(a, dtype=np.uint8)
+    y = np.ascontiguousarray(b, dtype=np.uint8)
+    if x.shape != y.shape or x.size % 4:
+        raise AstcError(Status.INVALID_ARG, "images must have the same RGBA8 shape")
+    res = ctypes.c_double(0.0)
+    _check(load_library().astc_normal_sse_gpu(x.ctypes.data, y.ctypes.data, x.size // 4, Memory.HOST, None,
+                                              ctypes.byref(res)))
+    return float(res.value)
+
+
+def normal_sse_numpy(a: np.ndarray, b: np.ndarray) -> float:
+    """The same measure as normal_sse in numpy (float64), for checking."""
+    def rebuilt(img):
+        xy = img[..., :2].astype(np.float64) * (2.0 / 255.0) - 1.0
+        z = np.sqrt(np.maximum(0.0, 1.0 - xy[..., 0] ** 2 - xy[..., 1] ** 2))
+        return np.concatenate([xy, z[..., None]], axis=-1)
+    d = (rebuilt(np.asarray(a)) - rebuilt(np.asarray(b))) * 127.5
+    return float(np.sum(d * d))
 
 
 def srgb_texel_values() -> np.ndarray:

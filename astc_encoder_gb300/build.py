@@ -41,6 +41,7 @@ LIB_SOURCES = [
     ("astc_encode_partitions.cu", ["--fmad=false"]),
     ("astc_encode_three.cu", ["--fmad=false"]),
     ("astc_encode_best.cu", ["--fmad=false"]),
+    ("astc_encode_coop.cu", ["--fmad=false"]),
     ("astc_batch.cu", ["--fmad=false"]),
     ("astc_mips.cu", []),
     ("astc_server.cu", []),

@@ -26,7 +26,6 @@
 #include <mutex>
 #include <new>
 #include <string>
-#include <unordered_set>
 #include <vector>
 
 #include "astc_internal.h"
@@ -77,9 +76,11 @@ astc_encode_persistent(const BatchJob* __restrict__ jobs, const WorkItem* __rest
     constexpr int N = DIM * DIM;
     extern __shared__ float4 s_texels[];            // FP32 4x4 keeps texels in shared memory
     __shared__ uint8_t s_trits[256];
-    __shared__ float s_lut[SRGB ? 256 : 1];
+    __shared__ float s_lut[(SRGB && PREC == ASTC_PRECISION_FP32) ? 256 : 1];
+    __shared__ uint8_t s_lin8[(SRGB && PREC == ASTC_PRECISION_HALF2) ? 256 : 1];
     __shared__ int s_item;
-    load_cta_tables<SRGB>(c_trit_pack_b, c_srgb_bits_b, s_trits, s_lut);
+    load_cta_tables<SRGB && PREC == ASTC_PRECISION_FP32>(c_trit_pack_b, c_srgb_bits_b, s_trits, s_lut);
+    if (SRGB && PREC == ASTC_PRECISION_HALF2) load_lin8_table(c_srgb_bits_b, s_lin8);
     const int end = q->end[fmt];
     const int begin = q->begin[fmt];
     for (;;) {
@@ -98,7 +99,7 @@ astc_encode_persistent(const BatchJob* __restrict__ jobs, const WorkItem* __rest
             load_block_packed<DIM>(j.tex, bx, by, px);
             uint4 r;
             if constexpr (PREC == ASTC_PRECISION_HALF2) {
-                r = encode_block_h2<DIM, ALPHA, NORMAL, SRGB>(px, s_lut, s_trits);
+                r = encode_block_h2<DIM, ALPHA, NORMAL, SRGB>(px, s_lin8, s_trits);
             } else if constexpr (DIM == 4) {
                 SharedTexels<N> st{s_texels + threadIdx.x, kBatchThreads};
 #pragma unroll
@@ -158,7 +159,6 @@ struct astc_batch {
     cudaEvent_t done = nullptr;
     bool pending = false;
     std::map<unsigned, cudaGraphExec_t> graphs;   // key: precision << 16 | format mask
-    std::unordered_set<uintptr_t> validated;      // device pointers already checked
 };
 
 namespace {
@@ -168,26 +168,8 @@ size_t items_offset(int max_items) {
     return (jobs_offset() + (size_t)max_items * sizeof(BatchJob) + 255) & ~(size_t)255;
 }
 
-astc_status check_ptr(astc_batch* b, const void* p, const char* what) {
-    const uintptr_t key = reinterpret_cast<uintptr_t>(p);
-    if (b->validated.count(key)) return ASTC_OK;
-    cudaPointerAttributes a;
-    const cudaError_t e = cudaPointerGetAttributes(&a, p);
-    if (e != cudaSuccess) {
-        cudaGetLastError();
-        return set_error(ASTC_ERR_INVALID_ARG, std::string(what) + " is not a CUDA pointer");
-    }
-    // device or managed memory, or the device view of pinned host memory
-    const bool host_view = a.type == cudaMemoryTypeHost && a.devicePointer == p;
-    if (a.type != cudaMemoryTypeDevice && a.type != cudaMemoryTypeManaged && !host_view)
-        return set_error(ASTC_ERR_INVALID_ARG, std::string(what) + " is not device-accessible memory");
-    if (b->validated.size() > 65536) b->validated.clear();
-    b->validated.insert(key);
-    return ASTC_OK;
-}
-
 // Checks item i of a batch call and adds its block count to *blocks.
-astc_status validate_item(astc_batch* b, const astc_batch_item& t, int i, long long* blocks) {
+astc_status validate_item(const astc_batch_item& t, int i, long long* blocks, SpanCache* seen) {
     if (t.block_dim != 4 && t.block_dim != 6)
         return set_error(ASTC_ERR_INVALID_ARG, "item " + std::to_string(i) + ": block_dim must be 4 or 6");
     if (t.width <= 0 || t.height <= 0 || t.width > 0xFFFFFF || t.height > 0xFFFFFF)
@@ -200,11 +182,12 @@ astc_status validate_item(astc_batch* b, const astc_batch_item& t, int i, long l
     if (!t.rgba8 || !t.out || reinterpret_cast<uintptr_t>(t.rgba8) % 4 || reinterpret_cast<uintptr_t>(t.out) % 16)
         return set_error(ASTC_ERR_INVALID_ARG,
                          "item " + std::to_string(i) + ": rgba8 must be 4-byte and out 16-byte aligned");
-    astc_status st;
-    if ((st = check_ptr(b, t.rgba8, "rgba8")) != ASTC_OK) return st;
-    if ((st = check_ptr(b, t.out, "out")) != ASTC_OK) return st;
     const long long nb = (long long)blocks_x(t.width, t.block_dim) * blocks_y(t.height, t.block_dim);
     if (nb > (1LL << 31)) return set_error(ASTC_ERR_INVALID_ARG, "texture has more than 2^31 blocks");
+    astc_status st = check_device_span(t.rgba8, pitch * (size_t)(t.height - 1) + (size_t)t.width * 4, "rgba8",
+                                       true, seen);
+    if (st == ASTC_OK) st = check_device_span(t.out, (size_t)nb * 16, "out", true, seen);
+    if (st != ASTC_OK) return set_error(st, "item " + std::to_string(i) + ": " + astc_last_error());
     *blocks += nb;
     return ASTC_OK;
 }
@@ -291,10 +274,11 @@ astc_status astc_batch_encode(astc_batch* b, const astc_batch_item* in, int coun
         // plan: validate, count work items per format
         long long blocks = 0;
         int per_fmt[kFormats] = {};
+        SpanCache seen;
         for (int i = 0; i < count; ++i) {
             const astc_batch_item& t = in[i];
             const long long before = blocks;
-            const astc_status st = validate_item(b, t, i, &blocks);
+            const astc_status st = validate_item(t, i, &blocks, &seen);
             if (st != ASTC_OK) return st;
             per_fmt[format_index(t.block_dim, t.has_alpha, t.is_normal, t.srgb)] +=
                 (int)((blocks - before + kBatchThreads - 1) / kBatchThreads);
@@ -397,8 +381,9 @@ astc_status astc_batch_encode_quality(astc_batch* b, const astc_batch_item* in, 
         if (e != cudaSuccess) return cuda_error(e, "cudaGetDevice");
         if (dev != b->device) return set_error(ASTC_ERR_INVALID_ARG, "batch was created on another device");
         long long blocks = 0;
+        SpanCache seen;
         for (int i = 0; i < count; ++i) {
-            const astc_status st = validate_item(b, in[i], i, &blocks);
+            const astc_status st = validate_item(in[i], i, &blocks, &seen);
             if (st != ASTC_OK) return st;
         }
         if (blocks > b->max_blocks) return set_error(ASTC_ERR_INVALID_ARG, "batch exceeds max_blocks");

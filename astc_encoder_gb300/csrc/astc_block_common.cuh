@@ -141,8 +141,10 @@ __device__ __forceinline__ void load_block_packed(const TextureView& p, int bx, 
 // texel stores: where the decoded FP32 texels of one block live
 // ---------------------------------------------------------------------------
 // registers / shared memory / registers with the count capped near 168 (three
-// 128-thread CTAs per SM) so the compiler trades a little spilling for warps
-enum TexelStore : int { kStoreRegisters = 0, kStoreShared = 1, kStoreRegistersCapped = 2 };
+// 128-thread CTAs per SM) so the compiler trades a little spilling for warps;
+// kStoreCoop is the cooperative mapping (four lanes per block, texels in a
+// shared-memory tile; astc_encode_coop.cu)
+enum TexelStore : int { kStoreRegisters = 0, kStoreShared = 1, kStoreRegistersCapped = 2, kStoreCoop = 3 };
 
 template <int N>
 struct RegTexels {

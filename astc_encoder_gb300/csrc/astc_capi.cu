@@ -9,6 +9,7 @@
 //   save_astc          astc_save.h:52-76            -> astc_save_file
 // Unlike the reference, every failure returns a status (the reference leaked
 // its D3D objects on each error path and never checked fopen).
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <stdio.h>
@@ -152,17 +153,8 @@ bool upload_ring_enabled() {
     return on;
 }
 
-astc_status check_device_pointer(const void* ptr, const char* what) {
-    cudaPointerAttributes a;
-    const cudaError_t e = cudaPointerGetAttributes(&a, ptr);
-    if (e != cudaSuccess) {
-        cudaGetLastError();
-        return set_error(ASTC_ERR_INVALID_ARG, std::string(what) + " is not a CUDA pointer");
-    }
-    if (a.type != cudaMemoryTypeDevice && a.type != cudaMemoryTypeManaged)
-        return set_error(ASTC_ERR_INVALID_ARG,
-                         std::string(what) + " is not device memory (memory = ASTC_MEMORY_DEVICE)");
-    return ASTC_OK;
+astc_status check_device_pointer(const void* ptr, size_t bytes, const char* what) {
+    return check_device_span(ptr, bytes, what, false, nullptr);
 }
 
 // Device view of a pinned (page-locked, device-mapped) host buffer, or NULL
@@ -177,6 +169,72 @@ bool zero_copy_enabled() {
 }
 
 }  // namespace
+
+// cuPointerGetAttributes through the runtime's driver entry point (no link
+// against the driver library); NULL where the driver does not provide it.
+using PointerAttrsFn = CUresult (*)(unsigned, CUpointer_attribute*, void**, CUdeviceptr);
+static PointerAttrsFn pointer_attrs_fn() {
+    static const PointerAttrsFn fn = [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuPointerGetAttributes", &f, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess || q != cudaDriverEntryPointSuccess) {
+            cudaGetLastError();
+            f = nullptr;
+        }
+        return reinterpret_cast<PointerAttrsFn>(f);
+    }();
+    return fn;
+}
+
+astc_status check_device_span(const void* p, size_t bytes, const char* what, bool allow_host_view,
+                              SpanCache* seen) {
+    const uintptr_t lo = reinterpret_cast<uintptr_t>(p), hi = lo + bytes;
+    if (hi < lo) return set_error(ASTC_ERR_INVALID_ARG, std::string(what) + ": extent overflows");
+    if (seen && seen->n) {
+        if (lo >= seen->r[seen->last].lo && hi <= seen->r[seen->last].hi) return ASTC_OK;
+        for (int i = 0; i < seen->n; ++i)
+            if (lo >= seen->r[i].lo && hi <= seen->r[i].hi) {
+                seen->last = i;
+                return ASTC_OK;
+            }
+    }
+    cudaPointerAttributes a;
+    const cudaError_t e = cudaPointerGetAttributes(&a, p);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return set_error(ASTC_ERR_INVALID_ARG, std::string(what) + " is not a CUDA pointer");
+    }
+    const bool host_view = allow_host_view && a.type == cudaMemoryTypeHost && a.devicePointer == p;
+    if (a.type != cudaMemoryTypeDevice && a.type != cudaMemoryTypeManaged && !host_view)
+        return set_error(ASTC_ERR_INVALID_ARG,
+                         std::string(what) + (allow_host_view ? " is not device-accessible memory"
+                                                              : " is not device memory (memory = ASTC_MEMORY_DEVICE)"));
+    if (a.type == cudaMemoryTypeDevice) {
+        int cur = 0;
+        if (cudaGetDevice(&cur) == cudaSuccess && a.device != cur)
+            return set_error(ASTC_ERR_INVALID_ARG, std::string(what) + " is memory of device " +
+                                                       std::to_string(a.device) + ", not of the current device " +
+                                                       std::to_string(cur));
+    }
+    // the allocation that holds p: the whole extent must lie inside it
+    if (PointerAttrsFn fn = pointer_attrs_fn()) {
+        CUpointer_attribute attrs[2] = {CU_POINTER_ATTRIBUTE_RANGE_START_ADDR, CU_POINTER_ATTRIBUTE_RANGE_SIZE};
+        CUdeviceptr start = 0;
+        size_t size = 0;
+        void* data[2] = {&start, &size};
+        if (fn(2, attrs, data, (CUdeviceptr)lo) == CUDA_SUCCESS && size > 0) {
+            if (hi > (uintptr_t)start + size)
+                return set_error(ASTC_ERR_INVALID_ARG, std::string(what) + ": " + std::to_string(bytes) +
+                                                           " bytes from the pointer run past the end of its allocation");
+            if (seen && seen->n < (int)(sizeof(seen->r) / sizeof(seen->r[0]))) {
+                seen->last = seen->n;
+                seen->r[seen->n++] = {(uintptr_t)start, (uintptr_t)start + size};
+            }
+        }
+    }
+    return ASTC_OK;
+}
 
 const void* pinned_device_view(const void* host) {
     if (!host || !zero_copy_enabled()) return nullptr;
@@ -287,8 +345,8 @@ astc_status astc_encode_gpu_pitched(const uint8_t* rgba8, int width, int height,
         job.quality = opts->quality;
 
         if (opts->memory == ASTC_MEMORY_DEVICE) {
-            if ((st = check_device_pointer(rgba8, "rgba8")) != ASTC_OK) return st;
-            if ((st = check_device_pointer(out, "out")) != ASTC_OK) return st;
+            if ((st = check_device_pointer(rgba8, in_bytes, "rgba8")) != ASTC_OK) return st;
+            if ((st = check_device_pointer(out, out_bytes, "out")) != ASTC_OK) return st;
             if (reinterpret_cast<uintptr_t>(rgba8) % 4 != 0)
                 return set_error(ASTC_ERR_INVALID_ARG, "device rgba8 must be 4-byte aligned");
             if (reinterpret_cast<uintptr_t>(out) % 16 != 0)
@@ -503,8 +561,8 @@ astc_status astc_decode_gpu(const uint8_t* blocks, int width, int height, int bl
         const size_t nblk = (size_t)((width + block_w - 1) / block_w) * ((height + block_h - 1) / block_h);
         const size_t in_bytes = 16 * nblk, out_bytes = (size_t)width * height * 4;
         if (memory == ASTC_MEMORY_DEVICE) {
-            if ((st = check_device_pointer(blocks, "blocks")) != ASTC_OK) return st;
-            if ((st = check_device_pointer(out_rgba8, "out_rgba8")) != ASTC_OK) return st;
+            if ((st = check_device_pointer(blocks, in_bytes, "blocks")) != ASTC_OK) return st;
+            if ((st = check_device_pointer(out_rgba8, out_bytes, "out_rgba8")) != ASTC_OK) return st;
             if (reinterpret_cast<uintptr_t>(blocks) % 16 != 0 || reinterpret_cast<uintptr_t>(out_rgba8) % 4 != 0)
                 return set_error(ASTC_ERR_INVALID_ARG, "blocks must be 16-byte and out 4-byte aligned");
             cudaError_t e = launch_decode(blocks, width, height, block_w, block_h, srgb, out_rgba8, s);
@@ -528,10 +586,14 @@ astc_status astc_decode_gpu(const uint8_t* blocks, int width, int height, int bl
     }
 }
 
-astc_status astc_sse_gpu(const uint8_t* a, const uint8_t* b, size_t texels, int memory, void* stream,
-                         uint64_t sse_rgba[4]) {
+// Shared body of the SSE reductions: stages host images through the pool,
+// zeroes the 32-byte accumulator, runs `launch(a, b, accumulator, stream)` and
+// reads the accumulator back into `result` (`result_bytes` of it).
+extern "C++" template <class Launch>
+astc_status sse_common(const uint8_t* a, const uint8_t* b, size_t texels, int memory, void* stream,
+                              void* result, size_t result_bytes, Launch launch) {
     try {
-        if (!a || !b || !sse_rgba) return set_error(ASTC_ERR_INVALID_ARG, "NULL pointer");
+        if (!a || !b || !result) return set_error(ASTC_ERR_INVALID_ARG, "NULL pointer");
         if (memory != ASTC_MEMORY_HOST && memory != ASTC_MEMORY_DEVICE)
             return set_error(ASTC_ERR_INVALID_ARG, "bad memory kind");
         DevicePool* pool = nullptr;
@@ -557,24 +619,41 @@ astc_status astc_sse_gpu(const uint8_t* a, const uint8_t* b, size_t texels, int 
             da = pool->d_in;
             db = pool->d_out;
         } else {
-            if ((st = check_device_pointer(a, "a")) != ASTC_OK) return st;
-            if ((st = check_device_pointer(b, "b")) != ASTC_OK) return st;
+            if ((st = check_device_pointer(a, texels * 4, "a")) != ASTC_OK) return st;
+            if ((st = check_device_pointer(b, texels * 4, "b")) != ASTC_OK) return st;
             if (reinterpret_cast<uintptr_t>(a) % 4 != 0 || reinterpret_cast<uintptr_t>(b) % 4 != 0)
                 return set_error(ASTC_ERR_INVALID_ARG, "images must be 4-byte aligned");
         }
         cudaError_t e = cudaMemsetAsync(pool->d_sse, 0, 4 * sizeof(unsigned long long), s);
         if (e != cudaSuccess) return cuda_error(e, "cudaMemsetAsync");
-        e = launch_sse(da, db, texels, pool->d_sse, s);
+        e = launch(da, db, pool->d_sse, s);
         if (e != cudaSuccess) return cuda_error(e, "sse kernel launch");
         unsigned long long h[4];
         e = cudaMemcpyAsync(h, pool->d_sse, sizeof(h), cudaMemcpyDeviceToHost, s);
         if (e == cudaSuccess) e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) return cuda_error(e, "sse");
-        for (int i = 0; i < 4; ++i) sse_rgba[i] = h[i];
+        memcpy(result, h, result_bytes);
         return ASTC_OK;
     } catch (...) {
         return set_error(ASTC_ERR_CUDA, "unexpected exception");
     }
+}
+
+astc_status astc_sse_gpu(const uint8_t* a, const uint8_t* b, size_t texels, int memory, void* stream,
+                         uint64_t sse_rgba[4]) {
+    return sse_common(a, b, texels, memory, stream, sse_rgba, 4 * sizeof(uint64_t),
+                      [texels](const uint8_t* da, const uint8_t* db, unsigned long long* acc, cudaStream_t s) {
+                          return launch_sse(da, db, texels, acc, s);
+                      });
+}
+
+astc_status astc_normal_sse_gpu(const uint8_t* a, const uint8_t* b, size_t texels, int memory, void* stream,
+                                double* sse) {
+    static_assert(sizeof(double) <= 4 * sizeof(unsigned long long), "accumulator size");
+    return sse_common(a, b, texels, memory, stream, sse, sizeof(double),
+                      [texels](const uint8_t* da, const uint8_t* db, unsigned long long* acc, cudaStream_t s) {
+                          return launch_normal_sse(da, db, texels, reinterpret_cast<double*>(acc), s);
+                      });
 }
 
 astc_status astc_get_device_caps(astc_device_caps* caps) {

@@ -407,7 +407,53 @@ astc_sse_rgba(const uint32_t* __restrict__ a, const uint32_t* __restrict__ b, si
     }
 }
 
+// Squared error of two normal maps in the -norm layout, on the reconstructed
+// unit normals: x, y = code * 2/255 - 1 from R and G, z = sqrt(max(0, 1 - x^2
+// - y^2)); each component's difference is scaled by 127.5 (the [-1, 1] range
+// mapped onto 0..255) so PSNR takes the usual 8-bit peak.  FP64 accumulation.
+__device__ __forceinline__ void normal_of(uint32_t px, float n[3]) {
+    n[0] = (float)(px & 0xFF) * (2.0f / 255.0f) - 1.0f;
+    n[1] = (float)((px >> 8) & 0xFF) * (2.0f / 255.0f) - 1.0f;
+    n[2] = sqrtf(fmaxf(0.0f, 1.0f - n[0] * n[0] - n[1] * n[1]));
+}
+
+__global__ void __launch_bounds__(256)
+astc_normal_sse(const uint32_t* __restrict__ a, const uint32_t* __restrict__ b, size_t n,
+                double* __restrict__ sse) {
+    double acc = 0.0;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x) {
+        float p[3], q[3];
+        normal_of(__ldg(a + i), p);
+        normal_of(__ldg(b + i), q);
+        float t = 0.0f;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const float d = (p[c] - q[c]) * 127.5f;
+            t += d * d;
+        }
+        acc += (double)t;
+    }
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xFFFFFFFFu, acc, o);
+    if ((threadIdx.x & 31) == 0 && acc != 0.0) atomicAdd(sse, acc);
+}
+
 }  // namespace
+
+cudaError_t launch_normal_sse(const uint8_t* a, const uint8_t* b, size_t texels, double* d_sse,
+                              cudaStream_t stream) {
+    if (texels == 0) return cudaSuccess;
+    int dev = 0, sms = 152;
+    if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    long long grid = ((long long)texels + 255) / 256;
+    const long long cap = (long long)sms * 8;
+    if (grid > cap) grid = cap;
+    astc_normal_sse<<<(unsigned)grid, 256, 0, stream>>>(reinterpret_cast<const uint32_t*>(a),
+                                                        reinterpret_cast<const uint32_t*>(b), texels, d_sse);
+    const cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) count_launches(1);
+    return e;
+}
 
 cudaError_t launch_decode(const uint8_t* blocks, int width, int height, int bw, int bh, int srgb,
                           uint8_t* out, cudaStream_t stream) {

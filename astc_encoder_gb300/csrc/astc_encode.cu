@@ -82,10 +82,13 @@ astc_encode_blocks_fp32(const Launch p) {
     }
 }
 
-// Kernel choice per format: texel store and CTA size.  Defaults come from
-// measurements on GB300 (profiles/); the autotuner may replace them.
+// Kernel choice per format and size class: texel store (or the cooperative
+// mapping) and CTA size.  Size class 0 holds launches of fewer blocks than
+// one wave of the one-thread mappings (SMs x 384 blocks), class 1 the rest.
+// Defaults come from measurements on GB300 (profiles/); the autotuner may
+// replace them.
 struct Choice { int store; int threads; };
-Choice g_choice[2][2][2][2] = {};     // [dim6][alpha][normal][srgb]
+Choice g_choice[2][2][2][2][2] = {};     // [class][dim6][alpha][normal][srgb]
 bool g_choice_init = false;
 std::mutex g_choice_mu;
 
@@ -99,7 +102,8 @@ std::mutex g_choice_mu;
 // (its re-reads cost more than the occupancy it gains); capping the register
 // store at 168 (no spills) lifts 6x6 from 8 to 12 warps per SM.  Normal maps
 // (two varying channels) fit in registers without the cap.
-Choice default_choice(int dim, bool /*alpha*/, bool normal, bool /*srgb*/) {
+Choice default_choice(int cls, int dim, bool /*alpha*/, bool normal, bool /*srgb*/) {
+    (void)cls;
     if (normal) return Choice{kStoreRegisters, 128};
     return dim == 6 ? Choice{kStoreRegistersCapped, 128} : Choice{kStoreShared, 128};
 }
@@ -143,17 +147,37 @@ cudaError_t launch_alpha(const Launch& p, bool alpha, bool normal, bool srgb, co
                  : launch_norm<DIM, false>(p, normal, srgb, c, s);
 }
 
-Choice current_choice(int dim, bool alpha, bool normal, bool srgb) {
+Choice current_choice(int cls, int dim, bool alpha, bool normal, bool srgb) {
     std::lock_guard<std::mutex> lk(g_choice_mu);
     if (!g_choice_init) {
-        for (int d = 0; d < 2; ++d)
-            for (int a = 0; a < 2; ++a)
-                for (int n = 0; n < 2; ++n)
-                    for (int r = 0; r < 2; ++r)
-                        g_choice[d][a][n][r] = default_choice(d ? 6 : 4, a, n, r);
+        for (int c = 0; c < 2; ++c)
+            for (int d = 0; d < 2; ++d)
+                for (int a = 0; a < 2; ++a)
+                    for (int n = 0; n < 2; ++n)
+                        for (int r = 0; r < 2; ++r)
+                            g_choice[c][d][a][n][r] = default_choice(c, d ? 6 : 4, a, n, r);
         g_choice_init = true;
     }
-    return g_choice[dim == 6][alpha][normal][srgb];
+    return g_choice[cls][dim == 6][alpha][normal][srgb];
+}
+
+// SM count of the current device, cached per device index
+int sm_count() {
+    static int cache[64] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+        cudaGetLastError();
+        return 152;
+    }
+    if (!cache[dev]) {
+        int sms = 0;
+        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) {
+            cudaGetLastError();
+            sms = 152;
+        }
+        cache[dev] = sms;
+    }
+    return cache[dev];
 }
 
 }  // namespace
@@ -172,8 +196,18 @@ TextureView make_view(const EncodeJob& j) {
     return t;
 }
 
+int encode_size_class(int width, int height, int block_dim) {
+    const long long nb = (long long)blocks_x(width, block_dim) * blocks_y(height, block_dim);
+    return nb < (long long)sm_count() * 384 ? 0 : 1;
+}
+
 cudaError_t launch_encode_variant(const EncodeJob& j, int store, int threads, cudaStream_t stream) {
     if (threads != 32 && threads != 64 && threads != 128 && threads != 256) return cudaErrorInvalidValue;
+    if (store == kStoreCoop) {
+        const cudaError_t e = launch_encode_coop(j, threads, stream);
+        if (e == cudaSuccess) count_launches(1);
+        return e;
+    }
     if (store != kStoreRegisters && store != kStoreShared && store != kStoreRegistersCapped)
         return cudaErrorInvalidValue;
     if (store == kStoreRegistersCapped && threads > 128) return cudaErrorInvalidValue;
@@ -190,18 +224,20 @@ cudaError_t launch_encode_variant(const EncodeJob& j, int store, int threads, cu
 }
 
 cudaError_t launch_encode(const EncodeJob& j, cudaStream_t stream) {
-    const Choice c = current_choice(j.block_dim, j.has_alpha != 0, j.is_normal != 0, j.srgb != 0);
+    const int cls = encode_size_class(j.width, j.height, j.block_dim);
+    const Choice c = current_choice(cls, j.block_dim, j.has_alpha != 0, j.is_normal != 0, j.srgb != 0);
     return launch_encode_variant(j, c.store, c.threads, stream);
 }
 
-void set_encode_choice(int dim, bool alpha, bool normal, bool srgb, int store, int threads) {
-    current_choice(dim, alpha, normal, srgb);
+void set_encode_choice(int dim, bool alpha, bool normal, bool srgb, int store, int threads, int cls) {
+    current_choice(0, dim, alpha, normal, srgb);
     std::lock_guard<std::mutex> lk(g_choice_mu);
-    g_choice[dim == 6][alpha][normal][srgb] = Choice{store, threads};
+    for (int c = 0; c < 2; ++c)
+        if (cls < 0 || cls == c) g_choice[c][dim == 6][alpha][normal][srgb] = Choice{store, threads};
 }
 
-void get_encode_choice(int dim, bool alpha, bool normal, bool srgb, int* store, int* threads) {
-    const Choice c = current_choice(dim, alpha, normal, srgb);
+void get_encode_choice(int dim, bool alpha, bool normal, bool srgb, int* store, int* threads, int cls) {
+    const Choice c = current_choice(cls, dim, alpha, normal, srgb);
     *store = c.store;
     *threads = c.threads;
 }

@@ -26,8 +26,9 @@ template <int DIM, bool ALPHA, bool NORMAL, bool SRGB>
 __global__ void __launch_bounds__(kH2Threads) astc_encode_blocks_h2(const LaunchH2 p) {
     constexpr int N = DIM * DIM;
     __shared__ uint8_t s_trits[256];
-    __shared__ float s_lut[SRGB ? 256 : 1];
-    load_cta_tables<SRGB>(c_trit_pack_h2, c_srgb_bits_h2, s_trits, s_lut);
+    __shared__ uint8_t s_lin8[SRGB ? 256 : 1];
+    load_cta_tables<false>(c_trit_pack_h2, c_srgb_bits_h2, s_trits, nullptr);
+    if (SRGB) load_lin8_table(c_srgb_bits_h2, s_lin8);
     __syncthreads();
     pdl_wait_prior();
     pdl_allow_next();
@@ -37,7 +38,7 @@ __global__ void __launch_bounds__(kH2Threads) astc_encode_blocks_h2(const Launch
     const int bx = (int)(b - (long long)by * p.tex.nbx);
     uint32_t px[N];
     load_block_packed<DIM>(p.tex, bx, by, px);
-    p.out[b] = encode_block_h2<DIM, ALPHA, NORMAL, SRGB>(px, s_lut, s_trits);
+    p.out[b] = encode_block_h2<DIM, ALPHA, NORMAL, SRGB>(px, s_lin8, s_trits);
 }
 
 template <int DIM, bool ALPHA, bool NORMAL, bool SRGB>

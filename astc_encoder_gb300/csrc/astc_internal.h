@@ -54,14 +54,22 @@ cudaError_t launch_pdl(void (*kern)(P...), unsigned grid, unsigned threads, size
 inline int blocks_x(int w, int dim) { return (w + dim - 1) / dim; }
 inline int blocks_y(int h, int dim) { return (h + dim - 1) / dim; }
 
+// The cooperative mapping (four lanes per block; astc_encode_coop.cu),
+// threads per CTA 64/128/256.
+cudaError_t launch_encode_coop(const EncodeJob& job, int threads, cudaStream_t stream);
+
 // Kernel launchers (astc_encode.cu).  Return cudaSuccess or the launch error.
 cudaError_t launch_encode(const EncodeJob& job, cudaStream_t stream);
 // One explicit kernel variant: store 0 = texels in registers, 1 = in shared
 // memory; threads per CTA 32/64/128/256.
 cudaError_t launch_encode_variant(const EncodeJob& job, int store, int threads, cudaStream_t stream);
 // The variant launch_encode uses for a format (process-wide; set by the autotuner).
-void set_encode_choice(int dim, bool alpha, bool normal, bool srgb, int store, int threads);
-void get_encode_choice(int dim, bool alpha, bool normal, bool srgb, int* store, int* threads);
+// Size class of a texture: 0 = fewer blocks than one wave of the
+// one-thread-per-block mappings (SMs x 384), 1 = the rest.  Choices are kept
+// per format and class; cls -1 in set_encode_choice sets both classes.
+int encode_size_class(int width, int height, int block_dim);
+void set_encode_choice(int dim, bool alpha, bool normal, bool srgb, int store, int threads, int cls);
+void get_encode_choice(int dim, bool alpha, bool normal, bool srgb, int* store, int* threads, int cls);
 struct TextureView;
 TextureView make_view(const EncodeJob& job);
 // Packed-half2 pipeline (astc_encode_h2.cu).
@@ -78,8 +86,26 @@ cudaError_t launch_encode_best(const EncodeJob& job, cudaStream_t stream);
 // Decoder / SSE launchers (astc_decode.cu).
 cudaError_t launch_decode(const uint8_t* blocks, int width, int height, int bw, int bh,
                           int srgb, uint8_t* out, cudaStream_t stream);
+cudaError_t launch_normal_sse(const uint8_t* a, const uint8_t* b, size_t texels, double* d_sse,
+                              cudaStream_t stream);
 cudaError_t launch_sse(const uint8_t* a, const uint8_t* b, size_t texels,
                        unsigned long long* d_sse4, cudaStream_t stream);
+
+// Pointer checks (astc_capi.cu).  check_device_span accepts [p, p + bytes)
+// when it is device memory of the current device or managed memory (and,
+// with allow_host_view, the device view of pinned host memory), lying inside
+// one allocation.  `seen` (may be NULL) collects the allocation ranges already
+// checked, so a call that passes many pointers into the same allocations
+// queries each allocation once; keep it for one call only (an address that is
+// freed and reused between calls is checked again).
+struct SpanCache {
+    struct Range { uintptr_t lo, hi; };
+    Range r[256];
+    int n = 0;
+    int last = 0;      // the range that matched last (pointers tend to repeat it)
+};
+astc_status check_device_span(const void* p, size_t bytes, const char* what, bool allow_host_view,
+                              SpanCache* seen);
 
 // Error plumbing (astc_capi.cu).
 astc_status set_error(astc_status st, const std::string& msg);

@@ -109,18 +109,6 @@ astc_status noalloc_scratch(unsigned long long** out) {
     return ASTC_OK;
 }
 
-astc_status check_device_ptr(const void* ptr, const char* what) {
-    cudaPointerAttributes at;
-    const cudaError_t e = cudaPointerGetAttributes(&at, ptr);
-    if (e != cudaSuccess) {
-        cudaGetLastError();
-        return set_error(ASTC_ERR_INVALID_ARG, std::string(what) + " is not a CUDA pointer");
-    }
-    if (at.type != cudaMemoryTypeDevice && at.type != cudaMemoryTypeManaged)
-        return set_error(ASTC_ERR_INVALID_ARG, std::string(what) + " is not device memory");
-    return ASTC_OK;
-}
-
 }  // namespace
 }  // namespace astc
 
@@ -141,9 +129,11 @@ extern "C" astc_status astc_sse_gpu_noalloc(const uint8_t* a, const uint8_t* b, 
             return set_error(ASTC_ERR_INVALID_ARG,
                              "images must be 4-byte and the output 8-byte aligned");
         astc_status st;
-        if ((st = check_device_ptr(a, "a")) != ASTC_OK) return st;
-        if ((st = check_device_ptr(b, "b")) != ASTC_OK) return st;
-        if ((st = check_device_ptr(sse_rgba, "sse_rgba")) != ASTC_OK) return st;
+        // device memory of the current device, each extent inside its allocation
+        if ((st = check_device_span(a, texels * 4, "a", false, nullptr)) != ASTC_OK) return st;
+        if ((st = check_device_span(b, texels * 4, "b", false, nullptr)) != ASTC_OK) return st;
+        if ((st = check_device_span(sse_rgba, 4 * sizeof(uint64_t), "sse_rgba", false, nullptr)) != ASTC_OK)
+            return st;
         unsigned long long* scratch = nullptr;
         if ((st = noalloc_scratch(&scratch)) != ASTC_OK) return st;
         cudaStream_t s = static_cast<cudaStream_t>(stream);

@@ -175,6 +175,30 @@ __device__ __forceinline__ float4 max_accumulation_axis(const S& st, const float
     return make_float4(k0, k1, k2, k3);
 }
 
+// The end of find_min_max (120-136): clamped endpoints m + v * a and
+// m + v * b from the extreme projections a, b, the darker (rounded RGB sum)
+// first; !ALPHA forces alpha 255.
+template <bool ALPHA>
+__device__ __forceinline__ void endpoints_from_range(const float4 m, const float4 v, float a, float b, float e0[4],
+                                                     float e1[4], uint32_t q0[4], uint32_t q1[4]) {
+    const float mv[4] = {m.x, m.y, m.z, m.w}, vv[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        e0[c] = fminf(fmaxf(__fmaf_rn(vv[c], a, mv[c]), 0.0f), 255.0f);
+        e1[c] = fminf(fmaxf(__fmaf_rn(vv[c], b, mv[c]), 0.0f), 255.0f);
+    }
+#pragma unroll
+    for (int c = 0; c < 4; ++c) { q0[c] = rint_u32(e0[c]); q1[c] = rint_u32(e1[c]); }
+    if (q0[0] + q0[1] + q0[2] > q1[0] + q1[1] + q1[2]) {      // dark endpoint first
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            const float tf = e0[c]; e0[c] = e1[c]; e1[c] = tf;
+            const uint32_t tq = q0[c]; q0[c] = q1[c]; q1[c] = tq;
+        }
+    }
+    if (!ALPHA) { e0[3] = 255.0f; e1[3] = 255.0f; q0[3] = 255u; q1[3] = 255u; }
+}
+
 // find_min_max (108-137): extreme projections on the axis, clamped
 // endpoints, the darker (rounded RGB sum) first; !ALPHA forces alpha 255.
 // e0/e1 are the float endpoints, q0/q1 their rounded (QUANT_256) values.
@@ -192,22 +216,7 @@ __device__ __forceinline__ void find_min_max(const S& st, const float4 m, const 
         a = fminf(a, p);
         b = fmaxf(b, p);
     }
-    const float mv[4] = {m.x, m.y, m.z, m.w}, vv[4] = {v.x, v.y, v.z, v.w};
-#pragma unroll
-    for (int c = 0; c < 4; ++c) {
-        e0[c] = fminf(fmaxf(__fmaf_rn(vv[c], a, mv[c]), 0.0f), 255.0f);
-        e1[c] = fminf(fmaxf(__fmaf_rn(vv[c], b, mv[c]), 0.0f), 255.0f);
-    }
-#pragma unroll
-    for (int c = 0; c < 4; ++c) { q0[c] = rint_u32(e0[c]); q1[c] = rint_u32(e1[c]); }
-    if (q0[0] + q0[1] + q0[2] > q1[0] + q1[1] + q1[2]) {      // dark endpoint first
-#pragma unroll
-        for (int c = 0; c < 4; ++c) {
-            const float tf = e0[c]; e0[c] = e1[c]; e1[c] = tf;
-            const uint32_t tq = q0[c]; q0[c] = q1[c]; q1[c] = tq;
-        }
-    }
-    if (!ALPHA) { e0[3] = 255.0f; e1[3] = 255.0f; q0[3] = 255u; q1[3] = 255u; }
+    endpoints_from_range<ALPHA>(m, v, a, b, e0, e1, q0, q1);
 }
 
 // the colour at weight-grid point g: the texel (4x4) or sample_texel's 2x2

@@ -5,17 +5,24 @@
 // encode_block 510-550: PCA axis by 8 power iterations, min/max projection
 // endpoints, 4x4-grid weights, QUANT_6/12 weights, QUANT_256 endpoints), with
 // the arithmetic split by what each stage needs:
-//   * mean and covariance: for UNORM8 input, exact integer sums -- four texels
-//     are byte-transposed (8 byte_perms) and every sum and cross product is a
-//     __dp4a -- so the covariance is exact up to one final FP32 rounding; for
-//     sRGB input, one FP32 pass over the linearised values;
-//   * power iteration, endpoint fit and rounding: FP32, with the hardware
-//     reciprocal square root for the normalisations;
+//   * texels: sRGB input is first mapped to linear light rounded to bytes
+//     (a 256-byte table: the same bytes a linear decode of the block is
+//     compared with), so every texel is an 8-bit integer from here on;
+//   * mean and covariance: exact integer sums -- four texels are
+//     byte-transposed (8 byte_perms) and every sum and cross product is a
+//     __dp4a -- so the covariance is exact up to one final FP32 rounding;
+//   * power iteration: FP32, as M^16 v0 (the direction the shader's eight
+//     rounds of v = normalize(M (M v)) reach): M is squared twice, each time
+//     scaled by its trace, then applied four times and normalised once;
+//   * endpoint fit and rounding: FP32, with the hardware reciprocal square
+//     root for the normalisations;
 //   * per-texel projection (find_min_max) and weights: packed half2, two
 //     channels per instruction, on differences (texel - mean, texel - the
 //     endpoints' midpoint) so the values stay small and a rounding of the
 //     reference point only shifts every texel by the same amount, which the
-//     min/max normalisation removes; 0..255 texels are exact in FP16;
+//     min/max normalisation removes; 0..255 texels are exact in FP16; the
+//     6x6 grid weights are the 2x2 tap sums of the texels' projections (the
+//     projection is linear, so this equals projecting the tap sums);
 //   * weight quantisation: one half2 FMA plus the 1024 magic add (FP16 has
 //     unit spacing at 1024, so the add rounds half to even).
 // Blocks are not bit-identical to the FP32 oracle; the gate is PSNR against
@@ -52,15 +59,106 @@ __device__ __forceinline__ __half2 pair_dot(__half2 s_i, __half2 s_j) {
     return __hadd2(__lows2half2(s_i, s_j), __highs2half2(s_i, s_j));
 }
 
+// sRGB -> linear light x 255 rounded to a byte, per channel (alpha stays)
+__device__ __forceinline__ uint32_t srgb_to_lin8(uint32_t px, const uint8_t* lin8) {
+    const uint32_t r = lin8[px & 0xFFu], g = lin8[(px >> 8) & 0xFFu], b = lin8[(px >> 16) & 0xFFu];
+    return r | (g << 8) | (b << 16) | (px & 0xFF000000u);
+}
+
+// Per-CTA table: the rounded FP32 texel values of the sRGB codes (the bytes
+// a linear decode is measured against).
+__device__ __forceinline__ void load_lin8_table(const SrgbBits& sb, uint8_t* s_lin8) {
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) {
+        const uint32_t q = rint_u32(__uint_as_float(sb.v[i]));
+        s_lin8[i] = (uint8_t)(q < 255u ? q : 255u);
+    }
+}
+
+// The principal axis of the symmetric 4x4 matrix c as the direction of
+// M^16 v0, v0 = (0.26726, 0.80178, 0.53452, 0) -- where the shader's eight
+// rounds of v = M v; v = normalize(M v) lead (eigen_vector,
+// ASTC_Encode.hlsl:93-106).  M is divided by its trace and squared, twice,
+// then applied four times; one normalisation at the end.  A zero matrix (a
+// flat block) gives the zero axis, as the shader's early return does.
+__device__ __forceinline__ float4 axis_by_squaring(float c00, float c01, float c02, float c03, float c11,
+                                                   float c12, float c13, float c22, float c23, float c33) {
+    float tr = c00 + c11 + c22 + c33;
+    if (!(tr > 0.0f)) return make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+        const float r = __frcp_rn(tr);
+        c00 *= r; c01 *= r; c02 *= r; c03 *= r; c11 *= r; c12 *= r; c13 *= r; c22 *= r; c23 *= r; c33 *= r;
+        const float n00 = dot4(c00, c01, c02, c03, c00, c01, c02, c03);
+        const float n01 = dot4(c00, c01, c02, c03, c01, c11, c12, c13);
+        const float n02 = dot4(c00, c01, c02, c03, c02, c12, c22, c23);
+        const float n03 = dot4(c00, c01, c02, c03, c03, c13, c23, c33);
+        const float n11 = dot4(c01, c11, c12, c13, c01, c11, c12, c13);
+        const float n12 = dot4(c01, c11, c12, c13, c02, c12, c22, c23);
+        const float n13 = dot4(c01, c11, c12, c13, c03, c13, c23, c33);
+        const float n22 = dot4(c02, c12, c22, c23, c02, c12, c22, c23);
+        const float n23 = dot4(c02, c12, c22, c23, c03, c13, c23, c33);
+        const float n33 = dot4(c03, c13, c23, c33, c03, c13, c23, c33);
+        c00 = n00; c01 = n01; c02 = n02; c03 = n03; c11 = n11; c12 = n12; c13 = n13; c22 = n22; c23 = n23;
+        c33 = n33;
+        tr = c00 + c11 + c22 + c33;
+        if (!(tr > 0.0f)) return make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    }
+    float v0 = 0.26726f, v1 = 0.80178f, v2 = 0.53452f, v3 = 0.0f;
+#pragma unroll
+    for (int it = 0; it < 4; ++it) {
+        const float t0 = dot4(c00, c01, c02, c03, v0, v1, v2, v3);
+        const float t1 = dot4(c01, c11, c12, c13, v0, v1, v2, v3);
+        const float t2 = dot4(c02, c12, c22, c23, v0, v1, v2, v3);
+        const float t3 = dot4(c03, c13, c23, c33, v0, v1, v2, v3);
+        v0 = t0; v1 = t1; v2 = t2; v3 = t3;
+    }
+    const float d = dot4(v0, v1, v2, v3, v0, v1, v2, v3);
+    if (!(d > 1e-30f)) return make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    const float r = rsqrtf(d);
+    return make_float4(v0 * r, v1 * r, v2 * r, v3 * r);
+}
+
+// axis_by_squaring for a matrix whose rows and columns 2 and 3 are zero
+// (normal maps: blue and alpha are the constant 255)
+__device__ __forceinline__ float4 axis_by_squaring_zw(float c00, float c01, float c11) {
+    float tr = c00 + c11;
+    if (!(tr > 0.0f)) return make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+        const float r = __frcp_rn(tr);
+        c00 *= r; c01 *= r; c11 *= r;
+        const float n00 = __fmaf_rn(c01, c01, c00 * c00);
+        const float n01 = c01 * (c00 + c11);
+        const float n11 = __fmaf_rn(c11, c11, c01 * c01);
+        c00 = n00; c01 = n01; c11 = n11;
+        tr = c00 + c11;
+        if (!(tr > 0.0f)) return make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    }
+    float v0 = 0.26726f, v1 = 0.80178f;
+#pragma unroll
+    for (int it = 0; it < 4; ++it) {
+        const float t0 = __fmaf_rn(c01, v1, c00 * v0);
+        const float t1 = __fmaf_rn(c11, v1, c01 * v0);
+        v0 = t0; v1 = t1;
+    }
+    const float d = __fmaf_rn(v1, v1, v0 * v0);
+    if (!(d > 1e-30f)) return make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    const float r = rsqrtf(d);
+    return make_float4(v0 * r, v1 * r, 0.0f, 0.0f);
+}
+
 template <int DIM, bool ALPHA, bool NORMAL, bool SRGB>
-__device__ __forceinline__ uint4 encode_block_h2(const uint32_t (&px)[DIM * DIM], const float* lut,
+__device__ __forceinline__ uint4 encode_block_h2(const uint32_t (&px_in)[DIM * DIM], const uint8_t* lin8,
                                                  const uint8_t* trits) {
     constexpr int N = DIM * DIM;
     float m0, m1, m2, m3;
     float c00, c01, c02, c03, c11, c12, c13, c22, c23, c33;
     __half2 trg[N], tba[N];                                // texels as (r,g), (b,a)
+    uint32_t px[N];
+#pragma unroll
+    for (int k = 0; k < N; ++k) px[k] = SRGB ? srgb_to_lin8(px_in[k], lin8) : px_in[k];
 
-    if constexpr (!SRGB) {
+    {
         // exact integer moments: S_c and S_cd over the block
         uint32_t sr = 0, sg = 0, sb = 0, sa = 0;
         uint32_t srr = 0, srg = 0, srb = 0, sra = 0, sgg = 0, sgb = 0, sga = 0, sbb = 0, sba = 0, saa = 0;
@@ -109,51 +207,12 @@ __device__ __forceinline__ uint4 encode_block_h2(const uint32_t (&px)[DIM * DIM]
             trg[k] = bytes_to_half2(px[k], 0x4140u);
             tba[k] = NORMAL ? __floats2half2_rn(255.0f, 255.0f) : bytes_to_half2(px[k], 0x4342u);
         }
-    } else {
-        // sRGB: one FP32 pass over the linearised texels
-        float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
-        float q00 = 0.f, q01 = 0.f, q02 = 0.f, q03 = 0.f, q11 = 0.f, q12 = 0.f, q13 = 0.f,
-              q22 = 0.f, q23 = 0.f, q33 = 0.f;
-#pragma unroll
-        for (int k = 0; k < N; ++k) {
-            const float4 t = decode_texel<true, NORMAL>(px[k], lut);
-            s0 += t.x; s1 += t.y; s2 += t.z; s3 += t.w;
-            q00 = fmaf(t.x, t.x, q00); q01 = fmaf(t.x, t.y, q01); q02 = fmaf(t.x, t.z, q02);
-            q03 = fmaf(t.x, t.w, q03); q11 = fmaf(t.y, t.y, q11); q12 = fmaf(t.y, t.z, q12);
-            q13 = fmaf(t.y, t.w, q13); q22 = fmaf(t.z, t.z, q22); q23 = fmaf(t.z, t.w, q23);
-            q33 = fmaf(t.w, t.w, q33);
-            trg[k] = __floats2half2_rn(t.x, t.y);
-            tba[k] = __floats2half2_rn(t.z, t.w);
-        }
-        constexpr float kInvN = 1.0f / (float)N;
-        constexpr float kInvN1 = 1.0f / (float)(N - 1);
-        m0 = s0 * kInvN; m1 = s1 * kInvN; m2 = s2 * kInvN; m3 = s3 * kInvN;
-        c00 = (q00 - s0 * m0) * kInvN1; c01 = (q01 - s0 * m1) * kInvN1; c02 = (q02 - s0 * m2) * kInvN1;
-        c03 = (q03 - s0 * m3) * kInvN1; c11 = (q11 - s1 * m1) * kInvN1; c12 = (q12 - s1 * m2) * kInvN1;
-        c13 = (q13 - s1 * m3) * kInvN1; c22 = (q22 - s2 * m2) * kInvN1; c23 = (q23 - s2 * m3) * kInvN1;
-        c33 = (q33 - s3 * m3) * kInvN1;
-        if (NORMAL) { c02 = c03 = c12 = c13 = c22 = c23 = c33 = 0.0f; m2 = m3 = 255.0f; }
     }
 
-    // power iteration (ASTC_Encode.hlsl:93-106), FP32, hardware rsqrt
-    float v0 = 0.26726f, v1 = 0.80178f, v2 = 0.53452f, v3 = 0.0f;
-#pragma unroll 1
-    for (int it = 0; it < 8; ++it) {
-        float t0 = dot4(c00, c01, c02, c03, v0, v1, v2, v3);
-        float t1 = dot4(c01, c11, c12, c13, v0, v1, v2, v3);
-        float t2 = dot4(c02, c12, c22, c23, v0, v1, v2, v3);
-        float t3 = dot4(c03, c13, c23, c33, v0, v1, v2, v3);
-        if (shorter_than_small_value(dot4(t0, t1, t2, t3, t0, t1, t2, t3))) {
-            v0 = t0; v1 = t1; v2 = t2; v3 = t3;
-            break;
-        }
-        const float u0 = dot4(c00, c01, c02, c03, t0, t1, t2, t3);
-        const float u1 = dot4(c01, c11, c12, c13, t0, t1, t2, t3);
-        const float u2 = dot4(c02, c12, c22, c23, t0, t1, t2, t3);
-        const float u3 = dot4(c03, c13, c23, c33, t0, t1, t2, t3);
-        const float r = rsqrtf(dot4(u0, u1, u2, u3, u0, u1, u2, u3));
-        v0 = u0 * r; v1 = u1 * r; v2 = u2 * r; v3 = u3 * r;
-    }
+    // power iteration (ASTC_Encode.hlsl:93-106): the direction of M^16 v0, FP32
+    const float4 ax = NORMAL ? axis_by_squaring_zw(c00, c01, c11)
+                             : axis_by_squaring(c00, c01, c02, c03, c11, c12, c13, c22, c23, c33);
+    const float v0 = ax.x, v1 = ax.y, v2 = ax.z, v3 = ax.w;
 
     // find_min_max (108-137): projections of (texel - mean) in half2
     const __half2 mrg = __floats2half2_rn(m0, m1), mba = __floats2half2_rn(m2, m3);
@@ -211,40 +270,54 @@ __device__ __forceinline__ uint4 encode_block_h2(const uint32_t (&px)[DIM * DIM]
         const bool use_ba = !NORMAL;                     // normal maps: e0.ba == e1.ba, k.b = k.a = 0
         __half2 wv[8];
         __half2 wmin = __floats2half2_rn(65504.0f, 65504.0f), wmax = __floats2half2_rn(-65504.0f, -65504.0f);
+        if constexpr (DIM == 6) {
+            // the texels' projections, in pairs (q_2i, q_2i+1)
+            __half2 qp[N / 2];
 #pragma unroll
-        for (int i = 0; i < 16; i += 2) {
-            __half2 s[2];
-#pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                const int g = i + h;
-                __half2 drg, dba;
-                if constexpr (DIM == 6) {
-                    const int i0 = grid_tap0(g);
-                    float f00, f01, f10, f11;
-                    grid_weights(g, f00, f01, f10, f11);
-                    const __half2 h00 = __float2half2_rn(f00), h01 = __float2half2_rn(f01),
-                                  h10 = __float2half2_rn(f10), h11 = __float2half2_rn(f11);
-                    drg = __hmul2(__hsub2(trg[i0], erg), h00);
-                    drg = __hfma2(__hsub2(trg[i0 + 1], erg), h01, drg);
-                    drg = __hfma2(__hsub2(trg[i0 + 6], erg), h10, drg);
-                    drg = __hfma2(__hsub2(trg[i0 + 7], erg), h11, drg);
-                    if (use_ba) {
-                        dba = __hmul2(__hsub2(tba[i0], eba), h00);
-                        dba = __hfma2(__hsub2(tba[i0 + 1], eba), h01, dba);
-                        dba = __hfma2(__hsub2(tba[i0 + 6], eba), h10, dba);
-                        dba = __hfma2(__hsub2(tba[i0 + 7], eba), h11, dba);
-                    }
-                } else {
-                    drg = __hsub2(trg[g], erg);
-                    if (use_ba) dba = __hsub2(tba[g], eba);
+            for (int i = 0; i < N / 2; ++i) {
+                __half2 sa = __hmul2(__hsub2(trg[2 * i], erg), wrg);
+                __half2 sb = __hmul2(__hsub2(trg[2 * i + 1], erg), wrg);
+                if (use_ba) {
+                    sa = __hfma2(__hsub2(tba[2 * i], eba), wba, sa);
+                    sb = __hfma2(__hsub2(tba[2 * i + 1], eba), wba, sb);
                 }
-                s[h] = __hmul2(drg, wrg);
-                if (use_ba) s[h] = __hfma2(dba, wba, s[h]);
+                qp[i] = pair_dot(sa, sb);
             }
-            const __half2 p = pair_dot(s[0], s[1]);
-            wv[i / 2] = p;
-            wmin = __hmin2(wmin, p);
-            wmax = __hmax2(wmax, p);
+            // (q_t, q_t+1) of consecutive texels t, t+1
+            auto pair_at = [&](int t) -> __half2 {
+                return (t & 1) ? __halves2half2(__high2half(qp[t >> 1]), __low2half(qp[(t >> 1) + 1]))
+                               : qp[t >> 1];
+            };
+            // grid points g, g+1 of a row sample texel columns one apart: the
+            // 2x2 taps of the pair are four consecutive-texel pairs
+#pragma unroll
+            for (int i = 0; i < 16; i += 2) {
+                const int t0 = grid_tap0(i);                 // grid_tap0(i + 1) == t0 + 1
+                float fa[4], fb[4];
+                grid_weights(i, fa[0], fa[1], fa[2], fa[3]);
+                grid_weights(i + 1, fb[0], fb[1], fb[2], fb[3]);
+                __half2 p = __hmul2(pair_at(t0), __floats2half2_rn(fa[0], fb[0]));
+                p = __hfma2(pair_at(t0 + 1), __floats2half2_rn(fa[1], fb[1]), p);
+                p = __hfma2(pair_at(t0 + 6), __floats2half2_rn(fa[2], fb[2]), p);
+                p = __hfma2(pair_at(t0 + 7), __floats2half2_rn(fa[3], fb[3]), p);
+                wv[i / 2] = p;
+                wmin = __hmin2(wmin, p);
+                wmax = __hmax2(wmax, p);
+            }
+        } else {
+#pragma unroll
+            for (int i = 0; i < 16; i += 2) {
+                __half2 sa = __hmul2(__hsub2(trg[i], erg), wrg);
+                __half2 sb = __hmul2(__hsub2(trg[i + 1], erg), wrg);
+                if (use_ba) {
+                    sa = __hfma2(__hsub2(tba[i], eba), wba, sa);
+                    sb = __hfma2(__hsub2(tba[i + 1], eba), wba, sb);
+                }
+                const __half2 p = pair_dot(sa, sb);
+                wv[i / 2] = p;
+                wmin = __hmin2(wmin, p);
+                wmax = __hmax2(wmax, p);
+            }
         }
         const __half lo_h = __hmin(__low2half(wmin), __high2half(wmin));   // exact: one of the w
         const float lo = __half2float(lo_h);

@@ -99,6 +99,7 @@ struct Req {
 struct Slot {
     cudaStream_t stream = nullptr;
     cudaEvent_t done = nullptr;
+    cudaEvent_t t_start = nullptr, t_end = nullptr;   // timing: the slot's work on the device
     astc_batch* batch = nullptr;
     std::vector<Req*> reqs;
     bool busy = false;
@@ -107,6 +108,13 @@ struct Slot {
 double us_since(Clock::time_point t0, Clock::time_point t) {
     return std::chrono::duration<double, std::micro>(t - t0).count();
 }
+
+// One retired slot launch: its device interval (ms after the server's
+// reference event) and how many requests it carried.
+struct Interval {
+    float start_ms, end_ms;
+    int requests;
+};
 
 }  // namespace
 }  // namespace astc
@@ -128,13 +136,16 @@ struct astc_server {
     std::thread worker;
     Clock::time_point t0 = Clock::now();
     std::string worker_error;
+    cudaEvent_t t0_event = nullptr;          // device clock origin of the intervals
+    std::vector<Interval> intervals;         // retired launches since the last reset
 };
 
 namespace {
 
 // Issues one slot's copies, encode and event.  Called without the lock.
 cudaError_t launch_slot(astc_server* s, Slot& slot) {
-    cudaError_t e = cudaSuccess;
+    cudaError_t e = cudaEventRecord(slot.t_start, slot.stream);
+    if (e != cudaSuccess) return e;
     std::vector<astc_batch_item> items;
     items.reserve(slot.reqs.size());
     for (Req* q : slot.reqs) {
@@ -200,6 +211,7 @@ cudaError_t launch_slot(astc_server* s, Slot& slot) {
         e = cudaMemcpyAsync(q->r.out, d_out, q->out_bytes, cudaMemcpyDeviceToHost, slot.stream);
         if (e != cudaSuccess) return e;
     }
+    if ((e = cudaEventRecord(slot.t_end, slot.stream)) != cudaSuccess) return e;
     return cudaEventRecord(slot.done, slot.stream);
 }
 
@@ -222,6 +234,12 @@ void worker_main(astc_server* s) {
             }
             if (q != cudaSuccess) {
                 s->worker_error = cudaGetErrorString(q);
+                cudaGetLastError();
+            } else {
+                float a = 0.0f, b = 0.0f;
+                if (cudaEventElapsedTime(&a, s->t0_event, slot.t_start) == cudaSuccess &&
+                    cudaEventElapsedTime(&b, s->t0_event, slot.t_end) == cudaSuccess)
+                    s->intervals.push_back({a, b, (int)slot.reqs.size()});
                 cudaGetLastError();
             }
             slot.reqs.clear();
@@ -304,13 +322,20 @@ astc_status astc_server_create(const astc_server_config* cfg, astc_server** out)
     astc_status st = ASTC_OK;
     for (Slot& slot : s->slots) {
         if ((e = cudaStreamCreateWithFlags(&slot.stream, cudaStreamNonBlocking)) != cudaSuccess ||
-            (e = cudaEventCreateWithFlags(&slot.done, cudaEventDisableTiming)) != cudaSuccess) {
+            (e = cudaEventCreateWithFlags(&slot.done, cudaEventDisableTiming)) != cudaSuccess ||
+            (e = cudaEventCreate(&slot.t_start)) != cudaSuccess || (e = cudaEventCreate(&slot.t_end)) != cudaSuccess) {
             st = cuda_error(e, "stream/event creation");
             break;
         }
         if (cfg->mode == ASTC_SERVE_BATCHED &&
             (st = astc_batch_create(cfg->max_batch, (long long)(s->cfg.pool_bytes / 16), &slot.batch)) != ASTC_OK)
             break;
+    }
+    if (st == ASTC_OK) {
+        if ((e = cudaEventCreate(&s->t0_event)) != cudaSuccess ||
+            (e = cudaEventRecord(s->t0_event, s->slots[0].stream)) != cudaSuccess ||
+            (e = cudaEventSynchronize(s->t0_event)) != cudaSuccess)
+            st = cuda_error(e, "reference event");
     }
     if (st != ASTC_OK) {
         astc_server_destroy(s.release());
@@ -423,6 +448,45 @@ astc_status astc_server_replay(astc_server* s, const astc_request* reqs, const d
     return first_err;
 }
 
+astc_status astc_server_get_stats(astc_server* s, int reset, astc_server_stats* out) {
+    if (!s || !out) return set_error(ASTC_ERR_INVALID_ARG, "NULL argument");
+    std::vector<Interval> iv;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        iv = s->intervals;
+        if (reset) s->intervals.clear();
+    }
+    memset(out, 0, sizeof(*out));
+    out->launches = (long long)iv.size();
+    if (iv.empty()) return ASTC_OK;
+    // sweep over the interval ends: time with >= 1 and >= 2 slots on the device
+    std::vector<std::pair<double, int>> ev;
+    ev.reserve(2 * iv.size());
+    double first = 1e300, last = -1e300;
+    for (const Interval& v : iv) {
+        out->requests += v.requests;
+        out->max_requests_per_launch = std::max(out->max_requests_per_launch, v.requests);
+        const double a = v.start_ms * 1e-3, b = std::max(v.start_ms, v.end_ms) * 1e-3;
+        out->device_slot_s += b - a;
+        ev.push_back({a, +1});
+        ev.push_back({b, -1});
+        first = std::min(first, a);
+        last = std::max(last, b);
+    }
+    std::sort(ev.begin(), ev.end());
+    int depth = 0;
+    double prev = ev.front().first;
+    for (const auto& p : ev) {
+        const double dt = p.first - prev;
+        if (depth >= 1) out->device_busy_s += dt;
+        if (depth >= 2) out->device_overlap_s += dt;
+        depth += p.second;
+        prev = p.first;
+    }
+    out->device_span_s = last - first;
+    return ASTC_OK;
+}
+
 astc_status astc_server_destroy(astc_server* s) {
     if (!s) return ASTC_OK;
     if (s->worker.joinable()) {
@@ -440,8 +504,11 @@ astc_status astc_server_destroy(astc_server* s) {
         if (slot.stream) cudaStreamSynchronize(slot.stream);
         if (slot.batch) astc_batch_destroy(slot.batch);
         if (slot.done) cudaEventDestroy(slot.done);
+        if (slot.t_start) cudaEventDestroy(slot.t_start);
+        if (slot.t_end) cudaEventDestroy(slot.t_end);
         if (slot.stream) cudaStreamDestroy(slot.stream);
     }
+    if (s->t0_event) cudaEventDestroy(s->t0_event);
     if (s->d_pool) cudaFree(s->d_pool);
     if (have) cudaSetDevice(cur);
     cudaGetLastError();

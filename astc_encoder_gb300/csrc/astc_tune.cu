@@ -1,16 +1,19 @@
 // astc_tune.cu -- autotuner for the encode kernel variants.
 //
-// The encoder has one thread per ASTC block (the reference's mapping,
-// ASTC_Encode.hlsl:553-561) and three ways to keep a block's decoded texels:
-// registers, a [texel][thread] shared-memory array, or registers with the
-// count capped near 168 (6x6: 36 float4 per block otherwise hold the register
-// count near 255 and the SM near 8 warps).  The CTA size trades scheduling
-// slack against shared memory.  astc_autotune times every (store, CTA size)
-// candidate for a format on a synthetic texture of the caller's size on the
-// current device and installs the fastest for that format in this process --
-// unless it beats the format's current choice by less than 3%, which then
-// stays (timing noise, e.g. under a profiler that serialises launches, does
-// not move the choice).
+// Two mappings of blocks to threads: one thread per ASTC block (the
+// reference's, ASTC_Encode.hlsl:553-561) with three ways to keep a block's
+// decoded texels -- registers, a [texel][thread] shared-memory array, or
+// registers with the count capped near 168 (6x6: 36 float4 per block
+// otherwise hold the register count near 255 and the SM near 8 warps) -- and
+// the cooperative mapping, four lanes per block (astc_encode_coop.cu), whose
+// shorter per-block path pays for launches that do not fill the GPU.  The CTA
+// size trades scheduling slack against shared memory.  astc_autotune times
+// every (mapping/store, CTA size) candidate for a format on a synthetic
+// texture of the caller's size on the current device and installs the
+// fastest for that format and size class (under one wave of the one-thread
+// mappings, or not) in this process -- unless it beats the current choice by
+// less than 3%, which then stays (timing noise, e.g. under a profiler that
+// serialises launches, does not move the choice).
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -47,12 +50,24 @@ extern "C" {
 astc_status astc_set_kernel_choice(int block_dim, int has_alpha, int is_normal, int srgb, int store,
                                    int threads) {
     if (block_dim != 4 && block_dim != 6) return set_error(ASTC_ERR_INVALID_ARG, "block_dim must be 4 or 6");
-    if (store < 0 || store > 2) return set_error(ASTC_ERR_INVALID_ARG, "store must be 0, 1 or 2");
+    if (store < 0 || store > 3) return set_error(ASTC_ERR_INVALID_ARG, "store must be 0, 1, 2 or 3");
     if (store == 2 && threads > 128)
         return set_error(ASTC_ERR_INVALID_ARG, "the capped-register store takes at most 128 threads");
     if (threads != 32 && threads != 64 && threads != 128 && threads != 256)
         return set_error(ASTC_ERR_INVALID_ARG, "threads must be 32, 64, 128 or 256");
-    set_encode_choice(block_dim, has_alpha != 0, is_normal != 0, srgb != 0, store, threads);
+    if (store == 3 && threads < 64)
+        return set_error(ASTC_ERR_INVALID_ARG, "the cooperative mapping takes 64, 128 or 256 threads");
+    set_encode_choice(block_dim, has_alpha != 0, is_normal != 0, srgb != 0, store, threads, -1);
+    return ASTC_OK;
+}
+
+astc_status astc_get_kernel_choice_for_size(int block_dim, int has_alpha, int is_normal, int srgb, int width,
+                                            int height, int* store, int* threads) {
+    if (block_dim != 4 && block_dim != 6) return set_error(ASTC_ERR_INVALID_ARG, "block_dim must be 4 or 6");
+    if (!store || !threads) return set_error(ASTC_ERR_INVALID_ARG, "NULL pointer");
+    if (width <= 0 || height <= 0) return set_error(ASTC_ERR_INVALID_ARG, "bad size");
+    get_encode_choice(block_dim, has_alpha != 0, is_normal != 0, srgb != 0, store, threads,
+                      encode_size_class(width, height, block_dim));
     return ASTC_OK;
 }
 
@@ -60,7 +75,7 @@ astc_status astc_get_kernel_choice(int block_dim, int has_alpha, int is_normal, 
                                    int* threads) {
     if (block_dim != 4 && block_dim != 6) return set_error(ASTC_ERR_INVALID_ARG, "block_dim must be 4 or 6");
     if (!store || !threads) return set_error(ASTC_ERR_INVALID_ARG, "NULL pointer");
-    get_encode_choice(block_dim, has_alpha != 0, is_normal != 0, srgb != 0, store, threads);
+    get_encode_choice(block_dim, has_alpha != 0, is_normal != 0, srgb != 0, store, threads, 1);
     return ASTC_OK;
 }
 
@@ -107,13 +122,14 @@ astc_status astc_autotune(int block_dim, int has_alpha, int is_normal, int srgb,
         job.border = ASTC_BORDER_CLAMP;
         job.precision = ASTC_PRECISION_FP32;
         job.out = d_out;
+        const int cls = encode_size_class(width, height, block_dim);
         int def_store = 0, def_threads = 128;
-        get_encode_choice(block_dim, has_alpha != 0, is_normal != 0, srgb != 0, &def_store, &def_threads);
-        const int stores[3] = {0, 1, 2};
+        get_encode_choice(block_dim, has_alpha != 0, is_normal != 0, srgb != 0, &def_store, &def_threads, cls);
+        const int stores[4] = {0, 1, 2, 3};
         const int sizes[3] = {64, 128, 256};
         float best = 1e30f, def_us = -1.0f;
         int best_store = def_store, best_threads = def_threads;
-        for (int si = 0; si < 3 && st == ASTC_OK; ++si)
+        for (int si = 0; si < 4 && st == ASTC_OK; ++si)
             for (int ti = 0; ti < 3 && st == ASTC_OK; ++ti) {
                 if (stores[si] == 2 && sizes[ti] > 128) continue;      // capped store: <= 128 threads
                 for (int w = 0; w < 2; ++w)
@@ -146,7 +162,7 @@ astc_status astc_autotune(int block_dim, int has_alpha, int is_normal, int srgb,
             best_threads = def_threads;
             best = def_us;
         }
-        set_encode_choice(block_dim, has_alpha != 0, is_normal != 0, srgb != 0, best_store, best_threads);
+        set_encode_choice(block_dim, has_alpha != 0, is_normal != 0, srgb != 0, best_store, best_threads, cls);
         if (result) {
             result->store = best_store;
             result->threads = best_threads;

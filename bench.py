@@ -61,7 +61,7 @@ def _parse():
     ap.add_argument("--no-serving", action="store_true", help="skip the serving sweep")
     ap.add_argument("--no-search", action="store_true",
                     help="skip the search-mode / max-accumulation throughput and PSNR leg")
-    ap.add_argument("--serving-rates", default="100,1000,5000,20000,50000,100000",
+    ap.add_argument("--serving-rates", default="100,1000,5000,10000,20000,30000,40000,50000,70000,100000",
                     help="offered request rates (req/s)")
     ap.add_argument("--precision", default="fp32", choices=["fp32", "half2"],
                     help="precision of the main workload")
@@ -230,6 +230,20 @@ def _cpu_baseline(img: np.ndarray, spec: dict, min_seconds: float = 2.0) -> dict
                       f"({el:.2f} s wall on {threads} threads)"}
 
 
+def _config(workload: str, img: np.ndarray, spec: dict, precision: str, world: int) -> dict:
+    """The workload description both arms print (identical dicts)."""
+    h, w = img.shape[:2]
+    d = spec["block_dim"]
+    return {"workload": workload, "texture": f"{w}x{h}",
+            "blocks_per_texture": ((w + d - 1) // d) * ((h + d - 1) // d),
+            "textures_per_step": TEXTURES_PER_STEP, "block_dim": d, "has_alpha": bool(spec["has_alpha"]),
+            "is_normal": bool(spec["is_normal"]), "srgb": bool(spec["srgb"]),
+            "border": "clamp" if spec["border"] else "zero", "precision": precision,
+            "l2": f"inputs {h * w * 4 * TEXTURES_PER_STEP / 2**20:.0f} MiB per step, distinct per texture "
+                  "(> 129 MB L2); no flush needed",
+            "parallelism": f"replicas{world}"}
+
+
 def run_reference(args) -> None:
     world, rank, _ = _dist()
     if rank != 0:
@@ -238,24 +252,28 @@ def run_reference(args) -> None:
     from oracle import oracle
     img, spec = synth.workload(args.workload)
     threads = os.cpu_count() or 1
+    h, w = img.shape[:2]
+    # the same step as the GPU arm: 16 distinct textures (2-D shifts of one)
+    texs = [np.ascontiguousarray(np.roll(img, ((i * 97) % h, (i * 331) % w), axis=(0, 1)))
+            for i in range(TEXTURES_PER_STEP)]
     oracle.encode(img[:64, :64], **spec, threads=threads)
     for _ in range(args.warmup):
-        oracle.encode(img, **spec, threads=threads)
+        oracle.encode(texs[0], **spec, threads=threads)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        oracle.encode(img, **spec, threads=threads)
+        for t in texs:
+            oracle.encode(t, **spec, threads=threads)
     el = time.perf_counter() - t0
-    texels = img.shape[0] * img.shape[1]
+    texels = h * w * len(texs)
     value = texels * args.steps / el / 1e6
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "Mtexels/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": el / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": args.workload, "texture": f"{img.shape[1]}x{img.shape[0]}",
-                   "textures_per_step": 1, **spec},
+        "config": _config(args.workload, img, spec, args.precision, world),
         "cpu_baseline": {"value": value, "unit": "Mtexels/s", "cores": threads, "kind": "port",
-                         "sample": f"{args.steps} timed encodes of one texture; the reference "
+                         "sample": f"{args.steps} timed steps of {len(texs)} textures; the reference "
                                    "shader is D3D11-only (unavailable on this box), so its FP32 "
                                    "CPU restatement (oracle/) runs with OpenMP"},
         "e2e": {"value": value, "unit": "Mtexels/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -358,13 +376,24 @@ def _traffic(workload: str, prec: int, tuned) -> dict:
 
 
 def _psnr_blocks(native, blocks: np.ndarray, tex: np.ndarray, spec: dict) -> float:
-    """Decoded PSNR in the space the encoder fits (GPU decoder, GPU SSE)."""
+    """Decoded PSNR (GPU decoder, GPU reduction) in the space the encoder fits:
+    RGB(A) codes, sRGB linearised; normal maps on the rebuilt unit normals
+    (z = sqrt(max(0, 1 - x^2 - y^2)) on both sides, 3 components)."""
     h, w = tex.shape[:2]
-    fitted = native.fitted_reference(tex, spec["srgb"], spec["is_normal"])
-    ch = 4 if spec["has_alpha"] else (2 if spec["is_normal"] else 3)
     d = native.decode(blocks, w, h, spec["block_dim"])
+    if spec["is_normal"]:
+        return native.psnr_from_sse(native.normal_sse(d, tex), h * w * 3)
+    fitted = native.fitted_reference(tex, spec["srgb"], spec["is_normal"])
+    ch = 4 if spec["has_alpha"] else 3
     s = native.sse(d, fitted)
     return native.psnr_from_sse(float(s[:ch].sum()), h * w * ch)
+
+
+def _psnr_space(spec: dict) -> str:
+    if spec["is_normal"]:
+        return "rebuilt unit normals (x, y from R, G; z = sqrt(1 - x^2 - y^2)), 3 components x 127.5"
+    return (("linearised sRGB x255 (what the encoder fits), " if spec["srgb"] else "") +
+            f"{4 if spec['has_alpha'] else 3} channels")
 
 
 def _bench_search(torch, native, headline: str, texs, outs, spec: dict) -> dict:
@@ -491,13 +520,9 @@ def _bench_batched(torch, native, oracle, count: int, reps: int = 5) -> dict:
         h2 = jobs[k][3].cpu().numpy()
         f32 = fp32_blocks[k]
         f64 = oracle.encode(img, fp64=True, **opts)
-        ref = native.fitted_reference(img, opts["srgb"], opts["is_normal"])
-        ch = 4 if opts["has_alpha"] else (2 if opts["is_normal"] else 3)
 
         def psnr(bl):
-            dec = native.decode(bl, w, h, opts["block_dim"])
-            s = native.sse(dec, ref)
-            return native.psnr_from_sse(float(s[:ch].sum()), w * h * ch)
+            return _psnr_blocks(native, bl, img, opts)
         p64 = psnr(f64)
         gaps.append((p64 - psnr(f32), p64 - psnr(h2)))
         same.append(float(np.all(h2 == f32, axis=1).mean()))
@@ -561,7 +586,8 @@ def _bench_serving(torch, native, rates, seconds: float = 2.0, max_requests: int
         ptr = base.data_ptr() + (y0 * 2048 + x0) * 4
         requests.append(native.make_request(int(ptr), s, s, int(out.data_ptr() + off), row_pitch=2048 * 4, **opts))
     texels = np.array([m[1] * m[1] for m in reqs_meta], np.float64)
-    result = {"pool_bytes": 2 << 30, "requests_max": n_max, "rates": {}}
+    result = {"pool_bytes": 2 << 30, "requests_max": n_max, "inflight_slots": 3, "max_batch": 256,
+              "rates": {}}
     for mode, label in ((native.SERVE_BATCHED, "batched"), (native.SERVE_PER_REQUEST, "per_request")):
         with native.Server(pool_bytes=2 << 30, max_batch=256, inflight=3, mode=mode) as srv:
             srv.replay(requests[:64], np.zeros(64))                       # warm-up (graphs, pools)
@@ -569,12 +595,36 @@ def _bench_serving(torch, native, rates, seconds: float = 2.0, max_requests: int
             for rate in rates:
                 n = int(min(n_max, max(64, rate * seconds)))
                 arrival = np.cumsum(np.random.default_rng(int(rate)).exponential(1e6 / rate, n))
+                srv.stats(reset=True)
                 lat, wall = srv.replay(requests[:n], arrival)
+                dev = srv.stats(reset=True)
+                busy = dev["device_busy_s"]
                 result["rates"].setdefault(str(rate), {})[label] = {
                     "requests": n, "p50_ms": float(np.percentile(lat, 50)) / 1e3,
                     "p99_ms": float(np.percentile(lat, 99)) / 1e3, "mean_ms": float(lat.mean()) / 1e3,
                     "throughput_req_s": n / wall, "Mtexels_s": float(texels[:n].sum()) / wall / 1e6,
-                    "offered_req_s": rate}
+                    "offered_req_s": rate,
+                    # device side (timing events on each slot's stream)
+                    "launches": dev["launches"],
+                    "requests_per_launch": dev["requests"] / max(1, dev["launches"]),
+                    "gpu_busy_frac": busy / wall if wall > 0 else None,
+                    "slots_in_flight_mean": dev["device_slot_s"] / busy if busy > 0 else 0.0,
+                    "overlap_frac": dev["device_overlap_s"] / busy if busy > 0 else 0.0}
+    # the knee: the lowest offered rate at which per-request launches fall
+    # behind batching: p99 above twice the batched p99, or under 90% of the
+    # batched throughput served
+    knee = None
+    for rate in rates:
+        r = result["rates"].get(str(rate), {})
+        if "batched" not in r or "per_request" not in r:
+            continue
+        b, p = r["batched"], r["per_request"]
+        if p["p99_ms"] > 2 * b["p99_ms"] or p["throughput_req_s"] < 0.9 * b["throughput_req_s"]:
+            knee = {"offered_req_s": rate, "p99_ms_batched": b["p99_ms"], "p99_ms_per_request": p["p99_ms"],
+                    "served_req_s_batched": b["throughput_req_s"],
+                    "served_req_s_per_request": p["throughput_req_s"]}
+            break
+    result["knee"] = knee
     return result
 
 
@@ -732,25 +782,18 @@ def run_ours(args) -> None:
     ora = oracle.encode(tex0, **spec)
     f64 = oracle.encode(tex0, **spec, fp64=True)
 
-    fitted = native.fitted_reference(tex0, spec["srgb"], spec["is_normal"])
-    ch = 4 if spec["has_alpha"] else (2 if spec["is_normal"] else 3)
-
     def psnr(blocks):
-        d = native.decode(blocks, w, h, dim)
-        s = native.sse(d, fitted)
-        return native.psnr_from_sse(float(s[:ch].sum()), h * w * ch)
+        return _psnr_blocks(native, blocks, tex0, spec)
 
     quality = {"identical_blocks_vs_fp32_oracle": float(np.all(got == ora, axis=1).mean()),
                "psnr_db": psnr(got), "psnr_fp32_oracle_db": psnr(ora), "psnr_fp64_oracle_db": psnr(f64),
-               "psnr_space": ("linearised sRGB x255 (what the encoder fits), " if spec["srgb"] else "") +
-                             f"{ch} channels, spec LDR decode on the GPU"}
+               "psnr_space": _psnr_space(spec) + ", spec LDR decode on the GPU"}
     quality["psnr_gap_to_fp64_db"] = quality["psnr_fp64_oracle_db"] - quality["psnr_db"]
 
+    # plain (one launch per texture) FP32 and HALF2 on the three workloads
     extra = {}
     if not args.no_extra:
-        for name in ("4x4_rgb_512", "4x4_normal_4096"):
-            if name == args.workload:
-                continue
+        for name in ("4x4_rgb_512", "6x6_rgba_srgb_2048", "4x4_normal_4096"):
             ximg, xspec = synth.workload(name)
             xh, xw = ximg.shape[:2]
             xd = xspec["block_dim"]
@@ -758,11 +801,19 @@ def run_ours(args) -> None:
             reps = max(1, (268 << 20) // (xh * xw * 4))     # keep each step above L2 size
             xt = _texture_batch(torch, ximg, reps, salt=7)
             xo = [torch.empty((xnb, 16), dtype=torch.uint8, device="cuda") for _ in xt]
-            _time_launches(torch, native, xt, xo, xspec, 3)
-            xper, xsteps, _ = _time_launches(torch, native, xt, xo, xspec, 10)
-            extra[name] = {"value": xh * xw * reps * 10 / (sum(xsteps) / 1e3) / 1e6, "unit": "Mtexels/s",
-                           "mean_launch_us": xper * 1e3,
-                           "textures_per_step": reps}
+            # the autotuner picks the FP32 mapping for this size (the
+            # cooperative one competes for textures under one wave)
+            xt_tuned = native.autotune(xd, xspec["has_alpha"], xspec["is_normal"], xspec["srgb"], xw, xh)
+            entry = {"textures_per_step": reps,
+                     "fp32_kernel_variant": {"store": xt_tuned.store, "threads_per_cta": xt_tuned.threads}}
+            for label, xp in (("fp32", 0), ("half2", 1)):
+                run = dict(xspec, precision=xp)
+                _time_launches(torch, native, xt, xo, run, 3)
+                xper, xsteps, _ = _time_launches(torch, native, xt, xo, run, 10)
+                entry[label] = {"value": xh * xw * reps * 10 / (sum(xsteps) / 1e3) / 1e6,
+                                "unit": "Mtexels/s", "mean_launch_us": xper * 1e3}
+            entry["speedup_half2_vs_fp32"] = entry["half2"]["value"] / entry["fp32"]["value"]
+            extra[name] = entry
             del xt, xo
 
     search = None if args.no_search else _bench_search(torch, native, args.workload, texs, outs, spec)
@@ -771,49 +822,58 @@ def run_ours(args) -> None:
         torch, native, [int(r) for r in args.serving_rates.split(",") if r])
     cpu = None if args.no_cpu else _cpu_baseline(img, spec)
 
+    hbm = {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
+           "frac": (achieved_gbs / hbm_peak) if hbm_peak else None, "peak_source": hbm_source,
+           "alg_bytes_per_launch": alg_bytes}
+    issue = _issue_roofline(args.workload, prec, tuned, mean_launch_s, clk.get("sm_mhz"),
+                            torch.cuda.get_device_properties(local).multi_processor_count)
     line = {
         "metric": METRIC, "value": value, "unit": "Mtexels/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_s / args.steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic",
-        "config": {"workload": args.workload, "texture": f"{w}x{h}", "blocks_per_texture": nblocks,
-                   "textures_per_step": len(texs), "block_dim": dim, "has_alpha": spec["has_alpha"],
-                   "is_normal": spec["is_normal"], "srgb": spec["srgb"],
-                   "border": "clamp" if spec["border"] else "zero", "precision": args.precision,
-                   "l2": f"inputs {texels_step * 4 / 2**20:.0f} MiB per step, distinct per texture "
-                         "(> 129 MB L2); no flush needed",
-                   "parallelism": f"replicas{world}",
-                   "kernel_variant": {"store": {0: "registers", 1: "shared",
-                                                2: "registers_capped"}.get(tuned.store, tuned.store),
-                                      "threads_per_cta": tuned.threads,
-                                      "autotune_best_us": tuned.best_us}},
+        "config": _config(args.workload, img, spec, args.precision, world),
+        "kernel_variant": {"store": {0: "registers", 1: "shared", 2: "registers_capped"}.get(tuned.store, tuned.store),
+                           "threads_per_cta": tuned.threads, "autotune_best_us": tuned.best_us},
         "e2e": {"value": e2e_value, "unit": "Mtexels/s",
                 "h2d_bytes_per_step": texels_step * 4, "d2h_bytes_per_step": nblocks * 16 * len(texs),
                 "entry_point": "astc_encode_gpu (ASTC_MEMORY_HOST, pinned buffers: inputs through the upload ring, blocks written in place over NVLink-C2C; one stream sync per step)",
                 "steps": e2e_steps},
         "gpu_launches": int(launches),
-        "roofline": {"bound": "hbm", "kernel": kernel, "achieved": achieved_gbs,
-                     "peak": hbm_peak, "unit": "GB/s",
-                     "frac": (achieved_gbs / hbm_peak) if hbm_peak else None,
+        # the binding bound: FP32/INT issue (the per-block algebra is not a
+        # contraction, so no tensor-core roof applies); HBM is the secondary roof
+        "roofline": {"bound": "fp32_issue", "kernel": kernel, "achieved": achieved_tf, "peak": fp32_peak,
+                     "unit": "TFLOP/s", "frac": achieved_tf / fp32_peak, "flops_per_launch": flops,
+                     "mean_launch_us": mean_launch_s * 1e6,
+                     "peak_source": "max of an FP32 FMA microbenchmark (libastc_fp32_peak.so) and an "
+                                    "8192^3 SGEMM (TF32 off), both measured in this run",
+                     "peak_fma_microbenchmark": fma_peak, "peak_sgemm": sgemm_peak,
                      **_traffic(args.workload, prec, tuned),
-                     "peak_source": hbm_source,
-                     "alg_bytes_per_launch": alg_bytes, "mean_launch_us": mean_launch_s * 1e6},
-        "roofline_fp32": {"bound": "fp32_issue", "achieved": achieved_tf, "peak": fp32_peak,
-                          "unit": "TFLOP/s", "frac": achieved_tf / fp32_peak,
-                          "flops_per_launch": flops,
-                          "peak_fma_microbenchmark": fma_peak, "peak_sgemm": sgemm_peak,
-                          "peak_source": "max of an FP32 FMA microbenchmark (libastc_fp32_peak.so) and an "
-                                         "8192^3 SGEMM (TF32 off), both measured in this run"},
-        "roofline_issue": _issue_roofline(args.workload, prec, tuned, mean_launch_s, clk.get("sm_mhz"),
-                                          torch.cuda.get_device_properties(local).multi_processor_count),
-        "quality": quality,
+                     "hbm": hbm, "issue": issue},
         "clocks": clk,
         "wall_s_timed_region": wall,
-        "extra_workloads": extra,
         "search_mode": search,
-        "batched_mixed": batched,
         "serving": serving,
+        "batched_mixed": batched,
+        "extra_workloads": extra,
+        "quality": quality,
     }
+    # compact spec figures last, where a tail of the line keeps them
+    ns = {"fp32_4x4_rgb_512_Mtexels_s": extra.get("4x4_rgb_512", {}).get("fp32", {}).get("value"),
+          "fp32_4x4_rgb_floor_Mtexels_s": 20000,
+          "speedup_half2_vs_fp32_plain": {k: v["speedup_half2_vs_fp32"] for k, v in extra.items()},
+          "identical_blocks_vs_fp32_oracle": quality["identical_blocks_vs_fp32_oracle"],
+          "psnr_gap_to_fp64_db": quality["psnr_gap_to_fp64_db"],
+          "roofline_frac_fp32": achieved_tf / fp32_peak,
+          "roofline_frac_hbm": hbm["frac"],
+          "roofline_frac_issue": issue["frac"] if issue else None}
+    if batched:
+        ns["speedup_half2_vs_fp32_batched"] = batched["speedup_half2_vs_fp32_batched"]
+        ns["batched_half2_max_gap_to_fp64_db"] = batched["psnr_gap_to_fp64_db"]["half2_max"]
+        ns["batched_half2_vs_plain_fp32"] = batched["speedup_batched_half2_vs_plain_fp32"]
+    if serving and serving.get("knee"):
+        ns["serving_knee"] = serving["knee"]
+    line["north_star"] = ns
     if cpu is not None:
         line["cpu_baseline"] = cpu
     print(json.dumps(line), flush=True)

@@ -269,6 +269,20 @@ astc_status astc_server_cancel(astc_server* server, uint64_t ticket);
 astc_status astc_server_replay(astc_server* server, const astc_request* requests,
                                const double* arrival_us, int count, double* latency_us,
                                double* wall_s);
+/* Device-side record of the slot launches retired since the last reset
+ * (timing events recorded on each slot's stream before its first copy and
+ * after its last): how busy the device was and how much the slots' work
+ * overlapped.  (No counterpart in the reference.) */
+typedef struct astc_server_stats {
+    long long launches;          /* slot launches (batches, or requests)       */
+    long long requests;          /* requests they carried                      */
+    int max_requests_per_launch;
+    double device_busy_s;        /* union of the launches' device intervals    */
+    double device_overlap_s;     /* time with two or more slots on the device  */
+    double device_slot_s;        /* sum of the intervals (busy x mean depth)   */
+    double device_span_s;        /* first interval start to last interval end  */
+} astc_server_stats;
+astc_status astc_server_get_stats(astc_server* server, int reset, astc_server_stats* out);
 /* Waits for the work in flight, then frees the server. */
 astc_status astc_server_destroy(astc_server* server);
 
@@ -313,12 +327,27 @@ astc_status astc_decode_gpu(const uint8_t* blocks, int width, int height,
 astc_status astc_sse_gpu(const uint8_t* a, const uint8_t* b, size_t texels,
                          int memory, void* stream, uint64_t sse_rgba[4]);
 
+/* Squared error of two normal maps in the -norm layout (the reference keeps
+ * X and Y in R and G, ASTC_Encode.hlsl:575-578), measured on the rebuilt unit
+ * normals: x, y = code * 2/255 - 1, z = sqrt(max(0, 1 - x^2 - y^2)); each
+ * component's difference is scaled by 127.5 so an 8-bit peak of 255 applies
+ * to PSNR over 3 * texels values.  Reduced on the GPU in FP64; memory/stream
+ * as in astc_sse_gpu.  (No counterpart in the reference.) */
+astc_status astc_normal_sse_gpu(const uint8_t* a, const uint8_t* b, size_t texels,
+                                int memory, void* stream, double* sse);
+
 /* Kernel variant of a format: where a block's decoded texels live
  * (store 0 = registers, 1 = shared memory, 2 = registers with the count
- * capped for occupancy, at most 128 threads) and the CTA size (32/64/128/256).
- * Every variant produces identical blocks; they differ in speed only.
- * (No counterpart in the reference, whose shader has one fixed mapping,
- * [numthreads(8,8,1)] at ASTC_Encode.hlsl:553.) */
+ * capped for occupancy, at most 128 threads) or, store 3, the cooperative
+ * mapping: four lanes of a warp share one block (a warp encodes eight
+ * blocks; texels staged in a shared-memory tile; 64/128/256 threads), which
+ * shortens each block's path for launches too small to fill the GPU; and
+ * the CTA size (32/64/128/256).  Every variant produces identical blocks;
+ * they differ in speed only.  Choices are kept per format and per size
+ * class: textures with fewer blocks than one wave of the one-thread
+ * mappings (SMs x 384 blocks) and the rest.  (No counterpart in the
+ * reference, whose shader has one fixed mapping, one thread per block,
+ * [numthreads(8,8,1)] at ASTC_Encode.hlsl:553-561.) */
 typedef struct astc_tune_result {
     int store;
     int threads;
@@ -327,14 +356,19 @@ typedef struct astc_tune_result {
 } astc_tune_result;
 
 /* Time every variant for a format on a synthetic width x height texture on
- * the current device and install the fastest for that format in this
- * process (it allocates its own test buffers). */
+ * the current device and install the fastest for that format and that
+ * size class in this process (it allocates its own test buffers). */
 astc_status astc_autotune(int block_dim, int has_alpha, int is_normal, int srgb,
                           int width, int height, astc_tune_result* result);
+/* Install a variant for a format, for every texture size. */
 astc_status astc_set_kernel_choice(int block_dim, int has_alpha, int is_normal, int srgb,
                                    int store, int threads);
+/* The variant installed for a format's textures of one wave or more. */
 astc_status astc_get_kernel_choice(int block_dim, int has_alpha, int is_normal, int srgb,
                                    int* store, int* threads);
+/* The variant astc_encode_gpu uses for a texture of this size. */
+astc_status astc_get_kernel_choice_for_size(int block_dim, int has_alpha, int is_normal, int srgb,
+                                            int width, int height, int* store, int* threads);
 
 /* astc_sse_gpu for callers that may not allocate device memory (no
  * counterpart in the reference).  Some hosts own the whole device-memory

@@ -31,6 +31,15 @@ def test_reference_arm_line():
     assert d["config"]["workload"] == "4x4_rgb_512"
     assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["value"] == d["value"]
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["d2h_bytes_per_step"] == 0
+    # the GPU arm prints the same config dict (same function, same workload)
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("bench_mod", BENCH)
+    bench = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bench)
+    from astc_encoder_gb300 import synth
+    img, wspec = synth.workload("4x4_rgb_512")
+    assert d["config"] == bench._config("4x4_rgb_512", img, wspec, "fp32", 1)
+    assert d["config"]["textures_per_step"] == bench.TEXTURES_PER_STEP
 
 
 def test_reference_arm_other_ranks_are_silent():

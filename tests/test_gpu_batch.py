@@ -127,10 +127,15 @@ def test_batch_rejects_over_capacity(native):
 
 
 def _psnr(native, blocks, img, opts):
+    """Decoded PSNR in the fit space; normal maps on the rebuilt unit normals
+    (z = sqrt(max(0, 1 - x^2 - y^2)), numpy float64)."""
     h, w = img.shape[:2]
-    ref = native.fitted_reference(img, opts.get("srgb", False), opts.get("is_normal", False))
     dec = native.decode(blocks, w, h, opts["block_dim"])
-    ch = 4 if opts.get("has_alpha") else (2 if opts.get("is_normal") else 3)
+    if opts.get("is_normal"):
+        mse = native.normal_sse_numpy(dec, img) / (h * w * 3)
+        return 10 * np.log10(255.0 ** 2 / mse)
+    ref = native.fitted_reference(img, opts.get("srgb", False), False)
+    ch = 4 if opts.get("has_alpha") else 3
     mse = np.mean((dec[..., :ch].astype(np.float64) - ref[..., :ch].astype(np.float64)) ** 2)
     return 10 * np.log10(255.0 ** 2 / mse)
 

@@ -267,6 +267,28 @@ def test_sse_matches_numpy(native):
     assert native.sse(a, b).tolist() == want.tolist()
 
 
+def test_normal_sse_matches_numpy(native):
+    """The reconstructed-normal error (z rebuilt from x and y) against its
+    numpy float64 statement; FP32 per texel, FP64 sums: relative 1e-5."""
+    from astc_encoder_gb300 import synth
+    rng = np.random.default_rng(4)
+    a = synth.normal_map(256, 192)
+    b = a.copy()
+    noise = rng.integers(-3, 4, b.shape[:2] + (2,))
+    b[..., :2] = np.clip(b[..., :2].astype(int) + noise, 0, 255).astype(np.uint8)
+    b[..., 2:] = rng.integers(0, 256, b.shape[:2] + (2,))     # B and A take no part
+    got = native.normal_sse(a, b)
+    want = native.normal_sse_numpy(a, b)
+    assert want > 0
+    assert abs(got - want) <= 1e-5 * want
+    assert native.normal_sse(a, a) == 0.0
+    # outside the unit disc z is 0 on both sides
+    c = np.zeros((4, 4, 4), np.uint8)
+    d = c.copy()
+    d[..., 0] = 255
+    assert abs(native.normal_sse(c, d) - native.normal_sse_numpy(c, d)) < 1e-3
+
+
 def test_fp32_peak_probe_is_plausible(native):
     """The FMA probe used as the FP32 roofline denominator: between half and 1.1x
     of SMs x 128 lanes x 2 FLOPs x the SM clock."""
@@ -298,9 +320,9 @@ def test_every_kernel_variant_bit_exact(native, oracle, dim, alpha, normal, srgb
     want = oracle.encode(img, **opts)
     saved = native.get_kernel_choice(dim, alpha, normal, srgb)
     try:
-        for store in (0, 1, 2):
+        for store in (0, 1, 2, 3):
             for threads in (32, 64, 128, 256):
-                if store == 2 and threads > 128:
+                if (store == 2 and threads > 128) or (store == 3 and threads < 64):
                     continue
                 native.set_kernel_choice(dim, alpha, normal, srgb, store, threads)
                 assert np.array_equal(native.encode(img, **opts), want), (store, threads)
@@ -308,11 +330,55 @@ def test_every_kernel_variant_bit_exact(native, oracle, dim, alpha, normal, srgb
         native.set_kernel_choice(dim, alpha, normal, srgb, *saved)
 
 
+@pytest.mark.parametrize("dim,alpha,normal,srgb", [(4, False, False, False), (4, True, False, True),
+                                                   (6, True, False, True), (6, False, True, False)])
+def test_cooperative_mapping_bit_exact(native, oracle, dim, alpha, normal, srgb):
+    """The four-lanes-per-block mapping on ragged sizes (groups past the end
+    of the texture, partial blocks on both borders), one-row and one-column
+    textures, a flat texture and the full-size workload of the format."""
+    from astc_encoder_gb300 import synth
+    saved = native.get_kernel_choice(dim, alpha, normal, srgb)
+    try:
+        for threads in (64, 128, 256):
+            native.set_kernel_choice(dim, alpha, normal, srgb, 3, threads)
+            for border in (0, 1):
+                opts = dict(block_dim=dim, has_alpha=alpha, is_normal=normal, srgb=srgb, border=border)
+                for h, w in ((1, 1), (5, 3), (37, 101), (1, 257), (203, 1), (64, 64)):
+                    img = _texture(h, w, seed=h * 7 + w + threads)
+                    assert np.array_equal(native.encode(img, **opts), oracle.encode(img, **opts)), (h, w, threads)
+        flat = np.full((24, 40, 4), 91, np.uint8)
+        opts = dict(block_dim=dim, has_alpha=alpha, is_normal=normal, srgb=srgb, border=1)
+        assert np.array_equal(native.encode(flat, **opts), oracle.encode(flat, **opts))
+        native.set_kernel_choice(dim, alpha, normal, srgb, 3, 128)
+        name = {4: "4x4_normal_4096" if normal else "4x4_rgb_512", 6: "6x6_rgba_srgb_2048"}[dim]
+        img, spec = synth.workload(name, scale=0.25)
+        spec = dict(spec, has_alpha=alpha, is_normal=normal, srgb=srgb)
+        assert np.array_equal(native.encode(img, **spec), oracle.encode(img, **spec))
+    finally:
+        native.set_kernel_choice(dim, alpha, normal, srgb, *saved)
+
+
+def test_choice_is_kept_per_size_class(native):
+    """Textures under one wave of the one-thread mappings and the rest keep
+    separate choices; set_kernel_choice sets both."""
+    saved = native.get_kernel_choice(4, False, False, False)
+    small, large = (256, 256), (4096, 4096)
+    try:
+        native.set_kernel_choice(4, False, False, False, 3, 128)
+        assert native.get_kernel_choice_for_size(4, False, False, False, *small) == (3, 128)
+        assert native.get_kernel_choice_for_size(4, False, False, False, *large) == (3, 128)
+        r = native.autotune(4, False, False, False, *small)
+        assert native.get_kernel_choice_for_size(4, False, False, False, *small) == (r.store, r.threads)
+        assert native.get_kernel_choice_for_size(4, False, False, False, *large) == (3, 128)
+    finally:
+        native.set_kernel_choice(4, False, False, False, *saved)
+
+
 def test_autotune_installs_a_valid_choice(native, oracle):
     saved = native.get_kernel_choice(6, True, False, True)
     try:
         r = native.autotune(6, True, False, True, 512, 384)
-        assert r.store in (0, 1, 2) and r.threads in (64, 128, 256)
+        assert r.store in (0, 1, 2, 3) and r.threads in (64, 128, 256)
         assert 0 < r.best_us <= r.default_us
         assert native.get_kernel_choice(6, True, False, True) == (r.store, r.threads)
         img = _texture(130, 70, seed=77)

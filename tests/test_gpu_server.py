@@ -66,6 +66,31 @@ def test_alone_equals_in_the_mix(native, oracle, mode, precision):
         assert np.array_equal(alone, oracle.encode(probe.img, **probe.opts))
 
 
+def test_server_device_stats(native):
+    """The device-side record: every retired launch and request counted,
+    busy time within the span, overlap within busy, reset clears it."""
+    with native.Server(pool_bytes=64 << 20, max_batch=8, inflight=3) as srv:
+        mix = _mix(native, 40, seed=21, max_side=300)
+        srv.stats(reset=True)
+        tickets = [srv.submit(r.req) for r in mix]
+        for t in tickets:
+            srv.wait(t)
+        st = srv.stats(reset=True)
+        assert st["requests"] == len(mix)
+        assert 1 <= st["launches"] <= len(mix)
+        assert 1 <= st["max_requests_per_launch"] <= 8
+        assert 0 < st["device_busy_s"] <= st["device_span_s"] + 1e-9
+        assert 0 <= st["device_overlap_s"] <= st["device_busy_s"] + 1e-9
+        assert st["device_slot_s"] >= st["device_busy_s"] - 1e-9
+        assert srv.stats()["launches"] == 0
+    with native.Server(pool_bytes=64 << 20, inflight=2, mode=1) as srv:
+        mix = _mix(native, 12, seed=22, max_side=200)
+        for t in [srv.submit(r.req) for r in mix]:
+            srv.wait(t)
+        st = srv.stats()
+        assert st["launches"] == st["requests"] == 12 and st["max_requests_per_launch"] == 1
+
+
 @pytest.mark.parametrize("mode", [0, 1])
 def test_server_quality_mode(native, mode):
     """A THOROUGH server returns each request's astc_encode_gpu blocks with
