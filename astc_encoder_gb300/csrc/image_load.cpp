@@ -419,10 +419,17 @@ bool decode_tga(const uint8_t* d, size_t n, Image& img, std::string& err) {
     };
     const int px = (bpp + 7) / 8;
     size_t pos = 18 + (size_t)idlen;
-    // colour map (present in any type when cmap == 1): clen entries of cbits
+    // colour map (present in any type when cmap == 1): clen entries of cbits.
+    // stb_image, which the reference loads through, takes the first-entry
+    // field as a count of bytes to skip before the entries of a mapped image
+    // and ignores the map of other types; this reader does the same.
     std::vector<uint8_t> colours;                        // RGBA per entry
-    if (cmap == 1) {
+    if (cmap == 1 && !mapped) {
+        pos += (size_t)clen * ((cbits + 7) / 8);         // not used
+    } else if (cmap == 1) {
+        pos += (size_t)cfirst;
         const int cb = (cbits + 7) / 8;
+        if (clen == 0) { err = "bad TGA colour map"; return false; }
         if (!(cbits == 15 || cbits == 16 || cbits == 24 || cbits == 32)) { err = "bad TGA colour map"; return false; }
         if (pos + (size_t)clen * cb > n) { err = "TGA colour map truncated"; return false; }
         colours.assign((size_t)clen * 4, 255);
@@ -472,8 +479,9 @@ bool decode_tga(const uint8_t* d, size_t n, Image& img, std::string& err) {
         for (int x = 0; x < w; ++x, s += px, o += 4) {
             if (grey) { o[0] = o[1] = o[2] = s[0]; continue; }
             if (mapped) {
-                const int i = s[0] - cfirst;
-                if (i < 0 || i >= clen) { err = "TGA colour index out of range"; return false; }
+                // the index is used as stored, an index past the colour map
+                // takes entry 0 (stb_image's reading)
+                const int i = s[0] < clen ? s[0] : 0;
                 memcpy(o, colours.data() + (size_t)i * 4, 4);
                 continue;
             }
@@ -553,6 +561,15 @@ bool decode_bmp(const uint8_t* d, size_t n, Image& img, std::string& err) {
                 for (int c = 0; c < 4; ++c) o[c] = channel(v, mask[c]);
             }
         }
+    }
+    // many 32-bit BI_RGB files leave the fourth byte 0 everywhere: read as
+    // opaque (stb_image, the reference's loader, does the same for 40- and
+    // 56-byte headers)
+    if (bpp == 32 && comp == 0 && (hdr == 40 || hdr == 56)) {
+        uint8_t any = 0;
+        for (size_t i = 3; i < img.rgba.size(); i += 4) any |= img.rgba[i];
+        if (!any)
+            for (size_t i = 3; i < img.rgba.size(); i += 4) img.rgba[i] = 255;
     }
     return true;
 }
@@ -1360,7 +1377,11 @@ bool decode_pic(const uint8_t* d, size_t n, Image& img, std::string& err) {
                         count = c - 127;
                     }
                 }
-                if (count <= 0 || x + count > w) { err = "bad PIC run"; return false; }
+                // a pure run-length packet is cut at the end of the row and may
+                // be empty (its value is still read); mixed packets may not
+                // overrun the row (what stb_image's reader does)
+                if (p.type == 1 && count > w - x) count = w - x;
+                if (count < 0 || x + count > w || (count == 0 && literal)) { err = "bad PIC run"; return false; }
                 if (!literal && !read_vals()) { err = "PIC data too short"; return false; }
                 for (int i = 0; i < count; ++i, ++x) {
                     if (literal && !read_vals()) { err = "PIC data too short"; return false; }

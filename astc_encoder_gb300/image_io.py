@@ -228,6 +228,10 @@ def load_bmp(path: str) -> np.ndarray:
         top = m >> shift
         x = (v & m) >> shift
         out[..., ch] = x if top == 255 else (x * 255 + top // 2) // top
+    # a 32-bit BI_RGB image whose fourth byte is 0 everywhere reads as opaque
+    # (stb_image, the reference's loader, for 40- and 56-byte headers)
+    if bpp == 32 and comp == 0 and hdr in (40, 56) and not out[..., 3].any():
+        out[..., 3] = 255
     return out
 
 
@@ -256,9 +260,14 @@ def load_tga(path: str) -> np.ndarray:
     px = (bpp + 7) // 8
     pos = 18 + idlen
     colours = None
-    if cmap == 1:
+    # as stb_image (the reference's loader): the map of an unmapped image is
+    # skipped; for a mapped one the first-entry field counts bytes to skip
+    if cmap == 1 and not mapped:
+        pos += clen * ((cbits + 7) // 8)
+    elif cmap == 1:
+        pos += cfirst
         cb = (cbits + 7) // 8
-        if cbits not in (15, 16, 24, 32):
+        if cbits not in (15, 16, 24, 32) or clen == 0:
             raise ValueError("bad TGA colour map")
         table = np.frombuffer(data, np.uint8, clen * cb, pos).reshape(clen, cb)
         pos += clen * cb
@@ -292,9 +301,8 @@ def load_tga(path: str) -> np.ndarray:
     if grey:
         out[..., :3] = raw[..., :1]
     elif mapped:
-        idx = raw[..., 0].astype(np.int64) - cfirst
-        if idx.min() < 0 or idx.max() >= clen:
-            raise ValueError("TGA colour index out of range")
+        idx = raw[..., 0].astype(np.int64)
+        idx = np.where(idx < clen, idx, 0)              # past the map: entry 0
         out[:] = colours[idx]
     elif px == 2:
         out[:] = _rgb16(raw[..., 0].astype(np.int64) | (raw[..., 1].astype(np.int64) << 8))
@@ -882,7 +890,7 @@ def load_pic(path: str) -> np.ndarray:
                     c = d[pos]
                     pos += 1
                     if typ == 1:
-                        count, literal = c, False
+                        count, literal = min(c, w - x), False   # cut at the row's end
                     elif c < 128:
                         count, literal = c + 1, True
                     elif c == 128:
@@ -890,7 +898,7 @@ def load_pic(path: str) -> np.ndarray:
                         pos += 2
                     else:
                         count, literal = c - 127, False
-                if count <= 0 or x + count > w:
+                if count < 0 or x + count > w or (count == 0 and literal):
                     raise ValueError("bad PIC run")
                 seg = out[y, x:x + count]
                 if literal:

@@ -265,14 +265,17 @@ def _bmp(path, arr, top_down=False, bitfields=False):
 
 
 def _tga_mapped(path, idx, colours, cbits, first=0, rle=False):
-    """Writes a colour-mapped TGA: 8-bit indices (offset by `first`) into a
-    15/16/24/32-bit colour map (`colours` holds the stored entries)."""
+    """Writes a colour-mapped TGA: 8-bit indices into a 15/16/24/32-bit colour
+    map (`colours` holds the stored entries).  The first-entry field is
+    `first`, written as that many bytes ahead of the entries: stb_image (the
+    reference's loader) skips that many bytes and then uses the indices as
+    stored."""
     h, w = idx.shape
     cb = (cbits + 7) // 8
     head = struct.pack("<BBBHHBHHHHBB", 0, 1, 9 if rle else 1, first, len(colours), cbits, 0, 0, w, h, 8, 0x20)
-    cmap = b"".join(bytes(int(x) for x in c[:cb]) for c in colours)
+    cmap = b"\xee" * first + b"".join(bytes(int(x) for x in c[:cb]) for c in colours)
     body = bytearray()
-    for r in (idx + first).astype(np.uint8):
+    for r in idx.astype(np.uint8):
         if rle:
             for v in r:                                     # one-pixel packets: raw (count 1)
                 body += bytes([0, int(v)])
@@ -309,6 +312,69 @@ def test_cli_reads_colour_mapped_tga(native, tmp_path, cbits, rle, first):
     want = table[idx].astype(np.uint8)
     assert np.array_equal(_dump(native, path, tmp_path), want[::-1])
     from astc_encoder_gb300 import image_io
+    assert np.array_equal(image_io.load_image(path), want)
+
+
+def test_tga_colour_map_rules_of_the_reference_loader(native, tmp_path):
+    """An index past the colour map takes entry 0; a colour map in an
+    unmapped (true-colour) file is skipped."""
+    from astc_encoder_gb300 import image_io
+    colours = np.array([[10, 20, 30], [40, 50, 60], [70, 80, 90]])
+    idx = np.array([[0, 1, 2, 3], [200, 2, 1, 0]])
+    path = str(tmp_path / "m.tga")
+    _tga_mapped(path, idx, colours, 24)
+    table = colours[:, [2, 1, 0]]
+    want = np.full((2, 4, 4), 255, np.uint8)
+    want[..., :3] = table[np.where(idx < 3, idx, 0)]
+    assert np.array_equal(_dump(native, path, tmp_path), want[::-1])
+    assert np.array_equal(image_io.load_image(path), want)
+    # true colour with a (useless) 2-entry 24-bit colour map before the pixels
+    arr = np.arange(2 * 3 * 3, dtype=np.uint8).reshape(2, 3, 3)
+    head = struct.pack("<BBBHHBHHHHBB", 0, 1, 2, 0, 2, 24, 0, 0, 3, 2, 24, 0x20)
+    with open(path, "wb") as fh:
+        fh.write(head + bytes(6) + arr[..., [2, 1, 0]].tobytes())
+    want = np.full((2, 3, 4), 255, np.uint8)
+    want[..., :3] = arr
+    assert np.array_equal(_dump(native, path, tmp_path), want[::-1])
+    assert np.array_equal(image_io.load_image(path), want)
+
+
+def test_bmp_all_zero_alpha_reads_opaque(native, tmp_path):
+    """32-bit BI_RGB (BGRX) files with every fourth byte 0 read as opaque, as
+    stb_image reads them; one nonzero alpha byte keeps the alpha."""
+    from astc_encoder_gb300 import image_io
+    rng = np.random.default_rng(3)
+    arr = rng.integers(0, 256, (5, 7, 4), dtype=np.uint8)
+    arr[..., 3] = 0
+    path = str(tmp_path / "x.bmp")
+    _bmp(path, arr)
+    want = arr.copy()
+    want[..., 3] = 255
+    assert np.array_equal(_dump(native, path, tmp_path), want[::-1])
+    assert np.array_equal(image_io.load_image(path), want)
+    arr[2, 3, 3] = 1
+    _bmp(path, arr)
+    assert np.array_equal(_dump(native, path, tmp_path), arr[::-1])
+    assert np.array_equal(image_io.load_image(path), arr)
+
+
+def test_pic_pure_runs_cut_at_the_row_end(native, tmp_path):
+    """Pure run-length PIC packets: a run past the end of the row is cut to
+    the row, an empty run reads its value and adds no pixels."""
+    from astc_encoder_gb300 import image_io
+    w, h = 5, 2
+    head = b"\x53\x80\xf6\x34" + struct.pack(">f", 3.71) + b"".ljust(80, b"\0")
+    head += b"PICT" + struct.pack(">HHfHH", w, h, 1.0, 3, 0) + bytes([0, 8, 1, 0xF0])
+    body = bytes([0, 1, 2, 3, 4]) + bytes([3, 9, 9, 9, 9]) + bytes([200, 7, 7, 7, 7])   # row 0: 0 + 3 + 2
+    body += bytes([255, 5, 6, 7, 8])                                                      # row 1: 255 -> 5
+    path = str(tmp_path / "r.pic")
+    with open(path, "wb") as fh:
+        fh.write(head + body)
+    want = np.zeros((h, w, 4), np.uint8)
+    want[0, :3] = (9, 9, 9, 9)
+    want[0, 3:] = (7, 7, 7, 7)
+    want[1, :] = (5, 6, 7, 8)
+    assert np.array_equal(_dump(native, path, tmp_path), want[::-1])
     assert np.array_equal(image_io.load_image(path), want)
 
 

@@ -152,8 +152,11 @@ def test_half2_quality_gate(native, oracle, name):
     # the FP32 kernel is the FP32 oracle bit for bit (its gap to the FP64 twin
     # is reported by the bench, not gated: it can go either way)
     assert _psnr(native, f32, img, spec) == _psnr(native, oracle.encode(img, **spec), img, spec)
-    # most blocks still agree with the FP32 path bit for bit
-    assert np.all(h2 == f32, axis=1).mean() > 0.5
+    # many blocks still agree with the FP32 path bit for bit: most for UNORM
+    # input; for sRGB input HALF2 fits the texels rounded to linear bytes
+    # (the values the decode is measured against), FP32 the unrounded ones
+    same = np.all(h2 == f32, axis=1).mean()
+    assert same > (0.3 if spec["srgb"] else 0.5), same
 
 
 def test_half2_edge_cases(native, oracle):

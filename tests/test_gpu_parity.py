@@ -375,12 +375,13 @@ def test_choice_is_kept_per_size_class(native):
 
 
 def test_autotune_installs_a_valid_choice(native, oracle):
-    saved = native.get_kernel_choice(6, True, False, True)
+    saved = native.get_kernel_choice_for_size(6, True, False, True, 512, 384)
     try:
         r = native.autotune(6, True, False, True, 512, 384)
         assert r.store in (0, 1, 2, 3) and r.threads in (64, 128, 256)
         assert 0 < r.best_us <= r.default_us
-        assert native.get_kernel_choice(6, True, False, True) == (r.store, r.threads)
+        # installed for the tuned size's class (512x384 6x6 is under one wave)
+        assert native.get_kernel_choice_for_size(6, True, False, True, 512, 384) == (r.store, r.threads)
         img = _texture(130, 70, seed=77)
         opts = dict(block_dim=6, has_alpha=True, srgb=True, border=1)
         assert np.array_equal(native.encode(img, **opts), oracle.encode(img, **opts))
