@@ -455,8 +455,10 @@ bool decode_tga(const uint8_t* d, size_t n, Image& img, std::string& err) {
         size_t o = 0;
         while (o < raw.size()) {
             if (pos >= n) { err = "TGA data too short"; return false; }
-            const int c = d[pos++], count = (c & 0x7F) + 1;
-            if (o + (size_t)count * px > raw.size()) { err = "TGA run past the image"; return false; }
+            const int c = d[pos++];
+            // a packet that runs past the last pixel ends with the image (as
+            // stb_image, the reference's loader, reads it)
+            const int count = (int)std::min<size_t>((size_t)(c & 0x7F) + 1, (raw.size() - o) / px);
             if (c & 0x80) {                               // one pixel repeated
                 if (pos + px > n) { err = "TGA data too short"; return false; }
                 for (int i = 0; i < count; ++i, o += px) std::copy(d + pos, d + pos + px, raw.begin() + o);
@@ -536,12 +538,23 @@ bool decode_bmp(const uint8_t* d, size_t n, Image& img, std::string& err) {
     img.width = w;
     img.height = h;
     img.rgba.assign((size_t)w * h * 4, 255);
+    // a mask's field widened to 8 bits the way stb_image -- the reference's
+    // loader -- widens it: the masked value is moved so the mask's top bit
+    // sits at bit 7, its top n bits (n = the mask's bit count) are the field,
+    // and the field's bits repeat to fill 8 bits (a 5-bit 11000 reads
+    // 11000110); a field of 8 bits or more keeps the 8 below the top bit
     auto channel = [](uint32_t v, uint32_t m) -> uint8_t {
         if (!m) return 255;
-        int shift = 0;
-        while (!((m >> shift) & 1)) ++shift;
-        const uint32_t x = (v & m) >> shift, top = m >> shift;
-        return (uint8_t)(top == 255 ? x : (uint32_t)(((uint64_t)x * 255 + top / 2) / top));
+        int hb = 31, n = 0;
+        while (!((m >> hb) & 1)) --hb;
+        for (int i = 0; i < 32; ++i) n += (m >> i) & 1;
+        const uint32_t y = (hb >= 7 ? (v & m) >> (hb - 7) : (v & m) << (7 - hb)) & 0xFFu;
+        if (n >= 8) return (uint8_t)y;
+        const uint32_t x = y >> (8 - n);
+        uint32_t acc = 0;
+        int bits = 0;
+        while (bits < 8) { acc = (acc << n) | x; bits += n; }
+        return (uint8_t)(acc >> (bits - 8));
     };
     for (int y = 0; y < h; ++y) {
         const uint8_t* s = d + off + (size_t)(top_down ? y : h - 1 - y) * stride;
@@ -590,17 +603,21 @@ struct JpegHuff {
     uint8_t sym[256] = {};
     int mincode[17] = {}, maxcode[18] = {}, valptr[17] = {};
     bool present = false;
-    void build() {
+    // false when the code lengths over-fill the code space (more codes of a
+    // length than the shorter ones leave), which T.81 forbids
+    bool build() {
         int code = 0, k = 0;
         for (int l = 1; l <= 16; ++l) {
             valptr[l] = k;
             mincode[l] = code;
             code += count[l];
             k += count[l];
+            if (code > (1 << l)) return false;
             maxcode[l] = count[l] ? code - 1 : -1;
             code <<= 1;
         }
         maxcode[17] = 0x7FFFFFFF;
+        return true;
     }
 };
 
@@ -838,7 +855,7 @@ bool decode_jpeg(const uint8_t* d, size_t n, Image& img, std::string& err) {
                 for (int l = 1; l <= 16; ++l) { h.count[l] = d[o + l]; total += h.count[l]; }
                 if (total > 256 || o + 17 + total > end) { err = "bad JPEG Huffman table"; return false; }
                 for (int i = 0; i < total; ++i) h.sym[i] = d[o + 17 + i];
-                h.build();
+                if (!h.build()) { err = "bad JPEG Huffman table"; return false; }
                 h.present = true;
                 o += 17 + total;
             }
@@ -1013,8 +1030,9 @@ bool decode_jpeg(const uint8_t* d, size_t n, Image& img, std::string& err) {
 // their high byte), grey(+alpha) or RGB(+alpha) from the first channels (extra
 // channels ignored), raw or PackBits run-length planes.  Photoshop mattes the
 // merged image's partly transparent pixels against white (c = a x + (1 - a)
-// 255); the matte is removed, x = 255 (c - 255 + A) / A for alpha A in 1..254,
-// rounded and clamped.
+// 255); the matte is removed for alpha A in 1..254 with the reference
+// loader's arithmetic: FP32 c / a + 255 (1 - 1 / a), a = A / 255, truncated,
+// 0 below 0.
 bool decode_psd(const uint8_t* d, size_t n, Image& img, std::string& err) {
     auto be16 = [&](size_t o) { return (uint32_t)((d[o] << 8) | d[o + 1]); };
     auto be32 = [&](size_t o) { return (be16(o) << 16) | be16(o + 2); };
@@ -1086,9 +1104,13 @@ bool decode_psd(const uint8_t* d, size_t n, Image& img, std::string& err) {
         const int a = ch[used - 1][i];
         o[3] = (uint8_t)a;
         if (a == 0 || a == 255) continue;
+        // stb_image's arithmetic (the reference's loader): FP32, c / a +
+        // 255 (1 - 1 / a) with a = A / 255, truncated; below 0 (where stb
+        // converts a negative float, which C leaves undefined) reads 0
+        const float af = (float)a / 255.0f, ra = 1.0f / af, inv_a = 255.0f * (1.0f - ra);
         for (int c = 0; c < 3; ++c) {
-            const int v = 255 * ((int)o[c] - 255 + a);
-            o[c] = (uint8_t)(v <= 0 ? 0 : std::min(255, (v + a / 2) / a));
+            const float v = (float)o[c] * ra + inv_a;
+            o[c] = v <= 0.0f ? 0 : (uint8_t)(int)v;
         }
     }
     return true;

@@ -90,7 +90,7 @@ def load_png(path: str) -> np.ndarray:
     chans = {0: 1, 2: 3, 3: 1, 4: 2, 6: 4}[ctype]
     if not (depth == 8 or (depth == 16 and ctype != 3) or (ctype in (0, 3) and depth in (1, 2, 4))):
         raise ValueError("bad PNG bit depth")
-    raw = zlib.decompress(b"".join(idat))
+    raw = _zlib_inflate(b"".join(idat))
     passes = [(0, 0, 8, 8), (4, 0, 8, 8), (0, 4, 4, 8), (2, 0, 4, 4), (0, 2, 2, 4), (1, 0, 2, 2),
               (0, 1, 1, 2)] if interlace else [(0, 0, 1, 1)]
     samples = np.zeros((h, w, chans), np.int64)               # in the image's own bit depth
@@ -224,15 +224,30 @@ def load_bmp(path: str) -> np.ndarray:
     for ch, m in enumerate(masks):
         if not m:
             continue
-        shift = (m & -m).bit_length() - 1
-        top = m >> shift
-        x = (v & m) >> shift
-        out[..., ch] = x if top == 255 else (x * 255 + top // 2) // top
+        out[..., ch] = _widen_field(v, m)
     # a 32-bit BI_RGB image whose fourth byte is 0 everywhere reads as opaque
     # (stb_image, the reference's loader, for 40- and 56-byte headers)
     if bpp == 32 and comp == 0 and hdr in (40, 56) and not out[..., 3].any():
         out[..., 3] = 255
     return out
+
+
+def _widen_field(v, m):
+    """A BMP mask's field widened to 8 bits as stb_image (the reference's
+    loader) widens it: the masked value moved so the mask's top bit sits at
+    bit 7, its top n bits (n = the mask's bit count) taken as the field and
+    repeated to fill 8 bits; 8 or more bits keep the 8 below the top bit."""
+    hb = m.bit_length() - 1
+    n = bin(m).count("1")
+    y = ((v & m) >> (hb - 7) if hb >= 7 else (v & m) << (7 - hb)) & 0xFF
+    if n >= 8:
+        return y.astype(np.uint8)
+    x = y >> (8 - n)
+    acc, bits = np.zeros_like(x), 0
+    while bits < 8:
+        acc = (acc << n) | x
+        bits += n
+    return (acc >> (bits - 8)).astype(np.uint8)
 
 
 def _rgb16(v):
@@ -319,11 +334,27 @@ _ZIGZAG = np.array([0, 1, 8, 16, 9, 2, 3, 10, 17, 24, 32, 25, 18, 11, 4, 5, 12, 
                     62, 63])
 
 
+def _zlib_inflate(z: bytes) -> bytes:
+    """A zlib stream's data: the header is checked (deflate, no preset
+    dictionary), the trailing Adler-32 is not -- as the command line tool's
+    reader and stb_image (the reference's loader) do."""
+    if len(z) < 6 or (z[0] & 0x0F) != 8 or ((z[0] << 8) | z[1]) % 31 or z[1] & 0x20:
+        raise ValueError("bad zlib header")
+    d = zlib.decompressobj(-15)
+    out = d.decompress(z[2:])
+    if not d.eof:
+        raise ValueError("zlib stream truncated")
+    return out
+
+
 def _jpeg_huffman(counts, syms):
-    """(code length, code) -> symbol, as a 16-bit peek table of (symbol, length)."""
+    """(code length, code) -> symbol, as a 16-bit peek table of (symbol, length).
+    Code lengths that over-fill the code space are refused (T.81)."""
     table = np.full((1 << 16, 2), -1, np.int32)
     code, k = 0, 0
     for length in range(1, 17):
+        if code + counts[length - 1] > (1 << length):
+            raise ValueError("bad JPEG Huffman table")
         for _ in range(counts[length - 1]):
             lo = code << (16 - length)
             table[lo:lo + (1 << (16 - length))] = (syms[k], length)
@@ -374,6 +405,8 @@ def load_jpeg(path: str) -> np.ndarray:
             while o < end:
                 counts = d[o + 1:o + 17]
                 total = sum(counts)
+                if d[o] >> 4 > 1 or d[o] & 15 > 3 or o + 17 > end or total > 256 or o + 17 + total > end:
+                    raise ValueError("bad JPEG Huffman table")
                 huff[(d[o] >> 4, d[o] & 15)] = _jpeg_huffman(counts, d[o + 17:o + 17 + total])
                 o += 17 + total
         elif m in (0xC0, 0xC1, 0xC2):
@@ -386,6 +419,8 @@ def load_jpeg(path: str) -> np.ndarray:
             for i in range(nc):
                 c = d[seg + 6 + 3 * i:seg + 9 + 3 * i]
                 comps.append({"id": c[0], "h": c[1] >> 4, "v": c[1] & 15, "tq": c[2] & 3})
+                if not (1 <= c[1] >> 4 <= 2 and 1 <= c[1] & 15 <= 2):
+                    raise ValueError("unsupported JPEG sampling")
             if nc == 1:
                 comps[0]["h"] = comps[0]["v"] = 1
             hmax = max(c["h"] for c in comps)
@@ -654,6 +689,8 @@ def load_psd(path: str) -> np.ndarray:
         raise ValueError("PSD colour mode not read (greyscale and RGB are)")
     if depth not in (8, 16):
         raise ValueError("only 8- and 16-bit PSD is read")
+    if not 1 <= channels <= 56:
+        raise ValueError("bad PSD channel count")
     if not (0 < w <= 1 << 30 and 0 < h <= 1 << 30 and w * h <= 1 << 30):
         raise ValueError("bad image size")
     pos = 26
@@ -703,8 +740,13 @@ def load_psd(path: str) -> np.ndarray:
         a = chans[-1].astype(np.int64)
         out[..., 3] = a
         part = (a > 0) & (a < 255)
-        v = 255 * (out[..., :3].astype(np.int64) - 255 + a[..., None])
-        x = np.where(v <= 0, 0, np.minimum(255, (v + a[..., None] // 2) // np.maximum(a[..., None], 1)))
+        # the reference loader's FP32 arithmetic: c / a + 255 (1 - 1 / a),
+        # a = A / 255, truncated, 0 below 0
+        af = a.astype(np.float32) / np.float32(255.0)
+        ra = np.float32(1.0) / np.maximum(af, np.float32(1e-30))
+        inv_a = np.float32(255.0) * (np.float32(1.0) - ra)
+        v = out[..., :3].astype(np.float32) * ra[..., None] + inv_a[..., None]
+        x = np.where(v <= 0, 0, np.floor(np.maximum(v, 0))).astype(np.uint8)
         out[..., :3] = np.where(part[..., None], x, out[..., :3])
     return out
 

@@ -508,9 +508,10 @@ def test_cli_reads_16bit_bmp(native, tmp_path, masks):
     want = np.full((h, w, 4), 255, np.uint8)
     for c, m in enumerate(masks or (0x7C00, 0x03E0, 0x001F)):
         shift = (m & -m).bit_length() - 1
-        top = m >> shift
+        n = bin(m >> shift).count("1")
         x = (v & m) >> shift
-        want[..., c] = (x * 255 + top // 2) // top
+        # the field's bits repeated, cut to 8: the binary fraction x / (2^n - 1)
+        want[..., c] = np.minimum(255, (x * 256) // ((1 << n) - 1))
     assert np.array_equal(_dump(native, path, tmp_path), want[::-1])
     from astc_encoder_gb300 import image_io
     assert np.array_equal(image_io.load_image(path), want)
@@ -1144,13 +1145,17 @@ def test_cli_reads_psd(native, tmp_path, mode, nch, extra, depth, rle):
         a = planes[-1].astype(np.int64)
         want[..., 3] = a
         part = (a > 0) & (a < 255)
-        v = 255 * (want[..., :3].astype(np.int64) - 255 + a[..., None])
-        x = np.where(v <= 0, 0, np.minimum(255, (v + a[..., None] // 2) // np.maximum(a[..., None], 1)))
+        # the matte comes off with the reference loader's FP32 arithmetic:
+        # c / f + 255 (1 - 1 / f) for f = A / 255, truncated (0 below 0)
+        f = a.astype(np.float32) / np.float32(255)
+        ra = np.float32(1) / np.maximum(f, np.float32(1e-30))
+        v = want[..., :3].astype(np.float32) * ra[..., None] + (np.float32(255) * (np.float32(1) - ra))[..., None]
+        x = np.where(v <= 0, 0, np.floor(np.maximum(v, 0))).astype(np.uint8)
         want[..., :3] = np.where(part[..., None], x, want[..., :3])
         # the un-matted colour is the original within the matte's rounding
         orig = color[:-1].transpose(1, 2, 0).astype(int) if mode == 3 else color[0][..., None].astype(int)
         sel = part & (a >= 32)
-        assert np.abs(want[..., :3].astype(int) - orig)[sel].max() <= 5
+        assert np.abs(want[..., :3].astype(int) - orig)[sel].max() <= 6
     assert np.array_equal(got, want)
     from astc_encoder_gb300 import image_io                 # the Python reader agrees
     assert np.array_equal(image_io.load_image(path), want)
