@@ -20,6 +20,7 @@
 // the atomicAdd that hands out items.
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <map>
@@ -156,6 +157,9 @@ struct astc_batch {
     uint8_t* h_buf = nullptr;       // pinned staging of the same layout
     size_t buf_bytes = 0;
     cudaStream_t capture_stream = nullptr;
+    // per-format branches of the captured graph (created with the first graph)
+    cudaStream_t branch[kFormats] = {};
+    cudaEvent_t fork = nullptr, join[kFormats] = {};
     cudaEvent_t done = nullptr;
     bool pending = false;
     std::map<unsigned, cudaGraphExec_t> graphs;   // key: precision << 16 | format mask
@@ -192,15 +196,40 @@ astc_status validate_item(const astc_batch_item& t, int i, long long* blocks, Sp
     return ASTC_OK;
 }
 
+// ASTC_GB300_BATCH_SERIAL=1 captures the formats' kernels one after another
+// on one stream instead of as parallel branches (for comparison).
+bool batch_serial() {
+    static const bool on = [] {
+        const char* v = getenv("ASTC_GB300_BATCH_SERIAL");
+        return v && v[0] == '1';
+    }();
+    return on;
+}
+
 // Captures one persistent kernel per format in `mask` (the descriptor upload
-// is issued before the launch with the exact sizes of each batch).
+// is issued before the launch with the exact sizes of each batch).  The
+// kernels are parallel branches of the graph: each fills every SM slot it
+// can get and drains its own format's queue, and the CTAs of the other
+// formats take the slots as they free up, so no format's tail leaves the
+// GPU idle before the next one starts.
 astc_status build_graph(astc_batch* b, unsigned mask, int prec, cudaGraphExec_t* out) {
+    cudaError_t e = cudaSuccess;
+    if (!b->fork) {
+        e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
+        for (int f = 0; f < kFormats && e == cudaSuccess; ++f) {
+            e = cudaStreamCreateWithFlags(&b->branch[f], cudaStreamNonBlocking);
+            if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->join[f], cudaEventDisableTiming);
+        }
+        if (e != cudaSuccess) return cuda_error(e, "batch branch streams");
+    }
+    const bool serial = batch_serial();
     cudaStream_t s = b->capture_stream;
-    cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+    e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return cuda_error(e, "cudaStreamBeginCapture");
     auto* q = reinterpret_cast<QueueState*>(b->d_buf);
     auto* jobs = reinterpret_cast<BatchJob*>(b->d_buf + jobs_offset());
     auto* items = reinterpret_cast<WorkItem*>(b->d_buf + items_offset(b->max_items));
+    if (!serial) e = cudaEventRecord(b->fork, s);
     for (int f = 0; f < kFormats && e == cudaSuccess; ++f) {
         if (!(mask & (1u << f))) continue;
         KernelFn k = prec == ASTC_PRECISION_HALF2 ? kernel_for<ASTC_PRECISION_HALF2>(f)
@@ -210,8 +239,14 @@ astc_status build_graph(astc_batch* b, unsigned mask, int prec, cudaGraphExec_t*
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, kBatchThreads, smem);
         if (e != cudaSuccess) break;
         const int grid = (occ > 0 ? occ : 1) * b->sms;
-        k<<<grid, kBatchThreads, smem, s>>>(jobs, items, q, f);
-        e = cudaGetLastError();
+        cudaStream_t ks = serial ? s : b->branch[f];
+        if (!serial && (e = cudaStreamWaitEvent(ks, b->fork, 0)) != cudaSuccess) break;
+        k<<<grid, kBatchThreads, smem, ks>>>(jobs, items, q, f);
+        if ((e = cudaGetLastError()) != cudaSuccess) break;
+        if (!serial) {
+            if ((e = cudaEventRecord(b->join[f], ks)) != cudaSuccess) break;
+            e = cudaStreamWaitEvent(s, b->join[f], 0);
+        }
     }
     cudaGraph_t g = nullptr;
     const cudaError_t e2 = cudaStreamEndCapture(s, &g);
@@ -421,6 +456,11 @@ astc_status astc_batch_destroy(astc_batch* b) {
     cudaSetDevice(b->device);
     if (b->pending && b->done) cudaEventSynchronize(b->done);
     for (auto& kv : b->graphs) cudaGraphExecDestroy(kv.second);
+    for (int f = 0; f < kFormats; ++f) {
+        if (b->branch[f]) cudaStreamDestroy(b->branch[f]);
+        if (b->join[f]) cudaEventDestroy(b->join[f]);
+    }
+    if (b->fork) cudaEventDestroy(b->fork);
     if (b->done) cudaEventDestroy(b->done);
     if (b->capture_stream) cudaStreamDestroy(b->capture_stream);
     if (b->d_buf) cudaFree(b->d_buf);
