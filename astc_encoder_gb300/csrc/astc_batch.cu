@@ -45,6 +45,8 @@ __constant__ SrgbBits c_srgb_bits_b = make_srgb_bits();
 struct BatchJob {
     TextureView tex;
     uint4* out;
+    int item_start;     // index of the job's first work item (items grouped by format)
+    int nblocks;
 };
 
 struct WorkItem {
@@ -58,8 +60,28 @@ struct QueueState {
     int counter[kFormats];
     int begin[kFormats];
     int end[kFormats];
-    int pad[kFormats];
+    int njobs;
+    int pad[kFormats - 1];
 };
+
+// Expands the jobs into their work items of <= 128 blocks on the device (the
+// host uploads only the per-texture descriptors, O(textures) per call).
+__global__ void __launch_bounds__(kBatchThreads)
+astc_batch_expand(const BatchJob* __restrict__ jobs, WorkItem* __restrict__ items, const QueueState* __restrict__ q) {
+    const int njobs = q->njobs;
+    for (int j = blockIdx.x; j < njobs; j += gridDim.x) {
+        const int start = jobs[j].item_start, nb = jobs[j].nblocks;
+        const int n = (nb + kBatchThreads - 1) / kBatchThreads;
+        for (int t = threadIdx.x; t < n; t += blockDim.x) {
+            WorkItem w;
+            w.job = j;
+            w.first = t * kBatchThreads;
+            w.count = nb - w.first < kBatchThreads ? nb - w.first : kBatchThreads;
+            w.pad = 0;
+            items[start + t] = w;
+        }
+    }
+}
 
 inline int format_index(int dim, bool alpha, bool normal, bool srgb) {
     return (dim == 6 ? 8 : 0) | (alpha ? 4 : 0) | (normal ? 2 : 0) | (srgb ? 1 : 0);
@@ -154,13 +176,14 @@ struct astc_batch {
     int sms = 0;
     // device: [QueueState][BatchJob x max_items][WorkItem x max_work]
     uint8_t* d_buf = nullptr;
-    uint8_t* h_buf = nullptr;       // pinned staging of the same layout
+    uint8_t* h_buf = nullptr;       // pinned staging of [QueueState][BatchJob x max_items]
     size_t buf_bytes = 0;
     cudaStream_t capture_stream = nullptr;
     // per-format branches of the captured graph (created with the first graph)
     cudaStream_t branch[kFormats] = {};
     cudaEvent_t fork = nullptr, join[kFormats] = {};
-    cudaEvent_t done = nullptr;
+    cudaEvent_t done = nullptr;       // the last batch's graph has finished
+    cudaEvent_t uploaded = nullptr;   // the last batch's descriptors have left h_buf
     bool pending = false;
     std::map<unsigned, cudaGraphExec_t> graphs;   // key: precision << 16 | format mask
 };
@@ -229,7 +252,9 @@ astc_status build_graph(astc_batch* b, unsigned mask, int prec, cudaGraphExec_t*
     auto* q = reinterpret_cast<QueueState*>(b->d_buf);
     auto* jobs = reinterpret_cast<BatchJob*>(b->d_buf + jobs_offset());
     auto* items = reinterpret_cast<WorkItem*>(b->d_buf + items_offset(b->max_items));
-    if (!serial) e = cudaEventRecord(b->fork, s);
+    astc_batch_expand<<<4 * b->sms, kBatchThreads, 0, s>>>(jobs, items, q);
+    e = cudaGetLastError();
+    if (!serial && e == cudaSuccess) e = cudaEventRecord(b->fork, s);
     for (int f = 0; f < kFormats && e == cudaSuccess; ++f) {
         if (!(mask & (1u << f))) continue;
         KernelFn k = prec == ASTC_PRECISION_HALF2 ? kernel_for<ASTC_PRECISION_HALF2>(f)
@@ -280,15 +305,17 @@ astc_status astc_batch_create(int max_textures, long long max_blocks, astc_batch
     cudaError_t e = cudaGetDevice(&b->device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, b->device);
     if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&b->d_buf), b->buf_bytes);
-    if (e == cudaSuccess) e = cudaMallocHost(reinterpret_cast<void**>(&b->h_buf), b->buf_bytes);
+    // the host stages the queue header and descriptors only (items are built on the device)
+    if (e == cudaSuccess) e = cudaMallocHost(reinterpret_cast<void**>(&b->h_buf), items_offset(max_textures));
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->capture_stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->uploaded, cudaEventDisableTiming);
     if (e != cudaSuccess) {
         const astc_status st = cuda_error(e, "batch allocation");
         astc_batch_destroy(b);
         return st;
     }
-    memset(b->h_buf, 0, b->buf_bytes);
+    memset(b->h_buf, 0, items_offset(max_textures));
     *out = b;
     return ASTC_OK;
 }
@@ -320,13 +347,12 @@ astc_status astc_batch_encode(astc_batch* b, const astc_batch_item* in, int coun
         }
         if (blocks > b->max_blocks) return set_error(ASTC_ERR_INVALID_ARG, "batch exceeds max_blocks");
         // the previous batch's upload must have left the pinned staging buffer
+        // (the host waits for that only; its kernels may still be running)
         if (b->pending) {
-            if ((e = cudaEventSynchronize(b->done)) != cudaSuccess) return cuda_error(e, "previous batch");
-            b->pending = false;
+            if ((e = cudaEventSynchronize(b->uploaded)) != cudaSuccess) return cuda_error(e, "previous batch");
         }
         auto* q = reinterpret_cast<QueueState*>(b->h_buf);
         auto* jobs = reinterpret_cast<BatchJob*>(b->h_buf + jobs_offset());
-        auto* items = reinterpret_cast<WorkItem*>(b->h_buf + items_offset(b->max_items));
         unsigned mask = 0;
         int cursor[kFormats];
         int total = 0;
@@ -356,14 +382,11 @@ astc_status astc_batch_encode(astc_batch* b, const astc_batch_item* in, int coun
             jobs[i].out = reinterpret_cast<uint4*>(t.out);
             const int nb = blocks_x(t.width, t.block_dim) * blocks_y(t.height, t.block_dim);
             int& c = cursor[format_index(t.block_dim, t.has_alpha, t.is_normal, t.srgb)];
-            for (int first = 0; first < nb; first += kBatchThreads) {
-                items[c].job = i;
-                items[c].first = first;
-                items[c].count = nb - first < kBatchThreads ? nb - first : kBatchThreads;
-                items[c].pad = 0;
-                ++c;
-            }
+            jobs[i].item_start = c;
+            jobs[i].nblocks = nb;
+            c += (nb + kBatchThreads - 1) / kBatchThreads;
         }
+        q->njobs = count;
         if (!mask) return ASTC_OK;
         const unsigned key = ((unsigned)precision << 16) | mask;
         auto it = b->graphs.find(key);
@@ -374,17 +397,20 @@ astc_status astc_batch_encode(astc_batch* b, const astc_batch_item* in, int coun
             it = b->graphs.emplace(key, g).first;
         }
         cudaStream_t s = static_cast<cudaStream_t>(stream);
-        // upload exactly this batch's queue header + descriptors, and its items
+        // the device buffers are rewritten only after the previous batch's
+        // kernels have finished with them, whatever stream each call uses
+        if (b->pending && (e = cudaStreamWaitEvent(s, b->done, 0)) != cudaSuccess)
+            return cuda_error(e, "cudaStreamWaitEvent");
+        // upload exactly this batch's queue header + descriptors; the graph's
+        // first kernel expands them into work items
         const size_t head = jobs_offset() + (size_t)count * sizeof(BatchJob);
-        const size_t ioff = items_offset(b->max_items);
-        if ((e = cudaMemcpyAsync(b->d_buf, b->h_buf, head, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
-            (e = cudaMemcpyAsync(b->d_buf + ioff, b->h_buf + ioff, (size_t)total * sizeof(WorkItem),
-                                 cudaMemcpyHostToDevice, s)) != cudaSuccess)
+        if ((e = cudaMemcpyAsync(b->d_buf, b->h_buf, head, cudaMemcpyHostToDevice, s)) != cudaSuccess)
             return cuda_error(e, "descriptor upload");
+        if ((e = cudaEventRecord(b->uploaded, s)) != cudaSuccess) return cuda_error(e, "cudaEventRecord");
         if ((e = cudaGraphLaunch(it->second, s)) != cudaSuccess) return cuda_error(e, "cudaGraphLaunch");
         if ((e = cudaEventRecord(b->done, s)) != cudaSuccess) return cuda_error(e, "cudaEventRecord");
         b->pending = true;
-        int kernels = 0;
+        int kernels = 1;                                  // the item expansion
         for (int f = 0; f < kFormats; ++f) kernels += (mask >> f) & 1;
         count_launches((uint64_t)kernels);
         if (!stream) {
@@ -462,6 +488,7 @@ astc_status astc_batch_destroy(astc_batch* b) {
     }
     if (b->fork) cudaEventDestroy(b->fork);
     if (b->done) cudaEventDestroy(b->done);
+    if (b->uploaded) cudaEventDestroy(b->uploaded);
     if (b->capture_stream) cudaStreamDestroy(b->capture_stream);
     if (b->d_buf) cudaFree(b->d_buf);
     if (b->h_buf) cudaFreeHost(b->h_buf);

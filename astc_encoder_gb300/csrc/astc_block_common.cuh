@@ -205,33 +205,34 @@ __device__ __forceinline__ void load_cta_tables(const TritPack& tp, const SrgbBi
 template <bool ALPHA>
 __device__ __forceinline__ uint4 assemble_block(const uint32_t q0[4], const uint32_t q1[4],
                                                 const uint32_t qw[16], const uint8_t* trits) {
-    // scramble (ASTC_Encode.hlsl:498-502) + trits ISE of 16 weights (ISE 142-176, 243-256)
+    // scramble (ASTC_Encode.hlsl:498-502) + trits ISE of 16 weights (ISE 142-176, 243-256):
+    // each group of five symbols packs into 5 B + 8 bits -- m0, T[1:0], m1, T[3:2], m2,
+    // T[4], m3, T[6:5], m4, T[7] -- assembled in 32 bits (the widest group is 18 bits),
+    // T's fields masked in place and shifted once each
     constexpr int WQ = ALPHA ? kQuant6 : kQuant12;
     constexpr int B = ALPHA ? 1 : 2;
+    constexpr int GW = 5 * B + 8;
+    constexpr uint32_t M = (1u << B) - 1u;
+    constexpr uint32_t R = ALPHA ? 5u : 11u;
     constexpr uint64_t kScr = scramble_nibbles(WQ);
-    constexpr uint32_t kScrLo = (uint32_t)kScr, kScrHi = (uint32_t)(kScr >> 32);
+    uint32_t sym[20];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+        const uint32_t q = qw[i];
+        sym[i] = (R < 8 ? ((uint32_t)kScr >> (4 * q)) : (uint32_t)(kScr >> (4 * q))) & 0xFu;
+    }
+#pragma unroll
+    for (int i = 16; i < 20; ++i) sym[i] = 0u;
     uint64_t ws = 0;
 #pragma unroll
     for (int g = 0; g < 4; ++g) {
-        uint32_t mm[5], tt[5];
-#pragma unroll
-        for (int j = 0; j < 5; ++j) {
-            const int idx = g * 5 + j;
-            uint32_t s = 0;
-            if (idx < 16) {
-                const uint32_t q = qw[idx < 16 ? idx : 0];
-                s = (q < 8 ? (kScrLo >> (4 * q)) : (kScrHi >> (4 * (q - 8)))) & 0xFu;
-            }
-            mm[j] = s & ((1u << B) - 1u);
-            tt[j] = s >> B;
-        }
-        const uint32_t T = trits[tt[4] * 81 + tt[3] * 27 + tt[2] * 9 + tt[1] * 3 + tt[0]];
-        const uint64_t grp = (uint64_t)mm[0] | ((uint64_t)(T & 3u) << B) |
-                             ((uint64_t)mm[1] << (B + 2)) | ((uint64_t)((T >> 2) & 3u) << (2 * B + 2)) |
-                             ((uint64_t)mm[2] << (2 * B + 4)) | ((uint64_t)((T >> 4) & 1u) << (3 * B + 4)) |
-                             ((uint64_t)mm[3] << (3 * B + 5)) | ((uint64_t)((T >> 5) & 3u) << (4 * B + 5)) |
-                             ((uint64_t)mm[4] << (4 * B + 7)) | ((uint64_t)((T >> 7) & 1u) << (5 * B + 7));
-        ws |= grp << (g * (5 * B + 8));
+        const uint32_t* v = sym + 5 * g;
+        const uint32_t T = trits[(v[0] >> B) + 3u * (v[1] >> B) + 9u * (v[2] >> B) + 27u * (v[3] >> B) +
+                                 81u * (v[4] >> B)];
+        const uint32_t grp = (v[0] & M) | ((T & 0x3u) << B) | ((v[1] & M) << (B + 2)) | ((T & 0xCu) << (2 * B)) |
+                             ((v[2] & M) << (2 * B + 4)) | ((T & 0x10u) << (3 * B)) | ((v[3] & M) << (3 * B + 5)) |
+                             ((T & 0x60u) << (4 * B)) | ((v[4] & M) << (4 * B + 7)) | ((T & 0x80u) << (5 * B));
+        ws |= (uint64_t)grp << (g * GW);
     }
     // endpoints in QUANT_256: r0 r1 g0 g1 b0 b1 [a0 a1], 8 bits each (bise_endpoints)
     uint64_t ep = (uint64_t)q0[0] | ((uint64_t)q1[0] << 8) | ((uint64_t)q0[1] << 16) |
