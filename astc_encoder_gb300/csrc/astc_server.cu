@@ -116,6 +116,10 @@ struct Interval {
     int requests;
 };
 
+// A server that is never asked to reset its statistics keeps the record of
+// its most recent 2^20 launches (16 MiB) and drops older halves.
+constexpr size_t kMaxIntervals = size_t(1) << 20;
+
 }  // namespace
 }  // namespace astc
 
@@ -137,7 +141,8 @@ struct astc_server {
     Clock::time_point t0 = Clock::now();
     std::string worker_error;
     cudaEvent_t t0_event = nullptr;          // device clock origin of the intervals
-    std::vector<Interval> intervals;         // retired launches since the last reset
+    std::vector<Interval> intervals;         // retired launches since the last reset (the
+                                             // most recent kMaxIntervals of them)
 };
 
 namespace {
@@ -238,8 +243,11 @@ void worker_main(astc_server* s) {
             } else {
                 float a = 0.0f, b = 0.0f;
                 if (cudaEventElapsedTime(&a, s->t0_event, slot.t_start) == cudaSuccess &&
-                    cudaEventElapsedTime(&b, s->t0_event, slot.t_end) == cudaSuccess)
+                    cudaEventElapsedTime(&b, s->t0_event, slot.t_end) == cudaSuccess) {
+                    if (s->intervals.size() >= kMaxIntervals)
+                        s->intervals.erase(s->intervals.begin(), s->intervals.begin() + kMaxIntervals / 2);
                     s->intervals.push_back({a, b, (int)slot.reqs.size()});
+                }
                 cudaGetLastError();
             }
             slot.reqs.clear();

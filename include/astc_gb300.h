@@ -272,7 +272,8 @@ astc_status astc_server_replay(astc_server* server, const astc_request* requests
 /* Device-side record of the slot launches retired since the last reset
  * (timing events recorded on each slot's stream before its first copy and
  * after its last): how busy the device was and how much the slots' work
- * overlapped.  (No counterpart in the reference.) */
+ * overlapped.  The record holds at most the most recent 2^20 launches.
+ * (No counterpart in the reference.) */
 typedef struct astc_server_stats {
     long long launches;          /* slot launches (batches, or requests)       */
     long long requests;          /* requests they carried                      */
