@@ -293,6 +293,64 @@ void count_launches(uint64_t n) { g_launches.fetch_add(n, std::memory_order_rela
 
 using namespace astc;
 
+namespace {
+
+// Shared body of the SSE reductions: stages host images through the pool,
+// zeroes the 32-byte accumulator, runs `launch(a, b, accumulator, stream)` and
+// reads the accumulator back into `result` (`result_bytes` of it).
+template <class Launch>
+astc_status sse_common(const uint8_t* a, const uint8_t* b, size_t texels, int memory, void* stream,
+                       void* result, size_t result_bytes, Launch launch) {
+    try {
+        if (!a || !b || !result) return set_error(ASTC_ERR_INVALID_ARG, "NULL pointer");
+        if (memory != ASTC_MEMORY_HOST && memory != ASTC_MEMORY_DEVICE)
+            return set_error(ASTC_ERR_INVALID_ARG, "bad memory kind");
+        if (texels > SIZE_MAX / 4) return set_error(ASTC_ERR_INVALID_ARG, "texel count overflows the byte size");
+        DevicePool* pool = nullptr;
+        int dev = 0;
+        astc_status st;
+        if ((st = pool_for_current(&pool, &dev)) != ASTC_OK) return st;
+        std::lock_guard<std::mutex> lk(pool->mu);
+        if ((st = pool_init_locked(*pool, dev)) != ASTC_OK) return st;
+        cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : pool->stream;
+        if (!pool->d_sse) {
+            cudaError_t e = cudaMalloc(reinterpret_cast<void**>(&pool->d_sse), 4 * sizeof(unsigned long long));
+            if (e != cudaSuccess) return cuda_error(e, "cudaMalloc of the SSE accumulator");
+        }
+        const uint8_t* da = a;
+        const uint8_t* db = b;
+        if (memory == ASTC_MEMORY_HOST) {
+            const size_t bytes = texels * 4;
+            if ((st = grow(&pool->d_in, &pool->in_cap, bytes)) != ASTC_OK) return st;
+            if ((st = grow(&pool->d_out, &pool->out_cap, bytes)) != ASTC_OK) return st;
+            cudaError_t e = cudaMemcpyAsync(pool->d_in, a, bytes, cudaMemcpyHostToDevice, s);
+            if (e == cudaSuccess) e = cudaMemcpyAsync(pool->d_out, b, bytes, cudaMemcpyHostToDevice, s);
+            if (e != cudaSuccess) return cuda_error(e, "host-to-device copy");
+            da = pool->d_in;
+            db = pool->d_out;
+        } else {
+            if ((st = check_device_pointer(a, texels * 4, "a")) != ASTC_OK) return st;
+            if ((st = check_device_pointer(b, texels * 4, "b")) != ASTC_OK) return st;
+            if (reinterpret_cast<uintptr_t>(a) % 4 != 0 || reinterpret_cast<uintptr_t>(b) % 4 != 0)
+                return set_error(ASTC_ERR_INVALID_ARG, "images must be 4-byte aligned");
+        }
+        cudaError_t e = cudaMemsetAsync(pool->d_sse, 0, 4 * sizeof(unsigned long long), s);
+        if (e != cudaSuccess) return cuda_error(e, "cudaMemsetAsync");
+        e = launch(da, db, pool->d_sse, s);
+        if (e != cudaSuccess) return cuda_error(e, "sse kernel launch");
+        unsigned long long h[4];
+        e = cudaMemcpyAsync(h, pool->d_sse, sizeof(h), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) return cuda_error(e, "sse");
+        memcpy(result, h, result_bytes);
+        return ASTC_OK;
+    } catch (...) {
+        return set_error(ASTC_ERR_CUDA, "unexpected exception");
+    }
+}
+
+}  // namespace
+
 extern "C" {
 
 void astc_opts_init(astc_opts* o) {
@@ -580,59 +638,6 @@ astc_status astc_decode_gpu(const uint8_t* blocks, int width, int height, int bl
         if (e != cudaSuccess) return cuda_error(e, "device-to-host copy");
         e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) return cuda_error(e, "decode");
-        return ASTC_OK;
-    } catch (...) {
-        return set_error(ASTC_ERR_CUDA, "unexpected exception");
-    }
-}
-
-// Shared body of the SSE reductions: stages host images through the pool,
-// zeroes the 32-byte accumulator, runs `launch(a, b, accumulator, stream)` and
-// reads the accumulator back into `result` (`result_bytes` of it).
-extern "C++" template <class Launch>
-astc_status sse_common(const uint8_t* a, const uint8_t* b, size_t texels, int memory, void* stream,
-                              void* result, size_t result_bytes, Launch launch) {
-    try {
-        if (!a || !b || !result) return set_error(ASTC_ERR_INVALID_ARG, "NULL pointer");
-        if (memory != ASTC_MEMORY_HOST && memory != ASTC_MEMORY_DEVICE)
-            return set_error(ASTC_ERR_INVALID_ARG, "bad memory kind");
-        DevicePool* pool = nullptr;
-        int dev = 0;
-        astc_status st;
-        if ((st = pool_for_current(&pool, &dev)) != ASTC_OK) return st;
-        std::lock_guard<std::mutex> lk(pool->mu);
-        if ((st = pool_init_locked(*pool, dev)) != ASTC_OK) return st;
-        cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : pool->stream;
-        if (!pool->d_sse) {
-            cudaError_t e = cudaMalloc(reinterpret_cast<void**>(&pool->d_sse), 4 * sizeof(unsigned long long));
-            if (e != cudaSuccess) return cuda_error(e, "cudaMalloc of the SSE accumulator");
-        }
-        const uint8_t* da = a;
-        const uint8_t* db = b;
-        if (memory == ASTC_MEMORY_HOST) {
-            const size_t bytes = texels * 4;
-            if ((st = grow(&pool->d_in, &pool->in_cap, bytes)) != ASTC_OK) return st;
-            if ((st = grow(&pool->d_out, &pool->out_cap, bytes)) != ASTC_OK) return st;
-            cudaError_t e = cudaMemcpyAsync(pool->d_in, a, bytes, cudaMemcpyHostToDevice, s);
-            if (e == cudaSuccess) e = cudaMemcpyAsync(pool->d_out, b, bytes, cudaMemcpyHostToDevice, s);
-            if (e != cudaSuccess) return cuda_error(e, "host-to-device copy");
-            da = pool->d_in;
-            db = pool->d_out;
-        } else {
-            if ((st = check_device_pointer(a, texels * 4, "a")) != ASTC_OK) return st;
-            if ((st = check_device_pointer(b, texels * 4, "b")) != ASTC_OK) return st;
-            if (reinterpret_cast<uintptr_t>(a) % 4 != 0 || reinterpret_cast<uintptr_t>(b) % 4 != 0)
-                return set_error(ASTC_ERR_INVALID_ARG, "images must be 4-byte aligned");
-        }
-        cudaError_t e = cudaMemsetAsync(pool->d_sse, 0, 4 * sizeof(unsigned long long), s);
-        if (e != cudaSuccess) return cuda_error(e, "cudaMemsetAsync");
-        e = launch(da, db, pool->d_sse, s);
-        if (e != cudaSuccess) return cuda_error(e, "sse kernel launch");
-        unsigned long long h[4];
-        e = cudaMemcpyAsync(h, pool->d_sse, sizeof(h), cudaMemcpyDeviceToHost, s);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-        if (e != cudaSuccess) return cuda_error(e, "sse");
-        memcpy(result, h, result_bytes);
         return ASTC_OK;
     } catch (...) {
         return set_error(ASTC_ERR_CUDA, "unexpected exception");
