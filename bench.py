@@ -5,11 +5,14 @@ Workload (default): the 6x6 LDR RGBA sRGB encode with edge clamp of a
 metric "encoded Mtexels/s" is quoted on.  One step encodes a batch of 16
 distinct 2048x2048 textures (268 MB of input, larger than the 129 MB L2, so
 no step reads its inputs from L2), each through the C ABI
-(astc_encode_gpu_pitched, device memory, on torch's current stream).
+(astc_encode_gpu_pitched, device memory), the launches spread round-robin
+over --streams CUDA streams (default 2) forked from torch's current stream.
 
 * value      -- Mtexels/s with inputs resident in HBM, timed with one CUDA
-                event pair around each step on the launching stream (a dedicated
-                non-default torch stream passed to the C ABI; max over ranks).
+                event pair around each step on the timed stream (a dedicated
+                non-default torch stream; the side streams join it before the
+                closing event; max over ranks).  `one_stream` repeats the step
+                with every launch on the timed stream, one after another.
 * e2e        -- the same metric through the same entry point with pinned
                 HOST buffers: each texture goes up through the library's upload
                 ring (copy engine, 32 MiB slots overlapped with the encode) and
@@ -54,6 +57,8 @@ def _parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="6x6_rgba_srgb_2048")
+    ap.add_argument("--streams", type=int, default=2,
+                    help="CUDA streams the headline step's launches are spread over (1 = one after another)")
     ap.add_argument("--no-extra", action="store_true", help="skip the secondary workloads")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--no-batched", action="store_true", help="skip the mixed batched workload")
@@ -281,19 +286,31 @@ def run_reference(args) -> None:
     print(json.dumps(line), flush=True)
 
 
-def _time_launches(torch, native, texs, outs, spec, steps):
+_SIDE_STREAMS: list = []
+
+
+def _time_launches(torch, native, texs, outs, spec, steps, streams: int = 1):
     """Runs `steps` steps over the batch with a CUDA event pair around each step
     (on the launching stream); returns (mean ms per launch, step ms list, launches).
-    Launches within a step run back to back, so step time / launches is the
-    mean launch duration."""
+
+    With `streams` = 1 the launches of a step run back to back on the current
+    stream, so step time / launches is the mean launch duration.  With more,
+    launch i goes to stream i mod `streams`: the side streams wait for the
+    current one at the start of the step and the current one waits for them
+    at its end, so the event pair still brackets the whole step, and one
+    texture's kernel fills the SM slots that the previous texture's last,
+    partial wave leaves idle (the textures are independent); step time /
+    launches is then the effective time per launch."""
     h, w = texs[0].shape[:2]
     stream = torch.cuda.current_stream()
     if stream.cuda_stream == 0:
         # a NULL stream means "synchronous on the library's own stream" in the C ABI
         raise RuntimeError("run the timed loop on a non-default stream")
+    while len(_SIDE_STREAMS) < streams - 1:
+        _SIDE_STREAMS.append(torch.cuda.Stream())
+    side = _SIDE_STREAMS[:streams - 1]
     lib = native.load_library()
-    opts = ctypes.byref(native.make_opts(memory=native.Memory.DEVICE, stream=stream.cuda_stream,
-                                         **spec))
+    opts = [native.make_opts(memory=native.Memory.DEVICE, stream=s.cuda_stream, **spec) for s in [stream] + side]
     ptrs = [(t.data_ptr(), o.data_ptr()) for t, o in zip(texs, outs)]
     enc = lib.astc_encode_gpu_pitched
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
@@ -301,10 +318,14 @@ def _time_launches(torch, native, texs, outs, spec, steps):
     l0 = native.kernel_launch_count()
     for s in range(steps):
         ev[s][0].record(stream)
-        for src, dst in ptrs:
-            st = enc(src, w, h, w * 4, opts, dst)
+        for ss in side:
+            ss.wait_stream(stream)
+        for i, (src, dst) in enumerate(ptrs):
+            st = enc(src, w, h, w * 4, ctypes.byref(opts[i % len(opts)]), dst)
             if st != 0:
                 raise native.AstcError(st, lib.astc_last_error().decode())
+        for ss in side:
+            stream.wait_stream(ss)
         ev[s][1].record(stream)
     torch.cuda.synchronize()
     launches = native.kernel_launch_count() - l0
@@ -696,10 +717,11 @@ def run_ours(args) -> None:
         return
 
     # warm-up (untimed) + a short sustained burn so clocks settle
-    _time_launches(torch, native, texs, outs, spec_run, max(3, args.warmup))
+    nstreams = max(1, args.streams)
+    _time_launches(torch, native, texs, outs, spec_run, max(3, args.warmup), nstreams)
     t_end = time.perf_counter() + 0.5
     while time.perf_counter() < t_end:
-        _time_launches(torch, native, texs, outs, spec_run, 2)
+        _time_launches(torch, native, texs, outs, spec_run, 2, nstreams)
 
     clocks = ClockSampler(local)
     if world > 1:
@@ -707,10 +729,16 @@ def run_ours(args) -> None:
     torch.cuda.synchronize()
     clocks.start()
     t0 = time.perf_counter()
-    per, per_step, launches = _time_launches(torch, native, texs, outs, spec_run, args.steps)
+    per, per_step, launches = _time_launches(torch, native, texs, outs, spec_run, args.steps, nstreams)
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
     clk = clocks.stop()
+    # the same step with every launch on one stream (each launch's partial
+    # last wave then runs with the GPU otherwise idle)
+    if nstreams > 1:
+        per1, per_step1, _ = _time_launches(torch, native, texs, outs, spec_run, args.steps, 1)
+    else:
+        per1, per_step1 = per, per_step
     dev_s = sum(per_step) / 1e3
     if world > 1:
         t = torch.tensor([dev_s], device="cuda")
@@ -812,6 +840,11 @@ def run_ours(args) -> None:
                 xper, xsteps, _ = _time_launches(torch, native, xt, xo, run, 10)
                 entry[label] = {"value": xh * xw * reps * 10 / (sum(xsteps) / 1e3) / 1e6,
                                 "unit": "Mtexels/s", "mean_launch_us": xper * 1e3}
+                if nstreams > 1:
+                    # the same launches spread over the headline's streams
+                    _time_launches(torch, native, xt, xo, run, 3, nstreams)
+                    _, xsteps, _ = _time_launches(torch, native, xt, xo, run, 10, nstreams)
+                    entry[label][f"value_{nstreams}_streams"] = xh * xw * reps * 10 / (sum(xsteps) / 1e3) / 1e6
             entry["speedup_half2_vs_fp32"] = entry["half2"]["value"] / entry["fp32"]["value"]
             extra[name] = entry
             del xt, xo
@@ -833,6 +866,11 @@ def run_ours(args) -> None:
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic",
         "config": _config(args.workload, img, spec, args.precision, world),
+        "launch": (f"one astc_encode_gpu_pitched call per texture, round-robin over {nstreams} CUDA streams "
+                   "forked from and joined to the timed stream each step" if nstreams > 1 else
+                   "one astc_encode_gpu_pitched call per texture, one after another on the timed stream"),
+        "one_stream": {"value": world * texels_step * args.steps / (sum(per_step1) / 1e3) / 1e6,
+                       "unit": "Mtexels/s", "mean_launch_us": per1 * 1e3},
         "kernel_variant": {"store": {0: "registers", 1: "shared", 2: "registers_capped"}.get(tuned.store, tuned.store),
                            "threads_per_cta": tuned.threads, "autotune_best_us": tuned.best_us},
         "e2e": {"value": e2e_value, "unit": "Mtexels/s",
@@ -845,6 +883,9 @@ def run_ours(args) -> None:
         "roofline": {"bound": "fp32_issue", "kernel": kernel, "achieved": achieved_tf, "peak": fp32_peak,
                      "unit": "TFLOP/s", "frac": achieved_tf / fp32_peak, "flops_per_launch": flops,
                      "mean_launch_us": mean_launch_s * 1e6,
+                     "launch_time": ("step time / launches over the timed region (launches on "
+                                     f"{nstreams} streams overlap where one texture's last wave ends)"
+                                     if nstreams > 1 else "step time / launches over the timed region"),
                      "peak_source": "max of an FP32 FMA microbenchmark (libastc_fp32_peak.so) and an "
                                     "8192^3 SGEMM (TF32 off), both measured in this run",
                      "peak_fma_microbenchmark": fma_peak, "peak_sgemm": sgemm_peak,
