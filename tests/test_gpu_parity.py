@@ -208,6 +208,39 @@ def test_back_to_back_launches_keep_stream_order(native, precision, axis, qualit
     assert np.array_equal(chained.cpu().numpy(), again)
 
 
+@pytest.mark.parametrize("precision", [0, 1])
+def test_launches_spread_over_streams(native, oracle, precision):
+    """Independent textures encoded round-robin on several streams (forked from
+    and joined to one stream, as bench.py's headline step does), so that one
+    stream's kernel runs in the SM slots the other's last partial wave leaves
+    idle: every texture's blocks equal the same texture encoded alone (and the
+    FP32 oracle's, for FP32), over five steps into the same outputs."""
+    import torch
+    h, w = 1030, 1201                              # ragged 6x6 edges, partial last waves
+    opts = dict(block_dim=6, has_alpha=True, srgb=True, border=1, precision=precision)
+    imgs = [_texture(h, w, seed=700 + i) for i in range(6)]
+    want = [native.encode(im, **opts) for im in imgs]
+    if precision == 0:
+        assert np.array_equal(want[0], oracle.encode(imgs[0], block_dim=6, has_alpha=True, srgb=True, border=1))
+    main = torch.cuda.Stream()
+    side = [torch.cuda.Stream() for _ in range(2)]
+    streams = [main] + side
+    srcs = [torch.from_numpy(im).cuda() for im in imgs]
+    outs = [torch.zeros(want[0].shape, dtype=torch.uint8, device="cuda") for _ in imgs]
+    torch.cuda.synchronize()
+    for _ in range(5):
+        for s in side:
+            s.wait_stream(main)
+        for i, (src, out) in enumerate(zip(srcs, outs)):
+            s = streams[i % len(streams)]
+            native.encode_device(src.data_ptr(), w, h, out.data_ptr(), stream=s.cuda_stream, **opts)
+        for s in side:
+            main.wait_stream(s)
+    main.synchronize()
+    for i in range(len(imgs)):
+        assert np.array_equal(outs[i].cpu().numpy(), want[i]), i
+
+
 @pytest.mark.parametrize("quality", [0, 1])
 def test_encode_captured_in_a_cuda_graph(native, quality):
     """A device-memory encode captured into a CUDA graph (as an engine's frame
