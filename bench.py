@@ -410,6 +410,11 @@ def _psnr_blocks(native, blocks: np.ndarray, tex: np.ndarray, spec: dict) -> flo
     return native.psnr_from_sse(float(s[:ch].sum()), h * w * ch)
 
 
+def _rmse(psnr_db: float, peak: float = 255.0) -> float:
+    """RMSE (in 8-bit code units, the PSNR's peak of 255) of a PSNR."""
+    return peak * 10.0 ** (-psnr_db / 20.0)
+
+
 def _psnr_space(spec: dict) -> str:
     if spec["is_normal"]:
         return "rebuilt unit normals (x, y from R, G; z = sqrt(1 - x^2 - y^2)), 3 components x 127.5"
@@ -458,6 +463,7 @@ def _bench_search(torch, native, headline: str, texs, outs, spec: dict) -> dict:
             entry[label] = {"value": sh * sw * len(st) * 5 / (sum(steps) / 1e3) / 1e6, "unit": "Mtexels/s",
                             "mean_launch_us": per * 1e3,
                             "psnr_db": _psnr_blocks(native, so[0].cpu().numpy(), tex0, sspec)}
+            entry[label]["rmse"] = _rmse(entry[label]["psnr_db"])
         entry["search_gain_db"] = entry["search"]["psnr_db"] - entry["fast"]["psnr_db"]
         entry["thorough_gain_db"] = entry["thorough"]["psnr_db"] - entry["fast"]["psnr_db"]
         entry["partitions_gain_db"] = entry["partitions"]["psnr_db"] - entry["fast"]["psnr_db"]
@@ -532,7 +538,7 @@ def _bench_batched(torch, native, oracle, count: int, reps: int = 5) -> dict:
     fp32_blocks = [o.cpu().numpy() for *_, o, _ in jobs]
     h2_ms, h2_launches = timed(lambda: batched_pass(1))
     # quality per texture (level 0): PSNR of FP32 / HALF2 against the FP64 oracle
-    gaps, same = [], []
+    gaps, same, rmses = [], [], []
     k = 0
     for t in texs:
         w, h, lvl = t["levels"][0]
@@ -544,8 +550,9 @@ def _bench_batched(torch, native, oracle, count: int, reps: int = 5) -> dict:
 
         def psnr(bl):
             return _psnr_blocks(native, bl, img, opts)
-        p64 = psnr(f64)
-        gaps.append((p64 - psnr(f32), p64 - psnr(h2)))
+        p64, p32, p16 = psnr(f64), psnr(f32), psnr(h2)
+        gaps.append((p64 - p32, p64 - p16))
+        rmses.append((_rmse(p64), _rmse(p32), _rmse(p16)))
         same.append(float(np.all(h2 == f32, axis=1).mean()))
         k += len(t["levels"])
     batch.close()
@@ -565,6 +572,11 @@ def _bench_batched(torch, native, oracle, count: int, reps: int = 5) -> dict:
         "psnr_gap_to_fp64_db": {"fp32_mean": float(g32.mean()), "fp32_max": float(g32.max()),
                                 "half2_mean": float(g16.mean()), "half2_max": float(g16.max()),
                                 "half2_textures_within_0.05dB": int((g16 <= 0.05).sum())},
+        "rmse_mean": {"fp64_oracle": float(np.mean([r[0] for r in rmses])),
+                      "fp32": float(np.mean([r[1] for r in rmses])),
+                      "half2": float(np.mean([r[2] for r in rmses])),
+                      "half2_max_vs_fp64_pct": float(max(100.0 * (r[2] / r[0] - 1.0) for r in rmses)),
+                      "unit": "8-bit codes, in each texture's PSNR space"},
         "half2_identical_blocks_vs_fp32_mean": float(np.mean(same)),
         "generation_s": gen_s,
     }
@@ -817,6 +829,8 @@ def run_ours(args) -> None:
                "psnr_db": psnr(got), "psnr_fp32_oracle_db": psnr(ora), "psnr_fp64_oracle_db": psnr(f64),
                "psnr_space": _psnr_space(spec) + ", spec LDR decode on the GPU"}
     quality["psnr_gap_to_fp64_db"] = quality["psnr_fp64_oracle_db"] - quality["psnr_db"]
+    quality["rmse"] = {"ours": _rmse(quality["psnr_db"]), "fp32_oracle": _rmse(quality["psnr_fp32_oracle_db"]),
+                       "fp64_oracle": _rmse(quality["psnr_fp64_oracle_db"]), "unit": "8-bit codes"}
 
     # plain (one launch per texture) FP32 and HALF2 on the three workloads
     extra = {}
