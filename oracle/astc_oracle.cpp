@@ -1,7 +1,7 @@
 /*
  * astc_oracle.cpp -- CPU oracle for the ASTC block encoder.
  *
- * TEST INFRASTRUCTURE ONLY: the checker the CUDA encoder is compared with.
+ * TEST INFRASTRUCTURE ONLY: the oracle the CUDA encoder is compared with.
  * The product library never links or loads this file.
  *
  * What it restates (niepp/astc_encoder, file:line):

@@ -1,7 +1,7 @@
 /*
  * astc_oracle.h -- CPU oracle for the ASTC block encoder.
  *
- * TEST INFRASTRUCTURE ONLY.  This library is the checker that the CUDA
+ * TEST INFRASTRUCTURE ONLY.  This library is the oracle that the CUDA
  * encoder is compared against; it is never linked into, loaded by or called
  * from the product library (libastc_gb300.so) or the CLI.  Only the test
  * suite, the smoke check and the CPU-baseline leg of the benchmark use it.

@@ -2,7 +2,8 @@
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, by ``__graft_entry__.smoke()``
 and by the CPU-baseline / reference legs of ``bench.py``, always as the
-checker or the timed CPU restatement -- never as the product path.
+reference the GPU results are compared with or as the timed CPU restatement --
+never as the product path.
 """
 from __future__ import annotations
 
