@@ -215,7 +215,7 @@ class DeviceCaps(ctypes.Structure):
     """``astc_device_caps`` of include/astc_gb300.h."""
     _fields_ = [(n, ctypes.c_int) for n in ("sm_count", "l2_bytes", "unified_addressing", "can_map_host_memory",
                                             "pageable_memory_access", "pageable_uses_host_page_tables",
-                                            "zero_copy")]
+                                            "zero_copy", "pageable_in_place")]
 
 
 def device_caps() -> dict:

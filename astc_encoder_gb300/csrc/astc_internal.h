@@ -114,4 +114,13 @@ void count_launches(uint64_t n);
 // Device view of a pinned, device-mapped host buffer (zero-copy), else NULL.
 const void* pinned_device_view(const void* host);
 
+// The address at which the current device reaches a host buffer: the device
+// view of pinned memory (pinned = true), or the pointer itself for pageable
+// memory on a device that reads the host's page tables; ptr NULL otherwise.
+struct HostView {
+    const void* ptr = nullptr;
+    bool pinned = false;
+};
+HostView host_device_view(const void* host);
+
 }  // namespace astc

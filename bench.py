@@ -18,6 +18,8 @@ over --streams CUDA streams (default 2) forked from torch's current stream.
                 ring (copy engine, 32 MiB slots overlapped with the encode) and
                 the kernels write its blocks back in place over NVLink-C2C, all
                 inside the timed region, one stream synchronize per step.
+                `e2e_pageable` repeats it with ordinary pageable (numpy)
+                buffers and synchronous calls, the reference's own usage.
 * roofline   -- the dominant kernel's algorithmic bytes (4 B/texel read +
                 16 B/block written) per launch over its mean launch time,
                 against the measured HBM copy bandwidth; roofline_fp32 gives
@@ -790,6 +792,33 @@ def run_ours(args) -> None:
         e2e_s = float(t.item())
     e2e_value = world * texels_step * e2e_steps / e2e_s / 1e6
 
+    # the same entry point with ordinary pageable buffers (numpy arrays) and
+    # no stream -- the reference's own usage: a malloc'd image in, a malloc'd
+    # block buffer out, each call returning with the blocks in place
+    page_in = [np.ascontiguousarray(t.cpu().numpy()) for t in texs]
+    page_out = [np.empty((nblocks, 16), np.uint8) for _ in texs]
+    opts_page = native.make_opts(memory=native.Memory.HOST, **spec_run)
+
+    def e2e_pageable_step():
+        for pi, po in zip(page_in, page_out):
+            st = lib.astc_encode_gpu(pi.ctypes.data, w, h, ctypes.byref(opts_page), po.ctypes.data)
+            if st != 0:
+                raise native.AstcError(st, lib.astc_last_error().decode())
+
+    for _ in range(max(3, args.warmup)):
+        e2e_pageable_step()
+    t1 = time.perf_counter()
+    for _ in range(e2e_steps):
+        e2e_pageable_step()
+    e2e_page_s = time.perf_counter() - t1
+    if world > 1:
+        t = torch.tensor([e2e_page_s], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_page_s = float(t.item())
+    e2e_page_value = world * texels_step * e2e_steps / e2e_page_s / 1e6
+    page_caps = native.device_caps()
+    del page_in, page_out
+
     if rank != 0:
         if world > 1:
             torch.distributed.barrier()
@@ -891,6 +920,11 @@ def run_ours(args) -> None:
                 "h2d_bytes_per_step": texels_step * 4, "d2h_bytes_per_step": nblocks * 16 * len(texs),
                 "entry_point": "astc_encode_gpu (ASTC_MEMORY_HOST, pinned buffers: inputs through the upload ring, blocks written in place over NVLink-C2C; one stream sync per step)",
                 "steps": e2e_steps},
+        "e2e_pageable": {"value": e2e_page_value, "unit": "Mtexels/s",
+                         "h2d_bytes_per_step": texels_step * 4, "d2h_bytes_per_step": nblocks * 16 * len(texs),
+                         "entry_point": "astc_encode_gpu (ASTC_MEMORY_HOST, pageable numpy buffers, no stream: "
+                                        "each call returns with its blocks in place)",
+                         "pageable_in_place": bool(page_caps["pageable_in_place"]), "steps": e2e_steps},
         "gpu_launches": int(launches),
         # the binding bound: FP32/INT issue (the per-block algebra is not a
         # contraction, so no tensor-core roof applies); HBM is the secondary roof

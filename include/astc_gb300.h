@@ -163,9 +163,11 @@ size_t astc_encoded_size(int width, int height, int block_dim);
  * Replaces encode_astc (astc_encode.h:87) + read_gpu (astc_save.h:34).
  * `out` must hold astc_encoded_size(width, height, opts->block_dim) bytes.
  * Host memory: pinned buffers are accessed in place by the kernel
- * (zero-copy), others are staged; the call returns when `out` is written,
- * except when both buffers are pinned and opts->stream is set -- then it is
- * asynchronous on that stream like a device-memory call. */
+ * (zero-copy), and so are pageable buffers on a device that reads the host's
+ * page tables (astc_device_caps.pageable_in_place: Grace systems over
+ * NVLink-C2C); other buffers are staged.  The call returns when `out` is
+ * written, except when both buffers are pinned and opts->stream is set --
+ * then it is asynchronous on that stream like a device-memory call. */
 astc_status astc_encode_gpu(const uint8_t* rgba8, int width, int height,
                             const astc_opts* opts, uint8_t* out);
 
@@ -393,15 +395,18 @@ astc_status astc_sse_gpu_noalloc(const uint8_t* a, const uint8_t* b, size_t texe
  * the reference.)  With `zero_copy` set, host-memory calls whose buffers are
  * pinned (page-locked and device-mapped) let the kernels read texels and
  * write blocks directly through the host link instead of staging them in
- * device memory; other host buffers are staged. */
+ * device memory; with `pageable_in_place` set, ordinary pageable buffers
+ * (malloc, new, numpy) are accessed the same way; other host buffers are
+ * staged. */
 typedef struct astc_device_caps {
     int sm_count;
     int l2_bytes;
     int unified_addressing;          /* pinned host memory has a device view    */
     int can_map_host_memory;
-    int pageable_memory_access;      /* reported only; pageable buffers are staged */
+    int pageable_memory_access;
     int pageable_uses_host_page_tables;
     int zero_copy;                   /* the library uses zero-copy for pinned buffers */
+    int pageable_in_place;           /* ... and accesses pageable buffers in place */
 } astc_device_caps;
 astc_status astc_get_device_caps(astc_device_caps* caps);
 

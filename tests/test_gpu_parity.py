@@ -455,6 +455,69 @@ def test_host_memory_zero_copy_paths(native, oracle):
         assert st == 0 and np.array_equal(pin_out.numpy(), want)
 
 
+def test_host_memory_pageable_in_place(native, oracle):
+    """On a device that reads the host's page tables (Grace over NVLink-C2C)
+    ordinary pageable buffers are read and written in place instead of being
+    staged.  Blocks equal the oracle's (FP32) or the device-memory encode's
+    (HALF2) for a small input, ring-sized inputs (4 MiB and more), a
+    row-pitched input, an output the device writes before the host ever
+    touches it, an output at an odd address (staged) and mixes with pinned
+    buffers; with a stream the call still returns only once the blocks are in
+    the pageable output."""
+    import torch
+    caps = native.device_caps()
+    if caps["pageable_memory_access"] and caps["pageable_uses_host_page_tables"]:
+        assert caps["pageable_in_place"] == 1
+    lib = native.load_library()
+    stream = torch.cuda.Stream()
+    # 131x77: read in place; 2049x2048 (16 MiB): one ring band; 4093x4096 6x6
+    # (64 MiB): two ring bands of whole block rows, the last ragged
+    cases = [((131, 77), dict(block_dim=4, has_alpha=True)),
+             ((2049, 2048), dict(block_dim=6, has_alpha=True, srgb=True, border=1)),
+             ((4093, 4096), dict(block_dim=6, has_alpha=True, srgb=True, border=1)),
+             ((1030, 1201), dict(block_dim=4, has_alpha=False, border=1)),
+             ((1030, 1201), dict(block_dim=6, has_alpha=True, srgb=True, precision=1))]
+    for (h, w), opts in cases:
+        img = _texture(h, w, seed=h * 7 + w)
+        d_in = torch.from_numpy(img).cuda()
+        d_out = torch.empty(((w + opts["block_dim"] - 1) // opts["block_dim"]) *
+                            ((h + opts["block_dim"] - 1) // opts["block_dim"]), 16, dtype=torch.uint8, device="cuda")
+        torch.cuda.synchronize()
+        native.encode_device(d_in.data_ptr(), w, h, d_out.data_ptr(), **opts)
+        want = d_out.cpu().numpy()
+        if opts.get("precision", 0) == 0 and h * w < 8 << 20:
+            assert np.array_equal(want, oracle.encode(img, **opts)), opts
+        o_sync = native.make_opts(memory=native.Memory.HOST, **opts)
+        o_async = native.make_opts(memory=native.Memory.HOST, stream=stream.cuda_stream, **opts)
+        # pageable in, pageable out never touched on the host
+        out = np.empty_like(want)
+        assert lib.astc_encode_gpu(img.ctypes.data, w, h, ctypes.byref(o_sync), out.ctypes.data) == 0
+        assert np.array_equal(out, want), opts
+        # with a stream: synchronous all the same for pageable buffers
+        out = np.zeros_like(want)
+        assert lib.astc_encode_gpu(img.ctypes.data, w, h, ctypes.byref(o_async), out.ctypes.data) == 0
+        assert np.array_equal(out, want), opts
+        # a row-pitched view into a wider pageable image
+        wide = np.zeros((h, w + 16, 4), np.uint8)
+        wide[:, :w] = img
+        out = np.zeros_like(want)
+        assert lib.astc_encode_gpu_pitched(wide.ctypes.data, w, h, (w + 16) * 4, ctypes.byref(o_sync),
+                                           out.ctypes.data) == 0
+        assert np.array_equal(out, want), opts
+        # an output at an odd address (staged) from a pageable input
+        raw = np.zeros(want.size + 1, np.uint8)
+        assert lib.astc_encode_gpu(img.ctypes.data, w, h, ctypes.byref(o_sync), raw.ctypes.data + 1) == 0
+        assert np.array_equal(raw[1:].reshape(want.shape), want), opts
+        # pinned in / pageable out and pageable in / pinned out
+        pin_in = torch.from_numpy(img).pin_memory()
+        pin_out = torch.zeros(want.shape, dtype=torch.uint8).pin_memory()
+        out = np.zeros_like(want)
+        assert lib.astc_encode_gpu(pin_in.data_ptr(), w, h, ctypes.byref(o_async), out.ctypes.data) == 0
+        assert np.array_equal(out, want), opts
+        assert lib.astc_encode_gpu(img.ctypes.data, w, h, ctypes.byref(o_async), pin_out.data_ptr()) == 0
+        assert np.array_equal(pin_out.numpy(), want), opts
+
+
 def test_host_memory_upload_ring(native, oracle):
     """Pinned inputs of 4 MiB and more are uploaded through a ring of device
     slots (copy engine, events; bands of whole block rows above a slot) while
