@@ -167,7 +167,9 @@ size_t astc_encoded_size(int width, int height, int block_dim);
  * page tables (astc_device_caps.pageable_in_place: Grace systems over
  * NVLink-C2C); other buffers are staged.  The call returns when `out` is
  * written, except when both buffers are pinned and opts->stream is set --
- * then it is asynchronous on that stream like a device-memory call. */
+ * then it is asynchronous on that stream like a device-memory call.  A host
+ * buffer the device accesses in place must hold its whole extent, writable
+ * for `out`: the device faults where a host copy would have. */
 astc_status astc_encode_gpu(const uint8_t* rgba8, int width, int height,
                             const astc_opts* opts, uint8_t* out);
 
