@@ -470,10 +470,12 @@ def test_host_memory_pageable_in_place(native, oracle):
         assert caps["pageable_in_place"] == 1
     lib = native.load_library()
     stream = torch.cuda.Stream()
-    # 131x77: read in place; 2049x2048 (16 MiB): one ring band; 4093x4096 6x6
+    # 131x77: read in place; 2049x2048 (16 MiB): one ring band; 2049x2051:
+    # rows of 8,204 bytes, copied into the ring in 4-byte words; 4093x4096 6x6
     # (64 MiB): two ring bands of whole block rows, the last ragged
     cases = [((131, 77), dict(block_dim=4, has_alpha=True)),
              ((2049, 2048), dict(block_dim=6, has_alpha=True, srgb=True, border=1)),
+             ((2049, 2051), dict(block_dim=4, has_alpha=True)),
              ((4093, 4096), dict(block_dim=6, has_alpha=True, srgb=True, border=1)),
              ((1030, 1201), dict(block_dim=4, has_alpha=False, border=1)),
              ((1030, 1201), dict(block_dim=6, has_alpha=True, srgb=True, precision=1))]
