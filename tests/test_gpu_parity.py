@@ -520,6 +520,41 @@ def test_host_memory_pageable_in_place(native, oracle):
         assert np.array_equal(pin_out.numpy(), want), opts
 
 
+def test_host_memory_pageable_staged(native):
+    """The staging path that pageable buffers take on devices without access
+    to the host's page tables (forced here with ASTC_GB300_PAGEABLE_IN_PLACE=0,
+    in a child process since the switch is read once): small and ring-sized
+    inputs, a pitched input, equal to the oracle's blocks."""
+    import subprocess
+    import sys
+    code = r'''
+import numpy as np, sys
+sys.path.insert(0, ROOT)
+import astc_encoder_gb300 as native
+from oracle import oracle
+assert native.device_caps()["pageable_in_place"] == 0
+rng = np.random.default_rng(4)
+for (h, w), opts in (((131, 77), dict(block_dim=4, has_alpha=True)),
+                     ((1031, 2048), dict(block_dim=6, has_alpha=True, srgb=True, border=1))):
+    img = rng.integers(0, 256, (h, w, 4), dtype=np.uint8)
+    img[h // 3:, : w // 2] = (30, 90, 200, 255)
+    want = oracle.encode(img, **opts)
+    assert np.array_equal(native.encode(img, **opts), want), (h, w)
+    wide = np.zeros((h, w + 8, 4), np.uint8)
+    wide[:, :w] = img
+    out = np.zeros_like(want)
+    o = native.make_opts(memory=native.Memory.HOST, **opts)
+    import ctypes
+    st = native.load_library().astc_encode_gpu_pitched(wide.ctypes.data, w, h, (w + 8) * 4, ctypes.byref(o),
+                                                        out.ctypes.data)
+    assert st == 0 and np.array_equal(out, want), (h, w)
+print("staged ok")
+'''.replace("ROOT", repr(os.path.dirname(os.path.dirname(os.path.abspath(__file__)))))
+    env = dict(os.environ, ASTC_GB300_PAGEABLE_IN_PLACE="0")
+    r = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0 and "staged ok" in r.stdout, r.stdout + r.stderr
+
+
 def test_host_memory_upload_ring(native, oracle):
     """Pinned inputs of 4 MiB and more are uploaded through a ring of device
     slots (copy engine, events; bands of whole block rows above a slot) while
