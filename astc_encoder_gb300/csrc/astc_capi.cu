@@ -257,6 +257,10 @@ astc_status check_device_span(const void* p, size_t bytes, const char* what, boo
         cudaGetLastError();
         return set_error(ASTC_ERR_INVALID_ARG, std::string(what) + " is not a CUDA pointer");
     }
+    // pageable host memory that the device reads through the host's page
+    // tables: accessed in place like pinned memory (it has no allocation
+    // range to check the extent against)
+    if (allow_host_view && a.type == cudaMemoryTypeUnregistered && pageable_in_place_available()) return ASTC_OK;
     const bool host_view = allow_host_view && a.type == cudaMemoryTypeHost && a.devicePointer == p;
     if (a.type != cudaMemoryTypeDevice && a.type != cudaMemoryTypeManaged && !host_view)
         return set_error(ASTC_ERR_INVALID_ARG,
@@ -321,6 +325,8 @@ bool pageable_host_access() {
     return c == 2;
 }
 
+bool pageable_in_place_available() { return pageable_in_place_enabled() && pageable_host_access(); }
+
 HostView host_device_view(const void* host) {
     HostView v;
     if (!host) return v;
@@ -332,7 +338,7 @@ HostView host_device_view(const void* host) {
     if (a.type == cudaMemoryTypeHost && a.devicePointer && zero_copy_enabled()) {
         v.ptr = a.devicePointer;
         v.pinned = true;
-    } else if (a.type == cudaMemoryTypeUnregistered && pageable_in_place_enabled() && pageable_host_access()) {
+    } else if (a.type == cudaMemoryTypeUnregistered && pageable_in_place_available()) {
         v.ptr = host;                                  // the same virtual address on the device
     }
     return v;

@@ -122,5 +122,7 @@ struct HostView {
     bool pinned = false;
 };
 HostView host_device_view(const void* host);
+// Whether pageable host memory is accessed in place on the current device.
+bool pageable_in_place_available();
 
 }  // namespace astc

@@ -157,11 +157,12 @@ cudaError_t launch_slot(astc_server* s, Slot& slot) {
         uint8_t* d_in = s->d_pool + q->off;
         uint8_t* d_out = d_in + round_up(q->in_bytes);
         const size_t row = (size_t)q->r.width * 4;
-        // pinned requests are read and written in place through their device
-        // views (zero-copy); the pool space stays reserved, so admission by
-        // memory behaves the same for every request
-        const void* in_view = pinned_device_view(q->r.rgba8);
-        void* out_view = const_cast<void*>(pinned_device_view(q->r.out));
+        // requests in host memory the device reaches in place (pinned, or
+        // pageable where the device reads the host's page tables) are read and
+        // written there (zero-copy); the pool space stays reserved, so
+        // admission by memory behaves the same for every request
+        const void* in_view = host_device_view(q->r.rgba8).ptr;
+        void* out_view = const_cast<void*>(host_device_view(q->r.out).ptr);
         q->out_direct = out_view && reinterpret_cast<uintptr_t>(out_view) % 16 == 0;
         astc_batch_item it;
         if (in_view && reinterpret_cast<uintptr_t>(in_view) % 4 == 0 && q->pitch % 4 == 0) {

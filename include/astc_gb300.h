@@ -187,11 +187,16 @@ astc_status astc_encode_gpu_pitched(const uint8_t* rgba8, int width, int height,
  * a device work queue.  Every texture's blocks are identical to what
  * astc_encode_gpu returns for it with the same precision. */
 typedef struct astc_batch_item {
-    const uint8_t* rgba8;   /* device memory, 4-byte aligned                 */
+    const uint8_t* rgba8;   /* device memory, 4-byte aligned (or host memory
+                               the device reaches in place: pinned, or
+                               pageable where astc_device_caps.
+                               pageable_in_place; the caller keeps it alive
+                               until the stream has run the batch)          */
     size_t row_pitch;       /* bytes between rows; 0 = 4 * width             */
     int width, height;
     int block_dim, has_alpha, is_normal, srgb, border;   /* as astc_opts     */
-    uint8_t* out;           /* device memory, 16-byte aligned, 16 B / block  */
+    uint8_t* out;           /* the same kinds of memory, 16-byte aligned,
+                               16 B / block                                  */
 } astc_batch_item;
 
 typedef struct astc_batch astc_batch;   /* opaque; owns descriptor buffers,
@@ -242,7 +247,9 @@ typedef struct astc_server_config {
 } astc_server_config;
 
 typedef struct astc_request {
-    const uint8_t* rgba8;   /* host memory; pinned memory copies asynchronously */
+    const uint8_t* rgba8;   /* host memory, read in place when the device reaches
+                               it (pinned, or pageable where astc_device_caps.
+                               pageable_in_place), else staged through the pool */
     size_t row_pitch;       /* 0 = 4 * width                                     */
     int width, height;
     int block_dim, has_alpha, is_normal, srgb, border;

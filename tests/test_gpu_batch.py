@@ -111,6 +111,31 @@ def test_batch_graph_reuse_and_many_mips(native, oracle):
                 assert np.array_equal(o.cpu().numpy(), oracle.encode(img, **opts))
 
 
+def test_batch_pageable_items(native, oracle):
+    """Items in ordinary pageable host memory: encoded in place where the device
+    reads the host's page tables (blocks equal to the oracle's), rejected
+    elsewhere."""
+    import torch
+    rng = np.random.default_rng(12)
+    imgs = [rng.integers(0, 256, (h, w, 4), dtype=np.uint8) for h, w in ((37, 61), (128, 96), (5, 300))]
+    opts = dict(block_dim=6, has_alpha=True, srgb=True, border=1)
+    outs = [np.zeros((((w + 5) // 6) * ((h + 5) // 6), 16), np.uint8) for h, w in (i.shape[:2] for i in imgs)]
+    items = [dict(rgba8=im.ctypes.data, width=im.shape[1], height=im.shape[0], out=o.ctypes.data, **opts)
+             for im, o in zip(imgs, outs)]
+    stream = torch.cuda.Stream()
+    with native.Batch(8, 4096) as b:
+        if not native.device_caps()["pageable_in_place"]:
+            with pytest.raises(native.AstcError):
+                b.encode(items, stream=stream.cuda_stream)
+            return
+        for prec in (0, 1):
+            b.encode(items, precision=prec, stream=stream.cuda_stream)
+            stream.synchronize()
+            for im, o in zip(imgs, outs):
+                assert np.array_equal(o, native.encode(im, precision=prec, **opts)), prec
+        assert np.array_equal(outs[0], oracle.encode(imgs[0], **opts))
+
+
 def test_batch_rejects_over_capacity(native):
     import torch
     dev = torch.zeros((8, 8, 4), dtype=torch.uint8, device="cuda")
