@@ -133,7 +133,8 @@ def test_batch_pageable_items(native, oracle):
             stream.synchronize()
             for im, o in zip(imgs, outs):
                 assert np.array_equal(o, native.encode(im, precision=prec, **opts)), prec
-        assert np.array_equal(outs[0], oracle.encode(imgs[0], **opts))
+            if prec == 0:
+                assert np.array_equal(outs[0], oracle.encode(imgs[0], **opts))
 
 
 def test_batch_rejects_over_capacity(native):
