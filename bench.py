@@ -584,14 +584,16 @@ def _bench_batched(torch, native, oracle, count: int, reps: int = 5) -> dict:
     }
 
 
-def _bench_serving(torch, native, rates, seconds: float = 2.0, max_requests: int = 2000) -> dict:
+def _bench_serving(torch, native, rates, seconds: float = 2.0, max_requests: int = 2000,
+                   host: str = "pinned") -> dict:
     """Open-loop serving: Poisson arrivals at each rate, single-texture requests.
 
     Request side lengths are log-uniform in [128, 2048] (square), formats mixed
     60% 4x4 RGB / 25% 6x6 RGBA sRGB / 15% 4x4 normal, content cropped from
-    2048x2048 synthetic textures held in pinned host memory; 2 GiB device
-    staging pool with admission by memory.  Batched = continuous batching
-    through astc_batch; per-request = one plain launch per request.
+    2048x2048 synthetic textures held in pinned host memory (`host` =
+    "pageable": ordinary numpy buffers); 2 GiB device staging pool with
+    admission by memory.  Batched = continuous batching through astc_batch;
+    per-request = one plain launch per request.
     """
     from astc_encoder_gb300 import synth
     bases = {
@@ -599,7 +601,10 @@ def _bench_serving(torch, native, rates, seconds: float = 2.0, max_requests: int
         "6x6_rgba_srgb": (synth.rgba_cutout(2048, 2048), dict(block_dim=6, has_alpha=True, srgb=True, border=1)),
         "4x4_normal": (synth.normal_map(2048, 2048), dict(block_dim=4, is_normal=True)),
     }
-    pinned = {k: torch.from_numpy(v[0]).pin_memory() for k, v in bases.items()}
+    if host == "pinned":
+        src_tex = {k: torch.from_numpy(v[0]).pin_memory() for k, v in bases.items()}
+    else:
+        src_tex = {k: torch.from_numpy(np.ascontiguousarray(v[0])) for k, v in bases.items()}
     names, probs = ["4x4_rgb", "6x6_rgba_srgb", "4x4_normal"], [0.60, 0.25, 0.15]
     rng = np.random.default_rng(synth.SEED_BASE + 4)
     n_max = max_requests
@@ -614,15 +619,20 @@ def _bench_serving(torch, native, rates, seconds: float = 2.0, max_requests: int
         nb = int(((int(s) + d - 1) // d) ** 2)
         reqs_meta.append((name, int(s), x0, y0, opts, out_bytes, nb))
         out_bytes += nb * 16
-    out = torch.empty(out_bytes, dtype=torch.uint8).pin_memory()
+    # pageable: zero-filled, so every page is resident before the device writes
+    # it (a service reuses its buffers; the device's first touch of a pageable
+    # page faults it in through the host and is slow)
+    out = torch.zeros(out_bytes, dtype=torch.uint8)
+    if host == "pinned":
+        out = out.pin_memory()
     requests = []
     for name, s, x0, y0, opts, off, nb in reqs_meta:
-        base = pinned[name]
+        base = src_tex[name]
         ptr = base.data_ptr() + (y0 * 2048 + x0) * 4
         requests.append(native.make_request(int(ptr), s, s, int(out.data_ptr() + off), row_pitch=2048 * 4, **opts))
     texels = np.array([m[1] * m[1] for m in reqs_meta], np.float64)
     result = {"pool_bytes": 2 << 30, "requests_max": n_max, "inflight_slots": 3, "max_batch": 256,
-              "rates": {}}
+              "host_buffers": host, "rates": {}}
     for mode, label in ((native.SERVE_BATCHED, "batched"), (native.SERVE_PER_REQUEST, "per_request")):
         with native.Server(pool_bytes=2 << 30, max_batch=256, inflight=3, mode=mode) as srv:
             srv.replay(requests[:64], np.zeros(64))                       # warm-up (graphs, pools)
@@ -896,6 +906,9 @@ def run_ours(args) -> None:
     batched = None if args.no_batched else _bench_batched(torch, native, oracle, args.batched_count)
     serving = None if args.no_serving else _bench_serving(
         torch, native, [int(r) for r in args.serving_rates.split(",") if r])
+    # the same requests in ordinary pageable buffers at three rates
+    serving_pageable = None if args.no_serving else _bench_serving(
+        torch, native, [20000, 50000, 100000], host="pageable")
     cpu = None if args.no_cpu else _cpu_baseline(img, spec)
 
     hbm = {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
@@ -943,6 +956,7 @@ def run_ours(args) -> None:
         "wall_s_timed_region": wall,
         "search_mode": search,
         "serving": serving,
+        "serving_pageable": serving_pageable,
         "batched_mixed": batched,
         "extra_workloads": extra,
         "quality": quality,

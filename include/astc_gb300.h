@@ -169,7 +169,9 @@ size_t astc_encoded_size(int width, int height, int block_dim);
  * written, except when both buffers are pinned and opts->stream is set --
  * then it is asynchronous on that stream like a device-memory call.  A host
  * buffer the device accesses in place must hold its whole extent, writable
- * for `out`: the device faults where a host copy would have. */
+ * for `out`: the device faults where a host copy would have.  Pages of a
+ * pageable `out` that the host has never touched are faulted in by the
+ * device's first write to them, which is slow (reuse or fill such buffers). */
 astc_status astc_encode_gpu(const uint8_t* rgba8, int width, int height,
                             const astc_opts* opts, uint8_t* out);
 
