@@ -344,16 +344,6 @@ HostView host_device_view(const void* host) {
     return v;
 }
 
-const void* pinned_device_view(const void* host) {
-    if (!host || !zero_copy_enabled()) return nullptr;
-    cudaPointerAttributes a;
-    if (cudaPointerGetAttributes(&a, host) != cudaSuccess) {
-        cudaGetLastError();
-        return nullptr;
-    }
-    if (a.type != cudaMemoryTypeHost || a.devicePointer == nullptr) return nullptr;
-    return a.devicePointer;
-}
 
 namespace {
 

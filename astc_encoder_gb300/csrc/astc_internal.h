@@ -111,9 +111,6 @@ astc_status check_device_span(const void* p, size_t bytes, const char* what, boo
 astc_status set_error(astc_status st, const std::string& msg);
 astc_status cuda_error(cudaError_t e, const char* what);
 void count_launches(uint64_t n);
-// Device view of a pinned, device-mapped host buffer (zero-copy), else NULL.
-const void* pinned_device_view(const void* host);
-
 // The address at which the current device reaches a host buffer: the device
 // view of pinned memory (pinned = true), or the pointer itself for pageable
 // memory on a device that reads the host's page tables; ptr NULL otherwise.
