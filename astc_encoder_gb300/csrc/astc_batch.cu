@@ -116,8 +116,8 @@ astc_encode_persistent(const BatchJob* __restrict__ jobs, const WorkItem* __rest
         if ((int)threadIdx.x < w.count) {
             const BatchJob j = jobs[w.job];
             const int b = w.first + threadIdx.x;
-            const int by = b / j.tex.nbx;
-            const int bx = b - by * j.tex.nbx;
+            int bx, by;
+            block_coords(j.tex, b, bx, by);
             uint32_t px[N];
             load_block_packed<DIM>(j.tex, bx, by, px);
             uint4 r;

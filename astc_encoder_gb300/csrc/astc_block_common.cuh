@@ -24,7 +24,30 @@ struct TextureView {
     int width, height, nbx;
     int vec_ok;           // 128-bit (4x4) / 64-bit (6x6) row loads allowed
     int clamp;            // ASTC_BORDER_CLAMP
+    uint32_t row_mul;     // block row of block b: (b * row_mul) >> row_shift
+    uint32_t row_shift;
 };
+
+// (row_mul, row_shift) for divisor d = nbx: with L = ceil(log2 d), m =
+// ceil(2^(31+L) / d) < 2^32 and floor(b * m / 2^(31+L)) = floor(b / d) for
+// every 0 <= b < 2^31 (Granlund and Montgomery, "Division by invariant
+// integers using multiplication", 1994: m = (2^(31+L) + e) / d with 0 <= e <
+// d adds less than b / 2^(31+L) < 1/d to b/d).  Textures hold at most 2^31
+// blocks, so every block index qualifies.
+inline void block_row_divisor(int d, uint32_t* mul, uint32_t* shift) {
+    int L = 0;
+    while ((1ull << L) < (unsigned long long)d) ++L;
+    const unsigned long long p = 1ull << (31 + L);
+    *mul = (uint32_t)((p + (unsigned long long)d - 1) / (unsigned long long)d);
+    *shift = (uint32_t)(31 + L);
+}
+
+// block (bx, by) of block index b < 2^31
+__device__ __forceinline__ void block_coords(const TextureView& t, long long b, int& bx, int& by) {
+    const uint32_t ub = (uint32_t)b;
+    by = (int)(((uint64_t)ub * t.row_mul) >> t.row_shift);
+    bx = (int)(ub - (uint32_t)by * (uint32_t)t.nbx);
+}
 
 // ---------------------------------------------------------------------------
 // exact FP32 primitives (the oracle's model)

@@ -65,8 +65,8 @@ astc_encode_blocks_fp32(const Launch p) {
     pdl_allow_next();
     const long long b = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= p.nblocks) return;
-    const int by = (int)(b / p.tex.nbx);
-    const int bx = (int)(b - (long long)by * p.tex.nbx);
+    int bx, by;
+    block_coords(p.tex, b, bx, by);
     uint32_t px[N];
     load_block_packed<DIM>(p.tex, bx, by, px);
     if constexpr (STORE == kStoreShared) {
@@ -193,6 +193,7 @@ TextureView make_view(const EncodeJob& j) {
     const size_t va = j.block_dim == 4 ? 16 : 8;
     t.vec_ok = (base % va == 0) && (j.pitch % va == 0);
     t.clamp = j.border == ASTC_BORDER_CLAMP;
+    block_row_divisor(t.nbx, &t.row_mul, &t.row_shift);
     return t;
 }
 

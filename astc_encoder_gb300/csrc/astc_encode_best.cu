@@ -100,8 +100,8 @@ __global__ void __launch_bounds__(128, 3) astc_encode_blocks_best(const BestLaun
     pdl_allow_next();
     const long long b = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= p.nblocks) return;
-    const int by = (int)(b / p.tex.nbx);
-    const int bx = (int)(b - (long long)by * p.tex.nbx);
+    int bx, by;
+    block_coords(p.tex, b, bx, by);
     uint32_t px[N];
     load_block_packed<DIM>(p.tex, bx, by, px);
     RegTexels<N> st;

@@ -110,8 +110,8 @@ __global__ void __launch_bounds__(256) astc_encode_blocks_coop(const LaunchCoop 
     // groups past the end encode the last block again and store nothing, so
     // every lane of the warp takes part in every shuffle
     const long long b = b_req < p.nblocks ? b_req : p.nblocks - 1;
-    const int by = (int)(b / p.tex.nbx);
-    const int bx = (int)(b - (long long)by * p.tex.nbx);
+    int bx, by;
+    block_coords(p.tex, b, bx, by);
 
     // fetch: lane l decodes rows l (and l + 4) into the tile
     {

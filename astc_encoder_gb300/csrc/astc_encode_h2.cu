@@ -34,8 +34,8 @@ __global__ void __launch_bounds__(kH2Threads) astc_encode_blocks_h2(const Launch
     pdl_allow_next();
     const long long b = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= p.nblocks) return;
-    const int by = (int)(b / p.tex.nbx);
-    const int bx = (int)(b - (long long)by * p.tex.nbx);
+    int bx, by;
+    block_coords(p.tex, b, bx, by);
     uint32_t px[N];
     load_block_packed<DIM>(p.tex, bx, by, px);
     p.out[b] = encode_block_h2<DIM, ALPHA, NORMAL, SRGB>(px, s_lin8, s_trits);
