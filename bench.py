@@ -635,8 +635,12 @@ def _bench_serving(torch, native, rates, seconds: float = 2.0, max_requests: int
               "host_buffers": host, "rates": {}}
     for mode, label in ((native.SERVE_BATCHED, "batched"), (native.SERVE_PER_REQUEST, "per_request")):
         with native.Server(pool_bytes=2 << 30, max_batch=256, inflight=3, mode=mode) as srv:
-            srv.replay(requests[:64], np.zeros(64))                       # warm-up (graphs, pools)
-            srv.replay(requests[:16], np.arange(16) * 2000.0)             # and single-request batches
+            # warm-up: graphs and pools, single-request batches, and one pass over
+            # every request's buffers (a device's first access to a pageable
+            # page goes through the host and is slow)
+            srv.replay(requests[:64], np.zeros(64))
+            srv.replay(requests[:16], np.arange(16) * 2000.0)
+            srv.replay(requests, np.zeros(len(requests)))
             for rate in rates:
                 n = int(min(n_max, max(64, rate * seconds)))
                 arrival = np.cumsum(np.random.default_rng(int(rate)).exponential(1e6 / rate, n))
