@@ -58,7 +58,7 @@ CLI_SOURCES = [
 ]
 HEADERS = ["astc_internal.h", "astc_tables.h", "astc_ise.h", "astc_block_common.cuh", "astc_pipeline_fp32.cuh",
            "astc_pipeline_h2.cuh", "astc_pipeline_search.cuh", "astc_pipeline_dual.cuh", "astc_pipeline_partition.cuh", "astc_pipeline_partition3.cuh", "astc_search_kernel.cuh",
-           "astc_partition_table.h", "astc_srgb_table.h", "image_load.h"]
+           "astc_partition_table.h", "astc_srgb_table.h", "astc_sse.cuh", "image_load.h"]
 
 
 def nvcc() -> str:

@@ -10,6 +10,7 @@
 #include <stdint.h>
 
 #include "astc_internal.h"
+#include "astc_sse.cuh"
 #include "astc_tables.h"
 
 namespace astc {
@@ -38,7 +39,7 @@ constexpr DecodeTables make_decode_tables() {
 
 __constant__ DecodeTables c_dec = make_decode_tables();
 
-constexpr int kDecodeThreads = 128;
+constexpr int kDecodeThreads = 256;
 
 struct Bits {
     uint32_t w[4];
@@ -389,19 +390,11 @@ astc_decode_ldr(const uint4* __restrict__ blocks, int width, int height, int bw,
 __global__ void __launch_bounds__(256)
 astc_sse_rgba(const uint32_t* __restrict__ a, const uint32_t* __restrict__ b, size_t n,
               unsigned long long* __restrict__ sse) {
-    unsigned long long acc[4] = {0, 0, 0, 0};
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-         i += (size_t)gridDim.x * blockDim.x) {
-        const uint32_t x = __ldg(a + i), y = __ldg(b + i);
-#pragma unroll
-        for (int c = 0; c < 4; ++c) {
-            const int d = (int)((x >> (8 * c)) & 0xFF) - (int)((y >> (8 * c)) & 0xFF);
-            acc[c] += (unsigned long long)(d * d);
-        }
-    }
+    SseAcc acc;
+    sse_range(a, b, 0, n, (size_t)blockIdx.x * blockDim.x + threadIdx.x, (size_t)gridDim.x * blockDim.x, acc);
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
-        unsigned long long v = acc[c];
+        unsigned long long v = acc.hi[c];
         for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, o);
         if ((threadIdx.x & 31) == 0 && v) atomicAdd(sse + c, v);
     }
@@ -473,7 +466,7 @@ cudaError_t launch_sse(const uint8_t* a, const uint8_t* b, size_t texels, unsign
     if (texels == 0) return cudaSuccess;
     int dev = 0, sms = 152;
     if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    long long grid = ((long long)texels + 255) / 256;
+    long long grid = ((long long)texels + 2047) / 2048;      // at least 8 texels per thread
     const long long cap = (long long)sms * 8;
     if (grid > cap) grid = cap;
     astc_sse_rgba<<<(unsigned)grid, 256, 0, stream>>>(reinterpret_cast<const uint32_t*>(a),

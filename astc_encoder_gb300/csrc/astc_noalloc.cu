@@ -9,8 +9,10 @@
 // accumulator (and, for host memory, staging) the first time it runs; this
 // entry point allocates nothing.
 //
-// How: the scratch -- one partial sum (4 x u64) per chunk of 65,536 texels --
-// is a file-scope static __device__ array of fixed size (4096 chunks, 128 KiB),
+// How: the scratch -- one partial sum (4 x u64) per chunk of texels (8,192
+// or, for images above 2^25 texels, 1/4096 of the image rounded up to 1,024;
+// at most 65,536), one CTA per chunk -- is a file-scope static __device__
+// array of fixed size (4096 chunks, 128 KiB),
 // which every GPU that loads this library holds until the process exits.  The
 // inputs (two RGBA8 images in device memory) and the output (4 x u64 in device
 // memory) are the caller's.  The first call on a device looks up the array's
@@ -26,12 +28,14 @@
 #include <string>
 
 #include "astc_internal.h"
+#include "astc_sse.cuh"
 
 namespace astc {
 namespace {
 
 constexpr int kNoAllocMaxChunks = 4096;
-constexpr size_t kNoAllocChunkTexels = size_t(1) << 16;
+constexpr size_t kNoAllocChunkTexels = size_t(1) << 16;                          // the largest chunk
+constexpr size_t kNoAllocMinChunkTexels = size_t(1) << 13;
 constexpr size_t kNoAllocMaxTexels = kNoAllocMaxChunks * kNoAllocChunkTexels;   // 2^28
 constexpr int kNoAllocThreads = 256;
 
@@ -53,25 +57,19 @@ __device__ __forceinline__ unsigned long long block_sum(unsigned long long v, un
     return s;
 }
 
-// One CTA per chunk: writes the chunk's R, G, B, A sums of squared differences.
+// One CTA per chunk of `chunk` texels (a multiple of 1,024): writes the
+// chunk's R, G, B, A sums of squared differences.
 __global__ void __launch_bounds__(kNoAllocThreads)
-astc_sse_chunks_static(const uint32_t* __restrict__ a, const uint32_t* __restrict__ b, size_t n,
+astc_sse_chunks_static(const uint32_t* __restrict__ a, const uint32_t* __restrict__ b, size_t n, size_t chunk,
                        unsigned long long* __restrict__ partials) {
     __shared__ unsigned long long red[kNoAllocThreads / 32];
-    const size_t begin = (size_t)blockIdx.x * kNoAllocChunkTexels;
-    const size_t end = begin + kNoAllocChunkTexels < n ? begin + kNoAllocChunkTexels : n;
-    unsigned long long acc[4] = {0, 0, 0, 0};
-    for (size_t i = begin + threadIdx.x; i < end; i += kNoAllocThreads) {
-        const uint32_t x = __ldg(a + i), y = __ldg(b + i);
-#pragma unroll
-        for (int c = 0; c < 4; ++c) {
-            const int d = (int)((x >> (8 * c)) & 0xFF) - (int)((y >> (8 * c)) & 0xFF);
-            acc[c] += (unsigned long long)(d * d);
-        }
-    }
+    const size_t begin = (size_t)blockIdx.x * chunk;
+    const size_t end = begin + chunk < n ? begin + chunk : n;
+    SseAcc acc;
+    sse_range(a, b, begin, end, threadIdx.x, kNoAllocThreads, acc);
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
-        const unsigned long long s = block_sum(acc[c], red);
+        const unsigned long long s = block_sum(acc.hi[c], red);
         if (threadIdx.x == 0) partials[(size_t)blockIdx.x * 4 + c] = s;
     }
 }
@@ -137,10 +135,14 @@ extern "C" astc_status astc_sse_gpu_noalloc(const uint8_t* a, const uint8_t* b, 
         unsigned long long* scratch = nullptr;
         if ((st = noalloc_scratch(&scratch)) != ASTC_OK) return st;
         cudaStream_t s = static_cast<cudaStream_t>(stream);
-        const int chunks = (int)((texels + kNoAllocChunkTexels - 1) / kNoAllocChunkTexels);
+        // chunks of at least 8,192 texels, at most 4096 of them
+        size_t chunk = (texels + kNoAllocMaxChunks - 1) / kNoAllocMaxChunks;
+        chunk = (chunk + 1023) / 1024 * 1024;
+        if (chunk < kNoAllocMinChunkTexels) chunk = kNoAllocMinChunkTexels;
+        const int chunks = (int)((texels + chunk - 1) / chunk);
         if (chunks > 0) {
             astc_sse_chunks_static<<<chunks, kNoAllocThreads, 0, s>>>(
-                reinterpret_cast<const uint32_t*>(a), reinterpret_cast<const uint32_t*>(b), texels,
+                reinterpret_cast<const uint32_t*>(a), reinterpret_cast<const uint32_t*>(b), texels, chunk,
                 scratch);
             cudaError_t e = cudaGetLastError();
             if (e != cudaSuccess) return cuda_error(e, "sse chunk kernel launch");

@@ -335,6 +335,81 @@ def _time_launches(torch, native, texs, outs, spec, steps, streams: int = 1):
     return sum(per_step) / max(1, launches), per_step, launches
 
 
+def _bench_aux(torch, native, texs, outs, spec: dict, hbm_peak: float, passes: int = 5) -> dict:
+    """The kernels around the encoder, on the headline's 16 textures and their
+    blocks, device-resident: the integer LDR decoder (16 B/block in, 4 B/texel
+    out), the no-alloc SSE reduction of source against decode (8 B/texel in)
+    and the box-filtered mip chain (each level reads the level above and
+    writes itself, 4 B/texel each way); algorithmic GB/s against the HBM copy
+    bandwidth, timed with a CUDA event pair around `passes` passes over the
+    16 textures (decoded images and sources above L2 size)."""
+    h, w = texs[0].shape[:2]
+    d = spec["block_dim"]
+    n = len(texs)
+    nb = ((w + d - 1) // d) * ((h + d - 1) // d)
+    stream = torch.cuda.current_stream()
+    lib = native.load_library()
+
+    def timed(fn):
+        fn()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        l0 = native.kernel_launch_count()
+        a.record(stream)
+        for _ in range(passes):
+            fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / 1e3 / passes, (native.kernel_launch_count() - l0) // passes
+
+    def entry(seconds, launches, nbytes, texels):
+        gbs = nbytes / seconds / 1e9
+        return {"GB_s": gbs, "frac_hbm": gbs / hbm_peak, "Mtexels_s": texels / seconds / 1e6,
+                "us_per_texture": seconds * 1e6 / n, "launches_per_pass": int(launches),
+                "alg_bytes_per_pass": int(nbytes)}
+
+    dec = [torch.empty((h, w, 4), dtype=torch.uint8, device="cuda") for _ in texs]
+
+    def decode_pass():
+        for o, dd in zip(outs, dec):
+            native.decode_device(o.data_ptr(), w, h, d, d, dd.data_ptr(), stream=stream.cuda_stream)
+
+    t, l = timed(decode_pass)
+    result = {"decode_ldr": entry(t, l, n * (nb * 16 + h * w * 4), n * h * w)}
+
+    sse_fn = lib.astc_sse_gpu_noalloc
+    sse_fn.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_void_p]
+    sse_fn.restype = ctypes.c_int
+    acc = torch.zeros(4, dtype=torch.int64, device="cuda")
+
+    def sse_pass():
+        for src, dd in zip(texs, dec):
+            st = sse_fn(src.data_ptr(), dd.data_ptr(), h * w, stream.cuda_stream, acc.data_ptr())
+            if st != 0:
+                raise native.AstcError(st, lib.astc_last_error().decode())
+
+    t, l = timed(sse_pass)
+    result["sse_noalloc"] = entry(t, l, n * h * w * 8, n * h * w)
+    del dec
+
+    levels = native.mip_levels(w, h)
+    sizes = native.mip_sizes(w, h, levels)
+    chain = native.mip_chain_bytes(w, h, levels)
+    mips = [torch.empty(chain, dtype=torch.uint8, device="cuda") for _ in texs]
+
+    def mip_pass():
+        for src, m in zip(texs, mips):
+            native.generate_mips(src.data_ptr(), w, h, levels, m.data_ptr(), srgb=bool(spec["srgb"]),
+                                 stream=stream.cuda_stream)
+
+    t, l = timed(mip_pass)
+    mip_bytes = sum(4 * (sizes[i - 1][0] * sizes[i - 1][1] + sizes[i][0] * sizes[i][1]) for i in range(1, levels))
+    result["mip_chain" + ("_srgb" if spec["srgb"] else "")] = entry(t, l, n * mip_bytes, n * h * w)
+    result["mip_chain" + ("_srgb" if spec["srgb"] else "")]["levels"] = levels
+    del mips
+    return result
+
+
 def _wave_sweep(torch, native, synth, warmup: int, steps: int) -> None:
     """Mean launch time of the fixed-mode 6x6 RGBA sRGB kernel for textures of
     0.5 to 4 full waves (12 resident warps per SM: 152 x 384 blocks per wave)
@@ -906,6 +981,7 @@ def run_ours(args) -> None:
             extra[name] = entry
             del xt, xo
 
+    aux = _bench_aux(torch, native, texs, outs, spec, hbm_peak)
     search = None if args.no_search else _bench_search(torch, native, args.workload, texs, outs, spec)
     batched = None if args.no_batched else _bench_batched(torch, native, oracle, args.batched_count)
     serving = None if args.no_serving else _bench_serving(
@@ -959,6 +1035,7 @@ def run_ours(args) -> None:
         "clocks": clk,
         "wall_s_timed_region": wall,
         "search_mode": search,
+        "aux_kernels": aux,
         "serving": serving,
         "serving_pageable": serving_pageable,
         "batched_mixed": batched,

@@ -392,9 +392,9 @@ astc_status astc_get_kernel_choice_for_size(int block_dim, int has_alpha, int is
  * also synchronise the device mid-frame.  This entry point calls no
  * cudaMalloc/cudaFree: `a` and `b` (RGBA8, 4-byte aligned) and `sse_rgba`
  * (4 x uint64, 8-byte aligned) are all caller-owned DEVICE memory, and its
- * scratch is a fixed static device array (one partial per 65,536 texels,
- * 4096 partials = 128 KiB) that every GPU loading this library holds until
- * exit.  Limit: texels <= 2^28 (268,435,456); larger calls return
+ * scratch is a fixed static device array (one partial per chunk of 8,192 to
+ * 65,536 texels, 4096 partials = 128 KiB) that every GPU loading this
+ * library holds until exit.  Limit: texels <= 2^28 (268,435,456); larger calls return
  * ASTC_ERR_INVALID_ARG.  Asynchronous on `stream` (NULL = the legacy default
  * stream).  The first call on a device looks up the scratch address with
  * that device current; make that first call before any stream capture.

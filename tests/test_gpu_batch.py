@@ -222,7 +222,10 @@ def _np_mips(img, levels, srgb):
     return out
 
 
-@pytest.mark.parametrize("h,w", [(64, 64), (37, 100), (1, 9), (6, 1)])
+# sizes: one tile, ragged tiles, one texel wide or high, several 64x64 tiles
+# per level and chains longer than the six levels one launch writes
+@pytest.mark.parametrize("h,w", [(64, 64), (37, 100), (1, 9), (6, 1), (300, 517), (2, 4100), (4099, 3),
+                                 (1030, 2048)])
 @pytest.mark.parametrize("srgb", [False, True])
 def test_mip_chain_matches_numpy(native, h, w, srgb):
     import torch

@@ -300,6 +300,37 @@ def test_sse_matches_numpy(native):
     assert native.sse(a, b).tolist() == want.tolist()
 
 
+def test_sse_vector_and_scalar_paths(native):
+    """Both SSE entry points on device images 16-byte aligned (four texels per
+    load) and only 4-byte aligned (one per load), with texel counts that are not
+    multiples of four and sizes from one texel to several hundred chunks: the
+    sums equal numpy's."""
+    import torch
+    lib = native.load_library()
+    noalloc = lib.astc_sse_gpu_noalloc
+    noalloc.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_void_p]
+    noalloc.restype = ctypes.c_int
+    rng = np.random.default_rng(31)
+    stream = torch.cuda.current_stream().cuda_stream
+    for texels in (1, 3, 4099, 1 << 20, (1 << 22) + 5):
+        a = rng.integers(0, 256, (texels + 1) * 4, dtype=np.uint8)
+        b = rng.integers(0, 256, (texels + 1) * 4, dtype=np.uint8)
+        da, db = torch.from_numpy(a).cuda(), torch.from_numpy(b).cuda()
+        out = torch.zeros(4, dtype=torch.int64, device="cuda")
+        for off in (0, 1):                          # texel offset 1: 4-byte aligned only
+            x = a[4 * off:4 * (off + texels)].reshape(-1, 4).astype(np.int64)
+            y = b[4 * off:4 * (off + texels)].reshape(-1, 4).astype(np.int64)
+            want = ((x - y) ** 2).sum(0).tolist()
+            res = (ctypes.c_uint64 * 4)()
+            st = lib.astc_sse_gpu(da.data_ptr() + 4 * off, db.data_ptr() + 4 * off, texels, 1, stream, res)
+            assert st == 0, lib.astc_last_error()
+            assert list(res) == want, (texels, off)
+            st = noalloc(da.data_ptr() + 4 * off, db.data_ptr() + 4 * off, texels, stream, out.data_ptr())
+            assert st == 0, lib.astc_last_error()
+            torch.cuda.synchronize()
+            assert [int(v) for v in out.cpu().tolist()] == want, (texels, off)
+
+
 def test_normal_sse_matches_numpy(native):
     """The reconstructed-normal error (z rebuilt from x and y) against its
     numpy float64 statement; FP32 per texel, FP64 sums: relative 1e-5."""
