@@ -19,8 +19,10 @@
 // device address with cudaGetSymbolAddress (with that device current) and
 // caches it; that first call should come before any stream capture.  All calls
 // share the array: two calls whose kernels overlap on the GPU race on it.
-// Each chunk's CTA overwrites its own partial and the final kernel reads only
-// the partials of the current call, so nothing has to start at zero.
+// Each chunk's CTA overwrites its own partial and counts itself done in the
+// array's last word; the CTA that counts last reads only the partials of the
+// current call, writes the totals and sets the count back to zero, so one
+// launch does the whole reduction.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -39,7 +41,9 @@ constexpr size_t kNoAllocMinChunkTexels = size_t(1) << 13;
 constexpr size_t kNoAllocMaxTexels = kNoAllocMaxChunks * kNoAllocChunkTexels;   // 2^28
 constexpr int kNoAllocThreads = 256;
 
-static __device__ __align__(256) unsigned long long g_noalloc_partials[kNoAllocMaxChunks * 4];
+// the partials, then one counter: CTAs of the current call that have written
+// theirs (the last one totals them and sets it back to zero)
+static __device__ __align__(256) unsigned long long g_noalloc_partials[kNoAllocMaxChunks * 4 + 1];
 
 constexpr int kMaxDevicesNoAlloc = 64;
 std::mutex g_noalloc_mu;
@@ -58,36 +62,42 @@ __device__ __forceinline__ unsigned long long block_sum(unsigned long long v, un
 }
 
 // One CTA per chunk of `chunk` texels (a multiple of 1,024): writes the
-// chunk's R, G, B, A sums of squared differences.
+// chunk's R, G, B, A sums of squared differences, then counts itself done;
+// the CTA that counts last totals every chunk's partials into `out` and sets
+// the counter back to zero for the next call (the fence before the count
+// makes each partial visible before it is counted).
 __global__ void __launch_bounds__(kNoAllocThreads)
 astc_sse_chunks_static(const uint32_t* __restrict__ a, const uint32_t* __restrict__ b, size_t n, size_t chunk,
-                       unsigned long long* __restrict__ partials) {
+                       unsigned long long* __restrict__ partials, unsigned long long* __restrict__ out) {
     __shared__ unsigned long long red[kNoAllocThreads / 32];
+    __shared__ bool last;
     const size_t begin = (size_t)blockIdx.x * chunk;
     const size_t end = begin + chunk < n ? begin + chunk : n;
     SseAcc acc;
-    sse_range(a, b, begin, end, threadIdx.x, kNoAllocThreads, acc);
+    if (begin < end) sse_range(a, b, begin, end, threadIdx.x, kNoAllocThreads, acc);
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
         const unsigned long long s = block_sum(acc.hi[c], red);
         if (threadIdx.x == 0) partials[(size_t)blockIdx.x * 4 + c] = s;
     }
-}
-
-// One CTA: totals of the `chunks` partials of this call into the caller's output.
-__global__ void __launch_bounds__(kNoAllocThreads)
-astc_sse_finish_static(const unsigned long long* __restrict__ partials, int chunks,
-                       unsigned long long* __restrict__ out) {
-    __shared__ unsigned long long red[kNoAllocThreads / 32];
-    unsigned long long acc[4] = {0, 0, 0, 0};
-    for (int i = threadIdx.x; i < chunks; i += kNoAllocThreads)
+    unsigned long long* counter = partials + (size_t)kNoAllocMaxChunks * 4;
+    if (threadIdx.x == 0) {
+        __threadfence();
+        last = atomicAdd(counter, 1ull) == (unsigned long long)gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    unsigned long long tot[4] = {0, 0, 0, 0};
+    for (unsigned i = threadIdx.x; i < gridDim.x; i += kNoAllocThreads)
 #pragma unroll
-        for (int c = 0; c < 4; ++c) acc[c] += partials[(size_t)i * 4 + c];
+        for (int c = 0; c < 4; ++c) tot[c] += __ldcg(partials + (size_t)i * 4 + c);
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
-        const unsigned long long s = block_sum(acc[c], red);
+        const unsigned long long s = block_sum(tot[c], red);
         if (threadIdx.x == 0) out[c] = s;
     }
+    if (threadIdx.x == 0) *counter = 0ull;
 }
 
 astc_status noalloc_scratch(unsigned long long** out) {
@@ -140,18 +150,12 @@ extern "C" astc_status astc_sse_gpu_noalloc(const uint8_t* a, const uint8_t* b, 
         chunk = (chunk + 1023) / 1024 * 1024;
         if (chunk < kNoAllocMinChunkTexels) chunk = kNoAllocMinChunkTexels;
         const int chunks = (int)((texels + chunk - 1) / chunk);
-        if (chunks > 0) {
-            astc_sse_chunks_static<<<chunks, kNoAllocThreads, 0, s>>>(
-                reinterpret_cast<const uint32_t*>(a), reinterpret_cast<const uint32_t*>(b), texels, chunk,
-                scratch);
-            cudaError_t e = cudaGetLastError();
-            if (e != cudaSuccess) return cuda_error(e, "sse chunk kernel launch");
-            count_launches(1);
-        }
-        astc_sse_finish_static<<<1, kNoAllocThreads, 0, s>>>(
-            scratch, chunks, reinterpret_cast<unsigned long long*>(sse_rgba));
+        // one CTA at least, so an empty call still writes its zero sums
+        astc_sse_chunks_static<<<chunks > 0 ? chunks : 1, kNoAllocThreads, 0, s>>>(
+            reinterpret_cast<const uint32_t*>(a), reinterpret_cast<const uint32_t*>(b), texels, chunk, scratch,
+            reinterpret_cast<unsigned long long*>(sse_rgba));
         cudaError_t e = cudaGetLastError();
-        if (e != cudaSuccess) return cuda_error(e, "sse finish kernel launch");
+        if (e != cudaSuccess) return cuda_error(e, "sse kernel launch");
         count_launches(1);
         return ASTC_OK;
     } catch (...) {
