@@ -265,10 +265,96 @@ __device__ Mode block_mode(int m) {
 
 __device__ __forceinline__ uint32_t rev32(uint32_t v) { return __brev(v); }
 
+// The blocks the fixed-mode encoder writes (single partition, a 4x4 weight
+// grid in QUANT_6 trits with CEM 8 or 12, or in QUANT_12 trits with CEM 8;
+// both leave room for QUANT_256 endpoints; no dual plane) decoded with the
+// block and grid sizes known at compile time:
+// the same arithmetic as the general path below, unrolled into registers.
+// Q = kQuant6 (1 bit + trit per weight) or kQuant12 (2 bits + trit).
+template <int DIM, int Q, class Sink>
+__device__ __forceinline__ void decode_fixed_grid4(const DecodeTables& T, const uint4 raw, bool alpha, bool srgb,
+                                                   Sink&& sink) {
+    constexpr int B = Q == kQuant6 ? 1 : 2;
+    constexpr int GW = 5 * B + 8;
+    constexpr int NBITS = ise_bit_count(Q, 16);
+    // endpoint bytes from bit 17: r0 r1 g0 g1 b0 b1 [a0 a1]
+    const uint64_t lo = ((uint64_t)raw.y << 32) | raw.x;
+    const uint64_t ep = (lo >> 17) | ((uint64_t)raw.z << 47);
+    int v[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) v[i] = (int)((ep >> (8 * i)) & 0xFFu);
+    const int a0 = alpha ? v[6] : 255, a1 = alpha ? v[7] : 255;
+    int e0[4], e1[4];
+    if (v[1] + v[3] + v[5] >= v[0] + v[2] + v[4]) {
+        e0[0] = v[0]; e0[1] = v[2]; e0[2] = v[4]; e0[3] = a0;
+        e1[0] = v[1]; e1[1] = v[3]; e1[2] = v[5]; e1[3] = a1;
+    } else {
+        e0[0] = (v[1] + v[5]) >> 1; e0[1] = (v[3] + v[5]) >> 1; e0[2] = v[5]; e0[3] = a1;
+        e1[0] = (v[0] + v[4]) >> 1; e1[1] = (v[2] + v[4]) >> 1; e1[2] = v[4]; e1[3] = a0;
+    }
+    // the weight stream, bit i = block bit 127 - i, cut to its length
+    const uint64_t ws = __brevll(((uint64_t)raw.w << 32) | raw.z) & ((1ull << NBITS) - 1ull);
+    int wv[16];
+#pragma unroll
+    for (int g = 0; g < 4; ++g) {
+        const uint32_t grp = (uint32_t)(ws >> (g * GW));
+        constexpr uint32_t M = (1u << B) - 1u;
+        const uint32_t m[5] = {grp & M, (grp >> (B + 2)) & M, (grp >> (2 * B + 4)) & M, (grp >> (3 * B + 5)) & M,
+                               (grp >> (4 * B + 7)) & M};
+        const uint32_t t = ((grp >> B) & 3u) | (((grp >> (2 * B + 2)) & 3u) << 2) | (((grp >> (3 * B + 4)) & 1u) << 4) |
+                           (((grp >> (4 * B + 5)) & 3u) << 5) | (((grp >> (5 * B + 7)) & 1u) << 7);
+#pragma unroll
+        for (int i = 0; i < 5; ++i)
+            if (5 * g + i < 16) wv[5 * g + i] = T.weight_unq[Q][(T.trit_unpack[t][i] << B) | m[i]];
+    }
+    constexpr int ds = (1024 + DIM / 2) / (DIM - 1);
+#pragma unroll
+    for (int t = 0; t < DIM; ++t)
+#pragma unroll
+        for (int s = 0; s < DIM; ++s) {
+            const int gs = (ds * s * 3 + 32) >> 6, gt = (ds * t * 3 + 32) >> 6;
+            const int js = gs >> 4, fs = gs & 0xF, jt = gt >> 4, ft = gt & 0xF;
+            const int w11 = (fs * ft + 8) >> 4, w10 = ft - w11, w01 = fs - w11, w00 = 16 - fs - ft + w11;
+            const int v0 = js + jt * 4;
+            int acc = wv[v0] * w00;
+            if (w01) acc += wv[v0 + 1] * w01;
+            if (w10) acc += wv[v0 + 4] * w10;
+            if (w11) acc += wv[v0 + 5] * w11;
+            const int wt = (acc + 8) >> 4;
+            uint32_t px = 0;
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                const int c0 = srgb ? ((e0[c] << 8) | 0x80) : e0[c] * 257;
+                const int c1 = srgb ? ((e1[c] << 8) | 0x80) : e1[c] * 257;
+                px |= (uint32_t)(((c0 * (64 - wt) + c1 * wt + 32) >> 6) >> 8) << (8 * c);
+            }
+            sink(s, t, px);
+        }
+}
+
 // Decode one block into `texel(s, t, rgba)`; returns false for an error block.
 template <class Sink>
 __device__ bool decode_one(const DecodeTables& T, const uint4 raw, int bw, int bh, bool srgb,
                            Sink&& sink) {
+    // the fixed-mode encoder's blocks: mode word, one partition, CEM 8 or 12
+    const uint32_t head = raw.x & 0x1FFFFu;
+    if (bw == bh && (bw == 4 || bw == 6)) {
+        const uint32_t mode11 = head & 0x7FFu, cem = head >> 13;
+        const bool q6 = mode11 == blockmode_4x4_grid(kQuant6), q12 = mode11 == blockmode_4x4_grid(kQuant12);
+        const bool alpha = cem == 12u;
+        // QUANT_12 weights leave 53 bits for the colours: QUANT_256 for six
+        // values (CEM 8), a smaller range for eight (CEM 12, the general path)
+        if ((head & 0x1800u) == 0 && (cem == 8u || cem == 12u) && (q6 || (q12 && !alpha))) {
+            if (bw == 4) {
+                if (q6) decode_fixed_grid4<4, kQuant6>(T, raw, alpha, srgb, sink);
+                else decode_fixed_grid4<4, kQuant12>(T, raw, alpha, srgb, sink);
+            } else {
+                if (q6) decode_fixed_grid4<6, kQuant6>(T, raw, alpha, srgb, sink);
+                else decode_fixed_grid4<6, kQuant12>(T, raw, alpha, srgb, sink);
+            }
+            return true;
+        }
+    }
     Bits b = {{raw.x, raw.y, raw.z, raw.w}};
     const int mode = (int)b.read(0, 11);
     if ((mode & 0x1FF) == 0x1FC) {

@@ -292,6 +292,25 @@ def test_decoder_matches_oracle_on_random_blocks(native, oracle):
         assert np.array_equal(got, want)
 
 
+@pytest.mark.parametrize("quality", [0, 1, 3])
+def test_decoder_matches_oracle_on_encoded_blocks(native, oracle, quality):
+    """The decoder's fixed-layout path (single partition, 4x4 weight grid in
+    QUANT_6 with CEM 8/12 or QUANT_12 with CEM 8, QUANT_256 endpoints: the
+    fixed mode's blocks) and its general path (every other block the quality
+    modes write, QUANT_12 with CEM 12 among them) against the oracle's spec
+    decoder, linear and sRGB decode, on ragged sizes."""
+    for dim, alpha, normal, srgb in itertools.product([4, 6], [False, True], [False, True], [False, True]):
+        img = _texture(37 + dim, 53, seed=dim * 8 + alpha * 4 + normal * 2 + srgb)
+        h, w = img.shape[:2]
+        blocks = native.encode(img, block_dim=dim, has_alpha=alpha, is_normal=normal, srgb=srgb, border=1,
+                               quality=quality)
+        for srgb_decode in (False, True):
+            want, errors = oracle.decode(blocks, w, h, dim, srgb=srgb_decode)
+            assert errors == 0
+            assert np.array_equal(native.decode(blocks, w, h, dim, srgb=srgb_decode), want), \
+                (dim, alpha, normal, srgb, srgb_decode)
+
+
 def test_sse_matches_numpy(native):
     rng = np.random.default_rng(3)
     a = rng.integers(0, 256, (123, 77, 4), dtype=np.uint8)
