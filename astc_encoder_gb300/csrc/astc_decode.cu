@@ -308,6 +308,7 @@ __device__ __forceinline__ void decode_fixed_grid4(const DecodeTables& T, const 
             if (5 * g + i < 16) wv[5 * g + i] = T.weight_unq[Q][(T.trit_unpack[t][i] << B) | m[i]];
     }
     constexpr int ds = (1024 + DIM / 2) / (DIM - 1);
+    uint32_t row[DIM];
 #pragma unroll
     for (int t = 0; t < DIM; ++t)
 #pragma unroll
@@ -328,7 +329,8 @@ __device__ __forceinline__ void decode_fixed_grid4(const DecodeTables& T, const 
                 const int c1 = srgb ? ((e1[c] << 8) | 0x80) : e1[c] * 257;
                 px |= (uint32_t)(((c0 * (64 - wt) + c1 * wt + 32) >> 6) >> 8) << (8 * c);
             }
-            sink(s, t, px);
+            row[s] = px;
+            if (s == DIM - 1) sink.row(t, row);
         }
 }
 
@@ -448,6 +450,35 @@ __device__ bool decode_one(const DecodeTables& T, const uint4 raw, int bw, int b
     return true;
 }
 
+// Writes decoded texels into the RGBA8 image: one at a time, or a block's
+// whole row (N texels) in 16-byte (N = 4) or 8-byte (N = 6) stores when the
+// block lies inside the image's width and the row's address allows it.
+struct TexelSink {
+    uint32_t* out;
+    int width, height, x0, y0;
+    bool full_width;
+    __device__ __forceinline__ void operator()(int s, int t, uint32_t px) const {
+        const int x = x0 + s, y = y0 + t;
+        if (x < width && y < height) out[(size_t)y * width + x] = px;
+    }
+    template <int N>
+    __device__ __forceinline__ void row(int t, const uint32_t (&px)[N]) const {
+        const int y = y0 + t;
+        if (y >= height) return;
+        uint32_t* dst = out + (size_t)y * width + x0;
+        const uintptr_t a = reinterpret_cast<uintptr_t>(dst);
+        if (full_width && N == 4 && a % 16 == 0) {
+            *reinterpret_cast<uint4*>(dst) = make_uint4(px[0], px[1], px[2], px[3 % N]);
+        } else if (full_width && N % 2 == 0 && a % 8 == 0) {
+#pragma unroll
+            for (int k = 0; k < N; k += 2) *reinterpret_cast<uint2*>(dst + k) = make_uint2(px[k], px[k + 1]);
+        } else {
+#pragma unroll
+            for (int s = 0; s < N; ++s) (*this)(s, t, px[s]);
+        }
+    }
+};
+
 __global__ void __launch_bounds__(kDecodeThreads)
 astc_decode_ldr(const uint4* __restrict__ blocks, int width, int height, int bw, int bh, int nbx,
                 long long nblocks, int srgb, uint32_t* __restrict__ out) {
@@ -462,10 +493,7 @@ astc_decode_ldr(const uint4* __restrict__ blocks, int width, int height, int bw,
     if (i >= nblocks) return;
     const int by = (int)(i / nbx), bx = (int)(i - (long long)by * nbx);
     const int x0 = bx * bw, y0 = by * bh;
-    auto sink = [&](int s, int t, uint32_t px) {
-        const int x = x0 + s, y = y0 + t;
-        if (x < width && y < height) out[(size_t)y * width + x] = px;
-    };
+    TexelSink sink{out, width, height, x0, y0, x0 + bw <= width};
     if (!decode_one(s_tab, blocks[i], bw, bh, srgb != 0, sink)) {
         for (int t = 0; t < bh; ++t)
             for (int s = 0; s < bw; ++s) sink(s, t, 0xFFFF00FFu);    // magenta
