@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "astc_block_common.cuh"
 #include "astc_internal.h"
 #include "astc_sse.cuh"
 #include "astc_tables.h"
@@ -489,6 +490,8 @@ astc_decode_ldr(const uint4* __restrict__ blocks, int width, int height, int bw,
         for (int i = threadIdx.x; i < (int)(sizeof(DecodeTables) / 4); i += blockDim.x) dst[i] = src[i];
     }
     __syncthreads();
+    pdl_wait_prior();
+    pdl_allow_next();
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nblocks) return;
     const int by = (int)(i / nbx), bx = (int)(i - (long long)by * nbx);
@@ -567,10 +570,9 @@ cudaError_t launch_decode(const uint8_t* blocks, int width, int height, int bw, 
     const int nbx = (width + bw - 1) / bw;
     const long long nb = (long long)nbx * ((height + bh - 1) / bh);
     const long long grid = (nb + kDecodeThreads - 1) / kDecodeThreads;
-    astc_decode_ldr<<<(unsigned)grid, kDecodeThreads, 0, stream>>>(
-        reinterpret_cast<const uint4*>(blocks), width, height, bw, bh, nbx, nb, srgb,
-        reinterpret_cast<uint32_t*>(out));
-    const cudaError_t e = cudaGetLastError();
+    const cudaError_t e = launch_pdl(astc_decode_ldr, (unsigned)grid, kDecodeThreads, 0, stream,
+                                     reinterpret_cast<const uint4*>(blocks), width, height, bw, bh, nbx, nb, srgb,
+                                     reinterpret_cast<uint32_t*>(out));
     if (e == cudaSuccess) count_launches(1);
     return e;
 }

@@ -17,6 +17,7 @@
 #include <cmath>
 #include <mutex>
 
+#include "astc_block_common.cuh"
 #include "astc_internal.h"
 
 namespace astc {
@@ -91,6 +92,10 @@ __global__ void __launch_bounds__(kPyrThreads) astc_mip_pyramid(const PyrParams 
         for (int i = threadIdx.x; i < 1024; i += kPyrThreads)
             reinterpret_cast<uint32_t*>(s_srgb)[i] = __ldg(t4 + i);
     }
+    // the tables are read-only: loaded before waiting for the previous kernel
+    // on the stream (the level this launch starts from may be its output)
+    pdl_wait_prior();
+    pdl_allow_next();
     const int ty = (int)(blockIdx.x / (unsigned)p.tiles_x), tx = (int)blockIdx.x - ty * p.tiles_x;
     const int ox = tx * kPyrTile, oy = ty * kPyrTile;
     for (int i = threadIdx.x; i < kPyrTile * kPyrTile; i += kPyrThreads) {
@@ -221,8 +226,8 @@ astc_status astc_generate_mips(const uint8_t* rgba8, int width, int height, int 
         }
         pp.tiles_x = (w + kPyrTile - 1) / kPyrTile;
         const long long tiles = (long long)pp.tiles_x * ((h + kPyrTile - 1) / kPyrTile);
-        astc_mip_pyramid<<<(unsigned)tiles, kPyrThreads, 0, s>>>(pp);
-        if ((e = cudaGetLastError()) != cudaSuccess) return cuda_error(e, "mip kernel launch");
+        if ((e = launch_pdl(astc_mip_pyramid, (unsigned)tiles, kPyrThreads, 0, s, pp)) != cudaSuccess)
+            return cuda_error(e, "mip kernel launch");
         count_launches(1);
         src = pp.lev[pp.nlev - 1].dst;
         w = lw;

@@ -29,6 +29,7 @@
 #include <mutex>
 #include <string>
 
+#include "astc_block_common.cuh"
 #include "astc_internal.h"
 #include "astc_sse.cuh"
 
@@ -71,6 +72,10 @@ astc_sse_chunks_static(const uint32_t* __restrict__ a, const uint32_t* __restric
                        unsigned long long* __restrict__ partials, unsigned long long* __restrict__ out) {
     __shared__ unsigned long long red[kNoAllocThreads / 32];
     __shared__ bool last;
+    // a launch may start while the previous kernel on the stream finishes; the
+    // scratch and the images are touched only after it has completed
+    pdl_wait_prior();
+    pdl_allow_next();
     const size_t begin = (size_t)blockIdx.x * chunk;
     const size_t end = begin + chunk < n ? begin + chunk : n;
     SseAcc acc;
@@ -151,10 +156,9 @@ extern "C" astc_status astc_sse_gpu_noalloc(const uint8_t* a, const uint8_t* b, 
         if (chunk < kNoAllocMinChunkTexels) chunk = kNoAllocMinChunkTexels;
         const int chunks = (int)((texels + chunk - 1) / chunk);
         // one CTA at least, so an empty call still writes its zero sums
-        astc_sse_chunks_static<<<chunks > 0 ? chunks : 1, kNoAllocThreads, 0, s>>>(
-            reinterpret_cast<const uint32_t*>(a), reinterpret_cast<const uint32_t*>(b), texels, chunk, scratch,
-            reinterpret_cast<unsigned long long*>(sse_rgba));
-        cudaError_t e = cudaGetLastError();
+        cudaError_t e = launch_pdl(astc_sse_chunks_static, (unsigned)(chunks > 0 ? chunks : 1), kNoAllocThreads, 0, s,
+                                   reinterpret_cast<const uint32_t*>(a), reinterpret_cast<const uint32_t*>(b),
+                                   texels, chunk, scratch, reinterpret_cast<unsigned long long*>(sse_rgba));
         if (e != cudaSuccess) return cuda_error(e, "sse kernel launch");
         count_launches(1);
         return ASTC_OK;
